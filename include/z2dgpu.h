@@ -1,0 +1,246 @@
+/*
+ * z2dgpu.h -- C ABI of the GB300-native fill-and-composite path.
+ *
+ * This is the drop-in boundary for z2d's painter.fill / SurfaceCompositor.run
+ * hot path.  Every entry point is plain C: pointers, sizes and small POD
+ * structs, no C++ or torch types.  Status codes mirror z2d's error sets.
+ *
+ * Reference interfaces replaced (paths are inside the z2d project):
+ *   z2dgpu_fill        <- painter.fill                  src/painter.zig:66-72
+ *   z2dgpu_fill_batch  <- N x painter.fill, same surface src/painter.zig:66-143
+ *                         (Context.fill loop, src/Context.zig:592-607)
+ *   z2dgpu_composite   <- compositor.SurfaceCompositor.run
+ *                                                       src/compositor.zig:302-309
+ *                         (and Surface.composite,       src/surface.zig:225-241)
+ *   z2d_surface        <- surface.Surface               src/surface.zig:74-83
+ *   z2d_node           <- PathNode                      src/internal/path_nodes.zig:16-41
+ *   z2d_pattern        <- pattern.Pattern               src/pattern.zig:32-36
+ *   z2d_gradient       <- gradient.Gradient             src/gradient.zig:42-95
+ *   z2d_fill_opts      <- painter.FillOptions           src/painter.zig:28-48
+ *   z2d_operation      <- SurfaceCompositor.Operation   src/compositor.zig:223-284
+ *
+ * Memory layout of surface data (identical to z2d's in-memory layout):
+ *   ARGB  4 B/px, bytes B,G,R,A        RGBA 4 B/px, bytes R,G,B,A
+ *   XRGB  4 B/px, bytes B,G,R,pad      RGB  4 B/px, bytes R,G,B,pad
+ *   ALPHA8 1 B/px
+ *   ALPHA4/2/1 packed: pixel i (flat index w*y+x) occupies bits
+ *     [i*bits, i*bits+bits) little-endian (LSB first); rows are NOT byte
+ *     aligned.  Buffer length ceil(w*h*bits/8).
+ *
+ * Threading: a context owns one CUDA stream and device scratch; calls on one
+ * context must not overlap.  Use one context per host thread.
+ */
+#ifndef Z2DGPU_H
+#define Z2DGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+#define Z2D_EXTERN extern "C"
+#else
+#define Z2D_EXTERN extern
+#endif
+#define Z2D_API Z2D_EXTERN __attribute__((visibility("default")))
+
+/* ---- status codes (src/painter.zig:54-63, src/surface.zig:85-91) ---- */
+enum {
+    Z2D_OK = 0,
+    Z2D_ERR_PATH_NOT_CLOSED = 1,          /* FillError.PathNotClosed */
+    Z2D_ERR_PIXEL_NOT_PREMULTIPLIED = 2,  /* FillError.PixelSourceNotPreMultiplied */
+    Z2D_ERR_INVALID_DIMENSIONS = 3,       /* Surface.Error.InvalidWidth/InvalidHeight */
+    Z2D_ERR_INVALID_STATE = 4,            /* InternalError.InvalidState */
+    Z2D_ERR_OUT_OF_MEMORY = 5,            /* Allocator.Error.OutOfMemory */
+    Z2D_ERR_CUDA = 6,                     /* CUDA runtime failure (see z2dgpu_last_error) */
+    Z2D_ERR_TIMEOUT = 7,                  /* a bounded device wait gave up */
+    Z2D_ERR_INVALID_ARGUMENT = 8          /* malformed descriptor */
+};
+
+/* ---- pixel formats (src/pixel.zig:47-56) ---- */
+enum {
+    Z2D_FORMAT_ARGB = 0,
+    Z2D_FORMAT_XRGB = 1,
+    Z2D_FORMAT_RGB = 2,
+    Z2D_FORMAT_RGBA = 3,
+    Z2D_FORMAT_ALPHA8 = 4,
+    Z2D_FORMAT_ALPHA4 = 5,
+    Z2D_FORMAT_ALPHA2 = 6,
+    Z2D_FORMAT_ALPHA1 = 7
+};
+
+/* where z2d_surface.data lives */
+enum { Z2D_MEM_HOST = 0, Z2D_MEM_DEVICE = 1 };
+
+/* operators (src/compositor.zig:46-158), same order */
+enum {
+    Z2D_OP_CLEAR = 0, Z2D_OP_SRC, Z2D_OP_DST, Z2D_OP_SRC_OVER, Z2D_OP_DST_OVER,
+    Z2D_OP_SRC_IN, Z2D_OP_DST_IN, Z2D_OP_SRC_OUT, Z2D_OP_DST_OUT, Z2D_OP_SRC_ATOP,
+    Z2D_OP_DST_ATOP, Z2D_OP_XOR, Z2D_OP_PLUS, Z2D_OP_MULTIPLY, Z2D_OP_SCREEN,
+    Z2D_OP_OVERLAY, Z2D_OP_DARKEN, Z2D_OP_LIGHTEN, Z2D_OP_COLOR_DODGE,
+    Z2D_OP_COLOR_BURN, Z2D_OP_HARD_LIGHT, Z2D_OP_SOFT_LIGHT, Z2D_OP_DIFFERENCE,
+    Z2D_OP_EXCLUSION, Z2D_OP_HUE, Z2D_OP_SATURATION, Z2D_OP_COLOR,
+    Z2D_OP_LUMINOSITY,
+    Z2D_OP_COUNT
+};
+
+enum { Z2D_PRECISION_INTEGER = 0, Z2D_PRECISION_FLOAT = 1 };  /* src/compositor.zig:214 */
+enum { Z2D_FILL_NON_ZERO = 0, Z2D_FILL_EVEN_ODD = 1 };         /* src/options.zig:23-37 */
+enum {                                                         /* src/options.zig:73-91 */
+    Z2D_AA_NONE = 0, Z2D_AA_DEFAULT = 1, Z2D_AA_MULTISAMPLE_4X = 2, Z2D_AA_SUPERSAMPLE_4X = 3
+};
+
+/* A pixel value in its own format.  For ALPHA4/2/1 `a` holds the raw
+ * 4/2/1-bit value.  For XRGB/RGB `a` is ignored. */
+typedef struct z2d_pixel {
+    int32_t format;
+    uint8_t r, g, b, a;
+} z2d_pixel;
+
+typedef struct z2d_surface {
+    int32_t format;
+    int32_t width;
+    int32_t height;
+    int32_t location;   /* Z2D_MEM_HOST or Z2D_MEM_DEVICE */
+    void *data;
+} z2d_surface;
+
+/* path nodes (src/internal/path_nodes.zig:9-14) */
+enum { Z2D_MOVE_TO = 0, Z2D_LINE_TO = 1, Z2D_CURVE_TO = 2, Z2D_CLOSE_PATH = 3 };
+
+/* move_to/line_to: point = (p[0], p[1]).  curve_to: p1 = (p[0], p[1]),
+ * p2 = (p[2], p[3]), p3 = (p[4], p[5]).  Device-space coordinates, as held
+ * by z2d's Path after transformation and clamping. 56 bytes. */
+typedef struct z2d_node {
+    int32_t tag;
+    int32_t _pad;
+    double p[6];
+} z2d_node;
+
+/* colors (src/color.zig:41-93); values are stored as after Color.init */
+enum { Z2D_COLOR_LINEAR_RGB = 0, Z2D_COLOR_SRGB = 1, Z2D_COLOR_HSL = 2 };
+typedef struct z2d_color {
+    int32_t space;
+    float c[4];         /* r,g,b,a or h,s,l,a */
+} z2d_color;
+
+/* gradient stop; offsets in insertion order, clamped to [0,1] and stably
+ * sorted by the library exactly as Stop.List.addAssumeCapacity does
+ * (src/gradient.zig:797-811). */
+typedef struct z2d_stop {
+    float offset;
+    z2d_color color;
+} z2d_stop;
+
+enum { Z2D_GRADIENT_LINEAR = 0, Z2D_GRADIENT_RADIAL = 1, Z2D_GRADIENT_CONIC = 2 };
+enum {  /* InterpolationMethod (src/color.zig:111-135) */
+    Z2D_INTERP_LINEAR_RGB = 0, Z2D_INTERP_SRGB = 1,
+    Z2D_INTERP_HSL_SHORTER = 2, Z2D_INTERP_HSL_LONGER = 3,
+    Z2D_INTERP_HSL_INCREASING = 4, Z2D_INTERP_HSL_DECREASING = 5
+};
+
+typedef struct z2d_gradient {
+    int32_t type;
+    int32_t method;
+    int32_t n_stops;
+    int32_t _pad;
+    /* linear: x0,y0,x1,y1; radial: inner_x,inner_y,inner_r,outer_x,outer_y,
+     * outer_r; conic: x,y,angle (radians, un-normalised) */
+    double geom[6];
+    /* the device->pattern matrix as stored by setTransformation (already
+     * inverted): ax, by, cx, dy, tx, ty.  Identity means "no transform". */
+    double transform[6];
+    const z2d_stop *stops;
+} z2d_gradient;
+
+/* pattern (src/pattern.zig:32) and dither (src/Dither.zig:28-70) */
+enum { Z2D_PATTERN_PIXEL = 0, Z2D_PATTERN_GRADIENT = 1, Z2D_PATTERN_DITHER = 2 };
+enum { Z2D_DITHER_NONE = 0, Z2D_DITHER_BAYER = 1, Z2D_DITHER_BLUE_NOISE = 2 };
+enum { Z2D_DITHER_SRC_PIXEL = 0, Z2D_DITHER_SRC_COLOR = 1, Z2D_DITHER_SRC_GRADIENT = 2 };
+
+typedef struct z2d_pattern {
+    int32_t kind;              /* Z2D_PATTERN_* */
+    z2d_pixel pixel;           /* PIXEL, or dither source pixel */
+    const z2d_gradient *gradient; /* GRADIENT, or dither source gradient */
+    int32_t dither_type;       /* DITHER: Z2D_DITHER_* */
+    int32_t dither_source;     /* DITHER: Z2D_DITHER_SRC_* */
+    int32_t dither_scale;      /* DITHER: bits per channel of the target (1..15) */
+    int32_t _pad;
+    z2d_color dither_color;    /* DITHER with COLOR source */
+} z2d_pattern;
+
+typedef struct z2d_fill_opts {
+    int32_t anti_aliasing;     /* Z2D_AA_* (default: Z2D_AA_DEFAULT) */
+    int32_t fill_rule;         /* Z2D_FILL_* (default: NON_ZERO) */
+    int32_t op;                /* Z2D_OP_* (default: SRC_OVER) */
+    int32_t precision;         /* Z2D_PRECISION_* (default: INTEGER) */
+    double tolerance;          /* default 0.1 */
+} z2d_fill_opts;
+
+/* Compositor parameters (SurfaceCompositor.Operation.Param) */
+enum {
+    Z2D_PARAM_NONE = 0, Z2D_PARAM_PIXEL = 1, Z2D_PARAM_GRADIENT = 2,
+    Z2D_PARAM_DITHER = 3, Z2D_PARAM_SURFACE = 4
+};
+typedef struct z2d_param {
+    int32_t kind;              /* Z2D_PARAM_* */
+    int32_t _pad;
+    z2d_pattern pattern;       /* PIXEL / GRADIENT / DITHER use the matching fields */
+    const z2d_surface *surface;/* SURFACE */
+} z2d_param;
+
+typedef struct z2d_operation {
+    int32_t op;
+    int32_t _pad;
+    z2d_param dst;
+    z2d_param src;
+} z2d_operation;
+
+/* one fill of a batch: nodes[node_offset, node_offset+n_nodes) of the batch
+ * node array, drawn with `pattern` and `opts` */
+typedef struct z2d_fill_cmd {
+    const z2d_pattern *pattern;
+    uint64_t node_offset;
+    uint64_t n_nodes;
+    z2d_fill_opts opts;
+} z2d_fill_cmd;
+
+typedef struct z2dgpu_ctx z2dgpu_ctx;
+
+/* ---- library / context ---- */
+Z2D_API const char *z2dgpu_version(void);
+/* Message of the last failing call on this thread ("" if none). */
+Z2D_API const char *z2dgpu_last_error(void);
+/* Creates a context on `device`.  `stream` is a cudaStream_t to run on, or
+ * NULL for a context-owned stream. */
+Z2D_API int z2dgpu_ctx_create(z2dgpu_ctx **out, int device, void *stream);
+Z2D_API int z2dgpu_ctx_destroy(z2dgpu_ctx *ctx);
+/* Blocks until all work queued on the context's stream has finished. */
+Z2D_API int z2dgpu_ctx_synchronize(z2dgpu_ctx *ctx);
+/* Number of kernels this context has launched since creation. */
+Z2D_API uint64_t z2dgpu_ctx_launch_count(const z2dgpu_ctx *ctx);
+
+/* Bytes of pixel storage for a surface (src/surface.zig:382-395, 621-635). */
+Z2D_API size_t z2dgpu_surface_bytes(int32_t format, int32_t width, int32_t height);
+
+/* painter.fill (src/painter.zig:66-143).  Synchronous for host surfaces;
+ * for device surfaces the work is queued on the context stream and the call
+ * returns after launch (validation errors are still reported). */
+Z2D_API int z2dgpu_fill(z2dgpu_ctx *ctx, z2d_surface *surface,
+                        const z2d_pattern *pattern, const z2d_node *nodes,
+                        size_t n_nodes, const z2d_fill_opts *opts);
+
+/* Equivalent to calling painter.fill for cmds[0..n_cmds) in order on one
+ * surface; the fills are flattened, binned and composited in one device
+ * pass that keeps per-pixel order.  `nodes` is the node array the commands
+ * index into. */
+Z2D_API int z2dgpu_fill_batch(z2dgpu_ctx *ctx, z2d_surface *surface,
+                              const z2d_node *nodes, size_t n_nodes,
+                              const z2d_fill_cmd *cmds, size_t n_cmds);
+
+/* SurfaceCompositor.run (src/compositor.zig:302-440) with 1 or 2 operations.
+ * Source/destination surfaces must live where `dst` lives. */
+Z2D_API int z2dgpu_composite(z2dgpu_ctx *ctx, z2d_surface *dst, int32_t dst_x,
+                             int32_t dst_y, int32_t n_ops,
+                             const z2d_operation *ops, int32_t precision);
+
+#endif /* Z2DGPU_H */

@@ -1,0 +1,139 @@
+"""ctypes binding and build recipe of the CPU oracle -- TEST INFRASTRUCTURE.
+
+build_oracle() compiles z2d_oracle.cpp with g++ into oracle/_build/ (strict
+IEEE flags: no FP contraction, no fast-math).  Oracle mirrors the product's
+painter.fill / SurfaceCompositor.run entry points on host surfaces, using
+the same C structs (include/z2dgpu.h).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import pathlib
+import subprocess
+import threading
+
+from z2d_gb300 import abi
+from z2d_gb300.types import FillOptions, Operation, Pattern, nodes_to_abi
+
+HERE = pathlib.Path(__file__).resolve().parent
+SRC = HERE / "z2d_oracle.cpp"
+BUILD = HERE / "_build"
+LIB = BUILD / "libz2doracle.so"
+DEPS = [SRC, HERE.parent / "include" / "z2dgpu.h", HERE.parent / "z2d_gb300" / "csrc" / "blue_noise_64x64.inc"]
+CXXFLAGS = ["-std=c++17", "-O3", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared"]
+
+_lock = threading.Lock()
+_lib = None
+
+
+def build_oracle(force: bool = False) -> pathlib.Path:
+    """Compiles the oracle if it is missing or older than its sources."""
+    BUILD.mkdir(exist_ok=True)
+    if not force and LIB.exists() and all(LIB.stat().st_mtime >= d.stat().st_mtime for d in DEPS):
+        return LIB
+    tmp = BUILD / f"libz2doracle.{os.getpid()}.so"
+    cmd = ["g++", *CXXFLAGS, "-o", str(tmp), str(SRC)]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def load_oracle():
+    global _lib
+    with _lock:
+        if _lib is None:
+            lib = C.CDLL(str(build_oracle()))
+            lib.z2doracle_fill.argtypes = [C.POINTER(abi.z2d_surface), C.POINTER(abi.z2d_pattern),
+                                           C.POINTER(abi.z2d_node), C.c_size_t, C.POINTER(abi.z2d_fill_opts)]
+            lib.z2doracle_fill.restype = C.c_int
+            lib.z2doracle_composite.argtypes = [C.POINTER(abi.z2d_surface), C.c_int32, C.c_int32, C.c_int32,
+                                                C.POINTER(abi.z2d_operation), C.c_int32]
+            lib.z2doracle_composite.restype = C.c_int
+            lib.z2doracle_run_pixel.argtypes = [C.c_int32, abi.z2d_pixel, abi.z2d_pixel, C.c_int32]
+            lib.z2doracle_run_pixel.restype = abi.z2d_pixel
+            lib.z2doracle_pixel_from_color.argtypes = [abi.z2d_color]
+            lib.z2doracle_pixel_from_color.restype = abi.z2d_pixel
+            lib.z2doracle_gradient_offset.argtypes = [C.POINTER(abi.z2d_gradient), C.c_int32, C.c_int32]
+            lib.z2doracle_gradient_offset.restype = C.c_float
+            lib.z2doracle_gradient_pixel.argtypes = [C.POINTER(abi.z2d_gradient), C.c_int32, C.c_int32]
+            lib.z2doracle_gradient_pixel.restype = abi.z2d_pixel
+            lib.z2doracle_dither_pixel.argtypes = [C.POINTER(abi.z2d_pattern), C.c_int32, C.c_int32]
+            lib.z2doracle_dither_pixel.restype = abi.z2d_pixel
+            lib.z2doracle_plot.argtypes = [C.POINTER(abi.z2d_node), C.c_size_t, C.c_double, C.c_double,
+                                           C.POINTER(C.c_double), C.c_size_t, C.POINTER(C.c_double)]
+            lib.z2doracle_plot.restype = C.c_int64
+            lib.z2doracle_msaa_spans.argtypes = [C.c_uint32, C.POINTER(C.c_uint32), C.c_size_t,
+                                                 C.POINTER(C.c_uint32), C.c_size_t]
+            lib.z2doracle_msaa_spans.restype = C.c_uint32
+            _lib = lib
+    return _lib
+
+
+def _host_abi(sfc) -> abi.z2d_surface:
+    s = sfc.to_abi()
+    if s.location != abi.MEM_HOST:
+        raise ValueError("the oracle works on host surfaces only")
+    return s
+
+
+class Oracle:
+    """painter.fill / SurfaceCompositor.run restated on the CPU."""
+
+    def __init__(self):
+        self.lib = load_oracle()
+
+    def fill(self, surface, pattern: Pattern, nodes, opts: FillOptions = FillOptions()) -> int:
+        keep: list = []
+        s = _host_abi(surface)
+        p = pattern.to_abi(keep)
+        arr = nodes_to_abi(nodes)
+        n = len(nodes)
+        return self.lib.z2doracle_fill(C.byref(s), C.byref(p), arr, n, C.byref(opts.to_abi()))
+
+    def composite(self, dst, dst_x: int, dst_y: int, ops, precision: str = "integer") -> int:
+        keep: list = []
+        s = _host_abi(dst)
+        arr = (abi.z2d_operation * max(1, len(ops)))()
+        for i, o in enumerate(ops):
+            arr[i] = o.to_abi(keep, _host_abi)
+        prec = abi.PRECISION_FLOAT if precision == "float" else abi.PRECISION_INTEGER
+        return self.lib.z2doracle_composite(C.byref(s), dst_x, dst_y, len(ops), arr, prec)
+
+    def run_pixel(self, precision: str, dst, src, op: str):
+        prec = abi.PRECISION_FLOAT if precision == "float" else abi.PRECISION_INTEGER
+        return self.lib.z2doracle_run_pixel(prec, dst.to_abi(), src.to_abi(), abi.OP[op])
+
+    def pixel_from_color(self, color):
+        return self.lib.z2doracle_pixel_from_color(color.to_abi())
+
+    def gradient_offset(self, gradient, x: int, y: int) -> float:
+        keep: list = []
+        g = gradient.to_abi(keep)
+        return self.lib.z2doracle_gradient_offset(C.byref(g), x, y)
+
+    def gradient_pixel(self, gradient, x: int, y: int):
+        keep: list = []
+        g = gradient.to_abi(keep)
+        return self.lib.z2doracle_gradient_pixel(C.byref(g), x, y)
+
+    def dither_pixel(self, pattern: Pattern, x: int, y: int):
+        keep: list = []
+        p = pattern.to_abi(keep)
+        return self.lib.z2doracle_dither_pixel(C.byref(p), x, y)
+
+    def plot(self, nodes, scale: float, tolerance: float, cap: int = 1 << 16):
+        arr = nodes_to_abi(nodes)
+        out = (C.c_double * (4 * cap))()
+        ext = (C.c_double * 4)()
+        n = self.lib.z2doracle_plot(arr, len(nodes), scale, tolerance, out, cap, ext)
+        if n < 0:
+            return int(n), [], tuple(ext)
+        edges = [tuple(out[4 * i: 4 * i + 4]) for i in range(min(n, cap))]
+        return int(n), edges, tuple(ext)
+
+    def msaa_spans(self, capacity: int, spans, cap: int = 4096):
+        flat = (C.c_uint32 * max(1, 2 * len(spans)))(*[v for s in spans for v in s])
+        out = (C.c_uint32 * (2 * cap))()
+        n = self.lib.z2doracle_msaa_spans(capacity, flat, len(spans), out, cap)
+        return int(n), [(out[2 * i], out[2 * i + 1]) for i in range(min(n, cap))]

@@ -1,0 +1,397 @@
+"""z2d spec scenes restated against a fill/composite backend.
+
+Each function below re-expresses the drawing commands of one of z2d's spec
+scenes (spec/NNN_*.zig, 0BSD) that exercise only painter.fill and the
+compositor, using a small stand-in for z2d's Context (src/Context.zig:36-61,
+592-607, 679-699).  A backend provides fill(surface, pattern, nodes, opts)
+and composite(dst, x, y, ops, precision): the oracle for golden pinning, the
+GPU library for parity.
+"""
+from __future__ import annotations
+
+import math
+
+from z2d_gb300 import abi
+from z2d_gb300.path import Path
+from z2d_gb300.surface import Surface
+from z2d_gb300.types import Color, FillOptions, Gradient, Operation, Pattern, Pixel, wrap_dither
+
+
+class Ctx:
+    """The subset of z2d.Context the fill scenes use."""
+
+    def __init__(self, backend, surface: Surface):
+        self.backend = backend
+        self.surface = surface
+        self.pattern = Pattern.from_pixel(Pixel.rgba(0, 0, 0, 0xFF))
+        self.aa = "default"
+        self.fill_rule = "non_zero"
+        self.operator = "src_over"
+        self.precision = "integer"
+        self.tolerance = 0.1
+        self.dither = "none"
+        self.transformation = (1.0, 0.0, 0.0, 1.0, 0.0, 0.0)
+        self.path = Path()
+
+    def set_source(self, px: Pixel):
+        self.pattern = Pattern.from_pixel(px)
+
+    def move_to(self, x, y):
+        self.path.move_to(x, y)
+
+    def line_to(self, x, y):
+        self.path.line_to(x, y)
+
+    def curve_to(self, *a):
+        self.path.curve_to(*a)
+
+    def close_path(self):
+        self.path.close()
+
+    def reset_path(self):
+        self.path.reset()
+
+    def fill(self):
+        pat = wrap_dither(self.pattern, self.dither, self.surface.format)
+        opts = FillOptions(self.aa, self.fill_rule, self.operator, self.precision, self.tolerance)
+        rc = self.backend.fill(self.surface, pat, self.path.nodes, opts)
+        if rc != abi.OK:
+            raise RuntimeError(f"fill failed: {rc}")
+
+
+def _white_rgb():
+    return Pixel.rgb(0xFF, 0xFF, 0xFF)
+
+
+# --------------------------------------------------------------- fill scenes
+def s003_fill_triangle(be, aa):
+    w = h = 300
+    s = Surface.init("rgb", w, h)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    m = 10
+    c.move_to(0 + m, 0 + m)
+    c.line_to(w - m - 1, 0 + m)
+    c.line_to(w // 2 - 1, h - m - 1)
+    c.close_path()
+    c.fill()
+    return s
+
+
+def s004_fill_square(be, aa):
+    w = h = 300
+    s = Surface.init("rgb", w, h)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    m = 50
+    c.move_to(m, m)
+    c.line_to(w - m - 1, m)
+    c.line_to(w - m - 1, h - m - 1)
+    c.line_to(m, h - m - 1)
+    c.close_path()
+    c.fill()
+    return s
+
+
+def s005_fill_trapezoid(be, aa):
+    w = h = 300
+    s = Surface.init("rgb", w, h)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    mt, mb, my = 89, 50, 100
+    c.move_to(mt, my)
+    c.line_to(w - mt - 1, my)
+    c.line_to(w - mb - 1, h - my - 1)
+    c.line_to(mb, h - my - 1)
+    c.close_path()
+    c.fill()
+    return s
+
+
+def _star(c, w, h, margin, xs, ys, xo=0, yo=0, sw=None, sh=None):
+    sw = w if sw is None else sw
+    sh = h if sh is None else sh
+    c.move_to(xo + sw // 2, yo + margin)
+    c.line_to(xo + sw - margin * xs - 1, yo + sh - margin - 1)
+    c.line_to(xo + margin, yo + margin * ys)
+    c.line_to(xo + sw - margin - 1, yo + margin * ys)
+    c.line_to(xo + margin * xs, yo + sh - margin - 1)
+    c.close_path()
+
+
+def s006_fill_star_even_odd(be, aa):
+    w = h = 300
+    s = Surface.init("rgb", w, h)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.fill_rule = "even_odd"
+    _star(c, w, h, 20, 3, 5)
+    c.fill()
+    return s
+
+
+def s016_fill_star_non_zero(be, aa):
+    w = h = 300
+    s = Surface.init("rgb", w, h)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.fill_rule = "non_zero"
+    _star(c, w, h, 20, 3, 5)
+    c.fill()
+    return s
+
+
+def s007_fill_bezier(be, aa):
+    s = Surface.init("rgb", 300, 300)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.move_to(19, 249)
+    c.curve_to(89, 49, 209, 49, 279, 249)
+    c.close_path()
+    c.fill()
+    return s
+
+
+def s013_fill_combined(be, aa):
+    w, h = 600, 400
+    s = Surface.init("rgb", w, h)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    scw, sch = w // 3, h // 2
+    m = 10
+    c.move_to(m, m)
+    c.line_to(scw - m - 1, m)
+    c.line_to(scw // 2 - 1, sch - m - 1)
+    c.close_path()
+    m = 50
+    xo = scw
+    c.move_to(xo + m, m)
+    c.line_to(xo + scw - m - 1, m)
+    c.line_to(xo + scw - m - 1, sch - m - 1)
+    c.line_to(xo + m, sch - m - 1)
+    c.close_path()
+    tmt, tmb, tmy = 59, 33, 66
+    xo = scw * 2
+    c.move_to(xo + tmt, tmy)
+    c.line_to(xo + scw - tmt - 1, tmy)
+    c.line_to(xo + scw - tmb - 1, sch - tmy - 1)
+    c.line_to(xo + tmb, sch - tmy - 1)
+    c.close_path()
+    m = 13
+    xo = w // 6
+    yo = sch
+    _star(c, w, h, m, 3, 5, xo, yo, scw, sch)
+    xo += scw
+    c.move_to(xo + 12, yo + 166)
+    c.curve_to(xo + 59, yo + 32, xo + 139, yo + 32, xo + 186, yo + 166)
+    c.close_path()
+    c.fill()
+    return s
+
+
+def _tri(c, w, h, m=10):
+    c.move_to(m, m)
+    c.line_to(w - m - 1, m)
+    c.line_to(w // 2 - 1, h - m - 1)
+    c.close_path()
+
+
+def s024_fill_triangle_direct_cross_format(be, aa):
+    s = Surface.init("rgb", 300, 300)
+    c = Ctx(be, s)
+    c.set_source(Pixel.rgba(0xFF, 0x8A, 0xA5, 0xFF))
+    c.aa = aa
+    _tri(c, 300, 300)
+    c.fill()
+    return s
+
+
+def s025_fill_diamond_clipped(be, aa):
+    w = h = 300
+    s = Surface.init("rgb", w, h)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.move_to(w // 2, 0 - h // 10)
+    c.line_to(w + w // 10, h // 2)
+    c.line_to(w // 2, h + h // 10)
+    c.line_to(0 - w // 10, h // 2)
+    c.close_path()
+    c.fill()
+    return s
+
+
+def s026_fill_triangle_full(be, aa):
+    w = h = 300
+    s = Surface.init("rgb", w, h)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.move_to(0, 0)
+    c.line_to(w, 0)
+    c.line_to(w // 2, h)
+    c.close_path()
+    c.fill()
+    return s
+
+
+def s028_fill_bezier_tolerance(be, aa):
+    s = Surface.init("rgb", 900, 300)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    for x0, tol in ((0, None), (300, 3), (600, 10)):
+        if tol is not None:
+            c.tolerance = tol
+        c.reset_path()
+        c.move_to(x0 + 19, 224)
+        c.curve_to(x0 + 89, 49, x0 + 209, 49, x0 + 279, 224)
+        c.close_path()
+        c.fill()
+    return s
+
+
+def s031_fill_quad_bezier(be, aa):
+    s = Surface.init("rgb", 300, 300)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.move_to(20, 130)
+    c.curve_to(20, 130, 20, 20, 130, 20)
+    c.close_path()
+    c.move_to(170, 20)
+    c.curve_to(280, 20, 280, 20, 280, 130)
+    c.close_path()
+    c.move_to(280, 170)
+    c.curve_to(280, 280, 170, 280, 170, 280)
+    c.close_path()
+    c.move_to(130, 280)
+    c.curve_to(20, 280, 20, 280, 20, 170)
+    c.close_path()
+    c.fill()
+    return s
+
+
+def s046_fill_triangle_alpha(be, aa):
+    s = Surface.init_pixel(Pixel.rgb(0xFF, 0xFF, 0xFF), 300, 300)
+    c = Ctx(be, s)
+    c.set_source(Pixel.alpha8(255))
+    c.aa = aa
+    _tri(c, 300, 300)
+    c.fill()
+    return s
+
+
+def _alpha_tri(fmt, px):
+    def scene(be, aa):
+        s = Surface.init(fmt, 300, 300)
+        c = Ctx(be, s)
+        c.set_source(px)
+        c.aa = aa
+        _tri(c, 300, 300)
+        c.fill()
+        return s
+    return scene
+
+
+def s048_fill_triangle_static(be, aa):
+    s = Surface.init("rgb", 300, 300)
+    p = Path()
+    _tri_path(p)
+    rc = be.fill(s, Pattern.from_pixel(_white_rgb()), p.nodes, FillOptions(anti_aliasing=aa))
+    assert rc == abi.OK
+    return s
+
+
+def _tri_path(p, w=300, h=300, m=10):
+    p.move_to(m, m)
+    p.line_to(w - m - 1, m)
+    p.line_to(w // 2 - 1, h - m - 1)
+    p.close()
+
+
+def s079_fill_degenerate_lineto(be, aa):
+    s = Surface.init("rgb", 100, 200)
+    c = Ctx(be, s)
+    c.aa = aa
+    c.set_source(_white_rgb())
+    groups = [
+        [("m", 180, 180), ("l", 190, 190), ("c",)],
+        [("m", 10, 10), ("l", 20, 10), ("l", 20, 20), ("l", 10, 20), ("c",), ("m", 50, 10), ("l", 70, 20), ("c",)],
+        [("m", 10, 50), ("l", 30, 70), ("c",), ("m", 50, 50), ("l", 60, 50), ("l", 60, 60), ("l", 50, 60), ("c",)],
+        [("m", -30, 80), ("l", -10, 100), ("c",), ("m", 50, 80), ("l", 60, 80), ("l", 60, 90), ("l", 50, 90), ("c",)],
+        [("m", 10, 110), ("l", 30, 130), ("c",), ("m", 150, 110), ("l", 160, 110), ("l", 160, 120), ("l", 150, 120),
+         ("c",)],
+        [("m", 10, 140), ("l", 20, 140), ("l", 20, 150), ("l", 10, 150), ("c",), ("m", 50, 140), ("l", 70, 150), ("c",)],
+    ]
+    for g in groups:
+        c.reset_path()
+        for cmd in g:
+            if cmd[0] == "m":
+                c.move_to(cmd[1], cmd[2])
+            elif cmd[0] == "l":
+                c.line_to(cmd[1], cmd[2])
+            else:
+                c.close_path()
+        c.fill()
+    return s
+
+
+# --------------------------------------------------------- gradient scenes
+def _linear_draw(be, dst, scratch, sx, sy, x0, y0, x1, y1):
+    # spec/061_linear_gradient.zig draw()
+    g = Gradient.linear(x0, y0, x1, y1)
+    g.add_stop(0, Color.rgb(1, 0, 0))
+    g.add_stop(0.5, Color.rgb(0, 1, 0))
+    g.add_stop(1, Color.rgb(0, 0, 1))
+    assert be.composite(scratch, 0, 0, [Operation("src_over", src=Pattern.from_gradient(g))]) == abi.OK
+    assert be.composite(dst, sx, sy, [Operation("src_over", src=scratch)]) == abi.OK
+
+
+def s061_linear_gradient(be, aa=None):
+    dst = Surface.init("rgb", 200, 400)
+    scratch = Surface.init("rgb", 100, 100)
+    for args in ((0, 0, 0, 49, 99, 49), (100, 0, 99, 49, 0, 49), (0, 100, 49, 0, 49, 99),
+                 (100, 100, 49, 99, 49, 0), (0, 200, 0, 0, 99, 99), (100, 200, 99, 0, 0, 99),
+                 (0, 300, 0, 99, 99, 0), (100, 300, 99, 99, 0, 0)):
+        _linear_draw(be, dst, scratch, *args)
+    return dst
+
+
+FILL_SCENES = {
+    "003_fill_triangle": s003_fill_triangle,
+    "004_fill_square": s004_fill_square,
+    "005_fill_trapezoid": s005_fill_trapezoid,
+    "006_fill_star_even_odd": s006_fill_star_even_odd,
+    "007_fill_bezier": s007_fill_bezier,
+    "013_fill_combined": s013_fill_combined,
+    "016_fill_star_non_zero": s016_fill_star_non_zero,
+    "024_fill_triangle_direct_cross_format": s024_fill_triangle_direct_cross_format,
+    "025_fill_diamond_clipped": s025_fill_diamond_clipped,
+    "026_fill_triangle_full": s026_fill_triangle_full,
+    "028_fill_bezier_tolerance": s028_fill_bezier_tolerance,
+    "031_fill_quad_bezier": s031_fill_quad_bezier,
+    "046_fill_triangle_alpha": s046_fill_triangle_alpha,
+    "047_fill_triangle_alpha_gray": _alpha_tri("alpha8", Pixel.alpha8(119)),
+    "048_fill_triangle_static": s048_fill_triangle_static,
+    "049_fill_triangle_alpha4_gray": _alpha_tri("alpha4", Pixel.alpha4(7)),
+    "050_fill_triangle_alpha2_gray": _alpha_tri("alpha2", Pixel.alpha2(2)),
+    "051_fill_triangle_alpha1_gray": _alpha_tri("alpha1", Pixel.alpha1(1)),
+    "052_fill_triangle_alpha4_gray_scaledown": _alpha_tri("alpha4", Pixel.alpha8(119)),
+    "053_fill_triangle_alpha8_gray_scaleup": _alpha_tri("alpha8", Pixel.alpha4(7)),
+    "079_fill_degenerate_lineto": s079_fill_degenerate_lineto,
+}
+
+COMPOSITOR_SCENES = {
+    "061_linear_gradient": s061_linear_gradient,
+}
+
+# AA mode -> golden suffix (spec/main_spec.zig:564-634, 772-831)
+AA_SUFFIX = {"none": "_pixelated", "supersample_4x": "_smooth", "multisample_4x": "_smooth_multisample"}

@@ -1,0 +1,48 @@
+"""Pins the CPU oracle to z2d itself: the reference's golden PNGs for the
+fill/compositor spec scenes and its compositor known-answer tests."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from pngio import export_pixels, golden_pixels
+from scenes import AA_SUFFIX, COMPOSITOR_SCENES, FILL_SCENES
+from z2d_gb300.types import Color, Pixel
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.mark.parametrize("aa", list(AA_SUFFIX))
+@pytest.mark.parametrize("name", list(FILL_SCENES))
+def test_fill_scene_matches_golden(oracle, golden_dir, name, aa):
+    path = os.path.join(golden_dir, name + AA_SUFFIX[aa] + ".png")
+    if not os.path.exists(path):  # MSAA falls back to the SSAA golden (spec/main_spec.zig:786-800)
+        path = os.path.join(golden_dir, name + "_smooth.png")
+    got = export_pixels(FILL_SCENES[name](oracle, aa))
+    exp = golden_pixels(path)
+    assert got.shape == exp.shape
+    assert int((got != exp).any(-1).sum()) == 0
+
+
+@pytest.mark.parametrize("name", list(COMPOSITOR_SCENES))
+def test_compositor_scene_matches_golden(oracle, golden_dir, name):
+    got = export_pixels(COMPOSITOR_SCENES[name](oracle))
+    exp = golden_pixels(os.path.join(golden_dir, name + ".png"))
+    assert got.shape == exp.shape
+    assert np.array_equal(got, exp)
+
+
+def _kats():
+    with open(os.path.join(HERE, "golden", "compositor_kats.json")) as f:
+        d = json.load(f)
+    return [(prec, i, c) for prec in ("integer", "float") for i, c in enumerate(d[prec])]
+
+
+@pytest.mark.parametrize("prec,idx,case", _kats(), ids=lambda v: str(v) if not isinstance(v, dict) else v["op"])
+def test_compositor_kat(oracle, prec, idx, case):
+    bg = oracle.pixel_from_color(Color.rgb(*case["bg"]))
+    fg = oracle.pixel_from_color(Color.rgb(*case["fg"]))
+    r = oracle.run_pixel(prec, Pixel(bg.format, bg.r, bg.g, bg.b, bg.a),
+                         Pixel(fg.format, fg.r, fg.g, fg.b, fg.a), case["op"])
+    assert [r.r, r.g, r.b, r.a] == case["expected"]
