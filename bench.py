@@ -1,0 +1,335 @@
+"""Benchmark: Mpix/s of z2d's fill+composite path on one GB300.
+
+Workload (one "step"): the large plain-fill configuration -- a 4096x4096
+RGBA surface holding seeded uniform premultiplied pixels, then 2,000 random
+closed paths (3-64 segments, half lines / half cubic Beziers, control points
+uniform in a random box of side 16-1024 px), fill rule alternating
+even-odd / non-zero, random premultiplied pixel sources with alpha
+U[32,255], src_over, drawn in order.  Synthetic, seeded.
+
+Pixels counted (algorithmic, fixed before timing): the sum over fills of
+the clamped multisample draw box (multisample.zig:46-78).
+
+Arms of this implementation:
+  value  -- batched: all 2,000 fills in one z2dgpu_fill_batch call on a
+            device-resident surface (CUDA events on the library's stream).
+  plain  -- the per-call drop-in: 2,000 z2dgpu_fill calls (reported beside).
+  e2e    -- batched through the C ABI with a pinned HOST surface: the call
+            uploads the surface and nodes and reads the surface back inside
+            the timed region.
+The surface (64 MiB) fits in L2, so L2 is flushed (256 MiB write) before
+every timed step, outside the timed region.
+
+--impl reference times the CPU restatement of z2d's path (z2d itself is Zig
+and no Zig toolchain exists on these machines) on a bounded sample of the
+same fills, single-threaded like z2d's painter.fill.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W = H = 4096
+N_FILLS = 2000
+SEED = 2025
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
+CPU_SAMPLE_FILLS = 2000   # cpu_baseline sample: the whole workload (~10-20 s single-threaded)
+REF_STEP_FILLS = 400      # --impl reference: fills per timed step
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d, "measured"
+    except Exception:
+        return PEAKS_FALLBACK, "fallback"
+
+
+def workload():
+    from z2d_gb300.workloads import fill_box_pixels, premultiplied_background, random_fills
+    rng = np.random.default_rng(SEED)
+    bg = premultiplied_background(rng, W, H)
+    fills = random_fills(SEED + 1, N_FILLS, W, H)
+    px = [fill_box_pixels(n, W, H) for _, n, _ in fills]
+    return bg, fills, px
+
+
+def pack(fills):
+    """One node array plus a ctypes command array (no per-call marshalling)."""
+    import ctypes as C
+    from z2d_gb300 import abi
+    keep = []
+    nodes = np.concatenate([n for _, n, _ in fills])
+    cmds = (abi.z2d_fill_cmd * len(fills))()
+    off = 0
+    for i, (pat, n, opts) in enumerate(fills):
+        p = pat.to_abi(keep)
+        cmds[i].pattern = C.pointer(p)
+        cmds[i].node_offset = off
+        cmds[i].n_nodes = len(n)
+        cmds[i].opts = opts.to_abi()
+        off += len(n)
+    return nodes, cmds, keep
+
+
+class ClockSampler:
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", "0", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def union_box_pixels(fills):
+    """Pixels covered by the union of the fills' draw boxes (surface bytes
+    the rasteriser must read and write at least once)."""
+    import math
+    from z2d_gb300 import abi
+    cov = np.zeros((H, W), bool)
+    for _, nodes, _ in fills:
+        pts = []
+        for nd in nodes:
+            t = nd["tag"]
+            if t in (abi.MOVE_TO, abi.LINE_TO):
+                pts.append(nd["p"][:2])
+            elif t == abi.CURVE_TO:
+                pts.extend([nd["p"][0:2], nd["p"][2:4], nd["p"][4:6]])
+        p = np.array(pts)
+        x0 = min(max(int(math.floor(p[:, 0].min())), 0), W - 1)
+        x1 = min(max(int(math.ceil(p[:, 0].max())), x0), W)
+        y0 = min(max(int(math.floor(p[:, 1].min())), 0), H - 1)
+        y1 = min(max(int(math.ceil(p[:, 1].max())), y0), H - 1)
+        cov[y0:y1 + 1, x0:x1] = True
+    return int(cov.sum())
+
+
+def cpu_sample(bg, fills, px, n_fills):
+    from oracle import Oracle
+    from z2d_gb300.surface import Surface
+    o = Oracle()
+    s = Surface("rgba", W, H, bg.copy())
+    t0 = time.perf_counter()
+    for pat, nodes, opts in fills[:n_fills]:
+        o.fill(s, pat, nodes, opts)
+    dt = time.perf_counter() - t0
+    return sum(px[:n_fills]) / 1e6 / dt, dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    bg, fills, px = workload()
+    from oracle import build_oracle
+    build_oracle()
+    times, mpix = [], 0.0
+    for _ in range(args.warmup):
+        cpu_sample(bg, fills, px, 4)
+    for _ in range(args.steps):
+        v, dt = cpu_sample(bg, fills, px, REF_STEP_FILLS)
+        times.append(dt)
+        mpix += sum(px[:REF_STEP_FILLS]) / 1e6
+    value = mpix / sum(times)
+    sample = f"first {REF_STEP_FILLS} of the {N_FILLS} fills of the 4096x4096 workload per step"
+    line = {
+        "impl": "reference", "metric": "Mpix/s fill+composite (src_over, 4096x4096 RGBA, 2000 random paths)",
+        "value": value, "unit": "Mpix/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded)",
+        "config": {"workload": "plain_large_4096x4096_2000_paths", "surface": "rgba 4096x4096", "paths": N_FILLS},
+        "cpu_baseline": {"value": value, "unit": "Mpix/s", "cores": 1, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "z2d is Zig; no Zig toolchain here, so the CPU restatement of its path is timed "
+                "(single-threaded: z2d's painter.fill on one surface is sequential)",
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from z2d_gb300 import painter
+    from z2d_gb300.native import Context
+    from z2d_gb300.surface import Surface
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    bg, fills, px = workload()
+    mpix_step = sum(px) / 1e6
+    nodes, cmds, keep = pack(fills)
+
+    stream = torch.cuda.Stream(device=dev)
+    ctx = Context(local, stream)
+    bg_dev = torch.from_numpy(bg).to(dev)
+    surf_t = bg_dev.clone()
+    surf = Surface("rgba", W, H, surf_t)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def restore():
+        with torch.cuda.stream(stream):
+            surf_t.copy_(bg_dev)
+            flush.fill_(1)
+
+    # ---- warm-up
+    for _ in range(max(args.warmup, 1)):
+        restore()
+        painter.fill_batch_arrays(surf, nodes, cmds, ctx=ctx)
+    stream.synchronize()
+
+    # ---- timed batched steps (device-resident)
+    ctx.set_timing(True)
+    launches0 = ctx.launch_count
+    clocks = ClockSampler()
+    clocks.start()
+    step_ms = []
+    for _ in range(args.steps):
+        restore()
+        if world > 1:
+            dist.barrier()
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        painter.fill_batch_arrays(surf, nodes, cmds, ctx=ctx)
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+    clk = clocks.stop()
+    launches = ctx.launch_count - launches0
+    raster_ms, raster_n = ctx.kernel_ms("raster")
+    ctx.set_timing(False)
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * mpix_step * args.steps / (total_ms / 1e3)
+
+    # ---- plain per-call arm (one step)
+    restore()
+    stream.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for pat, n, opts in fills:
+        painter.fill(surf, pat, n, opts, ctx=ctx)
+    e1.record(stream)
+    e1.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+
+    # ---- e2e: pinned host surface through the C ABI (H2D + D2H inside)
+    host_t = torch.empty(bg.size, dtype=torch.uint8, pin_memory=True)
+    host = host_t.numpy()
+    hsurf = Surface("rgba", W, H, host)
+    e2e_s = []
+    for _ in range(args.steps):
+        host[:] = bg
+        restore()
+        stream.synchronize()
+        t0 = time.perf_counter()
+        painter.fill_batch_arrays(hsurf, nodes, cmds, ctx=ctx)
+        e2e_s.append(time.perf_counter() - t0)
+    e2e_value = mpix_step * args.steps / sum(e2e_s)
+    h2d = bg.nbytes + nodes.nbytes + len(fills) * 64
+    d2h = bg.nbytes
+
+    if rank != 0:
+        return
+    peaks, peak_kind = load_peaks()
+    union_px = union_box_pixels(fills)
+    alg_bytes = 2 * 4 * union_px  # read + write of every surface pixel a fill box touches
+    raster_ms_per = raster_ms / max(raster_n, 1)
+    achieved = alg_bytes / (raster_ms_per / 1e3) / 1e9
+    cpu_v, cpu_dt = cpu_sample(bg, fills, px, CPU_SAMPLE_FILLS)
+    line = {
+        "metric": "Mpix/s fill+composite (src_over, 4096x4096 RGBA, 2000 random paths)",
+        "value": value, "unit": "Mpix/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded)",
+        "config": {"workload": "plain_large_4096x4096_2000_paths", "surface": "rgba 4096x4096",
+                   "paths": N_FILLS, "mpix_per_step": mpix_step, "l2": "flushed (256 MiB write) before each step",
+                   "mode": "batched (z2dgpu_fill_batch, device-resident surface)"},
+        "plain": {"value": mpix_step / (plain_ms / 1e3), "unit": "Mpix/s", "ms_per_step": plain_ms,
+                  "calls": len(fills)},
+        "batched_over_plain": (mpix_step / (total_ms / args.steps / 1e3)) / (mpix_step / (plain_ms / 1e3)),
+        "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "kernel": "k_raster", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                     "peak_source": peak_kind, "alg_bytes_per_launch": alg_bytes,
+                     "launch_ms": raster_ms_per},
+        "cpu_baseline": {"value": cpu_v, "unit": "Mpix/s", "cores": 1, "kind": "port",
+                         "sample": f"first {CPU_SAMPLE_FILLS} of {N_FILLS} fills, {cpu_dt:.1f} s"},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -25,7 +25,9 @@
  *   ALPHA8 1 B/px
  *   ALPHA4/2/1 packed: pixel i (flat index w*y+x) occupies bits
  *     [i*bits, i*bits+bits) little-endian (LSB first); rows are NOT byte
- *     aligned.  Buffer length ceil(w*h*bits/8).
+ *     aligned.  Buffer length ceil(w*h*bits/8); DEVICE buffers of these
+ *     formats must be allocated up to the next multiple of 4 bytes (pixels
+ *     are updated with 32-bit atomics).
  *
  * Threading: a context owns one CUDA stream and device scratch; calls on one
  * context must not overlap.  Use one context per host thread.
@@ -218,6 +220,15 @@ Z2D_API int z2dgpu_ctx_destroy(z2dgpu_ctx *ctx);
 Z2D_API int z2dgpu_ctx_synchronize(z2dgpu_ctx *ctx);
 /* Number of kernels this context has launched since creation. */
 Z2D_API uint64_t z2dgpu_ctx_launch_count(const z2dgpu_ctx *ctx);
+
+/* Kernel timing: when enabled, the context brackets its dominant kernels
+ * (the fill rasteriser "raster" and the compositor "composite") with CUDA
+ * events on its stream and accumulates their device time.  Reading a time
+ * synchronizes the context.  No reference counterpart (instrumentation). */
+Z2D_API int z2dgpu_ctx_set_timing(z2dgpu_ctx *ctx, int enable);
+/* Accumulated milliseconds and launch count of `kernel` since timing was
+ * enabled; returns -1 for an unknown name. */
+Z2D_API double z2dgpu_ctx_kernel_ms(z2dgpu_ctx *ctx, const char *kernel, uint64_t *launches);
 
 /* Bytes of pixel storage for a surface (src/surface.zig:382-395, 621-635). */
 Z2D_API size_t z2dgpu_surface_bytes(int32_t format, int32_t width, int32_t height);

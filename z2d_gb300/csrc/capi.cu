@@ -1,0 +1,669 @@
+// capi.cu -- the C ABI of include/z2dgpu.h: contexts, validation that
+// mirrors painter.fill's error checks, descriptor preparation, host <->
+// device staging, and dispatch into the fill and compositor kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fill.cuh"
+#include "z2d_internal.h"
+
+namespace z2dg {
+
+static thread_local std::string g_err;
+
+void set_error(const std::string &msg) { g_err = msg; }
+int cuda_fail(cudaError_t e, const char *what) {
+    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return Z2D_ERR_CUDA;
+}
+
+int DevBuf::ensure(size_t bytes) {
+    if (bytes <= cap) return 0;
+    size_t n = std::max(bytes, cap + cap / 2);
+    n = (n + 4095) & ~(size_t)4095;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    if (cudaMalloc(&ptr, n) != cudaSuccess) {
+        ptr = nullptr;
+        set_error("device allocation of " + std::to_string(n) + " bytes failed");
+        return 1;
+    }
+    cap = n;
+    return 0;
+}
+void DevBuf::release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+}
+int HostBuf::ensure(size_t bytes) {
+    if (bytes <= cap) return 0;
+    size_t n = std::max(bytes, cap + cap / 2);
+    n = (n + 4095) & ~(size_t)4095;
+    if (ptr) cudaFreeHost(ptr);
+    ptr = nullptr;
+    cap = 0;
+    if (cudaMallocHost(&ptr, n) != cudaSuccess) {
+        ptr = nullptr;
+        set_error("pinned host allocation failed");
+        return 1;
+    }
+    cap = n;
+    return 0;
+}
+void HostBuf::release() {
+    if (ptr) cudaFreeHost(ptr);
+    ptr = nullptr;
+    cap = 0;
+}
+
+cudaEvent_t Ctx::timer_begin(Timer &t) {
+    if (!timing) return nullptr;
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    cudaEventRecord(e, stream);
+    return e;
+}
+void Ctx::timer_end(Timer &t, cudaEvent_t start) {
+    if (!start) return;
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+        cudaEventDestroy(start);
+        return;
+    }
+    cudaEventRecord(e, stream);
+    t.pending.push_back(start);
+    t.pending.push_back(e);
+}
+void Ctx::timer_collect(Timer &t) {
+    for (size_t i = 0; i + 1 < t.pending.size(); i += 2) {
+        float ms = 0;
+        cudaEventSynchronize(t.pending[i + 1]);
+        if (cudaEventElapsedTime(&ms, t.pending[i], t.pending[i + 1]) == cudaSuccess) {
+            t.ms += ms;
+            t.n++;
+        }
+        cudaEventDestroy(t.pending[i]);
+        cudaEventDestroy(t.pending[i + 1]);
+    }
+    t.pending.clear();
+}
+
+// ---------------------------------------------- descriptor preparation
+int make_dev_gradient(const z2d_gradient &g, DevGradient &out) {
+    memset(&out, 0, sizeof(out));
+    if (g.n_stops < 0 || g.n_stops > kMaxStops || (g.n_stops > 0 && !g.stops)) {
+        set_error("gradient: 0.." + std::to_string(kMaxStops) + " stops supported");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    if (g.type < Z2D_GRADIENT_LINEAR || g.type > Z2D_GRADIENT_CONIC || g.method < 0 || g.method > Z2D_INTERP_HSL_DECREASING) {
+        set_error("gradient: bad type or interpolation method");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    out.type = g.type;
+    out.method = g.method;
+    out.n_stops = g.n_stops;
+    static const double ident[6] = {1, 0, 0, 1, 0, 0};
+    out.has_tf = 0;
+    for (int i = 0; i < 6; i++) {
+        out.g[i] = g.geom[i];
+        out.tf[i] = g.transform[i];
+        if (!(g.transform[i] == ident[i])) out.has_tf = 1;  // Transformation.equal
+    }
+    // Stop.List.addAssumeCapacity: clamp, then order by (offset, insertion)
+    struct S {
+        float off;
+        int idx;
+    };
+    std::vector<S> order((size_t)g.n_stops);
+    for (int i = 0; i < g.n_stops; i++) order[i] = S{std::fmax(0.0f, std::fmin(g.stops[i].offset, 1.0f)), i};
+    std::stable_sort(order.begin(), order.end(), [](const S &a, const S &b) {
+        if (a.off == b.off) return a.idx < b.idx;
+        return a.off < b.off;
+    });
+    for (int i = 0; i < g.n_stops; i++) {
+        out.offsets[i] = order[i].off;
+        out.colors[i] = g.stops[order[i].idx].color;
+    }
+    if (g.type == Z2D_GRADIENT_RADIAL) {  // Radial.initBuffer (src/gradient.zig:401-438)
+        const double ir = std::fmax(0.0, g.geom[2]), orr = std::fmax(0.0, g.geom[5]);
+        out.inner_r = ir;
+        out.outer_r = orr;
+        out.cdx = g.geom[3] - g.geom[0];
+        out.cdy = g.geom[4] - g.geom[1];
+        out.dr = orr - ir;
+        out.min_dr = -ir;
+        double a = 0;
+        a += out.cdx * out.cdx;
+        a += out.cdy * out.cdy;
+        a += out.dr * -out.dr;
+        out.a = a;
+        out.inv_a = (a != 0) ? 1 / a : 0;
+    } else if (g.type == Z2D_GRADIENT_CONIC) {  // Conic.initBuffer (:666-681)
+        const double twopi = 6.283185307179586;
+        const double r = std::fmod(g.geom[2], twopi);
+        out.angle = g.geom[2] < 0.0 ? std::fmod(r + twopi, twopi) : r;
+    }
+    return Z2D_OK;
+}
+
+static bool valid_format(int f) { return f >= Z2D_FORMAT_ARGB && f <= Z2D_FORMAT_ALPHA1; }
+
+static int check_pixel(const z2d_pixel &p) {
+    if (!valid_format(p.format)) {
+        set_error("pixel: bad format");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    if (fmt_packed(p.format) && p.a > fmt_max(p.format)) {
+        set_error("pixel: alpha out of range for its format");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    return Z2D_OK;
+}
+
+int make_dev_src_from_pattern(int param_kind, const z2d_pattern &p, DevSrc &out, bool &needs_grad, DevGradient &grad_out) {
+    memset(&out, 0, sizeof(out));
+    needs_grad = false;
+    out.kind = param_kind == Z2D_PARAM_PIXEL ? SRC_PIXEL : param_kind == Z2D_PARAM_GRADIENT ? SRC_GRADIENT : SRC_DITHER;
+    if (out.kind == SRC_PIXEL || (out.kind == SRC_DITHER && p.dither_source == Z2D_DITHER_SRC_PIXEL)) {
+        const int rc = check_pixel(p.pixel);
+        if (rc) return rc;
+        out.px = Px{p.pixel.format, p.pixel.r, p.pixel.g, p.pixel.b, p.pixel.a};
+        out.pix = i16_from_pixel(out.px);
+        out.pixf = F4{(float)out.pix.r / 255.0f, (float)out.pix.g / 255.0f, (float)out.pix.b / 255.0f, (float)out.pix.a / 255.0f};
+    }
+    if (out.kind == SRC_GRADIENT || (out.kind == SRC_DITHER && p.dither_source == Z2D_DITHER_SRC_GRADIENT)) {
+        if (!p.gradient) {
+            set_error("pattern: gradient missing");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+        const int rc = make_dev_gradient(*p.gradient, grad_out);
+        if (rc) return rc;
+        needs_grad = true;
+    }
+    if (out.kind == SRC_DITHER) {
+        if (p.dither_type < Z2D_DITHER_NONE || p.dither_type > Z2D_DITHER_BLUE_NOISE || p.dither_scale < 1 || p.dither_scale > 15 ||
+            p.dither_source < Z2D_DITHER_SRC_PIXEL || p.dither_source > Z2D_DITHER_SRC_GRADIENT) {
+            set_error("dither: bad type, source or scale");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+        out.dither_type = p.dither_type;
+        out.dither_source = p.dither_source;
+        out.dither_scale = p.dither_scale;
+        if (p.dither_source == Z2D_DITHER_SRC_PIXEL) {
+            // LinearRGB.decodeRGBA: integer demultiply, then /255 (src/color.zig:261-269)
+            I16 v = out.pix;
+            if (v.a == 0) v = I16{0, 0, 0, 0};
+            else v = I16{(v.r * 255 / v.a) & 0xFFu, (v.g * 255 / v.a) & 0xFFu, (v.b * 255 / v.a) & 0xFFu, v.a};
+            out.dither_base = RGBf{(float)v.r / 255.0f, (float)v.g / 255.0f, (float)v.b / 255.0f, (float)v.a / 255.0f};
+        } else if (p.dither_source == Z2D_DITHER_SRC_COLOR) {
+            // LinearRGB.fromColor (src/color.zig:227-249), same arithmetic
+            // on the host (compiled without FP contraction)
+            if (p.dither_color.space < Z2D_COLOR_LINEAR_RGB || p.dither_color.space > Z2D_COLOR_HSL) {
+                set_error("dither: bad color space");
+                return Z2D_ERR_INVALID_ARGUMENT;
+            }
+            out.dither_base = linear_from_color(p.dither_color);
+        }
+    }
+    return Z2D_OK;
+}
+
+static bool pixel_premultiplied(const z2d_pixel &p) {  // canDemultiply (src/pixel.zig:504-514)
+    if (p.format != Z2D_FORMAT_ARGB && p.format != Z2D_FORMAT_RGBA) return true;
+    if (p.a == 0) return true;
+    const int ch[3] = {p.r, p.g, p.b};
+    for (int v : ch)
+        if (v * 255 / p.a > 255) return false;
+    return true;
+}
+
+// PathNode.isClosedNodeSet (src/internal/path_nodes.zig:23-36)
+static bool is_closed(const z2d_node *nodes, size_t n) {
+    if (n == 0) return false;
+    bool closed = false;
+    for (size_t i = 0; i < n; i++) {
+        switch (nodes[i].tag) {
+            case Z2D_MOVE_TO:
+                if (!closed && i != 0) return false;
+                break;
+            case Z2D_CLOSE_PATH: closed = true; break;
+            default: closed = false; break;
+        }
+    }
+    return closed;
+}
+
+// The validation of painter.fill (src/painter.zig:73-91) plus the
+// conditions under which fill_plotter.plot reports InvalidState.
+static int check_fill(const z2d_surface &s, const z2d_pattern &p, const z2d_node *nodes, size_t n, const z2d_fill_opts &o) {
+    if (p.kind == Z2D_PATTERN_PIXEL) {
+        const int rc = check_pixel(p.pixel);
+        if (rc) return rc;
+        if (!pixel_premultiplied(p.pixel)) {
+            set_error("PixelSourceNotPreMultiplied");
+            return Z2D_ERR_PIXEL_NOT_PREMULTIPLIED;
+        }
+    } else if (p.kind != Z2D_PATTERN_GRADIENT && p.kind != Z2D_PATTERN_DITHER) {
+        set_error("pattern: bad kind");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    if (o.op < 0 || o.op >= Z2D_OP_COUNT || (o.fill_rule != Z2D_FILL_NON_ZERO && o.fill_rule != Z2D_FILL_EVEN_ODD) ||
+        o.anti_aliasing < Z2D_AA_NONE || o.anti_aliasing > Z2D_AA_SUPERSAMPLE_4X ||
+        (o.precision != Z2D_PRECISION_INTEGER && o.precision != Z2D_PRECISION_FLOAT) || !(o.tolerance == o.tolerance)) {
+        set_error("fill options out of range");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    if (n == 0) return Z2D_OK;
+    if (!nodes) return Z2D_ERR_INVALID_ARGUMENT;
+    if (!is_closed(nodes, n)) {
+        set_error("PathNotClosed");
+        return Z2D_ERR_PATH_NOT_CLOSED;
+    }
+    bool seen_move = false;
+    for (size_t i = 0; i < n; i++) {
+        const z2d_node &nd = nodes[i];
+        if (nd.tag < Z2D_MOVE_TO || nd.tag > Z2D_CLOSE_PATH) {
+            set_error("node: bad tag");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+        if (nd.tag == Z2D_MOVE_TO) seen_move = true;
+        if ((nd.tag == Z2D_LINE_TO || nd.tag == Z2D_CURVE_TO) && !seen_move) {
+            set_error("InvalidState: line_to/curve_to without a current point");
+            return Z2D_ERR_INVALID_STATE;
+        }
+        const int np = nd.tag == Z2D_CURVE_TO ? 6 : nd.tag == Z2D_CLOSE_PATH ? 0 : 2;
+        for (int k = 0; k < np; k++) {
+            if (!std::isfinite(nd.p[k])) {
+                set_error("InvalidState: non-finite coordinate");
+                return Z2D_ERR_INVALID_STATE;
+            }
+            if (std::fabs(nd.p[k]) > 16777216.0) {
+                set_error("coordinate outside +-2^24 (z2d's Path clamps to the i24 range)");
+                return Z2D_ERR_INVALID_ARGUMENT;
+            }
+        }
+    }
+    (void)s;
+    return Z2D_OK;
+}
+
+static int check_surface(const z2d_surface *s) {
+    if (!s) return Z2D_ERR_INVALID_ARGUMENT;
+    if (!valid_format(s->format)) {
+        set_error("surface: bad format");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    if (s->width < 1 || s->height < 1) {
+        set_error(s->width < 1 ? "InvalidWidth" : "InvalidHeight");
+        return Z2D_ERR_INVALID_DIMENSIONS;
+    }
+    if (!s->data || (s->location != Z2D_MEM_HOST && s->location != Z2D_MEM_DEVICE)) return Z2D_ERR_INVALID_ARGUMENT;
+    if (s->location == Z2D_MEM_DEVICE && fmt_bits(s->format) >= 32 && (reinterpret_cast<uintptr_t>(s->data) & 3)) {
+        set_error("surface: device data of 32-bit formats must be 4-byte aligned");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    if (s->location == Z2D_MEM_DEVICE && fmt_packed(s->format) && (reinterpret_cast<uintptr_t>(s->data) & 3)) {
+        set_error("surface: device data of packed formats must be 4-byte aligned");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    return Z2D_OK;
+}
+
+static size_t sfc_bytes(const z2d_surface &s) { return ((size_t)s.width * (size_t)s.height * (size_t)fmt_bits(s.format) + 7) / 8; }
+
+// Device view of a surface; host surfaces are staged through `buf` (sized
+// up to a 4-byte multiple so packed word atomics stay in bounds).
+static int stage_in(Ctx &c, const z2d_surface &s, DevBuf &buf, DevSurface &out) {
+    out.fmt = s.format;
+    out.w = s.width;
+    out.h = s.height;
+    if (s.location == Z2D_MEM_DEVICE) {
+        out.data = reinterpret_cast<uint8_t *>(s.data);
+        return Z2D_OK;
+    }
+    const size_t bytes = sfc_bytes(s);
+    if (buf.ensure(((bytes + 15) & ~(size_t)15) + 16)) return Z2D_ERR_OUT_OF_MEMORY;
+    Z2D_CUDA(cudaMemcpyAsync(buf.ptr, s.data, bytes, cudaMemcpyHostToDevice, c.stream));
+    out.data = buf.as<uint8_t>();
+    return Z2D_OK;
+}
+static int stage_out(Ctx &c, const z2d_surface &s, const DevSurface &d) {
+    if (s.location == Z2D_MEM_DEVICE) return Z2D_OK;
+    Z2D_CUDA(cudaMemcpyAsync(s.data, d.data, sfc_bytes(s), cudaMemcpyDeviceToHost, c.stream));
+    Z2D_CUDA(cudaStreamSynchronize(c.stream));
+    return Z2D_OK;
+}
+
+// Builds the prepared commands of a list of fills.
+static int prepare_fills(const z2d_surface &s, const z2d_node *nodes, size_t n_nodes, const z2d_fill_cmd *cmds, size_t n_cmds,
+                         std::vector<FillCmd> &fills, std::vector<int32_t> &node_fill, std::vector<DevGradient> &grads,
+                         std::vector<int32_t> &grad_of_fill) {
+    if (n_nodes > 0x7FFFFFFF || n_cmds > 0x7FFFFFF) {
+        set_error("batch too large");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    node_fill.assign(n_nodes, -1);
+    for (size_t i = 0; i < n_cmds; i++) {
+        const z2d_fill_cmd &cm = cmds[i];
+        if (!cm.pattern) return Z2D_ERR_INVALID_ARGUMENT;
+        if (cm.node_offset > n_nodes || cm.n_nodes > n_nodes - cm.node_offset) {
+            set_error("fill command outside the node array");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+        const z2d_node *nd = nodes + cm.node_offset;
+        int rc = check_fill(s, *cm.pattern, nd, cm.n_nodes, cm.opts);
+        if (rc) return rc;
+        if (cm.n_nodes == 0) continue;  // painter.fill returns early
+        const int aa = (s.format == Z2D_FORMAT_ALPHA1) ? Z2D_AA_NONE : cm.opts.anti_aliasing;
+        if (aa == Z2D_AA_SUPERSAMPLE_4X) {
+            set_error("supersample_4x is not implemented on the GPU path; use default/multisample_4x or none");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+        FillCmd F;
+        memset(&F, 0, sizeof(F));
+        F.node_off = (int32_t)cm.node_offset;
+        F.n_nodes = (int32_t)cm.n_nodes;
+        F.aa = aa == Z2D_AA_NONE ? Z2D_AA_NONE : Z2D_AA_MULTISAMPLE_4X;
+        F.rule = cm.opts.fill_rule;
+        F.op = cm.opts.op;
+        F.precision = requires_float(F.op) ? Z2D_PRECISION_FLOAT : cm.opts.precision;
+        F.tol = std::fmax(cm.opts.tolerance, 0.001);
+        F.scale = F.aa == Z2D_AA_NONE ? 1.0 : 4.0;
+        F.pattern_kind = cm.pattern->kind;
+        const int pk = cm.pattern->kind == Z2D_PATTERN_PIXEL      ? Z2D_PARAM_PIXEL
+                       : cm.pattern->kind == Z2D_PATTERN_GRADIENT ? Z2D_PARAM_GRADIENT
+                                                                  : Z2D_PARAM_DITHER;
+        bool needs_grad = false;
+        DevGradient g;
+        rc = make_dev_src_from_pattern(pk, *cm.pattern, F.src, needs_grad, g);
+        if (rc) return rc;
+        if (needs_grad) {
+            grad_of_fill.push_back((int32_t)grads.size());
+            grads.push_back(g);
+        } else {
+            grad_of_fill.push_back(-1);
+        }
+        if (F.pattern_kind == Z2D_PATTERN_PIXEL) {
+            const Px px = F.src.px;
+            bool opaque = (px.fmt == Z2D_FORMAT_XRGB || px.fmt == Z2D_FORMAT_RGB) ? true : px.a == fmt_max(px.fmt);
+            F.reduces = (F.op == Z2D_OP_SRC) || (F.op == Z2D_OP_SRC_OVER && opaque);
+            F.px_paint = convert_px(px, s.format);
+            F.px_rgba = to_i16(convert_px(px, Z2D_FORMAT_RGBA));
+        }
+        const int32_t fi = (int32_t)fills.size();
+        for (size_t k = 0; k < cm.n_nodes; k++) {
+            if (node_fill[cm.node_offset + k] != -1) {
+                set_error("fill commands must not share nodes");
+                return Z2D_ERR_INVALID_ARGUMENT;
+            }
+            node_fill[cm.node_offset + k] = fi;
+        }
+        fills.push_back(F);
+    }
+    return Z2D_OK;
+}
+
+static int do_fill_batch(Ctx &c, z2d_surface *surface, const z2d_node *nodes, size_t n_nodes, const z2d_fill_cmd *cmds,
+                         size_t n_cmds) {
+    int rc = check_surface(surface);
+    if (rc) return rc;
+    if (n_cmds > 0 && !cmds) return Z2D_ERR_INVALID_ARGUMENT;
+    std::vector<FillCmd> fills;
+    std::vector<int32_t> node_fill, grad_of_fill;
+    std::vector<DevGradient> grads;
+    rc = prepare_fills(*surface, nodes, n_nodes, cmds, n_cmds, fills, node_fill, grads, grad_of_fill);
+    if (rc) return rc;
+    if (fills.empty()) return Z2D_OK;
+    // compact the node array to the nodes that belong to a fill
+    std::vector<z2d_node> used;
+    std::vector<int32_t> used_fill;
+    used.reserve(n_nodes);
+    std::vector<int32_t> new_off(fills.size(), -1);
+    for (size_t i = 0; i < n_nodes; i++) {
+        const int32_t f = node_fill[i];
+        if (f < 0) continue;
+        if (new_off[f] < 0) new_off[f] = (int32_t)used.size();
+        used.push_back(nodes[i]);
+        used_fill.push_back(f);
+    }
+    for (size_t f = 0; f < fills.size(); f++) fills[f].node_off = new_off[f];
+    DevSurface ds;
+    rc = stage_in(c, *surface, c.surface, ds);
+    if (rc) return rc;
+    rc = run_fills(c, ds, used.data(), (int32_t)used.size(), fills, used_fill, grads, grad_of_fill);
+    if (rc) return rc;
+    return stage_out(c, *surface, ds);
+}
+
+}  // namespace z2dg
+
+using namespace z2dg;
+
+struct z2dgpu_ctx : public Ctx {};
+
+extern "C" {
+
+Z2D_API const char *z2dgpu_version(void) { return "z2dgpu 0.1.0 (sm_103a)"; }
+
+Z2D_API const char *z2dgpu_last_error(void) { return g_err.c_str(); }
+
+Z2D_API int z2dgpu_ctx_create(z2dgpu_ctx **out, int device, void *stream) {
+    if (!out) return Z2D_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    Z2D_CUDA(cudaSetDevice(device));
+    z2dgpu_ctx *c = new z2dgpu_ctx();
+    c->device = device;
+    if (stream) {
+        c->stream = reinterpret_cast<cudaStream_t>(stream);
+    } else {
+        cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            delete c;
+            return cuda_fail(e, "cudaStreamCreate");
+        }
+        c->own_stream = true;
+    }
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (c->sm_count <= 0) c->sm_count = 1;
+    *out = c;
+    return Z2D_OK;
+}
+
+Z2D_API int z2dgpu_ctx_destroy(z2dgpu_ctx *c) {
+    if (!c) return Z2D_OK;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    DevBuf *bufs[] = {&c->params, &c->nodes, &c->node_info, &c->edges, &c->fill_state, &c->counters, &c->band_fills,
+                      &c->bins, &c->bin_offsets, &c->masks, &c->surface, &c->surface2, &c->surface3, &c->scan_tmp};
+    for (DevBuf *b : bufs) b->release();
+    c->staging.release();
+    c->readback.release();
+    c->timer_collect(c->t_raster);
+    c->timer_collect(c->t_composite);
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return Z2D_OK;
+}
+
+Z2D_API int z2dgpu_ctx_synchronize(z2dgpu_ctx *c) {
+    if (!c) return Z2D_ERR_INVALID_ARGUMENT;
+    Z2D_CUDA(cudaStreamSynchronize(c->stream));
+    return Z2D_OK;
+}
+
+Z2D_API uint64_t z2dgpu_ctx_launch_count(const z2dgpu_ctx *c) { return c ? c->launches : 0; }
+
+Z2D_API int z2dgpu_ctx_set_timing(z2dgpu_ctx *c, int enable) {
+    if (!c) return Z2D_ERR_INVALID_ARGUMENT;
+    c->timer_collect(c->t_raster);
+    c->timer_collect(c->t_composite);
+    c->t_raster = Ctx::Timer{};
+    c->t_composite = Ctx::Timer{};
+    c->timing = enable != 0;
+    return Z2D_OK;
+}
+
+Z2D_API double z2dgpu_ctx_kernel_ms(z2dgpu_ctx *c, const char *kernel, uint64_t *launches) {
+    if (!c || !kernel) return -1.0;
+    Ctx::Timer *t = nullptr;
+    if (strcmp(kernel, "raster") == 0) t = &c->t_raster;
+    else if (strcmp(kernel, "composite") == 0) t = &c->t_composite;
+    if (!t) return -1.0;
+    c->timer_collect(*t);
+    if (launches) *launches = t->n;
+    return t->ms;
+}
+
+Z2D_API size_t z2dgpu_surface_bytes(int32_t format, int32_t width, int32_t height) {
+    if (!valid_format(format) || width < 1 || height < 1) return 0;
+    return ((size_t)width * (size_t)height * (size_t)fmt_bits(format) + 7) / 8;
+}
+
+Z2D_API int z2dgpu_fill(z2dgpu_ctx *c, z2d_surface *surface, const z2d_pattern *pattern, const z2d_node *nodes, size_t n_nodes,
+                        const z2d_fill_opts *opts) {
+    if (!c || !pattern || !opts) return Z2D_ERR_INVALID_ARGUMENT;
+    Z2D_CUDA(cudaSetDevice(c->device));
+    z2d_fill_cmd cmd;
+    cmd.pattern = pattern;
+    cmd.node_offset = 0;
+    cmd.n_nodes = n_nodes;
+    cmd.opts = *opts;
+    return do_fill_batch(*c, surface, nodes, n_nodes, &cmd, 1);
+}
+
+Z2D_API int z2dgpu_fill_batch(z2dgpu_ctx *c, z2d_surface *surface, const z2d_node *nodes, size_t n_nodes,
+                              const z2d_fill_cmd *cmds, size_t n_cmds) {
+    if (!c) return Z2D_ERR_INVALID_ARGUMENT;
+    Z2D_CUDA(cudaSetDevice(c->device));
+    return do_fill_batch(*c, surface, nodes, n_nodes, cmds, n_cmds);
+}
+
+Z2D_API int z2dgpu_composite(z2dgpu_ctx *c, z2d_surface *dst, int32_t dst_x, int32_t dst_y, int32_t n_ops,
+                             const z2d_operation *ops, int32_t precision) {
+    if (!c) return Z2D_ERR_INVALID_ARGUMENT;
+    int rc = check_surface(dst);
+    if (rc) return rc;
+    if (n_ops < 0 || n_ops > 2 || (n_ops > 0 && !ops)) {
+        set_error("composite: 0..2 operations supported");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    if (precision != Z2D_PRECISION_INTEGER && precision != Z2D_PRECISION_FLOAT) return Z2D_ERR_INVALID_ARGUMENT;
+    Z2D_CUDA(cudaSetDevice(c->device));
+    // SurfaceCompositor.run bounds (src/compositor.zig:310-387)
+    if (n_ops == 0) return Z2D_OK;
+    if (dst_x >= dst->width || dst_y >= dst->height) return Z2D_OK;
+    int prec = precision;
+    for (int k = 0; k < n_ops; k++) {
+        if (ops[k].op < 0 || ops[k].op >= Z2D_OP_COUNT) return Z2D_ERR_INVALID_ARGUMENT;
+        if (requires_float(ops[k].op)) prec = Z2D_PRECISION_FLOAT;
+    }
+    int32_t sw, sh;
+    const z2d_param &s0 = ops[0].src;
+    if (s0.kind == Z2D_PARAM_NONE) return Z2D_OK;
+    if (s0.kind == Z2D_PARAM_SURFACE) {
+        rc = check_surface(s0.surface);
+        if (rc) return rc;
+        sw = s0.surface->width;
+        sh = s0.surface->height;
+    } else {
+        if (dst_x != 0 || dst_y != 0) return Z2D_OK;
+        sw = dst->width;
+        sh = dst->height;
+    }
+    const int32_t ssx = dst_x < 0 ? -dst_x : 0, ssy = dst_y < 0 ? -dst_y : 0;
+    const int32_t width = (sw + dst_x > dst->width) ? dst->width - dst_x : sw;
+    const int32_t height = (sh + dst_y > dst->height) ? dst->height - dst_y : sh;
+    if (ssx >= width || ssy >= height) return Z2D_OK;
+    CompJob J;
+    memset(&J, 0, sizeof(J));
+    J.n_ops = n_ops;
+    J.precision = prec;
+    J.dst_x = dst_x;
+    J.dst_y = dst_y;
+    J.dsx = ssx + dst_x;
+    J.y0 = ssy + dst_y;
+    J.y1 = std::max(ssy, height) + dst_y;
+    J.line_w = std::max(0, width - ssx);
+    // stage destination and surface params
+    DevBuf *stage[3] = {&c->surface, &c->surface2, &c->surface3};
+    int used = 0;
+    rc = stage_in(*c, *dst, *stage[used++], J.dst);
+    if (rc) return rc;
+    std::vector<DevGradient> grads;
+    std::vector<DevSrc *> grad_users;
+    for (int k = 0; k < n_ops; k++) {
+        J.ops[k].op = ops[k].op;
+        const z2d_param *prm[2] = {&ops[k].dst, &ops[k].src};
+        DevSrc *outs[2] = {&J.ops[k].dst, &J.ops[k].src};
+        for (int j = 0; j < 2; j++) {
+            const z2d_param &p = *prm[j];
+            DevSrc &o = *outs[j];
+            memset(&o, 0, sizeof(o));
+            if (p.kind == Z2D_PARAM_NONE) {
+                o.kind = SRC_NONE;
+            } else if (p.kind == Z2D_PARAM_SURFACE) {
+                rc = check_surface(p.surface);
+                if (rc) return rc;
+                if (p.surface->location != dst->location) {
+                    set_error("composite: surface params must live where the destination lives");
+                    return Z2D_ERR_INVALID_ARGUMENT;
+                }
+                o.kind = SRC_SURFACE;
+                if (p.surface == dst || p.surface->data == dst->data) {
+                    o.sfc = J.dst;
+                } else {
+                    if (used >= 3) {
+                        set_error("composite: too many host surfaces");
+                        return Z2D_ERR_INVALID_ARGUMENT;
+                    }
+                    rc = stage_in(*c, *p.surface, *stage[used++], o.sfc);
+                    if (rc) return rc;
+                }
+            } else if (p.kind == Z2D_PARAM_PIXEL || p.kind == Z2D_PARAM_GRADIENT || p.kind == Z2D_PARAM_DITHER) {
+                bool needs_grad = false;
+                DevGradient g;
+                rc = make_dev_src_from_pattern(p.kind, p.pattern, o, needs_grad, g);
+                if (rc) return rc;
+                if (needs_grad) {
+                    grads.push_back(g);
+                    grad_users.push_back(&o);
+                }
+            } else {
+                return Z2D_ERR_INVALID_ARGUMENT;
+            }
+        }
+    }
+    if (!grads.empty()) {
+        const size_t bytes = sizeof(DevGradient) * grads.size();
+        if (c->params.ensure(bytes) || c->staging.ensure(bytes)) return Z2D_ERR_OUT_OF_MEMORY;
+        Z2D_CUDA(cudaStreamSynchronize(c->stream));
+        memcpy(c->staging.ptr, grads.data(), bytes);
+        Z2D_CUDA(cudaMemcpyAsync(c->params.ptr, c->staging.ptr, bytes, cudaMemcpyHostToDevice, c->stream));
+        for (size_t i = 0; i < grad_users.size(); i++) grad_users[i]->grad = c->params.as<DevGradient>() + i;
+    }
+    // z2d leaves surface params smaller than the batch region undefined; the
+    // GPU path rejects them instead of reading out of bounds
+    for (int k = 0; k < n_ops; k++) {
+        const DevSrc &ds = J.ops[k].dst, &ss = J.ops[k].src;
+        if (ds.kind == SRC_SURFACE && ((int64_t)ds.sfc.w < (int64_t)J.dsx + J.line_w || ds.sfc.h < J.y1)) {
+            set_error("composite: destination surface param smaller than the region");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+        if (ss.kind == SRC_SURFACE && ((int64_t)ss.sfc.w < (int64_t)(J.dsx - dst_x) + J.line_w || ss.sfc.h < J.y1 - dst_y)) {
+            set_error("composite: source surface param smaller than the region");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+    }
+    rc = launch_composite(*c, J);
+    if (rc) return rc;
+    return stage_out(*c, *dst, J.dst);
+}
+
+}  // extern "C"

@@ -1,0 +1,958 @@
+// fill.cu -- painter.fill on the GPU, for one fill or an ordered batch of
+// fills on one surface.
+//
+// Pipeline (one launch each, all on the context stream):
+//   k_node_count  thread per path node: how many edges each line/curve
+//                 emits (Bezier subdivision of Spline.zig:37-165)
+//   k_fill_scan   thread per fill: the sequential part of fill_plotter.plot
+//                 (fill_plotter.zig:21-97) -- start points, close_path edges,
+//                 per-node edge offsets, open-chain detection
+//   k_node_emit   thread per node: emits Polygon edges (Polygon.zig:61-109)
+//                 and per-fill extents
+//   k_fill_setup  thread per fill: Polygon.inBox and the draw box of
+//                 multisample.run / direct.run
+//   k_bin_count / k_bin_fill   (edge, 4-row band) lists per fill
+//   k_band_lists  CTA per band: the fills touching the band, in call order
+//   k_exact       thread per degenerate fill: literal restatement of the
+//                 sorted-span rasteriser, writing a per-pixel action mask
+//   k_raster      CTA per 4x256 tile: for each fill in order, winding deltas
+//                 per sub-scanline in shared memory, a warp prefix scan per
+//                 sub-scanline, coverage, then z2d's span compositing rules
+//                 (raster/shared.zig) applied to the tile held in registers.
+//
+// Why the winding scan equals z2d's sorted spans: on every sub-scanline
+// z2d sorts the active edges' rounded crossings, keeps the 0<->non-zero
+// transitions (non-zero) or all of them (even-odd) and fills [x_{2k},
+// x_{2k+1}).  A sample column c is then covered exactly when the crossings
+// at x <= c have non-zero (odd) winding, provided the row's crossings are
+// balanced.  Closed subpaths always give balanced rows; fills with an open
+// 2-point subpath are routed to k_exact.
+#include <cub/cub.cuh>
+#include <cuda_runtime.h>
+
+#include "fill.cuh"
+
+namespace z2dg {
+
+// ------------------------------------------------------------ helpers
+__device__ __forceinline__ bool pt_eq(double ax, double ay, double bx, double by) { return ax == bx && ay == by; }
+
+// Order-preserving map of finite doubles to u64 (for atomic min/max).
+__device__ __forceinline__ unsigned long long dkey(double v) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__host__ __device__ __forceinline__ double dkey_inv(unsigned long long k) {
+    unsigned long long b = (k & 0x8000000000000000ull) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)b);
+#else
+    double d;
+    memcpy(&d, &b, 8);
+    return d;
+#endif
+}
+
+struct Knots {
+    double ax, ay, bx, by, cx, cy, dx, dy;
+};
+
+// Spline.Knots.errorSq (Spline.zig:83-123)
+__device__ __forceinline__ double error_sq(const Knots &k) {
+    double bx = k.bx - k.ax, by = k.by - k.ay, cx = k.cx - k.ax, cy = k.cy - k.ay;
+    if (k.ax != k.dx || k.ay != k.dy) {
+        const double dx = k.dx - k.ax, dy = k.dy - k.ay;
+        const double dd = dx * dx + dy * dy;
+        const double bd = bx * dx + by * dy;
+        if (bd >= dd) {
+            bx -= dx;
+            by -= dy;
+        } else {
+            bx -= bd / dd * dx;
+            by -= bd / dd * dy;
+        }
+        const double cd = cx * dx + cy * dy;
+        if (cd >= dd) {
+            cx -= dx;
+            cy -= dy;
+        } else {
+            cx -= cd / dd * dx;
+            cy -= cd / dd * dy;
+        }
+    }
+    const double be = bx * bx + by * by, ce = cx * cx + cy * cy;
+    return be > ce ? be : ce;
+}
+__device__ __forceinline__ double lerp_half(double a, double b) { return a + ((b - a) / 2); }
+
+// Knots.deCasteljau (Spline.zig:128-152): k becomes the first half, the
+// second half is returned.
+__device__ __forceinline__ Knots de_casteljau(Knots &k) {
+    const double abx = lerp_half(k.ax, k.bx), aby = lerp_half(k.ay, k.by);
+    const double bcx = lerp_half(k.bx, k.cx), bcy = lerp_half(k.by, k.cy);
+    const double cdx = lerp_half(k.cx, k.dx), cdy = lerp_half(k.cy, k.dy);
+    const double abbcx = lerp_half(abx, bcx), abbcy = lerp_half(aby, bcy);
+    const double bccdx = lerp_half(bcx, cdx), bccdy = lerp_half(bcy, cdy);
+    const double fx = lerp_half(abbcx, bccdx), fy = lerp_half(abbcy, bccdy);
+    const Knots r{fx, fy, bccdx, bccdy, cdx, cdy, k.dx, k.dy};
+    k.bx = abx; k.by = aby;
+    k.cx = abbcx; k.cy = abbcy;
+    k.dx = fx; k.dy = fy;
+    return r;
+}
+
+// Depth-first subdivision (Spline.decomposeInto, Spline.zig:56-71) with an
+// explicit stack.  Calls emit(x, y) for every lineTo the reference issues,
+// including the final lineTo(d).  Returns false if the stack would overflow
+// (coordinates are bounded, so this does not happen for valid input).
+template <class F>
+__device__ __forceinline__ bool spline_walk(double ax, double ay, const double *p, double tol, F &&emit) {
+    const double bx = p[0], by = p[1], cx = p[2], cy = p[3], dx = p[4], dy = p[5];
+    if (pt_eq(ax, ay, bx, by) && pt_eq(cx, cy, dx, dy)) {  // Spline.zig:39-42
+        emit(dx, dy);
+        return true;
+    }
+    const double tol2 = tol * tol;
+    Knots stack[kSplineStack];
+    int sp = 0;
+    stack[sp++] = Knots{ax, ay, bx, by, cx, cy, dx, dy};
+    bool ok = true;
+    int32_t budget = kSplineMaxSplits;  // bounds the walk even for pathological input
+    while (sp > 0 && ok) {
+        Knots k = stack[--sp];
+        while (true) {
+            if (--budget < 0) {
+                ok = false;
+                break;
+            }
+            if (error_sq(k) < tol2) {
+                if (!pt_eq(k.ax, k.ay, ax, ay)) emit(k.ax, k.ay);
+                break;
+            }
+            const Knots second = de_casteljau(k);
+            if (sp >= kSplineStack) {  // cannot recurse deeper: give up on this branch
+                ok = false;
+                break;
+            }
+            stack[sp++] = second;  // processed after the first half
+        }
+    }
+    emit(dx, dy);
+    return ok;
+}
+
+// ------------------------------------------------------------ kernels
+__global__ void k_node_count(const z2d_node *__restrict__ nodes, const int32_t *__restrict__ node_fill,
+                             const FillCmd *__restrict__ fills, NodeInfo *__restrict__ info, int32_t n_nodes,
+                             int32_t *__restrict__ status) {
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_nodes) return;
+    const z2d_node nd = nodes[i];
+    NodeInfo inf{};
+    inf.n_emit = 0;
+    inf.n_added = 0;
+    const int32_t f = node_fill[i];
+    const FillCmd &F = fills[f];
+    const bool first_of_fill = (i == F.node_off);
+    if (nd.tag == Z2D_LINE_TO || nd.tag == Z2D_CURVE_TO) {
+        const z2d_node pv = first_of_fill ? nd : nodes[i - 1];
+        const bool static_start = !first_of_fill && (pv.tag == Z2D_MOVE_TO || pv.tag == Z2D_LINE_TO || pv.tag == Z2D_CURVE_TO);
+        if (!static_start) {
+            inf.n_emit = -1;  // resolved by k_fill_scan
+        } else {
+            const double sx = pv.tag == Z2D_CURVE_TO ? pv.p[4] : pv.p[0];
+            const double sy = pv.tag == Z2D_CURVE_TO ? pv.p[5] : pv.p[1];
+            if (nd.tag == Z2D_LINE_TO) {
+                inf.n_emit = 1;
+                inf.n_added = pt_eq(sx, sy, nd.p[0], nd.p[1]) ? 0 : 1;
+            } else {
+                int32_t ne = 0, na = 0;
+                double lx = sx, ly = sy;
+                auto cnt = [&](double x, double y) {
+                    ne++;
+                    if (!pt_eq(x, y, lx, ly)) na++;
+                    lx = x;
+                    ly = y;
+                };
+                if (!spline_walk(sx, sy, nd.p, F.tol, cnt)) atomicExch(status, Z2D_ERR_INVALID_STATE);
+                inf.n_emit = ne;
+                inf.n_added = na;
+            }
+        }
+    }
+    info[i] = inf;
+}
+
+// The sequential walk of fill_plotter.plot over one fill's nodes.
+__global__ void k_fill_scan(const z2d_node *__restrict__ nodes, const FillCmd *__restrict__ fills,
+                            NodeInfo *__restrict__ info, FillState *__restrict__ st, int32_t n_fills,
+                            int32_t *__restrict__ counters, int32_t *__restrict__ status) {
+    const int32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_fills) return;
+    const FillCmd F = fills[f];
+    double fx = 0, fy = 0, lx = 0, ly = 0;
+    int32_t count = 0;  // PointBuffer.len, saturating at 3
+    int32_t off = 0;
+    int32_t flags = 0;
+    for (int32_t j = 0; j < F.n_nodes; j++) {
+        const int32_t i = F.node_off + j;
+        const z2d_node nd = nodes[i];
+        NodeInfo inf = info[i];
+        inf.edge_off = off;
+        switch (nd.tag) {
+            case Z2D_MOVE_TO:
+                inf.n_emit = 0;
+                if (j == F.n_nodes - 1) break;  // trailing move_to (fill_plotter.zig:38-40)
+                fx = lx = nd.p[0];
+                fy = ly = nd.p[1];
+                count = 1;
+                break;
+            case Z2D_LINE_TO:
+                inf.sx = lx;
+                inf.sy = ly;
+                inf.n_emit = 1;
+                if (!pt_eq(lx, ly, nd.p[0], nd.p[1])) count = min(count + 1, 3);
+                lx = nd.p[0];
+                ly = nd.p[1];
+                break;
+            case Z2D_CURVE_TO: {
+                inf.sx = lx;
+                inf.sy = ly;
+                if (inf.n_emit < 0) {  // start depends on a preceding close_path
+                    int32_t ne = 0, na = 0;
+                    double px = lx, py = ly;
+                    auto cnt = [&](double x, double y) {
+                        ne++;
+                        if (!pt_eq(x, y, px, py)) na++;
+                        px = x;
+                        py = y;
+                    };
+                    if (!spline_walk(lx, ly, nd.p, F.tol, cnt)) atomicExch(status, Z2D_ERR_INVALID_STATE);
+                    inf.n_emit = ne;
+                    inf.n_added = na;
+                }
+                count = min(count + inf.n_added, 3);
+                lx = nd.p[4];
+                ly = nd.p[5];
+                break;
+            }
+            default:  // close_path (fill_plotter.zig:72-92)
+                inf.n_emit = 0;
+                inf.sx = lx;
+                inf.sy = ly;
+                inf.ex = fx;
+                inf.ey = fy;
+                if (count >= 3) {
+                    if (!pt_eq(lx, ly, fx, fy)) {
+                        inf.n_emit = 1;
+                        lx = fx;
+                        ly = fy;
+                    }
+                } else if (!pt_eq(lx, ly, fx, fy)) {
+                    flags |= FILL_OPEN_CHAIN;  // a lone edge stays unmatched
+                }
+                break;
+        }
+        off += inf.n_emit;
+        info[i] = inf;
+    }
+    st[f].n_edges = off;
+    st[f].edge_base = atomicAdd(&counters[CNT_EDGES], off);
+    st[f].flags = flags;
+    st[f].ext[0] = ~0ull;  // min slots start at the largest key
+    st[f].ext[1] = 0ull;
+    st[f].ext[2] = ~0ull;
+    st[f].ext[3] = 0ull;
+}
+
+__device__ __forceinline__ void add_edge(const FillCmd &F, DEdge *out, double x0, double y0, double x1, double y1,
+                                         double &et, double &eb, double &el, double &er, bool &any) {
+    // Polygon.addEdge (Polygon.zig:61-109)
+    const double ax = x0 * F.scale, ay = y0 * F.scale, bx = x1 * F.scale, by = y1 * F.scale;
+    DEdge e;
+    if (ay < by) {
+        e.top = ay;
+        e.x_start = ax;
+        e.x_inc = (bx - ax) / (by - ay);
+        e.dir = -1;
+        e.rb = (int32_t)round(by);
+    } else if (ay > by) {
+        e.top = by;
+        e.x_start = bx;
+        e.x_inc = (ax - bx) / (ay - by);
+        e.dir = 1;
+        e.rb = (int32_t)round(ay);
+    } else {
+        e.top = 0;
+        e.x_start = 0;
+        e.x_inc = 0;
+        e.dir = 0;
+        e.rt = 1;
+        e.rb = 0;  // horizontal: never active
+        *out = e;
+        return;
+    }
+    e.rt = (int32_t)round(e.top);
+    const double bot = ay < by ? by : ay;
+    const double l = ax < bx ? ax : bx, r = ax < bx ? bx : ax;
+    if (!any) {
+        et = e.top; eb = bot; el = l; er = r;
+        any = true;
+    } else {
+        if (e.top < et) et = e.top;
+        if (bot > eb) eb = bot;
+        if (l < el) el = l;
+        if (r > er) er = r;
+    }
+    *out = e;
+}
+
+__global__ void k_node_emit(const z2d_node *__restrict__ nodes, const int32_t *__restrict__ node_fill,
+                            const FillCmd *__restrict__ fills, const NodeInfo *__restrict__ info,
+                            FillState *__restrict__ st, DEdge *__restrict__ edges, int32_t n_nodes) {
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_nodes) return;
+    const NodeInfo inf = info[i];
+    if (inf.n_emit <= 0) return;
+    const z2d_node nd = nodes[i];
+    const int32_t f = node_fill[i];
+    const FillCmd F = fills[f];
+    DEdge *out = edges + st[f].edge_base + inf.edge_off;
+    double et = 0, eb = 0, el = 0, er = 0;
+    bool any = false;
+    if (nd.tag == Z2D_LINE_TO) {
+        add_edge(F, out, inf.sx, inf.sy, nd.p[0], nd.p[1], et, eb, el, er, any);
+    } else if (nd.tag == Z2D_CLOSE_PATH) {
+        add_edge(F, out, inf.sx, inf.sy, inf.ex, inf.ey, et, eb, el, er, any);
+    } else {
+        double px = inf.sx, py = inf.sy;
+        int32_t k = 0;
+        auto em = [&](double x, double y) {
+            if (k < inf.n_emit) add_edge(F, out + k, px, py, x, y, et, eb, el, er, any);
+            k++;
+            px = x;
+            py = y;
+        };
+        spline_walk(inf.sx, inf.sy, nd.p, F.tol, em);
+    }
+    if (any) {
+        FillState &S = st[f];
+        atomicMin(&S.ext[0], dkey(et));
+        atomicMax(&S.ext[1], dkey(eb));
+        atomicMin(&S.ext[2], dkey(el));
+        atomicMax(&S.ext[3], dkey(er));
+        atomicOr(&S.has_edges, 1);
+    }
+}
+
+__device__ __forceinline__ int32_t clampi(int32_t v, int32_t lo, int32_t hi) { return max(lo, min(v, hi)); }
+
+__global__ void k_fill_setup(const FillCmd *__restrict__ fills, FillState *__restrict__ st, int32_t n_fills,
+                             int32_t sw, int32_t sh, int32_t *__restrict__ counters) {
+    const int32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_fills) return;
+    const FillCmd F = fills[f];
+    FillState S = st[f];
+    S.active = 0;
+    if (!S.has_edges) {  // inBox of the empty polygon is false
+        st[f] = S;
+        return;
+    }
+    const double et = dkey_inv(S.ext[0]), eb = dkey_inv(S.ext[1]), el = dkey_inv(S.ext[2]), er = dkey_inv(S.ext[3]);
+    const double sc = F.scale;
+    // Polygon.inBox (Polygon.zig:142-201)
+    if (er < 0.0 || eb < 0.0) {
+        st[f] = S;
+        return;
+    }
+    const int32_t psx = (int32_t)floor(el / sc), psy = (int32_t)floor(et / sc);
+    const int32_t pex = (int32_t)ceil(er / sc), pey = (int32_t)ceil(eb / sc);
+    const int32_t pw = pex - psx, ph = pey - psy;
+    if (pw == 0 || ph == 0 || psx + pw < 0 || psy + ph < 0 || psx >= sw || psy >= sh) {
+        st[f] = S;
+        return;
+    }
+    S.active = 1;
+    const bool bounded = is_bounded(F.op);
+    if (F.aa == Z2D_AA_NONE) {  // direct.run (direct.zig:36-49)
+        const int32_t y0 = bounded ? (int32_t)floor(et) : 0;
+        const int32_t y1 = bounded ? (int32_t)ceil(eb) : sh - 1;
+        S.start_y = clampi(y0, 0, sh - 1);
+        S.end_y = clampi(y1, S.start_y, sh - 1);
+        // spans are clamped to the surface, not to the extents; crossings
+        // lie within one pixel of the x extents
+        S.start_x = clampi((int32_t)floor(el) - 1, 0, sw);
+        S.end_x = clampi((int32_t)ceil(er) + 2, S.start_x, sw);
+        if (!bounded) S.flags |= FILL_EXACT;
+    } else {  // multisample.run (multisample.zig:46-78)
+        S.start_y = clampi((int32_t)floor(et / 4.0), 0, sh - 1);
+        S.end_y = clampi((int32_t)ceil(eb / 4.0), S.start_y, sh - 1);
+        S.start_x = clampi((int32_t)floor(el / 4.0), 0, sw - 1);
+        S.end_x = clampi((int32_t)ceil(er / 4.0), S.start_x, sw);
+    }
+    if (S.flags & FILL_OPEN_CHAIN) S.flags |= FILL_EXACT;
+    // rows the fill touches: the draw rows, or every row for unbounded
+    // operators (their clears reach outside the draw box)
+    const int32_t ty0 = bounded ? S.start_y : 0;
+    const int32_t ty1 = bounded ? S.end_y : sh - 1;
+    S.band0 = ty0 / kTileRows;
+    S.band1 = ty1 / kTileRows;
+    S.fb_base = atomicAdd(&counters[CNT_FILL_BANDS], S.band1 - S.band0 + 1);
+    if (S.flags & FILL_EXACT) {
+        // action mask over the rows the exact rasteriser visits
+        S.mask_w = (F.aa == Z2D_AA_NONE) ? sw : (S.end_x - S.start_x);
+        S.mask_x0 = (F.aa == Z2D_AA_NONE) ? 0 : S.start_x;
+        // mask, then 8-byte aligned work arrays of 4 ints per edge
+        // (permutation, crossings, and 2 breakpoints)
+        const long long bytes = ((((long long)S.mask_w * (S.end_y - S.start_y + 1) + 7) & ~7ll) + 16ll * S.n_edges + 15) & ~7ll;
+        S.mask_base = atomicAdd(reinterpret_cast<unsigned long long *>(&counters[CNT_MASK_LO]), (unsigned long long)bytes);
+        atomicAdd(&counters[CNT_EXACT], 1);
+    }
+    atomicMin(&counters[CNT_BAND_MIN], S.band0);
+    atomicMax(&counters[CNT_BAND_MAX], S.band1);
+    const int32_t cx0 = bounded ? S.start_x : 0, cx1 = bounded ? S.end_x : sw;
+    atomicMin(&counters[CNT_TCOL_MIN], cx0 / kTileCols);
+    atomicMax(&counters[CNT_TCOL_MAX], (max(cx1, cx0 + 1) - 1) / kTileCols);
+    st[f] = S;
+}
+
+// Band range of an edge's active sample rows within the fill's draw rows.
+__device__ __forceinline__ bool edge_bands(const DEdge &e, const FillCmd &F, const FillState &S, int32_t &b0,
+                                           int32_t &b1) {
+    if (e.dir == 0) return false;
+    const int32_t S_ = (int32_t)F.scale;
+    const int32_t lo = max(e.rt, S.start_y * S_), hi = min(e.rb, (S.end_y + 1) * S_);
+    if (lo >= hi) return false;
+    b0 = lo / (kTileRows * S_);
+    b1 = (hi - 1) / (kTileRows * S_);
+    return true;
+}
+
+__global__ void k_bin_count(const FillCmd *__restrict__ fills, const FillState *__restrict__ st,
+                            const DEdge *__restrict__ edges, const int32_t *__restrict__ edge_fill, int32_t n_edges,
+                            int32_t *__restrict__ fb_count) {
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_edges) return;
+    const int32_t f = edge_fill[i];
+    if (f < 0) return;
+    const FillState &S = st[f];
+    if (!S.active || (S.flags & FILL_EXACT)) return;
+    int32_t b0, b1;
+    if (!edge_bands(edges[i], fills[f], S, b0, b1)) return;
+    for (int32_t b = b0; b <= b1; b++) atomicAdd(&fb_count[S.fb_base + (b - S.band0)], 1);
+}
+
+__global__ void k_bin_fill(const FillCmd *__restrict__ fills, const FillState *__restrict__ st,
+                           const DEdge *__restrict__ edges, const int32_t *__restrict__ edge_fill, int32_t n_edges,
+                           int32_t *__restrict__ fb_cursor, int32_t *__restrict__ bins) {
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_edges) return;
+    const int32_t f = edge_fill[i];
+    if (f < 0) return;
+    const FillState &S = st[f];
+    if (!S.active || (S.flags & FILL_EXACT)) return;
+    int32_t b0, b1;
+    if (!edge_bands(edges[i], fills[f], S, b0, b1)) return;
+    for (int32_t b = b0; b <= b1; b++) bins[atomicAdd(&fb_cursor[S.fb_base + (b - S.band0)], 1)] = i;
+}
+
+// Edge -> fill map (edges of one fill are contiguous).
+__global__ void k_edge_fill(const FillState *__restrict__ st, int32_t n_fills, int32_t *__restrict__ edge_fill) {
+    const int32_t f = blockIdx.x;
+    const FillState S = st[f];
+    for (int32_t k = threadIdx.x; k < S.n_edges; k += blockDim.x) edge_fill[S.edge_base + k] = f;
+}
+
+// Ordered list of the fills touching each band (call order preserved by a
+// block-wide stream compaction).
+__global__ void __launch_bounds__(256) k_band_lists(const FillState *__restrict__ st, int32_t n_fills, int32_t band_lo,
+                                                    int32_t *__restrict__ band_count, int32_t *__restrict__ band_fills) {
+    const int32_t b = band_lo + blockIdx.x;
+    __shared__ int32_t warp_tot[8];
+    __shared__ int32_t base;
+    if (threadIdx.x == 0) base = 0;
+    __syncthreads();
+    const int32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int32_t *out = band_fills + (size_t)blockIdx.x * n_fills;
+    for (int32_t f0 = 0; f0 < n_fills; f0 += blockDim.x) {
+        const int32_t f = f0 + threadIdx.x;
+        bool hit = false;
+        if (f < n_fills) {
+            const FillState &S = st[f];
+            hit = S.active && b >= S.band0 && b <= S.band1;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (lane == 0) warp_tot[wid] = __popc(m);
+        __syncthreads();
+        int32_t before = 0, total = 0;
+        for (int w = 0; w < 8; w++) {
+            if (w < wid) before += warp_tot[w];
+            total += warp_tot[w];
+        }
+        if (hit) out[base + before + __popc(m & ((1u << lane) - 1u))] = f;
+        __syncthreads();
+        if (threadIdx.x == 0) base += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) band_count[blockIdx.x] = base;
+}
+
+}  // namespace z2dg
+
+namespace z2dg {
+
+// ----------------------------------------------------------- exact path
+// Literal restatement of multisample.run / direct.run's sorted-span loop
+// (multisample.zig:115-188, direct.zig:51-126, Polygon.zig:232-353) for one
+// fill, one thread, writing a per-pixel action mask.  Used for fills whose
+// rows may be unbalanced (open 2-point subpaths) and for unbounded operators
+// without anti-aliasing, where z2d's per-span clears depend on span order.
+__device__ void sort_insertion(int32_t *perm, int32_t *xv, int32_t n) {
+    // std.sort.insertionContext; stable, so it orders ties like the stable
+    // sort the CPU oracle uses beyond 24 active edges
+    for (int32_t i = 1; i < n; i++)
+        for (int32_t j = i; j > 0 && xv[j] < xv[j - 1]; j--) {
+            const int32_t te = perm[j]; perm[j] = perm[j - 1]; perm[j - 1] = te;
+            const int32_t tx = xv[j]; xv[j] = xv[j - 1]; xv[j - 1] = tx;
+        }
+}
+
+__device__ void shell_sort_unique(int32_t *a, int32_t &n) {
+    for (int32_t gap = n / 2; gap > 0; gap /= 2)
+        for (int32_t i = gap; i < n; i++) {
+            const int32_t t = a[i];
+            int32_t j = i;
+            for (; j >= gap && a[j - gap] > t; j -= gap) a[j] = a[j - gap];
+            a[j] = t;
+        }
+    int32_t m = 0;
+    for (int32_t i = 0; i < n; i++)
+        if (m == 0 || a[i] != a[m - 1]) a[m++] = a[i];
+    n = m;
+}
+
+__global__ void k_exact(const FillCmd *__restrict__ fills, const FillState *__restrict__ st, const DEdge *__restrict__ edges,
+                        int32_t n_fills, int32_t sw, uint8_t *__restrict__ masks) {
+    const int32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_fills) return;
+    const FillState S = st[f];
+    if (!S.active || !(S.flags & FILL_EXACT)) return;
+    const FillCmd F = fills[f];
+    const DEdge *E = edges + S.edge_base;
+    uint8_t *mask = masks + S.mask_base;  // zeroed by the host
+    const int32_t mh = S.end_y - S.start_y + 1;
+    // work arrays live after the mask, 8-byte aligned
+    int32_t *perm = reinterpret_cast<int32_t *>(masks + S.mask_base + (((long long)S.mask_w * mh + 7) & ~7ll));
+    int32_t *xv = perm + S.n_edges;
+    int32_t *bp = xv + S.n_edges;
+    int32_t n = 0;
+    for (int32_t i = 0; i < S.n_edges; i++)
+        if (E[i].dir != 0) perm[n++] = i;
+    int32_t nbp = 0;
+    for (int32_t i = 0; i < n; i++) {
+        bp[nbp++] = E[perm[i]].rt;
+        bp[nbp++] = E[perm[i]].rb;
+    }
+    shell_sort_unique(bp, nbp);
+    int32_t bpi = -1;
+    for (int32_t i = 0; i < nbp; i++)
+        if (bp[i] >= S.start_y) {
+            bpi = i == 0 ? 0 : i - 1;
+            break;
+        }
+    if (bpi < 0) return;
+    const bool direct = F.aa == Z2D_AA_NONE;
+    const bool bounded = is_bounded(F.op);
+    const int32_t sc = direct ? 1 : 4;
+    int32_t n_active = 0;
+    const int32_t sxs = S.start_x * 4, dws = (S.end_x - S.start_x) * 4;
+    for (int32_t y = S.start_y; y <= S.end_y; y++) {
+        uint8_t *mrow = mask + (long long)(y - S.start_y) * S.mask_w;
+        for (int32_t off = 0; off < sc; off++) {
+            const int32_t ys = y * sc + off;
+            if (ys >= bp[bpi]) {  // WorkingEdgeSet.rescan (Polygon.zig:275-300)
+                int32_t to = 0;
+                for (int32_t from = 0; from < n; from++) {
+                    const DEdge &e = E[perm[from]];
+                    if (e.rt <= ys && ys < e.rb) {
+                        if (from != to) {
+                            const int32_t t = perm[to]; perm[to] = perm[from]; perm[from] = t;
+                        }
+                        to++;
+                    }
+                }
+                n_active = to;
+                if (bpi < nbp - 1) bpi++;
+            }
+            const double ym = (double)ys + 0.5;
+            for (int32_t k = 0; k < n_active; k++) {
+                const DEdge &e = E[perm[k]];
+                xv[k] = (int32_t)round(e.x_start + (e.x_inc * (ym - e.top)));
+            }
+            sort_insertion(perm, xv, n_active);
+            int32_t fl = n_active;
+            if (F.rule == Z2D_FILL_NON_ZERO) {  // WorkingEdgeSet.filter
+                int32_t wn = 0, to = 0;
+                for (int32_t from = 0; from < n_active; from++) {
+                    xv[to] = xv[from];
+                    if (wn == 0) {
+                        wn += E[perm[from]].dir;
+                        to++;
+                    } else {
+                        wn += E[perm[from]].dir;
+                        if (wn == 0) to++;
+                    }
+                }
+                fl = to;
+            }
+            if (direct) {
+                if (!bounded && fl == 0) {
+                    for (int32_t x = 0; x < sw; x++) mrow[x] = kMaskClear;
+                    continue;
+                }
+                for (int32_t p = 0; p < fl / 2; p++) {
+                    const int32_t sx = max(0, xv[2 * p]);
+                    if (sx >= sw) break;
+                    const int32_t ex = clampi(xv[2 * p + 1], sx, sw);
+                    if (!bounded)
+                        for (int32_t x = 0; x < sx; x++) mrow[x] = kMaskClear;
+                    for (int32_t x = sx; x < ex; x++) mrow[x] = (uint8_t)((mrow[x] & kMaskClear) | 1);
+                    if (!bounded)
+                        for (int32_t x = ex; x < sw; x++) mrow[x] = kMaskClear;
+                }
+            } else {
+                int32_t x_min = 0;
+                for (int32_t p = 0; p < fl / 2; p++) {
+                    const int32_t sx = max(x_min, xv[2 * p] - sxs);
+                    if (sx >= dws) break;
+                    const int32_t ex = clampi(xv[2 * p + 1] - sxs, sx, dws);
+                    for (int32_t c = sx; c < ex; c++) mrow[c >> 2] = (uint8_t)(mrow[c >> 2] + 1);
+                    x_min = ex;
+                }
+            }
+        }
+    }
+}
+
+// --------------------------------------------------------- compositing
+__device__ __forceinline__ I16 normalize(I16 v, int fmt) { return to_i16(from_i16(v, fmt)); }
+
+// One pixel of a fill with coverage `cov` (1..full) on destination lanes d,
+// following compositeOpaque / compositeOpacity (raster/shared.zig:9-104),
+// Surface.paintStride and Surface.compositeStride (surface.zig:537-581).
+__device__ __forceinline__ I16 apply_fill(const FillCmd &F, int fmt, int32_t x, int32_t y, int cov, int full, I16 d) {
+    if (F.op == Z2D_OP_CLEAR) return normalize(I16{0, 0, 0, 0}, fmt);
+    if (cov >= full) {
+        if (F.reduces) return to_i16(F.px_paint);
+        if (F.precision == Z2D_PRECISION_INTEGER) return normalize(int_op_any(F.op, d, src_i16_fast(F.src, x, y, 0)), fmt);
+        return normalize(encode_raw(float_op_any(F.op, decode_raw(d), src_f4_fast(F.src, x, y, 0))), fmt);
+    }
+    const uint32_t opacity = (uint32_t)min(max(cov * 16 - 1, 0), 255);
+    if (F.reduces) {
+        I16 s = F.px_rgba;
+        if (opacity < 255) s = normalize(int_op(Z2D_OP_DST_IN, s, I16{0, 0, 0, opacity}), Z2D_FORMAT_RGBA);
+        return normalize(int_op_any(F.op, d, s), fmt);
+    }
+    if (F.precision == Z2D_PRECISION_INTEGER) {
+        const I16 r = int_op(Z2D_OP_DST_IN, src_i16_fast(F.src, x, y, 0), I16{0, 0, 0, opacity});
+        return normalize(int_op_any(F.op, d, r), fmt);
+    }
+    const F4 r = float_op(Z2D_OP_DST_IN, src_f4_fast(F.src, x, y, 0), F4{0.f, 0.f, 0.f, (float)opacity / 255.0f});
+    return normalize(encode_raw(float_op_any(F.op, decode_raw(d), r)), fmt);
+}
+
+// multisample.run's clears for unbounded operators (multisample.zig:96-110),
+// including its quirks: the rows below the draw box are cleared up to the
+// surface WIDTH, and the right-hand clear starts at x = 0.
+__device__ __forceinline__ bool msaa_unbounded_clear(const FillState &S, int32_t x, int32_t y, int32_t sw) {
+    if (y < S.start_y) return true;
+    if (y > S.end_y) return y < sw;
+    return (S.start_x > 0 && x < S.start_x) || (S.end_x < sw && x < sw - S.end_x);
+}
+
+struct RasterArgs {
+    DevSurface dst;
+    const FillCmd *fills;
+    const FillState *st;
+    const DEdge *edges;
+    const int32_t *bins;
+    const int32_t *bin_off;
+    const int32_t *band_count;
+    const int32_t *band_fills;
+    const uint8_t *masks;
+    int32_t n_fills, band_lo, tcol_lo;
+};
+
+// Sample column c of a sub-scanline belongs to lane c / per (per = sample
+// columns per lane: 32 with 4x sampling, 8 without); it is stored at
+// (c % per) * 32 + lane so that a warp reading one k for all lanes hits 32
+// consecutive words.
+__device__ __forceinline__ int delta_index(int c, int per) { return ((c % per) << 5) | (c / per); }
+
+__global__ void __launch_bounds__(kRasterThreads) k_raster(const RasterArgs A) {
+    extern __shared__ int32_t smem[];
+    int32_t *delta = smem;                      // [16 sample rows][1024 sample columns]
+    int32_t *cov = smem + 16 * kTileCols * 4;   // [4 rows][256 px]
+    const int32_t b = A.band_lo + blockIdx.y;
+    const int32_t x0 = (A.tcol_lo + blockIdx.x) * kTileCols, y0 = b * kTileRows;
+    const int32_t cnt = A.band_count[blockIdx.y];
+    if (cnt == 0) return;
+    const int32_t *list = A.band_fills + (size_t)blockIdx.y * A.n_fills;
+    const int32_t W = A.dst.w, H = A.dst.h, fmt = A.dst.fmt;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    I16 d[2];
+    bool touched[2] = {false, false};
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+        const int p = tid + kRasterThreads * j;
+        const int32_t x = x0 + (p & (kTileCols - 1)), y = y0 + (p >> 8);
+        d[j] = (x < W && y < H) ? load_px(A.dst, (size_t)W * y + x) : I16{0, 0, 0, 0};
+    }
+    for (int i = tid; i < 16 * kTileCols * 4 + kTileRows * kTileCols; i += kRasterThreads) smem[i] = 0;
+    __syncthreads();
+
+    for (int32_t k = 0; k < cnt; k++) {
+        const int32_t f = list[k];
+        const FillState &S = A.st[f];
+        const FillCmd &F = A.fills[f];
+        const bool bounded = is_bounded(F.op);
+        const bool direct = F.aa == Z2D_AA_NONE;
+        const bool exact = (S.flags & FILL_EXACT) != 0;
+        if (bounded && (S.end_x <= x0 || S.start_x >= x0 + kTileCols)) continue;
+        const int32_t sc = direct ? 1 : 4;
+        const bool rows_here = !(S.end_y < y0 || S.start_y >= y0 + kTileRows);
+        if (!exact && rows_here) {
+            const int32_t sub0 = y0 * sc, sub1 = (y0 + kTileRows) * sc, col0 = x0 * sc, ncol = kTileCols * sc;
+            const int32_t fb = S.fb_base + (b - S.band0);
+            const int32_t e0 = A.bin_off[fb], e1 = A.bin_off[fb + 1];
+            for (int32_t ei = e0 + tid; ei < e1; ei += kRasterThreads) {
+                const DEdge e = A.edges[A.bins[ei]];
+                const int32_t lo = max(e.rt, sub0), hi = min(e.rb, sub1);
+                for (int32_t sr = lo; sr < hi; sr++) {
+                    const int32_t X = (int32_t)round(e.x_start + (e.x_inc * (((double)sr + 0.5) - e.top)));
+                    int32_t c = X - col0;
+                    if (c < 0) c = 0;
+                    if (c < ncol) atomicAdd(&delta[(sr - sub0) * 1024 + delta_index(c, 8 * sc)], e.dir);
+                }
+            }
+            __syncthreads();
+            if (warp < kTileRows * sc) {
+                const int per = 8 * sc;  // sample columns per lane
+                int32_t *row = delta + warp * 1024;
+                int32_t tot = 0;
+                for (int kk = 0; kk < per; kk++) tot += row[(kk << 5) | lane];
+                int32_t incl = tot;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += v;
+                }
+                int32_t wnd = incl - tot;
+                uint32_t bits = 0;
+                for (int kk = 0; kk < per; kk++) {
+                    const int32_t idx = (kk << 5) | lane;
+                    wnd += row[idx];
+                    row[idx] = 0;
+                    const bool in = (F.rule == Z2D_FILL_EVEN_ODD) ? ((wnd & 1) != 0) : (wnd != 0);
+                    bits |= (uint32_t)in << kk;
+                }
+                if (direct) {
+                    for (int q = 0; q < 8; q++) cov[warp * kTileCols + lane * 8 + q] = (bits >> q) & 1u;
+                } else {
+                    for (int q = 0; q < 8; q++) atomicAdd(&cov[(warp >> 2) * kTileCols + lane * 8 + q], __popc((bits >> (4 * q)) & 0xFu));
+                }
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            const int p = tid + kRasterThreads * j;
+            const int32_t col = p & (kTileCols - 1), r = p >> 8;
+            const int32_t x = x0 + col, y = y0 + r;
+            int c = 0;
+            if (!exact && rows_here) {
+                c = cov[r * kTileCols + col];
+                cov[r * kTileCols + col] = 0;
+            }
+            if (x >= W || y >= H) continue;
+            bool clear = false;
+            const bool in_rows = y >= S.start_y && y <= S.end_y;
+            if (exact && in_rows && x >= S.mask_x0 && x < S.mask_x0 + S.mask_w) {
+                const uint8_t m = A.masks[S.mask_base + (long long)(y - S.start_y) * S.mask_w + (x - S.mask_x0)];
+                c = m & 0x1F;
+                if (direct) clear = (m & kMaskClear) != 0;
+            }
+            if (!direct && !bounded) clear = msaa_unbounded_clear(S, x, y, W);
+            const bool in_box = in_rows && (direct ? true : (x >= S.start_x && x < S.end_x));
+            if (clear) {
+                d[j] = normalize(I16{0, 0, 0, 0}, fmt);
+                touched[j] = true;
+            }
+            if (in_box && c > 0) {
+                d[j] = apply_fill(F, fmt, x, y, c, direct ? 1 : 16, d[j]);
+                touched[j] = true;
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+        const int p = tid + kRasterThreads * j;
+        const int32_t x = x0 + (p & (kTileCols - 1)), y = y0 + (p >> 8);
+        if (touched[j] && x < W && y < H) store_px(A.dst, (size_t)W * y + x, d[j]);
+    }
+}
+
+// ----------------------------------------------------------- host side
+static inline unsigned grid_for(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+int run_fills(Ctx &c, const DevSurface &sfc, const z2d_node *nodes, int32_t n_nodes, std::vector<FillCmd> &fills,
+              const std::vector<int32_t> &node_fill, const std::vector<DevGradient> &grads,
+              const std::vector<int32_t> &grad_of_fill) {
+    const int32_t n_fills = (int32_t)fills.size();
+    if (n_fills == 0 || n_nodes == 0) return Z2D_OK;
+    // ---- upload: nodes | node_fill | gradients | fills | counters
+    auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    const size_t o_nodes = 0;
+    const size_t o_nfill = al(o_nodes + sizeof(z2d_node) * (size_t)n_nodes);
+    const size_t o_grads = al(o_nfill + sizeof(int32_t) * (size_t)n_nodes);
+    const size_t o_fills = al(o_grads + sizeof(DevGradient) * grads.size());
+    const size_t o_cnt = al(o_fills + sizeof(FillCmd) * (size_t)n_fills);
+    const size_t total = al(o_cnt + sizeof(int32_t) * CNT_COUNT);
+    if (c.params.ensure(total) || c.staging.ensure(total)) return Z2D_ERR_OUT_OF_MEMORY;
+    uint8_t *h = c.staging.as<uint8_t>();
+    uint8_t *dv = c.params.as<uint8_t>();
+    const DevGradient *dgrads = reinterpret_cast<const DevGradient *>(dv + o_grads);
+    for (int32_t i = 0; i < n_fills; i++)
+        if (grad_of_fill[i] >= 0) fills[i].src.grad = dgrads + grad_of_fill[i];
+    memcpy(h + o_nodes, nodes, sizeof(z2d_node) * (size_t)n_nodes);
+    memcpy(h + o_nfill, node_fill.data(), sizeof(int32_t) * (size_t)n_nodes);
+    if (!grads.empty()) memcpy(h + o_grads, grads.data(), sizeof(DevGradient) * grads.size());
+    memcpy(h + o_fills, fills.data(), sizeof(FillCmd) * (size_t)n_fills);
+    int32_t *cnt_h = reinterpret_cast<int32_t *>(h + o_cnt);
+    for (int i = 0; i < CNT_COUNT; i++) cnt_h[i] = 0;
+    cnt_h[CNT_BAND_MIN] = 0x7FFFFFFF;
+    cnt_h[CNT_BAND_MAX] = -1;
+    cnt_h[CNT_TCOL_MIN] = 0x7FFFFFFF;
+    cnt_h[CNT_TCOL_MAX] = -1;
+    // make sure the previous call's kernels no longer read the staging buffer
+    Z2D_CUDA(cudaStreamSynchronize(c.stream));
+    Z2D_CUDA(cudaMemcpyAsync(dv, h, total, cudaMemcpyHostToDevice, c.stream));
+    const z2d_node *d_nodes = reinterpret_cast<const z2d_node *>(dv + o_nodes);
+    const int32_t *d_nfill = reinterpret_cast<const int32_t *>(dv + o_nfill);
+    const FillCmd *d_fills = reinterpret_cast<const FillCmd *>(dv + o_fills);
+    int32_t *d_cnt = reinterpret_cast<int32_t *>(dv + o_cnt);
+
+    if (c.node_info.ensure(sizeof(NodeInfo) * (size_t)n_nodes) || c.fill_state.ensure(sizeof(FillState) * (size_t)n_fills))
+        return Z2D_ERR_OUT_OF_MEMORY;
+    NodeInfo *d_info = c.node_info.as<NodeInfo>();
+    FillState *d_st = c.fill_state.as<FillState>();
+    Z2D_CUDA(cudaMemsetAsync(d_st, 0, sizeof(FillState) * (size_t)n_fills, c.stream));
+
+    // ---- flatten
+    k_node_count<<<grid_for(n_nodes, 128), 128, 0, c.stream>>>(d_nodes, d_nfill, d_fills, d_info, n_nodes, d_cnt + CNT_STATUS);
+    k_fill_scan<<<grid_for(n_fills, 64), 64, 0, c.stream>>>(d_nodes, d_fills, d_info, d_st, n_fills, d_cnt, d_cnt + CNT_STATUS);
+    c.launches += 2;
+    if (c.readback.ensure(sizeof(int32_t) * CNT_COUNT)) return Z2D_ERR_OUT_OF_MEMORY;
+    int32_t *rb = c.readback.as<int32_t>();
+    Z2D_CUDA(cudaMemcpyAsync(rb, d_cnt, sizeof(int32_t) * CNT_COUNT, cudaMemcpyDeviceToHost, c.stream));
+    Z2D_CUDA(cudaStreamSynchronize(c.stream));
+    if (rb[CNT_STATUS] != 0) {
+        set_error("curve subdivision exceeded its depth bound");
+        return rb[CNT_STATUS];
+    }
+    const int32_t n_edges = rb[CNT_EDGES];
+    if (n_edges < 0) return Z2D_ERR_OUT_OF_MEMORY;
+    if (c.edges.ensure(sizeof(DEdge) * (size_t)std::max(n_edges, 1) + sizeof(int32_t) * (size_t)std::max(n_edges, 1)))
+        return Z2D_ERR_OUT_OF_MEMORY;
+    DEdge *d_edges = c.edges.as<DEdge>();
+    int32_t *d_edge_fill = reinterpret_cast<int32_t *>(d_edges + std::max(n_edges, 1));
+    // extents start at +inf/-inf keys: min slots 0xFF.., max slots 0
+    k_node_emit<<<grid_for(n_nodes, 128), 128, 0, c.stream>>>(d_nodes, d_nfill, d_fills, d_info, d_st, d_edges, n_nodes);
+    k_edge_fill<<<n_fills, 128, 0, c.stream>>>(d_st, n_fills, d_edge_fill);
+    k_fill_setup<<<grid_for(n_fills, 64), 64, 0, c.stream>>>(d_fills, d_st, n_fills, sfc.w, sfc.h, d_cnt);
+    c.launches += 3;
+    Z2D_CUDA(cudaMemcpyAsync(rb, d_cnt, sizeof(int32_t) * CNT_COUNT, cudaMemcpyDeviceToHost, c.stream));
+    Z2D_CUDA(cudaStreamSynchronize(c.stream));
+    const int32_t n_fb = rb[CNT_FILL_BANDS];
+    const long long mask_bytes = (long long)(((unsigned long long)(uint32_t)rb[CNT_MASK_LO + 1] << 32) | (uint32_t)rb[CNT_MASK_LO]);
+    const int32_t n_exact = rb[CNT_EXACT];
+    const int32_t band_lo = rb[CNT_BAND_MIN], band_hi = rb[CNT_BAND_MAX];
+    const int32_t tcol_lo = rb[CNT_TCOL_MIN], tcol_hi = rb[CNT_TCOL_MAX];
+    if (band_hi < band_lo || tcol_hi < tcol_lo) return Z2D_OK;  // nothing is drawn
+
+    // ---- bins: counts, exclusive scan, scatter
+    if (c.bin_offsets.ensure(sizeof(int32_t) * (2 * (size_t)n_fb + 2))) return Z2D_ERR_OUT_OF_MEMORY;
+    int32_t *d_fb_cnt = c.bin_offsets.as<int32_t>();
+    int32_t *d_fb_off = d_fb_cnt + (n_fb + 1);
+    Z2D_CUDA(cudaMemsetAsync(d_fb_cnt, 0, sizeof(int32_t) * (size_t)(n_fb + 1), c.stream));
+    if (n_edges > 0) {
+        k_bin_count<<<grid_for(n_edges, 256), 256, 0, c.stream>>>(d_fills, d_st, d_edges, d_edge_fill, n_edges, d_fb_cnt);
+        c.launches++;
+    }
+    size_t tmp_bytes = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, d_fb_cnt, d_fb_off, n_fb + 1, c.stream);
+    if (c.scan_tmp.ensure(tmp_bytes + 16)) return Z2D_ERR_OUT_OF_MEMORY;
+    Z2D_CUDA(cub::DeviceScan::ExclusiveSum(c.scan_tmp.ptr, tmp_bytes, d_fb_cnt, d_fb_off, n_fb + 1, c.stream));
+    c.launches++;
+    Z2D_CUDA(cudaMemcpyAsync(rb, d_fb_off + n_fb, sizeof(int32_t), cudaMemcpyDeviceToHost, c.stream));
+    Z2D_CUDA(cudaStreamSynchronize(c.stream));
+    const int32_t n_bin_entries = rb[0];
+    if (c.bins.ensure(sizeof(int32_t) * (size_t)std::max(n_bin_entries, 1))) return Z2D_ERR_OUT_OF_MEMORY;
+    // scatter with the counts array reused as cursors
+    Z2D_CUDA(cudaMemcpyAsync(d_fb_cnt, d_fb_off, sizeof(int32_t) * (size_t)(n_fb + 1), cudaMemcpyDeviceToDevice, c.stream));
+    if (n_edges > 0 && n_bin_entries > 0) {
+        k_bin_fill<<<grid_for(n_edges, 256), 256, 0, c.stream>>>(d_fills, d_st, d_edges, d_edge_fill, n_edges, d_fb_cnt,
+                                                                  c.bins.as<int32_t>());
+        c.launches++;
+    }
+
+    // ---- ordered fill lists per band
+    const int32_t n_bands = band_hi - band_lo + 1;
+    if (c.band_fills.ensure(sizeof(int32_t) * ((size_t)n_bands * (size_t)n_fills + (size_t)n_bands))) return Z2D_ERR_OUT_OF_MEMORY;
+    int32_t *d_band_count = c.band_fills.as<int32_t>();
+    int32_t *d_band_fills = d_band_count + n_bands;
+    k_band_lists<<<n_bands, 256, 0, c.stream>>>(d_st, n_fills, band_lo, d_band_count, d_band_fills);
+    c.launches++;
+
+    // ---- exact path
+    if (n_exact > 0) {
+        // mask plus per-fill work arrays (3 ints per edge, 8-byte aligned)
+        const size_t need = (size_t)mask_bytes + 64;
+        if (c.masks.ensure(need)) return Z2D_ERR_OUT_OF_MEMORY;
+        Z2D_CUDA(cudaMemsetAsync(c.masks.ptr, 0, (size_t)mask_bytes, c.stream));
+        k_exact<<<grid_for(n_fills, 32), 32, 0, c.stream>>>(d_fills, d_st, d_edges, n_fills, sfc.w, c.masks.as<uint8_t>());
+        c.launches++;
+    }
+
+    // ---- raster
+    RasterArgs A;
+    A.dst = sfc;
+    A.fills = d_fills;
+    A.st = d_st;
+    A.edges = d_edges;
+    A.bins = c.bins.as<int32_t>();
+    A.bin_off = d_fb_off;
+    A.band_count = d_band_count;
+    A.band_fills = d_band_fills;
+    A.masks = c.masks.as<uint8_t>();
+    A.n_fills = n_fills;
+    A.band_lo = band_lo;
+    A.tcol_lo = tcol_lo;
+    const size_t smem = sizeof(int32_t) * (16 * kTileCols * 4 + kTileRows * kTileCols);
+    static bool attr_set = false;
+    if (!attr_set) {
+        Z2D_CUDA(cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr_set = true;
+    }
+    dim3 grid((unsigned)(tcol_hi - tcol_lo + 1), (unsigned)n_bands);
+    cudaEvent_t t0 = c.timer_begin(c.t_raster);
+    k_raster<<<grid, kRasterThreads, smem, c.stream>>>(A);
+    c.timer_end(c.t_raster, t0);
+    c.launches++;
+    Z2D_CUDA(cudaGetLastError());
+    return Z2D_OK;
+}
+
+}  // namespace z2dg

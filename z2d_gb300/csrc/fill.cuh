@@ -1,0 +1,90 @@
+// fill.cuh -- device structures of the fill pipeline (fill.cu).
+#pragma once
+#include <stdint.h>
+
+#include "z2d_internal.h"
+
+namespace z2dg {
+
+constexpr int kSplineStack = 48;  // subdivision depth bound (coordinates are bounded)
+constexpr int32_t kSplineMaxSplits = 1 << 22;  // subdivisions per curve before giving up
+constexpr int kTileRows = 4;      // pixel rows per band / tile
+constexpr int kTileCols = 256;    // pixels per tile row
+constexpr int kRasterThreads = 512;
+
+// One fill command, prepared on the host.
+struct FillCmd {
+    int32_t node_off, n_nodes;
+    int32_t aa;         // Z2D_AA_NONE or Z2D_AA_MULTISAMPLE_4X
+    int32_t rule, op;
+    int32_t precision;  // after the float upgrade of multisample.zig:36 / direct.zig:25
+    int32_t pattern_kind;
+    int32_t reduces;    // pixel pattern whose operator reduces to the source (shared.zig:111-117)
+    double tol;         // max(tolerance, 0.001) (painter.zig:103)
+    double scale;       // 4 for multisample, 1 for none (painter.zig:93-97)
+    DevSrc src;         // the pattern as a compositor source
+    Px px_paint;        // pattern pixel converted to the surface format (paintStride)
+    I16 px_rgba;        // RGBA.fromPixel lanes of the pattern pixel (compositeStride)
+};
+
+// Per-node results of the flatten passes.
+struct NodeInfo {
+    double sx, sy;  // start point (the buffer's last point before the node)
+    double ex, ey;  // close_path: the subpath's first point
+    int32_t n_emit; // edges emitted (one per lineTo the reference issues)
+    int32_t n_added;
+    int32_t edge_off;
+    int32_t _pad;
+};
+
+// Polygon.Edge plus its rounded active range: the edge is active on sample
+// row y exactly when rt <= y < rb (top < y+0.5 <= bottom, Polygon.zig:284-285).
+struct DEdge {
+    double x_start, x_inc, top;
+    int32_t rt, rb;
+    int32_t dir;  // -1 down, +1 up, 0 horizontal (dropped)
+    int32_t _pad;
+};
+
+enum : int32_t {
+    FILL_OPEN_CHAIN = 1,  // an open 2-point subpath: rows may be unbalanced
+    FILL_EXACT = 2,       // rasterised by k_exact
+};
+
+struct FillState {
+    int32_t edge_base, n_edges, flags, has_edges;
+    unsigned long long ext[4];  // top(min), bottom(max), left(min), right(max) as ordered keys
+    int32_t active;             // inBox passed
+    int32_t start_y, end_y;     // draw rows [start_y, end_y]
+    int32_t start_x, end_x;     // draw columns [start_x, end_x)
+    int32_t band0, band1;       // bands the fill touches
+    int32_t fb_base;            // first (fill, band) slot
+    int32_t mask_w, mask_x0;
+    long long mask_base;        // exact-path action mask offset (bytes)
+};
+
+// counters (int32 slots; the mask byte count is a 64-bit pair)
+enum : int32_t {
+    CNT_EDGES = 0,
+    CNT_FILL_BANDS = 1,
+    CNT_MASK_LO = 2,  // + CNT_MASK_HI = 3
+    CNT_EXACT = 4,
+    CNT_BAND_MIN = 5,
+    CNT_BAND_MAX = 6,
+    CNT_TCOL_MIN = 7,
+    CNT_TCOL_MAX = 8,
+    CNT_STATUS = 9,
+    CNT_COUNT = 10
+};
+
+// action-mask byte of the exact path: bit 7 = clear first, bits 0-4 = coverage
+constexpr uint8_t kMaskClear = 0x80;
+
+// Runs an ordered list of fills on a device surface.  `fills` hold the
+// prepared commands (node offsets into `nodes`, host memory);
+// grad_of_fill[i] >= 0 names the gradient of fill i in `grads`.
+int run_fills(Ctx &c, const DevSurface &sfc, const z2d_node *nodes, int32_t n_nodes, std::vector<FillCmd> &fills,
+              const std::vector<int32_t> &node_fill, const std::vector<DevGradient> &grads,
+              const std::vector<int32_t> &grad_of_fill);
+
+}  // namespace z2dg

@@ -1,0 +1,106 @@
+// z2d_internal.h -- host-side internals shared by the library's .cu files:
+// the context (stream, device arena, pinned staging), error reporting and
+// conversion of C ABI descriptors into device descriptors.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/z2dgpu.h"
+#include "z2d_pixel.cuh"
+
+namespace z2dg {
+
+// thread-local message behind z2dgpu_last_error()
+void set_error(const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define Z2D_CUDA(call)                                        \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
+    } while (0)
+
+// A growable device buffer.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t cap = 0;
+    int ensure(size_t bytes);
+    void release();
+    template <class T>
+    T *as() const { return reinterpret_cast<T *>(ptr); }
+};
+// A growable pinned host buffer.
+struct HostBuf {
+    void *ptr = nullptr;
+    size_t cap = 0;
+    int ensure(size_t bytes);
+    void release();
+    template <class T>
+    T *as() const { return reinterpret_cast<T *>(ptr); }
+};
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    uint64_t launches = 0;
+    int sm_count = 0;
+    // device scratch, reused across calls on this context
+    DevBuf params;      // descriptors uploaded per call (patterns, gradients, fills)
+    DevBuf nodes;       // path nodes
+    DevBuf node_info;   // per-node flatten info
+    DevBuf edges;       // flattened edges
+    DevBuf fill_state;  // per-fill device state
+    DevBuf counters;    // small counters read back by the host
+    DevBuf band_fills;  // ordered fill lists per band
+    DevBuf bins;        // per (fill, band) edge lists
+    DevBuf bin_offsets; // per (fill, band) offsets/cursors
+    DevBuf masks;       // exact-path action masks
+    DevBuf surface;     // staging copy of host surfaces
+    DevBuf surface2;    // staging for a second host surface (compositor params)
+    DevBuf surface3;
+    DevBuf scan_tmp;    // temporary storage of device-wide scans
+    HostBuf staging;    // pinned upload staging
+    HostBuf readback;   // pinned readback
+    cudaEvent_t done = nullptr;
+    // kernel timing (z2dgpu_ctx_set_timing)
+    bool timing = false;
+    struct Timer {
+        std::vector<cudaEvent_t> pending;  // start/stop pairs not yet read
+        double ms = 0;
+        uint64_t n = 0;
+    } t_raster, t_composite;
+    cudaEvent_t timer_begin(Timer &t);
+    void timer_end(Timer &t, cudaEvent_t start);
+    void timer_collect(Timer &t);
+};
+
+// -------------------------------------------------- descriptor conversion
+// Fills `out` for a pattern or compositor param.  Gradients are written to
+// `grad_host` (the caller uploads them and patches DevSrc::grad).
+// Returns Z2D_OK or an error code.
+int make_dev_gradient(const z2d_gradient &g, DevGradient &out);
+int make_dev_src_from_pattern(int param_kind, const z2d_pattern &p, DevSrc &out, bool &needs_grad,
+                              DevGradient &grad_out);
+
+// --------------------------------------------------------------- kernels
+struct CompOp {
+    int32_t op;
+    DevSrc dst;  // kind SRC_NONE => the destination surface
+    DevSrc src;  // kind SRC_NONE => previous result
+};
+struct CompJob {
+    DevSurface dst;
+    int32_t n_ops, precision;
+    int32_t dst_x, dst_y;   // batch origin
+    int32_t dsx;            // first destination column
+    int32_t y0, y1;         // destination rows [y0, y1)
+    int32_t line_w;         // pixels per row
+    CompOp ops[2];
+};
+int launch_composite(Ctx &c, const CompJob &job);
+
+}  // namespace z2dg

@@ -1,0 +1,62 @@
+"""painter.fill with z2d's signature, running on the GPU (libz2dgpu.so).
+
+Mirrors src/painter.zig:66-143: the same options, defaults and errors
+(raised as native.Z2DError with z2d's error names).  fill_batch is the
+batched form: N fills on one surface in call order, one device pass.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import abi
+from .native import Context, check, default_context
+from .types import NODE_DTYPE, FillOptions, Pattern, nodes_to_abi
+
+
+def fill(surface, pattern: Pattern, nodes, opts: FillOptions = FillOptions(), ctx: Optional[Context] = None) -> None:
+    """Fills the path `nodes` onto `surface` with `pattern`."""
+    ctx = ctx or default_context()
+    keep: list = []
+    s = surface.to_abi()
+    p = pattern.to_abi(keep)
+    arr = nodes_to_abi(nodes)
+    check(ctx.lib.z2dgpu_fill(ctx.handle, C.byref(s), C.byref(p), arr, len(nodes), C.byref(opts.to_abi())))
+
+
+def fill_batch(surface, fills: Sequence[Tuple[Pattern, object, FillOptions]], ctx: Optional[Context] = None) -> None:
+    """Equivalent to fill() for each (pattern, nodes, opts) in order."""
+    ctx = ctx or default_context()
+    keep: list = []
+    node_arrays = []
+    cmds = (abi.z2d_fill_cmd * max(1, len(fills)))()
+    off = 0
+    for i, (pat, nodes, opts) in enumerate(fills):
+        arr = nodes if isinstance(nodes, np.ndarray) and nodes.dtype == NODE_DTYPE else None
+        if arr is None:
+            from .path import nodes_array
+            arr = nodes_array(nodes)
+        node_arrays.append(arr)
+        p = pat.to_abi(keep)
+        cmds[i].pattern = C.pointer(p)
+        cmds[i].node_offset = off
+        cmds[i].n_nodes = len(arr)
+        cmds[i].opts = opts.to_abi()
+        off += len(arr)
+    all_nodes = np.concatenate(node_arrays) if node_arrays else np.zeros(0, NODE_DTYPE)
+    all_nodes = np.ascontiguousarray(all_nodes)
+    s = surface.to_abi()
+    check(ctx.lib.z2dgpu_fill_batch(ctx.handle, C.byref(s),
+                                    all_nodes.ctypes.data_as(C.POINTER(abi.z2d_node)), len(all_nodes),
+                                    cmds, len(fills)))
+
+
+def fill_batch_arrays(surface, nodes: np.ndarray, cmds, ctx: Optional[Context] = None) -> None:
+    """Low-level batch entry: a NODE_DTYPE array and a ctypes z2d_fill_cmd
+    array that indexes into it (no per-call marshalling)."""
+    ctx = ctx or default_context()
+    s = surface.to_abi()
+    check(ctx.lib.z2dgpu_fill_batch(ctx.handle, C.byref(s), nodes.ctypes.data_as(C.POINTER(abi.z2d_node)),
+                                    len(nodes), cmds, len(cmds)))

@@ -72,8 +72,10 @@ class Surface:
         if data is None:
             data = np.zeros(nbytes, np.uint8)
         if getattr(data, "numel", None) is not None:  # torch tensor
-            if data.numel() != nbytes:
-                raise ValueError(f"surface buffer has {data.numel()} bytes, need {nbytes}")
+            # packed formats on the device are padded to a 4-byte multiple
+            padded = (nbytes + 3) // 4 * 4 if self.format >= abi.FORMAT_ALPHA4 else nbytes
+            if data.numel() not in (nbytes, padded) or (self.format >= abi.FORMAT_ALPHA4 and data.numel() != padded):
+                raise ValueError(f"surface buffer has {data.numel()} bytes, need {padded}")
         elif data.size != nbytes:
             raise ValueError(f"surface buffer has {data.size} bytes, need {nbytes}")
         self.data = data
@@ -118,7 +120,10 @@ class Surface:
 
     def to_device(self, device: str = "cuda") -> "Surface":
         import torch
-        t = torch.from_numpy(np.ascontiguousarray(self.numpy())).to(device)
+        h = np.ascontiguousarray(self.numpy())
+        if self.format >= abi.FORMAT_ALPHA4:  # pad to a 4-byte multiple (word atomics)
+            h = np.concatenate([h, np.zeros((-h.size) % 4, np.uint8)])
+        t = torch.from_numpy(h).to(device)
         return Surface(self.format, self.width, self.height, t)
 
     def to_host(self) -> "Surface":
@@ -127,7 +132,8 @@ class Surface:
     def numpy(self) -> np.ndarray:
         if isinstance(self.data, np.ndarray):
             return self.data
-        return self.data.detach().cpu().numpy()
+        nbytes = abi.surface_bytes(self.format, self.width, self.height)
+        return self.data.detach().cpu().numpy()[:nbytes]
 
     def copy(self) -> "Surface":
         if isinstance(self.data, np.ndarray):
