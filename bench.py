@@ -13,7 +13,8 @@ the clamped multisample draw box (multisample.zig:46-78).
 Arms of this implementation:
   value  -- batched: all 2,000 fills in one z2dgpu_fill_batch call on a
             device-resident surface (CUDA events on the library's stream).
-  plain  -- the per-call drop-in: 2,000 z2dgpu_fill calls (reported beside).
+  plain  -- the per-call drop-in: one z2dgpu_fill call per path, timed on the
+            first 300 fills (reported beside).
   e2e    -- batched through the C ABI with a pinned HOST surface: the call
             uploads the surface and nodes and reads the surface back inside
             the timed region.
@@ -45,6 +46,7 @@ SEED = 2025
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
 CPU_SAMPLE_FILLS = 2000   # cpu_baseline sample: the whole workload (~10-20 s single-threaded)
 REF_STEP_FILLS = 400      # --impl reference: fills per timed step
+PLAIN_FILLS = 300         # per-call arm: fills drawn with one z2dgpu_fill each
 
 
 def load_peaks():
@@ -258,17 +260,6 @@ def run_ours(args):
         total_ms = float(t.item())
     value = world * mpix_step * args.steps / (total_ms / 1e3)
 
-    # ---- plain per-call arm (one step)
-    restore()
-    stream.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for pat, n, opts in fills:
-        painter.fill(surf, pat, n, opts, ctx=ctx)
-    e1.record(stream)
-    e1.synchronize()
-    plain_ms = e0.elapsed_time(e1)
-
     # ---- e2e: pinned host surface through the C ABI (H2D + D2H inside)
     host_t = torch.empty(bg.size, dtype=torch.uint8, pin_memory=True)
     host = host_t.numpy()
@@ -284,6 +275,19 @@ def run_ours(args):
     e2e_value = mpix_step * args.steps / sum(e2e_s)
     h2d = bg.nbytes + nodes.nbytes + len(fills) * 64
     d2h = bg.nbytes
+
+    # ---- plain per-call arm: z2dgpu_fill once per path, on the first
+    # PLAIN_FILLS fills (same device-resident surface, same accounting)
+    restore()
+    stream.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for pat, n, opts in fills[:PLAIN_FILLS]:
+        painter.fill(surf, pat, n, opts, ctx=ctx)
+    e1.record(stream)
+    e1.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    plain_mpix = sum(px[:PLAIN_FILLS]) / 1e6
 
     if rank != 0:
         return
@@ -301,9 +305,9 @@ def run_ours(args):
         "config": {"workload": "plain_large_4096x4096_2000_paths", "surface": "rgba 4096x4096",
                    "paths": N_FILLS, "mpix_per_step": mpix_step, "l2": "flushed (256 MiB write) before each step",
                    "mode": "batched (z2dgpu_fill_batch, device-resident surface)"},
-        "plain": {"value": mpix_step / (plain_ms / 1e3), "unit": "Mpix/s", "ms_per_step": plain_ms,
-                  "calls": len(fills)},
-        "batched_over_plain": (mpix_step / (total_ms / args.steps / 1e3)) / (mpix_step / (plain_ms / 1e3)),
+        "plain": {"value": plain_mpix / (plain_ms / 1e3), "unit": "Mpix/s", "ms": plain_ms,
+                  "calls": PLAIN_FILLS, "note": f"z2dgpu_fill per path, first {PLAIN_FILLS} fills"},
+        "batched_over_plain": (mpix_step / (total_ms / args.steps / 1e3)) / (plain_mpix / (plain_ms / 1e3)),
         "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": "k_raster", "achieved": achieved, "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,

@@ -430,7 +430,7 @@ __device__ __forceinline__ bool edge_bands(const DEdge &e, const FillCmd &F, con
 
 __global__ void k_bin_count(const FillCmd *__restrict__ fills, const FillState *__restrict__ st,
                             const DEdge *__restrict__ edges, const int32_t *__restrict__ edge_fill, int32_t n_edges,
-                            int32_t *__restrict__ fb_count) {
+                            int32_t *__restrict__ fb_count, int32_t *__restrict__ status) {
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_edges) return;
     const int32_t f = edge_fill[i];
@@ -439,7 +439,8 @@ __global__ void k_bin_count(const FillCmd *__restrict__ fills, const FillState *
     if (!S.active || (S.flags & FILL_EXACT)) return;
     int32_t b0, b1;
     if (!edge_bands(edges[i], fills[f], S, b0, b1)) return;
-    for (int32_t b = b0; b <= b1; b++) atomicAdd(&fb_count[S.fb_base + (b - S.band0)], 1);
+    for (int32_t b = b0; b <= b1; b++)
+        if (atomicAdd(&fb_count[S.fb_base + (b - S.band0)], 1) >= kMaxBandEdges) atomicExch(status, Z2D_ERR_INVALID_ARGUMENT);
 }
 
 __global__ void k_bin_fill(const FillCmd *__restrict__ fills, const FillState *__restrict__ st,
@@ -683,101 +684,140 @@ struct RasterArgs {
     int32_t n_fills, band_lo, tcol_lo;
 };
 
-// Sample column c of a sub-scanline belongs to lane c / per (per = sample
-// columns per lane: 32 with 4x sampling, 8 without); it is stored at
-// (c % per) * 32 + lane so that a warp reading one k for all lanes hits 32
-// consecutive words.
-__device__ __forceinline__ int delta_index(int c, int per) { return ((c % per) << 5) | (c / per); }
+// Winding deltas of one warp: up to 4 sample rows x 1024 sample columns,
+// two biased 16-bit counters per word (bias 0x8000; a fill with at most
+// kMaxBandEdges edges in a band can never carry a counter across halves).
+constexpr int kWordsPerSubRow = 512;
+constexpr int kWarpWords = 4 * kWordsPerSubRow;
+constexpr uint32_t kBias2 = 0x80008000u;
 
-__global__ void __launch_bounds__(kRasterThreads) k_raster(const RasterArgs A) {
-    extern __shared__ int32_t smem[];
-    int32_t *delta = smem;                      // [16 sample rows][1024 sample columns]
-    int32_t *cov = smem + 16 * kTileCols * 4;   // [4 rows][256 px]
+// Sample column c of a sub-scanline belongs to lane c / per (per = sample
+// columns per lane: 32 with 4x sampling, 8 without); the pair holding it is
+// stored at ((c % per) / 2) * 32 + lane, so a warp reading pair k of every
+// lane touches 32 consecutive words.
+__device__ __forceinline__ int pair_index(int c, int per) { return (((c % per) >> 1) << 5) | (c / per); }
+
+__device__ __forceinline__ I16 raw_to_i16(uint32_t raw, int fmt) {
+    if (fmt <= Z2D_FORMAT_RGBA) return word_to_i16(raw, fmt);
+    return I16{0, 0, 0, scale_alpha(raw, fmt_bits(fmt), 8)};
+}
+__device__ __forceinline__ uint32_t i16_to_raw(I16 v, int fmt) {
+    if (fmt <= Z2D_FORMAT_RGBA) return i16_to_word(v, fmt);
+    return scale_alpha(v.a & 0xFFu, 8, fmt_bits(fmt));
+}
+__device__ __forceinline__ uint32_t load_raw(const DevSurface &s, size_t i) {
+    if (s.fmt <= Z2D_FORMAT_RGBA) return reinterpret_cast<const uint32_t *>(s.data)[i];
+    if (s.fmt == Z2D_FORMAT_ALPHA8) return s.data[i];
+    const int bits = fmt_bits(s.fmt);
+    const size_t bit = i * (size_t)bits;
+    return (s.data[bit >> 3] >> (bit & 7)) & ((1u << bits) - 1u);
+}
+__device__ __forceinline__ void store_raw(const DevSurface &s, size_t i, uint32_t v) {
+    if (s.fmt <= Z2D_FORMAT_RGBA) reinterpret_cast<uint32_t *>(s.data)[i] = v;
+    else if (s.fmt == Z2D_FORMAT_ALPHA8) s.data[i] = (uint8_t)v;
+    else store_raw_packed(s, i, v);
+}
+
+// One CTA per tile of 4 rows x 256 pixels; warp w owns pixel row w of the
+// tile and lane l its pixels [8l, 8l+8).  Warps never wait for each other:
+// each walks the band's fills in call order, accumulates the winding deltas
+// of its row's 4 (or 1) sample rows from the fill's band edges, prefix-scans
+// them across the warp, turns the inside bits into coverage and composites
+// its 8 pixels, which stay in registers from the first fill to the last.
+__global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A) {
+    extern __shared__ uint32_t smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t *words = smem + warp * kWarpWords;
     const int32_t b = A.band_lo + blockIdx.y;
-    const int32_t x0 = (A.tcol_lo + blockIdx.x) * kTileCols, y0 = b * kTileRows;
     const int32_t cnt = A.band_count[blockIdx.y];
     if (cnt == 0) return;
-    const int32_t *list = A.band_fills + (size_t)blockIdx.y * A.n_fills;
+    const int32_t x0 = (A.tcol_lo + blockIdx.x) * kTileCols, y = b * kTileRows + warp;
     const int32_t W = A.dst.w, H = A.dst.h, fmt = A.dst.fmt;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (y >= H) return;
+    const int32_t *list = A.band_fills + (size_t)blockIdx.y * A.n_fills;
+    const int32_t px0 = x0 + lane * 8;  // this lane's first pixel
 
-    I16 d[2];
-    bool touched[2] = {false, false};
+    for (int i = lane; i < kWarpWords; i += 32) words[i] = kBias2;
+    uint32_t raw[8];
+    uint32_t touched = 0;
 #pragma unroll
-    for (int j = 0; j < 2; j++) {
-        const int p = tid + kRasterThreads * j;
-        const int32_t x = x0 + (p & (kTileCols - 1)), y = y0 + (p >> 8);
-        d[j] = (x < W && y < H) ? load_px(A.dst, (size_t)W * y + x) : I16{0, 0, 0, 0};
-    }
-    for (int i = tid; i < 16 * kTileCols * 4 + kTileRows * kTileCols; i += kRasterThreads) smem[i] = 0;
-    __syncthreads();
+    for (int q = 0; q < 8; q++) raw[q] = (px0 + q < W) ? load_raw(A.dst, (size_t)W * y + px0 + q) : 0u;
+    __syncwarp();
 
     for (int32_t k = 0; k < cnt; k++) {
         const int32_t f = list[k];
         const FillState &S = A.st[f];
         const FillCmd &F = A.fills[f];
-        const bool bounded = is_bounded(F.op);
+        const int32_t op = F.op;
+        const bool bounded = is_bounded(op);
+        if (bounded && (S.end_x <= x0 || S.start_x >= x0 + kTileCols)) continue;
         const bool direct = F.aa == Z2D_AA_NONE;
         const bool exact = (S.flags & FILL_EXACT) != 0;
-        if (bounded && (S.end_x <= x0 || S.start_x >= x0 + kTileCols)) continue;
-        const int32_t sc = direct ? 1 : 4;
-        const bool rows_here = !(S.end_y < y0 || S.start_y >= y0 + kTileRows);
-        if (!exact && rows_here) {
-            const int32_t sub0 = y0 * sc, sub1 = (y0 + kTileRows) * sc, col0 = x0 * sc, ncol = kTileCols * sc;
+        const bool in_rows = y >= S.start_y && y <= S.end_y;
+        if (!in_rows && bounded) continue;
+        const int32_t sc = direct ? 1 : 4, per = 8 * sc;
+        int cov[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        if (!exact && in_rows) {
+            const int32_t sub0 = y * sc, col0 = x0 * sc, ncol = kTileCols * sc;
             const int32_t fb = S.fb_base + (b - S.band0);
             const int32_t e0 = A.bin_off[fb], e1 = A.bin_off[fb + 1];
-            for (int32_t ei = e0 + tid; ei < e1; ei += kRasterThreads) {
+            for (int32_t ei = e0 + lane; ei < e1; ei += 32) {
                 const DEdge e = A.edges[A.bins[ei]];
-                const int32_t lo = max(e.rt, sub0), hi = min(e.rb, sub1);
+                const int32_t lo = max(e.rt, sub0), hi = min(e.rb, sub0 + sc);
                 for (int32_t sr = lo; sr < hi; sr++) {
                     const int32_t X = (int32_t)round(e.x_start + (e.x_inc * (((double)sr + 0.5) - e.top)));
                     int32_t c = X - col0;
                     if (c < 0) c = 0;
-                    if (c < ncol) atomicAdd(&delta[(sr - sub0) * 1024 + delta_index(c, 8 * sc)], e.dir);
+                    if (c < ncol) {
+                        const uint32_t inc = (c & 1) ? ((uint32_t)e.dir << 16) : (uint32_t)e.dir;
+                        atomicAdd(&words[(sr - sub0) * kWordsPerSubRow + pair_index(c, per)], inc);
+                    }
                 }
             }
-            __syncthreads();
-            if (warp < kTileRows * sc) {
-                const int per = 8 * sc;  // sample columns per lane
-                int32_t *row = delta + warp * 1024;
+            __syncwarp();
+            const int pairs = per >> 1;
+            for (int s = 0; s < sc; s++) {
+                uint32_t *row = words + s * kWordsPerSubRow;
                 int32_t tot = 0;
-                for (int kk = 0; kk < per; kk++) tot += row[(kk << 5) | lane];
+                for (int kk = 0; kk < pairs; kk++) {
+                    const uint32_t v = row[(kk << 5) | lane];
+                    tot += (int32_t)(v & 0xFFFFu) + (int32_t)(v >> 16) - 0x10000;
+                }
                 int32_t incl = tot;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
-                    const int32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += v;
+                    const int32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += t;
                 }
                 int32_t wnd = incl - tot;
                 uint32_t bits = 0;
-                for (int kk = 0; kk < per; kk++) {
-                    const int32_t idx = (kk << 5) | lane;
-                    wnd += row[idx];
-                    row[idx] = 0;
-                    const bool in = (F.rule == Z2D_FILL_EVEN_ODD) ? ((wnd & 1) != 0) : (wnd != 0);
-                    bits |= (uint32_t)in << kk;
+                for (int kk = 0; kk < pairs; kk++) {
+                    const int idx = (kk << 5) | lane;
+                    const uint32_t v = row[idx];
+                    row[idx] = kBias2;
+                    wnd += (int32_t)(v & 0xFFFFu) - 0x8000;
+                    bool in = (F.rule == Z2D_FILL_EVEN_ODD) ? ((wnd & 1) != 0) : (wnd != 0);
+                    bits |= (uint32_t)in << (2 * kk);
+                    wnd += (int32_t)(v >> 16) - 0x8000;
+                    in = (F.rule == Z2D_FILL_EVEN_ODD) ? ((wnd & 1) != 0) : (wnd != 0);
+                    bits |= (uint32_t)in << (2 * kk + 1);
                 }
                 if (direct) {
-                    for (int q = 0; q < 8; q++) cov[warp * kTileCols + lane * 8 + q] = (bits >> q) & 1u;
+#pragma unroll
+                    for (int q = 0; q < 8; q++) cov[q] += (bits >> q) & 1u;
                 } else {
-                    for (int q = 0; q < 8; q++) atomicAdd(&cov[(warp >> 2) * kTileCols + lane * 8 + q], __popc((bits >> (4 * q)) & 0xFu));
+#pragma unroll
+                    for (int q = 0; q < 8; q++) cov[q] += __popc((bits >> (4 * q)) & 0xFu);
                 }
             }
-            __syncthreads();
+            __syncwarp();
         }
 #pragma unroll
-        for (int j = 0; j < 2; j++) {
-            const int p = tid + kRasterThreads * j;
-            const int32_t col = p & (kTileCols - 1), r = p >> 8;
-            const int32_t x = x0 + col, y = y0 + r;
-            int c = 0;
-            if (!exact && rows_here) {
-                c = cov[r * kTileCols + col];
-                cov[r * kTileCols + col] = 0;
-            }
-            if (x >= W || y >= H) continue;
+        for (int q = 0; q < 8; q++) {
+            const int32_t x = px0 + q;
+            if (x >= W) continue;
+            int c = cov[q];
             bool clear = false;
-            const bool in_rows = y >= S.start_y && y <= S.end_y;
             if (exact && in_rows && x >= S.mask_x0 && x < S.mask_x0 + S.mask_w) {
                 const uint8_t m = A.masks[S.mask_base + (long long)(y - S.start_y) * S.mask_w + (x - S.mask_x0)];
                 c = m & 0x1F;
@@ -785,23 +825,16 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(const RasterArgs A) {
             }
             if (!direct && !bounded) clear = msaa_unbounded_clear(S, x, y, W);
             const bool in_box = in_rows && (direct ? true : (x >= S.start_x && x < S.end_x));
-            if (clear) {
-                d[j] = normalize(I16{0, 0, 0, 0}, fmt);
-                touched[j] = true;
-            }
-            if (in_box && c > 0) {
-                d[j] = apply_fill(F, fmt, x, y, c, direct ? 1 : 16, d[j]);
-                touched[j] = true;
-            }
+            if (!clear && !(in_box && c > 0)) continue;
+            I16 d = clear ? normalize(I16{0, 0, 0, 0}, fmt) : raw_to_i16(raw[q], fmt);
+            if (in_box && c > 0) d = apply_fill(F, fmt, x, y, c, direct ? 1 : 16, d);
+            raw[q] = i16_to_raw(d, fmt);
+            touched |= 1u << q;
         }
-        __syncthreads();
     }
 #pragma unroll
-    for (int j = 0; j < 2; j++) {
-        const int p = tid + kRasterThreads * j;
-        const int32_t x = x0 + (p & (kTileCols - 1)), y = y0 + (p >> 8);
-        if (touched[j] && x < W && y < H) store_px(A.dst, (size_t)W * y + x, d[j]);
-    }
+    for (int q = 0; q < 8; q++)
+        if ((touched >> q) & 1u) store_raw(A.dst, (size_t)W * y + px0 + q, raw[q]);
 }
 
 // ----------------------------------------------------------- host side
@@ -888,7 +921,8 @@ int run_fills(Ctx &c, const DevSurface &sfc, const z2d_node *nodes, int32_t n_no
     int32_t *d_fb_off = d_fb_cnt + (n_fb + 1);
     Z2D_CUDA(cudaMemsetAsync(d_fb_cnt, 0, sizeof(int32_t) * (size_t)(n_fb + 1), c.stream));
     if (n_edges > 0) {
-        k_bin_count<<<grid_for(n_edges, 256), 256, 0, c.stream>>>(d_fills, d_st, d_edges, d_edge_fill, n_edges, d_fb_cnt);
+        k_bin_count<<<grid_for(n_edges, 256), 256, 0, c.stream>>>(d_fills, d_st, d_edges, d_edge_fill, n_edges, d_fb_cnt,
+                                                                   d_cnt + CNT_STATUS);
         c.launches++;
     }
     size_t tmp_bytes = 0;
@@ -897,8 +931,13 @@ int run_fills(Ctx &c, const DevSurface &sfc, const z2d_node *nodes, int32_t n_no
     Z2D_CUDA(cub::DeviceScan::ExclusiveSum(c.scan_tmp.ptr, tmp_bytes, d_fb_cnt, d_fb_off, n_fb + 1, c.stream));
     c.launches++;
     Z2D_CUDA(cudaMemcpyAsync(rb, d_fb_off + n_fb, sizeof(int32_t), cudaMemcpyDeviceToHost, c.stream));
+    Z2D_CUDA(cudaMemcpyAsync(rb + 1, d_cnt + CNT_STATUS, sizeof(int32_t), cudaMemcpyDeviceToHost, c.stream));
     Z2D_CUDA(cudaStreamSynchronize(c.stream));
     const int32_t n_bin_entries = rb[0];
+    if (rb[1] != 0) {
+        set_error("a fill has more than 32000 edges inside one 4-row band");
+        return rb[1];
+    }
     if (c.bins.ensure(sizeof(int32_t) * (size_t)std::max(n_bin_entries, 1))) return Z2D_ERR_OUT_OF_MEMORY;
     // scatter with the counts array reused as cursors
     Z2D_CUDA(cudaMemcpyAsync(d_fb_cnt, d_fb_off, sizeof(int32_t) * (size_t)(n_fb + 1), cudaMemcpyDeviceToDevice, c.stream));
@@ -940,7 +979,7 @@ int run_fills(Ctx &c, const DevSurface &sfc, const z2d_node *nodes, int32_t n_no
     A.n_fills = n_fills;
     A.band_lo = band_lo;
     A.tcol_lo = tcol_lo;
-    const size_t smem = sizeof(int32_t) * (16 * kTileCols * 4 + kTileRows * kTileCols);
+    const size_t smem = sizeof(uint32_t) * kWarpWords * kTileRows;
     static bool attr_set = false;
     if (!attr_set) {
         Z2D_CUDA(cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

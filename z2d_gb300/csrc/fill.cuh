@@ -10,7 +10,8 @@ constexpr int kSplineStack = 48;  // subdivision depth bound (coordinates are bo
 constexpr int32_t kSplineMaxSplits = 1 << 22;  // subdivisions per curve before giving up
 constexpr int kTileRows = 4;      // pixel rows per band / tile
 constexpr int kTileCols = 256;    // pixels per tile row
-constexpr int kRasterThreads = 512;
+constexpr int kRasterThreads = 32 * kTileRows;  // one warp per tile row
+constexpr int32_t kMaxBandEdges = 32000;  // edges of one fill in one band (16-bit winding counters)
 
 // One fill command, prepared on the host.
 struct FillCmd {
