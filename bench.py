@@ -195,6 +195,55 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def compositor_sweep(ctx, stream, dev, reps=3):
+    """The compositor configuration on one surface: 8192x8192 RGBA
+    destination with seeded premultiplied pixels, a seeded alpha8 mask, and
+    the batch [dst_in(dst = pixel source, src = mask), op] for every integer
+    operator.  HBM bound: 4 B read + 4 B written + 1 B mask per pixel.  The
+    surfaces (288 MiB) exceed L2, so no flush is needed."""
+    import torch
+    from z2d_gb300 import abi, compositor
+    from z2d_gb300.surface import Surface
+    from z2d_gb300.types import Operation, Pattern, Pixel
+    n = 8192
+    g = torch.Generator(device=dev)
+    g.manual_seed(SEED)
+    a = torch.randint(0, 256, (n * n,), device=dev, generator=g, dtype=torch.int32)
+    rgb = torch.randint(0, 256, (n * n, 3), device=dev, generator=g, dtype=torch.int32) * (a[:, None] + 1) // 256
+    dst_t = torch.cat([rgb, a[:, None]], 1).to(torch.uint8).reshape(-1).contiguous()
+    base = dst_t.clone()
+    mask_t = torch.randint(0, 256, (n * n,), device=dev, generator=g, dtype=torch.int32).to(torch.uint8)
+    dst = Surface("rgba", n, n, dst_t)
+    mask = Surface("alpha8", n, n, mask_t)
+    src = Pattern.from_pixel(Pixel.rgba(90, 40, 160, 200))
+    int_ops = [o for o in abi.OPERATORS if o not in abi.FLOAT_ONLY_OPS]
+    per_op = {}
+    for op in int_ops:
+        ops = [Operation("dst_in", dst=src, src=mask), Operation(op)]
+        compositor.SurfaceCompositor.run(dst, 0, 0, ops, ctx=ctx)  # warm
+        ctx.set_timing(True)
+        for _ in range(reps):
+            compositor.SurfaceCompositor.run(dst, 0, 0, ops, ctx=ctx)
+        ms, nl = ctx.kernel_ms("composite")
+        ctx.set_timing(False)
+        per_op[op] = ms / max(nl, 1)
+        with torch.cuda.stream(stream):
+            dst_t.copy_(base)
+    stream.synchronize()
+    bytes_px = 4 + 4 + 1
+    px = n * n
+    so = per_op["src_over"]
+    mean_ms = sum(per_op.values()) / len(per_op)
+    return {
+        "workload": "8192x8192 rgba, alpha8 mask, [dst_in(pixel, mask), op], 21 integer operators",
+        "mpix_per_s_src_over": px / 1e6 / (so / 1e3),
+        "gbs_src_over": bytes_px * px / (so / 1e3) / 1e9,
+        "gbs_mean_all_ops": bytes_px * px / (mean_ms / 1e3) / 1e9,
+        "ms_per_launch": {k: round(v, 4) for k, v in per_op.items()},
+        "bytes_per_px": bytes_px,
+    }
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -296,6 +345,10 @@ def run_ours(args):
     alg_bytes = 2 * 4 * union_px  # read + write of every surface pixel a fill box touches
     raster_ms_per = raster_ms / max(raster_n, 1)
     achieved = alg_bytes / (raster_ms_per / 1e3) / 1e9
+    comp = compositor_sweep(ctx, stream, dev)
+    comp_roof = {"bound": "hbm", "kernel": "k_mask_batch (src_over)", "achieved": comp["gbs_src_over"],
+                 "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": comp["gbs_src_over"] / peaks["hbm_gbs"],
+                 "traffic": None, "peak_source": peak_kind}
     cpu_v, cpu_dt = cpu_sample(bg, fills, px, CPU_SAMPLE_FILLS)
     line = {
         "metric": "Mpix/s fill+composite (src_over, 4096x4096 RGBA, 2000 random paths)",
@@ -315,6 +368,8 @@ def run_ours(args):
                      "launch_ms": raster_ms_per},
         "cpu_baseline": {"value": cpu_v, "unit": "Mpix/s", "cores": 1, "kind": "port",
                          "sample": f"first {CPU_SAMPLE_FILLS} of {N_FILLS} fills, {cpu_dt:.1f} s"},
+        "compositor": comp,
+        "compositor_roofline": comp_roof,
         "gpu_launches": launches,
         "clocks": clk,
     }

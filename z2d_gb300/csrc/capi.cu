@@ -396,6 +396,7 @@ static int prepare_fills(const z2d_surface &s, const z2d_node *nodes, size_t n_n
             F.reduces = (F.op == Z2D_OP_SRC) || (F.op == Z2D_OP_SRC_OVER && opaque);
             F.px_paint = convert_px(px, s.format);
             F.px_rgba = to_i16(convert_px(px, Z2D_FORMAT_RGBA));
+            if (F.op == Z2D_OP_SRC_OVER && F.precision == Z2D_PRECISION_INTEGER) F.fast_kind = FAST_PIXEL_SRC_OVER;
         }
         const int32_t fi = (int32_t)fills.size();
         for (size_t k = 0; k < cm.n_nodes; k++) {

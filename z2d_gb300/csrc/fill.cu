@@ -345,6 +345,320 @@ __global__ void k_node_emit(const z2d_node *__restrict__ nodes, const int32_t *_
     }
 }
 
+// ------------------------------------------- warp-cooperative flattening
+// One warp per curve.  The subdivision tree of Spline.decomposeInto is first
+// expanded breadth-first into an ordered frontier of up to kFrontier
+// subcurves (z2d's depth-first order is the frontier order), then lane l
+// walks frontier items l and l+32 depth-first.  Warp scans give each lane
+// the number of points emitted before it and the point emitted just before
+// its first one, so edges land where the sequential walk would put them.
+constexpr int kFrontier = 64;
+constexpr int kFlattenWarps = 4;
+
+struct WarpFrontier {
+    Knots k[kFrontier];
+    uint8_t leaf[kFrontier];  // 1: error below tolerance already established
+};
+
+// Expands the frontier of the curve from (ax, ay) through p[0..5].
+__device__ int frontier_expand(double ax, double ay, const double *p, double tol2, WarpFrontier &fr, int lane) {
+    if (lane == 0) {
+        fr.k[0] = Knots{ax, ay, p[0], p[1], p[2], p[3], p[4], p[5]};
+        fr.leaf[0] = 0;
+    }
+    __syncwarp();
+    int n = 1;
+    for (int round = 0; round < 8 && n < 32; round++) {
+        Knots k{};
+        bool leaf = true;
+        int grow = 0;
+        if (lane < n) {
+            k = fr.k[lane];
+            leaf = fr.leaf[lane] || error_sq(k) < tol2;
+            grow = leaf ? 1 : 2;
+        }
+        int incl = grow;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        const bool all_leaf = __all_sync(0xffffffffu, leaf);
+        __syncwarp();
+        if (all_leaf || total > kFrontier) {
+            if (lane < n) fr.leaf[lane] = leaf ? 1 : 0;
+            __syncwarp();
+            break;
+        }
+        const int pos = incl - grow;
+        if (lane < n) {
+            if (leaf) {
+                fr.k[pos] = k;
+                fr.leaf[pos] = 1;
+            } else {
+                const Knots second = de_casteljau(k);
+                fr.k[pos] = k;
+                fr.leaf[pos] = 0;
+                fr.k[pos + 1] = second;
+                fr.leaf[pos + 1] = 0;
+            }
+        }
+        __syncwarp();
+        n = total;
+    }
+    return n;
+}
+
+// Depth-first walk of one frontier item; emit(x, y) for each leaf start
+// that differs from the curve start (Spline.zig:56-71).  The final
+// lineTo(d) is not part of an item.
+template <class F>
+__device__ __forceinline__ bool walk_item(const Knots &k0, bool leaf, double ax, double ay, double tol2, F &&emit) {
+    if (leaf) {
+        if (!pt_eq(k0.ax, k0.ay, ax, ay)) emit(k0.ax, k0.ay);
+        return true;
+    }
+    Knots stack[kSplineStack];
+    int sp = 0;
+    stack[sp++] = k0;
+    int32_t budget = kSplineMaxSplits;
+    while (sp > 0) {
+        Knots k = stack[--sp];
+        while (true) {
+            if (--budget < 0) return false;
+            if (error_sq(k) < tol2) {
+                if (!pt_eq(k.ax, k.ay, ax, ay)) emit(k.ax, k.ay);
+                break;
+            }
+            const Knots second = de_casteljau(k);
+            if (sp >= kSplineStack) return false;
+            stack[sp++] = second;
+        }
+    }
+    return true;
+}
+
+// "Last valid value before this lane" across the warp, seeded with carry.
+__device__ __forceinline__ void prev_point_scan(bool has, double lx, double ly, double cx, double cy, int lane,
+                                                double &px, double &py) {
+    // inclusive "most recent valid" scan, then shift by one lane
+    int v = has ? 1 : 0;
+    double x = lx, y = ly;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int tv = __shfl_up_sync(0xffffffffu, v, o);
+        const double tx = __shfl_up_sync(0xffffffffu, x, o);
+        const double ty = __shfl_up_sync(0xffffffffu, y, o);
+        if (lane >= o && !v) {
+            v = tv;
+            x = tx;
+            y = ty;
+        }
+    }
+    const int pv = __shfl_up_sync(0xffffffffu, v, 1);
+    const double qx = __shfl_up_sync(0xffffffffu, x, 1);
+    const double qy = __shfl_up_sync(0xffffffffu, y, 1);
+    if (lane > 0 && pv) {
+        px = qx;
+        py = qy;
+    } else {
+        px = cx;
+        py = cy;
+    }
+}
+
+__device__ __forceinline__ int warp_excl_sum(int v, int lane, int &total) {
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    total = __shfl_sync(0xffffffffu, incl, 31);
+    return incl - v;
+}
+
+// Counts the lineTo calls (n_emit) and the points they add (n_added) of the
+// curve from (sx, sy) through p, cooperatively.  Result valid in all lanes.
+__device__ bool curve_count_warp(double sx, double sy, const double *p, double tol, WarpFrontier &fr, int lane,
+                                 int32_t &n_emit, int32_t &n_added) {
+    if (pt_eq(sx, sy, p[0], p[1]) && pt_eq(p[2], p[3], p[4], p[5])) {  // Spline.zig:39-42
+        n_emit = 1;
+        n_added = pt_eq(sx, sy, p[4], p[5]) ? 0 : 1;
+        return true;
+    }
+    const double tol2 = tol * tol;
+    const int n = frontier_expand(sx, sy, p, tol2, fr, lane);
+    bool ok = true;
+    int32_t emit_tot = 0, add_tot = 0;
+    double carry_x = sx, carry_y = sy;
+    for (int base = 0; base < n; base += 32) {
+        const int i = base + lane;
+        int32_t cnt = 0, internal = 0;
+        double fx = 0, fy = 0, lx = 0, ly = 0;
+        if (i < n) {
+            ok &= walk_item(fr.k[i], fr.leaf[i] != 0, sx, sy, tol2, [&](double x, double y) {
+                if (cnt == 0) {
+                    fx = x;
+                    fy = y;
+                } else if (!pt_eq(x, y, lx, ly)) {
+                    internal++;
+                }
+                lx = x;
+                ly = y;
+                cnt++;
+            });
+        }
+        double px, py;
+        prev_point_scan(cnt > 0, lx, ly, carry_x, carry_y, lane, px, py);
+        const int32_t first_add = (cnt > 0 && !pt_eq(fx, fy, px, py)) ? 1 : 0;
+        int rt = 0;
+        warp_excl_sum(cnt, lane, rt);
+        emit_tot += rt;
+        int at = 0;
+        warp_excl_sum(internal + first_add, lane, at);
+        add_tot += at;
+        // carry: the last point emitted so far
+        const unsigned m = __ballot_sync(0xffffffffu, cnt > 0);
+        if (m) {
+            const int src = 31 - __clz(m);
+            carry_x = __shfl_sync(0xffffffffu, lx, src);
+            carry_y = __shfl_sync(0xffffffffu, ly, src);
+        }
+    }
+    // final lineTo(d)
+    emit_tot += 1;
+    add_tot += pt_eq(p[4], p[5], carry_x, carry_y) ? 0 : 1;
+    n_emit = emit_tot;
+    n_added = add_tot;
+    return __all_sync(0xffffffffu, ok);
+}
+
+__global__ void __launch_bounds__(32 * kFlattenWarps) k_node_count_w(const z2d_node *__restrict__ nodes,
+                                                                     const int32_t *__restrict__ node_fill,
+                                                                     const FillCmd *__restrict__ fills,
+                                                                     NodeInfo *__restrict__ info, int32_t n_nodes,
+                                                                     int32_t *__restrict__ status) {
+    __shared__ WarpFrontier frs[kFlattenWarps];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    WarpFrontier &fr = frs[w];
+    for (int32_t i = blockIdx.x * kFlattenWarps + w; i < n_nodes; i += gridDim.x * kFlattenWarps) {
+        const z2d_node nd = nodes[i];
+        NodeInfo inf{};
+        const int32_t f = node_fill[i];
+        const FillCmd &F = fills[f];
+        const bool first_of_fill = (i == F.node_off);
+        if (nd.tag == Z2D_LINE_TO || nd.tag == Z2D_CURVE_TO) {
+            const z2d_node pv = first_of_fill ? nd : nodes[i - 1];
+            const bool static_start =
+                !first_of_fill && (pv.tag == Z2D_MOVE_TO || pv.tag == Z2D_LINE_TO || pv.tag == Z2D_CURVE_TO);
+            if (!static_start) {
+                inf.n_emit = -1;  // resolved by k_fill_scan
+            } else {
+                const double sx = pv.tag == Z2D_CURVE_TO ? pv.p[4] : pv.p[0];
+                const double sy = pv.tag == Z2D_CURVE_TO ? pv.p[5] : pv.p[1];
+                if (nd.tag == Z2D_LINE_TO) {
+                    inf.n_emit = 1;
+                    inf.n_added = pt_eq(sx, sy, nd.p[0], nd.p[1]) ? 0 : 1;
+                } else if (!curve_count_warp(sx, sy, nd.p, F.tol, fr, lane, inf.n_emit, inf.n_added)) {
+                    if (lane == 0) atomicExch(status, Z2D_ERR_INVALID_STATE);
+                }
+            }
+        }
+        if (lane == 0) info[i] = inf;
+        __syncwarp();
+    }
+}
+
+__global__ void __launch_bounds__(32 * kFlattenWarps) k_node_emit_w(const z2d_node *__restrict__ nodes,
+                                                                    const int32_t *__restrict__ node_fill,
+                                                                    const FillCmd *__restrict__ fills,
+                                                                    const NodeInfo *__restrict__ info,
+                                                                    FillState *__restrict__ st, DEdge *__restrict__ edges,
+                                                                    int32_t n_nodes) {
+    __shared__ WarpFrontier frs[kFlattenWarps];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    WarpFrontier &fr = frs[w];
+    for (int32_t i = blockIdx.x * kFlattenWarps + w; i < n_nodes; i += gridDim.x * kFlattenWarps) {
+        const NodeInfo inf = info[i];
+        if (inf.n_emit <= 0) continue;  // uniform across the warp
+        const z2d_node nd = nodes[i];
+        const int32_t f = node_fill[i];
+        const FillCmd &F = fills[f];
+        DEdge *out = edges + st[f].edge_base + inf.edge_off;
+        double et = 0, eb = 0, el = 0, er = 0;
+        bool any = false;
+        const bool straight = nd.tag == Z2D_CURVE_TO && pt_eq(inf.sx, inf.sy, nd.p[0], nd.p[1]) && pt_eq(nd.p[2], nd.p[3], nd.p[4], nd.p[5]);
+        if (nd.tag != Z2D_CURVE_TO || straight) {
+            if (lane == 0) {
+                if (nd.tag == Z2D_LINE_TO) add_edge(F, out, inf.sx, inf.sy, nd.p[0], nd.p[1], et, eb, el, er, any);
+                else if (nd.tag == Z2D_CLOSE_PATH) add_edge(F, out, inf.sx, inf.sy, inf.ex, inf.ey, et, eb, el, er, any);
+                else add_edge(F, out, inf.sx, inf.sy, nd.p[4], nd.p[5], et, eb, el, er, any);
+            }
+        } else {
+            const double tol2 = F.tol * F.tol;
+            const int n = frontier_expand(inf.sx, inf.sy, nd.p, tol2, fr, lane);
+            int32_t base_off = 0;
+            double carry_x = inf.sx, carry_y = inf.sy;
+            for (int base = 0; base < n; base += 32) {
+                const int i2 = base + lane;
+                int32_t cnt = 0;
+                double lx = 0, ly = 0;
+                if (i2 < n)
+                    walk_item(fr.k[i2], fr.leaf[i2] != 0, inf.sx, inf.sy, tol2, [&](double x, double y) {
+                        cnt++;
+                        lx = x;
+                        ly = y;
+                    });
+                double px, py;
+                prev_point_scan(cnt > 0, lx, ly, carry_x, carry_y, lane, px, py);
+                int tot = 0;
+                const int off = base_off + warp_excl_sum(cnt, lane, tot);
+                if (i2 < n && cnt > 0) {
+                    int32_t k = off;
+                    walk_item(fr.k[i2], fr.leaf[i2] != 0, inf.sx, inf.sy, tol2, [&](double x, double y) {
+                        if (k < inf.n_emit) add_edge(F, out + k, px, py, x, y, et, eb, el, er, any);
+                        k++;
+                        px = x;
+                        py = y;
+                    });
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, cnt > 0);
+                if (m) {
+                    const int src = 31 - __clz(m);
+                    carry_x = __shfl_sync(0xffffffffu, lx, src);
+                    carry_y = __shfl_sync(0xffffffffu, ly, src);
+                }
+                base_off += tot;
+            }
+            if (lane == 0 && base_off < inf.n_emit)  // final lineTo(d)
+                add_edge(F, out + base_off, carry_x, carry_y, nd.p[4], nd.p[5], et, eb, el, er, any);
+        }
+        // warp reduction of the extents of this node's edges
+        const unsigned anym = __ballot_sync(0xffffffffu, any);
+        if (anym) {
+            double mt = any ? et : 1e300, mb = any ? eb : -1e300, ml = any ? el : 1e300, mr = any ? er : -1e300;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                mt = fmin(mt, __shfl_xor_sync(0xffffffffu, mt, o));
+                mb = fmax(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+                ml = fmin(ml, __shfl_xor_sync(0xffffffffu, ml, o));
+                mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+            }
+            if (lane == 0) {
+                FillState &S = st[f];
+                atomicMin(&S.ext[0], dkey(mt));
+                atomicMax(&S.ext[1], dkey(mb));
+                atomicMin(&S.ext[2], dkey(ml));
+                atomicMax(&S.ext[3], dkey(mr));
+                atomicOr(&S.has_edges, 1);
+            }
+        }
+        __syncwarp();
+    }
+}
+
 __device__ __forceinline__ int32_t clampi(int32_t v, int32_t lo, int32_t hi) { return max(lo, min(v, hi)); }
 
 __global__ void k_fill_setup(const FillCmd *__restrict__ fills, FillState *__restrict__ st, int32_t n_fills,
@@ -411,6 +725,8 @@ __global__ void k_fill_setup(const FillCmd *__restrict__ fills, FillState *__res
     atomicMin(&counters[CNT_BAND_MIN], S.band0);
     atomicMax(&counters[CNT_BAND_MAX], S.band1);
     const int32_t cx0 = bounded ? S.start_x : 0, cx1 = bounded ? S.end_x : sw;
+    S.cull_x0 = cx0;
+    S.cull_x1 = cx1;
     atomicMin(&counters[CNT_TCOL_MIN], cx0 / kTileCols);
     atomicMax(&counters[CNT_TCOL_MAX], (max(cx1, cx0 + 1) - 1) / kTileCols);
     st[f] = S;
@@ -467,20 +783,23 @@ __global__ void k_edge_fill(const FillState *__restrict__ st, int32_t n_fills, i
 // Ordered list of the fills touching each band (call order preserved by a
 // block-wide stream compaction).
 __global__ void __launch_bounds__(256) k_band_lists(const FillState *__restrict__ st, int32_t n_fills, int32_t band_lo,
-                                                    int32_t *__restrict__ band_count, int32_t *__restrict__ band_fills) {
+                                                    int32_t *__restrict__ band_count, int4 *__restrict__ band_fills) {
     const int32_t b = band_lo + blockIdx.x;
     __shared__ int32_t warp_tot[8];
     __shared__ int32_t base;
     if (threadIdx.x == 0) base = 0;
     __syncthreads();
     const int32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int32_t *out = band_fills + (size_t)blockIdx.x * n_fills;
+    int4 *out = band_fills + (size_t)blockIdx.x * n_fills;
     for (int32_t f0 = 0; f0 < n_fills; f0 += blockDim.x) {
         const int32_t f = f0 + threadIdx.x;
         bool hit = false;
+        int4 ent = make_int4(f, 0, 0, 0);
         if (f < n_fills) {
             const FillState &S = st[f];
             hit = S.active && b >= S.band0 && b <= S.band1;
+            ent.y = S.cull_x0;
+            ent.z = S.cull_x1;
         }
         const unsigned m = __ballot_sync(0xffffffffu, hit);
         if (lane == 0) warp_tot[wid] = __popc(m);
@@ -490,7 +809,7 @@ __global__ void __launch_bounds__(256) k_band_lists(const FillState *__restrict_
             if (w < wid) before += warp_tot[w];
             total += warp_tot[w];
         }
-        if (hit) out[base + before + __popc(m & ((1u << lane) - 1u))] = f;
+        if (hit) out[base + before + __popc(m & ((1u << lane) - 1u))] = ent;
         __syncthreads();
         if (threadIdx.x == 0) base += total;
         __syncthreads();
@@ -641,7 +960,9 @@ __device__ __forceinline__ I16 normalize(I16 v, int fmt) { return to_i16(from_i1
 // One pixel of a fill with coverage `cov` (1..full) on destination lanes d,
 // following compositeOpaque / compositeOpacity (raster/shared.zig:9-104),
 // Surface.paintStride and Surface.compositeStride (surface.zig:537-581).
-__device__ __forceinline__ I16 apply_fill(const FillCmd &F, int fmt, int32_t x, int32_t y, int cov, int full, I16 d) {
+// Out of line: every operator, precision and source kind is reachable from
+// here, which keeps the rasteriser's hot loop small.
+static __device__ __noinline__ I16 apply_fill(const FillCmd &F, int fmt, int32_t x, int32_t y, int cov, int full, I16 d) {
     if (F.op == Z2D_OP_CLEAR) return normalize(I16{0, 0, 0, 0}, fmt);
     if (cov >= full) {
         if (F.reduces) return to_i16(F.px_paint);
@@ -679,7 +1000,7 @@ struct RasterArgs {
     const int32_t *bins;
     const int32_t *bin_off;
     const int32_t *band_count;
-    const int32_t *band_fills;
+    const int4 *band_fills;  // {fill, cull_x0, cull_x1, 0} per band, in call order
     const uint8_t *masks;
     int32_t n_fills, band_lo, tcol_lo;
 };
@@ -688,7 +1009,8 @@ struct RasterArgs {
 // two biased 16-bit counters per word (bias 0x8000; a fill with at most
 // kMaxBandEdges edges in a band can never carry a counter across halves).
 constexpr int kWordsPerSubRow = 512;
-constexpr int kWarpWords = 4 * kWordsPerSubRow;
+constexpr int kTouchOff = 4 * kWordsPerSubRow;  // then 4 x 32 words: pairs touched per (sample row, lane)
+constexpr int kWarpWords = kTouchOff + 4 * 32;
 constexpr uint32_t kBias2 = 0x80008000u;
 
 // Sample column c of a sub-scanline belongs to lane c / per (per = sample
@@ -724,7 +1046,7 @@ __device__ __forceinline__ void store_raw(const DevSurface &s, size_t i, uint32_
 // of its row's 4 (or 1) sample rows from the fill's band edges, prefix-scans
 // them across the warp, turns the inside bits into coverage and composites
 // its 8 pixels, which stay in registers from the first fill to the last.
-__global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A) {
+__global__ void __launch_bounds__(kRasterThreads, 5) k_raster(const RasterArgs A) {
     extern __shared__ uint32_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t *words = smem + warp * kWarpWords;
@@ -734,10 +1056,10 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
     const int32_t x0 = (A.tcol_lo + blockIdx.x) * kTileCols, y = b * kTileRows + warp;
     const int32_t W = A.dst.w, H = A.dst.h, fmt = A.dst.fmt;
     if (y >= H) return;
-    const int32_t *list = A.band_fills + (size_t)blockIdx.y * A.n_fills;
+    const int4 *list = A.band_fills + (size_t)blockIdx.y * A.n_fills;
     const int32_t px0 = x0 + lane * 8;  // this lane's first pixel
 
-    for (int i = lane; i < kWarpWords; i += 32) words[i] = kBias2;
+    for (int i = lane; i < kWarpWords; i += 32) words[i] = i < kTouchOff ? kBias2 : 0u;
     uint32_t raw[8];
     uint32_t touched = 0;
 #pragma unroll
@@ -745,7 +1067,9 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
     __syncwarp();
 
     for (int32_t k = 0; k < cnt; k++) {
-        const int32_t f = list[k];
+        const int4 ent = list[k];
+        if (ent.z <= x0 || ent.y >= x0 + kTileCols) continue;  // the fill misses this tile
+        const int32_t f = ent.x;
         const FillState &S = A.st[f];
         const FillCmd &F = A.fills[f];
         const int32_t op = F.op;
@@ -771,16 +1095,21 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
                     if (c < ncol) {
                         const uint32_t inc = (c & 1) ? ((uint32_t)e.dir << 16) : (uint32_t)e.dir;
                         atomicAdd(&words[(sr - sub0) * kWordsPerSubRow + pair_index(c, per)], inc);
+                        atomicOr(&words[kTouchOff + (sr - sub0) * 32 + c / per], 1u << ((c % per) >> 1));
                     }
                 }
             }
             __syncwarp();
             const int pairs = per >> 1;
+            const bool eo = F.rule == Z2D_FILL_EVEN_ODD;
+            (void)pairs;
             for (int s = 0; s < sc; s++) {
                 uint32_t *row = words + s * kWordsPerSubRow;
+                uint32_t *touch = words + kTouchOff + s * 32 + lane;
+                const uint32_t touched = *touch;  // pairs of this lane that received crossings
                 int32_t tot = 0;
-                for (int kk = 0; kk < pairs; kk++) {
-                    const uint32_t v = row[(kk << 5) | lane];
+                for (uint32_t m = touched; m; m &= m - 1) {
+                    const uint32_t v = row[((__ffs(m) - 1) << 5) | lane];
                     tot += (int32_t)(v & 0xFFFFu) + (int32_t)(v >> 16) - 0x10000;
                 }
                 int32_t incl = tot;
@@ -790,18 +1119,27 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
                     if (lane >= o) incl += t;
                 }
                 int32_t wnd = incl - tot;
+                // Between touched pairs the winding is constant, so inside
+                // bits are filled a range at a time.
+                bool in = eo ? ((wnd & 1) != 0) : (wnd != 0);
                 uint32_t bits = 0;
-                for (int kk = 0; kk < pairs; kk++) {
+                int pos = 0;
+                for (uint32_t m = touched; m; m &= m - 1) {
+                    const int kk = __ffs(m) - 1, s0 = 2 * kk;
                     const int idx = (kk << 5) | lane;
                     const uint32_t v = row[idx];
                     row[idx] = kBias2;
+                    if (in) bits |= ((1u << s0) - 1u) & ~((1u << pos) - 1u);
                     wnd += (int32_t)(v & 0xFFFFu) - 0x8000;
-                    bool in = (F.rule == Z2D_FILL_EVEN_ODD) ? ((wnd & 1) != 0) : (wnd != 0);
-                    bits |= (uint32_t)in << (2 * kk);
+                    in = eo ? ((wnd & 1) != 0) : (wnd != 0);
+                    bits |= (uint32_t)in << s0;
                     wnd += (int32_t)(v >> 16) - 0x8000;
-                    in = (F.rule == Z2D_FILL_EVEN_ODD) ? ((wnd & 1) != 0) : (wnd != 0);
-                    bits |= (uint32_t)in << (2 * kk + 1);
+                    in = eo ? ((wnd & 1) != 0) : (wnd != 0);
+                    bits |= (uint32_t)in << (s0 + 1);
+                    pos = s0 + 2;
                 }
+                if (in && pos < 32) bits |= ~((1u << pos) - 1u);
+                *touch = 0u;
                 if (direct) {
 #pragma unroll
                     for (int q = 0; q < 8; q++) cov[q] += (bits >> q) & 1u;
@@ -812,7 +1150,28 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
             }
             __syncwarp();
         }
+        if (F.fast_kind == FAST_PIXEL_SRC_OVER && !exact && bounded) {
+            // Pixel source, integer src_over: the compositeOpaque /
+            // compositeOpacity paths reduce to src_over(d, pixel) at full
+            // coverage and src_over(d, dst_in(pixel, opacity)) otherwise.
+            const I16 px = F.src.pix;
+            const int full = direct ? 1 : 16;
 #pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int32_t x = px0 + q;
+                const int c = cov[q];
+                if (c == 0 || x >= W || x < S.start_x || (!direct && x >= S.end_x) || !in_rows) continue;
+                I16 s = px;
+                if (c < full) {
+                    const uint32_t op8 = (uint32_t)(c * 16 - 1);
+                    s = I16{(px.r * op8) / 255u, (px.g * op8) / 255u, (px.b * op8) / 255u, (px.a * op8) / 255u};
+                }
+                raw[q] = i16_to_raw(int_op(Z2D_OP_SRC_OVER, raw_to_i16(raw[q], fmt), s), fmt);
+                touched |= 1u << q;
+            }
+            continue;
+        }
+#pragma unroll 1
         for (int q = 0; q < 8; q++) {
             const int32_t x = px0 + q;
             if (x >= W) continue;
@@ -884,7 +1243,9 @@ int run_fills(Ctx &c, const DevSurface &sfc, const z2d_node *nodes, int32_t n_no
     Z2D_CUDA(cudaMemsetAsync(d_st, 0, sizeof(FillState) * (size_t)n_fills, c.stream));
 
     // ---- flatten
-    k_node_count<<<grid_for(n_nodes, 128), 128, 0, c.stream>>>(d_nodes, d_nfill, d_fills, d_info, n_nodes, d_cnt + CNT_STATUS);
+    const unsigned flat_blocks = (unsigned)std::min<long long>(grid_for(n_nodes, kFlattenWarps), (long long)c.sm_count * 64);
+    k_node_count_w<<<flat_blocks, 32 * kFlattenWarps, 0, c.stream>>>(d_nodes, d_nfill, d_fills, d_info, n_nodes,
+                                                                    d_cnt + CNT_STATUS);
     k_fill_scan<<<grid_for(n_fills, 64), 64, 0, c.stream>>>(d_nodes, d_fills, d_info, d_st, n_fills, d_cnt, d_cnt + CNT_STATUS);
     c.launches += 2;
     if (c.readback.ensure(sizeof(int32_t) * CNT_COUNT)) return Z2D_ERR_OUT_OF_MEMORY;
@@ -902,7 +1263,8 @@ int run_fills(Ctx &c, const DevSurface &sfc, const z2d_node *nodes, int32_t n_no
     DEdge *d_edges = c.edges.as<DEdge>();
     int32_t *d_edge_fill = reinterpret_cast<int32_t *>(d_edges + std::max(n_edges, 1));
     // extents start at +inf/-inf keys: min slots 0xFF.., max slots 0
-    k_node_emit<<<grid_for(n_nodes, 128), 128, 0, c.stream>>>(d_nodes, d_nfill, d_fills, d_info, d_st, d_edges, n_nodes);
+    k_node_emit_w<<<flat_blocks, 32 * kFlattenWarps, 0, c.stream>>>(d_nodes, d_nfill, d_fills, d_info, d_st, d_edges,
+                                                                   n_nodes);
     k_edge_fill<<<n_fills, 128, 0, c.stream>>>(d_st, n_fills, d_edge_fill);
     k_fill_setup<<<grid_for(n_fills, 64), 64, 0, c.stream>>>(d_fills, d_st, n_fills, sfc.w, sfc.h, d_cnt);
     c.launches += 3;
@@ -949,9 +1311,10 @@ int run_fills(Ctx &c, const DevSurface &sfc, const z2d_node *nodes, int32_t n_no
 
     // ---- ordered fill lists per band
     const int32_t n_bands = band_hi - band_lo + 1;
-    if (c.band_fills.ensure(sizeof(int32_t) * ((size_t)n_bands * (size_t)n_fills + (size_t)n_bands))) return Z2D_ERR_OUT_OF_MEMORY;
+    const size_t count_bytes = ((sizeof(int32_t) * (size_t)n_bands) + 15) & ~(size_t)15;
+    if (c.band_fills.ensure(count_bytes + sizeof(int4) * (size_t)n_bands * (size_t)n_fills)) return Z2D_ERR_OUT_OF_MEMORY;
     int32_t *d_band_count = c.band_fills.as<int32_t>();
-    int32_t *d_band_fills = d_band_count + n_bands;
+    int4 *d_band_fills = reinterpret_cast<int4 *>(c.band_fills.as<uint8_t>() + count_bytes);
     k_band_lists<<<n_bands, 256, 0, c.stream>>>(d_st, n_fills, band_lo, d_band_count, d_band_fills);
     c.launches++;
 

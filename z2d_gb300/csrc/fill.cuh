@@ -21,6 +21,8 @@ struct FillCmd {
     int32_t precision;  // after the float upgrade of multisample.zig:36 / direct.zig:25
     int32_t pattern_kind;
     int32_t reduces;    // pixel pattern whose operator reduces to the source (shared.zig:111-117)
+    int32_t fast_kind;  // FAST_* specialisation the rasteriser may use
+    int32_t _pad0;
     double tol;         // max(tolerance, 0.001) (painter.zig:103)
     double scale;       // 4 for multisample, 1 for none (painter.zig:93-97)
     DevSrc src;         // the pattern as a compositor source
@@ -48,6 +50,11 @@ struct DEdge {
 };
 
 enum : int32_t {
+    FAST_NONE = 0,
+    FAST_PIXEL_SRC_OVER = 1,  // pixel pattern, integer precision, src_over
+};
+
+enum : int32_t {
     FILL_OPEN_CHAIN = 1,  // an open 2-point subpath: rows may be unbalanced
     FILL_EXACT = 2,       // rasterised by k_exact
 };
@@ -62,6 +69,7 @@ struct FillState {
     int32_t fb_base;            // first (fill, band) slot
     int32_t mask_w, mask_x0;
     long long mask_base;        // exact-path action mask offset (bytes)
+    int32_t cull_x0, cull_x1;   // columns a tile must overlap to be affected
 };
 
 // counters (int32 slots; the mask byte count is a 64-bit pair)
