@@ -254,4 +254,23 @@ Z2D_API int z2dgpu_composite(z2dgpu_ctx *ctx, z2d_surface *dst, int32_t dst_x,
                              int32_t dst_y, int32_t n_ops,
                              const z2d_operation *ops, int32_t precision);
 
+/* z2dgpu_composite for callers that may not allocate device memory, such as
+ * a plugin whose host owns every device allocation, or a per-frame loop in
+ * which a cudaMalloc/cudaFree would synchronise the whole device.  It has no
+ * counterpart in z2d.  It takes no context: the work is queued on `stream`
+ * (a cudaStream_t; NULL = the default stream) of `device`, and the call
+ * returns after launch.  `dst` and every surface param must be in device
+ * memory (packed formats padded to a multiple of 4 bytes).  Gradient
+ * descriptors go to a fixed device array inside the library, so one call
+ * takes at most 4 gradient params (pattern gradients and gradient-sourced
+ * dithers); more are rejected with Z2D_ERR_INVALID_ARGUMENT.  Each call
+ * writes every descriptor it reads, so nothing has to start at zero.  The
+ * array is shared by all calls on a device: calls whose GPU work overlaps
+ * (other streams, other threads) race on it, while calls queued in order on
+ * one stream do not.  The first call on a device looks up the array's
+ * device address, so make that call before any stream capture. */
+Z2D_API int z2dgpu_composite_noalloc(int device, void *stream, z2d_surface *dst,
+                                     int32_t dst_x, int32_t dst_y, int32_t n_ops,
+                                     const z2d_operation *ops, int32_t precision);
+
 #endif /* Z2DGPU_H */

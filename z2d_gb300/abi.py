@@ -121,4 +121,5 @@ EXPORTED_SYMBOLS = [
     "z2dgpu_ctx_synchronize", "z2dgpu_ctx_launch_count", "z2dgpu_ctx_set_timing",
     "z2dgpu_ctx_kernel_ms", "z2dgpu_surface_bytes",
     "z2dgpu_fill", "z2dgpu_fill_batch", "z2dgpu_composite",
+    "z2dgpu_composite_noalloc",
 ]

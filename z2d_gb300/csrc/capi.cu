@@ -4,8 +4,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdarg>
+#include <cstdio>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -14,11 +17,19 @@
 
 namespace z2dg {
 
-static thread_local std::string g_err;
+// Message of the last failing call on this thread.  A fixed buffer, so that
+// reporting an error never allocates.
+static thread_local char g_err[256];
 
-void set_error(const std::string &msg) { g_err = msg; }
+void set_error(const char *msg) { set_errorf("%s", msg); }
+void set_errorf(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
 int cuda_fail(cudaError_t e, const char *what) {
-    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    set_errorf("%s: %s", what, cudaGetErrorString(e));
     return Z2D_ERR_CUDA;
 }
 
@@ -31,7 +42,7 @@ int DevBuf::ensure(size_t bytes) {
     cap = 0;
     if (cudaMalloc(&ptr, n) != cudaSuccess) {
         ptr = nullptr;
-        set_error("device allocation of " + std::to_string(n) + " bytes failed");
+        set_errorf("device allocation of %zu bytes failed", n);
         return 1;
     }
     cap = n;
@@ -99,7 +110,7 @@ void Ctx::timer_collect(Timer &t) {
 int make_dev_gradient(const z2d_gradient &g, DevGradient &out) {
     memset(&out, 0, sizeof(out));
     if (g.n_stops < 0 || g.n_stops > kMaxStops || (g.n_stops > 0 && !g.stops)) {
-        set_error("gradient: 0.." + std::to_string(kMaxStops) + " stops supported");
+        set_errorf("gradient: 0..%d stops supported", kMaxStops);
         return Z2D_ERR_INVALID_ARGUMENT;
     }
     if (g.type < Z2D_GRADIENT_LINEAR || g.type > Z2D_GRADIENT_CONIC || g.method < 0 || g.method > Z2D_INTERP_HSL_DECREASING) {
@@ -121,12 +132,13 @@ int make_dev_gradient(const z2d_gradient &g, DevGradient &out) {
         float off;
         int idx;
     };
-    std::vector<S> order((size_t)g.n_stops);
-    for (int i = 0; i < g.n_stops; i++) order[i] = S{std::fmax(0.0f, std::fmin(g.stops[i].offset, 1.0f)), i};
-    std::stable_sort(order.begin(), order.end(), [](const S &a, const S &b) {
-        if (a.off == b.off) return a.idx < b.idx;
-        return a.off < b.off;
-    });
+    S order[kMaxStops];  // stable insertion sort on the stack (no allocation)
+    for (int i = 0; i < g.n_stops; i++) {
+        const S v{std::fmax(0.0f, std::fmin(g.stops[i].offset, 1.0f)), i};
+        int j = i;
+        for (; j > 0 && v.off < order[j - 1].off; j--) order[j] = order[j - 1];
+        order[j] = v;
+    }
     for (int i = 0; i < g.n_stops; i++) {
         out.offsets[i] = order[i].off;
         out.colors[i] = g.stops[order[i].idx].color;
@@ -443,6 +455,92 @@ static int do_fill_batch(Ctx &c, z2d_surface *surface, const z2d_node *nodes, si
     return stage_out(c, *surface, ds);
 }
 
+// SurfaceCompositor.run's precision upgrade and bounds
+// (src/compositor.zig:310-387): fills the geometry of J and sets `empty`
+// when nothing is drawn.
+static int composite_region(const z2d_surface *dst, int32_t dst_x, int32_t dst_y, int32_t n_ops,
+                            const z2d_operation *ops, int32_t precision, CompJob &J, bool &empty) {
+    memset(&J, 0, sizeof(J));
+    empty = true;
+    if (n_ops == 0) return Z2D_OK;
+    if (dst_x >= dst->width || dst_y >= dst->height) return Z2D_OK;
+    int prec = precision;
+    for (int k = 0; k < n_ops; k++) {
+        if (ops[k].op < 0 || ops[k].op >= Z2D_OP_COUNT) return Z2D_ERR_INVALID_ARGUMENT;
+        if (requires_float(ops[k].op)) prec = Z2D_PRECISION_FLOAT;
+    }
+    int32_t sw, sh;
+    const z2d_param &s0 = ops[0].src;
+    if (s0.kind == Z2D_PARAM_NONE) return Z2D_OK;
+    if (s0.kind == Z2D_PARAM_SURFACE) {
+        const int rc = check_surface(s0.surface);
+        if (rc) return rc;
+        sw = s0.surface->width;
+        sh = s0.surface->height;
+    } else {
+        if (dst_x != 0 || dst_y != 0) return Z2D_OK;
+        sw = dst->width;
+        sh = dst->height;
+    }
+    const int32_t ssx = dst_x < 0 ? -dst_x : 0, ssy = dst_y < 0 ? -dst_y : 0;
+    const int32_t width = (sw + dst_x > dst->width) ? dst->width - dst_x : sw;
+    const int32_t height = (sh + dst_y > dst->height) ? dst->height - dst_y : sh;
+    if (ssx >= width || ssy >= height) return Z2D_OK;
+    J.n_ops = n_ops;
+    J.precision = prec;
+    J.dst_x = dst_x;
+    J.dst_y = dst_y;
+    J.dsx = ssx + dst_x;
+    J.y0 = ssy + dst_y;
+    J.y1 = std::max(ssy, height) + dst_y;
+    J.line_w = std::max(0, width - ssx);
+    empty = false;
+    return Z2D_OK;
+}
+
+// z2d leaves surface params smaller than the batch region undefined; the
+// GPU path rejects them instead of reading out of bounds.
+static int check_param_bounds(const CompJob &J) {
+    for (int k = 0; k < J.n_ops; k++) {
+        const DevSrc &ds = J.ops[k].dst, &ss = J.ops[k].src;
+        if (ds.kind == SRC_SURFACE && ((int64_t)ds.sfc.w < (int64_t)J.dsx + J.line_w || ds.sfc.h < J.y1)) {
+            set_error("composite: destination surface param smaller than the region");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+        if (ss.kind == SRC_SURFACE &&
+            ((int64_t)ss.sfc.w < (int64_t)(J.dsx - J.dst_x) + J.line_w || ss.sfc.h < J.y1 - J.dst_y)) {
+            set_error("composite: source surface param smaller than the region");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+    }
+    return Z2D_OK;
+}
+
+// ------------------------------------------------- allocation-free compositing
+// Scratch of z2dgpu_composite_noalloc: the gradient descriptors its
+// operations read.  File-scope device memory, so no call allocates; every
+// GPU that loads the library holds it until the process exits.
+constexpr int kNoAllocGradients = 4;
+static __device__ __align__(256) DevGradient g_noalloc_gradients[kNoAllocGradients];
+
+// Device address of g_noalloc_gradients per device, looked up once per
+// device (the name is only a host-side stand-in in host code).
+constexpr int kMaxDevices = 64;
+static DevGradient *g_noalloc_addr[kMaxDevices];
+static std::mutex g_noalloc_mu;
+
+static int noalloc_scratch(int device, DevGradient **out) {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[device]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_gradients);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_gradients)");
+        g_noalloc_addr[device] = static_cast<DevGradient *>(p);
+    }
+    *out = g_noalloc_addr[device];
+    return Z2D_OK;
+}
+
 }  // namespace z2dg
 
 using namespace z2dg;
@@ -453,7 +551,7 @@ extern "C" {
 
 Z2D_API const char *z2dgpu_version(void) { return "z2dgpu 0.1.0 (sm_103a)"; }
 
-Z2D_API const char *z2dgpu_last_error(void) { return g_err.c_str(); }
+Z2D_API const char *z2dgpu_last_error(void) { return g_err; }
 
 Z2D_API int z2dgpu_ctx_create(z2dgpu_ctx **out, int device, void *stream) {
     if (!out) return Z2D_ERR_INVALID_ARGUMENT;
@@ -557,41 +655,10 @@ Z2D_API int z2dgpu_composite(z2dgpu_ctx *c, z2d_surface *dst, int32_t dst_x, int
     }
     if (precision != Z2D_PRECISION_INTEGER && precision != Z2D_PRECISION_FLOAT) return Z2D_ERR_INVALID_ARGUMENT;
     Z2D_CUDA(cudaSetDevice(c->device));
-    // SurfaceCompositor.run bounds (src/compositor.zig:310-387)
-    if (n_ops == 0) return Z2D_OK;
-    if (dst_x >= dst->width || dst_y >= dst->height) return Z2D_OK;
-    int prec = precision;
-    for (int k = 0; k < n_ops; k++) {
-        if (ops[k].op < 0 || ops[k].op >= Z2D_OP_COUNT) return Z2D_ERR_INVALID_ARGUMENT;
-        if (requires_float(ops[k].op)) prec = Z2D_PRECISION_FLOAT;
-    }
-    int32_t sw, sh;
-    const z2d_param &s0 = ops[0].src;
-    if (s0.kind == Z2D_PARAM_NONE) return Z2D_OK;
-    if (s0.kind == Z2D_PARAM_SURFACE) {
-        rc = check_surface(s0.surface);
-        if (rc) return rc;
-        sw = s0.surface->width;
-        sh = s0.surface->height;
-    } else {
-        if (dst_x != 0 || dst_y != 0) return Z2D_OK;
-        sw = dst->width;
-        sh = dst->height;
-    }
-    const int32_t ssx = dst_x < 0 ? -dst_x : 0, ssy = dst_y < 0 ? -dst_y : 0;
-    const int32_t width = (sw + dst_x > dst->width) ? dst->width - dst_x : sw;
-    const int32_t height = (sh + dst_y > dst->height) ? dst->height - dst_y : sh;
-    if (ssx >= width || ssy >= height) return Z2D_OK;
     CompJob J;
-    memset(&J, 0, sizeof(J));
-    J.n_ops = n_ops;
-    J.precision = prec;
-    J.dst_x = dst_x;
-    J.dst_y = dst_y;
-    J.dsx = ssx + dst_x;
-    J.y0 = ssy + dst_y;
-    J.y1 = std::max(ssy, height) + dst_y;
-    J.line_w = std::max(0, width - ssx);
+    bool empty = false;
+    rc = composite_region(dst, dst_x, dst_y, n_ops, ops, precision, J, empty);
+    if (rc || empty) return rc;
     // stage destination and surface params
     DevBuf *stage[3] = {&c->surface, &c->surface2, &c->surface3};
     int used = 0;
@@ -649,22 +716,106 @@ Z2D_API int z2dgpu_composite(z2dgpu_ctx *c, z2d_surface *dst, int32_t dst_x, int
         Z2D_CUDA(cudaMemcpyAsync(c->params.ptr, c->staging.ptr, bytes, cudaMemcpyHostToDevice, c->stream));
         for (size_t i = 0; i < grad_users.size(); i++) grad_users[i]->grad = c->params.as<DevGradient>() + i;
     }
-    // z2d leaves surface params smaller than the batch region undefined; the
-    // GPU path rejects them instead of reading out of bounds
-    for (int k = 0; k < n_ops; k++) {
-        const DevSrc &ds = J.ops[k].dst, &ss = J.ops[k].src;
-        if (ds.kind == SRC_SURFACE && ((int64_t)ds.sfc.w < (int64_t)J.dsx + J.line_w || ds.sfc.h < J.y1)) {
-            set_error("composite: destination surface param smaller than the region");
-            return Z2D_ERR_INVALID_ARGUMENT;
-        }
-        if (ss.kind == SRC_SURFACE && ((int64_t)ss.sfc.w < (int64_t)(J.dsx - dst_x) + J.line_w || ss.sfc.h < J.y1 - dst_y)) {
-            set_error("composite: source surface param smaller than the region");
-            return Z2D_ERR_INVALID_ARGUMENT;
-        }
-    }
+    rc = check_param_bounds(J);
+    if (rc) return rc;
     rc = launch_composite(*c, J);
     if (rc) return rc;
     return stage_out(*c, *dst, J.dst);
+}
+
+// SurfaceCompositor.run for callers that are not allowed to allocate device
+// memory: the operations' gradient descriptors go to the file-scope
+// g_noalloc_gradients instead of context scratch, and no context (with its
+// own allocations) is involved.  The first call on a device looks up the
+// scratch's device address; that call should come before any stream
+// capture.  Calls share the scratch: calls that overlap on the GPU race.
+Z2D_API int z2dgpu_composite_noalloc(int device, void *stream, z2d_surface *dst, int32_t dst_x, int32_t dst_y,
+                                     int32_t n_ops, const z2d_operation *ops, int32_t precision) {
+    int rc = check_surface(dst);
+    if (rc) return rc;
+    if (dst->location != Z2D_MEM_DEVICE) {
+        set_error("composite_noalloc: surfaces must be in device memory (host surfaces need staging buffers)");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    if (n_ops < 0 || n_ops > 2 || (n_ops > 0 && !ops)) {
+        set_error("composite_noalloc: 0..2 operations supported");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    if (precision != Z2D_PRECISION_INTEGER && precision != Z2D_PRECISION_FLOAT) return Z2D_ERR_INVALID_ARGUMENT;
+    if (device < 0 || device >= kMaxDevices) {
+        set_errorf("composite_noalloc: device index must be in [0, %d)", kMaxDevices);
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    int prev = -1;
+    Z2D_CUDA(cudaGetDevice(&prev));
+    if (prev != device) Z2D_CUDA(cudaSetDevice(device));
+    struct Restore {
+        int prev, dev;
+        ~Restore() {
+            if (prev != dev) cudaSetDevice(prev);
+        }
+    } restore{prev, device};
+
+    DevGradient *scratch = nullptr;
+    rc = noalloc_scratch(device, &scratch);
+    if (rc) return rc;
+    CompJob J;
+    bool empty = false;
+    rc = composite_region(dst, dst_x, dst_y, n_ops, ops, precision, J, empty);
+    if (rc || empty) return rc;
+    J.dst = DevSurface{reinterpret_cast<uint8_t *>(dst->data), dst->format, dst->width, dst->height};
+    DevGradient grads[kNoAllocGradients];
+    int n_grads = 0;
+    for (int k = 0; k < n_ops; k++) {
+        J.ops[k].op = ops[k].op;
+        const z2d_param *prm[2] = {&ops[k].dst, &ops[k].src};
+        DevSrc *outs[2] = {&J.ops[k].dst, &J.ops[k].src};
+        for (int j = 0; j < 2; j++) {
+            const z2d_param &p = *prm[j];
+            DevSrc &o = *outs[j];
+            memset(&o, 0, sizeof(o));
+            if (p.kind == Z2D_PARAM_NONE) {
+                o.kind = SRC_NONE;
+            } else if (p.kind == Z2D_PARAM_SURFACE) {
+                rc = check_surface(p.surface);
+                if (rc) return rc;
+                if (p.surface->location != Z2D_MEM_DEVICE) {
+                    set_error("composite_noalloc: surface params must be in device memory");
+                    return Z2D_ERR_INVALID_ARGUMENT;
+                }
+                o.kind = SRC_SURFACE;
+                o.sfc = DevSurface{reinterpret_cast<uint8_t *>(p.surface->data), p.surface->format, p.surface->width,
+                                   p.surface->height};
+            } else if (p.kind == Z2D_PARAM_PIXEL || p.kind == Z2D_PARAM_GRADIENT || p.kind == Z2D_PARAM_DITHER) {
+                bool needs_grad = false;
+                DevGradient g;
+                rc = make_dev_src_from_pattern(p.kind, p.pattern, o, needs_grad, g);
+                if (rc) return rc;
+                if (needs_grad) {
+                    if (n_grads == kNoAllocGradients) {
+                        set_errorf("composite_noalloc: at most %d gradient parameters per call", kNoAllocGradients);
+                        return Z2D_ERR_INVALID_ARGUMENT;
+                    }
+                    grads[n_grads] = g;
+                    o.grad = scratch + n_grads;
+                    n_grads++;
+                }
+            } else {
+                return Z2D_ERR_INVALID_ARGUMENT;
+            }
+        }
+    }
+    rc = check_param_bounds(J);
+    if (rc) return rc;
+    Ctx c;
+    c.device = device;
+    c.stream = reinterpret_cast<cudaStream_t>(stream);
+    Z2D_CUDA(cudaDeviceGetAttribute(&c.sm_count, cudaDevAttrMultiProcessorCount, device));
+    // Every descriptor a kernel reads is written here, so nothing in the
+    // scratch has to start at zero.  The copy reads `grads` before it returns.
+    if (n_grads > 0)
+        Z2D_CUDA(cudaMemcpyAsync(scratch, grads, sizeof(DevGradient) * (size_t)n_grads, cudaMemcpyHostToDevice, c.stream));
+    return launch_composite(c, J);
 }
 
 }  // extern "C"

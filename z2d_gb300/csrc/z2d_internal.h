@@ -14,7 +14,8 @@
 namespace z2dg {
 
 // thread-local message behind z2dgpu_last_error()
-void set_error(const std::string &msg);
+void set_error(const char *msg);
+void set_errorf(const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what);
 
 #define Z2D_CUDA(call)                                        \
