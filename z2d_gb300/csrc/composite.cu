@@ -159,77 +159,6 @@ __global__ void __launch_bounds__(256) k_composite_region(const CompJob J, size_
     }
 }
 
-// ------------------------------------------------------------ mask batch
-// The batch [dst_in(dst = pixel, src = alpha8 mask), op] over a whole
-// surface in integer precision -- the shape z2d's supersample rasteriser
-// and mask compositing use (supersample.zig:171-184).  Per pixel:
-// r = pixel * mask / 255 (IntegerOps.dstIn), d = op(d, r).  Each thread
-// iteration moves 16 bytes of destination and the matching mask bytes with
-// vector loads; the operator switch is warp-uniform and inlined.
-template <int FMT>
-__global__ void __launch_bounds__(256) k_mask_batch(uint8_t *__restrict__ dst, const uint8_t *__restrict__ mask,
-                                                    size_t n_chunks, I16 spx, int op) {
-    constexpr int PX = FMT <= Z2D_FORMAT_RGBA ? 4 : 16;  // pixels per 16-byte chunk
-    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n_chunks; c += (size_t)gridDim.x * blockDim.x) {
-        const uint4 v = reinterpret_cast<const uint4 *>(dst)[c];
-        uint32_t w[4] = {v.x, v.y, v.z, v.w};
-        if constexpr (FMT <= Z2D_FORMAT_RGBA) {
-            const uint32_t m4 = __ldcs(reinterpret_cast<const uint32_t *>(mask) + c);
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const uint32_t m = (m4 >> (8 * j)) & 0xFFu;
-                const I16 r{(spx.r * m) / 255u, (spx.g * m) / 255u, (spx.b * m) / 255u, (spx.a * m) / 255u};
-                w[j] = i16_to_word(int_op(op, word_to_i16(w[j], FMT), r), FMT);
-            }
-        } else {
-            const uint4 mv = __ldcs(reinterpret_cast<const uint4 *>(mask) + c);
-            const uint32_t mw[4] = {mv.x, mv.y, mv.z, mv.w};
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                uint32_t out = 0;
-#pragma unroll
-                for (int b = 0; b < 4; b++) {
-                    const uint32_t m = (mw[j] >> (8 * b)) & 0xFFu;
-                    const uint32_t da = (w[j] >> (8 * b)) & 0xFFu;
-                    const I16 r{0u, 0u, 0u, (spx.a * m) / 255u};
-                    out |= (int_op(op, I16{0u, 0u, 0u, da}, r).a & 0xFFu) << (8 * b);
-                }
-                w[j] = out;
-            }
-        }
-        reinterpret_cast<uint4 *>(dst)[c] = make_uint4(w[0], w[1], w[2], w[3]);
-        (void)PX;
-    }
-}
-
-// Returns true and launches when J is a whole-surface mask batch.
-static bool try_mask_batch(Ctx &c, const CompJob &J, bool flat) {
-    if (!flat || J.precision != Z2D_PRECISION_INTEGER || J.n_ops != 2) return false;
-    const CompOp &o0 = J.ops[0], &o1 = J.ops[1];
-    if (o0.op != Z2D_OP_DST_IN || o0.dst.kind != SRC_PIXEL || o0.src.kind != SRC_SURFACE) return false;
-    if (o0.src.sfc.fmt != Z2D_FORMAT_ALPHA8 || o0.src.sfc.w != J.dst.w || o0.src.sfc.h < J.dst.h) return false;
-    if (o1.dst.kind != SRC_NONE || o1.src.kind != SRC_NONE || J.dst.fmt > Z2D_FORMAT_ALPHA8) return false;
-    if ((reinterpret_cast<uintptr_t>(o0.src.sfc.data) & 15) != 0) return false;
-    const size_t px = (size_t)J.dst.w * J.dst.h;
-    const int per = J.dst.fmt <= Z2D_FORMAT_RGBA ? 4 : 16;
-    if (px % per != 0) return false;
-    const size_t n_chunks = px / per;
-    const int threads = 256;
-    size_t blocks = (n_chunks + threads - 1) / threads;
-    const size_t cap = (size_t)c.sm_count * 8;
-    if (blocks > cap) blocks = cap;
-    const I16 s = o0.dst.pix;
-    switch (J.dst.fmt) {
-        case Z2D_FORMAT_ARGB: k_mask_batch<Z2D_FORMAT_ARGB><<<(unsigned)blocks, threads, 0, c.stream>>>(J.dst.data, o0.src.sfc.data, n_chunks, s, o1.op); break;
-        case Z2D_FORMAT_XRGB: k_mask_batch<Z2D_FORMAT_XRGB><<<(unsigned)blocks, threads, 0, c.stream>>>(J.dst.data, o0.src.sfc.data, n_chunks, s, o1.op); break;
-        case Z2D_FORMAT_RGB: k_mask_batch<Z2D_FORMAT_RGB><<<(unsigned)blocks, threads, 0, c.stream>>>(J.dst.data, o0.src.sfc.data, n_chunks, s, o1.op); break;
-        case Z2D_FORMAT_RGBA: k_mask_batch<Z2D_FORMAT_RGBA><<<(unsigned)blocks, threads, 0, c.stream>>>(J.dst.data, o0.src.sfc.data, n_chunks, s, o1.op); break;
-        default: k_mask_batch<Z2D_FORMAT_ALPHA8><<<(unsigned)blocks, threads, 0, c.stream>>>(J.dst.data, o0.src.sfc.data, n_chunks, s, o1.op); break;
-    }
-    c.launches++;
-    return true;
-}
-
 template <int FMT, int PREC>
 static void launch_one(Ctx &c, const CompJob &J, bool flat) {
     const int threads = 256;

@@ -286,6 +286,7 @@ __device__ __forceinline__ void add_edge(const FillCmd &F, DEdge *out, double x0
         e.top = 0;
         e.x_start = 0;
         e.x_inc = 0;
+        e.fxs = e.fxi = e.ftp = 0.0f;
         e.dir = 0;
         e.rt = 1;
         e.rb = 0;  // horizontal: never active
@@ -293,6 +294,9 @@ __device__ __forceinline__ void add_edge(const FillCmd &F, DEdge *out, double x0
         return;
     }
     e.rt = (int32_t)round(e.top);
+    e.fxs = (float)e.x_start;
+    e.fxi = (float)e.x_inc;
+    e.ftp = (float)e.top;
     const double bot = ay < by ? by : ay;
     const double l = ax < bx ? ax : bx, r = ax < bx ? bx : ax;
     if (!any) {
@@ -1066,129 +1070,158 @@ __global__ void __launch_bounds__(kRasterThreads, 5) k_raster(const RasterArgs A
     for (int q = 0; q < 8; q++) raw[q] = (px0 + q < W) ? load_raw(A.dst, (size_t)W * y + px0 + q) : 0u;
     __syncwarp();
 
-    for (int32_t k = 0; k < cnt; k++) {
-        const int4 ent = list[k];
-        if (ent.z <= x0 || ent.y >= x0 + kTileCols) continue;  // the fill misses this tile
-        const int32_t f = ent.x;
-        const FillState &S = A.st[f];
-        const FillCmd &F = A.fills[f];
-        const int32_t op = F.op;
-        const bool bounded = is_bounded(op);
-        if (bounded && (S.end_x <= x0 || S.start_x >= x0 + kTileCols)) continue;
-        const bool direct = F.aa == Z2D_AA_NONE;
-        const bool exact = (S.flags & FILL_EXACT) != 0;
-        const bool in_rows = y >= S.start_y && y <= S.end_y;
-        if (!in_rows && bounded) continue;
-        const int32_t sc = direct ? 1 : 4, per = 8 * sc;
-        int cov[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        if (!exact && in_rows) {
-            const int32_t sub0 = y * sc, col0 = x0 * sc, ncol = kTileCols * sc;
-            const int32_t fb = S.fb_base + (b - S.band0);
-            const int32_t e0 = A.bin_off[fb], e1 = A.bin_off[fb + 1];
-            for (int32_t ei = e0 + lane; ei < e1; ei += 32) {
-                const DEdge e = A.edges[A.bins[ei]];
-                const int32_t lo = max(e.rt, sub0), hi = min(e.rb, sub0 + sc);
-                for (int32_t sr = lo; sr < hi; sr++) {
-                    const int32_t X = (int32_t)round(e.x_start + (e.x_inc * (((double)sr + 0.5) - e.top)));
-                    int32_t c = X - col0;
-                    if (c < 0) c = 0;
-                    if (c < ncol) {
-                        const uint32_t inc = (c & 1) ? ((uint32_t)e.dir << 16) : (uint32_t)e.dir;
-                        atomicAdd(&words[(sr - sub0) * kWordsPerSubRow + pair_index(c, per)], inc);
-                        atomicOr(&words[kTouchOff + (sr - sub0) * 32 + c / per], 1u << ((c % per) >> 1));
+    // The band's fill list is read 32 entries at a time, one per lane; the
+    // fills that overlap this tile are then walked in order from a ballot.
+    for (int32_t k0 = 0; k0 < cnt; k0 += 32) {
+        int4 ent = make_int4(0, 0, 0, 0);
+        const bool valid = k0 + lane < cnt;
+        if (valid) ent = list[k0 + lane];
+        uint32_t hits = __ballot_sync(0xffffffffu, valid && ent.z > x0 && ent.y < x0 + kTileCols);
+        while (hits) {
+            const int32_t f = __shfl_sync(0xffffffffu, ent.x, __ffs(hits) - 1);
+            hits &= hits - 1;
+            const FillState &S = A.st[f];
+            const FillCmd &F = A.fills[f];
+            const int32_t op = F.op;
+            const bool bounded = is_bounded(op);
+            if (bounded && (S.end_x <= x0 || S.start_x >= x0 + kTileCols)) continue;
+            const bool direct = F.aa == Z2D_AA_NONE;
+            const bool exact = (S.flags & FILL_EXACT) != 0;
+            const bool in_rows = y >= S.start_y && y <= S.end_y;
+            if (!in_rows && bounded) continue;
+            const int32_t sc = direct ? 1 : 4, per = 8 * sc;
+            int cov[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            if (!exact && in_rows) {
+                const int32_t sub0 = y * sc, col0 = x0 * sc, ncol = kTileCols * sc;
+                const int32_t fb = S.fb_base + (b - S.band0);
+                const int32_t e0 = A.bin_off[fb], e1 = A.bin_off[fb + 1];
+                // sample rows stay below 2^22, where sr + 0.5 is exact in f32
+                const bool f32_ok = sub0 < (1 << 22);
+                const float fsub = (float)sub0 + 0.5f;
+                for (int32_t ei = e0 + lane; ei < e1; ei += 32) {
+                    const int32_t id = A.bins[ei];
+                    const float4 ef = __ldg(reinterpret_cast<const float4 *>(A.edges + id));
+                    const int2 er = __ldg(reinterpret_cast<const int2 *>(&A.edges[id].rt));
+                    const int32_t dir = __float_as_int(ef.w);
+                    const int32_t lo = max(er.x, sub0), hi = min(er.y, sub0 + sc);
+                    for (int32_t sr = lo; sr < hi; sr++) {
+                        int32_t X;
+                        if (!(f32_ok && crossing_f32(ef.x, ef.y, ef.z, fsub + (float)(sr - sub0), X))) {
+                            const DEdge &e = A.edges[id];
+                            X = (int32_t)round(e.x_start + (e.x_inc * (((double)sr + 0.5) - e.top)));
+                        }
+                        int32_t c = X - col0;
+                        if (c < 0) c = 0;
+                        if (c < ncol) {
+                            const uint32_t inc = (c & 1) ? ((uint32_t)dir << 16) : (uint32_t)dir;
+                            atomicAdd(&words[(sr - sub0) * kWordsPerSubRow + pair_index(c, per)], inc);
+                            atomicOr(&words[kTouchOff + (sr - sub0) * 32 + c / per], 1u << ((c % per) >> 1));
+                        }
                     }
                 }
+                __syncwarp();
+                const int pairs = per >> 1;
+                const bool eo = F.rule == Z2D_FILL_EVEN_ODD;
+                (void)pairs;
+                for (int s = 0; s < sc; s++) {
+                    uint32_t *row = words + s * kWordsPerSubRow;
+                    uint32_t *touch = words + kTouchOff + s * 32 + lane;
+                    const uint32_t touched = *touch;  // pairs of this lane that received crossings
+                    int32_t tot = 0;
+                    for (uint32_t m = touched; m; m &= m - 1) {
+                        const uint32_t v = row[((__ffs(m) - 1) << 5) | lane];
+                        tot += (int32_t)(v & 0xFFFFu) + (int32_t)(v >> 16) - 0x10000;
+                    }
+                    int32_t incl = tot;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                        if (lane >= o) incl += t;
+                    }
+                    int32_t wnd = incl - tot;
+                    // Between touched pairs the winding is constant, so inside
+                    // bits are filled a range at a time.
+                    bool in = eo ? ((wnd & 1) != 0) : (wnd != 0);
+                    uint32_t bits = 0;
+                    int pos = 0;
+                    for (uint32_t m = touched; m; m &= m - 1) {
+                        const int kk = __ffs(m) - 1, s0 = 2 * kk;
+                        const int idx = (kk << 5) | lane;
+                        const uint32_t v = row[idx];
+                        row[idx] = kBias2;
+                        if (in) bits |= ((1u << s0) - 1u) & ~((1u << pos) - 1u);
+                        wnd += (int32_t)(v & 0xFFFFu) - 0x8000;
+                        in = eo ? ((wnd & 1) != 0) : (wnd != 0);
+                        bits |= (uint32_t)in << s0;
+                        wnd += (int32_t)(v >> 16) - 0x8000;
+                        in = eo ? ((wnd & 1) != 0) : (wnd != 0);
+                        bits |= (uint32_t)in << (s0 + 1);
+                        pos = s0 + 2;
+                    }
+                    if (in && pos < 32) bits |= ~((1u << pos) - 1u);
+                    *touch = 0u;
+                    if (direct) {
+#pragma unroll
+                        for (int q = 0; q < 8; q++) cov[q] += (bits >> q) & 1u;
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < 8; q++) cov[q] += __popc((bits >> (4 * q)) & 0xFu);
+                    }
+                }
+                __syncwarp();
             }
-            __syncwarp();
-            const int pairs = per >> 1;
-            const bool eo = F.rule == Z2D_FILL_EVEN_ODD;
-            (void)pairs;
-            for (int s = 0; s < sc; s++) {
-                uint32_t *row = words + s * kWordsPerSubRow;
-                uint32_t *touch = words + kTouchOff + s * 32 + lane;
-                const uint32_t touched = *touch;  // pairs of this lane that received crossings
-                int32_t tot = 0;
-                for (uint32_t m = touched; m; m &= m - 1) {
-                    const uint32_t v = row[((__ffs(m) - 1) << 5) | lane];
-                    tot += (int32_t)(v & 0xFFFFu) + (int32_t)(v >> 16) - 0x10000;
-                }
-                int32_t incl = tot;
+            if (F.fast_kind == FAST_PIXEL_SRC_OVER && !exact && bounded) {
+                // Pixel source, integer src_over: the compositeOpaque /
+                // compositeOpacity paths reduce to src_over(d, pixel) at full
+                // coverage and src_over(d, dst_in(pixel, opacity)) otherwise.
+                const I16 px = F.src.pix;
+                const int full = direct ? 1 : 16;
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += t;
+                for (int q = 0; q < 8; q++) {
+                    const int32_t x = px0 + q;
+                    const int c = cov[q];
+                    if (c == 0 || x >= W || x < S.start_x || (!direct && x >= S.end_x) || !in_rows) continue;
+                    I16 s = px;
+                    if (c < full) {
+                        const uint32_t op8 = (uint32_t)(c * 16 - 1);
+                        s = I16{(px.r * op8) / 255u, (px.g * op8) / 255u, (px.b * op8) / 255u, (px.a * op8) / 255u};
+                    }
+                    raw[q] = i16_to_raw(int_op(Z2D_OP_SRC_OVER, raw_to_i16(raw[q], fmt), s), fmt);
+                    touched |= 1u << q;
                 }
-                int32_t wnd = incl - tot;
-                // Between touched pairs the winding is constant, so inside
-                // bits are filled a range at a time.
-                bool in = eo ? ((wnd & 1) != 0) : (wnd != 0);
-                uint32_t bits = 0;
-                int pos = 0;
-                for (uint32_t m = touched; m; m &= m - 1) {
-                    const int kk = __ffs(m) - 1, s0 = 2 * kk;
-                    const int idx = (kk << 5) | lane;
-                    const uint32_t v = row[idx];
-                    row[idx] = kBias2;
-                    if (in) bits |= ((1u << s0) - 1u) & ~((1u << pos) - 1u);
-                    wnd += (int32_t)(v & 0xFFFFu) - 0x8000;
-                    in = eo ? ((wnd & 1) != 0) : (wnd != 0);
-                    bits |= (uint32_t)in << s0;
-                    wnd += (int32_t)(v >> 16) - 0x8000;
-                    in = eo ? ((wnd & 1) != 0) : (wnd != 0);
-                    bits |= (uint32_t)in << (s0 + 1);
-                    pos = s0 + 2;
-                }
-                if (in && pos < 32) bits |= ~((1u << pos) - 1u);
-                *touch = 0u;
-                if (direct) {
-#pragma unroll
-                    for (int q = 0; q < 8; q++) cov[q] += (bits >> q) & 1u;
-                } else {
-#pragma unroll
-                    for (int q = 0; q < 8; q++) cov[q] += __popc((bits >> (4 * q)) & 0xFu);
-                }
+                continue;
             }
-            __syncwarp();
-        }
-        if (F.fast_kind == FAST_PIXEL_SRC_OVER && !exact && bounded) {
-            // Pixel source, integer src_over: the compositeOpaque /
-            // compositeOpacity paths reduce to src_over(d, pixel) at full
-            // coverage and src_over(d, dst_in(pixel, opacity)) otherwise.
-            const I16 px = F.src.pix;
-            const int full = direct ? 1 : 16;
-#pragma unroll
+#pragma unroll 1
             for (int q = 0; q < 8; q++) {
                 const int32_t x = px0 + q;
-                const int c = cov[q];
-                if (c == 0 || x >= W || x < S.start_x || (!direct && x >= S.end_x) || !in_rows) continue;
-                I16 s = px;
-                if (c < full) {
-                    const uint32_t op8 = (uint32_t)(c * 16 - 1);
-                    s = I16{(px.r * op8) / 255u, (px.g * op8) / 255u, (px.b * op8) / 255u, (px.a * op8) / 255u};
+                if (x >= W) continue;
+                // raw[] and cov[] are read and written with constant indices
+                // only, so they stay in registers
+                int c = cov[0];
+                uint32_t rq = raw[0];
+#pragma unroll
+                for (int j = 1; j < 8; j++)
+                    if (q == j) {
+                        c = cov[j];
+                        rq = raw[j];
+                    }
+                bool clear = false;
+                if (exact && in_rows && x >= S.mask_x0 && x < S.mask_x0 + S.mask_w) {
+                    const uint8_t m = A.masks[S.mask_base + (long long)(y - S.start_y) * S.mask_w + (x - S.mask_x0)];
+                    c = m & 0x1F;
+                    if (direct) clear = (m & kMaskClear) != 0;
                 }
-                raw[q] = i16_to_raw(int_op(Z2D_OP_SRC_OVER, raw_to_i16(raw[q], fmt), s), fmt);
+                if (!direct && !bounded) clear = msaa_unbounded_clear(S, x, y, W);
+                const bool in_box = in_rows && (direct ? true : (x >= S.start_x && x < S.end_x));
+                if (!clear && !(in_box && c > 0)) continue;
+                I16 d = clear ? normalize(I16{0, 0, 0, 0}, fmt) : raw_to_i16(rq, fmt);
+                if (in_box && c > 0) d = apply_fill(F, fmt, x, y, c, direct ? 1 : 16, d);
+                rq = i16_to_raw(d, fmt);
+#pragma unroll
+                for (int j = 0; j < 8; j++)
+                    if (q == j) raw[j] = rq;
                 touched |= 1u << q;
             }
-            continue;
-        }
-#pragma unroll 1
-        for (int q = 0; q < 8; q++) {
-            const int32_t x = px0 + q;
-            if (x >= W) continue;
-            int c = cov[q];
-            bool clear = false;
-            if (exact && in_rows && x >= S.mask_x0 && x < S.mask_x0 + S.mask_w) {
-                const uint8_t m = A.masks[S.mask_base + (long long)(y - S.start_y) * S.mask_w + (x - S.mask_x0)];
-                c = m & 0x1F;
-                if (direct) clear = (m & kMaskClear) != 0;
-            }
-            if (!direct && !bounded) clear = msaa_unbounded_clear(S, x, y, W);
-            const bool in_box = in_rows && (direct ? true : (x >= S.start_x && x < S.end_x));
-            if (!clear && !(in_box && c > 0)) continue;
-            I16 d = clear ? normalize(I16{0, 0, 0, 0}, fmt) : raw_to_i16(raw[q], fmt);
-            if (in_box && c > 0) d = apply_fill(F, fmt, x, y, c, direct ? 1 : 16, d);
-            raw[q] = i16_to_raw(d, fmt);
-            touched |= 1u << q;
         }
     }
 #pragma unroll

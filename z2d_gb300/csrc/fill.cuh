@@ -42,12 +42,42 @@ struct NodeInfo {
 
 // Polygon.Edge plus its rounded active range: the edge is active on sample
 // row y exactly when rt <= y < rb (top < y+0.5 <= bottom, Polygon.zig:284-285).
+// fxs/fxi/ftp are x_start/x_inc/top rounded to f32 for crossing_f32; the
+// first 16 bytes load as one vector.
 struct DEdge {
-    double x_start, x_inc, top;
-    int32_t rt, rb;
+    float fxs, fxi, ftp;
     int32_t dir;  // -1 down, +1 up, 0 horizontal (dropped)
-    int32_t _pad;
+    int32_t rt, rb;
+    double x_start, x_inc, top;
 };
+
+static_assert(sizeof(DEdge) == 48, "DEdge layout: 16-byte f32 block, ranges, f64 fields");
+
+// The crossing of an edge with sample row sr is
+//   X = round(x_start + x_inc * ((sr + 0.5) - top))      (Polygon.zig:272-276)
+// in f64, rounded half away from zero.  crossing_f32 evaluates the same
+// expression in f32 from the f32-rounded inputs (s = sr + 0.5, exact) and
+// bounds its distance from the f64 value.  With u = 2^-24 and every f32
+// operation correctly rounded, to first order
+//   |fv - v| <= u * (|fv| + |fxs| + |fp| + |fxi| * (|ftp| + 2|ft|))
+// (input roundings of x_start, x_inc and top, then one rounding per
+// operation); the f64 evaluation's own error is ~2^-29 of that.  The bound
+// used is 1.25x the first-order one.  When fv is farther than the bound
+// from the nearest half-integer, the f64 value lies on the same side of it
+// and rounds to the same integer; otherwise the caller evaluates in f64.
+// Returns false when the f32 result does not decide X.
+Z2D_HD bool crossing_f32(float fxs, float fxi, float ftp, float s, int32_t &X) {
+    const float ft = s - ftp;
+    const float fp = fxi * ft;
+    const float fv = fxs + fp;
+    const float bound =
+        (fabsf(fv) + fabsf(fxs) + fabsf(fp) + fabsf(fxi) * (fabsf(ftp) + 2.0f * fabsf(ft))) * 7.450580596923828e-8f;
+    const float fl = floorf(fv);
+    const float h = fl + 0.5f;
+    if (!(fabsf(fv - h) > bound) || !(fabsf(fv) < 4194304.0f)) return false;  // NaN/inf fail here too
+    X = (int32_t)fl + (fv > h ? 1 : 0);
+    return true;
+}
 
 enum : int32_t {
     FAST_NONE = 0,

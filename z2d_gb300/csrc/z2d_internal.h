@@ -103,5 +103,8 @@ struct CompJob {
     CompOp ops[2];
 };
 int launch_composite(Ctx &c, const CompJob &job);
+// Launches the whole-surface mask batch [dst_in(pixel, alpha8 mask), op]
+// when J has that shape (composite_mask.cu); returns false otherwise.
+bool try_mask_batch(Ctx &c, const CompJob &J, bool flat);
 
 }  // namespace z2dg
