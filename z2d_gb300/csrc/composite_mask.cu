@@ -10,7 +10,9 @@
 // matching mask loads) before it computes, so that enough bytes are in
 // flight per SM to cover DRAM latency; the operator is a template
 // parameter, so every kernel holds one operator's arithmetic and nothing
-// else.  The grid is sized from the kernel's occupancy on this device.
+// else; dst_in(pixel, mask) comes from a 256-entry shared-memory table, and
+// src_over on the 4-byte formats works on two channels per 32-bit word.
+// The grid is sized from the kernel's occupancy on this device.
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -27,6 +29,17 @@ template <int FMT, int OP>
 __global__ void __launch_bounds__(kMaskThreads) k_mask_op(uint8_t *__restrict__ dst, const uint8_t *__restrict__ mask,
                                                          size_t n_chunks, I16 spx) {
     constexpr bool WIDE = FMT <= Z2D_FORMAT_RGBA;  // 4 px per chunk; else 16 one-byte px
+    constexpr bool HAS_ALPHA = FMT == Z2D_FORMAT_RGBA || FMT == Z2D_FORMAT_ARGB;
+    constexpr int ORDER = (FMT == Z2D_FORMAT_ARGB || FMT == Z2D_FORMAT_XRGB) ? Z2D_FORMAT_ARGB : Z2D_FORMAT_RGBA;
+    // r = dst_in(pixel, mask) depends on the mask byte only: one table entry
+    // per mask value, in the destination's byte order (alpha in byte 3).
+    __shared__ uint32_t lut[256];
+    for (int i = threadIdx.x; i < 256; i += kMaskThreads) {
+        const uint32_t m = (uint32_t)i;
+        const I16 r{(spx.r * m) / 255u, (spx.g * m) / 255u, (spx.b * m) / 255u, (spx.a * m) / 255u};
+        lut[i] = WIDE ? i16_to_word(r, ORDER) : r.a;
+    }
+    __syncthreads();
     const size_t tile = (size_t)kMaskThreads * kMaskUnroll;
     for (size_t base = (size_t)blockIdx.x * tile + threadIdx.x; base < n_chunks; base += (size_t)gridDim.x * tile) {
         uint4 v[kMaskUnroll];
@@ -47,12 +60,15 @@ __global__ void __launch_bounds__(kMaskThreads) k_mask_op(uint8_t *__restrict__ 
             const size_t c = base + (size_t)k * kMaskThreads;
             if (c >= n_chunks) break;
             uint32_t w[4] = {v[k].x, v[k].y, v[k].z, v[k].w};
-            if constexpr (WIDE) {
+            if constexpr (WIDE && OP == Z2D_OP_SRC_OVER) {
+                const uint32_t m4 = mv[k].x;
+#pragma unroll
+                for (int j = 0; j < 4; j++) w[j] = word_src_over(w[j], lut[(m4 >> (8 * j)) & 0xFFu], HAS_ALPHA);
+            } else if constexpr (WIDE) {
                 const uint32_t m4 = mv[k].x;
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
-                    const uint32_t m = (m4 >> (8 * j)) & 0xFFu;
-                    const I16 r{(spx.r * m) / 255u, (spx.g * m) / 255u, (spx.b * m) / 255u, (spx.a * m) / 255u};
+                    const I16 r = word_to_i16(lut[(m4 >> (8 * j)) & 0xFFu], ORDER);
                     w[j] = i16_to_word(int_op(OP, word_to_i16(w[j], FMT), r), FMT);
                 }
             } else {
@@ -62,9 +78,8 @@ __global__ void __launch_bounds__(kMaskThreads) k_mask_op(uint8_t *__restrict__ 
                     uint32_t out = 0;
 #pragma unroll
                     for (int b = 0; b < 4; b++) {
-                        const uint32_t m = (mw[j] >> (8 * b)) & 0xFFu;
                         const uint32_t da = (w[j] >> (8 * b)) & 0xFFu;
-                        const I16 r{0u, 0u, 0u, (spx.a * m) / 255u};
+                        const I16 r{0u, 0u, 0u, lut[(mw[j] >> (8 * b)) & 0xFFu]};
                         out |= (int_op(OP, I16{0u, 0u, 0u, da}, r).a & 0xFFu) << (8 * b);
                     }
                     w[j] = out;

@@ -1090,7 +1090,9 @@ __global__ void __launch_bounds__(kRasterThreads, 5) k_raster(const RasterArgs A
             const bool in_rows = y >= S.start_y && y <= S.end_y;
             if (!in_rows && bounded) continue;
             const int32_t sc = direct ? 1 : 4, per = 8 * sc;
-            int cov[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            // coverage of pixel q (0..16) is byte q / 2 of cov_ev (q even)
+            // or cov_od (q odd)
+            uint32_t cov_ev = 0, cov_od = 0;
             if (!exact && in_rows) {
                 const int32_t sub0 = y * sc, col0 = x0 * sc, ncol = kTileCols * sc;
                 const int32_t fb = S.fb_base + (b - S.band0);
@@ -1160,12 +1162,17 @@ __global__ void __launch_bounds__(kRasterThreads, 5) k_raster(const RasterArgs A
                     }
                     if (in && pos < 32) bits |= ~((1u << pos) - 1u);
                     *touch = 0u;
-                    if (direct) {
+                    if (direct) {  // one sample row: bit q is pixel q's sample
 #pragma unroll
-                        for (int q = 0; q < 8; q++) cov[q] += (bits >> q) & 1u;
-                    } else {
-#pragma unroll
-                        for (int q = 0; q < 8; q++) cov[q] += __popc((bits >> (4 * q)) & 0xFu);
+                        for (int q = 0; q < 8; q += 2) {
+                            cov_ev |= ((bits >> q) & 1u) << (4 * q);
+                            cov_od |= ((bits >> (q + 1)) & 1u) << (4 * q);
+                        }
+                    } else {  // nibble q holds pixel q's 4 samples of this row
+                        uint32_t n = bits - ((bits >> 1) & 0x55555555u);
+                        n = (n & 0x33333333u) + ((n >> 2) & 0x33333333u);
+                        cov_ev += n & 0x0F0F0F0Fu;
+                        cov_od += (n >> 4) & 0x0F0F0F0Fu;
                     }
                 }
                 __syncwarp();
@@ -1174,13 +1181,36 @@ __global__ void __launch_bounds__(kRasterThreads, 5) k_raster(const RasterArgs A
                 // Pixel source, integer src_over: the compositeOpaque /
                 // compositeOpacity paths reduce to src_over(d, pixel) at full
                 // coverage and src_over(d, dst_in(pixel, opacity)) otherwise.
+                // (A bounded fill outside its rows was skipped above.)
                 const I16 px = F.src.pix;
                 const int full = direct ? 1 : 16;
+                const int32_t xlo = S.start_x, xhi = direct ? W : min(S.end_x, W);
+                if (fmt <= Z2D_FORMAT_RGBA) {
+                    // Lane k holds the source word for coverage k: the pixel
+                    // at k = full, dst_in(pixel, k * 16 - 1) below it.
+                    I16 s = px;
+                    if (lane < full) {
+                        const uint32_t op8 = (uint32_t)max(lane * 16 - 1, 0);
+                        s = I16{(px.r * op8) / 255u, (px.g * op8) / 255u, (px.b * op8) / 255u, (px.a * op8) / 255u};
+                    }
+                    const uint32_t lut_w = i16_to_word(s, word_order(fmt));
+                    const bool has_alpha = fmt == Z2D_FORMAT_RGBA || fmt == Z2D_FORMAT_ARGB;
+#pragma unroll
+                    for (int q = 0; q < 8; q++) {
+                        const int c = (int)((((q & 1) ? cov_od : cov_ev) >> (8 * (q >> 1))) & 0xFFu);
+                        const uint32_t L = __shfl_sync(0xffffffffu, lut_w, c);
+                        const int32_t x = px0 + q;
+                        if (c == 0 || x < xlo || x >= xhi) continue;
+                        raw[q] = word_src_over(raw[q], L, has_alpha);
+                        touched |= 1u << q;
+                    }
+                    continue;
+                }
 #pragma unroll
                 for (int q = 0; q < 8; q++) {
                     const int32_t x = px0 + q;
-                    const int c = cov[q];
-                    if (c == 0 || x >= W || x < S.start_x || (!direct && x >= S.end_x) || !in_rows) continue;
+                    const int c = (int)((((q & 1) ? cov_od : cov_ev) >> (8 * (q >> 1))) & 0xFFu);
+                    if (c == 0 || x < xlo || x >= xhi) continue;
                     I16 s = px;
                     if (c < full) {
                         const uint32_t op8 = (uint32_t)(c * 16 - 1);
@@ -1195,16 +1225,13 @@ __global__ void __launch_bounds__(kRasterThreads, 5) k_raster(const RasterArgs A
             for (int q = 0; q < 8; q++) {
                 const int32_t x = px0 + q;
                 if (x >= W) continue;
-                // raw[] and cov[] are read and written with constant indices
-                // only, so they stay in registers
-                int c = cov[0];
+                // raw[] is read and written with constant indices only, so it
+                // stays in registers
+                int c = (int)((((q & 1) ? cov_od : cov_ev) >> (8 * (q >> 1))) & 0xFFu);
                 uint32_t rq = raw[0];
 #pragma unroll
                 for (int j = 1; j < 8; j++)
-                    if (q == j) {
-                        c = cov[j];
-                        rq = raw[j];
-                    }
+                    if (q == j) rq = raw[j];
                 bool clear = false;
                 if (exact && in_rows && x >= S.mask_x0 && x < S.mask_x0 + S.mask_w) {
                     const uint8_t m = A.masks[S.mask_base + (long long)(y - S.start_y) * S.mask_w + (x - S.mask_x0)];

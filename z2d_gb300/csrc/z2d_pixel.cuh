@@ -115,6 +115,36 @@ Z2D_HD uint32_t i16_to_word(I16 v, int fmt) {
 }
 Z2D_HD uint32_t px_to_word(Px p) { return i16_to_word(I16{p.r, p.g, p.b, p.a}, p.fmt); }
 
+// Byte order of a source word for word_src_over on a 4-byte format: the
+// colour bytes in the surface's order, alpha in byte 3.
+Z2D_HD int word_order(int fmt) {
+    return (fmt == Z2D_FORMAT_ARGB || fmt == Z2D_FORMAT_XRGB) ? Z2D_FORMAT_ARGB : Z2D_FORMAT_RGBA;
+}
+
+// floor(t / 255) in both 16-bit lanes of t, each lane at most 255 * 255:
+// on [0, 65025], floor(t / 255) == (t + floor(t / 256) + 1) >> 8, and no
+// lane carries into the other.
+Z2D_HD uint32_t div255x2(uint32_t t) {
+    return ((t + ((t >> 8) & 0x00FF00FFu) + 0x00010001u) >> 8) & 0x00FF00FFu;
+}
+
+// IntegerOps.srcOver (src/compositor.zig:1223-1230) of source word L over
+// destination word w of a 4-byte format, two channels per 32-bit operation:
+//   c = w16(s_c + d_c * (255 - s_a) / 255),  a = w16(s_a + d_a - s_a * d_a / 255)
+// stored as their low bytes.  L is in word_order(fmt) with the source alpha
+// in byte 3; without an alpha channel (XRGB, RGB) byte 3 is written as 0.
+Z2D_HD uint32_t word_src_over(uint32_t w, uint32_t L, bool has_alpha) {
+    const uint32_t ra = L >> 24, inv = 255u - ra;
+    const uint32_t e = div255x2((w & 0x00FF00FFu) * inv) + (L & 0x00FF00FFu);
+    const uint32_t o = div255x2(((w >> 8) & 0x00FF00FFu) * inv) + ((L >> 8) & 0x00FF00FFu);
+    uint32_t out = (e & 0x00FF00FFu) | ((o & 0xFFu) << 8);
+    if (has_alpha) {
+        const uint32_t da = w >> 24;
+        out |= ((ra + da - (ra * da) / 255u) & 0xFFu) << 24;
+    }
+    return out;
+}
+
 // Surface access by flat pixel index (w*y+x).  Packed formats are LSB
 // first (src/pixel.zig:664-677).
 struct DevSurface {
