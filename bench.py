@@ -47,6 +47,12 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
 CPU_SAMPLE_FILLS = 2000   # cpu_baseline sample: the whole workload (~10-20 s single-threaded)
 REF_STEP_FILLS = 400      # --impl reference: fills per timed step
 PLAIN_FILLS = 300         # per-call arm: fills drawn with one z2dgpu_fill each
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch,
+# from the ncu captures summarised under profiles/
+TRAFFIC = {
+    "k_raster": (214_508_288, "profiles/k_raster_rgba4096_2000paths.md"),
+    "k_mask_op": (544_317_696, "profiles/k_mask_op_rgba8192_src_over.md"),
+}
 
 
 def load_peaks():
@@ -405,7 +411,8 @@ def run_ours(args):
     clk = clocks.stop()  # sampled over the batched, e2e, plain and compositor timed regions
     comp_roof = {"bound": "hbm", "kernel": "k_mask_op<RGBA, src_over>", "achieved": comp["gbs_src_over"],
                  "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": comp["gbs_src_over"] / peaks["hbm_gbs"],
-                 "traffic": None, "peak_source": peak_kind}
+                 "traffic": TRAFFIC["k_mask_op"][0], "traffic_source": TRAFFIC["k_mask_op"][1],
+                 "alg_bytes_per_launch": comp["bytes_per_px"] * 8192 * 8192, "peak_source": peak_kind}
     cpu_v, cpu_dt = cpu_sample(bg, fills, px, CPU_SAMPLE_FILLS)
     line = {
         "metric": "Mpix/s fill+composite (src_over, 4096x4096 RGBA, 2000 random paths)",
@@ -420,7 +427,8 @@ def run_ours(args):
         "batched_over_plain": (mpix_step / (total_ms / args.steps / 1e3)) / (plain_mpix / (plain_ms / 1e3)),
         "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": "k_raster", "achieved": achieved, "peak": peaks["hbm_gbs"],
-                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": TRAFFIC["k_raster"][0],
+                     "traffic_source": TRAFFIC["k_raster"][1],
                      "peak_source": peak_kind, "alg_bytes_per_launch": alg_bytes,
                      "launch_ms": raster_ms_per},
         "cpu_baseline": {"value": cpu_v, "unit": "Mpix/s", "cores": 1, "kind": "port",

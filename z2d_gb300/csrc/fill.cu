@@ -30,6 +30,8 @@
 #include <cub/cub.cuh>
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "fill.cuh"
 
 namespace z2dg {
@@ -1050,7 +1052,7 @@ __device__ __forceinline__ void store_raw(const DevSurface &s, size_t i, uint32_
 // of its row's 4 (or 1) sample rows from the fill's band edges, prefix-scans
 // them across the warp, turns the inside bits into coverage and composites
 // its 8 pixels, which stay in registers from the first fill to the last.
-__global__ void __launch_bounds__(kRasterThreads, 5) k_raster(const RasterArgs A) {
+__global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A) {
     extern __shared__ uint32_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t *words = smem + warp * kWarpWords;
@@ -1403,10 +1405,13 @@ int run_fills(Ctx &c, const DevSurface &sfc, const z2d_node *nodes, int32_t n_no
     A.band_lo = band_lo;
     A.tcol_lo = tcol_lo;
     const size_t smem = sizeof(uint32_t) * kWarpWords * kTileRows;
-    static bool attr_set = false;
-    if (!attr_set) {
+    // function attributes are per device: set once on each
+    static std::atomic<uint64_t> attr_set{0};
+    const uint64_t dev_bit = 1ull << (c.device & 63);
+    if (!(attr_set.load(std::memory_order_relaxed) & dev_bit)) {
         Z2D_CUDA(cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr_set = true;
+        Z2D_CUDA(cudaFuncSetAttribute(k_raster, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        attr_set.fetch_or(dev_bit, std::memory_order_relaxed);
     }
     dim3 grid((unsigned)(tcol_hi - tcol_lo + 1), (unsigned)n_bands);
     cudaEvent_t t0 = c.timer_begin(c.t_raster);
