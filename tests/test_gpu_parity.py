@@ -38,7 +38,7 @@ def _cmp(a: Surface, b: Surface, tol: int = 0, what: str = ""):
     return ndiff
 
 
-@pytest.mark.parametrize("aa", ["none", "multisample_4x"])
+@pytest.mark.parametrize("aa", ["none", "multisample_4x", "supersample_4x"])
 @pytest.mark.parametrize("name", list(FILL_SCENES))
 def test_fill_scene(gpu, oracle, name, aa):
     _cmp(FILL_SCENES[name](gpu, aa), FILL_SCENES[name](oracle, aa), 0, name)

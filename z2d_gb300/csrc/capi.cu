@@ -373,16 +373,14 @@ static int prepare_fills(const z2d_surface &s, const z2d_node *nodes, size_t n_n
         int rc = check_fill(s, *cm.pattern, nd, cm.n_nodes, cm.opts);
         if (rc) return rc;
         if (cm.n_nodes == 0) continue;  // painter.fill returns early
+        // painter.fill's AA choice (painter.zig:86-97): alpha1 surfaces
+        // always draw without anti-aliasing; default is multisample
         const int aa = (s.format == Z2D_FORMAT_ALPHA1) ? Z2D_AA_NONE : cm.opts.anti_aliasing;
-        if (aa == Z2D_AA_SUPERSAMPLE_4X) {
-            set_error("supersample_4x is not implemented on the GPU path; use default/multisample_4x or none");
-            return Z2D_ERR_INVALID_ARGUMENT;
-        }
         FillCmd F;
         memset(&F, 0, sizeof(F));
         F.node_off = (int32_t)cm.node_offset;
         F.n_nodes = (int32_t)cm.n_nodes;
-        F.aa = aa == Z2D_AA_NONE ? Z2D_AA_NONE : Z2D_AA_MULTISAMPLE_4X;
+        F.aa = (aa == Z2D_AA_NONE || aa == Z2D_AA_SUPERSAMPLE_4X) ? aa : Z2D_AA_MULTISAMPLE_4X;
         F.rule = cm.opts.fill_rule;
         F.op = cm.opts.op;
         F.precision = requires_float(F.op) ? Z2D_PRECISION_FLOAT : cm.opts.precision;

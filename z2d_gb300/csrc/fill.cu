@@ -704,17 +704,51 @@ __global__ void k_fill_setup(const FillCmd *__restrict__ fills, FillState *__res
         S.start_x = clampi((int32_t)floor(el) - 1, 0, sw);
         S.end_x = clampi((int32_t)ceil(er) + 2, S.start_x, sw);
         if (!bounded) S.flags |= FILL_EXACT;
+    } else if (F.aa == Z2D_AA_SUPERSAMPLE_4X) {
+        // supersample.run (supersample.zig:41-84, 172-184): a 4x mask over
+        // [bx0, bx1] x [by0, by1] in sample units, downsampled 4x4 -> 1
+        // unless it is narrower or lower than 4 samples, then composited at
+        // (max(0, x0), max(0, y0)) and clipped to the surface by
+        // SurfaceCompositor.run (compositor.zig:313-374).  Downsampled mask
+        // pixel (i, j) averages the samples of surface pixel (cx + i, cy + j).
+        const int32_t x0 = bounded ? (int32_t)floor(el / 4.0) : 0;
+        const int32_t y0 = bounded ? (int32_t)floor(et / 4.0) : 0;
+        const int32_t x1 = bounded ? (int32_t)ceil(er / 4.0) : sw;
+        const int32_t y1 = bounded ? (int32_t)ceil(eb / 4.0) : sh;
+        const int32_t tw = sw * 4, th = sh * 4;
+        const int32_t bx0 = clampi(x0 * 4, 0, tw - 1), by0 = clampi(y0 * 4, 0, th - 1);
+        const int32_t bx1 = clampi(x1 * 4, bx0, tw - 1), by1 = clampi(y1 * 4, by0, th - 1);
+        const int32_t mw = bx1 + 1 - bx0, mh = by1 + 1 - by0;
+        const bool down = mw >= 4 && mh >= 4;
+        const int32_t rw = down ? mw / 4 : mw, rh = down ? mh / 4 : mh;
+        const int32_t cx = max(0, x0), cy = max(0, y0);
+        const int32_t w = (rw + cx > sw) ? sw - cx : rw, h = (rh + cy > sh) ? sh - cy : rh;
+        if (w <= 0 || h <= 0) {
+            S.active = 0;
+            st[f] = S;
+            return;
+        }
+        S.start_x = cx;
+        S.end_x = cx + w;
+        S.start_y = cy;
+        S.end_y = cy + h - 1;
+        // Without the downsample, nothing is ever painted into the mask: it
+        // is 1 sample wide (or high) only when extent_right (or _bottom) is
+        // 0 and the polygon lies left of (or above) the surface.
+        if (!down) S.flags |= FILL_SS_ZERO;
     } else {  // multisample.run (multisample.zig:46-78)
         S.start_y = clampi((int32_t)floor(et / 4.0), 0, sh - 1);
         S.end_y = clampi((int32_t)ceil(eb / 4.0), S.start_y, sh - 1);
         S.start_x = clampi((int32_t)floor(el / 4.0), 0, sw - 1);
         S.end_x = clampi((int32_t)ceil(er / 4.0), S.start_x, sw);
     }
-    if (S.flags & FILL_OPEN_CHAIN) S.flags |= FILL_EXACT;
+    if ((S.flags & FILL_OPEN_CHAIN) && !(S.flags & FILL_SS_ZERO)) S.flags |= FILL_EXACT;
     // rows the fill touches: the draw rows, or every row for unbounded
-    // operators (their clears reach outside the draw box)
-    const int32_t ty0 = bounded ? S.start_y : 0;
-    const int32_t ty1 = bounded ? S.end_y : sh - 1;
+    // operators (their clears reach outside the draw box); a supersample
+    // fill touches exactly its composite region
+    const bool boxed = bounded || F.aa == Z2D_AA_SUPERSAMPLE_4X;
+    const int32_t ty0 = boxed ? S.start_y : 0;
+    const int32_t ty1 = boxed ? S.end_y : sh - 1;
     S.band0 = ty0 / kTileRows;
     S.band1 = ty1 / kTileRows;
     S.fb_base = atomicAdd(&counters[CNT_FILL_BANDS], S.band1 - S.band0 + 1);
@@ -730,7 +764,7 @@ __global__ void k_fill_setup(const FillCmd *__restrict__ fills, FillState *__res
     }
     atomicMin(&counters[CNT_BAND_MIN], S.band0);
     atomicMax(&counters[CNT_BAND_MAX], S.band1);
-    const int32_t cx0 = bounded ? S.start_x : 0, cx1 = bounded ? S.end_x : sw;
+    const int32_t cx0 = boxed ? S.start_x : 0, cx1 = boxed ? S.end_x : sw;
     S.cull_x0 = cx0;
     S.cull_x1 = cx1;
     atomicMin(&counters[CNT_TCOL_MIN], cx0 / kTileCols);
@@ -989,6 +1023,27 @@ static __device__ __noinline__ I16 apply_fill(const FillCmd &F, int fmt, int32_t
     return normalize(encode_raw(float_op_any(F.op, decode_raw(d), r)), fmt);
 }
 
+// The supersample mask value of a pixel whose 4x4 sample block has n covered
+// samples, as 8-bit alpha: the mask is alpha8, or the surface's own format
+// for alpha4/2/1 surfaces (supersample.zig:69-83), each covered sample is
+// opaque, and downsampleBuffer averages the 16 (surface.zig:447-469).
+__device__ __forceinline__ uint32_t ss_mask8(int n, int fmt) {
+    if (fmt >= Z2D_FORMAT_ALPHA4) return scale_alpha(((uint32_t)n * fmt_max(fmt)) / 16u, fmt_bits(fmt), 8);
+    return ((uint32_t)n * 255u) / 16u;
+}
+
+// One pixel of the supersample batch [dst_in(dst = pattern, src = mask), op]
+// (supersample.zig:171-184) as StrideCompositor.runPrecision evaluates it
+// (compositor.zig:540-621): the mask reads as alpha-only lanes.
+static __device__ __noinline__ I16 apply_ssaa(const FillCmd &F, int32_t x, int32_t y, uint32_t m8, I16 d) {
+    if (F.precision == Z2D_PRECISION_INTEGER) {
+        const I16 r = int_op(Z2D_OP_DST_IN, src_i16_fast(F.src, x, y, 0), I16{0, 0, 0, m8});
+        return int_op_any(F.op, d, r);
+    }
+    const F4 r = float_op(Z2D_OP_DST_IN, src_f4_fast(F.src, x, y, 0), decode_raw(I16{0, 0, 0, m8}));
+    return encode_raw(float_op_any(F.op, decode_raw(d), r));
+}
+
 // multisample.run's clears for unbounded operators (multisample.zig:96-110),
 // including its quirks: the rows below the draw box are cleared up to the
 // surface WIDTH, and the right-hand clear starts at x = 0.
@@ -1086,16 +1141,18 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
             const FillCmd &F = A.fills[f];
             const int32_t op = F.op;
             const bool bounded = is_bounded(op);
-            if (bounded && (S.end_x <= x0 || S.start_x >= x0 + kTileCols)) continue;
+            const bool ssaa = F.aa == Z2D_AA_SUPERSAMPLE_4X;
+            const bool boxed = bounded || ssaa;  // touches only [start_x, end_x) x [start_y, end_y]
+            if (boxed && (S.end_x <= x0 || S.start_x >= x0 + kTileCols)) continue;
             const bool direct = F.aa == Z2D_AA_NONE;
             const bool exact = (S.flags & FILL_EXACT) != 0;
             const bool in_rows = y >= S.start_y && y <= S.end_y;
-            if (!in_rows && bounded) continue;
+            if (!in_rows && boxed) continue;
             const int32_t sc = direct ? 1 : 4, per = 8 * sc;
             // coverage of pixel q (0..16) is byte q / 2 of cov_ev (q even)
             // or cov_od (q odd)
             uint32_t cov_ev = 0, cov_od = 0;
-            if (!exact && in_rows) {
+            if (!exact && in_rows && !(S.flags & FILL_SS_ZERO)) {
                 const int32_t sub0 = y * sc, col0 = x0 * sc, ncol = kTileCols * sc;
                 const int32_t fb = S.fb_base + (b - S.band0);
                 const int32_t e0 = A.bin_off[fb], e1 = A.bin_off[fb + 1];
@@ -1183,16 +1240,19 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
                 // Pixel source, integer src_over: the compositeOpaque /
                 // compositeOpacity paths reduce to src_over(d, pixel) at full
                 // coverage and src_over(d, dst_in(pixel, opacity)) otherwise.
+                // The supersample batch [dst_in(pixel, mask), src_over] is the
+                // same with the downsampled mask value as opacity; at zero
+                // coverage both leave the pixel as it is.
                 // (A bounded fill outside its rows was skipped above.)
                 const I16 px = F.src.pix;
                 const int full = direct ? 1 : 16;
                 const int32_t xlo = S.start_x, xhi = direct ? W : min(S.end_x, W);
                 if (fmt <= Z2D_FORMAT_RGBA) {
                     // Lane k holds the source word for coverage k: the pixel
-                    // at k = full, dst_in(pixel, k * 16 - 1) below it.
+                    // at k = full, dst_in(pixel, opacity(k)) below it.
                     I16 s = px;
                     if (lane < full) {
-                        const uint32_t op8 = (uint32_t)max(lane * 16 - 1, 0);
+                        const uint32_t op8 = ssaa ? ss_mask8(lane, fmt) : (uint32_t)max(lane * 16 - 1, 0);
                         s = I16{(px.r * op8) / 255u, (px.g * op8) / 255u, (px.b * op8) / 255u, (px.a * op8) / 255u};
                     }
                     const uint32_t lut_w = i16_to_word(s, word_order(fmt));
@@ -1215,10 +1275,32 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
                     if (c == 0 || x < xlo || x >= xhi) continue;
                     I16 s = px;
                     if (c < full) {
-                        const uint32_t op8 = (uint32_t)(c * 16 - 1);
+                        const uint32_t op8 = ssaa ? ss_mask8(c, fmt) : (uint32_t)(c * 16 - 1);
                         s = I16{(px.r * op8) / 255u, (px.g * op8) / 255u, (px.b * op8) / 255u, (px.a * op8) / 255u};
                     }
                     raw[q] = i16_to_raw(int_op(Z2D_OP_SRC_OVER, raw_to_i16(raw[q], fmt), s), fmt);
+                    touched |= 1u << q;
+                }
+                continue;
+            }
+            if (ssaa) {
+                // every pixel of the composite region runs the batch
+                // [dst_in(pattern, mask), op] (supersample.zig:171-184)
+#pragma unroll 1
+                for (int q = 0; q < 8; q++) {
+                    const int32_t x = px0 + q;
+                    if (x >= W || x < S.start_x || x >= S.end_x) continue;
+                    int c = (int)((((q & 1) ? cov_od : cov_ev) >> (8 * (q >> 1))) & 0xFFu);
+                    if (exact && x >= S.mask_x0 && x < S.mask_x0 + S.mask_w)
+                        c = A.masks[S.mask_base + (long long)(y - S.start_y) * S.mask_w + (x - S.mask_x0)] & 0x1F;
+                    uint32_t rq = raw[0];
+#pragma unroll
+                    for (int j = 1; j < 8; j++)
+                        if (q == j) rq = raw[j];
+                    rq = i16_to_raw(apply_ssaa(F, x, y, ss_mask8(c, fmt), raw_to_i16(rq, fmt)), fmt);
+#pragma unroll
+                    for (int j = 0; j < 8; j++)
+                        if (q == j) raw[j] = rq;
                     touched |= 1u << q;
                 }
                 continue;

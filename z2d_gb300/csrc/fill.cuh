@@ -16,7 +16,7 @@ constexpr int32_t kMaxBandEdges = 32000;  // edges of one fill in one band (16-b
 // One fill command, prepared on the host.
 struct FillCmd {
     int32_t node_off, n_nodes;
-    int32_t aa;         // Z2D_AA_NONE or Z2D_AA_MULTISAMPLE_4X
+    int32_t aa;         // Z2D_AA_NONE, Z2D_AA_MULTISAMPLE_4X or Z2D_AA_SUPERSAMPLE_4X
     int32_t rule, op;
     int32_t precision;  // after the float upgrade of multisample.zig:36 / direct.zig:25
     int32_t pattern_kind;
@@ -87,13 +87,14 @@ enum : int32_t {
 enum : int32_t {
     FILL_OPEN_CHAIN = 1,  // an open 2-point subpath: rows may be unbalanced
     FILL_EXACT = 2,       // rasterised by k_exact
+    FILL_SS_ZERO = 4,     // supersample mask too small to downsample: all zero
 };
 
 struct FillState {
     int32_t edge_base, n_edges, flags, has_edges;
     unsigned long long ext[4];  // top(min), bottom(max), left(min), right(max) as ordered keys
     int32_t active;             // inBox passed
-    int32_t start_y, end_y;     // draw rows [start_y, end_y]
+    int32_t start_y, end_y;     // draw rows [start_y, end_y] (supersample: the composite region)
     int32_t start_x, end_x;     // draw columns [start_x, end_x)
     int32_t band0, band1;       // bands the fill touches
     int32_t fb_base;            // first (fill, band) slot
