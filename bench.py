@@ -306,6 +306,242 @@ def compositor_sweep(ctx, stream, dev, reps=3):
     }
 
 
+def compositor_breadth(ctx, stream, dev, reps=2):
+    """The rest of the compositor configuration, one timed pass each on
+    8192x8192 surfaces with the same [dst_in(dst = source, src = mask), op]
+    batch: the other pixel formats (integer operators, pixel source), the
+    float operators on RGBA, and gradient / dither sources (linear, radial,
+    conic x linear_rgb, srgb, hsl x no dither, Bayer, blue noise; 4 stops)."""
+    import torch
+    from z2d_gb300 import abi, compositor
+    from z2d_gb300.surface import Surface
+    from z2d_gb300.types import Color, Gradient, Operation, Pattern, Pixel
+    n = 8192
+    g = torch.Generator(device=dev)
+    g.manual_seed(SEED + 7)
+    mask = Surface("alpha8", n, n, torch.randint(0, 256, (n * n,), device=dev, generator=g,
+                                                  dtype=torch.int32).to(torch.uint8))
+    pix = Pattern.from_pixel(Pixel.rgba(90, 40, 160, 200))
+
+    def timed(dst, src, op, precision="integer"):
+        ops = [Operation("dst_in", dst=src, src=mask), Operation(op)]
+        compositor.SurfaceCompositor.run(dst, 0, 0, ops, precision, ctx=ctx)
+        ctx.set_timing(True)
+        for _ in range(reps):
+            compositor.SurfaceCompositor.run(dst, 0, 0, ops, precision, ctx=ctx)
+        ms, nl = ctx.kernel_ms("composite")
+        ctx.set_timing(False)
+        return ms / max(nl, 1)
+
+    out = {"formats": {}, "float_ops_rgba": {}, "sources_rgba_src_over": {}}
+    bpp = {"rgb": 4, "alpha8": 1, "alpha4": 0.5, "alpha2": 0.25, "alpha1": 0.125}
+    for fmt, b in bpp.items():
+        nbytes = abi.surface_bytes(abi.FORMAT_NAMES.index(fmt), n, n)
+        t = torch.randint(0, 256, ((nbytes + 3) // 4 * 4,), device=dev, generator=g, dtype=torch.int32).to(torch.uint8)
+        dst = Surface(fmt, n, n, t)
+        res = {}
+        for op in ("src_over", "xor", "multiply"):
+            ms = timed(dst, pix, op)
+            res[op] = {"ms": round(ms, 4), "gbs": (2 * b + 1) * n * n / (ms / 1e3) / 1e9}
+        out["formats"][fmt] = res
+        del dst, t
+    t = torch.randint(0, 256, (n * n * 4,), device=dev, generator=g, dtype=torch.int32).to(torch.uint8)
+    dst = Surface("rgba", n, n, t)
+    for op in ["src_over"] + sorted(abi.FLOAT_ONLY_OPS):
+        ms = timed(dst, pix, op, "float")
+        out["float_ops_rgba"][op] = {"ms": round(ms, 4), "mpix_s": n * n / 1e6 / (ms / 1e3)}
+    for kind in ("linear", "radial", "conic"):
+        for method in ("linear_rgb", "srgb", "hsl"):
+            gr = {"linear": Gradient.linear(100, 200, 8000, 7000, method=method),
+                  "radial": Gradient.radial(4000, 4000, 50, 4100, 4200, 5000, method=method),
+                  "conic": Gradient.conic(4096, 4096, 0.3, method=method)}[kind]
+            for i, c in enumerate((Color.rgb(1, 0, 0, 1), Color.rgb(0, 1, 0, 0.6), Color.rgb(0, 0, 1, 0.8),
+                                   Color.rgb(1, 1, 0, 1))):
+                gr.add_stop(i / 3, c)
+            for dither in ("none", "bayer", "blue_noise"):
+                src = Pattern.from_gradient(gr) if dither == "none" else Pattern.dither(dither, gr, 8)
+                ms = timed(dst, src, "src_over")
+                out["sources_rgba_src_over"][f"{kind}/{method}/{dither}"] = {
+                    "ms": round(ms, 4), "mpix_s": n * n / 1e6 / (ms / 1e3)}
+    stream.synchronize()
+    return out
+
+
+N_JOBS = 4096             # batched-jobs arm: RGBA jobs, sides log-uniform [16, 2048], 1-200 paths each
+JOBS_PLAIN_FILLS = 1500   # per-call sample of the jobs arm (complete jobs, in order)
+JOBS_CPU_SECONDS = 10.0   # CPU sample of the jobs arm: whole jobs in order until this much wall time
+
+
+def jobs_arm(ctx, stream, dev, steps=3):
+    """The batched-jobs configuration: N_JOBS independent RGBA surfaces, each
+    with its own ordered paths (z2d_gb300.workloads.batched_jobs; no strokes),
+    drawn by one z2dgpu_fill_jobs call per step.  Pixels counted: the sum of
+    the job surfaces' w x h.  Beside it: one z2dgpu_fill_batch call per
+    surface, one z2dgpu_fill call per path on a sample of whole jobs, and the
+    CPU restatement on all host threads (one job per thread) on a sample."""
+    import torch
+    from z2d_gb300 import painter
+    from z2d_gb300.batch import PackedBatch
+    from z2d_gb300.surface import Surface
+    from z2d_gb300.workloads import batched_jobs, job_fills
+    t_gen = time.perf_counter()
+    jobs = batched_jobs(SEED + 11, N_JOBS)
+    nodes, offs, cnts, pxs, rules, cmd_off, cmd_cnt = [], [], [], [], [], [], []
+    base = ncmd = 0
+    for w, h, nd, off, cnt, px, rl in jobs:
+        nodes.append(nd)
+        offs.append(off + base)
+        cnts.append(cnt)
+        pxs.append(px)
+        rules.append(rl)
+        cmd_off.append(ncmd)
+        cmd_cnt.append(len(off))
+        base += len(nd)
+        ncmd += len(off)
+    pb = PackedBatch(np.concatenate(nodes), np.concatenate(offs), np.concatenate(cnts), np.concatenate(pxs),
+                     np.concatenate(rules))
+    t_gen = time.perf_counter() - t_gen
+    sizes = [w * h * 4 for w, h, *_ in jobs]
+    starts = []
+    tot = 0
+    for sz in sizes:
+        starts.append(tot)
+        tot += (sz + 255) // 256 * 256
+    g = torch.Generator(device=dev)
+    g.manual_seed(SEED + 12)
+    a = torch.randint(0, 256, (tot // 4,), device=dev, generator=g, dtype=torch.int32)
+    rgb = torch.randint(0, 256, (tot // 4, 3), device=dev, generator=g, dtype=torch.int32) * (a[:, None] + 1) // 256
+    pristine = torch.cat([rgb, a[:, None]], 1).to(torch.uint8).reshape(-1).contiguous()
+    del a, rgb
+    buf = pristine.clone()
+    surfaces = [Surface("rgba", w, h, buf[o:o + sz]) for (w, h, *_), o, sz in zip(jobs, starts, sizes)]
+    pb.set_jobs(surfaces, cmd_off, cmd_cnt)
+    mpix = sum(w * h for w, h, *_ in jobs) / 1e6
+
+    def restore():
+        with torch.cuda.stream(stream):
+            buf.copy_(pristine)
+        stream.synchronize()
+
+    restore()
+    pb.fill_jobs(ctx)  # warm
+    ctx.set_timing(True)
+    walls = []
+    for _ in range(steps):
+        restore()
+        t0 = time.perf_counter()
+        pb.fill_jobs(ctx)
+        stream.synchronize()
+        walls.append(time.perf_counter() - t0)
+    stage_ms = {k: ctx.kernel_ms(k)[0] / steps for k in ("flatten", "bins", "raster")}
+    ctx.set_timing(False)
+    # one z2dgpu_fill_batch per surface
+    restore()
+    t0 = time.perf_counter()
+    for j, sfc in enumerate(surfaces):
+        pb.fill_batch(sfc, cmd_off[j], cmd_cnt[j], ctx=ctx)
+    stream.synchronize()
+    per_surface_s = time.perf_counter() - t0
+    # one z2dgpu_fill per path on whole jobs from the start
+    restore()
+    k, nf = 0, 0
+    while k < len(jobs) and nf < JOBS_PLAIN_FILLS:
+        nf += cmd_cnt[k]
+        k += 1
+    plain_fills = [(surfaces[j], job_fills(jobs[j])) for j in range(k)]
+    t0 = time.perf_counter()
+    for sfc, fl in plain_fills:
+        for pat, nd, opts in fl:
+            painter.fill(sfc, pat, nd, opts, ctx=ctx)
+    stream.synchronize()
+    plain_s = time.perf_counter() - t0
+    plain_mpix = sum(jobs[j][0] * jobs[j][1] for j in range(k)) / 1e6
+    out = {
+        "workload": f"{N_JOBS} RGBA jobs, sides log-uniform [16, 2048], 1-200 paths each (no strokes)",
+        "jobs": N_JOBS, "fills": int(ncmd), "nodes": int(base), "mpix_per_step": mpix,
+        "value": mpix * steps / sum(walls), "unit": "Mpix/s (sum of job surfaces w x h)",
+        "ms_per_step": 1000 * sum(walls) / steps,
+        "stage_ms_per_step": stage_ms,
+        "per_surface_batch": {"value": mpix / per_surface_s, "calls": N_JOBS},
+        "plain": {"value": plain_mpix / plain_s, "jobs": k, "calls": nf},
+        "note": "wall time of the call (host validation and packing, uploads, kernels); "
+                "inputs in host memory, surfaces on the device",
+        "generation_s": t_gen,
+    }
+    del buf, pristine, surfaces
+    # CPU restatement on all host threads, one job per thread, whole jobs in
+    # order until JOBS_CPU_SECONDS have passed
+    from oracle import load_oracle
+    from concurrent.futures import ThreadPoolExecutor
+    import ctypes as C
+    from z2d_gb300 import abi as A
+    from z2d_gb300.types import nodes_to_abi
+    lib = load_oracle()
+
+    def prepare(j):
+        w, h = jobs[j][0], jobs[j][1]
+        host = np.zeros(w * h * 4, np.uint8)
+        keep, calls = [], []
+        for pat, nd, opts in job_fills(jobs[j]):
+            p, o, arr = pat.to_abi(keep), opts.to_abi(), nodes_to_abi(nd)
+            keep += [p, o, arr]
+            calls.append((C.byref(p), arr, len(nd), C.byref(o)))
+        sfc = A.z2d_surface(format=A.FORMAT_RGBA, width=w, height=h, location=A.MEM_HOST,
+                            data=host.ctypes.data_as(C.c_void_p))
+        return (sfc, host, keep, calls)
+
+    def run(item):
+        sfc, _, _, calls = item
+        for p, arr, n, o in calls:
+            lib.z2doracle_fill(C.byref(sfc), p, arr, n, o)
+
+    nt = host_threads()
+    k = nf = 0
+    cpu_s = 0.0
+    with ThreadPoolExecutor(nt) as ex:
+        while k < len(jobs) and cpu_s < JOBS_CPU_SECONDS:
+            chunk = list(range(k, min(len(jobs), k + 4 * nt)))
+            work = [prepare(j) for j in chunk]
+            t0 = time.perf_counter()
+            list(ex.map(run, work))
+            cpu_s += time.perf_counter() - t0
+            k = chunk[-1] + 1
+            nf += sum(cmd_cnt[j] for j in chunk)
+    out["cpu"] = {"value": sum(jobs[j][0] * jobs[j][1] for j in range(k)) / 1e6 / cpu_s, "jobs": k, "fills": nf,
+                  "cores": nt, "seconds": cpu_s, "kind": "port"}
+    return out
+
+
+def star_latency(ctx, dev, iters=200):
+    """The small plain configuration: the 300x300 star, one painter.fill per
+    call, on a device surface and on a host surface (synchronous calls:
+    host wall time per call, p50/p99)."""
+    import torch
+    from z2d_gb300 import painter
+    from z2d_gb300.surface import Surface
+    from z2d_gb300.workloads import fill_box_pixels, star_300
+    w, h, nodes, pat, opts = star_300()
+    px = fill_box_pixels(nodes, w, h)
+    res = {}
+    for where in ("device", "host"):
+        s = Surface.init("rgba", w, h)
+        if where == "device":
+            s = s.to_device(dev)
+        lat = []
+        for i in range(iters + 5):
+            t0 = time.perf_counter()
+            painter.fill(s, pat, nodes, opts, ctx=ctx)
+            if where == "device":
+                ctx.synchronize()
+            if i >= 5:
+                lat.append((time.perf_counter() - t0) * 1e6)
+        lat.sort()
+        res[where] = {"p50_us": lat[len(lat) // 2], "p99_us": lat[int(len(lat) * 0.99) - 1],
+                      "mpix_s": px / 1e6 / (statistics.mean(lat) / 1e6)}
+    res["fill_box_px"] = px
+    return res
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -362,6 +598,7 @@ def run_ours(args):
         step_ms.append(e0.elapsed_time(e1))
     launches = ctx.launch_count - launches0
     raster_ms, raster_n = ctx.kernel_ms("raster")
+    stage = {k: ctx.kernel_ms(k)[0] / args.steps for k in ("flatten", "bins", "raster")}
     ctx.set_timing(False)
     total_ms = sum(step_ms)
     if world > 1:
@@ -392,12 +629,16 @@ def run_ours(args):
     stream.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
+    call_us = []
     for pat, n, opts in fills[:PLAIN_FILLS]:
+        t0 = time.perf_counter()
         painter.fill(surf, pat, n, opts, ctx=ctx)
+        call_us.append((time.perf_counter() - t0) * 1e6)
     e1.record(stream)
     e1.synchronize()
     plain_ms = e0.elapsed_time(e1)
     plain_mpix = sum(px[:PLAIN_FILLS]) / 1e6
+    call_us.sort()
 
     if rank != 0:
         clocks.stop()
@@ -407,13 +648,23 @@ def run_ours(args):
     alg_bytes = 2 * 4 * union_px  # read + write of every surface pixel a fill box touches
     raster_ms_per = raster_ms / max(raster_n, 1)
     achieved = alg_bytes / (raster_ms_per / 1e3) / 1e9
-    comp = compositor_sweep(ctx, stream, dev)
+    arms = set(args.arms.split(",")) if args.arms not in ("all", "") else {"compositor", "breadth", "star", "jobs",
+                                                                            "cpu"}
+    comp = comp_roof = star = jobs = None
+    if "compositor" in arms:
+        comp = compositor_sweep(ctx, stream, dev)
+        comp_roof = {"bound": "hbm", "kernel": "k_mask_op<RGBA, src_over>", "achieved": comp["gbs_src_over"],
+                     "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": comp["gbs_src_over"] / peaks["hbm_gbs"],
+                     "traffic": TRAFFIC["k_mask_op"][0], "traffic_source": TRAFFIC["k_mask_op"][1],
+                     "alg_bytes_per_launch": comp["bytes_per_px"] * 8192 * 8192, "peak_source": peak_kind}
     clk = clocks.stop()  # sampled over the batched, e2e, plain and compositor timed regions
-    comp_roof = {"bound": "hbm", "kernel": "k_mask_op<RGBA, src_over>", "achieved": comp["gbs_src_over"],
-                 "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": comp["gbs_src_over"] / peaks["hbm_gbs"],
-                 "traffic": TRAFFIC["k_mask_op"][0], "traffic_source": TRAFFIC["k_mask_op"][1],
-                 "alg_bytes_per_launch": comp["bytes_per_px"] * 8192 * 8192, "peak_source": peak_kind}
-    cpu_v, cpu_dt = cpu_sample(bg, fills, px, CPU_SAMPLE_FILLS)
+    if comp is not None and "breadth" in arms:
+        comp["breadth"] = compositor_breadth(ctx, stream, dev)
+    if "star" in arms:
+        star = star_latency(ctx, dev)
+    if "jobs" in arms:
+        jobs = jobs_arm(ctx, stream, dev)
+    cpu_v, cpu_dt = cpu_sample(bg, fills, px, CPU_SAMPLE_FILLS) if "cpu" in arms else (None, 0.0)
     line = {
         "metric": "Mpix/s fill+composite (src_over, 4096x4096 RGBA, 2000 random paths)",
         "value": value, "unit": "Mpix/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -422,8 +673,14 @@ def run_ours(args):
         "config": {"workload": "plain_large_4096x4096_2000_paths", "surface": "rgba 4096x4096",
                    "paths": N_FILLS, "mpix_per_step": mpix_step, "l2": "flushed (256 MiB write) before each step",
                    "mode": "batched (z2dgpu_fill_batch, device-resident surface)"},
+        "stage_ms_per_step": stage,
         "plain": {"value": plain_mpix / (plain_ms / 1e3), "unit": "Mpix/s", "ms": plain_ms,
-                  "calls": PLAIN_FILLS, "note": f"z2dgpu_fill per path, first {PLAIN_FILLS} fills"},
+                  "calls": PLAIN_FILLS, "note": f"z2dgpu_fill per path, first {PLAIN_FILLS} fills",
+                  "latency_us": {"p50": call_us[len(call_us) // 2], "p99": call_us[int(len(call_us) * 0.99) - 1],
+                                 "note": "host wall time per call (the call returns after its fill is queued "
+                                         "and its sizes are read back)"}},
+        "star_300": star,
+        "jobs": jobs,
         "batched_over_plain": (mpix_step / (total_ms / args.steps / 1e3)) / (plain_mpix / (plain_ms / 1e3)),
         "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": "k_raster", "achieved": achieved, "peak": peaks["hbm_gbs"],
@@ -448,6 +705,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--arms", default="all",
+                    help="extra arms beside the batched / e2e / per-call fill arms: 'all', 'none' or a comma "
+                         "list of compositor, breadth, star, jobs, cpu (shorter runs for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

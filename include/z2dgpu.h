@@ -9,6 +9,7 @@
  *   z2dgpu_fill        <- painter.fill                  src/painter.zig:66-72
  *   z2dgpu_fill_batch  <- N x painter.fill, same surface src/painter.zig:66-143
  *                         (Context.fill loop, src/Context.zig:592-607)
+ *   z2dgpu_fill_jobs   <- the same over many surfaces
  *   z2dgpu_composite   <- compositor.SurfaceCompositor.run
  *                                                       src/compositor.zig:302-309
  *                         (and Surface.composite,       src/surface.zig:225-241)
@@ -206,6 +207,14 @@ typedef struct z2d_fill_cmd {
     z2d_fill_opts opts;
 } z2d_fill_cmd;
 
+/* one surface of a multi-surface batch: cmds[cmd_offset, cmd_offset+n_cmds)
+ * of the batch command array, drawn in order on `surface` */
+typedef struct z2d_job {
+    z2d_surface surface;
+    uint64_t cmd_offset;
+    uint64_t n_cmds;
+} z2d_job;
+
 typedef struct z2dgpu_ctx z2dgpu_ctx;
 
 /* ---- library / context ---- */
@@ -226,8 +235,11 @@ Z2D_API uint64_t z2dgpu_ctx_launch_count(const z2dgpu_ctx *ctx);
  * events on its stream and accumulates their device time.  Reading a time
  * synchronizes the context.  No reference counterpart (instrumentation). */
 Z2D_API int z2dgpu_ctx_set_timing(z2dgpu_ctx *ctx, int enable);
-/* Accumulated milliseconds and launch count of `kernel` since timing was
- * enabled; returns -1 for an unknown name. */
+/* Accumulated milliseconds and launch count of a stage since timing was
+ * enabled: "raster" (k_raster), "composite" (compositor kernels), "flatten"
+ * (path flattening and fill setup, two intervals per fill call) or "bins"
+ * (edge binning, band lists and the exact path).  Returns -1 for an unknown
+ * name. */
 Z2D_API double z2dgpu_ctx_kernel_ms(z2dgpu_ctx *ctx, const char *kernel, uint64_t *launches);
 
 /* Bytes of pixel storage for a surface (src/surface.zig:382-395, 621-635). */
@@ -247,6 +259,16 @@ Z2D_API int z2dgpu_fill(z2dgpu_ctx *ctx, z2d_surface *surface,
 Z2D_API int z2dgpu_fill_batch(z2dgpu_ctx *ctx, z2d_surface *surface,
                               const z2d_node *nodes, size_t n_nodes,
                               const z2d_fill_cmd *cmds, size_t n_cmds);
+
+/* Many independent surfaces in one device pass: for every job, the
+ * equivalent of calling painter.fill for its commands in order on its
+ * surface (z2d's callers loop over surfaces; there is no batch call in z2d
+ * itself).  Surfaces must be in device memory and distinct; the commands
+ * index one shared node array.  The work is queued on the context stream and
+ * the call returns after launch. */
+Z2D_API int z2dgpu_fill_jobs(z2dgpu_ctx *ctx, const z2d_job *jobs, size_t n_jobs,
+                             const z2d_node *nodes, size_t n_nodes,
+                             const z2d_fill_cmd *cmds, size_t n_cmds);
 
 /* SurfaceCompositor.run (src/compositor.zig:302-440) with 1 or 2 operations.
  * Source/destination surfaces must live where `dst` lives. */

@@ -110,6 +110,10 @@ class z2d_fill_cmd(C.Structure):
                 ("n_nodes", C.c_uint64), ("opts", z2d_fill_opts)]
 
 
+class z2d_job(C.Structure):
+    _fields_ = [("surface", z2d_surface), ("cmd_offset", C.c_uint64), ("n_cmds", C.c_uint64)]
+
+
 def surface_bytes(fmt: int, width: int, height: int) -> int:
     """Storage size of a surface (src/surface.zig:382-395, 621-635)."""
     return (width * height * FORMAT_BITS[fmt] + 7) // 8
@@ -120,6 +124,6 @@ EXPORTED_SYMBOLS = [
     "z2dgpu_version", "z2dgpu_last_error", "z2dgpu_ctx_create", "z2dgpu_ctx_destroy",
     "z2dgpu_ctx_synchronize", "z2dgpu_ctx_launch_count", "z2dgpu_ctx_set_timing",
     "z2dgpu_ctx_kernel_ms", "z2dgpu_surface_bytes",
-    "z2dgpu_fill", "z2dgpu_fill_batch", "z2dgpu_composite",
+    "z2dgpu_fill", "z2dgpu_fill_batch", "z2dgpu_fill_jobs", "z2dgpu_composite",
     "z2dgpu_composite_noalloc",
 ]

@@ -353,15 +353,17 @@ static int stage_out(Ctx &c, const z2d_surface &s, const DevSurface &d) {
     return Z2D_OK;
 }
 
-// Builds the prepared commands of a list of fills.
-static int prepare_fills(const z2d_surface &s, const z2d_node *nodes, size_t n_nodes, const z2d_fill_cmd *cmds, size_t n_cmds,
-                         std::vector<FillCmd> &fills, std::vector<int32_t> &node_fill, std::vector<DevGradient> &grads,
+// Appends the prepared commands of a list of fills on surface `s` (job
+// `job` of the batch).  node_fill must hold n_nodes entries, -1 for nodes
+// no command has claimed yet.
+static int prepare_fills(const z2d_surface &s, int32_t job, const z2d_node *nodes, size_t n_nodes,
+                         const z2d_fill_cmd *cmds, size_t n_cmds, std::vector<FillCmd> &fills,
+                         std::vector<int32_t> &node_fill, std::vector<DevGradient> &grads,
                          std::vector<int32_t> &grad_of_fill) {
-    if (n_nodes > 0x7FFFFFFF || n_cmds > 0x7FFFFFF) {
+    if (n_nodes > 0x7FFFFFFF || n_cmds > 0x7FFFFFF || fills.size() + n_cmds > 0x7FFFFFF) {
         set_error("batch too large");
         return Z2D_ERR_INVALID_ARGUMENT;
     }
-    node_fill.assign(n_nodes, -1);
     for (size_t i = 0; i < n_cmds; i++) {
         const z2d_fill_cmd &cm = cmds[i];
         if (!cm.pattern) return Z2D_ERR_INVALID_ARGUMENT;
@@ -380,6 +382,7 @@ static int prepare_fills(const z2d_surface &s, const z2d_node *nodes, size_t n_n
         memset(&F, 0, sizeof(F));
         F.node_off = (int32_t)cm.node_offset;
         F.n_nodes = (int32_t)cm.n_nodes;
+        F.job = job;
         F.aa = (aa == Z2D_AA_NONE || aa == Z2D_AA_SUPERSAMPLE_4X) ? aa : Z2D_AA_MULTISAMPLE_4X;
         F.rule = cm.opts.fill_rule;
         F.op = cm.opts.op;
@@ -421,21 +424,25 @@ static int prepare_fills(const z2d_surface &s, const z2d_node *nodes, size_t n_n
     return Z2D_OK;
 }
 
-static int do_fill_batch(Ctx &c, z2d_surface *surface, const z2d_node *nodes, size_t n_nodes, const z2d_fill_cmd *cmds,
-                         size_t n_cmds) {
-    int rc = check_surface(surface);
-    if (rc) return rc;
-    if (n_cmds > 0 && !cmds) return Z2D_ERR_INVALID_ARGUMENT;
-    std::vector<FillCmd> fills;
-    std::vector<int32_t> node_fill, grad_of_fill;
-    std::vector<DevGradient> grads;
-    rc = prepare_fills(*surface, nodes, n_nodes, cmds, n_cmds, fills, node_fill, grads, grad_of_fill);
-    if (rc) return rc;
-    if (fills.empty()) return Z2D_OK;
-    // compact the node array to the nodes that belong to a fill
-    std::vector<z2d_node> used;
-    std::vector<int32_t> used_fill;
+// True when the fills own every node and their node ranges follow each
+// other in order, so the caller's node array can be uploaded as it is.
+static bool nodes_in_order(size_t n_nodes, const std::vector<FillCmd> &fills) {
+    size_t next = 0;
+    for (const FillCmd &F : fills) {
+        if ((size_t)F.node_off != next) return false;
+        next += (size_t)F.n_nodes;
+    }
+    return next == n_nodes;
+}
+
+// Keeps only the nodes some fill owns, in order, and points the fills at
+// their nodes in the compacted array.
+static void compact_nodes(const z2d_node *nodes, size_t n_nodes, const std::vector<int32_t> &node_fill,
+                          std::vector<FillCmd> &fills, std::vector<z2d_node> &used, std::vector<int32_t> &used_fill) {
+    used.clear();
+    used_fill.clear();
     used.reserve(n_nodes);
+    used_fill.reserve(n_nodes);
     std::vector<int32_t> new_off(fills.size(), -1);
     for (size_t i = 0; i < n_nodes; i++) {
         const int32_t f = node_fill[i];
@@ -445,12 +452,73 @@ static int do_fill_batch(Ctx &c, z2d_surface *surface, const z2d_node *nodes, si
         used_fill.push_back(f);
     }
     for (size_t f = 0; f < fills.size(); f++) fills[f].node_off = new_off[f];
-    DevSurface ds;
-    rc = stage_in(c, *surface, c.surface, ds);
+}
+
+static int do_fill_batch(Ctx &c, z2d_surface *surface, const z2d_node *nodes, size_t n_nodes, const z2d_fill_cmd *cmds,
+                         size_t n_cmds) {
+    int rc = check_surface(surface);
     if (rc) return rc;
-    rc = run_fills(c, ds, used.data(), (int32_t)used.size(), fills, used_fill, grads, grad_of_fill);
+    if (n_cmds > 0 && !cmds) return Z2D_ERR_INVALID_ARGUMENT;
+    std::vector<FillCmd> fills;
+    std::vector<int32_t> node_fill(n_nodes, -1), grad_of_fill;
+    std::vector<DevGradient> grads;
+    rc = prepare_fills(*surface, 0, nodes, n_nodes, cmds, n_cmds, fills, node_fill, grads, grad_of_fill);
+    if (rc) return rc;
+    if (fills.empty()) return Z2D_OK;
+    std::vector<z2d_node> used;
+    std::vector<int32_t> used_fill;
+    compact_nodes(nodes, n_nodes, node_fill, fills, used, used_fill);
+    std::vector<DevJob> jobs(1);
+    memset(jobs.data(), 0, sizeof(DevJob));
+    rc = stage_in(c, *surface, c.surface, jobs[0].sfc);
+    if (rc) return rc;
+    jobs[0].fill0 = 0;
+    jobs[0].fill1 = (int32_t)fills.size();
+    const DevSurface ds = jobs[0].sfc;
+    rc = run_jobs(c, jobs, used.data(), (int32_t)used.size(), fills, used_fill, grads, grad_of_fill);
     if (rc) return rc;
     return stage_out(c, *surface, ds);
+}
+
+// Many surfaces, each with its own ordered fill commands (device surfaces).
+static int do_fill_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_node *nodes, size_t n_nodes,
+                        const z2d_fill_cmd *cmds, size_t n_cmds) {
+    if ((n_jobs > 0 && !jobs_in) || (n_cmds > 0 && !cmds) || (n_nodes > 0 && !nodes)) return Z2D_ERR_INVALID_ARGUMENT;
+    if (n_jobs > 0x7FFFFFF) {
+        set_error("batch too large");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    std::vector<FillCmd> fills;
+    std::vector<int32_t> node_fill(n_nodes, -1), grad_of_fill;
+    std::vector<DevGradient> grads;
+    std::vector<DevJob> jobs(n_jobs);
+    if (n_jobs > 0) memset(jobs.data(), 0, sizeof(DevJob) * n_jobs);
+    for (size_t j = 0; j < n_jobs; j++) {
+        const z2d_job &jb = jobs_in[j];
+        int rc = check_surface(&jb.surface);
+        if (rc) return rc;
+        if (jb.surface.location != Z2D_MEM_DEVICE) {
+            set_error("fill_jobs: surfaces must be in device memory");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+        if (jb.cmd_offset > n_cmds || jb.n_cmds > n_cmds - jb.cmd_offset) {
+            set_error("fill_jobs: job commands outside the command array");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+        jobs[j].sfc = DevSurface{reinterpret_cast<uint8_t *>(jb.surface.data), jb.surface.format, jb.surface.width,
+                                 jb.surface.height};
+        jobs[j].fill0 = (int32_t)fills.size();
+        rc = prepare_fills(jb.surface, (int32_t)j, nodes, n_nodes, cmds + jb.cmd_offset, jb.n_cmds, fills, node_fill,
+                           grads, grad_of_fill);
+        if (rc) return rc;
+        jobs[j].fill1 = (int32_t)fills.size();
+    }
+    if (fills.empty()) return Z2D_OK;
+    if (nodes_in_order(n_nodes, fills)) return run_jobs(c, jobs, nodes, (int32_t)n_nodes, fills, node_fill, grads, grad_of_fill);
+    std::vector<z2d_node> used;
+    std::vector<int32_t> used_fill;
+    compact_nodes(nodes, n_nodes, node_fill, fills, used, used_fill);
+    return run_jobs(c, jobs, used.data(), (int32_t)used.size(), fills, used_fill, grads, grad_of_fill);
 }
 
 // SurfaceCompositor.run's precision upgrade and bounds
@@ -582,8 +650,7 @@ Z2D_API int z2dgpu_ctx_destroy(z2dgpu_ctx *c) {
     for (DevBuf *b : bufs) b->release();
     c->staging.release();
     c->readback.release();
-    c->timer_collect(c->t_raster);
-    c->timer_collect(c->t_composite);
+    for (Ctx::Timer *t : {&c->t_raster, &c->t_composite, &c->t_flatten, &c->t_bins}) c->timer_collect(*t);
     if (c->own_stream) cudaStreamDestroy(c->stream);
     delete c;
     return Z2D_OK;
@@ -599,10 +666,10 @@ Z2D_API uint64_t z2dgpu_ctx_launch_count(const z2dgpu_ctx *c) { return c ? c->la
 
 Z2D_API int z2dgpu_ctx_set_timing(z2dgpu_ctx *c, int enable) {
     if (!c) return Z2D_ERR_INVALID_ARGUMENT;
-    c->timer_collect(c->t_raster);
-    c->timer_collect(c->t_composite);
-    c->t_raster = Ctx::Timer{};
-    c->t_composite = Ctx::Timer{};
+    for (Ctx::Timer *t : {&c->t_raster, &c->t_composite, &c->t_flatten, &c->t_bins}) {
+        c->timer_collect(*t);
+        *t = Ctx::Timer{};
+    }
     c->timing = enable != 0;
     return Z2D_OK;
 }
@@ -612,6 +679,8 @@ Z2D_API double z2dgpu_ctx_kernel_ms(z2dgpu_ctx *c, const char *kernel, uint64_t 
     Ctx::Timer *t = nullptr;
     if (strcmp(kernel, "raster") == 0) t = &c->t_raster;
     else if (strcmp(kernel, "composite") == 0) t = &c->t_composite;
+    else if (strcmp(kernel, "flatten") == 0) t = &c->t_flatten;
+    else if (strcmp(kernel, "bins") == 0) t = &c->t_bins;
     if (!t) return -1.0;
     c->timer_collect(*t);
     if (launches) *launches = t->n;
@@ -640,6 +709,13 @@ Z2D_API int z2dgpu_fill_batch(z2dgpu_ctx *c, z2d_surface *surface, const z2d_nod
     if (!c) return Z2D_ERR_INVALID_ARGUMENT;
     Z2D_CUDA(cudaSetDevice(c->device));
     return do_fill_batch(*c, surface, nodes, n_nodes, cmds, n_cmds);
+}
+
+Z2D_API int z2dgpu_fill_jobs(z2dgpu_ctx *c, const z2d_job *jobs, size_t n_jobs, const z2d_node *nodes, size_t n_nodes,
+                             const z2d_fill_cmd *cmds, size_t n_cmds) {
+    if (!c) return Z2D_ERR_INVALID_ARGUMENT;
+    Z2D_CUDA(cudaSetDevice(c->device));
+    return do_fill_jobs(*c, jobs, n_jobs, nodes, n_nodes, cmds, n_cmds);
 }
 
 Z2D_API int z2dgpu_composite(z2dgpu_ctx *c, z2d_surface *dst, int32_t dst_x, int32_t dst_y, int32_t n_ops,

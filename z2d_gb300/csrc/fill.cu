@@ -85,7 +85,121 @@ __device__ __forceinline__ double error_sq(const Knots &k) {
     const double be = bx * bx + by * by, ce = cx * cx + cy * cy;
     return be > ce ? be : ce;
 }
-__device__ __forceinline__ double lerp_half(double a, double b) { return a + ((b - a) / 2); }
+// f64 -> f32 by truncating the mantissa (relative error < 2^-23) with
+// integer operations only, so that no FP64 instruction is spent on it.
+// False outside f32's normal range (zero excepted).
+__device__ __forceinline__ bool f32_trunc(double v, float &out) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const uint32_t hi = (uint32_t)(b >> 32);
+    const uint32_t sign = hi & 0x80000000u;
+    if ((b << 1) == 0ull) {
+        out = __uint_as_float(sign);
+        return true;
+    }
+    const int32_t fe = (int32_t)((hi >> 20) & 0x7FFu) - 1023 + 127;
+    if (fe <= 0 || fe >= 255) return false;
+    out = __uint_as_float(sign | ((uint32_t)fe << 23) | ((uint32_t)(b >> 29) & 0x7FFFFFu));
+    return true;
+}
+
+// The decision errorSq(k) < tol2 of Spline.decomposeInto, taken in f32 when
+// that is safe.  GB300 runs f64 at a small fraction of its f32 rate, and the
+// error test is most of the subdivision's f64 work; only the control-point
+// differences (exact f64 subtractions, as in errorSq) stay in f64.  Every
+// f32 quantity carries an error bound built from first-order rounding
+// analysis with slack: inputs (truncation) < 2u, each operation u
+// (u = 2^-24), propagated through the projection and the squared norms.
+// Returns 1 / 0 when the f32 value is farther than its bound from tol2 and,
+// on the projection branches, from the branch condition; -1 otherwise (the
+// caller then evaluates errorSq in f64).
+__device__ __forceinline__ int error_sq_lt_f32(double bx64, double by64, double cx64, double cy64, bool proj,
+                                               double dx64, double dy64, float tol2f, float tol2e) {
+    const float U = 5.9604644775390625e-8f;  // 2^-24
+    float bx, by, cx, cy, dx = 0.0f, dy = 0.0f;
+    if (!f32_trunc(bx64, bx) || !f32_trunc(by64, by) || !f32_trunc(cx64, cx) || !f32_trunc(cy64, cy)) return -1;
+    float ebx = 2.0f * U * fabsf(bx), eby = 2.0f * U * fabsf(by), ecx = 2.0f * U * fabsf(cx), ecy = 2.0f * U * fabsf(cy);
+    if (proj) {
+        if (!f32_trunc(dx64, dx) || !f32_trunc(dy64, dy)) return -1;
+        const float edx = 2.0f * U * fabsf(dx), edy = 2.0f * U * fabsf(dy);
+        const float dd = dx * dx + dy * dy;
+        const float edd = 8.0f * U * dd;
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            float &px = i ? cx : bx, &py = i ? cy : by;
+            float &epx = i ? ecx : ebx, &epy = i ? ecy : eby;
+            const float t1 = px * dx, t2 = py * dy;
+            const float pd = t1 + t2;
+            const float epd = 8.0f * U * (fabsf(t1) + fabsf(t2));
+            const float diff = pd - dd;
+            const float m = 1.125f * (epd + edd) + 2.0f * U * fabsf(diff) + 1e-30f;
+            if (diff > m) {  // pd >= dd: subtract the whole chord
+                const float nx = px - dx, ny = py - dy;
+                epx = epx + edx + 2.0f * U * fabsf(nx);
+                epy = epy + edy + 2.0f * U * fabsf(ny);
+                px = nx;
+                py = ny;
+            } else if (diff < -m && dd > 0.0f) {  // subtract the projection onto the chord
+                const float t = pd / dd;
+                const float et = (epd + fabsf(t) * edd) / dd * 1.125f + 2.0f * U * fabsf(t) + 1e-30f;
+                const float rx = t * dx, ry = t * dy;
+                const float nx = px - rx, ny = py - ry;
+                epx = epx + fabsf(dx) * et + fabsf(t) * edx + 2.0f * U * (fabsf(rx) + fabsf(nx));
+                epy = epy + fabsf(dy) * et + fabsf(t) * edy + 2.0f * U * (fabsf(ry) + fabsf(ny));
+                px = nx;
+                py = ny;
+            } else {
+                return -1;
+            }
+        }
+    }
+    const float be = bx * bx + by * by, ce = cx * cx + cy * cy;
+    const float ebe = 2.0f * fabsf(bx) * ebx + 2.0f * fabsf(by) * eby + ebx * ebx + eby * eby + 4.0f * U * be;
+    const float ece = 2.0f * fabsf(cx) * ecx + 2.0f * fabsf(cy) * ecy + ecx * ecx + ecy * ecy + 4.0f * U * ce;
+    const float e = be > ce ? be : ce;
+    const float E = 1.25f * (ebe > ece ? ebe : ece) + 4.0f * U * e + 1e-30f + tol2e;
+    if (!(E < 1e30f)) return -1;
+    if (e + E < tol2f) return 1;
+    if (e - E > tol2f) return 0;
+    return -1;
+}
+
+// The squared tolerance of a subdivision, in f64 and as a truncated f32
+// with its error bound.
+struct Tol {
+    double d;
+    float f, e;
+    bool f_ok;
+};
+__device__ __forceinline__ Tol make_tol(double tol) {
+    Tol t;
+    t.d = tol * tol;  // decomposeInto's tolerance argument (Spline.zig:52)
+    t.f = 0.0f;
+    t.f_ok = f32_trunc(t.d, t.f);
+    t.e = 4.0f * 5.9604644775390625e-8f * t.f;
+    return t;
+}
+
+// errorSq(k) < t.d, exactly as the f64 comparison decides it.
+__device__ __forceinline__ bool below_tol(const Knots &k, const Tol &t) {
+    if (t.f_ok) {
+        const bool proj = k.ax != k.dx || k.ay != k.dy;
+        const int r = error_sq_lt_f32(k.bx - k.ax, k.by - k.ay, k.cx - k.ax, k.cy - k.ay, proj, k.dx - k.ax,
+                                      k.dy - k.ay, t.f, t.e);
+        if (r >= 0) return r != 0;
+    }
+    return error_sq(k) < t.d;
+}
+
+// x / 2.  For normal x whose half is normal this only lowers the exponent,
+// which integer operations do exactly (an f64 multiply is an expensive
+// instruction on GB300); zeros, subnormals and non-finite values divide.
+__device__ __forceinline__ double half_of(double x) {
+    const long long b = __double_as_longlong(x);
+    const uint32_t e = (uint32_t)(b >> 52) & 0x7FFu;
+    if (e > 1u && e < 0x7FFu) return __longlong_as_double(b - (1ll << 52));
+    return x / 2;
+}
+__device__ __forceinline__ double lerp_half(double a, double b) { return a + half_of(b - a); }
 
 // Knots.deCasteljau (Spline.zig:128-152): k becomes the first half, the
 // second half is returned.
@@ -114,7 +228,7 @@ __device__ __forceinline__ bool spline_walk(double ax, double ay, const double *
         emit(dx, dy);
         return true;
     }
-    const double tol2 = tol * tol;
+    const Tol t = make_tol(tol);
     Knots stack[kSplineStack];
     int sp = 0;
     stack[sp++] = Knots{ax, ay, bx, by, cx, cy, dx, dy};
@@ -127,7 +241,7 @@ __device__ __forceinline__ bool spline_walk(double ax, double ay, const double *
                 ok = false;
                 break;
             }
-            if (error_sq(k) < tol2) {
+            if (below_tol(k, t)) {
                 if (!pt_eq(k.ax, k.ay, ax, ay)) emit(k.ax, k.ay);
                 break;
             }
@@ -367,7 +481,7 @@ struct WarpFrontier {
 };
 
 // Expands the frontier of the curve from (ax, ay) through p[0..5].
-__device__ int frontier_expand(double ax, double ay, const double *p, double tol2, WarpFrontier &fr, int lane) {
+__device__ int frontier_expand(double ax, double ay, const double *p, const Tol &tol, WarpFrontier &fr, int lane) {
     if (lane == 0) {
         fr.k[0] = Knots{ax, ay, p[0], p[1], p[2], p[3], p[4], p[5]};
         fr.leaf[0] = 0;
@@ -380,7 +494,7 @@ __device__ int frontier_expand(double ax, double ay, const double *p, double tol
         int grow = 0;
         if (lane < n) {
             k = fr.k[lane];
-            leaf = fr.leaf[lane] || error_sq(k) < tol2;
+            leaf = fr.leaf[lane] || below_tol(k, tol);
             grow = leaf ? 1 : 2;
         }
         int incl = grow;
@@ -416,13 +530,12 @@ __device__ int frontier_expand(double ax, double ay, const double *p, double tol
     return n;
 }
 
-// Depth-first walk of one frontier item; emit(x, y) for each leaf start
-// that differs from the curve start (Spline.zig:56-71).  The final
-// lineTo(d) is not part of an item.
-template <class F>
-__device__ __forceinline__ bool walk_item(const Knots &k0, bool leaf, double ax, double ay, double tol2, F &&emit) {
-    if (leaf) {
-        if (!pt_eq(k0.ax, k0.ay, ax, ay)) emit(k0.ax, k0.ay);
+// Depth-first walk of one frontier item (Spline.zig:56-71): leaf(k) for
+// every subcurve that decomposeInto stops at, in order.
+template <class L>
+__device__ __forceinline__ bool walk_leaves(const Knots &k0, bool is_leaf, const Tol &tol, L &&leaf) {
+    if (is_leaf) {
+        leaf(k0);
         return true;
     }
     Knots stack[kSplineStack];
@@ -433,8 +546,8 @@ __device__ __forceinline__ bool walk_item(const Knots &k0, bool leaf, double ax,
         Knots k = stack[--sp];
         while (true) {
             if (--budget < 0) return false;
-            if (error_sq(k) < tol2) {
-                if (!pt_eq(k.ax, k.ay, ax, ay)) emit(k.ax, k.ay);
+            if (below_tol(k, tol)) {
+                leaf(k);
                 break;
             }
             const Knots second = de_casteljau(k);
@@ -443,6 +556,15 @@ __device__ __forceinline__ bool walk_item(const Knots &k0, bool leaf, double ax,
         }
     }
     return true;
+}
+
+// emit(x, y) for each leaf start that differs from the curve start: the
+// lineTo calls of decomposeInto.  The final lineTo(d) is not part of an item.
+template <class F>
+__device__ __forceinline__ bool walk_item(const Knots &k0, bool is_leaf, double ax, double ay, const Tol &tol, F &&emit) {
+    return walk_leaves(k0, is_leaf, tol, [&](const Knots &k) {
+        if (!pt_eq(k.ax, k.ay, ax, ay)) emit(k.ax, k.ay);
+    });
 }
 
 // "Last valid value before this lane" across the warp, seeded with carry.
@@ -487,24 +609,35 @@ __device__ __forceinline__ int warp_excl_sum(int v, int lane, int &total) {
 
 // Counts the lineTo calls (n_emit) and the points they add (n_added) of the
 // curve from (sx, sy) through p, cooperatively.  Result valid in all lanes.
+// Counts the lineTo calls (n_emit) and the points PointBuffer keeps
+// (n_added) of one curve, and the leaves of each frontier item
+// (item_leaves[0..kFrontier)).  chords is set when the curve's edges are
+// exactly its leaves' chords: every leaf start but the first differs from the
+// curve start (consecutive leaves share their end points, so the lineTo
+// sequence start, a1, a2, ..., d is the chord sequence), and every item has
+// fewer than 65536 leaves.
 __device__ bool curve_count_warp(double sx, double sy, const double *p, double tol, WarpFrontier &fr, int lane,
-                                 int32_t &n_emit, int32_t &n_added) {
+                                 int32_t &n_emit, int32_t &n_added, uint16_t *item_leaves, int32_t &chords) {
+    chords = 0;
     if (pt_eq(sx, sy, p[0], p[1]) && pt_eq(p[2], p[3], p[4], p[5])) {  // Spline.zig:39-42
         n_emit = 1;
         n_added = pt_eq(sx, sy, p[4], p[5]) ? 0 : 1;
         return true;
     }
-    const double tol2 = tol * tol;
+    const Tol tol2 = make_tol(tol);
     const int n = frontier_expand(sx, sy, p, tol2, fr, lane);
-    bool ok = true;
-    int32_t emit_tot = 0, add_tot = 0;
+    bool ok = true, small = true;
+    int32_t emit_tot = 0, add_tot = 0, leaf_tot = 0;
     double carry_x = sx, carry_y = sy;
     for (int base = 0; base < n; base += 32) {
         const int i = base + lane;
-        int32_t cnt = 0, internal = 0;
+        int32_t cnt = 0, internal = 0, leaves = 0;
         double fx = 0, fy = 0, lx = 0, ly = 0;
         if (i < n) {
-            ok &= walk_item(fr.k[i], fr.leaf[i] != 0, sx, sy, tol2, [&](double x, double y) {
+            ok &= walk_leaves(fr.k[i], fr.leaf[i] != 0, tol2, [&](const Knots &k) {
+                leaves++;
+                if (pt_eq(k.ax, k.ay, sx, sy)) return;  // decomposeInto plots no point equal to the start
+                const double x = k.ax, y = k.ay;
                 if (cnt == 0) {
                     fx = x;
                     fy = y;
@@ -515,7 +648,12 @@ __device__ bool curve_count_warp(double sx, double sy, const double *p, double t
                 ly = y;
                 cnt++;
             });
+            small &= leaves < 65536;
+            item_leaves[i] = (uint16_t)leaves;
         }
+        int lt = 0;
+        warp_excl_sum(leaves, lane, lt);
+        leaf_tot += lt;
         double px, py;
         prev_point_scan(cnt > 0, lx, ly, carry_x, carry_y, lane, px, py);
         const int32_t first_add = (cnt > 0 && !pt_eq(fx, fy, px, py)) ? 1 : 0;
@@ -534,6 +672,7 @@ __device__ bool curve_count_warp(double sx, double sy, const double *p, double t
         }
     }
     // final lineTo(d)
+    chords = (__all_sync(0xffffffffu, small) && leaf_tot == emit_tot + 1) ? 1 : 0;
     emit_tot += 1;
     add_tot += pt_eq(p[4], p[5], carry_x, carry_y) ? 0 : 1;
     n_emit = emit_tot;
@@ -545,6 +684,7 @@ __global__ void __launch_bounds__(32 * kFlattenWarps) k_node_count_w(const z2d_n
                                                                      const int32_t *__restrict__ node_fill,
                                                                      const FillCmd *__restrict__ fills,
                                                                      NodeInfo *__restrict__ info, int32_t n_nodes,
+                                                                     uint16_t *__restrict__ item_leaves,
                                                                      int32_t *__restrict__ status) {
     __shared__ WarpFrontier frs[kFlattenWarps];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -567,7 +707,8 @@ __global__ void __launch_bounds__(32 * kFlattenWarps) k_node_count_w(const z2d_n
                 if (nd.tag == Z2D_LINE_TO) {
                     inf.n_emit = 1;
                     inf.n_added = pt_eq(sx, sy, nd.p[0], nd.p[1]) ? 0 : 1;
-                } else if (!curve_count_warp(sx, sy, nd.p, F.tol, fr, lane, inf.n_emit, inf.n_added)) {
+                } else if (!curve_count_warp(sx, sy, nd.p, F.tol, fr, lane, inf.n_emit, inf.n_added,
+                                             item_leaves + (size_t)i * kFrontier, inf.chords)) {
                     if (lane == 0) atomicExch(status, Z2D_ERR_INVALID_STATE);
                 }
             }
@@ -582,6 +723,7 @@ __global__ void __launch_bounds__(32 * kFlattenWarps) k_node_emit_w(const z2d_no
                                                                     const FillCmd *__restrict__ fills,
                                                                     const NodeInfo *__restrict__ info,
                                                                     FillState *__restrict__ st, DEdge *__restrict__ edges,
+                                                                    const uint16_t *__restrict__ item_leaves,
                                                                     int32_t n_nodes) {
     __shared__ WarpFrontier frs[kFlattenWarps];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -602,8 +744,29 @@ __global__ void __launch_bounds__(32 * kFlattenWarps) k_node_emit_w(const z2d_no
                 else if (nd.tag == Z2D_CLOSE_PATH) add_edge(F, out, inf.sx, inf.sy, inf.ex, inf.ey, et, eb, el, er, any);
                 else add_edge(F, out, inf.sx, inf.sy, nd.p[4], nd.p[5], et, eb, el, er, any);
             }
+        } else if (inf.chords) {
+            // One walk: the edges are the leaves' chords (a -> d), and the
+            // count pass left each frontier item's leaf count.
+            const Tol tol2 = make_tol(F.tol);
+            const int n = frontier_expand(inf.sx, inf.sy, nd.p, tol2, fr, lane);
+            const uint16_t *il = item_leaves + (size_t)i * kFrontier;
+            int32_t base_off = 0;
+            for (int base = 0; base < n; base += 32) {
+                const int i2 = base + lane;
+                const int32_t cnt = i2 < n ? (int32_t)il[i2] : 0;
+                int tot = 0;
+                const int off = base_off + warp_excl_sum(cnt, lane, tot);
+                if (i2 < n && cnt > 0) {
+                    int32_t k = off;
+                    walk_leaves(fr.k[i2], fr.leaf[i2] != 0, tol2, [&](const Knots &kn) {
+                        if (k < inf.n_emit) add_edge(F, out + k, kn.ax, kn.ay, kn.dx, kn.dy, et, eb, el, er, any);
+                        k++;
+                    });
+                }
+                base_off += tot;
+            }
         } else {
-            const double tol2 = F.tol * F.tol;
+            const Tol tol2 = make_tol(F.tol);
             const int n = frontier_expand(inf.sx, inf.sy, nd.p, tol2, fr, lane);
             int32_t base_off = 0;
             double carry_x = inf.sx, carry_y = inf.sy;
@@ -668,10 +831,12 @@ __global__ void __launch_bounds__(32 * kFlattenWarps) k_node_emit_w(const z2d_no
 __device__ __forceinline__ int32_t clampi(int32_t v, int32_t lo, int32_t hi) { return max(lo, min(v, hi)); }
 
 __global__ void k_fill_setup(const FillCmd *__restrict__ fills, FillState *__restrict__ st, int32_t n_fills,
-                             int32_t sw, int32_t sh, int32_t *__restrict__ counters) {
+                             DevJob *__restrict__ jobs, int32_t *__restrict__ counters) {
     const int32_t f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= n_fills) return;
     const FillCmd F = fills[f];
+    DevJob &J = jobs[F.job];
+    const int32_t sw = J.sfc.w, sh = J.sfc.h;
     FillState S = st[f];
     S.active = 0;
     if (!S.has_edges) {  // inBox of the empty polygon is false
@@ -762,13 +927,13 @@ __global__ void k_fill_setup(const FillCmd *__restrict__ fills, FillState *__res
         S.mask_base = atomicAdd(reinterpret_cast<unsigned long long *>(&counters[CNT_MASK_LO]), (unsigned long long)bytes);
         atomicAdd(&counters[CNT_EXACT], 1);
     }
-    atomicMin(&counters[CNT_BAND_MIN], S.band0);
-    atomicMax(&counters[CNT_BAND_MAX], S.band1);
+    atomicMin(&J.band_lo, S.band0);
+    atomicMax(&J.band_hi, S.band1);
     const int32_t cx0 = boxed ? S.start_x : 0, cx1 = boxed ? S.end_x : sw;
     S.cull_x0 = cx0;
     S.cull_x1 = cx1;
-    atomicMin(&counters[CNT_TCOL_MIN], cx0 / kTileCols);
-    atomicMax(&counters[CNT_TCOL_MAX], (max(cx1, cx0 + 1) - 1) / kTileCols);
+    atomicMin(&J.tcol_lo, cx0 / kTileCols);
+    atomicMax(&J.tcol_hi, (max(cx1, cx0 + 1) - 1) / kTileCols);
     st[f] = S;
 }
 
@@ -784,33 +949,67 @@ __device__ __forceinline__ bool edge_bands(const DEdge &e, const FillCmd &F, con
     return true;
 }
 
+// Binning visits every (edge, band) pair.  A long edge spans hundreds of
+// bands, so a thread per edge would serialise its atomics; instead each warp
+// takes 32 edges and walks their pairs 32 at a time, every lane finding the
+// edge of its pair by a binary search over the warp's prefix sums.
+template <class Visit>
+__device__ __forceinline__ void for_edge_bands(const FillCmd *__restrict__ fills, const FillState *__restrict__ st,
+                                               const DEdge *__restrict__ edges, const int32_t *__restrict__ edge_fill,
+                                               int32_t n_edges, Visit &&visit) {
+    const int lane = threadIdx.x & 31;
+    const int32_t stride = gridDim.x * blockDim.x;
+    for (int32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n_edges; base += stride) {
+        const int32_t i = base + lane;
+        int32_t nb = 0, fb0 = 0;
+        if (i < n_edges) {
+            const int32_t f = edge_fill[i];
+            if (f >= 0) {
+                const FillState &S = st[f];
+                int32_t b0, b1;
+                if (S.active && !(S.flags & FILL_EXACT) && edge_bands(edges[i], fills[f], S, b0, b1)) {
+                    nb = b1 - b0 + 1;
+                    fb0 = S.fb_base + (b0 - S.band0);
+                }
+            }
+        }
+        int32_t incl = nb;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int32_t excl = incl - nb;
+        const int32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        for (int32_t k0 = 0; k0 < total; k0 += 32) {
+            const int32_t k = k0 + lane;
+            // the last lane whose first pair is <= k owns pair k
+            int owner = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                const int32_t e = __shfl_sync(0xffffffffu, excl, owner + step);
+                if (e <= k) owner += step;
+            }
+            const int32_t o_excl = __shfl_sync(0xffffffffu, excl, owner);
+            const int32_t o_fb0 = __shfl_sync(0xffffffffu, fb0, owner);
+            if (k < total) visit(base + owner, o_fb0 + (k - o_excl));
+        }
+    }
+}
+
 __global__ void k_bin_count(const FillCmd *__restrict__ fills, const FillState *__restrict__ st,
                             const DEdge *__restrict__ edges, const int32_t *__restrict__ edge_fill, int32_t n_edges,
                             int32_t *__restrict__ fb_count, int32_t *__restrict__ status) {
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_edges) return;
-    const int32_t f = edge_fill[i];
-    if (f < 0) return;
-    const FillState &S = st[f];
-    if (!S.active || (S.flags & FILL_EXACT)) return;
-    int32_t b0, b1;
-    if (!edge_bands(edges[i], fills[f], S, b0, b1)) return;
-    for (int32_t b = b0; b <= b1; b++)
-        if (atomicAdd(&fb_count[S.fb_base + (b - S.band0)], 1) >= kMaxBandEdges) atomicExch(status, Z2D_ERR_INVALID_ARGUMENT);
+    for_edge_bands(fills, st, edges, edge_fill, n_edges, [&](int32_t, int32_t fb) {
+        if (atomicAdd(&fb_count[fb], 1) >= kMaxBandEdges) atomicExch(status, Z2D_ERR_INVALID_ARGUMENT);
+    });
 }
 
 __global__ void k_bin_fill(const FillCmd *__restrict__ fills, const FillState *__restrict__ st,
                            const DEdge *__restrict__ edges, const int32_t *__restrict__ edge_fill, int32_t n_edges,
                            int32_t *__restrict__ fb_cursor, int32_t *__restrict__ bins) {
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_edges) return;
-    const int32_t f = edge_fill[i];
-    if (f < 0) return;
-    const FillState &S = st[f];
-    if (!S.active || (S.flags & FILL_EXACT)) return;
-    int32_t b0, b1;
-    if (!edge_bands(edges[i], fills[f], S, b0, b1)) return;
-    for (int32_t b = b0; b <= b1; b++) bins[atomicAdd(&fb_cursor[S.fb_base + (b - S.band0)], 1)] = i;
+    for_edge_bands(fills, st, edges, edge_fill, n_edges,
+                   [&](int32_t edge, int32_t fb) { bins[atomicAdd(&fb_cursor[fb], 1)] = edge; });
 }
 
 // Edge -> fill map (edges of one fill are contiguous).
@@ -822,20 +1021,41 @@ __global__ void k_edge_fill(const FillState *__restrict__ st, int32_t n_fills, i
 
 // Ordered list of the fills touching each band (call order preserved by a
 // block-wide stream compaction).
-__global__ void __launch_bounds__(256) k_band_lists(const FillState *__restrict__ st, int32_t n_fills, int32_t band_lo,
-                                                    int32_t *__restrict__ band_count, int4 *__restrict__ band_fills) {
-    const int32_t b = band_lo + blockIdx.x;
+// The job a global index belongs to: the last job whose base is <= i
+// (bases ascending; jobs with nothing to draw repeat the next base).
+template <class Base>
+__device__ __forceinline__ int32_t job_of(const DevJob *__restrict__ jobs, int32_t n_jobs, long long i, Base base) {
+    int32_t lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {
+        const int32_t mid = (lo + hi + 1) >> 1;
+        if (base(jobs[mid]) <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// One CTA per global band: the job's fills touching the band, in call order
+// (ordered compaction), with the tile-column range each one can affect.
+__global__ void __launch_bounds__(256) k_band_lists(const FillState *__restrict__ st, const DevJob *__restrict__ jobs,
+                                                    int32_t n_jobs, int32_t *__restrict__ band_count,
+                                                    int4 *__restrict__ band_fills) {
+    const int32_t gb = blockIdx.x;
+    const int32_t j = job_of(jobs, n_jobs, gb, [](const DevJob &J) { return (long long)J.gband_base; });
+    const DevJob J = jobs[j];
+    const int32_t lb = gb - J.gband_base;
+    const int32_t b = J.band_lo + lb;
+    const int32_t nf = J.fill1 - J.fill0;
     __shared__ int32_t warp_tot[8];
     __shared__ int32_t base;
     if (threadIdx.x == 0) base = 0;
     __syncthreads();
     const int32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int4 *out = band_fills + (size_t)blockIdx.x * n_fills;
-    for (int32_t f0 = 0; f0 < n_fills; f0 += blockDim.x) {
+    int4 *out = band_fills + J.list_base + (long long)lb * nf;
+    for (int32_t f0 = J.fill0; f0 < J.fill1; f0 += blockDim.x) {
         const int32_t f = f0 + threadIdx.x;
         bool hit = false;
         int4 ent = make_int4(f, 0, 0, 0);
-        if (f < n_fills) {
+        if (f < J.fill1) {
             const FillState &S = st[f];
             hit = S.active && b >= S.band0 && b <= S.band1;
             ent.y = S.cull_x0;
@@ -854,7 +1074,7 @@ __global__ void __launch_bounds__(256) k_band_lists(const FillState *__restrict_
         if (threadIdx.x == 0) base += total;
         __syncthreads();
     }
-    if (threadIdx.x == 0) band_count[blockIdx.x] = base;
+    if (threadIdx.x == 0) band_count[gb] = base;
 }
 
 }  // namespace z2dg
@@ -892,12 +1112,13 @@ __device__ void shell_sort_unique(int32_t *a, int32_t &n) {
 }
 
 __global__ void k_exact(const FillCmd *__restrict__ fills, const FillState *__restrict__ st, const DEdge *__restrict__ edges,
-                        int32_t n_fills, int32_t sw, uint8_t *__restrict__ masks) {
+                        int32_t n_fills, const DevJob *__restrict__ jobs, uint8_t *__restrict__ masks) {
     const int32_t f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= n_fills) return;
     const FillState S = st[f];
     if (!S.active || !(S.flags & FILL_EXACT)) return;
     const FillCmd F = fills[f];
+    const int32_t sw = jobs[F.job].sfc.w;
     const DEdge *E = edges + S.edge_base;
     uint8_t *mask = masks + S.mask_base;  // zeroed by the host
     const int32_t mh = S.end_y - S.start_y + 1;
@@ -1054,16 +1275,17 @@ __device__ __forceinline__ bool msaa_unbounded_clear(const FillState &S, int32_t
 }
 
 struct RasterArgs {
-    DevSurface dst;
+    DevJob job0;                // the job of a one-surface batch, by value
+    const DevJob *jobs;
     const FillCmd *fills;
     const FillState *st;
     const DEdge *edges;
     const int32_t *bins;
     const int32_t *bin_off;
-    const int32_t *band_count;
-    const int4 *band_fills;  // {fill, cull_x0, cull_x1, 0} per band, in call order
+    const int32_t *band_count;  // per global band
+    const int4 *band_fills;     // {fill, cull_x0, cull_x1, 0} per band, in call order
     const uint8_t *masks;
-    int32_t n_fills, band_lo, tcol_lo;
+    int32_t n_jobs;
 };
 
 // Winding deltas of one warp: up to 4 sample rows x 1024 sample columns,
@@ -1107,24 +1329,37 @@ __device__ __forceinline__ void store_raw(const DevSurface &s, size_t i, uint32_
 // of its row's 4 (or 1) sample rows from the fill's band edges, prefix-scans
 // them across the warp, turns the inside bits into coverage and composites
 // its 8 pixels, which stay in registers from the first fill to the last.
+// MULTI = false draws a one-surface batch from A.job0, whose fields are
+// kernel parameters (warp-uniform values that need no registers);
+// MULTI = true finds each CTA's job in the job table.
+template <bool MULTI>
 __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A) {
     extern __shared__ uint32_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t *words = smem + warp * kWarpWords;
-    const int32_t b = A.band_lo + blockIdx.y;
-    const int32_t cnt = A.band_count[blockIdx.y];
+    // CTA -> (job, band, tile column): jobs hold consecutive CTA ranges
+    int32_t jb = 0;
+    if constexpr (MULTI) jb = job_of(A.jobs, A.n_jobs, blockIdx.x, [](const DevJob &J) { return (long long)J.tile_base; });
+    const DevJob &JB = MULTI ? A.jobs[jb] : A.job0;
+    const int32_t local = blockIdx.x - JB.tile_base, ncols = JB.tcol_hi - JB.tcol_lo + 1;
+    const int32_t lb = local / ncols;
+    const int32_t b = JB.band_lo + lb;
+    const int32_t cnt = A.band_count[JB.gband_base + lb];
     if (cnt == 0) return;
-    const int32_t x0 = (A.tcol_lo + blockIdx.x) * kTileCols, y = b * kTileRows + warp;
-    const int32_t W = A.dst.w, H = A.dst.h, fmt = A.dst.fmt;
+    const int32_t x0 = (JB.tcol_lo + local % ncols) * kTileCols, y = b * kTileRows + warp;
+    const int32_t W = JB.sfc.w, H = JB.sfc.h, fmt = JB.sfc.fmt;
     if (y >= H) return;
-    const int4 *list = A.band_fills + (size_t)blockIdx.y * A.n_fills;
+    const int4 *list = A.band_fills + JB.list_base + (long long)lb * (JB.fill1 - JB.fill0);
     const int32_t px0 = x0 + lane * 8;  // this lane's first pixel
 
     for (int i = lane; i < kWarpWords; i += 32) words[i] = i < kTouchOff ? kBias2 : 0u;
     uint32_t raw[8];
     uint32_t touched = 0;
+    {
+        const DevSurface dst = JB.sfc;
 #pragma unroll
-    for (int q = 0; q < 8; q++) raw[q] = (px0 + q < W) ? load_raw(A.dst, (size_t)W * y + px0 + q) : 0u;
+        for (int q = 0; q < 8; q++) raw[q] = (px0 + q < W) ? load_raw(dst, (size_t)W * y + px0 + q) : 0u;
+    }
     __syncwarp();
 
     // The band's fill list is read 32 entries at a time, one per lane; the
@@ -1335,26 +1570,41 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
             }
         }
     }
+    // the surface pointer is read again here rather than kept in registers
+    // through the fill loop
+    DevSurface dst;
+    dst.data = MULTI ? *reinterpret_cast<uint8_t *const volatile *>(&A.jobs[jb].sfc.data) : A.job0.sfc.data;
+    dst.fmt = fmt;
+    dst.w = W;
+    dst.h = 0;  // unused by the stores
 #pragma unroll
     for (int q = 0; q < 8; q++)
-        if ((touched >> q) & 1u) store_raw(A.dst, (size_t)W * y + px0 + q, raw[q]);
+        if ((touched >> q) & 1u) store_raw(dst, (size_t)W * y + px0 + q, raw[q]);
 }
 
 // ----------------------------------------------------------- host side
 static inline unsigned grid_for(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
-int run_fills(Ctx &c, const DevSurface &sfc, const z2d_node *nodes, int32_t n_nodes, std::vector<FillCmd> &fills,
-              const std::vector<int32_t> &node_fill, const std::vector<DevGradient> &grads,
-              const std::vector<int32_t> &grad_of_fill) {
+int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n_nodes, std::vector<FillCmd> &fills,
+             const std::vector<int32_t> &node_fill, const std::vector<DevGradient> &grads,
+             const std::vector<int32_t> &grad_of_fill) {
     const int32_t n_fills = (int32_t)fills.size();
-    if (n_fills == 0 || n_nodes == 0) return Z2D_OK;
-    // ---- upload: nodes | node_fill | gradients | fills | counters
+    const int32_t n_jobs = (int32_t)jobs.size();
+    if (n_fills == 0 || n_nodes == 0 || n_jobs == 0) return Z2D_OK;
+    for (DevJob &J : jobs) {
+        J.band_lo = J.tcol_lo = 0x7FFFFFFF;
+        J.band_hi = J.tcol_hi = -1;
+        J.gband_base = J.tile_base = 0;
+        J.list_base = 0;
+    }
+    // ---- upload: nodes | node_fill | gradients | fills | jobs | counters
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
     const size_t o_nodes = 0;
     const size_t o_nfill = al(o_nodes + sizeof(z2d_node) * (size_t)n_nodes);
     const size_t o_grads = al(o_nfill + sizeof(int32_t) * (size_t)n_nodes);
     const size_t o_fills = al(o_grads + sizeof(DevGradient) * grads.size());
-    const size_t o_cnt = al(o_fills + sizeof(FillCmd) * (size_t)n_fills);
+    const size_t o_jobs = al(o_fills + sizeof(FillCmd) * (size_t)n_fills);
+    const size_t o_cnt = al(o_jobs + sizeof(DevJob) * (size_t)n_jobs);
     const size_t total = al(o_cnt + sizeof(int32_t) * CNT_COUNT);
     if (c.params.ensure(total) || c.staging.ensure(total)) return Z2D_ERR_OUT_OF_MEMORY;
     uint8_t *h = c.staging.as<uint8_t>();
@@ -1362,38 +1612,44 @@ int run_fills(Ctx &c, const DevSurface &sfc, const z2d_node *nodes, int32_t n_no
     const DevGradient *dgrads = reinterpret_cast<const DevGradient *>(dv + o_grads);
     for (int32_t i = 0; i < n_fills; i++)
         if (grad_of_fill[i] >= 0) fills[i].src.grad = dgrads + grad_of_fill[i];
+    // make sure the previous call's kernels no longer read the staging buffer
+    Z2D_CUDA(cudaStreamSynchronize(c.stream));
     memcpy(h + o_nodes, nodes, sizeof(z2d_node) * (size_t)n_nodes);
     memcpy(h + o_nfill, node_fill.data(), sizeof(int32_t) * (size_t)n_nodes);
     if (!grads.empty()) memcpy(h + o_grads, grads.data(), sizeof(DevGradient) * grads.size());
     memcpy(h + o_fills, fills.data(), sizeof(FillCmd) * (size_t)n_fills);
+    memcpy(h + o_jobs, jobs.data(), sizeof(DevJob) * (size_t)n_jobs);
     int32_t *cnt_h = reinterpret_cast<int32_t *>(h + o_cnt);
     for (int i = 0; i < CNT_COUNT; i++) cnt_h[i] = 0;
-    cnt_h[CNT_BAND_MIN] = 0x7FFFFFFF;
-    cnt_h[CNT_BAND_MAX] = -1;
-    cnt_h[CNT_TCOL_MIN] = 0x7FFFFFFF;
-    cnt_h[CNT_TCOL_MAX] = -1;
-    // make sure the previous call's kernels no longer read the staging buffer
-    Z2D_CUDA(cudaStreamSynchronize(c.stream));
     Z2D_CUDA(cudaMemcpyAsync(dv, h, total, cudaMemcpyHostToDevice, c.stream));
     const z2d_node *d_nodes = reinterpret_cast<const z2d_node *>(dv + o_nodes);
     const int32_t *d_nfill = reinterpret_cast<const int32_t *>(dv + o_nfill);
     const FillCmd *d_fills = reinterpret_cast<const FillCmd *>(dv + o_fills);
+    DevJob *d_jobs = reinterpret_cast<DevJob *>(dv + o_jobs);
     int32_t *d_cnt = reinterpret_cast<int32_t *>(dv + o_cnt);
 
-    if (c.node_info.ensure(sizeof(NodeInfo) * (size_t)n_nodes) || c.fill_state.ensure(sizeof(FillState) * (size_t)n_fills))
+    // node info, then the per-node leaf counts of the curves' frontier items
+    const size_t info_bytes = (sizeof(NodeInfo) * (size_t)n_nodes + 255) & ~(size_t)255;
+    if (c.node_info.ensure(info_bytes + sizeof(uint16_t) * kFrontier * (size_t)n_nodes) ||
+        c.fill_state.ensure(sizeof(FillState) * (size_t)n_fills))
         return Z2D_ERR_OUT_OF_MEMORY;
     NodeInfo *d_info = c.node_info.as<NodeInfo>();
+    uint16_t *d_items = reinterpret_cast<uint16_t *>(c.node_info.as<uint8_t>() + info_bytes);
     FillState *d_st = c.fill_state.as<FillState>();
     Z2D_CUDA(cudaMemsetAsync(d_st, 0, sizeof(FillState) * (size_t)n_fills, c.stream));
 
     // ---- flatten
     const unsigned flat_blocks = (unsigned)std::min<long long>(grid_for(n_nodes, kFlattenWarps), (long long)c.sm_count * 64);
+    cudaEvent_t tf = c.timer_begin(c.t_flatten);
     k_node_count_w<<<flat_blocks, 32 * kFlattenWarps, 0, c.stream>>>(d_nodes, d_nfill, d_fills, d_info, n_nodes,
-                                                                    d_cnt + CNT_STATUS);
+                                                                    d_items, d_cnt + CNT_STATUS);
     k_fill_scan<<<grid_for(n_fills, 64), 64, 0, c.stream>>>(d_nodes, d_fills, d_info, d_st, n_fills, d_cnt, d_cnt + CNT_STATUS);
+    c.timer_end(c.t_flatten, tf);
     c.launches += 2;
-    if (c.readback.ensure(sizeof(int32_t) * CNT_COUNT)) return Z2D_ERR_OUT_OF_MEMORY;
+    const size_t rb_bytes = sizeof(int32_t) * CNT_COUNT + sizeof(DevJob) * (size_t)n_jobs;
+    if (c.readback.ensure(rb_bytes)) return Z2D_ERR_OUT_OF_MEMORY;
     int32_t *rb = c.readback.as<int32_t>();
+    DevJob *rb_jobs = reinterpret_cast<DevJob *>(c.readback.as<uint8_t>() + sizeof(int32_t) * CNT_COUNT);
     Z2D_CUDA(cudaMemcpyAsync(rb, d_cnt, sizeof(int32_t) * CNT_COUNT, cudaMemcpyDeviceToHost, c.stream));
     Z2D_CUDA(cudaStreamSynchronize(c.stream));
     if (rb[CNT_STATUS] != 0) {
@@ -1407,25 +1663,56 @@ int run_fills(Ctx &c, const DevSurface &sfc, const z2d_node *nodes, int32_t n_no
     DEdge *d_edges = c.edges.as<DEdge>();
     int32_t *d_edge_fill = reinterpret_cast<int32_t *>(d_edges + std::max(n_edges, 1));
     // extents start at +inf/-inf keys: min slots 0xFF.., max slots 0
+    tf = c.timer_begin(c.t_flatten);
     k_node_emit_w<<<flat_blocks, 32 * kFlattenWarps, 0, c.stream>>>(d_nodes, d_nfill, d_fills, d_info, d_st, d_edges,
-                                                                   n_nodes);
+                                                                   d_items, n_nodes);
     k_edge_fill<<<n_fills, 128, 0, c.stream>>>(d_st, n_fills, d_edge_fill);
-    k_fill_setup<<<grid_for(n_fills, 64), 64, 0, c.stream>>>(d_fills, d_st, n_fills, sfc.w, sfc.h, d_cnt);
+    k_fill_setup<<<grid_for(n_fills, 64), 64, 0, c.stream>>>(d_fills, d_st, n_fills, d_jobs, d_cnt);
+    c.timer_end(c.t_flatten, tf);
     c.launches += 3;
     Z2D_CUDA(cudaMemcpyAsync(rb, d_cnt, sizeof(int32_t) * CNT_COUNT, cudaMemcpyDeviceToHost, c.stream));
+    Z2D_CUDA(cudaMemcpyAsync(rb_jobs, d_jobs, sizeof(DevJob) * (size_t)n_jobs, cudaMemcpyDeviceToHost, c.stream));
     Z2D_CUDA(cudaStreamSynchronize(c.stream));
     const int32_t n_fb = rb[CNT_FILL_BANDS];
     const long long mask_bytes = (long long)(((unsigned long long)(uint32_t)rb[CNT_MASK_LO + 1] << 32) | (uint32_t)rb[CNT_MASK_LO]);
     const int32_t n_exact = rb[CNT_EXACT];
-    const int32_t band_lo = rb[CNT_BAND_MIN], band_hi = rb[CNT_BAND_MAX];
-    const int32_t tcol_lo = rb[CNT_TCOL_MIN], tcol_hi = rb[CNT_TCOL_MAX];
-    if (band_hi < band_lo || tcol_hi < tcol_lo) return Z2D_OK;  // nothing is drawn
+    // ---- layout: global bands, raster CTAs and band-list slots, job after job
+    long long n_gbands = 0, n_tiles = 0, n_slots = 0;
+    for (int32_t j = 0; j < n_jobs; j++) {
+        DevJob &J = jobs[j];
+        J.band_lo = rb_jobs[j].band_lo;
+        J.band_hi = rb_jobs[j].band_hi;
+        J.tcol_lo = rb_jobs[j].tcol_lo;
+        J.tcol_hi = rb_jobs[j].tcol_hi;
+        J.gband_base = (int32_t)n_gbands;
+        J.tile_base = (int32_t)n_tiles;
+        J.list_base = n_slots;
+        if (J.band_hi < J.band_lo || J.tcol_hi < J.tcol_lo) {  // nothing is drawn on this surface
+            J.band_lo = 0;
+            J.band_hi = -1;
+            J.tcol_lo = 0;
+            J.tcol_hi = -1;
+            continue;
+        }
+        const long long nb = J.band_hi - J.band_lo + 1, nc = J.tcol_hi - J.tcol_lo + 1;
+        n_gbands += nb;
+        n_tiles += nb * nc;
+        n_slots += nb * (J.fill1 - J.fill0);
+    }
+    if (n_gbands == 0) return Z2D_OK;  // nothing is drawn
+    if (n_tiles > 0x7FFFFFFFll || n_gbands > 0x7FFFFFFFll) {
+        set_error("batch too large: more than 2^31 tiles");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    memcpy(rb_jobs, jobs.data(), sizeof(DevJob) * (size_t)n_jobs);
+    Z2D_CUDA(cudaMemcpyAsync(d_jobs, rb_jobs, sizeof(DevJob) * (size_t)n_jobs, cudaMemcpyHostToDevice, c.stream));
 
     // ---- bins: counts, exclusive scan, scatter
     if (c.bin_offsets.ensure(sizeof(int32_t) * (2 * (size_t)n_fb + 2))) return Z2D_ERR_OUT_OF_MEMORY;
     int32_t *d_fb_cnt = c.bin_offsets.as<int32_t>();
     int32_t *d_fb_off = d_fb_cnt + (n_fb + 1);
     Z2D_CUDA(cudaMemsetAsync(d_fb_cnt, 0, sizeof(int32_t) * (size_t)(n_fb + 1), c.stream));
+    cudaEvent_t tb = c.timer_begin(c.t_bins);
     if (n_edges > 0) {
         k_bin_count<<<grid_for(n_edges, 256), 256, 0, c.stream>>>(d_fills, d_st, d_edges, d_edge_fill, n_edges, d_fb_cnt,
                                                                    d_cnt + CNT_STATUS);
@@ -1435,6 +1722,7 @@ int run_fills(Ctx &c, const DevSurface &sfc, const z2d_node *nodes, int32_t n_no
     cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, d_fb_cnt, d_fb_off, n_fb + 1, c.stream);
     if (c.scan_tmp.ensure(tmp_bytes + 16)) return Z2D_ERR_OUT_OF_MEMORY;
     Z2D_CUDA(cub::DeviceScan::ExclusiveSum(c.scan_tmp.ptr, tmp_bytes, d_fb_cnt, d_fb_off, n_fb + 1, c.stream));
+    c.timer_end(c.t_bins, tb);
     c.launches++;
     Z2D_CUDA(cudaMemcpyAsync(rb, d_fb_off + n_fb, sizeof(int32_t), cudaMemcpyDeviceToHost, c.stream));
     Z2D_CUDA(cudaMemcpyAsync(rb + 1, d_cnt + CNT_STATUS, sizeof(int32_t), cudaMemcpyDeviceToHost, c.stream));
@@ -1447,19 +1735,19 @@ int run_fills(Ctx &c, const DevSurface &sfc, const z2d_node *nodes, int32_t n_no
     if (c.bins.ensure(sizeof(int32_t) * (size_t)std::max(n_bin_entries, 1))) return Z2D_ERR_OUT_OF_MEMORY;
     // scatter with the counts array reused as cursors
     Z2D_CUDA(cudaMemcpyAsync(d_fb_cnt, d_fb_off, sizeof(int32_t) * (size_t)(n_fb + 1), cudaMemcpyDeviceToDevice, c.stream));
+    tb = c.timer_begin(c.t_bins);
     if (n_edges > 0 && n_bin_entries > 0) {
         k_bin_fill<<<grid_for(n_edges, 256), 256, 0, c.stream>>>(d_fills, d_st, d_edges, d_edge_fill, n_edges, d_fb_cnt,
                                                                   c.bins.as<int32_t>());
         c.launches++;
     }
 
-    // ---- ordered fill lists per band
-    const int32_t n_bands = band_hi - band_lo + 1;
-    const size_t count_bytes = ((sizeof(int32_t) * (size_t)n_bands) + 15) & ~(size_t)15;
-    if (c.band_fills.ensure(count_bytes + sizeof(int4) * (size_t)n_bands * (size_t)n_fills)) return Z2D_ERR_OUT_OF_MEMORY;
+    // ---- ordered fill lists per global band
+    const size_t count_bytes = ((sizeof(int32_t) * (size_t)n_gbands) + 15) & ~(size_t)15;
+    if (c.band_fills.ensure(count_bytes + sizeof(int4) * (size_t)std::max(n_slots, 1ll))) return Z2D_ERR_OUT_OF_MEMORY;
     int32_t *d_band_count = c.band_fills.as<int32_t>();
     int4 *d_band_fills = reinterpret_cast<int4 *>(c.band_fills.as<uint8_t>() + count_bytes);
-    k_band_lists<<<n_bands, 256, 0, c.stream>>>(d_st, n_fills, band_lo, d_band_count, d_band_fills);
+    k_band_lists<<<(unsigned)n_gbands, 256, 0, c.stream>>>(d_st, d_jobs, n_jobs, d_band_count, d_band_fills);
     c.launches++;
 
     // ---- exact path
@@ -1468,13 +1756,14 @@ int run_fills(Ctx &c, const DevSurface &sfc, const z2d_node *nodes, int32_t n_no
         const size_t need = (size_t)mask_bytes + 64;
         if (c.masks.ensure(need)) return Z2D_ERR_OUT_OF_MEMORY;
         Z2D_CUDA(cudaMemsetAsync(c.masks.ptr, 0, (size_t)mask_bytes, c.stream));
-        k_exact<<<grid_for(n_fills, 32), 32, 0, c.stream>>>(d_fills, d_st, d_edges, n_fills, sfc.w, c.masks.as<uint8_t>());
+        k_exact<<<grid_for(n_fills, 32), 32, 0, c.stream>>>(d_fills, d_st, d_edges, n_fills, d_jobs, c.masks.as<uint8_t>());
         c.launches++;
     }
+    c.timer_end(c.t_bins, tb);
 
     // ---- raster
     RasterArgs A;
-    A.dst = sfc;
+    A.jobs = d_jobs;
     A.fills = d_fills;
     A.st = d_st;
     A.edges = d_edges;
@@ -1483,21 +1772,22 @@ int run_fills(Ctx &c, const DevSurface &sfc, const z2d_node *nodes, int32_t n_no
     A.band_count = d_band_count;
     A.band_fills = d_band_fills;
     A.masks = c.masks.as<uint8_t>();
-    A.n_fills = n_fills;
-    A.band_lo = band_lo;
-    A.tcol_lo = tcol_lo;
+    A.n_jobs = n_jobs;
+    A.job0 = jobs[0];
     const size_t smem = sizeof(uint32_t) * kWarpWords * kTileRows;
     // function attributes are per device: set once on each
     static std::atomic<uint64_t> attr_set{0};
     const uint64_t dev_bit = 1ull << (c.device & 63);
     if (!(attr_set.load(std::memory_order_relaxed) & dev_bit)) {
-        Z2D_CUDA(cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        Z2D_CUDA(cudaFuncSetAttribute(k_raster, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        for (auto k : {k_raster<false>, k_raster<true>}) {
+            Z2D_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            Z2D_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        }
         attr_set.fetch_or(dev_bit, std::memory_order_relaxed);
     }
-    dim3 grid((unsigned)(tcol_hi - tcol_lo + 1), (unsigned)n_bands);
     cudaEvent_t t0 = c.timer_begin(c.t_raster);
-    k_raster<<<grid, kRasterThreads, smem, c.stream>>>(A);
+    if (n_jobs == 1) k_raster<false><<<(unsigned)n_tiles, kRasterThreads, smem, c.stream>>>(A);
+    else k_raster<true><<<(unsigned)n_tiles, kRasterThreads, smem, c.stream>>>(A);
     c.timer_end(c.t_raster, t0);
     c.launches++;
     Z2D_CUDA(cudaGetLastError());

@@ -22,7 +22,7 @@ struct FillCmd {
     int32_t pattern_kind;
     int32_t reduces;    // pixel pattern whose operator reduces to the source (shared.zig:111-117)
     int32_t fast_kind;  // FAST_* specialisation the rasteriser may use
-    int32_t _pad0;
+    int32_t job;        // index of the surface (job) the fill draws on
     double tol;         // max(tolerance, 0.001) (painter.zig:103)
     double scale;       // 4 for multisample, 1 for none (painter.zig:93-97)
     DevSrc src;         // the pattern as a compositor source
@@ -37,7 +37,7 @@ struct NodeInfo {
     int32_t n_emit; // edges emitted (one per lineTo the reference issues)
     int32_t n_added;
     int32_t edge_off;
-    int32_t _pad;
+    int32_t chords; // curve whose edges are its subdivision leaves' chords (see k_node_emit_w)
 };
 
 // Polygon.Edge plus its rounded active range: the edge is active on sample
@@ -109,22 +109,33 @@ enum : int32_t {
     CNT_FILL_BANDS = 1,
     CNT_MASK_LO = 2,  // + CNT_MASK_HI = 3
     CNT_EXACT = 4,
-    CNT_BAND_MIN = 5,
-    CNT_BAND_MAX = 6,
-    CNT_TCOL_MIN = 7,
-    CNT_TCOL_MAX = 8,
-    CNT_STATUS = 9,
-    CNT_COUNT = 10
+    CNT_STATUS = 5,
+    CNT_COUNT = 6
 };
 
 // action-mask byte of the exact path: bit 7 = clear first, bits 0-4 = coverage
 constexpr uint8_t kMaskClear = 0x80;
 
-// Runs an ordered list of fills on a device surface.  `fills` hold the
-// prepared commands (node offsets into `nodes`, host memory);
-// grad_of_fill[i] >= 0 names the gradient of fill i in `grads`.
-int run_fills(Ctx &c, const DevSurface &sfc, const z2d_node *nodes, int32_t n_nodes, std::vector<FillCmd> &fills,
-              const std::vector<int32_t> &node_fill, const std::vector<DevGradient> &grads,
-              const std::vector<int32_t> &grad_of_fill);
+// One surface of a batch with the contiguous range of its fills.  The host
+// sets sfc and fill0/fill1; k_fill_setup widens the touched band and tile
+// column ranges; the host then lays out global bands, tiles and band-list
+// storage job after job.
+struct DevJob {
+    DevSurface sfc;
+    int32_t fill0, fill1;      // fills [fill0, fill1), in call order
+    int32_t band_lo, band_hi;  // 4-row bands touched (band_hi < band_lo: none)
+    int32_t tcol_lo, tcol_hi;  // 256-pixel tile columns touched
+    int32_t gband_base;        // first global band of the job
+    int32_t tile_base;         // first CTA of the job in k_raster's grid
+    long long list_base;       // first band-list entry (one slot per fill and band)
+};
+
+// Runs ordered lists of fills on device surfaces (one list per job; jobs are
+// independent).  `fills` hold the prepared commands grouped by job (node
+// offsets into `nodes`, host memory); grad_of_fill[i] >= 0 names the
+// gradient of fill i in `grads`.
+int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n_nodes, std::vector<FillCmd> &fills,
+             const std::vector<int32_t> &node_fill, const std::vector<DevGradient> &grads,
+             const std::vector<int32_t> &grad_of_fill);
 
 }  // namespace z2dg

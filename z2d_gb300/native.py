@@ -68,12 +68,14 @@ def load(build_if_missing: bool = True):
                                     P(abi.z2d_fill_opts)]
         lib.z2dgpu_fill_batch.argtypes = [C.c_void_p, P(abi.z2d_surface), P(abi.z2d_node), C.c_size_t,
                                           P(abi.z2d_fill_cmd), C.c_size_t]
+        lib.z2dgpu_fill_jobs.argtypes = [C.c_void_p, P(abi.z2d_job), C.c_size_t, P(abi.z2d_node), C.c_size_t,
+                                         P(abi.z2d_fill_cmd), C.c_size_t]
         lib.z2dgpu_composite.argtypes = [C.c_void_p, P(abi.z2d_surface), C.c_int32, C.c_int32, C.c_int32,
                                          P(abi.z2d_operation), C.c_int32]
         lib.z2dgpu_composite_noalloc.argtypes = [C.c_int, C.c_void_p, P(abi.z2d_surface), C.c_int32, C.c_int32,
                                                  C.c_int32, P(abi.z2d_operation), C.c_int32]
         for name in ("z2dgpu_ctx_create", "z2dgpu_ctx_destroy", "z2dgpu_ctx_synchronize", "z2dgpu_fill",
-                     "z2dgpu_fill_batch", "z2dgpu_composite", "z2dgpu_composite_noalloc"):
+                     "z2dgpu_fill_batch", "z2dgpu_fill_jobs", "z2dgpu_composite", "z2dgpu_composite_noalloc"):
             getattr(lib, name).restype = C.c_int
         _lib = lib
         return lib

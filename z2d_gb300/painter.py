@@ -60,3 +60,47 @@ def fill_batch_arrays(surface, nodes: np.ndarray, cmds, ctx: Optional[Context] =
     s = surface.to_abi()
     check(ctx.lib.z2dgpu_fill_batch(ctx.handle, C.byref(s), nodes.ctypes.data_as(C.POINTER(abi.z2d_node)),
                                     len(nodes), cmds, len(cmds)))
+
+
+def fill_jobs(jobs: Sequence[Tuple[object, Sequence[Tuple[Pattern, object, FillOptions]]]],
+              ctx: Optional[Context] = None) -> None:
+    """Many surfaces in one device pass: for each (surface, fills) job, the
+    equivalent of fill() for each (pattern, nodes, opts) in order on that
+    surface.  Surfaces must be device-resident (Surface.to_device) and
+    distinct."""
+    ctx = ctx or default_context()
+    keep: list = []
+    node_arrays = []
+    n_cmds = sum(len(f) for _, f in jobs)
+    cmds = (abi.z2d_fill_cmd * max(1, n_cmds))()
+    jarr = (abi.z2d_job * max(1, len(jobs)))()
+    off = 0
+    ci = 0
+    for j, (surface, fills) in enumerate(jobs):
+        jarr[j].surface = surface.to_abi()
+        jarr[j].cmd_offset = ci
+        jarr[j].n_cmds = len(fills)
+        for pat, nodes, opts in fills:
+            arr = nodes if isinstance(nodes, np.ndarray) and nodes.dtype == NODE_DTYPE else None
+            if arr is None:
+                from .path import nodes_array
+                arr = nodes_array(nodes)
+            node_arrays.append(arr)
+            p = pat.to_abi(keep)
+            cmds[ci].pattern = C.pointer(p)
+            cmds[ci].node_offset = off
+            cmds[ci].n_nodes = len(arr)
+            cmds[ci].opts = opts.to_abi()
+            off += len(arr)
+            ci += 1
+    all_nodes = np.ascontiguousarray(np.concatenate(node_arrays) if node_arrays else np.zeros(0, NODE_DTYPE))
+    check(ctx.lib.z2dgpu_fill_jobs(ctx.handle, jarr, len(jobs), all_nodes.ctypes.data_as(C.POINTER(abi.z2d_node)),
+                                   len(all_nodes), cmds, n_cmds))
+
+
+def fill_jobs_arrays(jarr, nodes: np.ndarray, cmds, ctx: Optional[Context] = None) -> None:
+    """Low-level multi-surface entry: ctypes z2d_job and z2d_fill_cmd arrays
+    and the NODE_DTYPE array they index (no per-call marshalling)."""
+    ctx = ctx or default_context()
+    check(ctx.lib.z2dgpu_fill_jobs(ctx.handle, jarr, len(jarr), nodes.ctypes.data_as(C.POINTER(abi.z2d_node)),
+                                   len(nodes), cmds, len(cmds)))

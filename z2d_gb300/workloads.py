@@ -112,3 +112,70 @@ def fill_box_pixels(nodes: np.ndarray, w: int, h: int, scale: float = 4.0) -> in
     sx = min(max(int(math.floor(el / scale)), 0), w - 1)
     ex = min(max(int(math.ceil(er / scale)), sx), w)
     return (ey - sy + 1) * (ex - sx)
+
+
+def random_path_batch(rng: np.random.Generator, n: int, w: int, h: int, side_lo: float, side_hi: float,
+                      seg_lo: int = 3, seg_hi: int = 64) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """n paths distributed like random_path, generated together: returns the
+    concatenated node array and each path's node offset and count.  Each path
+    is move_to + segments + close_path + move_to(initial)."""
+    side = rng.uniform(side_lo, side_hi, n)
+    x0 = rng.uniform(0.0, 1.0, n) * np.maximum(0.0, w - side)
+    y0 = rng.uniform(0.0, 1.0, n) * np.maximum(0.0, h - side)
+    nseg = rng.integers(seg_lo, seg_hi + 1, n)
+    count = nseg + 3
+    off = np.zeros(n, np.int64)
+    np.cumsum(count[:-1], out=off[1:])
+    total = int(count.sum())
+    nodes = np.zeros(total, NODE_DTYPE)
+    pid = np.repeat(np.arange(n), count)
+    k = np.arange(total) - off[pid]          # position inside the path
+    pts = rng.uniform(0.0, 1.0, (total, 6)) * side[pid, None]
+    pts[:, 0::2] += x0[pid, None]
+    pts[:, 1::2] += y0[pid, None]
+    curve = rng.random(total) >= 0.5
+    tag = np.where(curve, abi.CURVE_TO, abi.LINE_TO).astype(np.int32)
+    tag[k == 0] = abi.MOVE_TO
+    last = off + count - 1
+    tag[last - 1] = abi.CLOSE_PATH
+    tag[last] = abi.MOVE_TO
+    pts[tag != abi.CURVE_TO, 2:] = 0.0
+    pts[tag == abi.CLOSE_PATH] = 0.0
+    pts[last, :2] = pts[off, :2]              # the move_to after close returns to the start
+    nodes["tag"] = tag
+    nodes["p"] = pts
+    return nodes, off, count
+
+
+def batched_jobs(seed: int, n_jobs: int, side_lo: int = 16, side_hi: int = 2048, paths_lo: int = 1,
+                 paths_hi: int = 200):
+    """The batched-jobs configuration: RGBA jobs whose sides are
+    log-uniform in [side_lo, side_hi], each with paths_lo..paths_hi random
+    closed paths generated like the large plain workload (3-64 segments, half
+    lines and half cubics, rule alternating, premultiplied pixel sources with
+    alpha U[32,255], src_over) with path boxes scaled to the job (side
+    U[side/64, side/2]).  Stroked paths are not included.  Returns, per job,
+    (width, height, nodes, node offsets, node counts, pixels (n x 4 RGBA),
+    rules)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_jobs):
+        w = int(round(math.exp(rng.uniform(math.log(side_lo), math.log(side_hi)))))
+        h = int(round(math.exp(rng.uniform(math.log(side_lo), math.log(side_hi)))))
+        n = int(rng.integers(paths_lo, paths_hi + 1))
+        s = min(w, h)
+        nodes, off, cnt = random_path_batch(rng, n, w, h, max(2.0, s / 64), max(4.0, s / 2))
+        a = rng.integers(32, 256, n)
+        rgb = (rng.random((n, 3)) * (a[:, None] + 1)).astype(np.int64)
+        px = np.concatenate([np.minimum(rgb, a[:, None]), a[:, None]], 1).astype(np.uint8)
+        rules = np.where(np.arange(n) % 2 == 0, abi.FILL_EVEN_ODD, abi.FILL_NON_ZERO).astype(np.int32)
+        out.append((w, h, nodes, off, cnt, px, rules))
+    return out
+
+
+def job_fills(job) -> List[Tuple[Pattern, np.ndarray, FillOptions]]:
+    """The (pattern, nodes, options) list of one batched_jobs entry."""
+    w, h, nodes, off, cnt, px, rules = job
+    names = {abi.FILL_EVEN_ODD: "even_odd", abi.FILL_NON_ZERO: "non_zero"}
+    return [(Pattern.from_pixel(Pixel.rgba(*map(int, px[i]))), nodes[off[i]:off[i] + cnt[i]],
+             FillOptions(fill_rule=names[int(rules[i])])) for i in range(len(off))]
