@@ -512,6 +512,122 @@ def jobs_arm(ctx, stream, dev, steps=3):
     return out
 
 
+SERVE_RATES = (5000, 20000, 50000)  # requests per second (Poisson arrivals)
+SERVE_SECONDS = 1.5                 # arrival window per rate
+
+
+def serving_arm(dev):
+    """The serving configuration: requests arrive as a Poisson process and go
+    through the native request queue (z2d_gb300.server, one worker thread
+    batching up to 512 requests within 300 us).  Mix: 80 % glyph-like
+    requests (one outline of 20-200 cubics on its own 64x64 RGBA surface;
+    half with a linear-gradient source), 20 % jobs of the batched-jobs
+    distribution with sides up to 512.  Every request draws on its own
+    surface.  Reported per rate: achieved request rate, latency p50/p99
+    (submit to completion, measured by the server) and Mpix/s of surface
+    area."""
+    import ctypes as C
+    import threading
+    import torch
+    from z2d_gb300 import abi
+    from z2d_gb300.server import Server
+    from z2d_gb300.surface import Surface
+    from z2d_gb300.types import Color, FillOptions, Gradient, Pattern, Pixel
+    from z2d_gb300.workloads import batched_jobs, glyph_path, job_fills, random_premultiplied_pixel
+    rng = np.random.default_rng(SEED + 21)
+    n_req = int(max(SERVE_RATES) * SERVE_SECONDS)
+    pool = 2000  # distinct request contents; request k draws pool entry k % pool on its own surface
+    jobs = batched_jobs(SEED + 22, pool // 5, side_lo=16, side_hi=512, paths_lo=1, paths_hi=50)
+    grad = Gradient.linear(0, 0, 64, 64)
+    grad.add_stop(0.0, Color.rgb(0.9, 0.1, 0.1, 1.0))
+    grad.add_stop(1.0, Color.rgb(0.1, 0.2, 0.9, 0.8))
+    reqs = []  # (w, h, nodes, cmds ctypes array, keep)
+    ji = 0
+    for i in range(pool):
+        if i % 5 == 4 and ji < len(jobs):
+            w, h = jobs[ji][0], jobs[ji][1]
+            fills = job_fills(jobs[ji])
+            ji += 1
+        else:
+            w = h = 64
+            pat = Pattern.from_gradient(grad) if i % 2 else Pattern.from_pixel(random_premultiplied_pixel(rng))
+            fills = [(pat, glyph_path(rng), FillOptions())]
+        keep = []
+        cmds = (abi.z2d_fill_cmd * len(fills))()
+        arrs, off = [], 0
+        for k, (pat, nd, opts) in enumerate(fills):
+            p = pat.to_abi(keep)
+            keep.append(p)
+            cmds[k].pattern = C.pointer(p)
+            cmds[k].node_offset = off
+            cmds[k].n_nodes = len(nd)
+            cmds[k].opts = opts.to_abi()
+            off += len(nd)
+            arrs.append(nd)
+        reqs.append((w, h, np.ascontiguousarray(np.concatenate(arrs)), cmds, keep))
+    sizes = [reqs[k % pool][0] * reqs[k % pool][1] * 4 for k in range(n_req)]
+    starts, tot = [], 0
+    for sz in sizes:
+        starts.append(tot)
+        tot += (sz + 255) // 256 * 256
+    buf = torch.zeros(tot, dtype=torch.uint8, device=dev)
+    sfcs = []
+    for k, (o, sz) in enumerate(zip(starts, sizes)):
+        w, h = reqs[k % pool][0], reqs[k % pool][1]
+        sfcs.append(Surface("rgba", w, h, buf[o:o + sz]).to_abi())
+    results = {}
+    with Server(max_batch_jobs=512, max_wait_us=300) as srv:
+        lib = srv.lib
+        # warm-up
+        for i in range(64):
+            w, h, nodes, cmds, _ = reqs[i]
+            srv.wait(_submit(lib, srv.handle, sfcs[i], nodes, cmds))
+        for rate in SERVE_RATES:
+            n = int(rate * SERVE_SECONDS)
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+            tickets = [0] * n
+            lat = [0.0] * n
+            submitted = threading.Semaphore(0)
+
+            def waiter():
+                for k in range(n):
+                    submitted.acquire()
+                    lat[k] = srv.wait(tickets[k])
+
+            th = threading.Thread(target=waiter)
+            th.start()
+            t0 = time.perf_counter()
+            for k in range(n):
+                while time.perf_counter() - t0 < arrivals[k]:
+                    pass
+                w, h, nodes, cmds, _ = reqs[k % pool]
+                tickets[k] = _submit(lib, srv.handle, sfcs[k], nodes, cmds)
+                submitted.release()
+            t_sub = time.perf_counter() - t0
+            th.join()
+            wall = time.perf_counter() - t0
+            ls = sorted(lat)
+            px = sum(sizes[:n]) // 4
+            results[str(rate)] = {"requests": n, "offered_per_s": rate, "submitted_per_s": n / t_sub,
+                                  "completed_per_s": n / wall, "p50_us": ls[n // 2], "p99_us": ls[int(n * 0.99) - 1],
+                                  "mpix_s": px / 1e6 / wall}
+        b, r, busy = srv.stats()
+    return {"workload": "Poisson arrivals; 80% glyphs (20-200 cubics, 64x64, half gradient), 20% jobs "
+                        "(sides 16-512, 1-50 paths); one surface per request",
+            "server": {"max_batch_jobs": 512, "max_wait_us": 300, "batches": b, "requests": r, "busy_ms": busy},
+            "rates": results}
+
+
+def _submit(lib, handle, sfc, nodes, cmds):
+    import ctypes as C
+    from z2d_gb300 import abi
+    from z2d_gb300.native import check
+    t = C.c_uint64()
+    check(lib.z2dgpu_server_submit(handle, C.byref(sfc), nodes.ctypes.data_as(C.POINTER(abi.z2d_node)), len(nodes),
+                                   cmds, len(cmds), C.byref(t)))
+    return t.value
+
+
 def star_latency(ctx, dev, iters=200):
     """The small plain configuration: the 300x300 star, one painter.fill per
     call, on a device surface and on a host surface (synchronous calls:
@@ -649,7 +765,7 @@ def run_ours(args):
     raster_ms_per = raster_ms / max(raster_n, 1)
     achieved = alg_bytes / (raster_ms_per / 1e3) / 1e9
     arms = set(args.arms.split(",")) if args.arms not in ("all", "") else {"compositor", "breadth", "star", "jobs",
-                                                                            "cpu"}
+                                                                            "serving", "cpu"}
     comp = comp_roof = star = jobs = None
     if "compositor" in arms:
         comp = compositor_sweep(ctx, stream, dev)
@@ -664,6 +780,7 @@ def run_ours(args):
         star = star_latency(ctx, dev)
     if "jobs" in arms:
         jobs = jobs_arm(ctx, stream, dev)
+    serving = serving_arm(dev) if "serving" in arms else None
     cpu_v, cpu_dt = cpu_sample(bg, fills, px, CPU_SAMPLE_FILLS) if "cpu" in arms else (None, 0.0)
     line = {
         "metric": "Mpix/s fill+composite (src_over, 4096x4096 RGBA, 2000 random paths)",
@@ -681,6 +798,7 @@ def run_ours(args):
                                          "and its sizes are read back)"}},
         "star_300": star,
         "jobs": jobs,
+        "serving": serving,
         "batched_over_plain": (mpix_step / (total_ms / args.steps / 1e3)) / (plain_mpix / (plain_ms / 1e3)),
         "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": "k_raster", "achieved": achieved, "peak": peaks["hbm_gbs"],
@@ -707,7 +825,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--arms", default="all",
                     help="extra arms beside the batched / e2e / per-call fill arms: 'all', 'none' or a comma "
-                         "list of compositor, breadth, star, jobs, cpu (shorter runs for profiling)")
+                         "list of compositor, breadth, star, jobs, serving, cpu (shorter runs for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -295,4 +295,34 @@ Z2D_API int z2dgpu_composite_noalloc(int device, void *stream, z2d_surface *dst,
                                      int32_t dst_x, int32_t dst_y, int32_t n_ops,
                                      const z2d_operation *ops, int32_t precision);
 
+/* ---------------------------------------------------------------- serving
+ * A request queue in front of z2dgpu_fill_jobs, for callers that submit fills
+ * for many surfaces from many threads (no counterpart in z2d).  One worker
+ * thread per server owns a context and a stream; it draws the requests that
+ * arrived within `max_wait_us` of the oldest waiting one (at most
+ * `max_batch_jobs` per pass) in one z2dgpu_fill_jobs pass.  Requests on the
+ * same surface are drawn in submission order; requests are copied at
+ * submit, so the caller's node/command/pattern buffers can be reused when
+ * submit returns, but surfaces (device memory) must stay valid until the
+ * request completes. */
+typedef struct z2dgpu_server z2dgpu_server;
+
+Z2D_API int z2dgpu_server_create(z2dgpu_server **server, int device, int32_t max_batch_jobs,
+                                 int32_t max_wait_us);
+/* Queues painter.fill for cmds[0..n_cmds) in order on `surface`; *ticket
+ * identifies the request. */
+Z2D_API int z2dgpu_server_submit(z2dgpu_server *server, const z2d_surface *surface,
+                                 const z2d_node *nodes, size_t n_nodes,
+                                 const z2d_fill_cmd *cmds, size_t n_cmds, uint64_t *ticket);
+/* Waits for a request (timeout_ms < 0: no limit) and returns its status, or
+ * Z2D_ERR_TIMEOUT if it is still pending (the ticket stays valid).
+ * *latency_us (optional) = completion time - submit time. */
+Z2D_API int z2dgpu_server_wait(z2dgpu_server *server, uint64_t ticket, int32_t timeout_ms,
+                               double *latency_us);
+/* Passes run, requests completed and worker busy time so far. */
+Z2D_API int z2dgpu_server_stats(z2dgpu_server *server, uint64_t *batches, uint64_t *requests,
+                                double *busy_ms);
+/* Draws every queued request, then stops the worker and frees the server. */
+Z2D_API int z2dgpu_server_destroy(z2dgpu_server *server);
+
 #endif /* Z2DGPU_H */

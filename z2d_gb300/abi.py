@@ -125,5 +125,6 @@ EXPORTED_SYMBOLS = [
     "z2dgpu_ctx_synchronize", "z2dgpu_ctx_launch_count", "z2dgpu_ctx_set_timing",
     "z2dgpu_ctx_kernel_ms", "z2dgpu_surface_bytes",
     "z2dgpu_fill", "z2dgpu_fill_batch", "z2dgpu_fill_jobs", "z2dgpu_composite",
-    "z2dgpu_composite_noalloc",
+    "z2dgpu_composite_noalloc", "z2dgpu_server_create", "z2dgpu_server_submit", "z2dgpu_server_wait",
+    "z2dgpu_server_stats", "z2dgpu_server_destroy",
 ]

@@ -28,6 +28,7 @@ void set_errorf(const char *fmt, ...) {
     vsnprintf(g_err, sizeof(g_err), fmt, ap);
     va_end(ap);
 }
+const char *last_error() { return g_err; }
 int cuda_fail(cudaError_t e, const char *what) {
     set_errorf("%s: %s", what, cudaGetErrorString(e));
     return Z2D_ERR_CUDA;
@@ -481,7 +482,7 @@ static int do_fill_batch(Ctx &c, z2d_surface *surface, const z2d_node *nodes, si
 }
 
 // Many surfaces, each with its own ordered fill commands (device surfaces).
-static int do_fill_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_node *nodes, size_t n_nodes,
+int fill_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_node *nodes, size_t n_nodes,
                         const z2d_fill_cmd *cmds, size_t n_cmds) {
     if ((n_jobs > 0 && !jobs_in) || (n_cmds > 0 && !cmds) || (n_nodes > 0 && !nodes)) return Z2D_ERR_INVALID_ARGUMENT;
     if (n_jobs > 0x7FFFFFF) {
@@ -611,7 +612,6 @@ static int noalloc_scratch(int device, DevGradient **out) {
 
 using namespace z2dg;
 
-struct z2dgpu_ctx : public Ctx {};
 
 extern "C" {
 
@@ -715,7 +715,7 @@ Z2D_API int z2dgpu_fill_jobs(z2dgpu_ctx *c, const z2d_job *jobs, size_t n_jobs, 
                              const z2d_fill_cmd *cmds, size_t n_cmds) {
     if (!c) return Z2D_ERR_INVALID_ARGUMENT;
     Z2D_CUDA(cudaSetDevice(c->device));
-    return do_fill_jobs(*c, jobs, n_jobs, nodes, n_nodes, cmds, n_cmds);
+    return fill_jobs(*c, jobs, n_jobs, nodes, n_nodes, cmds, n_cmds);
 }
 
 Z2D_API int z2dgpu_composite(z2dgpu_ctx *c, z2d_surface *dst, int32_t dst_x, int32_t dst_y, int32_t n_ops,

@@ -79,6 +79,13 @@ struct Ctx {
     void timer_collect(Timer &t);
 };
 
+}  // namespace z2dg
+
+// The opaque handle of include/z2dgpu.h is a context.
+struct z2dgpu_ctx : public z2dg::Ctx {};
+
+namespace z2dg {
+
 // -------------------------------------------------- descriptor conversion
 // Fills `out` for a pattern or compositor param.  Gradients are written to
 // `grad_host` (the caller uploads them and patches DevSrc::grad).
@@ -103,6 +110,11 @@ struct CompJob {
     CompOp ops[2];
 };
 int launch_composite(Ctx &c, const CompJob &job);
+// z2dgpu_fill_jobs on a context (capi.cu); the caller has made c's device current.
+int fill_jobs(Ctx &c, const z2d_job *jobs, size_t n_jobs, const z2d_node *nodes, size_t n_nodes,
+              const z2d_fill_cmd *cmds, size_t n_cmds);
+// Message of the last failing call on this thread.
+const char *last_error();
 // Launches the whole-surface mask batch [dst_in(pixel, alpha8 mask), op]
 // when J has that shape (composite_mask.cu); returns false otherwise.
 bool try_mask_batch(Ctx &c, const CompJob &J, bool flat);

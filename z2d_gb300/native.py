@@ -74,6 +74,15 @@ def load(build_if_missing: bool = True):
                                          P(abi.z2d_operation), C.c_int32]
         lib.z2dgpu_composite_noalloc.argtypes = [C.c_int, C.c_void_p, P(abi.z2d_surface), C.c_int32, C.c_int32,
                                                  C.c_int32, P(abi.z2d_operation), C.c_int32]
+        lib.z2dgpu_server_create.argtypes = [P(C.c_void_p), C.c_int, C.c_int32, C.c_int32]
+        lib.z2dgpu_server_submit.argtypes = [C.c_void_p, P(abi.z2d_surface), P(abi.z2d_node), C.c_size_t,
+                                             P(abi.z2d_fill_cmd), C.c_size_t, P(C.c_uint64)]
+        lib.z2dgpu_server_wait.argtypes = [C.c_void_p, C.c_uint64, C.c_int32, P(C.c_double)]
+        lib.z2dgpu_server_stats.argtypes = [C.c_void_p, P(C.c_uint64), P(C.c_uint64), P(C.c_double)]
+        lib.z2dgpu_server_destroy.argtypes = [C.c_void_p]
+        for name in ("z2dgpu_server_create", "z2dgpu_server_submit", "z2dgpu_server_wait", "z2dgpu_server_stats",
+                     "z2dgpu_server_destroy"):
+            getattr(lib, name).restype = C.c_int
         for name in ("z2dgpu_ctx_create", "z2dgpu_ctx_destroy", "z2dgpu_ctx_synchronize", "z2dgpu_fill",
                      "z2dgpu_fill_batch", "z2dgpu_fill_jobs", "z2dgpu_composite", "z2dgpu_composite_noalloc"):
             getattr(lib, name).restype = C.c_int

@@ -179,3 +179,24 @@ def job_fills(job) -> List[Tuple[Pattern, np.ndarray, FillOptions]]:
     names = {abi.FILL_EVEN_ODD: "even_odd", abi.FILL_NON_ZERO: "non_zero"}
     return [(Pattern.from_pixel(Pixel.rgba(*map(int, px[i]))), nodes[off[i]:off[i] + cnt[i]],
              FillOptions(fill_rule=names[int(rules[i])])) for i in range(len(off))]
+
+
+def glyph_path(rng: np.random.Generator, box: float = 64.0, cubics_lo: int = 20, cubics_hi: int = 200) -> np.ndarray:
+    """A glyph-like closed outline: 20-200 cubic Beziers whose control points
+    wander around an ellipse inside a box x box square (several subpaths
+    for counters are not modelled)."""
+    n = int(rng.integers(cubics_lo, cubics_hi + 1))
+    t = np.sort(rng.uniform(0.0, 2 * math.pi, n))
+    rx, ry = box * rng.uniform(0.25, 0.45), box * rng.uniform(0.25, 0.45)
+    cx, cy = box / 2, box / 2
+    wob = rng.uniform(0.6, 1.0, n)
+    ends = np.stack([cx + rx * wob * np.cos(t), cy + ry * wob * np.sin(t)], 1)
+    pts = [(abi.MOVE_TO, float(ends[-1, 0]), float(ends[-1, 1]))]
+    prev = ends[-1]
+    for k in range(n):
+        c1 = prev + rng.uniform(-box / 8, box / 8, 2)
+        c2 = ends[k] + rng.uniform(-box / 8, box / 8, 2)
+        pts.append((abi.CURVE_TO, *map(float, np.clip(c1, 0, box)), *map(float, np.clip(c2, 0, box)),
+                    float(ends[k, 0]), float(ends[k, 1])))
+        prev = ends[k]
+    return _path_nodes(pts)
