@@ -10,6 +10,7 @@
  *   z2dgpu_fill_batch  <- N x painter.fill, same surface src/painter.zig:66-143
  *                         (Context.fill loop, src/Context.zig:592-607)
  *   z2dgpu_fill_jobs   <- the same over many surfaces
+ *   z2dgpu_stroke      <- painter.stroke                src/painter.zig:214-344
  *   z2dgpu_composite   <- compositor.SurfaceCompositor.run
  *                                                       src/compositor.zig:302-309
  *                         (and Surface.composite,       src/surface.zig:225-241)
@@ -110,6 +111,10 @@ typedef struct z2d_surface {
 /* path nodes (src/internal/path_nodes.zig:9-14) */
 enum { Z2D_MOVE_TO = 0, Z2D_LINE_TO = 1, Z2D_CURVE_TO = 2, Z2D_CLOSE_PATH = 3 };
 
+/* options.JoinMode / options.CapMode (src/options.zig:40-70) */
+enum { Z2D_JOIN_MITER = 0, Z2D_JOIN_ROUND = 1, Z2D_JOIN_BEVEL = 2 };
+enum { Z2D_CAP_BUTT = 0, Z2D_CAP_ROUND = 1, Z2D_CAP_SQUARE = 2 };
+
 /* move_to/line_to: point = (p[0], p[1]).  curve_to: p1 = (p[0], p[1]),
  * p2 = (p[2], p[3]), p3 = (p[4], p[5]).  Device-space coordinates, as held
  * by z2d's Path after transformation and clamping. 56 bytes. */
@@ -207,6 +212,25 @@ typedef struct z2d_fill_cmd {
     z2d_fill_opts opts;
 } z2d_fill_cmd;
 
+/* painter.StrokeOptions (src/painter.zig:145-195).  Defaults: AA default,
+ * miter join, butt cap, line width 2, miter limit 10, tolerance 0.1,
+ * identity transformation, no dashes, no hairline, src_over, integer. */
+typedef struct z2d_stroke_opts {
+    int32_t anti_aliasing;     /* Z2D_AA_* */
+    int32_t line_join;         /* Z2D_JOIN_* */
+    int32_t line_cap;          /* Z2D_CAP_* */
+    int32_t op;                /* Z2D_OP_* */
+    int32_t precision;         /* Z2D_PRECISION_* */
+    int32_t hairline;          /* nonzero: hairline mode (not supported yet) */
+    double line_width;
+    double miter_limit;
+    double tolerance;
+    double dash_offset;
+    double transformation[6];  /* ax, by, cx, dy, tx, ty (Transformation.zig) */
+    const double *dashes;      /* dash array (not supported yet when valid) */
+    uint64_t n_dashes;
+} z2d_stroke_opts;
+
 /* one surface of a multi-surface batch: cmds[cmd_offset, cmd_offset+n_cmds)
  * of the batch command array, drawn in order on `surface` */
 typedef struct z2d_job {
@@ -259,6 +283,27 @@ Z2D_API int z2dgpu_fill(z2dgpu_ctx *ctx, z2d_surface *surface,
 Z2D_API int z2dgpu_fill_batch(z2dgpu_ctx *ctx, z2d_surface *surface,
                               const z2d_node *nodes, size_t n_nodes,
                               const z2d_fill_cmd *cmds, size_t n_cmds);
+
+/* painter.stroke (src/painter.zig:214-344): the stroke polygon is built on
+ * the host exactly as z2d's stroke plotter builds it (joins, caps, pens)
+ * and filled with the non-zero rule by the GPU rasterisers.  Dashes and
+ * hairline mode return Z2D_ERR_INVALID_ARGUMENT (not supported yet); a
+ * transformation that cannot be inverted also returns
+ * Z2D_ERR_INVALID_ARGUMENT (Transformation.Error.InvalidMatrix). */
+Z2D_API int z2dgpu_stroke(z2dgpu_ctx *ctx, z2d_surface *surface,
+                          const z2d_pattern *pattern, const z2d_node *nodes,
+                          size_t n_nodes, const z2d_stroke_opts *opts);
+
+/* Host only (no device work): the polygon painter.stroke would rasterise
+ * for a surface of `surface_format`, as closed contours of points already
+ * multiplied by the rasteriser scale (written to *scale).  points receives
+ * x, y pairs, contour_ends[k] the index one past contour k's last point.
+ * The counts are returned even when the capacities are too small. */
+Z2D_API int z2dgpu_stroke_contours(const z2d_node *nodes, size_t n_nodes,
+                                   const z2d_stroke_opts *opts, int32_t surface_format,
+                                   double *points, size_t cap_points, uint64_t *n_points,
+                                   uint64_t *contour_ends, size_t cap_contours,
+                                   uint64_t *n_contours, double *scale);
 
 /* Many independent surfaces in one device pass: for every job, the
  * equivalent of calling painter.fill for its commands in order on its

@@ -47,6 +47,10 @@ def load_oracle():
             lib.z2doracle_fill.argtypes = [C.POINTER(abi.z2d_surface), C.POINTER(abi.z2d_pattern),
                                            C.POINTER(abi.z2d_node), C.c_size_t, C.POINTER(abi.z2d_fill_opts)]
             lib.z2doracle_fill.restype = C.c_int
+            lib.z2doracle_fill_contours.argtypes = [C.POINTER(abi.z2d_surface), C.POINTER(abi.z2d_pattern),
+                                                    C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.c_size_t,
+                                                    C.POINTER(abi.z2d_fill_opts)]
+            lib.z2doracle_fill_contours.restype = C.c_int
             lib.z2doracle_composite.argtypes = [C.POINTER(abi.z2d_surface), C.c_int32, C.c_int32, C.c_int32,
                                                 C.POINTER(abi.z2d_operation), C.c_int32]
             lib.z2doracle_composite.restype = C.c_int
@@ -90,6 +94,20 @@ class Oracle:
         arr = nodes_to_abi(nodes)
         n = len(nodes)
         return self.lib.z2doracle_fill(C.byref(s), C.byref(p), arr, n, C.byref(opts.to_abi()))
+
+    def fill_contours(self, surface, pattern: Pattern, contours, opts: FillOptions = FillOptions()) -> int:
+        """The rasterisers on a polygon given as closed contours of
+        already-scaled points (a list of (n, 2) arrays)."""
+        import numpy as np
+        keep: list = []
+        s = _host_abi(surface)
+        p = pattern.to_abi(keep)
+        pts = np.ascontiguousarray(np.concatenate([np.asarray(c, np.float64).reshape(-1, 2) for c in contours])
+                                   if contours else np.zeros((1, 2)), dtype=np.float64)
+        ends = np.cumsum([len(c) for c in contours]).astype(np.uint64) if contours else np.zeros(1, np.uint64)
+        return self.lib.z2doracle_fill_contours(C.byref(s), C.byref(p), pts.ctypes.data_as(C.POINTER(C.c_double)),
+                                                ends.ctypes.data_as(C.POINTER(C.c_uint64)), len(contours),
+                                                C.byref(opts.to_abi()))
 
     def composite(self, dst, dst_x: int, dst_y: int, ops, precision: str = "integer") -> int:
         keep: list = []

@@ -1830,4 +1830,45 @@ __attribute__((visibility("default"))) z2d_pixel z2doracle_gradient_pixel(const 
     return z2d_pixel{Z2D_FORMAT_RGBA, (uint8_t)v.r, (uint8_t)v.g, (uint8_t)v.b, (uint8_t)v.a};
 }
 
+// The rasterisers of painter.fill / painter.stroke on a polygon given as
+// closed contours of already-scaled points (Polygon.addEdgesFromContour,
+// Polygon.zig:115-139, with the polygon's own scale of 1), as
+// painter.stroke hands its stroke polygon over (painter.zig:306-341).
+// contour_ends[k] is one past contour k's last point.
+__attribute__((visibility("default"))) int z2doracle_fill_contours(z2d_surface *surface, const z2d_pattern *pattern,
+                                                                   const double *points, const uint64_t *contour_ends,
+                                                                   size_t n_contours, const z2d_fill_opts *opts) {
+    if (!surface || !pattern || !opts || (n_contours && (!points || !contour_ends))) return Z2D_ERR_INVALID_ARGUMENT;
+    if (surface->width < 1 || surface->height < 1) return Z2D_ERR_INVALID_DIMENSIONS;
+    if (pattern->kind == Z2D_PATTERN_PIXEL && !pixel_premultiplied(pattern->pixel))
+        return Z2D_ERR_PIXEL_NOT_PREMULTIPLIED;
+    Sfc s = sfc_from_abi(surface);
+    const int aa = (s.fmt == Z2D_FORMAT_ALPHA1) ? Z2D_AA_NONE : opts->anti_aliasing;
+    Poly poly;
+    uint64_t start = 0;
+    for (size_t k = 0; k < n_contours; k++) {
+        const uint64_t end = contour_ends[k];
+        for (uint64_t i = start; i + 1 < end; i++)
+            poly.add_edge(Pt{points[2 * i], points[2 * i + 1]}, Pt{points[2 * i + 2], points[2 * i + 3]});
+        if (end > start)
+            poly.add_edge(Pt{points[2 * (end - 1)], points[2 * (end - 1) + 1]}, Pt{points[2 * start], points[2 * start + 1]});
+        start = end;
+    }
+    FillSrc pat;
+    pat.kind = pattern->kind;
+    const int pk = pattern->kind == Z2D_PATTERN_PIXEL      ? Z2D_PARAM_PIXEL
+                   : pattern->kind == Z2D_PATTERN_GRADIENT ? Z2D_PARAM_GRADIENT
+                                                           : Z2D_PARAM_DITHER;
+    pat.src = make_src_from_pattern(pk, *pattern);
+    if (poly.edges.empty()) return Z2D_OK;
+    if (!(std::isfinite(poly.el) && std::isfinite(poly.et) && std::isfinite(poly.er) && std::isfinite(poly.eb)))
+        return Z2D_ERR_INVALID_STATE;
+    switch (aa) {
+        case Z2D_AA_NONE: run_direct(s, pat, poly, opts->fill_rule, opts->op, opts->precision); break;
+        case Z2D_AA_SUPERSAMPLE_4X: run_ssaa(s, pat, poly, opts->fill_rule, opts->op, opts->precision); break;
+        default: run_msaa(s, pat, poly, opts->fill_rule, opts->op, opts->precision); break;
+    }
+    return Z2D_OK;
+}
+
 }  // extern "C"

@@ -27,3 +27,36 @@ class GpuBackend:
         except Z2DError as e:
             return e.code
         return abi.OK
+
+    def stroke(self, surface, pattern, nodes, opts):
+        try:
+            self.painter.stroke(surface, pattern, nodes, opts, ctx=self.ctx)
+        except Z2DError as e:
+            return e.code
+        return abi.OK
+
+
+class StrokeOracle:
+    """The oracle with painter.stroke: z2d's stroke polygon comes from the
+    library's host-side stroke builder (z2dgpu_stroke_contours, pinned to
+    z2d by the stroke scenes' golden PNGs) and is rasterised by the oracle."""
+
+    def __init__(self, oracle):
+        self.oracle = oracle
+
+    def fill(self, surface, pattern, nodes, opts):
+        return self.oracle.fill(surface, pattern, nodes, opts)
+
+    def composite(self, dst, x, y, ops, precision="integer"):
+        return self.oracle.composite(dst, x, y, ops, precision)
+
+    def stroke(self, surface, pattern, nodes, opts):
+        from z2d_gb300 import painter
+        from z2d_gb300.types import FillOptions
+        try:
+            contours, _ = painter.stroke_contours(nodes, opts, surface.format)
+        except Z2DError as e:
+            return e.code
+        aa = "none" if surface.format == abi.FORMAT_ALPHA1 else opts.anti_aliasing
+        fo = FillOptions(anti_aliasing=aa, fill_rule="non_zero", operator=opts.operator, precision=opts.precision)
+        return self.oracle.fill_contours(surface, pattern, contours, fo)

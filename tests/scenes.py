@@ -31,6 +31,10 @@ class Ctx:
         self.tolerance = 0.1
         self.dither = "none"
         self.transformation = (1.0, 0.0, 0.0, 1.0, 0.0, 0.0)
+        self.line_width = 2.0      # Context defaults (src/Context.zig:36-61)
+        self.line_join = "miter"
+        self.line_cap = "butt"
+        self.miter_limit = 10.0
         self.path = Path()
 
     def set_source(self, px: Pixel):
@@ -50,6 +54,17 @@ class Ctx:
 
     def reset_path(self):
         self.path.reset()
+
+    def stroke(self):
+        from z2d_gb300.types import StrokeOptions
+        pat = wrap_dither(self.pattern, self.dither, self.surface.format)
+        opts = StrokeOptions(anti_aliasing=self.aa, line_cap=self.line_cap, line_join=self.line_join,
+                             line_width=self.line_width, miter_limit=self.miter_limit, operator=self.operator,
+                             precision=self.precision, tolerance=self.tolerance,
+                             transformation=self.transformation)
+        rc = self.backend.stroke(self.surface, pat, self.path.nodes, opts)
+        if rc != abi.OK:
+            raise RuntimeError(f"stroke failed: {rc}")
 
     def fill(self):
         pat = wrap_dither(self.pattern, self.dither, self.surface.format)
@@ -364,6 +379,273 @@ def s061_linear_gradient(be, aa=None):
         _linear_draw(be, dst, scratch, *args)
     return dst
 
+
+# ------------------------------------------------------------- stroke scenes
+def _stroke_canvas(be, aa, w, h):
+    s = Surface.init("rgb", w, h)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    return s, c
+
+
+def s008_stroke_triangle(be, aa):
+    w = h = 300
+    s, c = _stroke_canvas(be, aa, w, h)
+    m = 10
+    c.move_to(0 + m, 0 + m)
+    c.line_to(w - m - 1, 0 + m)
+    c.line_to(w // 2 - 1, h - m - 1)
+    c.close_path()
+    c.stroke()
+    return s
+
+
+def s009_stroke_square(be, aa):
+    w = h = 300
+    s, c = _stroke_canvas(be, aa, w, h)
+    m = 50
+    c.move_to(0 + m, 0 + m)
+    c.line_to(w - m - 1, 0 + m)
+    c.line_to(w - m - 1, h - m - 1)
+    c.line_to(0 + m, h - m - 1)
+    c.close_path()
+    c.stroke()
+    return s
+
+
+def s010_stroke_trapezoid(be, aa):
+    w = h = 300
+    s, c = _stroke_canvas(be, aa, w, h)
+    mt, mb, my = 89, 50, 100
+    c.move_to(0 + mt, 0 + my)
+    c.line_to(w - mt - 1, 0 + my)
+    c.line_to(w - mb - 1, h - my - 1)
+    c.line_to(0 + mb, h - my - 1)
+    c.close_path()
+    c.stroke()
+    return s
+
+
+def _stroke_star(c, w, h):
+    m, xs, ys = 20, 3, 5
+    c.move_to(w // 2, 0 + m)
+    c.line_to(w - m * xs - 1, h - m - 1)
+    c.line_to(0 + m, 0 + m * ys)
+    c.line_to(w - m - 1, 0 + m * ys)
+    c.line_to(0 + m * xs, h - m - 1)
+    c.close_path()
+
+
+def s011_stroke_star(be, aa):
+    s, c = _stroke_canvas(be, aa, 300, 300)
+    c.line_width = 6
+    _stroke_star(c, 300, 300)
+    c.stroke()
+    return s
+
+
+def s017_stroke_star_round(be, aa):
+    s, c = _stroke_canvas(be, aa, 300, 300)
+    c.line_width = 10
+    c.line_join = "round"
+    _stroke_star(c, 300, 300)
+    c.stroke()
+    return s
+
+
+def s012_stroke_bezier(be, aa):
+    s, c = _stroke_canvas(be, aa, 300, 300)
+    c.move_to(19, 149)
+    c.curve_to(89, 0, 209, 0, 279, 149)
+    c.stroke()
+    c.line_width = 6
+    c.reset_path()
+    c.move_to(19, 199)
+    c.curve_to(89, 24, 209, 24, 279, 199)
+    c.stroke()
+    c.line_width = 10
+    c.reset_path()
+    c.move_to(19, 249)
+    c.curve_to(89, 49, 209, 49, 279, 249)
+    c.stroke()
+    return s
+
+
+def s014_stroke_lines(be, aa):
+    w, h = 800, 400
+    s, c = _stroke_canvas(be, aa, w, h)
+    sw, sh, m = w // 4, h // 2, 10
+    x, y = 0, 0
+    c.move_to(x + m, y + m)
+    c.line_to(x + sw - m - 1, y + sh - m - 1)
+    x = sw
+    c.move_to(x + m, y + sh - m - 1)
+    c.line_to(x + sw - m - 1, y + m)
+    x, y = 0, sh
+    c.move_to(x + sw - m - 1, y + m)
+    c.line_to(x + m, y + sh - m - 1)
+    x, y = sw, sh
+    c.move_to(x + sw - m - 1, y + sh - m - 1)
+    c.line_to(x + m, y + m)
+    x, y = sw * 2, 0
+    c.move_to(x + m, y + sh // 2)
+    c.line_to(x + sw - m - 1, y + sh // 2)
+    x, y = sw * 2, sh
+    c.move_to(x + sw // 2, y + m)
+    c.line_to(x + sw // 2, y + sh - m - 1)
+    x, y = sw * 3, 0
+    c.move_to(x + sw // 2, y + sh - m - 1)
+    c.line_to(x + sw // 2, y + m)
+    x, y = sw * 3, sh
+    c.move_to(x + sw - m - 1, y + sh // 2)
+    c.line_to(x + m, y + sh // 2)
+    c.stroke()
+    return s
+
+
+_SPIRAL = [(10, 10), (100, 20), (110, 120), (10, 110), (20, 30), (90, 40), (95, 100), (30, 95), (30, 50), (80, 50),
+           (75, 85), (45, 80), (50, 60), (65, 70)]
+
+
+def _spirals(c):
+    xo, yo = 120, 130
+    for fx, fy in ((False, False), (True, False), (False, True), (True, True)):
+        for i, (px, py) in enumerate(_SPIRAL):
+            x = (xo + 120 - px) if fx else px
+            y = (yo + 130 - py) if fy else py
+            (c.move_to if i == 0 else c.line_to)(x, y)
+
+
+def s015_stroke_miter(be, aa):
+    s, c = _stroke_canvas(be, aa, 240, 260)
+    c.line_width = 6
+    _spirals(c)
+    c.stroke()
+    return s
+
+
+def s018_stroke_square_spiral_round(be, aa):
+    s, c = _stroke_canvas(be, aa, 240, 260)
+    c.line_width = 10
+    c.line_join = "round"
+    _spirals(c)
+    c.stroke()
+    return s
+
+
+def s019_stroke_bevel_miterlimit(be, aa):
+    s, c = _stroke_canvas(be, aa, 375, 560)
+    c.line_width = 5
+    settings = [("bevel", 10.0), ("miter", 4.0), ("miter", 1.0), ("miter", 6.0), ("miter", 10.0)]
+    xs = [(10, 80, 150), (170, 205, 240), (260, 280, 300), (320, 327.5, 335), (355, 360, 365)]
+    for row, (join, limit) in enumerate(settings):
+        c.line_join = join
+        if join == "miter":
+            c.miter_limit = limit
+        c.reset_path()
+        y = 90 + 100 * row
+        for x0, x1, x2 in xs:
+            c.move_to(x0, y)
+            c.line_to(x1, y - 30)
+            c.line_to(x2, y)
+        c.stroke()
+    return s
+
+
+def _caps(be, aa, cap):
+    w, h = 800, 600
+    s, c = _stroke_canvas(be, aa, w, h)
+    c.line_cap = cap
+    if cap == "round":
+        c.line_join = "round"
+    c.line_width = 20
+    sw, m = w // 4, 30
+    sh = h / 3
+    x, y = 0.0, 0.0
+    c.move_to(x + m, y + m)
+    c.line_to(x + sw - m - 1, y + sh - m - 1)
+    x = sw
+    c.move_to(x + m, y + sh - m - 1)
+    c.line_to(x + sw - m - 1, y + m)
+    x, y = 0, sh
+    c.move_to(x + sw - m - 1, y + m)
+    c.line_to(x + m, y + sh - m - 1)
+    x, y = sw, sh
+    c.move_to(x + sw - m - 1, y + sh - m - 1)
+    c.line_to(x + m, y + m)
+    x, y = sw * 2, 0
+    c.move_to(x + m, y + sh / 2)
+    c.line_to(x + sw - m - 1, y + sh / 2)
+    x, y = sw * 2, sh
+    c.move_to(x + sw / 2, y + m)
+    c.line_to(x + sw / 2, y + sh - m - 1)
+    x, y = sw * 3, 0
+    c.move_to(x + sw / 2, y + sh - m - 1)
+    c.line_to(x + sw / 2, y + m)
+    x, y = sw * 3, sh
+    c.move_to(x + sw - m - 1, y + sh / 2)
+    c.line_to(x + m, y + sh / 2)
+    x, y = 0, sh * 2
+    c.move_to(x + m, y + m)
+    c.line_to(x + sw - m - 1, y + sh / 2 - 1)
+    c.line_to(x + m, y + sh - m - 1)
+    x = sw
+    c.move_to(x + sw - m - 1, y + m)
+    c.line_to(x + m, y + sh / 2 - 1)
+    c.line_to(x + sw - m - 1, y + sh - m - 1)
+    x = sw * 2
+    sh = sh / 2
+    c.move_to(x + m, y + m)
+    c.line_to(x + sw / 2 - 1, y + sh - m - 1)
+    c.line_to(x + sw - m - 1, y + m)
+    x = sw * 3
+    c.move_to(x + m, y + sh - m - 1)
+    c.line_to(x + sw / 2 - 1, y + m)
+    c.line_to(x + sw - m - 1, y + sh - m - 1)
+    x = sw * 2
+    y = y + sh
+    c.move_to(x + sw - m - 1, y + sh - m - 1)
+    c.line_to(x + sw / 2 - 1, y + m)
+    c.line_to(x + m, y + sh - m - 1)
+    x = sw * 3
+    c.move_to(x + sw - m - 1, y + m)
+    c.line_to(x + sw / 2 - 1, y + sh - m - 1)
+    c.line_to(x + m, y + m)
+    c.stroke()
+    c.set_source(Pixel.rgb(0xF3, 0x00, 0x00))
+    c.line_width = 1
+    c.stroke()
+    return s
+
+
+def s020_stroke_lines_round_caps(be, aa):
+    return _caps(be, aa, "round")
+
+
+def s021_stroke_lines_square_caps(be, aa):
+    return _caps(be, aa, "square")
+
+
+def s022_stroke_lines_butt_caps(be, aa):
+    return _caps(be, aa, "butt")
+
+
+STROKE_SCENES = {
+    "008_stroke_triangle": s008_stroke_triangle,
+    "009_stroke_square": s009_stroke_square,
+    "010_stroke_trapezoid": s010_stroke_trapezoid,
+    "011_stroke_star": s011_stroke_star,
+    "012_stroke_bezier": s012_stroke_bezier,
+    "014_stroke_lines": s014_stroke_lines,
+    "015_stroke_miter": s015_stroke_miter,
+    "017_stroke_star_round": s017_stroke_star_round,
+    "018_stroke_square_spiral_round": s018_stroke_square_spiral_round,
+    "019_stroke_bevel_miterlimit": s019_stroke_bevel_miterlimit,
+    "020_stroke_lines_round_caps": s020_stroke_lines_round_caps,
+    "021_stroke_lines_square_caps": s021_stroke_lines_square_caps,
+    "022_stroke_lines_butt_caps": s022_stroke_lines_butt_caps,
+}
 
 FILL_SCENES = {
     "003_fill_triangle": s003_fill_triangle,

@@ -1,0 +1,142 @@
+"""painter.stroke on the GPU (z2dgpu_stroke) against the oracle rasterising
+the same stroke polygon (StrokeOracle).  The polygon builder itself is
+pinned to z2d by the stroke scenes' golden PNGs (test_oracle_golden.py)."""
+import math
+
+import numpy as np
+import pytest
+
+from backends import GpuBackend, StrokeOracle
+from scenes import STROKE_SCENES
+from z2d_gb300 import abi
+from z2d_gb300.surface import Surface
+from z2d_gb300.types import Color, Gradient, Pattern, Pixel, StrokeOptions
+from z2d_gb300.workloads import premultiplied_background, random_path, random_premultiplied_pixel
+
+pytestmark = pytest.mark.gpu
+
+FLOAT_TOL = 1
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    return GpuBackend()
+
+
+def _cmp(a, b, tol, what):
+    d = np.abs(a.numpy().astype(np.int16) - b.numpy().astype(np.int16))
+    assert int(d.max(initial=0)) <= tol, f"{what}: {int((d > 0).sum())} bytes differ (max {int(d.max())})"
+
+
+def _bg(fmt, w, h, seed):
+    rng = np.random.default_rng(seed)
+    s = Surface.init(fmt, w, h)
+    if fmt in ("rgba", "argb"):
+        s.data[:] = premultiplied_background(rng, w, h)
+    elif fmt in ("rgb", "xrgb"):
+        d = rng.integers(0, 256, size=s.data.size, dtype=np.uint8)
+        d.reshape(-1, 4)[:, 3] = 0
+        s.data[:] = d
+    else:
+        s.data[:] = rng.integers(0, 256, size=s.data.size, dtype=np.uint8)
+    return s
+
+
+@pytest.mark.parametrize("aa", ["none", "multisample_4x", "supersample_4x"])
+@pytest.mark.parametrize("name", list(STROKE_SCENES))
+def test_stroke_scene(gpu, oracle, name, aa):
+    _cmp(STROKE_SCENES[name](gpu, aa), STROKE_SCENES[name](StrokeOracle(oracle), aa), 0, name)
+
+
+def _open_path(rng, w, h, n):
+    pts = [(abi.MOVE_TO, *rng.uniform([5, 5], [w - 5, h - 5]), 0, 0, 0, 0)]
+    for _ in range(n):
+        if rng.random() < 0.6:
+            pts.append((abi.LINE_TO, *rng.uniform([5, 5], [w - 5, h - 5]), 0, 0, 0, 0))
+        else:
+            pts.append((abi.CURVE_TO, *rng.uniform([5, 5, 5, 5, 5, 5], [w - 5, h - 5] * 3)))
+    return pts
+
+
+TRANSFORMS = {
+    "identity": (1, 0, 0, 1, 0, 0),
+    "scale": (1.5, 0, 0, 0.75, 3, -2),
+    "rotate": (math.cos(0.4), -math.sin(0.4), math.sin(0.4), math.cos(0.4), 0, 0),
+    "skew_flip": (1.0, 0.3, 0.2, -1.1, 0, 0),
+}
+
+
+@pytest.mark.parametrize("tf", list(TRANSFORMS))
+@pytest.mark.parametrize("join", ["miter", "round", "bevel"])
+@pytest.mark.parametrize("cap", ["butt", "round", "square"])
+def test_random_strokes(gpu, oracle, join, cap, tf):
+    rng = np.random.default_rng(hash((join, cap, tf)) & 0xFFFF)
+    w, h = 160, 120
+    a, b = _bg("rgba", w, h, 3), _bg("rgba", w, h, 3)
+    so = StrokeOracle(oracle)
+    for i in range(4):
+        nodes = _open_path(rng, w, h, int(rng.integers(1, 6)))
+        if i % 2:
+            nodes.append((abi.CLOSE_PATH, 0, 0, 0, 0, 0, 0))
+        opts = StrokeOptions(line_join=join, line_cap=cap, line_width=float(rng.choice([0.5, 1.5, 3.0, 7.0, 12.0])),
+                             miter_limit=float(rng.choice([1.0, 4.0, 10.0])), transformation=TRANSFORMS[tf],
+                             anti_aliasing=("default", "none", "supersample_4x")[i % 3])
+        pat = Pattern.from_pixel(random_premultiplied_pixel(rng))
+        assert gpu.stroke(a, pat, nodes, opts) == abi.OK
+        assert so.stroke(b, pat, nodes, opts) == abi.OK
+    _cmp(a, b, 0, f"{join}/{cap}/{tf}")
+
+
+@pytest.mark.parametrize("fmt", ["rgb", "alpha8", "alpha4", "alpha1"])
+@pytest.mark.parametrize("op", ["src_over", "src_in", "xor", "color_burn"])
+def test_stroke_formats_operators(gpu, oracle, fmt, op):
+    rng = np.random.default_rng(abi.OP[op] * 10 + len(fmt))
+    w, h = 97, 71
+    a, b = _bg(fmt, w, h, 5), _bg(fmt, w, h, 5)
+    g = Gradient.linear(0, 0, w, h)
+    g.add_stop(0.0, Color.rgb(1, 0.2, 0, 0.9))
+    g.add_stop(1.0, Color.rgb(0, 0.3, 1, 0.6))
+    so = StrokeOracle(oracle)
+    for i in range(3):
+        nodes = _open_path(rng, w, h, 3)
+        opts = StrokeOptions(line_join="round", line_cap="square", line_width=5.0, operator=op,
+                             precision="float" if i == 2 else "integer")
+        pat = Pattern.from_gradient(g) if i == 1 else Pattern.from_pixel(random_premultiplied_pixel(rng))
+        assert gpu.stroke(a, pat, nodes, opts) == abi.OK
+        assert so.stroke(b, pat, nodes, opts) == abi.OK
+    _cmp(a, b, FLOAT_TOL, f"{fmt}/{op}")
+
+
+def test_stroke_degenerate_paths(gpu, oracle):
+    so = StrokeOracle(oracle)
+    cases = [
+        [(abi.MOVE_TO, 20, 20, 0, 0, 0, 0), (abi.CLOSE_PATH, 0, 0, 0, 0, 0, 0)],                     # dot
+        [(abi.MOVE_TO, 20, 20, 0, 0, 0, 0), (abi.LINE_TO, 20, 20, 0, 0, 0, 0)],                      # zero length
+        [(abi.MOVE_TO, 10, 10, 0, 0, 0, 0), (abi.LINE_TO, 50, 10, 0, 0, 0, 0),
+         (abi.LINE_TO, 90, 10, 0, 0, 0, 0)],                                                           # colinear
+        [(abi.MOVE_TO, 10, 40, 0, 0, 0, 0), (abi.LINE_TO, 60, 40, 0, 0, 0, 0),
+         (abi.LINE_TO, 10, 40, 0, 0, 0, 0)],                                                           # reversal
+        [(abi.MOVE_TO, 30, 30, 0, 0, 0, 0), (abi.LINE_TO, 70, 60, 0, 0, 0, 0),
+         (abi.LINE_TO, 30, 30, 0, 0, 0, 0), (abi.CLOSE_PATH, 0, 0, 0, 0, 0, 0)],                     # closed back
+    ]
+    for cap in ("butt", "round", "square"):
+        for k, nodes in enumerate(cases):
+            a, b = _bg("rgba", 100, 80, k), _bg("rgba", 100, 80, k)
+            opts = StrokeOptions(line_cap=cap, line_join="round", line_width=9.0)
+            pat = Pattern.from_pixel(Pixel.rgba(200, 100, 50, 255))
+            assert gpu.stroke(a, pat, nodes, opts) == abi.OK
+            assert so.stroke(b, pat, nodes, opts) == abi.OK
+            _cmp(a, b, 0, f"case {k} {cap}")
+
+
+def test_stroke_errors(gpu):
+    s = Surface.init("rgba", 10, 10)
+    nodes = [(abi.MOVE_TO, 1, 1, 0, 0, 0, 0), (abi.LINE_TO, 8, 8, 0, 0, 0, 0)]
+    px = Pattern.from_pixel(Pixel.rgba(1, 2, 3, 4))
+    assert gpu.stroke(s, px, nodes, StrokeOptions(transformation=(1, 2, 2, 4, 0, 0))) == abi.ERR_INVALID_ARGUMENT
+    assert gpu.stroke(s, Pattern.from_pixel(Pixel.rgba(200, 2, 3, 4)), nodes,
+                      StrokeOptions()) == abi.ERR_PIXEL_NOT_PREMULTIPLIED
+    assert gpu.stroke(s, px, nodes, StrokeOptions(dashes=(2.0, 1.0))) == abi.ERR_INVALID_ARGUMENT
+    assert gpu.stroke(s, px, nodes, StrokeOptions(hairline=True)) == abi.ERR_INVALID_ARGUMENT
+    assert gpu.stroke(s, px, [], StrokeOptions()) == abi.OK
+    assert gpu.stroke(s, px, nodes, StrokeOptions(dashes=(0.0, 0.0))) == abi.OK  # invalid dashes: solid stroke

@@ -7,7 +7,8 @@ import numpy as np
 import pytest
 
 from pngio import export_pixels, golden_pixels
-from scenes import AA_SUFFIX, COMPOSITOR_SCENES, FILL_SCENES
+from backends import StrokeOracle
+from scenes import AA_SUFFIX, COMPOSITOR_SCENES, FILL_SCENES, STROKE_SCENES
 from z2d_gb300.types import Color, Pixel
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -20,6 +21,20 @@ def test_fill_scene_matches_golden(oracle, golden_dir, name, aa):
     if not os.path.exists(path):  # MSAA falls back to the SSAA golden (spec/main_spec.zig:786-800)
         path = os.path.join(golden_dir, name + "_smooth.png")
     got = export_pixels(FILL_SCENES[name](oracle, aa))
+    exp = golden_pixels(path)
+    assert got.shape == exp.shape
+    assert int((got != exp).any(-1).sum()) == 0
+
+
+@pytest.mark.parametrize("aa", list(AA_SUFFIX))
+@pytest.mark.parametrize("name", list(STROKE_SCENES))
+def test_stroke_scene_matches_golden(oracle, golden_dir, name, aa):
+    """Pins the host stroke builder (z2dgpu_stroke_contours) to z2d: its
+    polygons, rasterised by the oracle, reproduce the golden PNGs."""
+    path = os.path.join(golden_dir, name + AA_SUFFIX[aa] + ".png")
+    if not os.path.exists(path):
+        path = os.path.join(golden_dir, name + "_smooth.png")
+    got = export_pixels(STROKE_SCENES[name](StrokeOracle(oracle), aa))
     exp = golden_pixels(path)
     assert got.shape == exp.shape
     assert int((got != exp).any(-1).sum()) == 0

@@ -110,6 +110,17 @@ class z2d_fill_cmd(C.Structure):
                 ("n_nodes", C.c_uint64), ("opts", z2d_fill_opts)]
 
 
+JOIN_MITER, JOIN_ROUND, JOIN_BEVEL = 0, 1, 2
+CAP_BUTT, CAP_ROUND, CAP_SQUARE = 0, 1, 2
+
+
+class z2d_stroke_opts(C.Structure):
+    _fields_ = [("anti_aliasing", C.c_int32), ("line_join", C.c_int32), ("line_cap", C.c_int32), ("op", C.c_int32),
+                ("precision", C.c_int32), ("hairline", C.c_int32), ("line_width", C.c_double),
+                ("miter_limit", C.c_double), ("tolerance", C.c_double), ("dash_offset", C.c_double),
+                ("transformation", C.c_double * 6), ("dashes", C.POINTER(C.c_double)), ("n_dashes", C.c_uint64)]
+
+
 class z2d_job(C.Structure):
     _fields_ = [("surface", z2d_surface), ("cmd_offset", C.c_uint64), ("n_cmds", C.c_uint64)]
 
@@ -124,7 +135,8 @@ EXPORTED_SYMBOLS = [
     "z2dgpu_version", "z2dgpu_last_error", "z2dgpu_ctx_create", "z2dgpu_ctx_destroy",
     "z2dgpu_ctx_synchronize", "z2dgpu_ctx_launch_count", "z2dgpu_ctx_set_timing",
     "z2dgpu_ctx_kernel_ms", "z2dgpu_surface_bytes",
-    "z2dgpu_fill", "z2dgpu_fill_batch", "z2dgpu_fill_jobs", "z2dgpu_composite",
+    "z2dgpu_fill", "z2dgpu_fill_batch", "z2dgpu_fill_jobs", "z2dgpu_stroke", "z2dgpu_stroke_contours",
+    "z2dgpu_composite",
     "z2dgpu_composite_noalloc", "z2dgpu_server_create", "z2dgpu_server_submit", "z2dgpu_server_wait",
     "z2dgpu_server_stats", "z2dgpu_server_destroy",
 ]

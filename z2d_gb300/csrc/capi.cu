@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "fill.cuh"
+#include "stroke.h"
 #include "z2d_internal.h"
 
 namespace z2dg {
@@ -390,6 +391,7 @@ static int prepare_fills(const z2d_surface &s, int32_t job, const z2d_node *node
         F.precision = requires_float(F.op) ? Z2D_PRECISION_FLOAT : cm.opts.precision;
         F.tol = std::fmax(cm.opts.tolerance, 0.001);
         F.scale = F.aa == Z2D_AA_NONE ? 1.0 : 4.0;
+        F.edge_scale = F.scale;
         F.pattern_kind = cm.pattern->kind;
         const int pk = cm.pattern->kind == Z2D_PATTERN_PIXEL      ? Z2D_PARAM_PIXEL
                        : cm.pattern->kind == Z2D_PATTERN_GRADIENT ? Z2D_PARAM_GRADIENT
@@ -520,6 +522,135 @@ int fill_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_node *nod
     std::vector<int32_t> used_fill;
     compact_nodes(nodes, n_nodes, node_fill, fills, used, used_fill);
     return run_jobs(c, jobs, used.data(), (int32_t)used.size(), fills, used_fill, grads, grad_of_fill);
+}
+
+// ------------------------------------------------------------------ strokes
+// painter.stroke's option handling (painter.zig:221-304) and the stroke
+// polygon.  aa receives the anti-aliasing mode actually used.
+static int stroke_polygon(const z2d_node *nodes, size_t n_nodes, const z2d_stroke_opts &o, int32_t surface_format,
+                          int &aa, std::vector<std::vector<double>> &contours, double &scale) {
+    if (o.line_join < Z2D_JOIN_MITER || o.line_join > Z2D_JOIN_BEVEL || o.line_cap < Z2D_CAP_BUTT ||
+        o.line_cap > Z2D_CAP_SQUARE || o.anti_aliasing < Z2D_AA_NONE || o.anti_aliasing > Z2D_AA_SUPERSAMPLE_4X ||
+        !(o.line_width == o.line_width) || !(o.tolerance == o.tolerance) || (o.n_dashes > 0 && !o.dashes)) {
+        set_error("stroke options out of range");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    if (!stroke::transformation_invertible(o.transformation)) {
+        set_error("InvalidMatrix: the stroke transformation cannot be inverted");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    contours.clear();
+    aa = (surface_format == Z2D_FORMAT_ALPHA1) ? Z2D_AA_NONE : o.anti_aliasing;
+    scale = aa == Z2D_AA_NONE ? 1.0 : 4.0;
+    if (n_nodes == 0) return Z2D_OK;
+    if (!nodes) return Z2D_ERR_INVALID_ARGUMENT;
+    if (o.hairline) {
+        set_error("hairline strokes are not supported on the GPU path yet");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    bool dashed = false;  // Dasher.validate (Dasher.zig:15-26)
+    for (uint64_t i = 0; i < o.n_dashes; i++) {
+        if (o.dashes[i] < 0) {
+            dashed = false;
+            break;
+        }
+        if (o.dashes[i] > 0) dashed = true;
+    }
+    if (dashed) {
+        set_error("dashed strokes are not supported on the GPU path yet");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    for (size_t i = 0; i < n_nodes; i++)
+        if (nodes[i].tag < Z2D_MOVE_TO || nodes[i].tag > Z2D_CLOSE_PATH) {
+            set_error("node: bad tag");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+    const bool wide = o.line_width >= 2;
+    stroke::Options so;
+    so.cap = wide ? o.line_cap : Z2D_CAP_BUTT;
+    so.join = wide ? o.line_join : Z2D_JOIN_MITER;
+    so.miter_limit = wide ? o.miter_limit : 10.0;
+    for (int k = 0; k < 6; k++) so.ctm[k] = o.transformation[k];
+    so.scale = scale;
+    so.thickness = o.line_width >= 0.00390625 ? o.line_width : 0.00390625;
+    so.tolerance = std::fmax(o.tolerance, 0.001);
+    const int rc = stroke::plot(nodes, n_nodes, so, contours);
+    if (rc) set_error("InvalidState: stroke path node sequence");
+    return rc;
+}
+
+// The contours as path nodes for the fill pipeline: each one is
+// move_to + line_to for every further point + line_to back to the start +
+// close_path, so the edges are exactly Polygon.addEdgesFromContour's
+// (consecutive points, then last -> first) whatever the number of points.
+static void contours_to_nodes(const std::vector<std::vector<double>> &contours, std::vector<z2d_node> &out) {
+    out.clear();
+    for (const auto &c : contours) {
+        const size_t n = c.size() / 2;
+        if (n == 0) continue;
+        z2d_node nd;
+        memset(&nd, 0, sizeof(nd));
+        nd.tag = Z2D_MOVE_TO;
+        nd.p[0] = c[0];
+        nd.p[1] = c[1];
+        out.push_back(nd);
+        for (size_t k = 1; k <= n; k++) {
+            nd.tag = Z2D_LINE_TO;
+            nd.p[0] = c[2 * (k % n)];
+            nd.p[1] = c[2 * (k % n) + 1];
+            out.push_back(nd);
+        }
+        nd.tag = Z2D_CLOSE_PATH;
+        nd.p[0] = nd.p[1] = 0;
+        out.push_back(nd);
+    }
+}
+
+static int do_stroke(Ctx &c, z2d_surface *surface, const z2d_pattern *pattern, const z2d_node *nodes, size_t n_nodes,
+                     const z2d_stroke_opts &o) {
+    int rc = check_surface(surface);
+    if (rc) return rc;
+    if (pattern->kind == Z2D_PATTERN_PIXEL) {  // painter.zig:221-227
+        rc = check_pixel(pattern->pixel);
+        if (rc) return rc;
+        if (!pixel_premultiplied(pattern->pixel)) {
+            set_error("PixelSourceNotPreMultiplied");
+            return Z2D_ERR_PIXEL_NOT_PREMULTIPLIED;
+        }
+    }
+    std::vector<std::vector<double>> contours;
+    int aa = 0;
+    double scale = 1;
+    rc = stroke_polygon(nodes, n_nodes, o, surface->format, aa, contours, scale);
+    if (rc || n_nodes == 0) return rc;
+    std::vector<z2d_node> cn;
+    contours_to_nodes(contours, cn);
+    if (cn.empty()) return Z2D_OK;
+    z2d_fill_cmd cmd;
+    cmd.pattern = pattern;
+    cmd.node_offset = 0;
+    cmd.n_nodes = cn.size();
+    cmd.opts.anti_aliasing = aa;
+    cmd.opts.fill_rule = Z2D_FILL_NON_ZERO;  // painter.zig:306-341
+    cmd.opts.op = o.op;
+    cmd.opts.precision = o.precision;
+    cmd.opts.tolerance = o.tolerance;
+    std::vector<FillCmd> fills;
+    std::vector<int32_t> node_fill(cn.size(), -1), grad_of_fill;
+    std::vector<DevGradient> grads;
+    rc = prepare_fills(*surface, 0, cn.data(), cn.size(), &cmd, 1, fills, node_fill, grads, grad_of_fill);
+    if (rc || fills.empty()) return rc;
+    fills[0].edge_scale = 1.0;  // contour points are already scaled
+    std::vector<DevJob> jobs(1);
+    memset(jobs.data(), 0, sizeof(DevJob));
+    rc = stage_in(c, *surface, c.surface, jobs[0].sfc);
+    if (rc) return rc;
+    jobs[0].fill0 = 0;
+    jobs[0].fill1 = 1;
+    const DevSurface ds = jobs[0].sfc;
+    rc = run_jobs(c, jobs, cn.data(), (int32_t)cn.size(), fills, node_fill, grads, grad_of_fill);
+    if (rc) return rc;
+    return stage_out(c, *surface, ds);
 }
 
 // SurfaceCompositor.run's precision upgrade and bounds
@@ -709,6 +840,37 @@ Z2D_API int z2dgpu_fill_batch(z2dgpu_ctx *c, z2d_surface *surface, const z2d_nod
     if (!c) return Z2D_ERR_INVALID_ARGUMENT;
     Z2D_CUDA(cudaSetDevice(c->device));
     return do_fill_batch(*c, surface, nodes, n_nodes, cmds, n_cmds);
+}
+
+Z2D_API int z2dgpu_stroke(z2dgpu_ctx *c, z2d_surface *surface, const z2d_pattern *pattern, const z2d_node *nodes,
+                          size_t n_nodes, const z2d_stroke_opts *opts) {
+    if (!c || !pattern || !opts) return Z2D_ERR_INVALID_ARGUMENT;
+    Z2D_CUDA(cudaSetDevice(c->device));
+    return do_stroke(*c, surface, pattern, nodes, n_nodes, *opts);
+}
+
+Z2D_API int z2dgpu_stroke_contours(const z2d_node *nodes, size_t n_nodes, const z2d_stroke_opts *opts,
+                                   int32_t surface_format, double *points, size_t cap_points, uint64_t *n_points,
+                                   uint64_t *contour_ends, size_t cap_contours, uint64_t *n_contours, double *scale) {
+    if (!opts) return Z2D_ERR_INVALID_ARGUMENT;
+    std::vector<std::vector<double>> contours;
+    int aa = 0;
+    double sc = 1;
+    const int rc = stroke_polygon(nodes, n_nodes, *opts, surface_format, aa, contours, sc);
+    if (rc) return rc;
+    uint64_t np = 0, nc = 0;
+    for (const auto &cn : contours) {
+        for (size_t k = 0; k < cn.size(); k++) {
+            if (points && np * 2 + k < cap_points * 2) points[np * 2 + k] = cn[k];
+        }
+        np += cn.size() / 2;
+        if (contour_ends && nc < cap_contours) contour_ends[nc] = np;
+        nc++;
+    }
+    if (n_points) *n_points = np;
+    if (n_contours) *n_contours = nc;
+    if (scale) *scale = sc;
+    return Z2D_OK;
 }
 
 Z2D_API int z2dgpu_fill_jobs(z2dgpu_ctx *c, const z2d_job *jobs, size_t n_jobs, const z2d_node *nodes, size_t n_nodes,

@@ -384,7 +384,7 @@ __global__ void k_fill_scan(const z2d_node *__restrict__ nodes, const FillCmd *_
 __device__ __forceinline__ void add_edge(const FillCmd &F, DEdge *out, double x0, double y0, double x1, double y1,
                                          double &et, double &eb, double &el, double &er, bool &any) {
     // Polygon.addEdge (Polygon.zig:61-109)
-    const double ax = x0 * F.scale, ay = y0 * F.scale, bx = x1 * F.scale, by = y1 * F.scale;
+    const double ax = x0 * F.edge_scale, ay = y0 * F.edge_scale, bx = x1 * F.edge_scale, by = y1 * F.edge_scale;
     DEdge e;
     if (ay < by) {
         e.top = ay;

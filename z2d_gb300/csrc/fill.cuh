@@ -24,7 +24,9 @@ struct FillCmd {
     int32_t fast_kind;  // FAST_* specialisation the rasteriser may use
     int32_t job;        // index of the surface (job) the fill draws on
     double tol;         // max(tolerance, 0.001) (painter.zig:103)
-    double scale;       // 4 for multisample, 1 for none (painter.zig:93-97)
+    double scale;       // 4 for multisample / supersample, 1 for none (painter.zig:93-97)
+    double edge_scale;  // multiplier of node coordinates in Polygon.addEdge: scale, or 1 for
+                        // stroke contours whose points are already scaled
     DevSrc src;         // the pattern as a compositor source
     Px px_paint;        // pattern pixel converted to the surface format (paintStride)
     I16 px_rgba;        // RGBA.fromPixel lanes of the pattern pixel (compositeStride)

@@ -1,0 +1,36 @@
+// stroke.h -- painter.stroke's polygon builder (stroke.cpp).
+#pragma once
+#include <stddef.h>
+
+#include <vector>
+
+#include "../../include/z2dgpu.h"
+
+namespace z2dg {
+namespace stroke {
+
+enum { kJoinMiter = Z2D_JOIN_MITER, kJoinRound = Z2D_JOIN_ROUND, kJoinBevel = Z2D_JOIN_BEVEL };
+enum { kCapButt = Z2D_CAP_BUTT, kCapRound = Z2D_CAP_ROUND, kCapSquare = Z2D_CAP_SQUARE };
+enum { kErrInvalidState = Z2D_ERR_INVALID_STATE };
+
+// stroke_plotter.PlotterOptions (stroke_plotter.zig:28-38), after
+// painter.stroke's adjustments (painter.zig:286-304).
+struct Options {
+    int cap, join;
+    double ctm[6];  // ax, by, cx, dy, tx, ty
+    double miter_limit;
+    double scale;
+    double thickness;
+    double tolerance;
+};
+
+// Transformation.inverse succeeds (painter.zig:231).
+bool transformation_invertible(const double m[6]);
+
+// stroke_plotter.plot: the closed contours (x, y pairs, already multiplied
+// by opts.scale) whose edges form the stroke polygon, in the order z2d adds
+// them.  Returns Z2D_OK or an error code.
+int plot(const z2d_node *nodes, size_t n_nodes, const Options &opts, std::vector<std::vector<double>> &contours);
+
+}  // namespace stroke
+}  // namespace z2dg

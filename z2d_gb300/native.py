@@ -68,6 +68,13 @@ def load(build_if_missing: bool = True):
                                     P(abi.z2d_fill_opts)]
         lib.z2dgpu_fill_batch.argtypes = [C.c_void_p, P(abi.z2d_surface), P(abi.z2d_node), C.c_size_t,
                                           P(abi.z2d_fill_cmd), C.c_size_t]
+        lib.z2dgpu_stroke.argtypes = [C.c_void_p, P(abi.z2d_surface), P(abi.z2d_pattern), P(abi.z2d_node), C.c_size_t,
+                                      P(abi.z2d_stroke_opts)]
+        lib.z2dgpu_stroke_contours.argtypes = [P(abi.z2d_node), C.c_size_t, P(abi.z2d_stroke_opts), C.c_int32,
+                                               P(C.c_double), C.c_size_t, P(C.c_uint64), P(C.c_uint64), C.c_size_t,
+                                               P(C.c_uint64), P(C.c_double)]
+        lib.z2dgpu_stroke.restype = C.c_int
+        lib.z2dgpu_stroke_contours.restype = C.c_int
         lib.z2dgpu_fill_jobs.argtypes = [C.c_void_p, P(abi.z2d_job), C.c_size_t, P(abi.z2d_node), C.c_size_t,
                                          P(abi.z2d_fill_cmd), C.c_size_t]
         lib.z2dgpu_composite.argtypes = [C.c_void_p, P(abi.z2d_surface), C.c_int32, C.c_int32, C.c_int32,

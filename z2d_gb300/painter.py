@@ -104,3 +104,45 @@ def fill_jobs_arrays(jarr, nodes: np.ndarray, cmds, ctx: Optional[Context] = Non
     ctx = ctx or default_context()
     check(ctx.lib.z2dgpu_fill_jobs(ctx.handle, jarr, len(jarr), nodes.ctypes.data_as(C.POINTER(abi.z2d_node)),
                                    len(nodes), cmds, len(cmds)))
+
+
+def stroke(surface, pattern: Pattern, nodes, opts: Optional["StrokeOptions"] = None,
+           ctx: Optional[Context] = None) -> None:
+    """painter.stroke (src/painter.zig:214-344): the stroke polygon is built
+    on the host like z2d's stroke plotter, then filled on the GPU."""
+    from .types import StrokeOptions
+    ctx = ctx or default_context()
+    opts = opts or StrokeOptions()
+    keep: list = []
+    arr = nodes_to_abi(nodes)
+    s = surface.to_abi()
+    p = pattern.to_abi(keep)
+    o = opts.to_abi(keep)
+    check(ctx.lib.z2dgpu_stroke(ctx.handle, C.byref(s), C.byref(p), arr, len(arr), C.byref(o)))
+
+
+def stroke_contours(nodes, opts: Optional["StrokeOptions"] = None, surface_format="rgba"):
+    """The stroke polygon painter.stroke rasterises on a surface of
+    `surface_format`: (list of (n, 2) arrays of already-scaled points, one
+    per closed contour, and the rasteriser scale).  Host only."""
+    from .native import load
+    from .types import StrokeOptions, _fmt
+    lib = load()
+    opts = opts or StrokeOptions()
+    keep: list = []
+    arr = nodes_to_abi(nodes)
+    o = opts.to_abi(keep)
+    npts, nc, sc = C.c_uint64(), C.c_uint64(), C.c_double()
+    fmt = _fmt(surface_format)
+    check(lib.z2dgpu_stroke_contours(arr, len(arr), C.byref(o), fmt, None, 0, C.byref(npts), None, 0, C.byref(nc),
+                                     C.byref(sc)))
+    pts = np.zeros(max(1, npts.value) * 2, np.float64)
+    ends = np.zeros(max(1, nc.value), np.uint64)
+    check(lib.z2dgpu_stroke_contours(arr, len(arr), C.byref(o), fmt, pts.ctypes.data_as(C.POINTER(C.c_double)),
+                                     npts.value, C.byref(npts), ends.ctypes.data_as(C.POINTER(C.c_uint64)), nc.value,
+                                     C.byref(nc), C.byref(sc)))
+    out, start = [], 0
+    for e in ends[:nc.value]:
+        out.append(pts[2 * start:2 * int(e)].reshape(-1, 2).copy())
+        start = int(e)
+    return out, sc.value

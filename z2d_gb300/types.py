@@ -295,6 +295,46 @@ class FillOptions:
         return o
 
 
+@dataclass
+class StrokeOptions:
+    """painter.StrokeOptions (src/painter.zig:145-195)."""
+    anti_aliasing: str = "default"
+    dashes: Sequence[float] = ()
+    dash_offset: float = 0.0
+    line_cap: str = "butt"
+    line_join: str = "miter"
+    line_width: float = 2.0
+    miter_limit: float = 10.0
+    operator: Union[str, int] = "src_over"
+    precision: str = "integer"
+    tolerance: float = 0.1
+    transformation: Sequence[float] = (1.0, 0.0, 0.0, 1.0, 0.0, 0.0)  # ax, by, cx, dy, tx, ty
+    hairline: bool = False
+
+    def to_abi(self, keep: list) -> abi.z2d_stroke_opts:
+        o = abi.z2d_stroke_opts()
+        o.anti_aliasing = {"none": abi.AA_NONE, "default": abi.AA_DEFAULT,
+                           "multisample_4x": abi.AA_MULTISAMPLE_4X,
+                           "supersample_4x": abi.AA_SUPERSAMPLE_4X}[self.anti_aliasing]
+        o.line_join = {"miter": abi.JOIN_MITER, "round": abi.JOIN_ROUND, "bevel": abi.JOIN_BEVEL}[self.line_join]
+        o.line_cap = {"butt": abi.CAP_BUTT, "round": abi.CAP_ROUND, "square": abi.CAP_SQUARE}[self.line_cap]
+        o.op = _op(self.operator)
+        o.precision = {"integer": abi.PRECISION_INTEGER, "float": abi.PRECISION_FLOAT}[self.precision]
+        o.hairline = 1 if self.hairline else 0
+        o.line_width = float(self.line_width)
+        o.miter_limit = float(self.miter_limit)
+        o.tolerance = float(self.tolerance)
+        o.dash_offset = float(self.dash_offset)
+        for i, v in enumerate(self.transformation):
+            o.transformation[i] = float(v)
+        if len(self.dashes):
+            arr = (C.c_double * len(self.dashes))(*map(float, self.dashes))
+            keep.append(arr)
+            o.dashes = C.cast(arr, C.POINTER(C.c_double))
+            o.n_dashes = len(self.dashes)
+        return o
+
+
 # --------------------------------------------------------------------------
 # Compositor operations          SurfaceCompositor.Operation (compositor.zig:223-284)
 # --------------------------------------------------------------------------
