@@ -227,7 +227,7 @@ typedef struct z2d_stroke_opts {
     double tolerance;
     double dash_offset;
     double transformation[6];  /* ax, by, cx, dy, tx, ty (Transformation.zig) */
-    const double *dashes;      /* dash array (not supported yet when valid) */
+    const double *dashes;      /* dash array (Dasher.zig); ignored unless it has a positive entry and no negative one */
     uint64_t n_dashes;
 } z2d_stroke_opts;
 
@@ -286,8 +286,9 @@ Z2D_API int z2dgpu_fill_batch(z2dgpu_ctx *ctx, z2d_surface *surface,
 
 /* painter.stroke (src/painter.zig:214-344): the stroke polygon is built on
  * the host exactly as z2d's stroke plotter builds it (joins, caps, pens)
- * and filled with the non-zero rule by the GPU rasterisers.  Dashes and
- * hairline mode return Z2D_ERR_INVALID_ARGUMENT (not supported yet); a
+ * and filled with the non-zero rule by the GPU rasterisers (dashes
+ * included).  Hairline mode returns Z2D_ERR_INVALID_ARGUMENT (not supported
+ * yet); a
  * transformation that cannot be inverted also returns
  * Z2D_ERR_INVALID_ARGUMENT (Transformation.Error.InvalidMatrix). */
 Z2D_API int z2dgpu_stroke(z2dgpu_ctx *ctx, z2d_surface *surface,

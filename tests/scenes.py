@@ -35,6 +35,7 @@ class Ctx:
         self.line_join = "miter"
         self.line_cap = "butt"
         self.miter_limit = 10.0
+        self.dashes = ()
         self.path = Path()
 
     def set_source(self, px: Pixel):
@@ -61,7 +62,7 @@ class Ctx:
         opts = StrokeOptions(anti_aliasing=self.aa, line_cap=self.line_cap, line_join=self.line_join,
                              line_width=self.line_width, miter_limit=self.miter_limit, operator=self.operator,
                              precision=self.precision, tolerance=self.tolerance,
-                             transformation=self.transformation)
+                             transformation=self.transformation, dashes=self.dashes)
         rc = self.backend.stroke(self.surface, pat, self.path.nodes, opts)
         if rc != abi.OK:
             raise RuntimeError(f"stroke failed: {rc}")
@@ -631,6 +632,72 @@ def s022_stroke_lines_butt_caps(be, aa):
     return _caps(be, aa, "butt")
 
 
+def _lines(c, w, h):
+    sw, sh, m = w // 4, h // 2, 10
+    c.move_to(m, m)
+    c.line_to(sw - m - 1, sh - m - 1)
+    c.move_to(sw + m, sh - m - 1)
+    c.line_to(sw + sw - m - 1, m)
+    c.move_to(sw - m - 1, sh + m)
+    c.line_to(m, sh + sh - m - 1)
+    c.move_to(sw + sw - m - 1, sh + sh - m - 1)
+    c.line_to(sw + m, sh + m)
+    c.move_to(sw * 2 + m, sh // 2)
+    c.line_to(sw * 2 + sw - m - 1, sh // 2)
+    c.move_to(sw * 2 + sw // 2, sh + m)
+    c.line_to(sw * 2 + sw // 2, sh + sh - m - 1)
+    c.move_to(sw * 3 + sw // 2, sh - m - 1)
+    c.line_to(sw * 3 + sw // 2, m)
+    c.move_to(sw * 3 + sw - m - 1, sh + sh // 2)
+    c.line_to(sw * 3 + m, sh + sh // 2)
+
+
+def s054_stroke_lines_dashed(be, aa):
+    s, c = _stroke_canvas(be, aa, 800, 400)
+    c.dashes = (10, 5)
+    _lines(c, 800, 400)
+    c.stroke()
+    return s
+
+
+def s055_stroke_miter_dashed(be, aa):
+    s, c = _stroke_canvas(be, aa, 240, 260)
+    c.dashes = (15, 5)
+    _spirals(c)
+    c.stroke()
+    return s
+
+
+def s056_stroke_star_dashed(be, aa):
+    s, c = _stroke_canvas(be, aa, 300, 300)
+    c.line_width = 6
+    c.dashes = (12, 3)
+    _stroke_star(c, 300, 300)
+    c.stroke()
+    return s
+
+
+def s057_stroke_bezier_dashed(be, aa):
+    s, c = _stroke_canvas(be, aa, 300, 300)
+    c.dashes = (6, 2)
+    c.move_to(19, 149)
+    c.curve_to(89, 0, 209, 0, 279, 149)
+    c.stroke()
+    c.line_width = 6
+    c.dashes = (18, 6)
+    c.reset_path()
+    c.move_to(19, 199)
+    c.curve_to(89, 24, 209, 24, 279, 199)
+    c.stroke()
+    c.line_width = 10
+    c.dashes = (30, 10)
+    c.reset_path()
+    c.move_to(19, 249)
+    c.curve_to(89, 49, 209, 49, 279, 249)
+    c.stroke()
+    return s
+
+
 STROKE_SCENES = {
     "008_stroke_triangle": s008_stroke_triangle,
     "009_stroke_square": s009_stroke_square,
@@ -645,6 +712,10 @@ STROKE_SCENES = {
     "020_stroke_lines_round_caps": s020_stroke_lines_round_caps,
     "021_stroke_lines_square_caps": s021_stroke_lines_square_caps,
     "022_stroke_lines_butt_caps": s022_stroke_lines_butt_caps,
+    "054_stroke_lines_dashed": s054_stroke_lines_dashed,
+    "055_stroke_miter_dashed": s055_stroke_miter_dashed,
+    "056_stroke_star_dashed": s056_stroke_star_dashed,
+    "057_stroke_bezier_dashed": s057_stroke_bezier_dashed,
 }
 
 FILL_SCENES = {

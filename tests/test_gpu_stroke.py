@@ -136,7 +136,27 @@ def test_stroke_errors(gpu):
     assert gpu.stroke(s, px, nodes, StrokeOptions(transformation=(1, 2, 2, 4, 0, 0))) == abi.ERR_INVALID_ARGUMENT
     assert gpu.stroke(s, Pattern.from_pixel(Pixel.rgba(200, 2, 3, 4)), nodes,
                       StrokeOptions()) == abi.ERR_PIXEL_NOT_PREMULTIPLIED
-    assert gpu.stroke(s, px, nodes, StrokeOptions(dashes=(2.0, 1.0))) == abi.ERR_INVALID_ARGUMENT
     assert gpu.stroke(s, px, nodes, StrokeOptions(hairline=True)) == abi.ERR_INVALID_ARGUMENT
     assert gpu.stroke(s, px, [], StrokeOptions()) == abi.OK
     assert gpu.stroke(s, px, nodes, StrokeOptions(dashes=(0.0, 0.0))) == abi.OK  # invalid dashes: solid stroke
+
+
+@pytest.mark.parametrize("dashes,offset", [((10.0, 5.0), 0.0), ((3.0, 1.0, 0.0, 2.0), 1.5), ((7.0,), -2.0),
+                                           ((0.0, 4.0), 0.0), ((2.5, 2.5), 40.0)])
+@pytest.mark.parametrize("cap", ["butt", "round", "square"])
+def test_dashed_strokes(gpu, oracle, dashes, offset, cap):
+    rng = np.random.default_rng(int(sum(dashes) * 10 + offset * 3) + len(cap))
+    w, h = 150, 110
+    a, b = _bg("rgba", w, h, 7), _bg("rgba", w, h, 7)
+    so = StrokeOracle(oracle)
+    for i in range(4):
+        nodes = _open_path(rng, w, h, int(rng.integers(1, 6)))
+        if i % 2:
+            nodes.append((abi.CLOSE_PATH, 0, 0, 0, 0, 0, 0))
+        opts = StrokeOptions(line_cap=cap, line_join=("miter", "round", "bevel")[i % 3], line_width=4.0 + i,
+                             dashes=dashes, dash_offset=offset,
+                             transformation=TRANSFORMS[("identity", "scale", "rotate", "skew_flip")[i]])
+        pat = Pattern.from_pixel(random_premultiplied_pixel(rng))
+        assert gpu.stroke(a, pat, nodes, opts) == abi.OK
+        assert so.stroke(b, pat, nodes, opts) == abi.OK
+    _cmp(a, b, 0, f"{dashes}/{offset}/{cap}")

@@ -548,18 +548,11 @@ static int stroke_polygon(const z2d_node *nodes, size_t n_nodes, const z2d_strok
         set_error("hairline strokes are not supported on the GPU path yet");
         return Z2D_ERR_INVALID_ARGUMENT;
     }
-    bool dashed = false;  // Dasher.validate (Dasher.zig:15-26)
-    for (uint64_t i = 0; i < o.n_dashes; i++) {
-        if (o.dashes[i] < 0) {
-            dashed = false;
-            break;
+    for (uint64_t i = 0; i < o.n_dashes; i++)
+        if (!(o.dashes[i] == o.dashes[i]) || !(o.dash_offset == o.dash_offset)) {
+            set_error("stroke dashes must be numbers");
+            return Z2D_ERR_INVALID_ARGUMENT;
         }
-        if (o.dashes[i] > 0) dashed = true;
-    }
-    if (dashed) {
-        set_error("dashed strokes are not supported on the GPU path yet");
-        return Z2D_ERR_INVALID_ARGUMENT;
-    }
     for (size_t i = 0; i < n_nodes; i++)
         if (nodes[i].tag < Z2D_MOVE_TO || nodes[i].tag > Z2D_CLOSE_PATH) {
             set_error("node: bad tag");
@@ -574,6 +567,9 @@ static int stroke_polygon(const z2d_node *nodes, size_t n_nodes, const z2d_strok
     so.scale = scale;
     so.thickness = o.line_width >= 0.00390625 ? o.line_width : 0.00390625;
     so.tolerance = std::fmax(o.tolerance, 0.001);
+    so.dashes = o.dashes;
+    so.n_dashes = (size_t)o.n_dashes;
+    so.dash_offset = o.dash_offset;
     const int rc = stroke::plot(nodes, n_nodes, so, contours);
     if (rc) set_error("InvalidState: stroke path node sequence");
     return rc;

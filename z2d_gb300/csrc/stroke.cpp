@@ -347,23 +347,92 @@ struct PointBuffer {
     Pt tail(size_t n) const { return items[len - n]; }
 };
 
-struct Plotter {
+// The contours and clockwise state of one polygon under construction: the
+// plotter's own, or the saved first dash of a closed dashed path (the
+// InitialPolygon of dashed_plotter.zig:54-64).
+struct Side {
+    Contour outer, inner;
+    int clockwise = -1;  // -1: unset (null)
+    void set_scale(double sc) { outer.scale = inner.scale = sc; }
+};
+
+// Dasher.zig
+struct Dasher {
+    const double *dashes = nullptr;
+    size_t n = 0;
+    double offset = 0;
+    size_t idx = 0;
+    bool on = true;
+    double remain = 0;
+    void init(const double *d, size_t count, double off) {
+        dashes = d;
+        n = count;
+        offset = off;
+        reset();
+    }
+    bool stuck = false;  // the offset did not settle (guard; z2d would loop)
+    void apply_offset() {  // Dasher.applyOffset (Dasher.zig:40-54)
+        remain -= offset;
+        int64_t guard = 0;
+        while (remain < 0 || remain > dashes[idx]) {
+            if (++guard > (int64_t)1 << 26) {
+                stuck = true;
+                return;
+            }
+            if (remain < 0) {
+                remain += dashes[idx];
+                idx = (idx >= n - 1) ? 0 : idx + 1;
+            } else {
+                remain -= dashes[idx];
+                idx = (idx == 0) ? n - 1 : idx - 1;
+            }
+            on = !on;
+        }
+    }
+    void reset() {
+        idx = 0;
+        on = true;
+        remain = dashes[0];
+        apply_offset();
+    }
+    bool step(double len) {  // Dasher.step (Dasher.zig:63-76)
+        bool stepped = false;
+        remain -= len;
+        if (remain <= 0) {
+            stepped = true;
+            on = !on;
+            idx += 1;
+            if (idx >= n) idx = 0;
+            remain = dashes[idx];
+        }
+        return stepped;
+    }
+};
+// Dasher.validate (Dasher.zig:15-26)
+bool dashes_valid(const double *d, size_t n) {
+    bool valid = false;
+    for (size_t i = 0; i < n; i++) {
+        if (d[i] < 0) return false;
+        if (d[i] > 0) valid = true;
+    }
+    return valid;
+}
+
+// What both plotters share: options, pen, the result and the polygon
+// pieces of stroke_plotter.zig that operate on a Side.
+struct Common {
     const Options &o;
     Tf ctm;
     Pen pen;
-    PointBuffer points;
-    int clockwise = -1;  // -1: unset
-    Contour outer, inner;
     std::vector<std::vector<double>> &result;
     int error = 0;
 
-    Plotter(const Options &opts, std::vector<std::vector<double>> &res) : o(opts), result(res) {
+    Common(const Options &opts, std::vector<std::vector<double>> &res) : o(opts), result(res) {
         ctm = Tf{o.ctm[0], o.ctm[1], o.ctm[2], o.ctm[3], o.ctm[4], o.ctm[5]};
-        outer.scale = inner.scale = o.scale;
         if (o.join == kJoinRound || o.cap == kCapRound) pen = make_pen(o.thickness, o.tolerance, ctm);
     }
 
-    // Polygon.addEdgesFromContour: the contour's points, closed by the caller
+    // Polygon.addEdgesFromContour: the contour's points, closed later
     void emit(const Contour &c) {
         std::vector<double> pts;
         pts.reserve(c.pts.size() * 2);
@@ -373,39 +442,34 @@ struct Plotter {
         }
         result.push_back(std::move(pts));
     }
-    void reset_outer() {
-        outer.pts.clear();
-        clockwise = -1;
-    }
 
     // join (stroke_plotter.zig:405-545)
-    void join(int mode, Pt p0, Pt p1, Pt p2, bool use_before, Contour::It before_outer) {
+    void join(Side &sd, int mode, Pt p0, Pt p1, Pt p2, bool use_before, Contour::It before_outer) {
         if (eq(p0, p1) || eq(p1, p2)) {
-            if (clockwise < 0) clockwise = 0;
+            if (sd.clockwise < 0) sd.clockwise = 0;
             return;
         }
         const Face in = face_init(p0, p1, o.thickness, ctm);
         const Face out = face_init(p1, p2, o.thickness, ctm);
         const bool jcw = compare(in.dev_slope, out.dev_slope) < 0;
-        const bool pcw = clockwise >= 0 ? clockwise != 0 : jcw;
+        const bool pcw = sd.clockwise >= 0 ? sd.clockwise != 0 : jcw;
         const bool switched = jcw != pcw;
+        auto to_outer = [&](Pt p) {
+            if (use_before) sd.outer.plot(p, before_outer);
+            else sd.outer.plot(p);
+        };
         auto plot_outer = [&](Pt p) {
-            if (switched) inner.plot_reverse(p);
-            else if (use_before) outer.plot(p, before_outer);
-            else outer.plot(p);
+            if (switched) sd.inner.plot_reverse(p);
+            else to_outer(p);
         };
         auto plot_inner = [&](Pt p) {
-            if (switched) {
-                if (use_before) outer.plot(p, before_outer);
-                else outer.plot(p);
-            } else {
-                inner.plot_reverse(p);
-            }
+            if (switched) to_outer(p);
+            else sd.inner.plot_reverse(p);
         };
         if (compare(in.dev_slope, out.dev_slope) == 0) {
             plot_outer(jcw ? in.p1_ccw : in.p1_cw);
             plot_inner(jcw ? in.p1_cw : in.p1_ccw);
-            if (clockwise < 0) clockwise = pcw ? 1 : 0;
+            if (sd.clockwise < 0) sd.clockwise = pcw ? 1 : 0;
             return;
         }
         if (mode == kJoinMiter || mode == kJoinBevel) {
@@ -426,14 +490,14 @@ struct Plotter {
         plot_inner(jcw ? in.p1_cw : in.p1_ccw);
         plot_inner(p1);
         plot_inner(jcw ? out.p0_cw : out.p0_ccw);
-        if (clockwise < 0) clockwise = pcw ? 1 : 0;
+        if (sd.clockwise < 0) sd.clockwise = pcw ? 1 : 0;
     }
 
     // Face.cap (Face.zig:156-246); points go to `sink`
     template <class Sink>
-    void cap(const Face &f, bool clockwise_, Sink &&sink) {
+    void cap(const Face &f, bool cw, Sink &&sink) {
         if (o.cap == kCapButt) {
-            if (clockwise_) {
+            if (cw) {
                 sink(f.p1_ccw);
                 sink(f.p1_cw);
             } else {
@@ -443,7 +507,7 @@ struct Plotter {
         } else if (o.cap == kCapSquare) {
             double ox = f.user_slope.dx * f.half_width, oy = f.user_slope.dy * f.half_width;
             user_to_device_distance(f.ctm, ox, oy);
-            if (clockwise_) {
+            if (cw) {
                 sink(f.p1_ccw);
                 sink(Pt{f.p1_ccw.x + ox, f.p1_ccw.y + oy});
                 sink(Pt{f.p1_cw.x + ox, f.p1_cw.y + oy});
@@ -455,12 +519,12 @@ struct Plotter {
                 sink(f.p1_ccw);
             }
         } else {
-            sink(clockwise_ ? f.p1_ccw : f.p1_cw);
-            for (int32_t k : pen_vertices_for(pen, f.dev_slope, Slope{-f.dev_slope.dx, -f.dev_slope.dy}, clockwise_)) {
+            sink(cw ? f.p1_ccw : f.p1_cw);
+            for (int32_t k : pen_vertices_for(pen, f.dev_slope, Slope{-f.dev_slope.dx, -f.dev_slope.dy}, cw)) {
                 const Pt v = pen.v[(size_t)k].point;
                 sink(Pt{f.p1.x + v.x, f.p1.y + v.y});
             }
-            sink(clockwise_ ? f.p1_cw : f.p1_ccw);
+            sink(cw ? f.p1_cw : f.p1_ccw);
         }
     }
     template <class Sink>
@@ -468,78 +532,66 @@ struct Plotter {
         cap(face_init(f.p1, f.p0, f.width, f.ctm), cw, sink);
     }
 
+    void clear(Side &sd) {
+        sd.outer.pts.clear();
+        sd.inner.pts.clear();
+        sd.clockwise = -1;
+    }
+
     // plotSingle (stroke_plotter.zig:232-279)
-    void plot_single(Pt start, Pt end) {
+    void plot_single(Side &sd, Pt start, Pt end) {
         const Face f = face_init(start, end, o.thickness, ctm);
-        auto sink = [&](Pt p) { outer.plot(p); };
+        auto sink = [&](Pt p) { sd.outer.plot(p); };
         cap_p0(f, true, sink);
         cap(f, true, sink);
-        emit(outer);
-        reset_outer();
+        emit(sd.outer);
+        sd.outer.pts.clear();
+        sd.clockwise = -1;
     }
 
     // plotOpenJoined (stroke_plotter.zig:281-363)
-    void plot_open_joined(Pt s0, Pt e0, Pt s1, Pt e1) {
+    void plot_open_joined(Side &sd, Pt s0, Pt e0, Pt s1, Pt e1) {
         const Face fs = face_init(s0, e0, o.thickness, ctm);
         const Face fe = face_init(s1, e1, o.thickness, ctm);
-        const bool cw = clockwise >= 0 ? clockwise != 0 : true;
-        const Contour::It first = outer.pts.begin();  // insertion point captured before plotting
-        auto before_first = [&](Pt p) { outer.plot(p, first); };
+        const bool cw = sd.clockwise >= 0 ? sd.clockwise != 0 : true;
+        const Contour::It first = sd.outer.pts.begin();  // the insertion point is captured before plotting
+        auto before_first = [&](Pt p) { sd.outer.plot(p, first); };
         cap_p0(fs, cw, before_first);
-        auto append = [&](Pt p) { outer.plot(p); };
+        auto append = [&](Pt p) { sd.outer.plot(p); };
         cap(fe, cw, append);
-        outer.pts.splice(outer.pts.end(), inner.pts);
-        emit(outer);
-        outer.pts.clear();
-        inner.pts.clear();
-        clockwise = -1;
+        sd.outer.pts.splice(sd.outer.pts.end(), sd.inner.pts);
+        emit(sd.outer);
+        clear(sd);
     }
 
-    // plotClosedJoined (stroke_plotter.zig:365-403)
-    void plot_closed_joined(Pt i0, Pt i1, Pt p1, Pt p2) {
-        if (!eq(p2, i0)) {
-            join(o.join, p1, p2, i0, false, outer.pts.end());
-            join(o.join, p2, i0, i1, false, outer.pts.end());
-        } else {
-            join(o.join, p1, i0, i1, false, outer.pts.end());
-        }
-        emit(outer);
-        emit(inner);
-        outer.pts.clear();
-        inner.pts.clear();
-        clockwise = -1;
-    }
-
-    // plotDotted (stroke_plotter.zig:183-219)
-    void plot_dotted(Pt p) {
+    // The dots of zero-length strokes: round caps draw the pen; the dashed
+    // plotter also draws square dots and always resets the state
+    // (stroke_plotter.zig:183-219, dashed_plotter.zig:387-470).
+    void plot_dot(Side &sd, Pt p, bool dashed_plotter, Slope slope) {
         if (o.cap == kCapRound) {
-            for (const PenVertex &v : pen.v) outer.plot(Pt{p.x + v.point.x, p.y + v.point.y});
-            emit(outer);
-            reset_outer();
+            for (const PenVertex &v : pen.v) sd.outer.plot(Pt{p.x + v.point.x, p.y + v.point.y});
+            emit(sd.outer);
+        } else if (dashed_plotter && o.cap == kCapSquare) {
+            const Face f = face_init2(p, p, slope, o.thickness, ctm);
+            double ox = f.user_slope.dx * f.half_width, oy = f.user_slope.dy * f.half_width;
+            user_to_device_distance(ctm, ox, oy);
+            sd.outer.plot(Pt{f.p1_cw.x - ox, f.p1_cw.y - oy});
+            sd.outer.plot(Pt{f.p1_cw.x + ox, f.p1_cw.y + oy});
+            sd.outer.plot(Pt{f.p1_ccw.x + ox, f.p1_ccw.y + oy});
+            sd.outer.plot(Pt{f.p1_ccw.x - ox, f.p1_ccw.y - oy});
+            emit(sd.outer);
+        } else if (!dashed_plotter) {
+            return;  // stroke_plotter's dot draws nothing and leaves the state alone
         }
+        sd.outer.pts.clear();
+        sd.clockwise = -1;
     }
 
-    void line_to(int join_mode, Pt p) {
-        if (points.len == 0) {
-            error = kErrInvalidState;
-            return;
-        }
-        if (eq(p, points.tail(1))) return;  // degenerate node
-        points.add(p);
-        if (points.len > 2) join(join_mode, points.tail(3), points.tail(2), points.tail(1), false, outer.pts.end());
-    }
-
-    // Spline.decompose with the stroke plotter's lineTo (round joins inside
-    // curves, stroke_plotter.zig:126-150, 221-230)
-    void curve_to(Pt b, Pt c, Pt d) {
-        if (points.len == 0) {
-            error = kErrInvalidState;
-            return;
-        }
-        if (!pen.ok) pen = make_pen(o.thickness, o.tolerance, ctm);
-        const Pt a = points.tail(1);
+    // Spline.decompose (Spline.zig:37-71) with `line` as the lineTo
+    template <class Line>
+    void spline(Pt a, Pt b, Pt c, Pt d, Line &&line) {
         if (eq(a, b) && eq(c, d)) {
-            line_to(kJoinRound, d);
+            line(d);
             return;
         }
         struct K {
@@ -577,13 +629,13 @@ struct Plotter {
         while (!stack.empty() && error == 0) {
             K k = stack.back();
             stack.pop_back();
-            while (true) {
+            while (error == 0) {
                 if (--budget < 0 || stack.size() > 64) {
                     error = kErrInvalidState;
                     break;
                 }
                 if (error_sq(k) < tol) {
-                    if (!eq(k.a, a)) line_to(kJoinRound, k.a);
+                    if (!eq(k.a, a)) line(k.a);
                     break;
                 }
                 const Pt ab = lerp(k.a, k.b), bc = lerp(k.b, k.c), cd = lerp(k.c, k.d);
@@ -592,22 +644,64 @@ struct Plotter {
                 k = K{k.a, ab, abbc, fin};
             }
         }
-        line_to(kJoinRound, d);
+        if (error == 0) line(d);
+    }
+};
+
+// stroke_plotter.Plotter (stroke_plotter.zig:77-230)
+struct SolidPlotter : Common {
+    PointBuffer points;
+    Side sd;
+
+    SolidPlotter(const Options &opts, std::vector<std::vector<double>> &res) : Common(opts, res) {
+        sd.set_scale(opts.scale);
+    }
+
+    void line_to(int join_mode, Pt p) {
+        if (points.len == 0) {
+            error = kErrInvalidState;
+            return;
+        }
+        if (eq(p, points.tail(1))) return;  // degenerate node
+        points.add(p);
+        if (points.len > 2) join(sd, join_mode, points.tail(3), points.tail(2), points.tail(1), false, sd.outer.pts.end());
+    }
+
+    void curve_to(Pt b, Pt c, Pt d) {  // curves join their pieces round (stroke_plotter.zig:126-150)
+        if (points.len == 0) {
+            error = kErrInvalidState;
+            return;
+        }
+        if (!pen.ok) pen = make_pen(o.thickness, o.tolerance, ctm);
+        spline(points.tail(1), b, c, d, [&](Pt q) { line_to(kJoinRound, q); });
+    }
+
+    // plotClosedJoined (stroke_plotter.zig:365-403)
+    void plot_closed_joined(Pt i0, Pt i1, Pt p1, Pt p2) {
+        if (!eq(p2, i0)) {
+            join(sd, o.join, p1, p2, i0, false, sd.outer.pts.end());
+            join(sd, o.join, p2, i0, i1, false, sd.outer.pts.end());
+        } else {
+            join(sd, o.join, p1, i0, i1, false, sd.outer.pts.end());
+        }
+        emit(sd.outer);
+        emit(sd.inner);
+        clear(sd);
     }
 
     void close_path() {
         switch (points.len) {
             case 0: break;
-            case 1: plot_dotted(points.head(0)); break;
-            case 2: plot_single(points.head(0), points.head(1)); break;
+            case 1: plot_dot(sd, points.head(0), false, Slope{0, 0}); break;
+            case 2: plot_single(sd, points.head(0), points.head(1)); break;
             default: plot_closed_joined(points.head(0), points.head(1), points.tail(2), points.tail(1)); break;
         }
         points.len = 0;
     }
 
     void finish() {
-        if (points.len == 2) plot_single(points.head(0), points.head(1));
-        else if (points.len > 2) plot_open_joined(points.head(0), points.head(1), points.tail(2), points.tail(1));
+        if (points.len == 2) plot_single(sd, points.head(0), points.head(1));
+        else if (points.len > 2) plot_open_joined(sd, points.head(0), points.head(1), points.tail(2), points.tail(1));
     }
 
     void move_to(Pt p) {
@@ -617,21 +711,190 @@ struct Plotter {
     }
 };
 
-}  // namespace
+// dashed_plotter.Plotter (dashed_plotter.zig:52-600)
+struct DashedPlotter : Common {
+    PointBuffer points;
+    Side sd;
+    Dasher dasher;
+    Slope current_slope{0, 0};
+    enum { kNone, kOff, kOn } init_kind = kNone;
+    Pt init_off{0, 0};
+    PointBuffer init_points;
+    Side init_side;
+    Slope init_slope{0, 0};
 
-bool transformation_invertible(const double m[6]) {
-    Tf inv;
-    return inverse(Tf{m[0], m[1], m[2], m[3], m[4], m[5]}, inv);
-}
+    DashedPlotter(const Options &opts, std::vector<std::vector<double>> &res) : Common(opts, res) {
+        sd.set_scale(opts.scale);
+        init_side.set_scale(opts.scale);
+        dasher.init(opts.dashes, opts.n_dashes, opts.dash_offset);
+        if (dasher.stuck) error = kErrInvalidState;
+    }
 
-int plot(const z2d_node *nodes, size_t n_nodes, const Options &opts, std::vector<std::vector<double>> &contours) {
-    contours.clear();
-    Plotter p(opts, contours);
+    void line_to(int join_mode, Pt p) {  // _runLineTo (dashed_plotter.zig:113-187)
+        if (points.len == 0) {
+            error = kErrInvalidState;
+            return;
+        }
+        const Pt first = points.tail(1);
+        if (eq(p, first)) return;
+        Slope sl = slope(first, p);
+        current_slope = normalized(sl);
+        device_to_user_distance(ctm, sl.dx, sl.dy);
+        const double total = normalize(sl);
+        double remaining = total;
+        double step_len = std::min(dasher.remain, remaining);
+        int64_t guard = 0;
+        while (remaining > 0 && error == 0) {
+            if (++guard > (int64_t)1 << 26) {  // dash steps of one segment (guard)
+                error = kErrInvalidState;
+                break;
+            }
+            remaining -= step_len;
+            double xo = sl.dx * (total - remaining), yo = sl.dy * (total - remaining);
+            user_to_device_distance(ctm, xo, yo);
+            const Pt cdp{first.x + xo, first.y + yo};
+            if (!eq(cdp, points.tail(1))) points.add(cdp);
+            if (dasher.on && points.len > 2)
+                join(sd, join_mode, points.tail(3), points.tail(2), points.tail(1), false, sd.outer.pts.end());
+            if (dasher.step(step_len)) next_segment(cdp);
+            step_len = std::min(dasher.remain, remaining);
+        }
+    }
+
+    void curve_to(Pt b, Pt c, Pt d) {
+        if (points.len == 0) {
+            error = kErrInvalidState;
+            return;
+        }
+        if (!pen.ok) pen = make_pen(o.thickness, o.tolerance, ctm);
+        spline(points.tail(1), b, c, d, [&](Pt q) { line_to(kJoinRound, q); });
+    }
+
+    // the segment that just ended, if it was on (dashed_plotter.zig:283-310)
+    void plot_segment() {
+        switch (points.len) {
+            case 0: break;
+            case 1: plot_dot(sd, points.head(0), true, current_slope); break;
+            case 2: plot_single(sd, points.head(0), points.head(1)); break;
+            default: plot_open_joined(sd, points.head(0), points.head(1), points.tail(2), points.tail(1)); break;
+        }
+    }
+
+    void next_segment(Pt p) {
+        if (init_kind == kNone) save_initial();
+        else if (!dasher.on) plot_segment();
+        points.len = 0;
+        points.add(p);
+    }
+
+    void save_initial() {  // saveInitial (dashed_plotter.zig:472-501)
+        if (!dasher.on) {
+            init_kind = kOn;
+            init_points = points;
+            init_side.outer.pts.clear();
+            init_side.inner.pts.clear();
+            init_side.outer.pts.splice(init_side.outer.pts.end(), sd.outer.pts);
+            init_side.inner.pts.splice(init_side.inner.pts.end(), sd.inner.pts);
+            init_side.clockwise = sd.clockwise;
+            init_slope = current_slope;
+        } else {
+            init_kind = kOff;
+            init_off = points.head(0);
+        }
+        clear(sd);
+    }
+
+    void finish_initial_dotted() {
+        plot_dot(sd, init_points.head(0), true, init_slope);
+        init_kind = kNone;
+    }
+
+    void finish_initial(Pt a, Pt b) {
+        plot_open_joined(init_side, a, b, init_points.tail(2), init_points.tail(1));
+        init_kind = kNone;
+    }
+
+    void join_and_cap_initial() {  // joinAndCapInitial (dashed_plotter.zig:531-588)
+        if (points.len > 2) {
+            join(sd, o.join, points.tail(2), init_points.head(0), init_points.head(1), false, sd.outer.pts.end());
+            sd.outer.pts.splice(sd.outer.pts.end(), init_side.outer.pts);
+            init_side.inner.pts.splice(init_side.inner.pts.end(), sd.inner.pts);
+            init_side.outer.pts.swap(sd.outer.pts);
+            sd.outer.pts.clear();
+            plot_open_joined(init_side, points.head(0), points.head(1), init_points.tail(2), init_points.tail(1));
+        } else {
+            join(init_side, o.join, points.tail(2), init_points.head(0), init_points.head(1), true,
+                 init_side.outer.pts.begin());
+            plot_open_joined(init_side, points.head(0), init_points.head(0), init_points.tail(2), init_points.tail(1));
+        }
+        init_kind = kNone;
+        clear(sd);
+    }
+
+    void close_path() {  // runClosePath (dashed_plotter.zig:201-281)
+        if (points.len == 0) {
+            error = kErrInvalidState;
+            return;
+        }
+        const Pt target = init_kind == kOn ? init_points.head(0) : (init_kind == kOff ? init_off : points.head(0));
+        line_to(o.join, target);
+        if (error) return;
+        if (init_kind == kOn) {
+            if (dasher.on && points.len > 1) {
+                if (init_points.len == 1) {
+                    plot_open_joined(sd, points.head(0), points.head(1), points.tail(2), points.tail(1));
+                    init_kind = kNone;
+                } else {
+                    join_and_cap_initial();
+                }
+            } else if (init_points.len == 1) {
+                finish_initial_dotted();
+            } else {
+                finish_initial(init_points.head(0), init_points.head(1));
+            }
+        } else if (init_kind == kOff) {
+            init_kind = kNone;
+        } else {
+            switch (points.len) {
+                case 1: plot_dot(sd, points.head(0), true, current_slope); break;
+                case 2: plot_single(sd, points.head(0), points.head(1)); break;
+                default:
+                    join(sd, o.join, points.tail(2), points.head(0), points.head(1), false, sd.outer.pts.end());
+                    emit(sd.outer);
+                    emit(sd.inner);
+                    clear(sd);
+                    break;
+            }
+        }
+        points.len = 0;
+    }
+
+    void finish() {  // finish (dashed_plotter.zig:346-385)
+        if (init_kind == kOn) {
+            if (init_points.len == 1) finish_initial_dotted();
+            else finish_initial(init_points.head(0), init_points.head(1));
+        } else if (init_kind == kOff) {
+            init_kind = kNone;
+        }
+        if (dasher.on) plot_segment();
+    }
+
+    void move_to(Pt p) {
+        finish();
+        dasher.reset();
+        if (dasher.stuck) error = kErrInvalidState;
+        points.len = 0;
+        points.add(p);
+    }
+};
+
+template <class P>
+int run(P &p, const z2d_node *nodes, size_t n_nodes) {
     for (size_t i = 0; i < n_nodes && p.error == 0; i++) {
         const z2d_node &nd = nodes[i];
         switch (nd.tag) {
             case Z2D_MOVE_TO: p.move_to(Pt{nd.p[0], nd.p[1]}); break;
-            case Z2D_LINE_TO: p.line_to(opts.join, Pt{nd.p[0], nd.p[1]}); break;
+            case Z2D_LINE_TO: p.line_to(p.o.join, Pt{nd.p[0], nd.p[1]}); break;
             case Z2D_CURVE_TO: p.curve_to(Pt{nd.p[0], nd.p[1]}, Pt{nd.p[2], nd.p[3]}, Pt{nd.p[4], nd.p[5]}); break;
             case Z2D_CLOSE_PATH: p.close_path(); break;
             default: return kErrInvalidState;
@@ -640,6 +903,25 @@ int plot(const z2d_node *nodes, size_t n_nodes, const Options &opts, std::vector
     if (p.error) return p.error;
     p.finish();
     return p.error;
+}
+
+}  // namespace
+
+bool transformation_invertible(const double m[6]) {
+    Tf inv;
+    return inverse(Tf{m[0], m[1], m[2], m[3], m[4], m[5]}, inv);
+}
+
+bool dashed(const Options &opts) { return opts.n_dashes > 0 && dashes_valid(opts.dashes, opts.n_dashes); }
+
+int plot(const z2d_node *nodes, size_t n_nodes, const Options &opts, std::vector<std::vector<double>> &contours) {
+    contours.clear();
+    if (dashed(opts)) {  // stroke_plotter.plot (stroke_plotter.zig:40-44)
+        DashedPlotter p(opts, contours);
+        return run(p, nodes, n_nodes);
+    }
+    SolidPlotter p(opts, contours);
+    return run(p, nodes, n_nodes);
 }
 
 }  // namespace stroke

@@ -22,7 +22,13 @@ struct Options {
     double scale;
     double thickness;
     double tolerance;
+    const double *dashes;  // Dasher input (used when Dasher.validate accepts it)
+    size_t n_dashes;
+    double dash_offset;
 };
+
+// Dasher.validate: the dash array draws dashes (stroke_plotter.zig:40-44).
+bool dashed(const Options &opts);
 
 // Transformation.inverse succeeds (painter.zig:231).
 bool transformation_invertible(const double m[6]);
