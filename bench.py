@@ -372,20 +372,28 @@ JOBS_PLAIN_FILLS = 1500   # per-call sample of the jobs arm (complete jobs, in o
 JOBS_CPU_SECONDS = 10.0   # CPU sample of the jobs arm: whole jobs in order until this much wall time
 
 
+JOBS_STROKED = 0.3        # share of paths stroked instead of filled
+JOBS_SURFACE_SAMPLE = 512  # per-surface arm: the first jobs, one z2dgpu_draw_jobs call each
+
+
 def jobs_arm(ctx, stream, dev, steps=3):
     """The batched-jobs configuration: N_JOBS independent RGBA surfaces, each
-    with its own ordered paths (z2d_gb300.workloads.batched_jobs; no strokes),
-    drawn by one z2dgpu_fill_jobs call per step.  Pixels counted: the sum of
-    the job surfaces' w x h.  Beside it: one z2dgpu_fill_batch call per
-    surface, one z2dgpu_fill call per path on a sample of whole jobs, and the
-    CPU restatement on all host threads (one job per thread) on a sample."""
+    with its own ordered paths (z2d_gb300.workloads.batched_jobs); 30 % of
+    the paths are stroked (width U[0.5, 20], join and cap uniform, half of
+    them dashed with 2-6 dash lengths in [1, 40]), the rest filled; one
+    z2dgpu_draw_jobs call per step.  Pixels counted: the sum of the job
+    surfaces' w x h.  Beside it: one call per surface on the first jobs, one
+    painter call per path on the first jobs, and the CPU restatement on all
+    host threads (one job per thread) on a sample."""
     import torch
-    from z2d_gb300 import painter
-    from z2d_gb300.batch import PackedBatch
+    from z2d_gb300 import abi, painter
+    from z2d_gb300.batch import PackedDrawBatch
     from z2d_gb300.surface import Surface
+    from z2d_gb300.types import StrokeOptions
     from z2d_gb300.workloads import batched_jobs, job_fills
     t_gen = time.perf_counter()
     jobs = batched_jobs(SEED + 11, N_JOBS)
+    srng = np.random.default_rng(SEED + 13)
     nodes, offs, cnts, pxs, rules, cmd_off, cmd_cnt = [], [], [], [], [], [], []
     base = ncmd = 0
     for w, h, nd, off, cnt, px, rl in jobs:
@@ -398,8 +406,14 @@ def jobs_arm(ctx, stream, dev, steps=3):
         cmd_cnt.append(len(off))
         base += len(nd)
         ncmd += len(off)
-    pb = PackedBatch(np.concatenate(nodes), np.concatenate(offs), np.concatenate(cnts), np.concatenate(pxs),
-                     np.concatenate(rules))
+    stroke = srng.random(ncmd) < JOBS_STROKED
+    widths = srng.uniform(0.5, 20.0, ncmd)
+    joins = srng.integers(0, 3, ncmd)
+    caps = srng.integers(0, 3, ncmd)
+    dashed = stroke & (srng.random(ncmd) < 0.5)
+    dashes = [tuple(srng.uniform(1.0, 40.0, int(srng.integers(2, 7)))) if d else () for d in dashed]
+    pb = PackedDrawBatch(np.concatenate(nodes), np.concatenate(offs), np.concatenate(cnts), np.concatenate(pxs),
+                         np.concatenate(rules), stroke, widths, joins, caps, dashes)
     t_gen = time.perf_counter() - t_gen
     sizes = [w * h * 4 for w, h, *_ in jobs]
     starts = []
@@ -424,47 +438,64 @@ def jobs_arm(ctx, stream, dev, steps=3):
         stream.synchronize()
 
     restore()
-    pb.fill_jobs(ctx)  # warm
+    pb.draw_jobs(ctx)  # warm
     ctx.set_timing(True)
     walls = []
     for _ in range(steps):
         restore()
         t0 = time.perf_counter()
-        pb.fill_jobs(ctx)
+        pb.draw_jobs(ctx)
         stream.synchronize()
         walls.append(time.perf_counter() - t0)
     stage_ms = {k: ctx.kernel_ms(k)[0] / steps for k in ("flatten", "bins", "raster")}
     ctx.set_timing(False)
-    # one z2dgpu_fill_batch per surface
+    # one call per surface, first jobs
     restore()
+    ns = min(JOBS_SURFACE_SAMPLE, len(jobs))
     t0 = time.perf_counter()
-    for j, sfc in enumerate(surfaces):
-        pb.fill_batch(sfc, cmd_off[j], cmd_cnt[j], ctx=ctx)
+    for j in range(ns):
+        pb.draw_job(j, ctx)
     stream.synchronize()
     per_surface_s = time.perf_counter() - t0
-    # one z2dgpu_fill per path on whole jobs from the start
+    per_surface_mpix = sum(jobs[j][0] * jobs[j][1] for j in range(ns)) / 1e6
+    # one painter call per path on whole jobs from the start
     restore()
+
+    def ops_of(j):
+        out = []
+        for k, (pat, nd, fo) in enumerate(job_fills(jobs[j])):
+            i = cmd_off[j] + k
+            if stroke[i]:
+                so = StrokeOptions(line_width=float(widths[i]), line_join=("miter", "round", "bevel")[joins[i]],
+                                   line_cap=("butt", "round", "square")[caps[i]], dashes=dashes[i])
+                out.append(("stroke", pat, nd, so))
+            else:
+                out.append(("fill", pat, nd, fo))
+        return out
+
     k, nf = 0, 0
     while k < len(jobs) and nf < JOBS_PLAIN_FILLS:
         nf += cmd_cnt[k]
         k += 1
-    plain_fills = [(surfaces[j], job_fills(jobs[j])) for j in range(k)]
+    plain_ops = [(surfaces[j], ops_of(j)) for j in range(k)]
     t0 = time.perf_counter()
-    for sfc, fl in plain_fills:
-        for pat, nd, opts in fl:
-            painter.fill(sfc, pat, nd, opts, ctx=ctx)
+    for sfc, ops in plain_ops:
+        for kind, pat, nd, o in ops:
+            (painter.fill if kind == "fill" else painter.stroke)(sfc, pat, nd, o, ctx=ctx)
     stream.synchronize()
     plain_s = time.perf_counter() - t0
     plain_mpix = sum(jobs[j][0] * jobs[j][1] for j in range(k)) / 1e6
     out = {
-        "workload": f"{N_JOBS} RGBA jobs, sides log-uniform [16, 2048], 1-200 paths each (no strokes)",
-        "jobs": N_JOBS, "fills": int(ncmd), "nodes": int(base), "mpix_per_step": mpix,
+        "workload": f"{N_JOBS} RGBA jobs, sides log-uniform [16, 2048], 1-200 paths each, "
+                    f"{int(JOBS_STROKED * 100)}% stroked (half of those dashed)",
+        "jobs": N_JOBS, "commands": int(ncmd), "strokes": int(stroke.sum()), "nodes": int(base),
+        "mpix_per_step": mpix,
         "value": mpix * steps / sum(walls), "unit": "Mpix/s (sum of job surfaces w x h)",
         "ms_per_step": 1000 * sum(walls) / steps,
         "stage_ms_per_step": stage_ms,
-        "per_surface_batch": {"value": mpix / per_surface_s, "calls": N_JOBS},
+        "per_surface": {"value": per_surface_mpix / per_surface_s, "calls": ns},
         "plain": {"value": plain_mpix / plain_s, "jobs": k, "calls": nf},
-        "note": "wall time of the call (host validation and packing, uploads, kernels); "
+        "note": "wall time of the call (host validation, stroke building, packing, uploads, kernels); "
                 "inputs in host memory, surfaces on the device",
         "generation_s": t_gen,
     }
@@ -482,18 +513,33 @@ def jobs_arm(ctx, stream, dev, steps=3):
         w, h = jobs[j][0], jobs[j][1]
         host = np.zeros(w * h * 4, np.uint8)
         keep, calls = [], []
-        for pat, nd, opts in job_fills(jobs[j]):
-            p, o, arr = pat.to_abi(keep), opts.to_abi(), nodes_to_abi(nd)
-            keep += [p, o, arr]
-            calls.append((C.byref(p), arr, len(nd), C.byref(o)))
+        for kind, pat, nd, o in ops_of(j):
+            p = pat.to_abi(keep)
+            keep.append(p)
+            if kind == "fill":
+                fo, arr = o.to_abi(), nodes_to_abi(nd)
+                keep += [fo, arr]
+                calls.append(("fill", C.byref(p), arr, len(nd), C.byref(fo)))
+            else:
+                contours, _ = painter.stroke_contours(nd, o, "rgba")
+                pts = np.ascontiguousarray(np.concatenate(contours) if contours else np.zeros((1, 2)))
+                ends = (np.cumsum([len(c_) for c_ in contours]) if contours else np.zeros(1)).astype(np.uint64)
+                fo = A.z2d_fill_opts(anti_aliasing=A.AA_DEFAULT, fill_rule=A.FILL_NON_ZERO, op=A.OP["src_over"],
+                                     precision=A.PRECISION_INTEGER, tolerance=0.1)
+                keep += [pts, ends, fo]
+                calls.append(("stroke", C.byref(p), pts, ends, len(contours), C.byref(fo)))
         sfc = A.z2d_surface(format=A.FORMAT_RGBA, width=w, height=h, location=A.MEM_HOST,
                             data=host.ctypes.data_as(C.c_void_p))
         return (sfc, host, keep, calls)
 
     def run(item):
         sfc, _, _, calls = item
-        for p, arr, n, o in calls:
-            lib.z2doracle_fill(C.byref(sfc), p, arr, n, o)
+        for c_ in calls:
+            if c_[0] == "fill":
+                lib.z2doracle_fill(C.byref(sfc), c_[1], c_[2], c_[3], c_[4])
+            else:
+                lib.z2doracle_fill_contours(C.byref(sfc), c_[1], c_[2].ctypes.data_as(C.POINTER(C.c_double)),
+                                            c_[3].ctypes.data_as(C.POINTER(C.c_uint64)), c_[4], c_[5])
 
     nt = host_threads()
     k = nf = 0
@@ -507,8 +553,9 @@ def jobs_arm(ctx, stream, dev, steps=3):
             cpu_s += time.perf_counter() - t0
             k = chunk[-1] + 1
             nf += sum(cmd_cnt[j] for j in chunk)
-    out["cpu"] = {"value": sum(jobs[j][0] * jobs[j][1] for j in range(k)) / 1e6 / cpu_s, "jobs": k, "fills": nf,
-                  "cores": nt, "seconds": cpu_s, "kind": "port"}
+    out["cpu"] = {"value": sum(jobs[j][0] * jobs[j][1] for j in range(k)) / 1e6 / cpu_s, "jobs": k, "commands": nf,
+                  "cores": nt, "seconds": cpu_s, "kind": "port",
+                  "note": "stroke polygons built on the host beforehand (not timed); fills and polygons rasterised"}
     return out
 
 

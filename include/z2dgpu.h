@@ -231,6 +231,20 @@ typedef struct z2d_stroke_opts {
     uint64_t n_dashes;
 } z2d_stroke_opts;
 
+/* one drawing operation of a mixed batch: painter.fill (kind FILL, `fill`
+ * options) or painter.stroke (kind STROKE, `stroke` options) of
+ * nodes[node_offset, node_offset+n_nodes) with `pattern` */
+enum { Z2D_DRAW_FILL = 0, Z2D_DRAW_STROKE = 1 };
+typedef struct z2d_draw_cmd {
+    int32_t kind;
+    int32_t _pad;
+    const z2d_pattern *pattern;
+    uint64_t node_offset;
+    uint64_t n_nodes;
+    z2d_fill_opts fill;
+    z2d_stroke_opts stroke;
+} z2d_draw_cmd;
+
 /* one surface of a multi-surface batch: cmds[cmd_offset, cmd_offset+n_cmds)
  * of the batch command array, drawn in order on `surface` */
 typedef struct z2d_job {
@@ -315,6 +329,14 @@ Z2D_API int z2dgpu_stroke_contours(const z2d_node *nodes, size_t n_nodes,
 Z2D_API int z2dgpu_fill_jobs(z2dgpu_ctx *ctx, const z2d_job *jobs, size_t n_jobs,
                              const z2d_node *nodes, size_t n_nodes,
                              const z2d_fill_cmd *cmds, size_t n_cmds);
+
+/* z2dgpu_fill_jobs with fills and strokes mixed: each job's commands are
+ * drawn in order on its surface (job.cmd_offset / n_cmds index `cmds`).
+ * Stroke polygons are built on the host (in parallel across commands),
+ * then every job is drawn in one device pass. */
+Z2D_API int z2dgpu_draw_jobs(z2dgpu_ctx *ctx, const z2d_job *jobs, size_t n_jobs,
+                             const z2d_node *nodes, size_t n_nodes,
+                             const z2d_draw_cmd *cmds, size_t n_cmds);
 
 /* SurfaceCompositor.run (src/compositor.zig:302-440) with 1 or 2 operations.
  * Source/destination surfaces must live where `dst` lives. */

@@ -33,7 +33,8 @@ def test_library_loads_and_exports_every_symbol():
 
 
 STRUCTS = ["z2d_pixel", "z2d_surface", "z2d_node", "z2d_color", "z2d_stop", "z2d_gradient", "z2d_pattern",
-           "z2d_fill_opts", "z2d_param", "z2d_operation", "z2d_fill_cmd", "z2d_job"]
+           "z2d_fill_opts", "z2d_param", "z2d_operation", "z2d_fill_cmd", "z2d_job", "z2d_stroke_opts",
+           "z2d_draw_cmd"]
 
 
 def test_ctypes_layout_matches_header():

@@ -160,3 +160,41 @@ def test_dashed_strokes(gpu, oracle, dashes, offset, cap):
         assert gpu.stroke(a, pat, nodes, opts) == abi.OK
         assert so.stroke(b, pat, nodes, opts) == abi.OK
     _cmp(a, b, 0, f"{dashes}/{offset}/{cap}")
+
+
+def test_draw_jobs_mixed(oracle):
+    """z2dgpu_draw_jobs: fills and strokes (dashed or not) interleaved over
+    many surfaces equal the same calls one by one."""
+    torch = pytest.importorskip("torch")
+    from z2d_gb300 import painter
+    from z2d_gb300.types import FillOptions
+    from z2d_gb300.workloads import random_fills
+    so = StrokeOracle(oracle)
+    rng = np.random.default_rng(99)
+    jobs, refs = [], []
+    for j in range(20):
+        w, h = int(rng.integers(20, 180)), int(rng.integers(20, 140))
+        fmt = ("rgba", "rgb", "alpha8", "alpha4")[j % 4]
+        dev = _bg(fmt, w, h, 500 + j).to_device("cuda")
+        ref = _bg(fmt, w, h, 500 + j)
+        ops = []
+        fills = random_fills(seed=900 + j, n=int(rng.integers(0, 6)), w=w, h=h, side_lo=2, side_hi=max(3, min(w, h)),
+                             seg_lo=3, seg_hi=10)
+        for k, (pat, nodes, fo) in enumerate(fills):
+            ops.append(("fill", pat, nodes, fo))
+            if k % 2 == 0:
+                sn = _open_path(rng, w, h, int(rng.integers(1, 5)))
+                st = StrokeOptions(line_width=float(rng.uniform(0.5, 12)), line_join=("miter", "round", "bevel")[k % 3],
+                                   line_cap=("butt", "round", "square")[(k + j) % 3],
+                                   dashes=(6.0, 3.0) if (k + j) % 4 == 0 else (),
+                                   anti_aliasing=("default", "none", "supersample_4x")[j % 3])
+                ops.append(("stroke", Pattern.from_pixel(random_premultiplied_pixel(rng)), sn, st))
+        for kind, pat, nodes, o in ops:
+            rc = oracle.fill(ref, pat, nodes, o) if kind == "fill" else so.stroke(ref, pat, nodes, o)
+            assert rc == abi.OK
+        jobs.append((dev, ops))
+        refs.append(ref)
+    painter.draw_jobs(jobs)
+    torch.cuda.synchronize()
+    for j, ((dev, _), ref) in enumerate(zip(jobs, refs)):
+        _cmp(dev.to_host(), ref, 0, f"job {j}")

@@ -121,6 +121,15 @@ class z2d_stroke_opts(C.Structure):
                 ("transformation", C.c_double * 6), ("dashes", C.POINTER(C.c_double)), ("n_dashes", C.c_uint64)]
 
 
+DRAW_FILL, DRAW_STROKE = 0, 1
+
+
+class z2d_draw_cmd(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("_pad", C.c_int32), ("pattern", C.POINTER(z2d_pattern)),
+                ("node_offset", C.c_uint64), ("n_nodes", C.c_uint64), ("fill", z2d_fill_opts),
+                ("stroke", z2d_stroke_opts)]
+
+
 class z2d_job(C.Structure):
     _fields_ = [("surface", z2d_surface), ("cmd_offset", C.c_uint64), ("n_cmds", C.c_uint64)]
 
@@ -135,7 +144,8 @@ EXPORTED_SYMBOLS = [
     "z2dgpu_version", "z2dgpu_last_error", "z2dgpu_ctx_create", "z2dgpu_ctx_destroy",
     "z2dgpu_ctx_synchronize", "z2dgpu_ctx_launch_count", "z2dgpu_ctx_set_timing",
     "z2dgpu_ctx_kernel_ms", "z2dgpu_surface_bytes",
-    "z2dgpu_fill", "z2dgpu_fill_batch", "z2dgpu_fill_jobs", "z2dgpu_stroke", "z2dgpu_stroke_contours",
+    "z2dgpu_fill", "z2dgpu_fill_batch", "z2dgpu_fill_jobs", "z2dgpu_draw_jobs", "z2dgpu_stroke",
+    "z2dgpu_stroke_contours",
     "z2dgpu_composite",
     "z2dgpu_composite_noalloc", "z2dgpu_server_create", "z2dgpu_server_submit", "z2dgpu_server_wait",
     "z2dgpu_server_stats", "z2dgpu_server_destroy",

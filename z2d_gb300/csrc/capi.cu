@@ -8,8 +8,10 @@
 #include <cstdio>
 #include <cmath>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "fill.cuh"
@@ -649,6 +651,174 @@ static int do_stroke(Ctx &c, z2d_surface *surface, const z2d_pattern *pattern, c
     return stage_out(c, *surface, ds);
 }
 
+// Fills and strokes over many device surfaces.  Stroke polygons are built
+// on host threads first (each command independently), then every command
+// becomes a prepared fill: strokes as their contours (already-scaled nodes
+// appended after the caller's, edge scale 1), fills on the caller's nodes.
+static int draw_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_node *nodes, size_t n_nodes,
+              const z2d_draw_cmd *cmds, size_t n_cmds) {
+    if ((n_jobs > 0 && !jobs_in) || (n_cmds > 0 && !cmds) || (n_nodes > 0 && !nodes)) return Z2D_ERR_INVALID_ARGUMENT;
+    if (n_jobs > 0x7FFFFFF || n_cmds > 0x7FFFFFF) {
+        set_error("batch too large");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    // stroke polygons, in parallel
+    std::vector<size_t> strokes;
+    for (size_t i = 0; i < n_cmds; i++) {
+        if (cmds[i].kind == Z2D_DRAW_STROKE) strokes.push_back(i);
+        else if (cmds[i].kind != Z2D_DRAW_FILL) {
+            set_error("draw command: bad kind");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+    }
+    // the surface format decides the stroke's anti-aliasing (alpha1: none)
+    std::vector<int32_t> cmd_fmt(n_cmds, Z2D_FORMAT_RGBA);
+    for (size_t j = 0; j < n_jobs; j++) {
+        const z2d_job &jb = jobs_in[j];
+        if (jb.cmd_offset > n_cmds || jb.n_cmds > n_cmds - jb.cmd_offset) {
+            set_error("draw_jobs: job commands outside the command array");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+        for (uint64_t k = 0; k < jb.n_cmds; k++) cmd_fmt[jb.cmd_offset + k] = jb.surface.format;
+    }
+    std::vector<std::vector<std::vector<double>>> polys(strokes.size());
+    std::vector<int> aas(strokes.size(), 0), rcs(strokes.size(), 0);
+    std::vector<std::string> errs(strokes.size());
+    {
+        const size_t nt = std::max<size_t>(1, std::min<size_t>(std::thread::hardware_concurrency(), strokes.size() / 64 + 1));
+        std::atomic<size_t> next{0};
+        auto work = [&] {
+            for (size_t k; (k = next.fetch_add(1)) < strokes.size();) {
+                const z2d_draw_cmd &cm = cmds[strokes[k]];
+                if (!cm.pattern || cm.node_offset > n_nodes || cm.n_nodes > n_nodes - cm.node_offset) {
+                    rcs[k] = Z2D_ERR_INVALID_ARGUMENT;
+                    errs[k] = "stroke command outside the node array";
+                    continue;
+                }
+                double sc = 1;
+                rcs[k] = stroke_polygon(nodes + cm.node_offset, cm.n_nodes, cm.stroke, cmd_fmt[strokes[k]], aas[k],
+                                        polys[k], sc);
+                if (rcs[k]) errs[k] = last_error();
+            }
+        };
+        std::vector<std::thread> pool;
+        for (size_t t = 1; t < nt; t++) pool.emplace_back(work);
+        work();
+        for (auto &t : pool) t.join();
+        for (size_t k = 0; k < strokes.size(); k++)
+            if (rcs[k]) {
+                set_error(errs[k].c_str());
+                return rcs[k];
+            }
+    }
+    // the strokes' contour nodes, as a second node segment after the caller's
+    std::vector<z2d_node> extra;
+    std::vector<uint64_t> stroke_off(strokes.size()), stroke_cnt(strokes.size());
+    std::vector<z2d_node> cn;
+    for (size_t k = 0; k < strokes.size(); k++) {
+        contours_to_nodes(polys[k], cn);
+        stroke_off[k] = extra.size();
+        stroke_cnt[k] = cn.size();
+        extra.insert(extra.end(), cn.begin(), cn.end());
+    }
+    std::vector<int64_t> stroke_of(n_cmds, -1);
+    for (size_t k = 0; k < strokes.size(); k++) stroke_of[strokes[k]] = (int64_t)k;
+    std::vector<FillCmd> fills;
+    std::vector<uint8_t> from_extra;
+    std::vector<int32_t> fill_c(n_nodes, -1), fill_s(extra.size(), -1), grad_of_fill;
+    std::vector<DevGradient> grads;
+    std::vector<DevJob> jobs(n_jobs);
+    if (n_jobs > 0) memset(jobs.data(), 0, sizeof(DevJob) * n_jobs);
+    for (size_t j = 0; j < n_jobs; j++) {
+        const z2d_job &jb = jobs_in[j];
+        int rc = check_surface(&jb.surface);
+        if (rc) return rc;
+        if (jb.surface.location != Z2D_MEM_DEVICE) {
+            set_error("draw_jobs: surfaces must be in device memory");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+        jobs[j].sfc = DevSurface{reinterpret_cast<uint8_t *>(jb.surface.data), jb.surface.format, jb.surface.width,
+                                 jb.surface.height};
+        jobs[j].fill0 = (int32_t)fills.size();
+        for (uint64_t q = 0; q < jb.n_cmds; q++) {
+            const size_t i = jb.cmd_offset + q;
+            const z2d_draw_cmd &cm = cmds[i];
+            z2d_fill_cmd fc;
+            fc.pattern = cm.pattern;
+            const size_t before = fills.size();
+            if (cm.kind == Z2D_DRAW_FILL) {
+                fc.node_offset = cm.node_offset;
+                fc.n_nodes = cm.n_nodes;
+                fc.opts = cm.fill;
+                rc = prepare_fills(jb.surface, (int32_t)j, nodes, n_nodes, &fc, 1, fills, fill_c, grads, grad_of_fill);
+            } else {
+                const size_t k = (size_t)stroke_of[i];
+                if (cm.pattern && cm.pattern->kind == Z2D_PATTERN_PIXEL && !pixel_premultiplied(cm.pattern->pixel)) {
+                    set_error("PixelSourceNotPreMultiplied");
+                    return Z2D_ERR_PIXEL_NOT_PREMULTIPLIED;
+                }
+                fc.node_offset = stroke_off[k];
+                fc.n_nodes = stroke_cnt[k];
+                fc.opts.anti_aliasing = aas[k];
+                fc.opts.fill_rule = Z2D_FILL_NON_ZERO;
+                fc.opts.op = cm.stroke.op;
+                fc.opts.precision = cm.stroke.precision;
+                fc.opts.tolerance = cm.stroke.tolerance;
+                rc = prepare_fills(jb.surface, (int32_t)j, extra.data(), extra.size(), &fc, 1, fills, fill_s, grads,
+                                   grad_of_fill);
+            }
+            if (rc) return rc;
+            for (size_t f = before; f < fills.size(); f++) {
+                from_extra.push_back(cm.kind == Z2D_DRAW_STROKE);
+                if (cm.kind == Z2D_DRAW_STROKE) fills[f].edge_scale = 1.0;  // contour points are already scaled
+            }
+        }
+        jobs[j].fill1 = (int32_t)fills.size();
+    }
+    if (fills.empty()) return Z2D_OK;
+    // the caller's nodes as they are when the fills own them in order,
+    // else compacted; the stroke nodes follow
+    bool in_order = true;
+    {
+        size_t next = 0;
+        for (size_t f = 0; f < fills.size() && in_order; f++) {
+            if (from_extra[f]) continue;
+            if ((size_t)fills[f].node_off != next) in_order = false;
+            next += (size_t)fills[f].n_nodes;
+        }
+        in_order = in_order && next == n_nodes;
+    }
+    std::vector<z2d_node> used;
+    std::vector<int32_t> node_fill;
+    const z2d_node *first = nodes;
+    size_t n_first = n_nodes;
+    if (!in_order) {
+        std::vector<int32_t> new_off(fills.size(), -1);
+        for (size_t i = 0; i < n_nodes; i++) {
+            const int32_t f = fill_c[i];
+            if (f < 0) continue;
+            if (new_off[f] < 0) new_off[f] = (int32_t)used.size();
+            used.push_back(nodes[i]);
+            node_fill.push_back(f);
+        }
+        for (size_t f = 0; f < fills.size(); f++)
+            if (!from_extra[f]) fills[f].node_off = new_off[f];
+        first = used.data();
+        n_first = used.size();
+    } else {
+        node_fill = fill_c;
+    }
+    for (size_t f = 0; f < fills.size(); f++)
+        if (from_extra[f]) fills[f].node_off += (int32_t)n_first;
+    node_fill.insert(node_fill.end(), fill_s.begin(), fill_s.end());
+    if (n_first + extra.size() > 0x7FFFFFFF) {
+        set_error("batch too large");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    return run_jobs(c, jobs, first, (int32_t)n_first, fills, node_fill, grads, grad_of_fill, extra.data(),
+                    (int32_t)extra.size());
+}
+
 // SurfaceCompositor.run's precision upgrade and bounds
 // (src/compositor.zig:310-387): fills the geometry of J and sets `empty`
 // when nothing is drawn.
@@ -867,6 +1037,13 @@ Z2D_API int z2dgpu_stroke_contours(const z2d_node *nodes, size_t n_nodes, const 
     if (n_contours) *n_contours = nc;
     if (scale) *scale = sc;
     return Z2D_OK;
+}
+
+Z2D_API int z2dgpu_draw_jobs(z2dgpu_ctx *c, const z2d_job *jobs, size_t n_jobs, const z2d_node *nodes, size_t n_nodes,
+                             const z2d_draw_cmd *cmds, size_t n_cmds) {
+    if (!c) return Z2D_ERR_INVALID_ARGUMENT;
+    Z2D_CUDA(cudaSetDevice(c->device));
+    return draw_jobs(*c, jobs, n_jobs, nodes, n_nodes, cmds, n_cmds);
 }
 
 Z2D_API int z2dgpu_fill_jobs(z2dgpu_ctx *c, const z2d_job *jobs, size_t n_jobs, const z2d_node *nodes, size_t n_nodes,

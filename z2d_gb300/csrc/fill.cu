@@ -1585,9 +1585,11 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
 // ----------------------------------------------------------- host side
 static inline unsigned grid_for(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
-int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n_nodes, std::vector<FillCmd> &fills,
+int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n_first, std::vector<FillCmd> &fills,
              const std::vector<int32_t> &node_fill, const std::vector<DevGradient> &grads,
-             const std::vector<int32_t> &grad_of_fill) {
+             const std::vector<int32_t> &grad_of_fill, const z2d_node *nodes2, int32_t n_second) {
+    if (n_first < 0 || n_second < 0 || (int64_t)n_first + n_second > 0x7FFFFFFF) return Z2D_ERR_INVALID_ARGUMENT;
+    const int32_t n_nodes = n_first + n_second;
     const int32_t n_fills = (int32_t)fills.size();
     const int32_t n_jobs = (int32_t)jobs.size();
     if (n_fills == 0 || n_nodes == 0 || n_jobs == 0) return Z2D_OK;
@@ -1614,7 +1616,8 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
         if (grad_of_fill[i] >= 0) fills[i].src.grad = dgrads + grad_of_fill[i];
     // make sure the previous call's kernels no longer read the staging buffer
     Z2D_CUDA(cudaStreamSynchronize(c.stream));
-    memcpy(h + o_nodes, nodes, sizeof(z2d_node) * (size_t)n_nodes);
+    if (n_first > 0) memcpy(h + o_nodes, nodes, sizeof(z2d_node) * (size_t)n_first);
+    if (n_second > 0) memcpy(h + o_nodes + sizeof(z2d_node) * (size_t)n_first, nodes2, sizeof(z2d_node) * (size_t)n_second);
     memcpy(h + o_nfill, node_fill.data(), sizeof(int32_t) * (size_t)n_nodes);
     if (!grads.empty()) memcpy(h + o_grads, grads.data(), sizeof(DevGradient) * grads.size());
     memcpy(h + o_fills, fills.data(), sizeof(FillCmd) * (size_t)n_fills);

@@ -136,8 +136,10 @@ struct DevJob {
 // independent).  `fills` hold the prepared commands grouped by job (node
 // offsets into `nodes`, host memory); grad_of_fill[i] >= 0 names the
 // gradient of fill i in `grads`.
-int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n_nodes, std::vector<FillCmd> &fills,
+// The node array is nodes[0, n_first) followed by nodes2[0, n_second)
+// (node_fill covers both).
+int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n_first, std::vector<FillCmd> &fills,
              const std::vector<int32_t> &node_fill, const std::vector<DevGradient> &grads,
-             const std::vector<int32_t> &grad_of_fill);
+             const std::vector<int32_t> &grad_of_fill, const z2d_node *nodes2 = nullptr, int32_t n_second = 0);
 
 }  // namespace z2dg

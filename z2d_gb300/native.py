@@ -74,6 +74,9 @@ def load(build_if_missing: bool = True):
                                                P(C.c_double), C.c_size_t, P(C.c_uint64), P(C.c_uint64), C.c_size_t,
                                                P(C.c_uint64), P(C.c_double)]
         lib.z2dgpu_stroke.restype = C.c_int
+        lib.z2dgpu_draw_jobs.argtypes = [C.c_void_p, P(abi.z2d_job), C.c_size_t, P(abi.z2d_node), C.c_size_t,
+                                         P(abi.z2d_draw_cmd), C.c_size_t]
+        lib.z2dgpu_draw_jobs.restype = C.c_int
         lib.z2dgpu_stroke_contours.restype = C.c_int
         lib.z2dgpu_fill_jobs.argtypes = [C.c_void_p, P(abi.z2d_job), C.c_size_t, P(abi.z2d_node), C.c_size_t,
                                          P(abi.z2d_fill_cmd), C.c_size_t]

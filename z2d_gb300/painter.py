@@ -146,3 +146,42 @@ def stroke_contours(nodes, opts: Optional["StrokeOptions"] = None, surface_forma
         out.append(pts[2 * start:2 * int(e)].reshape(-1, 2).copy())
         start = int(e)
     return out, sc.value
+
+
+def draw_jobs(jobs, ctx: Optional[Context] = None) -> None:
+    """Fills and strokes over many surfaces in one pass: jobs is a sequence
+    of (surface, ops) with ops a sequence of ("fill", pattern, nodes,
+    FillOptions) or ("stroke", pattern, nodes, StrokeOptions), drawn in
+    order on their device-resident surface."""
+    ctx = ctx or default_context()
+    keep: list = []
+    node_arrays = []
+    n_cmds = sum(len(o) for _, o in jobs)
+    cmds = (abi.z2d_draw_cmd * max(1, n_cmds))()
+    jarr = (abi.z2d_job * max(1, len(jobs)))()
+    off = ci = 0
+    for j, (surface, ops) in enumerate(jobs):
+        jarr[j].surface = surface.to_abi()
+        jarr[j].cmd_offset = ci
+        jarr[j].n_cmds = len(ops)
+        for kind, pat, nodes, opts in ops:
+            arr = nodes if isinstance(nodes, np.ndarray) and nodes.dtype == NODE_DTYPE else None
+            if arr is None:
+                from .path import nodes_array
+                arr = nodes_array(nodes)
+            node_arrays.append(arr)
+            p = pat.to_abi(keep)
+            cmds[ci].pattern = C.pointer(p)
+            cmds[ci].node_offset = off
+            cmds[ci].n_nodes = len(arr)
+            if kind == "fill":
+                cmds[ci].kind = abi.DRAW_FILL
+                cmds[ci].fill = opts.to_abi()
+            else:
+                cmds[ci].kind = abi.DRAW_STROKE
+                cmds[ci].stroke = opts.to_abi(keep)
+            off += len(arr)
+            ci += 1
+    all_nodes = np.ascontiguousarray(np.concatenate(node_arrays) if node_arrays else np.zeros(0, NODE_DTYPE))
+    check(ctx.lib.z2dgpu_draw_jobs(ctx.handle, jarr, len(jobs), all_nodes.ctypes.data_as(C.POINTER(abi.z2d_node)),
+                                   len(all_nodes), cmds, n_cmds))
