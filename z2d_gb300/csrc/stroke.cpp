@@ -10,57 +10,29 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
-#include <list>
+#include <utility>
 #include <vector>
 
 #include "stroke.h"
+#include "stroke_geom.h"
 
 namespace z2dg {
 namespace stroke {
 namespace {
 
-struct Pt {
-    double x, y;
-};
-inline bool eq(Pt a, Pt b) { return a.x == b.x && a.y == b.y; }
-
-// Transformation.zig
-struct Tf {
-    double ax, by, cx, dy, tx, ty;
-};
-const Tf kIdentity{1, 0, 0, 1, 0, 0};
-inline bool tf_equal(const Tf &a, const Tf &b) {
-    return a.ax == b.ax && a.by == b.by && a.cx == b.cx && a.dy == b.dy && a.tx == b.tx && a.ty == b.ty;
-}
-inline double determinant(const Tf &a) { return a.ax * a.dy - a.by * a.cx; }
-// Transformation.inverse (Transformation.zig:103-162)
-bool inverse(const Tf &a, Tf &out) {
-    if (a.by == 0 && a.cx == 0) {
-        if (a.ax == 0 || a.dy == 0) return false;
-        if (a.ax != 1 || a.dy != 1) {
-            out = Tf{1 / a.ax, 0, 0, 1 / a.dy, -a.tx / a.ax, -a.ty / a.dy};
-        } else {
-            out = Tf{1, 0, 0, 1, -a.tx, -a.ty};
-        }
-        return true;
-    }
-    const double det = determinant(a);
-    if (det == 0) return false;
-    const Tf adj{a.dy, -a.by, -a.cx, a.ax, a.by * a.ty - a.dy * a.tx, a.cx * a.tx - a.ax * a.ty};
-    const double s = 1 / det;  // mulScalar(1 / det)
-    out = Tf{adj.ax * s, adj.by * s, adj.cx * s, adj.dy * s, adj.tx * s, adj.ty * s};
-    return true;
-}
-inline void user_to_device_distance(const Tf &a, double &x, double &y) {
-    const double ix = x, iy = y;
-    x = a.ax * ix + a.by * iy;
-    y = a.cx * ix + a.dy * iy;
-}
-inline void device_to_user_distance(const Tf &a, double &x, double &y) {
-    Tf inv;
-    inverse(a, inv);  // validated by the caller
-    user_to_device_distance(inv, x, y);
-}
+using sg::compare;
+using sg::compare_for_miter_limit;
+using sg::determinant;
+using sg::eq;
+using sg::Face;
+using sg::intersect;
+using sg::normalized;
+using sg::PenVertex;
+using sg::Pt;
+using sg::slope;
+using sg::Slope;
+using sg::Tf;
+using sg::user_to_device_distance;
 
 // arc.transformed_circle_major_axis (arc.zig:92-262)
 double transformed_circle_major_axis(const Tf &m, double radius) {
@@ -79,71 +51,8 @@ double transformed_circle_major_axis(const Tf &m, double radius) {
     return radius * std::sqrt(f + std::hypot(g, h));
 }
 
-// Slope.zig
-struct Slope {
-    double dx, dy;
-};
-inline Slope slope(Pt a, Pt b) { return Slope{b.x - a.x, b.y - a.y}; }
-inline int fsign(double v) { return v > 0 ? 1 : (v < 0 ? -1 : 0); }
-// Slope.compare (Slope.zig:46-85)
-int compare(Slope a, Slope b) {
-    const double fe = 2.220446049250313e-16;  // floatEps(f64)
-    const double bdy = (std::fabs(b.dy - a.dy) > fe) ? b.dy : a.dy;
-    const double bdx = (std::fabs(b.dx - a.dx) > fe) ? b.dx : a.dx;
-    const int cmp = fsign(a.dy * bdx - bdy * a.dx);
-    if (cmp != 0) return cmp;
-    if (a.dx == 0 && a.dy == 0 && bdx == 0 && bdy == 0) return 0;
-    if (a.dx == 0 && a.dy == 0) return 1;
-    if (bdx == 0 && bdy == 0) return -1;
-    if (fsign(a.dx) != fsign(bdx) || fsign(a.dy) != fsign(bdy)) return (a.dx > 0 || (a.dx == 0 && a.dy > 0)) ? -1 : 1;
-    return 0;
-}
-// Slope.normalize (Slope.zig:117-146)
-double normalize(Slope &s) {
-    double rx, ry, mag;
-    if (s.dx == 0.0) {
-        rx = 0.0;
-        if (s.dy > 0.0) {
-            mag = s.dy;
-            ry = 1.0;
-        } else {
-            mag = -s.dy;
-            ry = -1.0;
-        }
-    } else if (s.dy == 0.0) {
-        ry = 0.0;
-        if (s.dx > 0.0) {
-            mag = s.dx;
-            rx = 1.0;
-        } else {
-            mag = -s.dx;
-            rx = -1.0;
-        }
-    } else {
-        mag = std::hypot(s.dx, s.dy);
-        rx = s.dx / mag;
-        ry = s.dy / mag;
-    }
-    s.dx = rx;
-    s.dy = ry;
-    return mag;
-}
-inline Slope normalized(Slope s) {
-    normalize(s);
-    return s;
-}
-// Slope.compare_for_miter_limit (Slope.zig:88-105)
-bool compare_for_miter_limit(Slope in, Slope out, double miter_limit) {
-    const Slope a = normalized(in), b = normalized(out);
-    const double in_dot_out = a.dx * b.dx + a.dy * b.dy;
-    return 2 <= miter_limit * miter_limit * (1 + in_dot_out);
-}
 
 // Pen.zig
-struct PenVertex {
-    Pt point;
-    Slope slope_cw, slope_ccw;
-};
 struct Pen {
     std::vector<PenVertex> v;
     bool ok = false;
@@ -186,146 +95,73 @@ Pen make_pen(double thickness, double tolerance, const Tf &ctm) {
     }
     return pen;
 }
-// Pen.vertexIteratorFor (Pen.zig:100-195): the vertex indices to visit.
-std::vector<int32_t> pen_vertices_for(const Pen &pen, Slope from, Slope to, bool clockwise) {
-    const int32_t len = (int32_t)pen.v.size();
-    int32_t start = 0, end = 0;
-    auto V = [&](int32_t k) -> const PenVertex & { return pen.v[(size_t)k]; };
-    if (len == 0) return {};
-    if (clockwise) {
-        int32_t low = 0, high = len, i = (low + high) >> 1;
-        while (high - low > 1) {
-            if (compare(V(i).slope_cw, from) < 0) low = i;
-            else high = i;
-            i = (low + high) >> 1;
-        }
-        if (compare(V(i).slope_cw, from) < 0) {
-            i += 1;
-            if (i == len) i = 0;
-        }
-        start = i;
-        if (compare(to, V(i).slope_ccw) >= 0) {
-            low = i;
-            high = i + len;
-            i = (low + high) >> 1;
-            while (high - low > 1) {
-                const int32_t j = i >= len ? i - len : i;
-                if (compare(V(j).slope_cw, to) > 0) high = i;
-                else low = i;
-                i = (low + high) >> 1;
-            }
-            if (i >= len) i -= len;
-        }
-        end = i;
-    } else {
-        int32_t low = 0, high = len, i = (low + high) >> 1;
-        while (high - low > 1) {
-            if (compare(from, V(i).slope_ccw) < 0) low = i;
-            else high = i;
-            i = (low + high) >> 1;
-        }
-        if (compare(from, V(i).slope_ccw) < 0) {
-            i += 1;
-            if (i == len) i = 0;
-        }
-        start = i;
-        if (compare(V(i).slope_cw, to) <= 0) {
-            low = i;
-            high = i + len;
-            i = (low + high) >> 1;
-            while (high - low > 1) {
-                const int32_t j = i >= len ? i - len : i;
-                if (compare(to, V(j).slope_ccw) > 0) high = i;
-                else low = i;
-                i = (low + high) >> 1;
-            }
-            if (i >= len) i -= len;
-        }
-        end = i;
-    }
-    // VertexIterator.next (Pen.zig:204-222)
-    std::vector<int32_t> out;
-    int32_t idx = std::max(0, start);
-    const int32_t e = std::max(0, end);
-    while (idx != e) {
-        out.push_back(idx);
-        if (clockwise) {
-            idx += 1;
-            if (idx == len) idx = 0;
-        } else {
-            if (idx == 0) idx = len;
-            idx -= 1;
-        }
-        if (out.size() > (size_t)len + 1) break;  // cannot happen; guards a corrupt pen
-    }
-    return out;
-}
-
-// Face.zig
-struct Face {
-    Pt p0, p1;
-    double width;
-    Slope dev_slope, user_slope;
-    double half_width;
-    Pt p0_cw, p0_ccw, p1_cw, p1_ccw;
-    Tf ctm;
+// A doubly linked list of points whose nodes live in one per-thread arena
+// (reset by each plot call), so that inserting a point allocates nothing
+// and splicing two lists is O(1).  Position -1 is end().
+struct ListNode {
+    Pt p;
+    int32_t prev, next;
 };
-Face face_init2(Pt p0, Pt p1, Slope dev_slope, double thickness, const Tf &ctm) {
-    const double half = thickness / 2;
-    double ox, oy;
-    Slope user_slope = dev_slope;
-    if (!tf_equal(ctm, kIdentity)) {
-        double dx = dev_slope.dx, dy = dev_slope.dy;
-        device_to_user_distance(ctm, dx, dy);
-        user_slope = normalized(Slope{dx, dy});
-        if (determinant(ctm) >= 0) {
-            ox = -user_slope.dy * half;
-            oy = user_slope.dx * half;
-        } else {
-            ox = user_slope.dy * half;
-            oy = -user_slope.dx * half;
-        }
-        user_to_device_distance(ctm, ox, oy);
-    } else {
-        ox = -dev_slope.dy * half;
-        oy = dev_slope.dx * half;
+thread_local std::vector<ListNode> t_arena;
+
+struct PtList {
+    int32_t head = -1, tail = -1;
+    size_t n = 0;
+    using It = int32_t;
+    It begin() const { return head; }
+    It end() const { return -1; }
+    size_t size() const { return n; }
+    void clear() {
+        head = tail = -1;
+        n = 0;
     }
-    const double cwx = ox, cwy = oy, ccwx = -cwx, ccwy = -cwy;
-    Face f;
-    f.p0 = p0;
-    f.p1 = p1;
-    f.width = thickness;
-    f.dev_slope = dev_slope;
-    f.user_slope = user_slope;
-    f.half_width = half;
-    f.p0_cw = Pt{p0.x + cwx, p0.y + cwy};
-    f.p0_ccw = Pt{p0.x + ccwx, p0.y + ccwy};
-    f.p1_cw = Pt{p1.x + cwx, p1.y + cwy};
-    f.p1_ccw = Pt{p1.x + ccwx, p1.y + ccwy};
-    f.ctm = ctm;
-    return f;
-}
-// Face.init (Face.zig:41-48)
-Face face_init(Pt p0, Pt p1, double thickness, const Tf &ctm) {
-    return face_init2(p0, p1, normalized(slope(p0, p1)), thickness, ctm);
-}
-// Face.intersect (Face.zig:96-125)
-Pt intersect(const Face &in, const Face &out, bool clockwise) {
-    const Pt ip = clockwise ? in.p1_ccw : in.p1_cw;
-    const Pt op = clockwise ? out.p0_ccw : out.p0_cw;
-    const Slope is = normalized(in.dev_slope), os = normalized(out.dev_slope);
-    const double ry = ((op.x - ip.x) * is.dy * os.dy - op.y * os.dx * is.dy + ip.y * is.dx * os.dy) /
-                      (is.dx * os.dy - os.dx * is.dy);
-    const double rx = (std::fabs(is.dy) >= std::fabs(os.dy)) ? (ry - ip.y) * is.dx / is.dy + ip.x
-                                                              : (ry - op.y) * os.dx / os.dy + op.x;
-    return Pt{rx, ry};
-}
+    void insert(It before, Pt p) {
+        const int32_t k = (int32_t)t_arena.size();
+        if (before < 0) {
+            t_arena.push_back(ListNode{p, tail, -1});
+            if (tail >= 0) t_arena[(size_t)tail].next = k;
+            else head = k;
+            tail = k;
+        } else {
+            const int32_t pv = t_arena[(size_t)before].prev;
+            t_arena.push_back(ListNode{p, pv, before});
+            t_arena[(size_t)before].prev = k;
+            if (pv >= 0) t_arena[(size_t)pv].next = k;
+            else head = k;
+        }
+        n++;
+    }
+    void push_back(Pt p) { insert(-1, p); }
+    void push_front(Pt p) { insert(head, p); }
+    // std::list::splice(end(), other): other's points move to the back
+    void splice_back(PtList &o) {
+        if (o.head < 0) return;
+        if (tail >= 0) {
+            t_arena[(size_t)tail].next = o.head;
+            t_arena[(size_t)o.head].prev = tail;
+        } else {
+            head = o.head;
+        }
+        tail = o.tail;
+        n += o.n;
+        o.clear();
+    }
+    void swap(PtList &o) {
+        std::swap(head, o.head);
+        std::swap(tail, o.tail);
+        std::swap(n, o.n);
+    }
+    template <class F>
+    void for_each(F &&f) const {
+        for (int32_t i = head; i >= 0; i = t_arena[(size_t)i].next) f(t_arena[(size_t)i].p);
+    }
+};
 
 // Polygon.Contour: a doubly linked list of scaled points.
 struct Contour {
-    std::list<Pt> pts;
+    PtList pts;
     double scale = 1;
-    using It = std::list<Pt>::iterator;
+    using It = PtList::It;
     void plot(Pt p, It before) { pts.insert(before, Pt{p.x * scale, p.y * scale}); }
     void plot(Pt p) { pts.push_back(Pt{p.x * scale, p.y * scale}); }
     void plot_reverse(Pt p) { pts.push_front(Pt{p.x * scale, p.y * scale}); }
@@ -436,10 +272,10 @@ struct Common {
     void emit(const Contour &c) {
         std::vector<double> pts;
         pts.reserve(c.pts.size() * 2);
-        for (const Pt &p : c.pts) {
+        c.pts.for_each([&](Pt p) {
             pts.push_back(p.x);
             pts.push_back(p.y);
-        }
+        });
         result.push_back(std::move(pts));
     }
 
@@ -449,8 +285,8 @@ struct Common {
             if (sd.clockwise < 0) sd.clockwise = 0;
             return;
         }
-        const Face in = face_init(p0, p1, o.thickness, ctm);
-        const Face out = face_init(p1, p2, o.thickness, ctm);
+        const Face in = sg::face_init(p0, p1, o.thickness, ctm);
+        const Face out = sg::face_init(p1, p2, o.thickness, ctm);
         const bool jcw = compare(in.dev_slope, out.dev_slope) < 0;
         const bool pcw = sd.clockwise >= 0 ? sd.clockwise != 0 : jcw;
         const bool switched = jcw != pcw;
@@ -481,8 +317,11 @@ struct Common {
             }
         } else {
             plot_outer(jcw ? in.p1_ccw : in.p1_cw);
-            for (int32_t k : pen_vertices_for(pen, in.dev_slope, out.dev_slope, jcw)) {
-                const Pt v = pen.v[(size_t)k].point;
+            const int32_t len = (int32_t)pen.v.size();
+            int32_t start;
+            const int32_t n = sg::pen_range(pen.v.data(), len, in.dev_slope, out.dev_slope, jcw, start);
+            for (int32_t k = 0; k < n; k++) {
+                const Pt v = pen.v[(size_t)sg::pen_step(start, k, len, jcw)].point;
                 plot_outer(Pt{p1.x + v.x, p1.y + v.y});
             }
             plot_outer(jcw ? out.p0_ccw : out.p0_cw);
@@ -506,7 +345,7 @@ struct Common {
             }
         } else if (o.cap == kCapSquare) {
             double ox = f.user_slope.dx * f.half_width, oy = f.user_slope.dy * f.half_width;
-            user_to_device_distance(f.ctm, ox, oy);
+            user_to_device_distance(ctm, ox, oy);
             if (cw) {
                 sink(f.p1_ccw);
                 sink(Pt{f.p1_ccw.x + ox, f.p1_ccw.y + oy});
@@ -520,8 +359,12 @@ struct Common {
             }
         } else {
             sink(cw ? f.p1_ccw : f.p1_cw);
-            for (int32_t k : pen_vertices_for(pen, f.dev_slope, Slope{-f.dev_slope.dx, -f.dev_slope.dy}, cw)) {
-                const Pt v = pen.v[(size_t)k].point;
+            const int32_t len = (int32_t)pen.v.size();
+            int32_t start;
+            const int32_t n =
+                sg::pen_range(pen.v.data(), len, f.dev_slope, Slope{-f.dev_slope.dx, -f.dev_slope.dy}, cw, start);
+            for (int32_t k = 0; k < n; k++) {
+                const Pt v = pen.v[(size_t)sg::pen_step(start, k, len, cw)].point;
                 sink(Pt{f.p1.x + v.x, f.p1.y + v.y});
             }
             sink(cw ? f.p1_cw : f.p1_ccw);
@@ -529,7 +372,7 @@ struct Common {
     }
     template <class Sink>
     void cap_p0(const Face &f, bool cw, Sink &&sink) {
-        cap(face_init(f.p1, f.p0, f.width, f.ctm), cw, sink);
+        cap(sg::face_init(f.p1, f.p0, f.width, ctm), cw, sink);
     }
 
     void clear(Side &sd) {
@@ -540,7 +383,7 @@ struct Common {
 
     // plotSingle (stroke_plotter.zig:232-279)
     void plot_single(Side &sd, Pt start, Pt end) {
-        const Face f = face_init(start, end, o.thickness, ctm);
+        const Face f = sg::face_init(start, end, o.thickness, ctm);
         auto sink = [&](Pt p) { sd.outer.plot(p); };
         cap_p0(f, true, sink);
         cap(f, true, sink);
@@ -551,15 +394,15 @@ struct Common {
 
     // plotOpenJoined (stroke_plotter.zig:281-363)
     void plot_open_joined(Side &sd, Pt s0, Pt e0, Pt s1, Pt e1) {
-        const Face fs = face_init(s0, e0, o.thickness, ctm);
-        const Face fe = face_init(s1, e1, o.thickness, ctm);
+        const Face fs = sg::face_init(s0, e0, o.thickness, ctm);
+        const Face fe = sg::face_init(s1, e1, o.thickness, ctm);
         const bool cw = sd.clockwise >= 0 ? sd.clockwise != 0 : true;
         const Contour::It first = sd.outer.pts.begin();  // the insertion point is captured before plotting
         auto before_first = [&](Pt p) { sd.outer.plot(p, first); };
         cap_p0(fs, cw, before_first);
         auto append = [&](Pt p) { sd.outer.plot(p); };
         cap(fe, cw, append);
-        sd.outer.pts.splice(sd.outer.pts.end(), sd.inner.pts);
+        sd.outer.pts.splice_back(sd.inner.pts);
         emit(sd.outer);
         clear(sd);
     }
@@ -572,7 +415,7 @@ struct Common {
             for (const PenVertex &v : pen.v) sd.outer.plot(Pt{p.x + v.point.x, p.y + v.point.y});
             emit(sd.outer);
         } else if (dashed_plotter && o.cap == kCapSquare) {
-            const Face f = face_init2(p, p, slope, o.thickness, ctm);
+            const Face f = sg::face_init2(p, p, slope, o.thickness, ctm);
             double ox = f.user_slope.dx * f.half_width, oy = f.user_slope.dy * f.half_width;
             user_to_device_distance(ctm, ox, oy);
             sd.outer.plot(Pt{f.p1_cw.x - ox, f.p1_cw.y - oy});
@@ -793,8 +636,8 @@ struct DashedPlotter : Common {
             init_points = points;
             init_side.outer.pts.clear();
             init_side.inner.pts.clear();
-            init_side.outer.pts.splice(init_side.outer.pts.end(), sd.outer.pts);
-            init_side.inner.pts.splice(init_side.inner.pts.end(), sd.inner.pts);
+            init_side.outer.pts.splice_back(sd.outer.pts);
+            init_side.inner.pts.splice_back(sd.inner.pts);
             init_side.clockwise = sd.clockwise;
             init_slope = current_slope;
         } else {
@@ -817,8 +660,8 @@ struct DashedPlotter : Common {
     void join_and_cap_initial() {  // joinAndCapInitial (dashed_plotter.zig:531-588)
         if (points.len > 2) {
             join(sd, o.join, points.tail(2), init_points.head(0), init_points.head(1), false, sd.outer.pts.end());
-            sd.outer.pts.splice(sd.outer.pts.end(), init_side.outer.pts);
-            init_side.inner.pts.splice(init_side.inner.pts.end(), sd.inner.pts);
+            sd.outer.pts.splice_back(init_side.outer.pts);
+            init_side.inner.pts.splice_back(sd.inner.pts);
             init_side.outer.pts.swap(sd.outer.pts);
             sd.outer.pts.clear();
             plot_open_joined(init_side, points.head(0), points.head(1), init_points.tail(2), init_points.tail(1));
@@ -916,6 +759,7 @@ bool dashed(const Options &opts) { return opts.n_dashes > 0 && dashes_valid(opts
 
 int plot(const z2d_node *nodes, size_t n_nodes, const Options &opts, std::vector<std::vector<double>> &contours) {
     contours.clear();
+    t_arena.clear();
     if (dashed(opts)) {  // stroke_plotter.plot (stroke_plotter.zig:40-44)
         DashedPlotter p(opts, contours);
         return run(p, nodes, n_nodes);
