@@ -129,6 +129,74 @@ def test_stroke_degenerate_paths(gpu, oracle):
             _cmp(a, b, 0, f"case {k} {cap}")
 
 
+def _multi_subpath_path(rng, w, h):
+    """Several subpaths of every kind the plotter distinguishes: open and
+    closed polylines with curves, lone points, dots, curves whose control
+    points coincide with their ends, paths that return to their start."""
+    nodes = []
+    for _ in range(int(rng.integers(2, 6))):
+        kind = rng.integers(0, 6)
+        x, y = rng.uniform([8, 8], [w - 8, h - 8])
+        nodes.append((abi.MOVE_TO, x, y, 0, 0, 0, 0))
+        if kind == 0:  # lone move_to or dot
+            if rng.random() < 0.5:
+                nodes.append((abi.CLOSE_PATH, 0, 0, 0, 0, 0, 0))
+            continue
+        for _ in range(int(rng.integers(1, 7))):
+            r = rng.random()
+            if r < 0.45:
+                nodes.append((abi.LINE_TO, *rng.uniform([8, 8], [w - 8, h - 8]), 0, 0, 0, 0))
+            elif r < 0.55:  # repeated point
+                last = nodes[-1][1:3] if nodes[-1][0] != abi.CURVE_TO else nodes[-1][5:7]
+                nodes.append((abi.LINE_TO, *last, 0, 0, 0, 0))
+            elif r < 0.65:  # degenerate control points
+                last = nodes[-1][1:3] if nodes[-1][0] != abi.CURVE_TO else nodes[-1][5:7]
+                e = rng.uniform([8, 8], [w - 8, h - 8])
+                nodes.append((abi.CURVE_TO, *last, *e, *e))
+            else:
+                nodes.append((abi.CURVE_TO, *rng.uniform([8, 8, 8, 8, 8, 8], [w - 8, h - 8] * 3)))
+        if kind == 5:
+            nodes.append((abi.LINE_TO, x, y, 0, 0, 0, 0))  # back to the start
+        if kind >= 3:
+            nodes.append((abi.CLOSE_PATH, 0, 0, 0, 0, 0, 0))
+    return nodes
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_multi_subpath_strokes(gpu, oracle, seed):
+    rng = np.random.default_rng(900 + seed)
+    w, h = 180, 140
+    a, b = _bg("rgba", w, h, seed), _bg("rgba", w, h, seed)
+    so = StrokeOracle(oracle)
+    tfs = list(TRANSFORMS.values())
+    for i in range(6):
+        nodes = _multi_subpath_path(rng, w, h)
+        opts = StrokeOptions(line_join=("miter", "round", "bevel")[i % 3], line_cap=("butt", "round", "square")[i // 2 % 3],
+                             line_width=float(rng.choice([0.3, 1.0, 2.0, 4.5, 9.0, 16.0])),
+                             miter_limit=float(rng.choice([1.2, 4.0, 10.0])), transformation=tfs[i % len(tfs)],
+                             tolerance=float(rng.choice([0.05, 0.1, 0.5])))
+        pat = Pattern.from_pixel(random_premultiplied_pixel(rng))
+        assert gpu.stroke(a, pat, nodes, opts) == abi.OK
+        assert so.stroke(b, pat, nodes, opts) == abi.OK
+    _cmp(a, b, 0, f"seed {seed}")
+
+
+def test_stroke_node_sequence_errors(gpu):
+    s = Surface.init("rgba", 20, 20)
+    px = Pattern.from_pixel(Pixel.rgba(1, 2, 3, 4))
+    m, l, c, z = abi.MOVE_TO, abi.LINE_TO, abi.CURVE_TO, abi.CLOSE_PATH
+    bad = [
+        [(l, 1, 1, 0, 0, 0, 0), (l, 5, 5, 0, 0, 0, 0)],                                   # no current point
+        [(m, 1, 1, 0, 0, 0, 0), (l, 5, 5, 0, 0, 0, 0), (z, 0, 0, 0, 0, 0, 0), (l, 9, 9, 0, 0, 0, 0)],
+        [(m, 1, 1, 0, 0, 0, 0), (z, 0, 0, 0, 0, 0, 0), (c, 1, 2, 3, 4, 5, 6)],
+        [(m, 1, 1, 0, 0, 0, 0), (l, float("nan"), 5, 0, 0, 0, 0)],
+    ]
+    for nodes in bad:
+        assert gpu.stroke(s, px, nodes, StrokeOptions(line_width=3.0)) == abi.ERR_INVALID_STATE, nodes
+    ok = [(z, 0, 0, 0, 0, 0, 0), (m, 3, 3, 0, 0, 0, 0), (z, 0, 0, 0, 0, 0, 0), (z, 0, 0, 0, 0, 0, 0), (m, 4, 4, 0, 0, 0, 0)]
+    assert gpu.stroke(s, px, ok, StrokeOptions(line_width=3.0)) == abi.OK
+
+
 def test_stroke_errors(gpu):
     s = Surface.init("rgba", 10, 10)
     nodes = [(abi.MOVE_TO, 1, 1, 0, 0, 0, 0), (abi.LINE_TO, 8, 8, 0, 0, 0, 0)]

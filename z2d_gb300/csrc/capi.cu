@@ -16,6 +16,7 @@
 
 #include "fill.cuh"
 #include "stroke.h"
+#include "stroke_gpu.cuh"
 #include "z2d_internal.h"
 
 namespace z2dg {
@@ -387,6 +388,7 @@ static int prepare_fills(const z2d_surface &s, int32_t job, const z2d_node *node
         F.node_off = (int32_t)cm.node_offset;
         F.n_nodes = (int32_t)cm.n_nodes;
         F.job = job;
+        F.stroke = -1;
         F.aa = (aa == Z2D_AA_NONE || aa == Z2D_AA_SUPERSAMPLE_4X) ? aa : Z2D_AA_MULTISAMPLE_4X;
         F.rule = cm.opts.fill_rule;
         F.op = cm.opts.op;
@@ -529,8 +531,9 @@ int fill_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_node *nod
 // ------------------------------------------------------------------ strokes
 // painter.stroke's option handling (painter.zig:221-304) and the stroke
 // polygon.  aa receives the anti-aliasing mode actually used.
-static int stroke_polygon(const z2d_node *nodes, size_t n_nodes, const z2d_stroke_opts &o, int32_t surface_format,
-                          int &aa, std::vector<std::vector<double>> &contours, double &scale) {
+// painter.stroke's option checks and adjustments (painter.zig:228-304):
+// the rasteriser's AA mode and scale, and the plotter options.
+static int stroke_options(const z2d_stroke_opts &o, int32_t surface_format, int &aa, stroke::Options &so) {
     if (o.line_join < Z2D_JOIN_MITER || o.line_join > Z2D_JOIN_BEVEL || o.line_cap < Z2D_CAP_BUTT ||
         o.line_cap > Z2D_CAP_SQUARE || o.anti_aliasing < Z2D_AA_NONE || o.anti_aliasing > Z2D_AA_SUPERSAMPLE_4X ||
         !(o.line_width == o.line_width) || !(o.tolerance == o.tolerance) || (o.n_dashes > 0 && !o.dashes)) {
@@ -541,10 +544,23 @@ static int stroke_polygon(const z2d_node *nodes, size_t n_nodes, const z2d_strok
         set_error("InvalidMatrix: the stroke transformation cannot be inverted");
         return Z2D_ERR_INVALID_ARGUMENT;
     }
-    contours.clear();
     aa = (surface_format == Z2D_FORMAT_ALPHA1) ? Z2D_AA_NONE : o.anti_aliasing;
-    scale = aa == Z2D_AA_NONE ? 1.0 : 4.0;
-    if (n_nodes == 0) return Z2D_OK;
+    const bool wide = o.line_width >= 2;
+    so.cap = wide ? o.line_cap : Z2D_CAP_BUTT;
+    so.join = wide ? o.line_join : Z2D_JOIN_MITER;
+    so.miter_limit = wide ? o.miter_limit : 10.0;
+    for (int k = 0; k < 6; k++) so.ctm[k] = o.transformation[k];
+    so.scale = aa == Z2D_AA_NONE ? 1.0 : 4.0;
+    so.thickness = o.line_width >= 0.00390625 ? o.line_width : 0.00390625;
+    so.tolerance = std::fmax(o.tolerance, 0.001);
+    so.dashes = o.dashes;
+    so.n_dashes = (size_t)o.n_dashes;
+    so.dash_offset = o.dash_offset;
+    return Z2D_OK;
+}
+
+// The checks of a non-empty stroke's path and dashes.
+static int stroke_checks(const z2d_node *nodes, size_t n_nodes, const z2d_stroke_opts &o) {
     if (!nodes) return Z2D_ERR_INVALID_ARGUMENT;
     if (o.hairline) {
         set_error("hairline strokes are not supported on the GPU path yet");
@@ -560,19 +576,20 @@ static int stroke_polygon(const z2d_node *nodes, size_t n_nodes, const z2d_strok
             set_error("node: bad tag");
             return Z2D_ERR_INVALID_ARGUMENT;
         }
-    const bool wide = o.line_width >= 2;
+    return Z2D_OK;
+}
+
+static int stroke_polygon(const z2d_node *nodes, size_t n_nodes, const z2d_stroke_opts &o, int32_t surface_format,
+                          int &aa, std::vector<std::vector<double>> &contours, double &scale) {
     stroke::Options so;
-    so.cap = wide ? o.line_cap : Z2D_CAP_BUTT;
-    so.join = wide ? o.line_join : Z2D_JOIN_MITER;
-    so.miter_limit = wide ? o.miter_limit : 10.0;
-    for (int k = 0; k < 6; k++) so.ctm[k] = o.transformation[k];
-    so.scale = scale;
-    so.thickness = o.line_width >= 0.00390625 ? o.line_width : 0.00390625;
-    so.tolerance = std::fmax(o.tolerance, 0.001);
-    so.dashes = o.dashes;
-    so.n_dashes = (size_t)o.n_dashes;
-    so.dash_offset = o.dash_offset;
-    const int rc = stroke::plot(nodes, n_nodes, so, contours);
+    contours.clear();
+    int rc = stroke_options(o, surface_format, aa, so);
+    if (rc) return rc;
+    scale = so.scale;
+    if (n_nodes == 0) return Z2D_OK;
+    rc = stroke_checks(nodes, n_nodes, o);
+    if (rc) return rc;
+    rc = stroke::plot(nodes, n_nodes, so, contours);
     if (rc) set_error("InvalidState: stroke path node sequence");
     return rc;
 }
@@ -604,65 +621,105 @@ static void contours_to_nodes(const std::vector<std::vector<double>> &contours, 
     }
 }
 
-static int do_stroke(Ctx &c, z2d_surface *surface, const z2d_pattern *pattern, const z2d_node *nodes, size_t n_nodes,
-                     const z2d_stroke_opts &o) {
-    int rc = check_surface(surface);
-    if (rc) return rc;
-    if (pattern->kind == Z2D_PATTERN_PIXEL) {  // painter.zig:221-227
-        rc = check_pixel(pattern->pixel);
-        if (rc) return rc;
-        if (!pixel_premultiplied(pattern->pixel)) {
-            set_error("PixelSourceNotPreMultiplied");
-            return Z2D_ERR_PIXEL_NOT_PREMULTIPLIED;
+// The device stroker's input for one solid stroke: the subpaths the
+// plotter walks (node indices relative to the stroke's nodes) and the pen.
+// The node sequence is checked the way the plotter does: line_to /
+// curve_to need a current point (stroke_plotter.zig:104-150), and after
+// close_path only move_to or close_path may follow.
+struct StrokePrep {
+    std::vector<SubpathDev> subs;
+    int64_t n_local = 0;
+    int32_t pen_n = 0;
+    bool reflect = false;
+};
+static int stroke_prepare(const z2d_node *nodes, size_t n_nodes, const stroke::Options &so, StrokePrep &out) {
+    out.subs.clear();
+    out.n_local = 0;
+    SubpathDev cur{};
+    bool open = false;
+    auto end = [&](bool closed) {
+        cur.closed = closed ? 1 : 0;
+        out.n_local += cur.n_nodes;
+        out.subs.push_back(cur);
+        open = false;
+    };
+    if (n_nodes > 0x7FFFFFFF) return Z2D_ERR_INVALID_ARGUMENT;
+    for (size_t i = 0; i < n_nodes; i++) {
+        const z2d_node &nd = nodes[i];
+        const int np = nd.tag == Z2D_CURVE_TO ? 6 : nd.tag == Z2D_CLOSE_PATH ? 0 : 2;
+        for (int k = 0; k < np; k++)
+            if (!std::isfinite(nd.p[k])) {
+                set_error("InvalidState: non-finite coordinate");
+                return Z2D_ERR_INVALID_STATE;
+            }
+        switch (nd.tag) {
+            case Z2D_MOVE_TO:
+                if (open) end(false);
+                cur = SubpathDev{};
+                cur.node0 = (int32_t)i;
+                cur.n_nodes = 1;
+                open = true;
+                break;
+            case Z2D_LINE_TO:
+            case Z2D_CURVE_TO:
+                if (!open) {
+                    set_error("InvalidState: stroke path node sequence");
+                    return Z2D_ERR_INVALID_STATE;
+                }
+                cur.n_nodes++;
+                break;
+            default:
+                if (open) end(true);
+                break;
         }
     }
-    std::vector<std::vector<double>> contours;
-    int aa = 0;
-    double scale = 1;
-    rc = stroke_polygon(nodes, n_nodes, o, surface->format, aa, contours, scale);
-    if (rc || n_nodes == 0) return rc;
-    std::vector<z2d_node> cn;
-    contours_to_nodes(contours, cn);
-    if (cn.empty()) return Z2D_OK;
-    z2d_fill_cmd cmd;
-    cmd.pattern = pattern;
-    cmd.node_offset = 0;
-    cmd.n_nodes = cn.size();
-    cmd.opts.anti_aliasing = aa;
-    cmd.opts.fill_rule = Z2D_FILL_NON_ZERO;  // painter.zig:306-341
-    cmd.opts.op = o.op;
-    cmd.opts.precision = o.precision;
-    cmd.opts.tolerance = o.tolerance;
-    std::vector<FillCmd> fills;
-    std::vector<int32_t> node_fill(cn.size(), -1), grad_of_fill;
-    std::vector<DevGradient> grads;
-    rc = prepare_fills(*surface, 0, cn.data(), cn.size(), &cmd, 1, fills, node_fill, grads, grad_of_fill);
-    if (rc || fills.empty()) return rc;
-    fills[0].edge_scale = 1.0;  // contour points are already scaled
-    std::vector<DevJob> jobs(1);
-    memset(jobs.data(), 0, sizeof(DevJob));
-    rc = stage_in(c, *surface, c.surface, jobs[0].sfc);
-    if (rc) return rc;
-    jobs[0].fill0 = 0;
-    jobs[0].fill1 = 1;
-    const DevSurface ds = jobs[0].sfc;
-    rc = run_jobs(c, jobs, cn.data(), (int32_t)cn.size(), fills, node_fill, grads, grad_of_fill);
-    if (rc) return rc;
-    return stage_out(c, *surface, ds);
+    if (open) end(false);
+    out.pen_n = stroke::pen_vertex_count(so.thickness, so.tolerance, so.ctm);
+    out.reflect = so.ctm[0] * so.ctm[3] - so.ctm[1] * so.ctm[2] < 0;
+    return Z2D_OK;
 }
 
-// Fills and strokes over many device surfaces.  Stroke polygons are built
-// on host threads first (each command independently), then every command
-// becomes a prepared fill: strokes as their contours (already-scaled nodes
-// appended after the caller's, edge scale 1), fills on the caller's nodes.
+// A prepared fill drawing a pattern with given options (the pattern part
+// of prepare_fills), for polygons that come from elsewhere than nodes.
+static int prepare_polygon_fill(const z2d_surface &s, int32_t job, const z2d_pattern *pattern, int aa, int32_t op,
+                                int32_t precision, double tolerance, std::vector<FillCmd> &fills,
+                                std::vector<DevGradient> &grads, std::vector<int32_t> &grad_of_fill) {
+    z2d_fill_cmd fc;
+    memset(&fc, 0, sizeof(fc));
+    fc.pattern = pattern;
+    fc.opts.anti_aliasing = aa;
+    fc.opts.fill_rule = Z2D_FILL_NON_ZERO;  // painter.zig:306-341
+    fc.opts.op = op;
+    fc.opts.precision = precision;
+    fc.opts.tolerance = tolerance;
+    // one placeholder node so that prepare_fills keeps the command
+    z2d_node nd[2];
+    memset(nd, 0, sizeof(nd));
+    nd[0].tag = Z2D_MOVE_TO;
+    nd[1].tag = Z2D_CLOSE_PATH;
+    fc.n_nodes = 2;
+    std::vector<int32_t> owner(2, -1);
+    const int rc = prepare_fills(s, job, nd, 2, &fc, 1, fills, owner, grads, grad_of_fill);
+    if (rc) return rc;
+    fills.back().node_off = 0;
+    fills.back().n_nodes = 0;
+    fills.back().edge_scale = 1.0;  // the stroker's points are already scaled
+    return Z2D_OK;
+}
+
+// Fills and strokes over many device surfaces.  Solid strokes are
+// tessellated on the device from the caller's nodes; dashed strokes are
+// built on host threads (each command independently) and drawn as their
+// contours (already-scaled nodes appended after the caller's, edge scale
+// 1); fills use the caller's nodes.  The caller's node array is uploaded
+// as it is.
 static int draw_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_node *nodes, size_t n_nodes,
-              const z2d_draw_cmd *cmds, size_t n_cmds) {
+                     const z2d_draw_cmd *cmds, size_t n_cmds) {
     if ((n_jobs > 0 && !jobs_in) || (n_cmds > 0 && !cmds) || (n_nodes > 0 && !nodes)) return Z2D_ERR_INVALID_ARGUMENT;
-    if (n_jobs > 0x7FFFFFF || n_cmds > 0x7FFFFFF) {
+    if (n_jobs > 0x7FFFFFF || n_cmds > 0x7FFFFFF || n_nodes > 0x7FFFFFFF) {
         set_error("batch too large");
         return Z2D_ERR_INVALID_ARGUMENT;
     }
-    // stroke polygons, in parallel
     std::vector<size_t> strokes;
     for (size_t i = 0; i < n_cmds; i++) {
         if (cmds[i].kind == Z2D_DRAW_STROKE) strokes.push_back(i);
@@ -681,54 +738,79 @@ static int draw_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_no
         }
         for (uint64_t k = 0; k < jb.n_cmds; k++) cmd_fmt[jb.cmd_offset + k] = jb.surface.format;
     }
-    std::vector<std::vector<std::vector<double>>> polys(strokes.size());
-    std::vector<int> aas(strokes.size(), 0), rcs(strokes.size(), 0);
-    std::vector<std::string> errs(strokes.size());
+    // per stroke: options, then the device stroker's input (solid) or the
+    // host-built polygon (dashed), in parallel
+    const size_t ns = strokes.size();
+    std::vector<std::vector<std::vector<double>>> polys(ns);
+    std::vector<StrokePrep> preps(ns);
+    std::vector<stroke::Options> sopts(ns);
+    std::vector<uint8_t> on_device(ns, 0);
+    std::vector<int> aas(ns, 0), rcs(ns, 0);
+    std::vector<std::string> errs(ns);
     {
-        const size_t nt = std::max<size_t>(1, std::min<size_t>(std::thread::hardware_concurrency(), strokes.size() / 64 + 1));
+        const size_t nt = std::max<size_t>(1, std::min<size_t>(std::thread::hardware_concurrency(), ns / 256 + 1));
         std::atomic<size_t> next{0};
         auto work = [&] {
-            for (size_t k; (k = next.fetch_add(1)) < strokes.size();) {
+            for (size_t k; (k = next.fetch_add(1)) < ns;) {
                 const z2d_draw_cmd &cm = cmds[strokes[k]];
                 if (!cm.pattern || cm.node_offset > n_nodes || cm.n_nodes > n_nodes - cm.node_offset) {
                     rcs[k] = Z2D_ERR_INVALID_ARGUMENT;
                     errs[k] = "stroke command outside the node array";
                     continue;
                 }
-                double sc = 1;
-                rcs[k] = stroke_polygon(nodes + cm.node_offset, cm.n_nodes, cm.stroke, cmd_fmt[strokes[k]], aas[k],
-                                        polys[k], sc);
-                if (rcs[k]) errs[k] = last_error();
+                const z2d_node *nd = nodes + cm.node_offset;
+                int rc = stroke_options(cm.stroke, cmd_fmt[strokes[k]], aas[k], sopts[k]);
+                if (!rc && cm.n_nodes > 0) rc = stroke_checks(nd, cm.n_nodes, cm.stroke);
+                if (!rc && cm.n_nodes > 0) {
+                    if (stroke::dashed(sopts[k])) {
+                        rc = stroke::plot(nd, cm.n_nodes, sopts[k], polys[k]);
+                        if (rc) set_error("InvalidState: stroke path node sequence");
+                    } else {
+                        on_device[k] = 1;
+                        rc = stroke_prepare(nd, cm.n_nodes, sopts[k], preps[k]);
+                    }
+                }
+                rcs[k] = rc;
+                if (rc) errs[k] = last_error();
             }
         };
         std::vector<std::thread> pool;
         for (size_t t = 1; t < nt; t++) pool.emplace_back(work);
         work();
         for (auto &t : pool) t.join();
-        for (size_t k = 0; k < strokes.size(); k++)
+        for (size_t k = 0; k < ns; k++)
             if (rcs[k]) {
                 set_error(errs[k].c_str());
                 return rcs[k];
             }
     }
-    // the strokes' contour nodes, as a second node segment after the caller's
+    // the dashed strokes' contour nodes, as a second node segment
     std::vector<z2d_node> extra;
-    std::vector<uint64_t> stroke_off(strokes.size()), stroke_cnt(strokes.size());
-    std::vector<z2d_node> cn;
-    for (size_t k = 0; k < strokes.size(); k++) {
-        contours_to_nodes(polys[k], cn);
-        stroke_off[k] = extra.size();
-        stroke_cnt[k] = cn.size();
-        extra.insert(extra.end(), cn.begin(), cn.end());
+    std::vector<uint64_t> stroke_off(ns), stroke_cnt(ns);
+    {
+        std::vector<z2d_node> cn;
+        for (size_t k = 0; k < ns; k++) {
+            if (on_device[k]) continue;
+            contours_to_nodes(polys[k], cn);
+            stroke_off[k] = extra.size();
+            stroke_cnt[k] = cn.size();
+            extra.insert(extra.end(), cn.begin(), cn.end());
+        }
+    }
+    if (n_nodes + extra.size() > 0x7FFFFFFF) {
+        set_error("batch too large");
+        return Z2D_ERR_INVALID_ARGUMENT;
     }
     std::vector<int64_t> stroke_of(n_cmds, -1);
-    for (size_t k = 0; k < strokes.size(); k++) stroke_of[strokes[k]] = (int64_t)k;
+    for (size_t k = 0; k < ns; k++) stroke_of[strokes[k]] = (int64_t)k;
     std::vector<FillCmd> fills;
-    std::vector<uint8_t> from_extra;
-    std::vector<int32_t> fill_c(n_nodes, -1), fill_s(extra.size(), -1), grad_of_fill;
+    std::vector<int32_t> node_fill(n_nodes, -1), fill_s(extra.size(), -1), grad_of_fill;
     std::vector<DevGradient> grads;
     std::vector<DevJob> jobs(n_jobs);
     if (n_jobs > 0) memset(jobs.data(), 0, sizeof(DevJob) * n_jobs);
+    StrokeSet sset;
+    std::vector<std::pair<int32_t, int32_t>> trig_keys;  // (n, reflect) of each table, in trig order
+    std::vector<int32_t> trig_at;
     for (size_t j = 0; j < n_jobs; j++) {
         const z2d_job &jb = jobs_in[j];
         int rc = check_surface(&jb.surface);
@@ -743,20 +825,25 @@ static int draw_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_no
         for (uint64_t q = 0; q < jb.n_cmds; q++) {
             const size_t i = jb.cmd_offset + q;
             const z2d_draw_cmd &cm = cmds[i];
-            z2d_fill_cmd fc;
-            fc.pattern = cm.pattern;
-            const size_t before = fills.size();
             if (cm.kind == Z2D_DRAW_FILL) {
+                z2d_fill_cmd fc;
+                fc.pattern = cm.pattern;
                 fc.node_offset = cm.node_offset;
                 fc.n_nodes = cm.n_nodes;
                 fc.opts = cm.fill;
-                rc = prepare_fills(jb.surface, (int32_t)j, nodes, n_nodes, &fc, 1, fills, fill_c, grads, grad_of_fill);
-            } else {
-                const size_t k = (size_t)stroke_of[i];
-                if (cm.pattern && cm.pattern->kind == Z2D_PATTERN_PIXEL && !pixel_premultiplied(cm.pattern->pixel)) {
-                    set_error("PixelSourceNotPreMultiplied");
-                    return Z2D_ERR_PIXEL_NOT_PREMULTIPLIED;
-                }
+                rc = prepare_fills(jb.surface, (int32_t)j, nodes, n_nodes, &fc, 1, fills, node_fill, grads,
+                                   grad_of_fill);
+                if (rc) return rc;
+                continue;
+            }
+            const size_t k = (size_t)stroke_of[i];
+            if (cm.pattern->kind == Z2D_PATTERN_PIXEL && !pixel_premultiplied(cm.pattern->pixel)) {
+                set_error("PixelSourceNotPreMultiplied");
+                return Z2D_ERR_PIXEL_NOT_PREMULTIPLIED;
+            }
+            if (!on_device[k]) {
+                z2d_fill_cmd fc;
+                fc.pattern = cm.pattern;
                 fc.node_offset = stroke_off[k];
                 fc.n_nodes = stroke_cnt[k];
                 fc.opts.anti_aliasing = aas[k];
@@ -764,59 +851,114 @@ static int draw_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_no
                 fc.opts.op = cm.stroke.op;
                 fc.opts.precision = cm.stroke.precision;
                 fc.opts.tolerance = cm.stroke.tolerance;
+                const size_t before = fills.size();
                 rc = prepare_fills(jb.surface, (int32_t)j, extra.data(), extra.size(), &fc, 1, fills, fill_s, grads,
                                    grad_of_fill);
+                if (rc) return rc;
+                for (size_t f = before; f < fills.size(); f++) {
+                    fills[f].edge_scale = 1.0;  // contour points are already scaled
+                    fills[f].node_off += (int32_t)n_nodes;
+                }
+                continue;
             }
+            // a device-stroked command
+            StrokePrep &pr = preps[k];
+            if (pr.subs.empty()) continue;  // nothing is drawn
+            rc = prepare_polygon_fill(jb.surface, (int32_t)j, cm.pattern, aas[k], cm.stroke.op, cm.stroke.precision,
+                                      cm.stroke.tolerance, fills, grads, grad_of_fill);
             if (rc) return rc;
-            for (size_t f = before; f < fills.size(); f++) {
-                from_extra.push_back(cm.kind == Z2D_DRAW_STROKE);
-                if (cm.kind == Z2D_DRAW_STROKE) fills[f].edge_scale = 1.0;  // contour points are already scaled
+            const stroke::Options &so = sopts[k];
+            StrokeDev S;
+            memset(&S, 0, sizeof(S));
+            S.fill = (int32_t)fills.size() - 1;
+            fills.back().stroke = (int32_t)sset.strokes.size();
+            S.sub0 = (int32_t)sset.subs.size();
+            S.n_sub = (int32_t)pr.subs.size();
+            S.join = so.join;
+            S.cap = so.cap;
+            S.pen_n = pr.pen_n;
+            S.pen_off = (int32_t)sset.n_pen;
+            S.thickness = so.thickness;
+            S.miter_limit = so.miter_limit;
+            S.tolerance = so.tolerance;
+            S.scale = so.scale;
+            for (int t = 0; t < 6; t++) S.ctm[t] = so.ctm[t];
+            // the pen's cos/sin table, shared by pens of the same size and handedness
+            int32_t tab = -1;
+            for (size_t t = 0; t < trig_keys.size(); t++)
+                if (trig_keys[t].first == pr.pen_n && trig_keys[t].second == (int32_t)pr.reflect) {
+                    tab = trig_at[t];
+                    break;
+                }
+            if (tab < 0) {
+                tab = (int32_t)(sset.trig.size() / 2);
+                trig_keys.emplace_back(pr.pen_n, (int32_t)pr.reflect);
+                trig_at.push_back(tab);
+                sset.trig.resize(sset.trig.size() + 2 * (size_t)pr.pen_n);
+                stroke::pen_trig(pr.pen_n, pr.reflect, sset.trig.data() + 2 * (size_t)tab);
+            }
+            S.pen_tab = tab;
+            sset.n_pen += pr.pen_n;
+            for (SubpathDev sp : pr.subs) {
+                sp.node0 += (int32_t)cm.node_offset;
+                sp.local0 = (int32_t)sset.n_local;
+                sp.stroke = (int32_t)sset.strokes.size();
+                sset.n_local += sp.n_nodes;
+                sset.subs.push_back(sp);
+            }
+            sset.strokes.push_back(S);
+            if (sset.n_local > 0x7FFFFFFF || sset.n_pen > 0x7FFFFFFF) {
+                set_error("batch too large");
+                return Z2D_ERR_INVALID_ARGUMENT;
             }
         }
         jobs[j].fill1 = (int32_t)fills.size();
     }
     if (fills.empty()) return Z2D_OK;
-    // the caller's nodes as they are when the fills own them in order,
-    // else compacted; the stroke nodes follow
-    bool in_order = true;
-    {
-        size_t next = 0;
-        for (size_t f = 0; f < fills.size() && in_order; f++) {
-            if (from_extra[f]) continue;
-            if ((size_t)fills[f].node_off != next) in_order = false;
-            next += (size_t)fills[f].n_nodes;
-        }
-        in_order = in_order && next == n_nodes;
-    }
-    std::vector<z2d_node> used;
-    std::vector<int32_t> node_fill;
-    const z2d_node *first = nodes;
-    size_t n_first = n_nodes;
-    if (!in_order) {
-        std::vector<int32_t> new_off(fills.size(), -1);
-        for (size_t i = 0; i < n_nodes; i++) {
-            const int32_t f = fill_c[i];
-            if (f < 0) continue;
-            if (new_off[f] < 0) new_off[f] = (int32_t)used.size();
-            used.push_back(nodes[i]);
-            node_fill.push_back(f);
-        }
-        for (size_t f = 0; f < fills.size(); f++)
-            if (!from_extra[f]) fills[f].node_off = new_off[f];
-        first = used.data();
-        n_first = used.size();
-    } else {
-        node_fill = fill_c;
-    }
-    for (size_t f = 0; f < fills.size(); f++)
-        if (from_extra[f]) fills[f].node_off += (int32_t)n_first;
     node_fill.insert(node_fill.end(), fill_s.begin(), fill_s.end());
-    if (n_first + extra.size() > 0x7FFFFFFF) {
-        set_error("batch too large");
-        return Z2D_ERR_INVALID_ARGUMENT;
+    return run_jobs(c, jobs, nodes, (int32_t)n_nodes, fills, node_fill, grads, grad_of_fill, extra.data(),
+                    (int32_t)extra.size(), &sset);
+}
+
+static int do_stroke(Ctx &c, z2d_surface *surface, const z2d_pattern *pattern, const z2d_node *nodes, size_t n_nodes,
+                     const z2d_stroke_opts &o) {
+    int rc = check_surface(surface);
+    if (rc) return rc;
+    if (pattern->kind == Z2D_PATTERN_PIXEL) {  // painter.zig:221-227
+        rc = check_pixel(pattern->pixel);
+        if (rc) return rc;
+        if (!pixel_premultiplied(pattern->pixel)) {
+            set_error("PixelSourceNotPreMultiplied");
+            return Z2D_ERR_PIXEL_NOT_PREMULTIPLIED;
+        }
     }
-    return run_jobs(c, jobs, first, (int32_t)n_first, fills, node_fill, grads, grad_of_fill, extra.data(),
-                    (int32_t)extra.size());
+    int aa = 0;
+    stroke::Options so;
+    rc = stroke_options(o, surface->format, aa, so);
+    if (rc || n_nodes == 0) return rc;
+    rc = stroke_checks(nodes, n_nodes, o);
+    if (rc) return rc;
+    // one job on the (staged) surface
+    DevSurface ds;
+    rc = stage_in(c, *surface, c.surface, ds);
+    if (rc) return rc;
+    z2d_job jb;
+    memset(&jb, 0, sizeof(jb));
+    jb.surface = *surface;
+    jb.surface.location = Z2D_MEM_DEVICE;
+    jb.surface.data = ds.data;
+    jb.cmd_offset = 0;
+    jb.n_cmds = 1;
+    z2d_draw_cmd cm;
+    memset(&cm, 0, sizeof(cm));
+    cm.kind = Z2D_DRAW_STROKE;
+    cm.pattern = pattern;
+    cm.node_offset = 0;
+    cm.n_nodes = n_nodes;
+    cm.stroke = o;
+    rc = draw_jobs(c, &jb, 1, nodes, n_nodes, &cm, 1);
+    if (rc) return rc;
+    return stage_out(c, *surface, ds);
 }
 
 // SurfaceCompositor.run's precision upgrade and bounds
@@ -943,11 +1085,12 @@ Z2D_API int z2dgpu_ctx_destroy(z2dgpu_ctx *c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     DevBuf *bufs[] = {&c->params, &c->nodes, &c->node_info, &c->edges, &c->fill_state, &c->counters, &c->band_fills,
-                      &c->bins, &c->bin_offsets, &c->masks, &c->surface, &c->surface2, &c->surface3, &c->scan_tmp};
+                      &c->bins, &c->bin_offsets, &c->masks, &c->surface, &c->surface2, &c->surface3, &c->scan_tmp,
+                      &c->stroke_a, &c->stroke_b, &c->stroke_c};
     for (DevBuf *b : bufs) b->release();
     c->staging.release();
     c->readback.release();
-    for (Ctx::Timer *t : {&c->t_raster, &c->t_composite, &c->t_flatten, &c->t_bins}) c->timer_collect(*t);
+    for (Ctx::Timer *t : {&c->t_raster, &c->t_composite, &c->t_flatten, &c->t_bins, &c->t_stroke}) c->timer_collect(*t);
     if (c->own_stream) cudaStreamDestroy(c->stream);
     delete c;
     return Z2D_OK;
@@ -963,7 +1106,7 @@ Z2D_API uint64_t z2dgpu_ctx_launch_count(const z2dgpu_ctx *c) { return c ? c->la
 
 Z2D_API int z2dgpu_ctx_set_timing(z2dgpu_ctx *c, int enable) {
     if (!c) return Z2D_ERR_INVALID_ARGUMENT;
-    for (Ctx::Timer *t : {&c->t_raster, &c->t_composite, &c->t_flatten, &c->t_bins}) {
+    for (Ctx::Timer *t : {&c->t_raster, &c->t_composite, &c->t_flatten, &c->t_bins, &c->t_stroke}) {
         c->timer_collect(*t);
         *t = Ctx::Timer{};
     }
@@ -978,6 +1121,7 @@ Z2D_API double z2dgpu_ctx_kernel_ms(z2dgpu_ctx *c, const char *kernel, uint64_t 
     else if (strcmp(kernel, "composite") == 0) t = &c->t_composite;
     else if (strcmp(kernel, "flatten") == 0) t = &c->t_flatten;
     else if (strcmp(kernel, "bins") == 0) t = &c->t_bins;
+    else if (strcmp(kernel, "stroke") == 0) t = &c->t_stroke;
     if (!t) return -1.0;
     c->timer_collect(*t);
     if (launches) *launches = t->n;

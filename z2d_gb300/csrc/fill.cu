@@ -33,229 +33,13 @@
 #include <atomic>
 
 #include "fill.cuh"
+#include "edges.cuh"
+#include "spline.cuh"
+#include "stroke_gpu.cuh"
 
 namespace z2dg {
 
 // ------------------------------------------------------------ helpers
-__device__ __forceinline__ bool pt_eq(double ax, double ay, double bx, double by) { return ax == bx && ay == by; }
-
-// Order-preserving map of finite doubles to u64 (for atomic min/max).
-__device__ __forceinline__ unsigned long long dkey(double v) {
-    unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
-}
-__host__ __device__ __forceinline__ double dkey_inv(unsigned long long k) {
-    unsigned long long b = (k & 0x8000000000000000ull) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
-#ifdef __CUDA_ARCH__
-    return __longlong_as_double((long long)b);
-#else
-    double d;
-    memcpy(&d, &b, 8);
-    return d;
-#endif
-}
-
-struct Knots {
-    double ax, ay, bx, by, cx, cy, dx, dy;
-};
-
-// Spline.Knots.errorSq (Spline.zig:83-123)
-__device__ __forceinline__ double error_sq(const Knots &k) {
-    double bx = k.bx - k.ax, by = k.by - k.ay, cx = k.cx - k.ax, cy = k.cy - k.ay;
-    if (k.ax != k.dx || k.ay != k.dy) {
-        const double dx = k.dx - k.ax, dy = k.dy - k.ay;
-        const double dd = dx * dx + dy * dy;
-        const double bd = bx * dx + by * dy;
-        if (bd >= dd) {
-            bx -= dx;
-            by -= dy;
-        } else {
-            bx -= bd / dd * dx;
-            by -= bd / dd * dy;
-        }
-        const double cd = cx * dx + cy * dy;
-        if (cd >= dd) {
-            cx -= dx;
-            cy -= dy;
-        } else {
-            cx -= cd / dd * dx;
-            cy -= cd / dd * dy;
-        }
-    }
-    const double be = bx * bx + by * by, ce = cx * cx + cy * cy;
-    return be > ce ? be : ce;
-}
-// f64 -> f32 by truncating the mantissa (relative error < 2^-23) with
-// integer operations only, so that no FP64 instruction is spent on it.
-// False outside f32's normal range (zero excepted).
-__device__ __forceinline__ bool f32_trunc(double v, float &out) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    const uint32_t hi = (uint32_t)(b >> 32);
-    const uint32_t sign = hi & 0x80000000u;
-    if ((b << 1) == 0ull) {
-        out = __uint_as_float(sign);
-        return true;
-    }
-    const int32_t fe = (int32_t)((hi >> 20) & 0x7FFu) - 1023 + 127;
-    if (fe <= 0 || fe >= 255) return false;
-    out = __uint_as_float(sign | ((uint32_t)fe << 23) | ((uint32_t)(b >> 29) & 0x7FFFFFu));
-    return true;
-}
-
-// The decision errorSq(k) < tol2 of Spline.decomposeInto, taken in f32 when
-// that is safe.  GB300 runs f64 at a small fraction of its f32 rate, and the
-// error test is most of the subdivision's f64 work; only the control-point
-// differences (exact f64 subtractions, as in errorSq) stay in f64.  Every
-// f32 quantity carries an error bound built from first-order rounding
-// analysis with slack: inputs (truncation) < 2u, each operation u
-// (u = 2^-24), propagated through the projection and the squared norms.
-// Returns 1 / 0 when the f32 value is farther than its bound from tol2 and,
-// on the projection branches, from the branch condition; -1 otherwise (the
-// caller then evaluates errorSq in f64).
-__device__ __forceinline__ int error_sq_lt_f32(double bx64, double by64, double cx64, double cy64, bool proj,
-                                               double dx64, double dy64, float tol2f, float tol2e) {
-    const float U = 5.9604644775390625e-8f;  // 2^-24
-    float bx, by, cx, cy, dx = 0.0f, dy = 0.0f;
-    if (!f32_trunc(bx64, bx) || !f32_trunc(by64, by) || !f32_trunc(cx64, cx) || !f32_trunc(cy64, cy)) return -1;
-    float ebx = 2.0f * U * fabsf(bx), eby = 2.0f * U * fabsf(by), ecx = 2.0f * U * fabsf(cx), ecy = 2.0f * U * fabsf(cy);
-    if (proj) {
-        if (!f32_trunc(dx64, dx) || !f32_trunc(dy64, dy)) return -1;
-        const float edx = 2.0f * U * fabsf(dx), edy = 2.0f * U * fabsf(dy);
-        const float dd = dx * dx + dy * dy;
-        const float edd = 8.0f * U * dd;
-#pragma unroll
-        for (int i = 0; i < 2; i++) {
-            float &px = i ? cx : bx, &py = i ? cy : by;
-            float &epx = i ? ecx : ebx, &epy = i ? ecy : eby;
-            const float t1 = px * dx, t2 = py * dy;
-            const float pd = t1 + t2;
-            const float epd = 8.0f * U * (fabsf(t1) + fabsf(t2));
-            const float diff = pd - dd;
-            const float m = 1.125f * (epd + edd) + 2.0f * U * fabsf(diff) + 1e-30f;
-            if (diff > m) {  // pd >= dd: subtract the whole chord
-                const float nx = px - dx, ny = py - dy;
-                epx = epx + edx + 2.0f * U * fabsf(nx);
-                epy = epy + edy + 2.0f * U * fabsf(ny);
-                px = nx;
-                py = ny;
-            } else if (diff < -m && dd > 0.0f) {  // subtract the projection onto the chord
-                const float t = pd / dd;
-                const float et = (epd + fabsf(t) * edd) / dd * 1.125f + 2.0f * U * fabsf(t) + 1e-30f;
-                const float rx = t * dx, ry = t * dy;
-                const float nx = px - rx, ny = py - ry;
-                epx = epx + fabsf(dx) * et + fabsf(t) * edx + 2.0f * U * (fabsf(rx) + fabsf(nx));
-                epy = epy + fabsf(dy) * et + fabsf(t) * edy + 2.0f * U * (fabsf(ry) + fabsf(ny));
-                px = nx;
-                py = ny;
-            } else {
-                return -1;
-            }
-        }
-    }
-    const float be = bx * bx + by * by, ce = cx * cx + cy * cy;
-    const float ebe = 2.0f * fabsf(bx) * ebx + 2.0f * fabsf(by) * eby + ebx * ebx + eby * eby + 4.0f * U * be;
-    const float ece = 2.0f * fabsf(cx) * ecx + 2.0f * fabsf(cy) * ecy + ecx * ecx + ecy * ecy + 4.0f * U * ce;
-    const float e = be > ce ? be : ce;
-    const float E = 1.25f * (ebe > ece ? ebe : ece) + 4.0f * U * e + 1e-30f + tol2e;
-    if (!(E < 1e30f)) return -1;
-    if (e + E < tol2f) return 1;
-    if (e - E > tol2f) return 0;
-    return -1;
-}
-
-// The squared tolerance of a subdivision, in f64 and as a truncated f32
-// with its error bound.
-struct Tol {
-    double d;
-    float f, e;
-    bool f_ok;
-};
-__device__ __forceinline__ Tol make_tol(double tol) {
-    Tol t;
-    t.d = tol * tol;  // decomposeInto's tolerance argument (Spline.zig:52)
-    t.f = 0.0f;
-    t.f_ok = f32_trunc(t.d, t.f);
-    t.e = 4.0f * 5.9604644775390625e-8f * t.f;
-    return t;
-}
-
-// errorSq(k) < t.d, exactly as the f64 comparison decides it.
-__device__ __forceinline__ bool below_tol(const Knots &k, const Tol &t) {
-    if (t.f_ok) {
-        const bool proj = k.ax != k.dx || k.ay != k.dy;
-        const int r = error_sq_lt_f32(k.bx - k.ax, k.by - k.ay, k.cx - k.ax, k.cy - k.ay, proj, k.dx - k.ax,
-                                      k.dy - k.ay, t.f, t.e);
-        if (r >= 0) return r != 0;
-    }
-    return error_sq(k) < t.d;
-}
-
-// x / 2.  For normal x whose half is normal this only lowers the exponent,
-// which integer operations do exactly (an f64 multiply is an expensive
-// instruction on GB300); zeros, subnormals and non-finite values divide.
-__device__ __forceinline__ double half_of(double x) {
-    const long long b = __double_as_longlong(x);
-    const uint32_t e = (uint32_t)(b >> 52) & 0x7FFu;
-    if (e > 1u && e < 0x7FFu) return __longlong_as_double(b - (1ll << 52));
-    return x / 2;
-}
-__device__ __forceinline__ double lerp_half(double a, double b) { return a + half_of(b - a); }
-
-// Knots.deCasteljau (Spline.zig:128-152): k becomes the first half, the
-// second half is returned.
-__device__ __forceinline__ Knots de_casteljau(Knots &k) {
-    const double abx = lerp_half(k.ax, k.bx), aby = lerp_half(k.ay, k.by);
-    const double bcx = lerp_half(k.bx, k.cx), bcy = lerp_half(k.by, k.cy);
-    const double cdx = lerp_half(k.cx, k.dx), cdy = lerp_half(k.cy, k.dy);
-    const double abbcx = lerp_half(abx, bcx), abbcy = lerp_half(aby, bcy);
-    const double bccdx = lerp_half(bcx, cdx), bccdy = lerp_half(bcy, cdy);
-    const double fx = lerp_half(abbcx, bccdx), fy = lerp_half(abbcy, bccdy);
-    const Knots r{fx, fy, bccdx, bccdy, cdx, cdy, k.dx, k.dy};
-    k.bx = abx; k.by = aby;
-    k.cx = abbcx; k.cy = abbcy;
-    k.dx = fx; k.dy = fy;
-    return r;
-}
-
-// Depth-first subdivision (Spline.decomposeInto, Spline.zig:56-71) with an
-// explicit stack.  Calls emit(x, y) for every lineTo the reference issues,
-// including the final lineTo(d).  Returns false if the stack would overflow
-// (coordinates are bounded, so this does not happen for valid input).
-template <class F>
-__device__ __forceinline__ bool spline_walk(double ax, double ay, const double *p, double tol, F &&emit) {
-    const double bx = p[0], by = p[1], cx = p[2], cy = p[3], dx = p[4], dy = p[5];
-    if (pt_eq(ax, ay, bx, by) && pt_eq(cx, cy, dx, dy)) {  // Spline.zig:39-42
-        emit(dx, dy);
-        return true;
-    }
-    const Tol t = make_tol(tol);
-    Knots stack[kSplineStack];
-    int sp = 0;
-    stack[sp++] = Knots{ax, ay, bx, by, cx, cy, dx, dy};
-    bool ok = true;
-    int32_t budget = kSplineMaxSplits;  // bounds the walk even for pathological input
-    while (sp > 0 && ok) {
-        Knots k = stack[--sp];
-        while (true) {
-            if (--budget < 0) {
-                ok = false;
-                break;
-            }
-            if (below_tol(k, t)) {
-                if (!pt_eq(k.ax, k.ay, ax, ay)) emit(k.ax, k.ay);
-                break;
-            }
-            const Knots second = de_casteljau(k);
-            if (sp >= kSplineStack) {  // cannot recurse deeper: give up on this branch
-                ok = false;
-                break;
-            }
-            stack[sp++] = second;  // processed after the first half
-        }
-    }
-    emit(dx, dy);
-    return ok;
-}
 
 // ------------------------------------------------------------ kernels
 __global__ void k_node_count(const z2d_node *__restrict__ nodes, const int32_t *__restrict__ node_fill,
@@ -302,13 +86,21 @@ __global__ void k_node_count(const z2d_node *__restrict__ nodes, const int32_t *
 // The sequential walk of fill_plotter.plot over one fill's nodes.
 __global__ void k_fill_scan(const z2d_node *__restrict__ nodes, const FillCmd *__restrict__ fills,
                             NodeInfo *__restrict__ info, FillState *__restrict__ st, int32_t n_fills,
-                            int32_t *__restrict__ counters, int32_t *__restrict__ status) {
+                            int32_t *__restrict__ counters, int32_t *__restrict__ status,
+                            const int32_t *__restrict__ stroke_edges) {
     const int32_t f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= n_fills) return;
     const FillCmd F = fills[f];
     double fx = 0, fy = 0, lx = 0, ly = 0;
     int32_t count = 0;  // PointBuffer.len, saturating at 3
     int32_t off = 0;
+    if (F.stroke >= 0) {  // a device-stroked polygon: its edge count is known
+        off = stroke_edges[F.stroke];
+        if (off < 0) {
+            atomicExch(status, Z2D_ERR_INVALID_ARGUMENT);
+            off = 0;
+        }
+    }
     int32_t flags = 0;
     for (int32_t j = 0; j < F.n_nodes; j++) {
         const int32_t i = F.node_off + j;
@@ -379,52 +171,6 @@ __global__ void k_fill_scan(const z2d_node *__restrict__ nodes, const FillCmd *_
     st[f].ext[1] = 0ull;
     st[f].ext[2] = ~0ull;
     st[f].ext[3] = 0ull;
-}
-
-__device__ __forceinline__ void add_edge(const FillCmd &F, DEdge *out, double x0, double y0, double x1, double y1,
-                                         double &et, double &eb, double &el, double &er, bool &any) {
-    // Polygon.addEdge (Polygon.zig:61-109)
-    const double ax = x0 * F.edge_scale, ay = y0 * F.edge_scale, bx = x1 * F.edge_scale, by = y1 * F.edge_scale;
-    DEdge e;
-    if (ay < by) {
-        e.top = ay;
-        e.x_start = ax;
-        e.x_inc = (bx - ax) / (by - ay);
-        e.dir = -1;
-        e.rb = (int32_t)round(by);
-    } else if (ay > by) {
-        e.top = by;
-        e.x_start = bx;
-        e.x_inc = (ax - bx) / (ay - by);
-        e.dir = 1;
-        e.rb = (int32_t)round(ay);
-    } else {
-        e.top = 0;
-        e.x_start = 0;
-        e.x_inc = 0;
-        e.fxs = e.fxi = e.ftp = 0.0f;
-        e.dir = 0;
-        e.rt = 1;
-        e.rb = 0;  // horizontal: never active
-        *out = e;
-        return;
-    }
-    e.rt = (int32_t)round(e.top);
-    e.fxs = (float)e.x_start;
-    e.fxi = (float)e.x_inc;
-    e.ftp = (float)e.top;
-    const double bot = ay < by ? by : ay;
-    const double l = ax < bx ? ax : bx, r = ax < bx ? bx : ax;
-    if (!any) {
-        et = e.top; eb = bot; el = l; er = r;
-        any = true;
-    } else {
-        if (e.top < et) et = e.top;
-        if (bot > eb) eb = bot;
-        if (l < el) el = l;
-        if (r > er) er = r;
-    }
-    *out = e;
 }
 
 __global__ void k_node_emit(const z2d_node *__restrict__ nodes, const int32_t *__restrict__ node_fill,
@@ -690,9 +436,13 @@ __global__ void __launch_bounds__(32 * kFlattenWarps) k_node_count_w(const z2d_n
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     WarpFrontier &fr = frs[w];
     for (int32_t i = blockIdx.x * kFlattenWarps + w; i < n_nodes; i += gridDim.x * kFlattenWarps) {
-        const z2d_node nd = nodes[i];
         NodeInfo inf{};
         const int32_t f = node_fill[i];
+        if (f < 0) {  // no fill owns the node
+            if (lane == 0) info[i] = inf;
+            continue;
+        }
+        const z2d_node nd = nodes[i];
         const FillCmd &F = fills[f];
         const bool first_of_fill = (i == F.node_off);
         if (nd.tag == Z2D_LINE_TO || nd.tag == Z2D_CURVE_TO) {
@@ -1587,7 +1337,8 @@ static inline unsigned grid_for(long long n, int threads) { return (unsigned)((n
 
 int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n_first, std::vector<FillCmd> &fills,
              const std::vector<int32_t> &node_fill, const std::vector<DevGradient> &grads,
-             const std::vector<int32_t> &grad_of_fill, const z2d_node *nodes2, int32_t n_second) {
+             const std::vector<int32_t> &grad_of_fill, const z2d_node *nodes2, int32_t n_second,
+             const StrokeSet *strokes) {
     if (n_first < 0 || n_second < 0 || (int64_t)n_first + n_second > 0x7FFFFFFF) return Z2D_ERR_INVALID_ARGUMENT;
     const int32_t n_nodes = n_first + n_second;
     const int32_t n_fills = (int32_t)fills.size();
@@ -1607,7 +1358,13 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     const size_t o_fills = al(o_grads + sizeof(DevGradient) * grads.size());
     const size_t o_jobs = al(o_fills + sizeof(FillCmd) * (size_t)n_fills);
     const size_t o_cnt = al(o_jobs + sizeof(DevJob) * (size_t)n_jobs);
-    const size_t total = al(o_cnt + sizeof(int32_t) * CNT_COUNT);
+    const bool has_strokes = strokes && !strokes->empty();
+    const size_t n_sk = has_strokes ? strokes->strokes.size() : 0, n_sb = has_strokes ? strokes->subs.size() : 0;
+    const size_t n_tr = has_strokes ? strokes->trig.size() : 0;
+    const size_t o_sk = al(o_cnt + sizeof(int32_t) * CNT_COUNT);
+    const size_t o_sb = al(o_sk + sizeof(StrokeDev) * n_sk);
+    const size_t o_tr = al(o_sb + sizeof(SubpathDev) * n_sb);
+    const size_t total = al(o_tr + sizeof(double) * n_tr);
     if (c.params.ensure(total) || c.staging.ensure(total)) return Z2D_ERR_OUT_OF_MEMORY;
     uint8_t *h = c.staging.as<uint8_t>();
     uint8_t *dv = c.params.as<uint8_t>();
@@ -1624,6 +1381,11 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     memcpy(h + o_jobs, jobs.data(), sizeof(DevJob) * (size_t)n_jobs);
     int32_t *cnt_h = reinterpret_cast<int32_t *>(h + o_cnt);
     for (int i = 0; i < CNT_COUNT; i++) cnt_h[i] = 0;
+    if (has_strokes) {
+        memcpy(h + o_sk, strokes->strokes.data(), sizeof(StrokeDev) * n_sk);
+        memcpy(h + o_sb, strokes->subs.data(), sizeof(SubpathDev) * n_sb);
+        if (n_tr > 0) memcpy(h + o_tr, strokes->trig.data(), sizeof(double) * n_tr);
+    }
     Z2D_CUDA(cudaMemcpyAsync(dv, h, total, cudaMemcpyHostToDevice, c.stream));
     const z2d_node *d_nodes = reinterpret_cast<const z2d_node *>(dv + o_nodes);
     const int32_t *d_nfill = reinterpret_cast<const int32_t *>(dv + o_nfill);
@@ -1646,18 +1408,42 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     cudaEvent_t tf = c.timer_begin(c.t_flatten);
     k_node_count_w<<<flat_blocks, 32 * kFlattenWarps, 0, c.stream>>>(d_nodes, d_nfill, d_fills, d_info, n_nodes,
                                                                     d_items, d_cnt + CNT_STATUS);
-    k_fill_scan<<<grid_for(n_fills, 64), 64, 0, c.stream>>>(d_nodes, d_fills, d_info, d_st, n_fills, d_cnt, d_cnt + CNT_STATUS);
+    StrokeRun srun;
+    if (has_strokes) {
+        srun.nodes = d_nodes;
+        srun.strokes = reinterpret_cast<const StrokeDev *>(dv + o_sk);
+        srun.subs = reinterpret_cast<const SubpathDev *>(dv + o_sb);
+        srun.trig = reinterpret_cast<const double *>(dv + o_tr);
+        srun.n_strokes = (int32_t)n_sk;
+        srun.n_subs = (int32_t)n_sb;
+        srun.n_local = strokes->n_local;
+        srun.n_pen = strokes->n_pen;
+        const int rc = stroke_count(c, srun, d_cnt + CNT_STATUS);
+        if (rc) return rc;
+    }
+    k_fill_scan<<<grid_for(n_fills, 64), 64, 0, c.stream>>>(d_nodes, d_fills, d_info, d_st, n_fills, d_cnt,
+                                                             d_cnt + CNT_STATUS, srun.stroke_edges);
     c.timer_end(c.t_flatten, tf);
     c.launches += 2;
-    const size_t rb_bytes = sizeof(int32_t) * CNT_COUNT + sizeof(DevJob) * (size_t)n_jobs;
+    const size_t rb_jobs_off = al(sizeof(int32_t) * CNT_COUNT + 2 * sizeof(long long));
+    const size_t rb_bytes = rb_jobs_off + sizeof(DevJob) * (size_t)n_jobs;
     if (c.readback.ensure(rb_bytes)) return Z2D_ERR_OUT_OF_MEMORY;
     int32_t *rb = c.readback.as<int32_t>();
-    DevJob *rb_jobs = reinterpret_cast<DevJob *>(c.readback.as<uint8_t>() + sizeof(int32_t) * CNT_COUNT);
+    long long *rb_tot = reinterpret_cast<long long *>(rb + CNT_COUNT);  // stroke contour totals (8-aligned: CNT_COUNT even)
+    DevJob *rb_jobs = reinterpret_cast<DevJob *>(c.readback.as<uint8_t>() + rb_jobs_off);
     Z2D_CUDA(cudaMemcpyAsync(rb, d_cnt, sizeof(int32_t) * CNT_COUNT, cudaMemcpyDeviceToHost, c.stream));
+    if (has_strokes)
+        Z2D_CUDA(cudaMemcpyAsync(rb_tot, stroke_totals_dev(srun), 2 * sizeof(long long), cudaMemcpyDeviceToHost,
+                                 c.stream));
     Z2D_CUDA(cudaStreamSynchronize(c.stream));
     if (rb[CNT_STATUS] != 0) {
-        set_error("curve subdivision exceeded its depth bound");
+        set_error(rb[CNT_STATUS] == Z2D_ERR_INVALID_STATE ? "curve subdivision exceeded its depth bound"
+                                                          : "batch too large: more than 2^31 edges in one polygon");
         return rb[CNT_STATUS];
+    }
+    if (has_strokes) {
+        srun.n_a = rb_tot[0];
+        srun.n_b = rb_tot[1];
     }
     const int32_t n_edges = rb[CNT_EDGES];
     if (n_edges < 0) return Z2D_ERR_OUT_OF_MEMORY;
@@ -1669,6 +1455,10 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     tf = c.timer_begin(c.t_flatten);
     k_node_emit_w<<<flat_blocks, 32 * kFlattenWarps, 0, c.stream>>>(d_nodes, d_nfill, d_fills, d_info, d_st, d_edges,
                                                                    d_items, n_nodes);
+    if (has_strokes) {
+        const int rc = stroke_emit(c, srun, d_fills, d_st, d_edges);
+        if (rc) return rc;
+    }
     k_edge_fill<<<n_fills, 128, 0, c.stream>>>(d_st, n_fills, d_edge_fill);
     k_fill_setup<<<grid_for(n_fills, 64), 64, 0, c.stream>>>(d_fills, d_st, n_fills, d_jobs, d_cnt);
     c.timer_end(c.t_flatten, tf);

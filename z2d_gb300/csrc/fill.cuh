@@ -23,6 +23,7 @@ struct FillCmd {
     int32_t reduces;    // pixel pattern whose operator reduces to the source (shared.zig:111-117)
     int32_t fast_kind;  // FAST_* specialisation the rasteriser may use
     int32_t job;        // index of the surface (job) the fill draws on
+    int32_t stroke;     // device-stroked command whose polygon this fill draws, or -1
     double tol;         // max(tolerance, 0.001) (painter.zig:103)
     double scale;       // 4 for multisample / supersample, 1 for none (painter.zig:93-97)
     double edge_scale;  // multiplier of node coordinates in Polygon.addEdge: scale, or 1 for
@@ -138,8 +139,13 @@ struct DevJob {
 // gradient of fill i in `grads`.
 // The node array is nodes[0, n_first) followed by nodes2[0, n_second)
 // (node_fill covers both).
+// Nodes that no fill owns (node_fill -1) are skipped; device-stroked
+// commands (`strokes`, fills with stroke >= 0) read their nodes from the
+// same array.
+struct StrokeSet;
 int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n_first, std::vector<FillCmd> &fills,
              const std::vector<int32_t> &node_fill, const std::vector<DevGradient> &grads,
-             const std::vector<int32_t> &grad_of_fill, const z2d_node *nodes2 = nullptr, int32_t n_second = 0);
+             const std::vector<int32_t> &grad_of_fill, const z2d_node *nodes2 = nullptr, int32_t n_second = 0,
+             const StrokeSet *strokes = nullptr);
 
 }  // namespace z2dg

@@ -18,6 +18,44 @@
 
 namespace z2dg {
 namespace stroke {
+
+int32_t pen_vertex_count(double thickness, double tolerance, const double m[6]) {  // Pen.init (Pen.zig:25-60)
+    const sg::Tf ctm{m[0], m[1], m[2], m[3], m[4], m[5]};
+    const double radius = thickness / 2;
+    const double a = ctm.ax, b = ctm.by, c = ctm.cx, d = ctm.dy;
+    // arc.transformed_circle_major_axis (arc.zig:92-262)
+    double major;
+    const double eps = 0.00390625;
+    const double det = a * d - b * c;
+    if (std::fabs(det * det - 1.0) < eps &&
+        ((std::fabs(b) < eps && std::fabs(c) < eps) || (std::fabs(a) < eps && std::fabs(d) < eps))) {
+        major = radius;
+    } else {
+        const double i = a * a + b * b;
+        const double j = c * c + d * d;
+        const double f = 0.5 * (i + j);
+        const double g = 0.5 * (i - j);
+        const double h = a * c + b * d;
+        major = radius * std::sqrt(f + std::hypot(g, h));
+    }
+    if (tolerance >= major * 4) return 1;
+    if (tolerance >= major) return 4;
+    const double delta = std::acos(1 - tolerance / major);
+    if (delta == 0) return 4;
+    const double nf = std::ceil(2 * M_PI / delta);
+    const int32_t k = (int32_t)nf;
+    return k < 4 ? 4 : ((k % 2 != 0) ? k + 1 : k);
+}
+
+void pen_trig(int32_t n, bool reflect, double *out) {  // Pen.init (Pen.zig:62-75)
+    for (int32_t i = 0; i < n; i++) {
+        double t = 2 * M_PI * (double)i / (double)n;
+        if (reflect) t = -t;
+        out[2 * (size_t)i] = std::cos(t);
+        out[2 * (size_t)i + 1] = std::sin(t);
+    }
+}
+
 namespace {
 
 using sg::compare;
@@ -34,22 +72,6 @@ using sg::Slope;
 using sg::Tf;
 using sg::user_to_device_distance;
 
-// arc.transformed_circle_major_axis (arc.zig:92-262)
-double transformed_circle_major_axis(const Tf &m, double radius) {
-    const double a = m.ax, b = m.by, c = m.cx, d = m.dy;
-    const double eps = 0.00390625;
-    const double det = m.ax * m.dy - m.by * m.cx;
-    if (std::fabs(det * det - 1.0) < eps) {
-        if (std::fabs(m.by) < eps && std::fabs(m.cx) < eps) return radius;
-        if (std::fabs(m.ax) < eps && std::fabs(m.dy) < eps) return radius;
-    }
-    const double i = a * a + b * b;
-    const double j = c * c + d * d;
-    const double f = 0.5 * (i + j);
-    const double g = 0.5 * (i - j);
-    const double h = a * c + b * d;
-    return radius * std::sqrt(f + std::hypot(g, h));
-}
 
 
 // Pen.zig
@@ -62,28 +84,13 @@ Pen make_pen(double thickness, double tolerance, const Tf &ctm) {
     Pen pen;
     pen.ok = true;
     const double radius = thickness / 2;
-    int32_t n;
-    const double major = transformed_circle_major_axis(ctm, radius);
-    if (tolerance >= major * 4) {
-        n = 1;
-    } else if (tolerance >= major) {
-        n = 4;
-    } else {
-        const double delta = std::acos(1 - tolerance / major);
-        if (delta == 0) {
-            n = 4;
-        } else {
-            const double nf = std::ceil(2 * M_PI / delta);
-            const int32_t k = (int32_t)nf;
-            n = k < 4 ? 4 : ((k % 2 != 0) ? k + 1 : k);
-        }
-    }
-    const bool reflect = determinant(ctm) < 0;
+    const double m[6] = {ctm.ax, ctm.by, ctm.cx, ctm.dy, ctm.tx, ctm.ty};
+    const int32_t n = pen_vertex_count(thickness, tolerance, m);
+    std::vector<double> trig((size_t)std::max(0, n) * 2);
+    pen_trig(n, determinant(ctm) < 0, trig.data());
     pen.v.resize((size_t)std::max(0, n));
     for (int32_t i = 0; i < n; i++) {
-        double t = 2 * M_PI * (double)i / (double)n;
-        if (reflect) t = -t;
-        double dx = radius * std::cos(t), dy = radius * std::sin(t);
+        double dx = radius * trig[2 * (size_t)i], dy = radius * trig[2 * (size_t)i + 1];
         user_to_device_distance(ctm, dx, dy);
         pen.v[(size_t)i].point = Pt{dx, dy};
     }

@@ -1,6 +1,7 @@
 // stroke.h -- painter.stroke's polygon builder (stroke.cpp).
 #pragma once
 #include <stddef.h>
+#include <stdint.h>
 
 #include <vector>
 
@@ -29,6 +30,13 @@ struct Options {
 
 // Dasher.validate: the dash array draws dashes (stroke_plotter.zig:40-44).
 bool dashed(const Options &opts);
+
+// Pen.init's vertex count for a pen of width `thickness` through the CTM m
+// (ax, by, cx, dy, tx, ty) at `tolerance` (Pen.zig:25-60).
+int32_t pen_vertex_count(double thickness, double tolerance, const double m[6]);
+// The n (cos t, sin t) pairs of the pen's vertex angles t = 2 pi i / n,
+// negated when the CTM reflects (Pen.zig:62-75).
+void pen_trig(int32_t n, bool reflect, double *out);
 
 // Transformation.inverse succeeds (painter.zig:231).
 bool transformation_invertible(const double m[6]);

@@ -64,6 +64,9 @@ struct Ctx {
     DevBuf surface2;    // staging for a second host surface (compositor params)
     DevBuf surface3;
     DevBuf scan_tmp;    // temporary storage of device-wide scans
+    DevBuf stroke_a;    // device stroker: per node / subpath / stroke state
+    DevBuf stroke_b;    // device stroker: per point state
+    DevBuf stroke_c;    // device stroker: contour points
     HostBuf staging;    // pinned upload staging
     HostBuf readback;   // pinned readback
     cudaEvent_t done = nullptr;
@@ -73,7 +76,7 @@ struct Ctx {
         std::vector<cudaEvent_t> pending;  // start/stop pairs not yet read
         double ms = 0;
         uint64_t n = 0;
-    } t_raster, t_composite, t_flatten, t_bins;
+    } t_raster, t_composite, t_flatten, t_bins, t_stroke;
     cudaEvent_t timer_begin(Timer &t);
     void timer_end(Timer &t, cudaEvent_t start);
     void timer_collect(Timer &t);
