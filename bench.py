@@ -447,7 +447,7 @@ def jobs_arm(ctx, stream, dev, steps=3):
         pb.draw_jobs(ctx)
         stream.synchronize()
         walls.append(time.perf_counter() - t0)
-    stage_ms = {k: ctx.kernel_ms(k)[0] / steps for k in ("flatten", "bins", "raster")}
+    stage_ms = {k: ctx.kernel_ms(k)[0] / steps for k in ("flatten", "stroke", "bins", "raster")}
     ctx.set_timing(False)
     # one call per surface, first jobs
     restore()

@@ -389,6 +389,7 @@ static int prepare_fills(const z2d_surface &s, int32_t job, const z2d_node *node
         F.n_nodes = (int32_t)cm.n_nodes;
         F.job = job;
         F.stroke = -1;
+        F.poly = -1;
         F.aa = (aa == Z2D_AA_NONE || aa == Z2D_AA_SUPERSAMPLE_4X) ? aa : Z2D_AA_MULTISAMPLE_4X;
         F.rule = cm.opts.fill_rule;
         F.op = cm.opts.op;
@@ -580,7 +581,7 @@ static int stroke_checks(const z2d_node *nodes, size_t n_nodes, const z2d_stroke
 }
 
 static int stroke_polygon(const z2d_node *nodes, size_t n_nodes, const z2d_stroke_opts &o, int32_t surface_format,
-                          int &aa, std::vector<std::vector<double>> &contours, double &scale) {
+                          int &aa, stroke::Polygon &contours, double &scale) {
     stroke::Options so;
     contours.clear();
     int rc = stroke_options(o, surface_format, aa, so);
@@ -592,33 +593,6 @@ static int stroke_polygon(const z2d_node *nodes, size_t n_nodes, const z2d_strok
     rc = stroke::plot(nodes, n_nodes, so, contours);
     if (rc) set_error("InvalidState: stroke path node sequence");
     return rc;
-}
-
-// The contours as path nodes for the fill pipeline: each one is
-// move_to + line_to for every further point + line_to back to the start +
-// close_path, so the edges are exactly Polygon.addEdgesFromContour's
-// (consecutive points, then last -> first) whatever the number of points.
-static void contours_to_nodes(const std::vector<std::vector<double>> &contours, std::vector<z2d_node> &out) {
-    out.clear();
-    for (const auto &c : contours) {
-        const size_t n = c.size() / 2;
-        if (n == 0) continue;
-        z2d_node nd;
-        memset(&nd, 0, sizeof(nd));
-        nd.tag = Z2D_MOVE_TO;
-        nd.p[0] = c[0];
-        nd.p[1] = c[1];
-        out.push_back(nd);
-        for (size_t k = 1; k <= n; k++) {
-            nd.tag = Z2D_LINE_TO;
-            nd.p[0] = c[2 * (k % n)];
-            nd.p[1] = c[2 * (k % n) + 1];
-            out.push_back(nd);
-        }
-        nd.tag = Z2D_CLOSE_PATH;
-        nd.p[0] = nd.p[1] = 0;
-        out.push_back(nd);
-    }
 }
 
 // The device stroker's input for one solid stroke: the subpaths the
@@ -709,10 +683,9 @@ static int prepare_polygon_fill(const z2d_surface &s, int32_t job, const z2d_pat
 
 // Fills and strokes over many device surfaces.  Solid strokes are
 // tessellated on the device from the caller's nodes; dashed strokes are
-// built on host threads (each command independently) and drawn as their
-// contours (already-scaled nodes appended after the caller's, edge scale
-// 1); fills use the caller's nodes.  The caller's node array is uploaded
-// as it is.
+// built on host threads (each command independently) and uploaded as
+// their polygons' points (already scaled); fills use the caller's nodes.
+// The caller's node array is uploaded as it is.
 static int draw_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_node *nodes, size_t n_nodes,
                      const z2d_draw_cmd *cmds, size_t n_cmds) {
     if ((n_jobs > 0 && !jobs_in) || (n_cmds > 0 && !cmds) || (n_nodes > 0 && !nodes)) return Z2D_ERR_INVALID_ARGUMENT;
@@ -741,7 +714,7 @@ static int draw_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_no
     // per stroke: options, then the device stroker's input (solid) or the
     // host-built polygon (dashed), in parallel
     const size_t ns = strokes.size();
-    std::vector<std::vector<std::vector<double>>> polys(ns);
+    std::vector<stroke::Polygon> polys(ns);
     std::vector<StrokePrep> preps(ns);
     std::vector<stroke::Options> sopts(ns);
     std::vector<uint8_t> on_device(ns, 0);
@@ -784,27 +757,10 @@ static int draw_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_no
                 return rcs[k];
             }
     }
-    // the dashed strokes' contour nodes, as a second node segment
-    std::vector<z2d_node> extra;
-    std::vector<uint64_t> stroke_off(ns), stroke_cnt(ns);
-    {
-        std::vector<z2d_node> cn;
-        for (size_t k = 0; k < ns; k++) {
-            if (on_device[k]) continue;
-            contours_to_nodes(polys[k], cn);
-            stroke_off[k] = extra.size();
-            stroke_cnt[k] = cn.size();
-            extra.insert(extra.end(), cn.begin(), cn.end());
-        }
-    }
-    if (n_nodes + extra.size() > 0x7FFFFFFF) {
-        set_error("batch too large");
-        return Z2D_ERR_INVALID_ARGUMENT;
-    }
     std::vector<int64_t> stroke_of(n_cmds, -1);
     for (size_t k = 0; k < ns; k++) stroke_of[strokes[k]] = (int64_t)k;
     std::vector<FillCmd> fills;
-    std::vector<int32_t> node_fill(n_nodes, -1), fill_s(extra.size(), -1), grad_of_fill;
+    std::vector<int32_t> node_fill(n_nodes, -1), grad_of_fill;
     std::vector<DevGradient> grads;
     std::vector<DevJob> jobs(n_jobs);
     if (n_jobs > 0) memset(jobs.data(), 0, sizeof(DevJob) * n_jobs);
@@ -841,24 +797,13 @@ static int draw_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_no
                 set_error("PixelSourceNotPreMultiplied");
                 return Z2D_ERR_PIXEL_NOT_PREMULTIPLIED;
             }
-            if (!on_device[k]) {
-                z2d_fill_cmd fc;
-                fc.pattern = cm.pattern;
-                fc.node_offset = stroke_off[k];
-                fc.n_nodes = stroke_cnt[k];
-                fc.opts.anti_aliasing = aas[k];
-                fc.opts.fill_rule = Z2D_FILL_NON_ZERO;
-                fc.opts.op = cm.stroke.op;
-                fc.opts.precision = cm.stroke.precision;
-                fc.opts.tolerance = cm.stroke.tolerance;
-                const size_t before = fills.size();
-                rc = prepare_fills(jb.surface, (int32_t)j, extra.data(), extra.size(), &fc, 1, fills, fill_s, grads,
-                                   grad_of_fill);
+            if (!on_device[k]) {  // a host-built polygon
+                if (polys[k].points() == 0) continue;  // nothing is drawn
+                rc = prepare_polygon_fill(jb.surface, (int32_t)j, cm.pattern, aas[k], cm.stroke.op,
+                                          cm.stroke.precision, cm.stroke.tolerance, fills, grads, grad_of_fill);
                 if (rc) return rc;
-                for (size_t f = before; f < fills.size(); f++) {
-                    fills[f].edge_scale = 1.0;  // contour points are already scaled
-                    fills[f].node_off += (int32_t)n_nodes;
-                }
+                fills.back().poly = (int32_t)sset.polys.size();
+                sset.polys.push_back(&polys[k]);
                 continue;
             }
             // a device-stroked command
@@ -915,9 +860,7 @@ static int draw_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_no
         jobs[j].fill1 = (int32_t)fills.size();
     }
     if (fills.empty()) return Z2D_OK;
-    node_fill.insert(node_fill.end(), fill_s.begin(), fill_s.end());
-    return run_jobs(c, jobs, nodes, (int32_t)n_nodes, fills, node_fill, grads, grad_of_fill, extra.data(),
-                    (int32_t)extra.size(), &sset);
+    return run_jobs(c, jobs, nodes, (int32_t)n_nodes, fills, node_fill, grads, grad_of_fill, &sset);
 }
 
 static int do_stroke(Ctx &c, z2d_surface *surface, const z2d_pattern *pattern, const z2d_node *nodes, size_t n_nodes,
@@ -1163,20 +1106,14 @@ Z2D_API int z2dgpu_stroke_contours(const z2d_node *nodes, size_t n_nodes, const 
                                    int32_t surface_format, double *points, size_t cap_points, uint64_t *n_points,
                                    uint64_t *contour_ends, size_t cap_contours, uint64_t *n_contours, double *scale) {
     if (!opts) return Z2D_ERR_INVALID_ARGUMENT;
-    std::vector<std::vector<double>> contours;
+    stroke::Polygon poly;
     int aa = 0;
     double sc = 1;
-    const int rc = stroke_polygon(nodes, n_nodes, *opts, surface_format, aa, contours, sc);
+    const int rc = stroke_polygon(nodes, n_nodes, *opts, surface_format, aa, poly, sc);
     if (rc) return rc;
-    uint64_t np = 0, nc = 0;
-    for (const auto &cn : contours) {
-        for (size_t k = 0; k < cn.size(); k++) {
-            if (points && np * 2 + k < cap_points * 2) points[np * 2 + k] = cn[k];
-        }
-        np += cn.size() / 2;
-        if (contour_ends && nc < cap_contours) contour_ends[nc] = np;
-        nc++;
-    }
+    const uint64_t np = poly.points(), nc = poly.ends.size();
+    if (points) memcpy(points, poly.xy.data(), sizeof(double) * 2 * std::min<uint64_t>(np, cap_points));
+    if (contour_ends) memcpy(contour_ends, poly.ends.data(), sizeof(uint64_t) * std::min<uint64_t>(nc, cap_contours));
     if (n_points) *n_points = np;
     if (n_contours) *n_contours = nc;
     if (scale) *scale = sc;

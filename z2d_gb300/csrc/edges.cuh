@@ -71,4 +71,41 @@ __device__ __forceinline__ void add_edge(const FillCmd &F, DEdge *out, double x0
     *out = e;
 }
 
+// Merges the lanes' edge extents into their fills' FillState: one set of
+// atomics per warp when every lane that has edges draws the same fill, one
+// per lane otherwise.  All 32 lanes must call it.
+__device__ __forceinline__ void merge_extents(FillState *st, int32_t f, bool any, double et, double eb, double el,
+                                              double er) {
+    const unsigned all = 0xffffffffu;
+    const unsigned am = __ballot_sync(all, any);
+    if (!am) return;
+    const int lead = __ffs(am) - 1;
+    const int32_t f0 = __shfl_sync(all, f, lead);
+    if (__all_sync(all, !any || f == f0)) {
+        double mt = any ? et : 1e300, mb = any ? eb : -1e300, ml = any ? el : 1e300, mr = any ? er : -1e300;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            mt = fmin(mt, __shfl_xor_sync(all, mt, o));
+            mb = fmax(mb, __shfl_xor_sync(all, mb, o));
+            ml = fmin(ml, __shfl_xor_sync(all, ml, o));
+            mr = fmax(mr, __shfl_xor_sync(all, mr, o));
+        }
+        if ((int)(threadIdx.x & 31) == lead) {
+            FillState &S = st[f0];
+            atomicMin(&S.ext[0], dkey(mt));
+            atomicMax(&S.ext[1], dkey(mb));
+            atomicMin(&S.ext[2], dkey(ml));
+            atomicMax(&S.ext[3], dkey(mr));
+            atomicOr(&S.has_edges, 1);
+        }
+    } else if (any) {
+        FillState &S = st[f];
+        atomicMin(&S.ext[0], dkey(et));
+        atomicMax(&S.ext[1], dkey(eb));
+        atomicMin(&S.ext[2], dkey(el));
+        atomicMax(&S.ext[3], dkey(er));
+        atomicOr(&S.has_edges, 1);
+    }
+}
+
 }  // namespace z2dg

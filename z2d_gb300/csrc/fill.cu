@@ -2,13 +2,17 @@
 // fills on one surface.
 //
 // Pipeline (one launch each, all on the context stream):
-//   k_node_count  thread per path node: how many edges each line/curve
-//                 emits (Bezier subdivision of Spline.zig:37-165)
-//   k_fill_scan   thread per fill: the sequential part of fill_plotter.plot
+//   k_node_count_w  32 nodes per warp: how many edges each line/curve
+//                 emits (Bezier subdivision of Spline.zig:37-165; curves
+//                 subdivided by the whole warp)
+//   stroke_count  device-stroked commands (stroke_gpu.cu): their polygons'
+//                 edge counts
+//   k_fill_scan   warp per fill: the sequential part of fill_plotter.plot
 //                 (fill_plotter.zig:21-97) -- start points, close_path edges,
 //                 per-node edge offsets, open-chain detection
-//   k_node_emit   thread per node: emits Polygon edges (Polygon.zig:61-109)
-//                 and per-fill extents
+//   k_node_emit_w 32 nodes per warp: emits Polygon edges (Polygon.zig:61-109)
+//                 and per-fill extents; stroke_emit does the same for the
+//                 stroke polygons
 //   k_fill_setup  thread per fill: Polygon.inBox and the draw box of
 //                 multisample.run / direct.run
 //   k_bin_count / k_bin_fill   (edge, 4-row band) lists per fill
@@ -30,7 +34,10 @@
 #include <cub/cub.cuh>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
+#include <thread>
+#include <vector>
 
 #include "fill.cuh"
 #include "edges.cuh"
@@ -39,177 +46,153 @@
 
 namespace z2dg {
 
-// ------------------------------------------------------------ helpers
-
 // ------------------------------------------------------------ kernels
-__global__ void k_node_count(const z2d_node *__restrict__ nodes, const int32_t *__restrict__ node_fill,
-                             const FillCmd *__restrict__ fills, NodeInfo *__restrict__ info, int32_t n_nodes,
-                             int32_t *__restrict__ status) {
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_nodes) return;
-    const z2d_node nd = nodes[i];
-    NodeInfo inf{};
-    inf.n_emit = 0;
-    inf.n_added = 0;
-    const int32_t f = node_fill[i];
-    const FillCmd &F = fills[f];
-    const bool first_of_fill = (i == F.node_off);
-    if (nd.tag == Z2D_LINE_TO || nd.tag == Z2D_CURVE_TO) {
-        const z2d_node pv = first_of_fill ? nd : nodes[i - 1];
-        const bool static_start = !first_of_fill && (pv.tag == Z2D_MOVE_TO || pv.tag == Z2D_LINE_TO || pv.tag == Z2D_CURVE_TO);
-        if (!static_start) {
-            inf.n_emit = -1;  // resolved by k_fill_scan
-        } else {
-            const double sx = pv.tag == Z2D_CURVE_TO ? pv.p[4] : pv.p[0];
-            const double sy = pv.tag == Z2D_CURVE_TO ? pv.p[5] : pv.p[1];
-            if (nd.tag == Z2D_LINE_TO) {
-                inf.n_emit = 1;
-                inf.n_added = pt_eq(sx, sy, nd.p[0], nd.p[1]) ? 0 : 1;
-            } else {
-                int32_t ne = 0, na = 0;
-                double lx = sx, ly = sy;
-                auto cnt = [&](double x, double y) {
-                    ne++;
-                    if (!pt_eq(x, y, lx, ly)) na++;
-                    lx = x;
-                    ly = y;
-                };
-                if (!spline_walk(sx, sy, nd.p, F.tol, cnt)) atomicExch(status, Z2D_ERR_INVALID_STATE);
-                inf.n_emit = ne;
-                inf.n_added = na;
-            }
-        }
-    }
-    info[i] = inf;
-}
+// The sequential walk of fill_plotter.plot over one fill's nodes, one warp
+// per fill: the warp stages 32 nodes at a time in shared memory, lane 0
+// walks them, and the warp writes their NodeInfo back.
+constexpr int kScanWarps = 4;
+struct ScanStage {
+    double x[32], y[32];    // node end point (curve: p[4], p[5])
+    double sx[32], sy[32];  // NodeInfo fields the walk sets
+    double ex[32], ey[32];
+    int32_t tag[32], n_emit[32], n_added[32], off[32];
+};
 
-// The sequential walk of fill_plotter.plot over one fill's nodes.
-__global__ void k_fill_scan(const z2d_node *__restrict__ nodes, const FillCmd *__restrict__ fills,
-                            NodeInfo *__restrict__ info, FillState *__restrict__ st, int32_t n_fills,
-                            int32_t *__restrict__ counters, int32_t *__restrict__ status,
-                            const int32_t *__restrict__ stroke_edges) {
-    const int32_t f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= n_fills) return;
-    const FillCmd F = fills[f];
+__global__ void __launch_bounds__(32 * kScanWarps) k_fill_scan(const z2d_node *__restrict__ nodes,
+                                                               const FillCmd *__restrict__ fills,
+                                                               NodeInfo *__restrict__ info, FillState *__restrict__ st,
+                                                               int32_t n_fills, int32_t *__restrict__ counters,
+                                                               int32_t *__restrict__ status,
+                                                               const int32_t *__restrict__ stroke_edges,
+                                                               const int32_t *__restrict__ poly_edges) {
+    __shared__ ScanStage stages[kScanWarps];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int32_t f = blockIdx.x * kScanWarps + w;
+    if (f >= n_fills) return;  // uniform across the warp
+    ScanStage &S = stages[w];
+    const int32_t node_off = fills[f].node_off, n_nodes = fills[f].n_nodes;
+    const double tol = fills[f].tol;
     double fx = 0, fy = 0, lx = 0, ly = 0;
     int32_t count = 0;  // PointBuffer.len, saturating at 3
     int32_t off = 0;
-    if (F.stroke >= 0) {  // a device-stroked polygon: its edge count is known
-        off = stroke_edges[F.stroke];
+    if (fills[f].stroke >= 0) {  // a device-stroked polygon: its edge count is known
+        off = stroke_edges[fills[f].stroke];
         if (off < 0) {
-            atomicExch(status, Z2D_ERR_INVALID_ARGUMENT);
+            if (lane == 0) atomicExch(status, Z2D_ERR_INVALID_ARGUMENT);
             off = 0;
         }
+    } else if (fills[f].poly >= 0) {  // a host-built polygon: one edge per point
+        off = poly_edges[fills[f].poly];
     }
     int32_t flags = 0;
-    for (int32_t j = 0; j < F.n_nodes; j++) {
-        const int32_t i = F.node_off + j;
-        const z2d_node nd = nodes[i];
-        NodeInfo inf = info[i];
-        inf.edge_off = off;
-        switch (nd.tag) {
-            case Z2D_MOVE_TO:
-                inf.n_emit = 0;
-                if (j == F.n_nodes - 1) break;  // trailing move_to (fill_plotter.zig:38-40)
-                fx = lx = nd.p[0];
-                fy = ly = nd.p[1];
-                count = 1;
-                break;
-            case Z2D_LINE_TO:
-                inf.sx = lx;
-                inf.sy = ly;
-                inf.n_emit = 1;
-                if (!pt_eq(lx, ly, nd.p[0], nd.p[1])) count = min(count + 1, 3);
-                lx = nd.p[0];
-                ly = nd.p[1];
-                break;
-            case Z2D_CURVE_TO: {
-                inf.sx = lx;
-                inf.sy = ly;
-                if (inf.n_emit < 0) {  // start depends on a preceding close_path
-                    int32_t ne = 0, na = 0;
-                    double px = lx, py = ly;
-                    auto cnt = [&](double x, double y) {
-                        ne++;
-                        if (!pt_eq(x, y, px, py)) na++;
-                        px = x;
-                        py = y;
-                    };
-                    if (!spline_walk(lx, ly, nd.p, F.tol, cnt)) atomicExch(status, Z2D_ERR_INVALID_STATE);
-                    inf.n_emit = ne;
-                    inf.n_added = na;
-                }
-                count = min(count + inf.n_added, 3);
-                lx = nd.p[4];
-                ly = nd.p[5];
-                break;
-            }
-            default:  // close_path (fill_plotter.zig:72-92)
-                inf.n_emit = 0;
-                inf.sx = lx;
-                inf.sy = ly;
-                inf.ex = fx;
-                inf.ey = fy;
-                if (count >= 3) {
-                    if (!pt_eq(lx, ly, fx, fy)) {
-                        inf.n_emit = 1;
-                        lx = fx;
-                        ly = fy;
-                    }
-                } else if (!pt_eq(lx, ly, fx, fy)) {
-                    flags |= FILL_OPEN_CHAIN;  // a lone edge stays unmatched
-                }
-                break;
+    for (int32_t base = 0; base < n_nodes; base += 32) {
+        const int32_t j = base + lane;
+        const bool valid = j < n_nodes;
+        NodeInfo inf{};
+        if (valid) {
+            const z2d_node nd = nodes[node_off + j];
+            inf = info[node_off + j];
+            S.tag[lane] = nd.tag;
+            S.x[lane] = nd.tag == Z2D_CURVE_TO ? nd.p[4] : nd.p[0];
+            S.y[lane] = nd.tag == Z2D_CURVE_TO ? nd.p[5] : nd.p[1];
+            S.n_emit[lane] = inf.n_emit;
+            S.n_added[lane] = inf.n_added;
+            S.sx[lane] = inf.sx;
+            S.sy[lane] = inf.sy;
+            S.ex[lane] = inf.ex;
+            S.ey[lane] = inf.ey;
         }
-        off += inf.n_emit;
-        info[i] = inf;
+        __syncwarp();
+        if (lane == 0) {
+            const int32_t m = min(32, n_nodes - base);
+            for (int32_t k = 0; k < m; k++) {
+                S.off[k] = off;
+                int32_t ne;
+                const double px = S.x[k], py = S.y[k];
+                switch (S.tag[k]) {
+                    case Z2D_MOVE_TO:
+                        ne = 0;
+                        if (base + k == n_nodes - 1) break;  // trailing move_to (fill_plotter.zig:38-40)
+                        fx = lx = px;
+                        fy = ly = py;
+                        count = 1;
+                        break;
+                    case Z2D_LINE_TO:
+                        S.sx[k] = lx;
+                        S.sy[k] = ly;
+                        ne = 1;
+                        if (!pt_eq(lx, ly, px, py)) count = min(count + 1, 3);
+                        lx = px;
+                        ly = py;
+                        break;
+                    case Z2D_CURVE_TO: {
+                        S.sx[k] = lx;
+                        S.sy[k] = ly;
+                        ne = S.n_emit[k];
+                        if (ne < 0) {  // start depends on a preceding close_path
+                            int32_t cne = 0, cna = 0;
+                            double qx = lx, qy = ly;
+                            auto cnt = [&](double x, double y) {
+                                cne++;
+                                if (!pt_eq(x, y, qx, qy)) cna++;
+                                qx = x;
+                                qy = y;
+                            };
+                            if (!spline_walk(lx, ly, nodes[node_off + base + k].p, tol, cnt))
+                                atomicExch(status, Z2D_ERR_INVALID_STATE);
+                            ne = cne;
+                            S.n_added[k] = cna;
+                        }
+                        count = min(count + S.n_added[k], 3);
+                        lx = px;
+                        ly = py;
+                        break;
+                    }
+                    default:  // close_path (fill_plotter.zig:72-92)
+                        ne = 0;
+                        S.sx[k] = lx;
+                        S.sy[k] = ly;
+                        S.ex[k] = fx;
+                        S.ey[k] = fy;
+                        if (count >= 3) {
+                            if (!pt_eq(lx, ly, fx, fy)) {
+                                ne = 1;
+                                lx = fx;
+                                ly = fy;
+                            }
+                        } else if (!pt_eq(lx, ly, fx, fy)) {
+                            flags |= FILL_OPEN_CHAIN;  // a lone edge stays unmatched
+                        }
+                        break;
+                }
+                S.n_emit[k] = ne;
+                off += ne;
+            }
+        }
+        __syncwarp();
+        if (valid) {
+            inf.edge_off = S.off[lane];
+            inf.n_emit = S.n_emit[lane];
+            inf.n_added = S.n_added[lane];
+            inf.sx = S.sx[lane];
+            inf.sy = S.sy[lane];
+            inf.ex = S.ex[lane];
+            inf.ey = S.ey[lane];
+            info[node_off + j] = inf;
+        }
+        __syncwarp();
     }
-    st[f].n_edges = off;
-    st[f].edge_base = atomicAdd(&counters[CNT_EDGES], off);
-    st[f].flags = flags;
-    st[f].ext[0] = ~0ull;  // min slots start at the largest key
-    st[f].ext[1] = 0ull;
-    st[f].ext[2] = ~0ull;
-    st[f].ext[3] = 0ull;
+    if (lane == 0) {
+        st[f].n_edges = off;
+        st[f].edge_base = atomicAdd(&counters[CNT_EDGES], off);
+        st[f].flags = flags;
+        st[f].ext[0] = ~0ull;  // min slots start at the largest key
+        st[f].ext[1] = 0ull;
+        st[f].ext[2] = ~0ull;
+        st[f].ext[3] = 0ull;
+    }
 }
 
-__global__ void k_node_emit(const z2d_node *__restrict__ nodes, const int32_t *__restrict__ node_fill,
-                            const FillCmd *__restrict__ fills, const NodeInfo *__restrict__ info,
-                            FillState *__restrict__ st, DEdge *__restrict__ edges, int32_t n_nodes) {
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_nodes) return;
-    const NodeInfo inf = info[i];
-    if (inf.n_emit <= 0) return;
-    const z2d_node nd = nodes[i];
-    const int32_t f = node_fill[i];
-    const FillCmd F = fills[f];
-    DEdge *out = edges + st[f].edge_base + inf.edge_off;
-    double et = 0, eb = 0, el = 0, er = 0;
-    bool any = false;
-    if (nd.tag == Z2D_LINE_TO) {
-        add_edge(F, out, inf.sx, inf.sy, nd.p[0], nd.p[1], et, eb, el, er, any);
-    } else if (nd.tag == Z2D_CLOSE_PATH) {
-        add_edge(F, out, inf.sx, inf.sy, inf.ex, inf.ey, et, eb, el, er, any);
-    } else {
-        double px = inf.sx, py = inf.sy;
-        int32_t k = 0;
-        auto em = [&](double x, double y) {
-            if (k < inf.n_emit) add_edge(F, out + k, px, py, x, y, et, eb, el, er, any);
-            k++;
-            px = x;
-            py = y;
-        };
-        spline_walk(inf.sx, inf.sy, nd.p, F.tol, em);
-    }
-    if (any) {
-        FillState &S = st[f];
-        atomicMin(&S.ext[0], dkey(et));
-        atomicMax(&S.ext[1], dkey(eb));
-        atomicMin(&S.ext[2], dkey(el));
-        atomicMax(&S.ext[3], dkey(er));
-        atomicOr(&S.has_edges, 1);
-    }
-}
 
 // ------------------------------------------- warp-cooperative flattening
 // One warp per curve.  The subdivision tree of Spline.decomposeInto is first
@@ -426,46 +409,148 @@ __device__ bool curve_count_warp(double sx, double sy, const double *p, double t
     return __all_sync(0xffffffffu, ok);
 }
 
+// Appends idx to a device list (one atomic per warp); all lanes call it.
+__device__ __forceinline__ void queue_push(bool push, int32_t idx, int32_t *list, int32_t *count, int lane) {
+    const unsigned all = 0xffffffffu;
+    const unsigned m = __ballot_sync(all, push);
+    if (!m) return;
+    int32_t base = 0;
+    if (lane == 0) base = atomicAdd(count, __popc(m));
+    base = __shfl_sync(all, base, 0);
+    if (push) list[base + __popc(m & ((1u << lane) - 1u))] = idx;
+}
+
+// The node kernels take 32 consecutive nodes per warp: every lane handles
+// its own line, move and close_path node and queues its curve, if it has
+// one; the curve kernels then subdivide one queued curve per warp.
 __global__ void __launch_bounds__(32 * kFlattenWarps) k_node_count_w(const z2d_node *__restrict__ nodes,
                                                                      const int32_t *__restrict__ node_fill,
                                                                      const FillCmd *__restrict__ fills,
                                                                      NodeInfo *__restrict__ info, int32_t n_nodes,
-                                                                     uint16_t *__restrict__ item_leaves,
-                                                                     int32_t *__restrict__ status) {
+                                                                     int32_t *__restrict__ curves,
+                                                                     int32_t *__restrict__ counters) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int32_t base = (blockIdx.x * kFlattenWarps + w) * 32; base < n_nodes;
+         base += gridDim.x * kFlattenWarps * 32) {
+        const int32_t i = base + lane;
+        NodeInfo inf{};
+        bool curve = false;
+        if (i < n_nodes) {
+            const int32_t f = node_fill[i];
+            if (f >= 0) {  // else no fill owns the node
+                const z2d_node nd = nodes[i];
+                const bool first_of_fill = (i == fills[f].node_off);
+                if (nd.tag == Z2D_LINE_TO || nd.tag == Z2D_CURVE_TO) {
+                    const z2d_node pv = first_of_fill ? nd : nodes[i - 1];
+                    const bool static_start = !first_of_fill && (pv.tag == Z2D_MOVE_TO || pv.tag == Z2D_LINE_TO ||
+                                                                 pv.tag == Z2D_CURVE_TO);
+                    if (!static_start) {
+                        inf.n_emit = -1;  // resolved by k_fill_scan
+                    } else if (nd.tag == Z2D_LINE_TO) {
+                        const double sx = pv.tag == Z2D_CURVE_TO ? pv.p[4] : pv.p[0];
+                        const double sy = pv.tag == Z2D_CURVE_TO ? pv.p[5] : pv.p[1];
+                        inf.n_emit = 1;
+                        inf.n_added = pt_eq(sx, sy, nd.p[0], nd.p[1]) ? 0 : 1;
+                    } else {
+                        curve = true;  // k_curve_count_w fills in its info
+                    }
+                }
+            }
+        }
+        if (i < n_nodes && !curve) info[i] = inf;
+        queue_push(curve, i, curves, counters + CNT_CURVES, lane);
+    }
+}
+
+__global__ void __launch_bounds__(32 * kFlattenWarps) k_curve_count_w(const z2d_node *__restrict__ nodes,
+                                                                      const int32_t *__restrict__ node_fill,
+                                                                      const FillCmd *__restrict__ fills,
+                                                                      NodeInfo *__restrict__ info,
+                                                                      const int32_t *__restrict__ curves,
+                                                                      const int32_t *__restrict__ counters,
+                                                                      uint16_t *__restrict__ item_leaves,
+                                                                      int32_t *__restrict__ status) {
     __shared__ WarpFrontier frs[kFlattenWarps];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     WarpFrontier &fr = frs[w];
-    for (int32_t i = blockIdx.x * kFlattenWarps + w; i < n_nodes; i += gridDim.x * kFlattenWarps) {
-        NodeInfo inf{};
-        const int32_t f = node_fill[i];
-        if (f < 0) {  // no fill owns the node
-            if (lane == 0) info[i] = inf;
-            continue;
-        }
+    const int32_t n = counters[CNT_CURVES];
+    for (int32_t q = blockIdx.x * kFlattenWarps + w; q < n; q += gridDim.x * kFlattenWarps) {
+        const int32_t i = curves[q];
         const z2d_node nd = nodes[i];
-        const FillCmd &F = fills[f];
-        const bool first_of_fill = (i == F.node_off);
-        if (nd.tag == Z2D_LINE_TO || nd.tag == Z2D_CURVE_TO) {
-            const z2d_node pv = first_of_fill ? nd : nodes[i - 1];
-            const bool static_start =
-                !first_of_fill && (pv.tag == Z2D_MOVE_TO || pv.tag == Z2D_LINE_TO || pv.tag == Z2D_CURVE_TO);
-            if (!static_start) {
-                inf.n_emit = -1;  // resolved by k_fill_scan
-            } else {
-                const double sx = pv.tag == Z2D_CURVE_TO ? pv.p[4] : pv.p[0];
-                const double sy = pv.tag == Z2D_CURVE_TO ? pv.p[5] : pv.p[1];
-                if (nd.tag == Z2D_LINE_TO) {
-                    inf.n_emit = 1;
-                    inf.n_added = pt_eq(sx, sy, nd.p[0], nd.p[1]) ? 0 : 1;
-                } else if (!curve_count_warp(sx, sy, nd.p, F.tol, fr, lane, inf.n_emit, inf.n_added,
-                                             item_leaves + (size_t)i * kFrontier, inf.chords)) {
-                    if (lane == 0) atomicExch(status, Z2D_ERR_INVALID_STATE);
-                }
-            }
+        const z2d_node pv = nodes[i - 1];
+        const double sx = pv.tag == Z2D_CURVE_TO ? pv.p[4] : pv.p[0];
+        const double sy = pv.tag == Z2D_CURVE_TO ? pv.p[5] : pv.p[1];
+        NodeInfo inf{};
+        if (!curve_count_warp(sx, sy, nd.p, fills[node_fill[i]].tol, fr, lane, inf.n_emit, inf.n_added,
+                              item_leaves + (size_t)i * kFrontier, inf.chords)) {
+            if (lane == 0) atomicExch(status, Z2D_ERR_INVALID_STATE);
         }
         if (lane == 0) info[i] = inf;
         __syncwarp();
     }
+}
+
+// Emits the edges of one curve with the whole warp.
+__device__ __forceinline__ void curve_emit_warp(const FillCmd &F, DEdge *out, const NodeInfo &inf, const double *p,
+                                                const uint16_t *il, WarpFrontier &fr, int lane, double &et, double &eb,
+                                                double &el, double &er, bool &any) {
+    const Tol tol2 = make_tol(F.tol);
+    const int n = frontier_expand(inf.sx, inf.sy, p, tol2, fr, lane);
+    if (inf.chords) {
+        // One walk: the edges are the leaves' chords (a -> d), and the
+        // count pass left each frontier item's leaf count.
+        int32_t base_off = 0;
+        for (int base = 0; base < n; base += 32) {
+            const int i2 = base + lane;
+            const int32_t cnt = i2 < n ? (int32_t)il[i2] : 0;
+            int tot = 0;
+            const int off = base_off + warp_excl_sum(cnt, lane, tot);
+            if (i2 < n && cnt > 0) {
+                int32_t k = off;
+                walk_leaves(fr.k[i2], fr.leaf[i2] != 0, tol2, [&](const Knots &kn) {
+                    if (k < inf.n_emit) add_edge(F, out + k, kn.ax, kn.ay, kn.dx, kn.dy, et, eb, el, er, any);
+                    k++;
+                });
+            }
+            base_off += tot;
+        }
+        return;
+    }
+    int32_t base_off = 0;
+    double carry_x = inf.sx, carry_y = inf.sy;
+    for (int base = 0; base < n; base += 32) {
+        const int i2 = base + lane;
+        int32_t cnt = 0;
+        double lx = 0, ly = 0;
+        if (i2 < n)
+            walk_item(fr.k[i2], fr.leaf[i2] != 0, inf.sx, inf.sy, tol2, [&](double x, double y) {
+                cnt++;
+                lx = x;
+                ly = y;
+            });
+        double px, py;
+        prev_point_scan(cnt > 0, lx, ly, carry_x, carry_y, lane, px, py);
+        int tot = 0;
+        const int off = base_off + warp_excl_sum(cnt, lane, tot);
+        if (i2 < n && cnt > 0) {
+            int32_t k = off;
+            walk_item(fr.k[i2], fr.leaf[i2] != 0, inf.sx, inf.sy, tol2, [&](double x, double y) {
+                if (k < inf.n_emit) add_edge(F, out + k, px, py, x, y, et, eb, el, er, any);
+                k++;
+                px = x;
+                py = y;
+            });
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, cnt > 0);
+        if (m) {
+            const int src = 31 - __clz(m);
+            carry_x = __shfl_sync(0xffffffffu, lx, src);
+            carry_y = __shfl_sync(0xffffffffu, ly, src);
+        }
+        base_off += tot;
+    }
+    if (lane == 0 && base_off < inf.n_emit)  // final lineTo(d)
+        add_edge(F, out + base_off, carry_x, carry_y, p[4], p[5], et, eb, el, er, any);
 }
 
 __global__ void __launch_bounds__(32 * kFlattenWarps) k_node_emit_w(const z2d_node *__restrict__ nodes,
@@ -473,107 +558,60 @@ __global__ void __launch_bounds__(32 * kFlattenWarps) k_node_emit_w(const z2d_no
                                                                     const FillCmd *__restrict__ fills,
                                                                     const NodeInfo *__restrict__ info,
                                                                     FillState *__restrict__ st, DEdge *__restrict__ edges,
-                                                                    const uint16_t *__restrict__ item_leaves,
-                                                                    int32_t n_nodes) {
+                                                                    int32_t n_nodes, int32_t *__restrict__ curves,
+                                                                    int32_t *__restrict__ counters) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int32_t base = (blockIdx.x * kFlattenWarps + w) * 32; base < n_nodes;
+         base += gridDim.x * kFlattenWarps * 32) {
+        const int32_t i = base + lane;
+        int32_t f = -1;
+        bool curve = false;
+        double et = 0, eb = 0, el = 0, er = 0;
+        bool any = false;
+        if (i < n_nodes) {
+            const NodeInfo inf = info[i];
+            if (inf.n_emit > 0) {
+                const z2d_node nd = nodes[i];
+                f = node_fill[i];
+                const FillCmd &F = fills[f];
+                DEdge *out = edges + st[f].edge_base + inf.edge_off;
+                const bool straight = nd.tag == Z2D_CURVE_TO && pt_eq(inf.sx, inf.sy, nd.p[0], nd.p[1]) &&
+                                      pt_eq(nd.p[2], nd.p[3], nd.p[4], nd.p[5]);
+                if (nd.tag == Z2D_LINE_TO) add_edge(F, out, inf.sx, inf.sy, nd.p[0], nd.p[1], et, eb, el, er, any);
+                else if (nd.tag == Z2D_CLOSE_PATH) add_edge(F, out, inf.sx, inf.sy, inf.ex, inf.ey, et, eb, el, er, any);
+                else if (straight) add_edge(F, out, inf.sx, inf.sy, nd.p[4], nd.p[5], et, eb, el, er, any);
+                else curve = true;  // k_curve_emit_w emits it
+            }
+        }
+        queue_push(curve, i, curves, counters + CNT_CURVES_EMIT, lane);
+        merge_extents(st, f, any, et, eb, el, er);
+    }
+}
+
+__global__ void __launch_bounds__(32 * kFlattenWarps) k_curve_emit_w(const z2d_node *__restrict__ nodes,
+                                                                     const int32_t *__restrict__ node_fill,
+                                                                     const FillCmd *__restrict__ fills,
+                                                                     const NodeInfo *__restrict__ info,
+                                                                     FillState *__restrict__ st,
+                                                                     DEdge *__restrict__ edges,
+                                                                     const int32_t *__restrict__ curves,
+                                                                     const int32_t *__restrict__ counters,
+                                                                     const uint16_t *__restrict__ item_leaves) {
     __shared__ WarpFrontier frs[kFlattenWarps];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     WarpFrontier &fr = frs[w];
-    for (int32_t i = blockIdx.x * kFlattenWarps + w; i < n_nodes; i += gridDim.x * kFlattenWarps) {
+    const int32_t n = counters[CNT_CURVES_EMIT];
+    for (int32_t q = blockIdx.x * kFlattenWarps + w; q < n; q += gridDim.x * kFlattenWarps) {
+        const int32_t i = curves[q];
         const NodeInfo inf = info[i];
-        if (inf.n_emit <= 0) continue;  // uniform across the warp
         const z2d_node nd = nodes[i];
         const int32_t f = node_fill[i];
         const FillCmd &F = fills[f];
         DEdge *out = edges + st[f].edge_base + inf.edge_off;
         double et = 0, eb = 0, el = 0, er = 0;
         bool any = false;
-        const bool straight = nd.tag == Z2D_CURVE_TO && pt_eq(inf.sx, inf.sy, nd.p[0], nd.p[1]) && pt_eq(nd.p[2], nd.p[3], nd.p[4], nd.p[5]);
-        if (nd.tag != Z2D_CURVE_TO || straight) {
-            if (lane == 0) {
-                if (nd.tag == Z2D_LINE_TO) add_edge(F, out, inf.sx, inf.sy, nd.p[0], nd.p[1], et, eb, el, er, any);
-                else if (nd.tag == Z2D_CLOSE_PATH) add_edge(F, out, inf.sx, inf.sy, inf.ex, inf.ey, et, eb, el, er, any);
-                else add_edge(F, out, inf.sx, inf.sy, nd.p[4], nd.p[5], et, eb, el, er, any);
-            }
-        } else if (inf.chords) {
-            // One walk: the edges are the leaves' chords (a -> d), and the
-            // count pass left each frontier item's leaf count.
-            const Tol tol2 = make_tol(F.tol);
-            const int n = frontier_expand(inf.sx, inf.sy, nd.p, tol2, fr, lane);
-            const uint16_t *il = item_leaves + (size_t)i * kFrontier;
-            int32_t base_off = 0;
-            for (int base = 0; base < n; base += 32) {
-                const int i2 = base + lane;
-                const int32_t cnt = i2 < n ? (int32_t)il[i2] : 0;
-                int tot = 0;
-                const int off = base_off + warp_excl_sum(cnt, lane, tot);
-                if (i2 < n && cnt > 0) {
-                    int32_t k = off;
-                    walk_leaves(fr.k[i2], fr.leaf[i2] != 0, tol2, [&](const Knots &kn) {
-                        if (k < inf.n_emit) add_edge(F, out + k, kn.ax, kn.ay, kn.dx, kn.dy, et, eb, el, er, any);
-                        k++;
-                    });
-                }
-                base_off += tot;
-            }
-        } else {
-            const Tol tol2 = make_tol(F.tol);
-            const int n = frontier_expand(inf.sx, inf.sy, nd.p, tol2, fr, lane);
-            int32_t base_off = 0;
-            double carry_x = inf.sx, carry_y = inf.sy;
-            for (int base = 0; base < n; base += 32) {
-                const int i2 = base + lane;
-                int32_t cnt = 0;
-                double lx = 0, ly = 0;
-                if (i2 < n)
-                    walk_item(fr.k[i2], fr.leaf[i2] != 0, inf.sx, inf.sy, tol2, [&](double x, double y) {
-                        cnt++;
-                        lx = x;
-                        ly = y;
-                    });
-                double px, py;
-                prev_point_scan(cnt > 0, lx, ly, carry_x, carry_y, lane, px, py);
-                int tot = 0;
-                const int off = base_off + warp_excl_sum(cnt, lane, tot);
-                if (i2 < n && cnt > 0) {
-                    int32_t k = off;
-                    walk_item(fr.k[i2], fr.leaf[i2] != 0, inf.sx, inf.sy, tol2, [&](double x, double y) {
-                        if (k < inf.n_emit) add_edge(F, out + k, px, py, x, y, et, eb, el, er, any);
-                        k++;
-                        px = x;
-                        py = y;
-                    });
-                }
-                const unsigned m = __ballot_sync(0xffffffffu, cnt > 0);
-                if (m) {
-                    const int src = 31 - __clz(m);
-                    carry_x = __shfl_sync(0xffffffffu, lx, src);
-                    carry_y = __shfl_sync(0xffffffffu, ly, src);
-                }
-                base_off += tot;
-            }
-            if (lane == 0 && base_off < inf.n_emit)  // final lineTo(d)
-                add_edge(F, out + base_off, carry_x, carry_y, nd.p[4], nd.p[5], et, eb, el, er, any);
-        }
-        // warp reduction of the extents of this node's edges
-        const unsigned anym = __ballot_sync(0xffffffffu, any);
-        if (anym) {
-            double mt = any ? et : 1e300, mb = any ? eb : -1e300, ml = any ? el : 1e300, mr = any ? er : -1e300;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                mt = fmin(mt, __shfl_xor_sync(0xffffffffu, mt, o));
-                mb = fmax(mb, __shfl_xor_sync(0xffffffffu, mb, o));
-                ml = fmin(ml, __shfl_xor_sync(0xffffffffu, ml, o));
-                mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
-            }
-            if (lane == 0) {
-                FillState &S = st[f];
-                atomicMin(&S.ext[0], dkey(mt));
-                atomicMax(&S.ext[1], dkey(mb));
-                atomicMin(&S.ext[2], dkey(ml));
-                atomicMax(&S.ext[3], dkey(mr));
-                atomicOr(&S.has_edges, 1);
-            }
-        }
+        curve_emit_warp(F, out, inf, nd.p, item_leaves + (size_t)i * kFrontier, fr, lane, et, eb, el, er, any);
+        merge_extents(st, f, any, et, eb, el, er);
         __syncwarp();
     }
 }
@@ -1335,12 +1373,28 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
 // ----------------------------------------------------------- host side
 static inline unsigned grid_for(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
-int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n_first, std::vector<FillCmd> &fills,
+// memcpy, split over host threads when it is large
+static void par_copy(void *dst, const void *src, size_t bytes) {
+    constexpr size_t kChunk = (size_t)64 << 20;
+    const size_t nt = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), bytes / kChunk + 1);
+    if (nt <= 1) {
+        memcpy(dst, src, bytes);
+        return;
+    }
+    const size_t per = (bytes + nt - 1) / nt;
+    std::vector<std::thread> pool;
+    for (size_t t = 0; t < nt; t++) {
+        const size_t a = t * per, b = std::min(bytes, a + per);
+        if (a >= b) break;
+        pool.emplace_back([=] { memcpy(static_cast<uint8_t *>(dst) + a, static_cast<const uint8_t *>(src) + a, b - a); });
+    }
+    for (auto &th : pool) th.join();
+}
+
+int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n_nodes, std::vector<FillCmd> &fills,
              const std::vector<int32_t> &node_fill, const std::vector<DevGradient> &grads,
-             const std::vector<int32_t> &grad_of_fill, const z2d_node *nodes2, int32_t n_second,
-             const StrokeSet *strokes) {
-    if (n_first < 0 || n_second < 0 || (int64_t)n_first + n_second > 0x7FFFFFFF) return Z2D_ERR_INVALID_ARGUMENT;
-    const int32_t n_nodes = n_first + n_second;
+             const std::vector<int32_t> &grad_of_fill, const StrokeSet *strokes) {
+    if (n_nodes < 0) return Z2D_ERR_INVALID_ARGUMENT;
     const int32_t n_fills = (int32_t)fills.size();
     const int32_t n_jobs = (int32_t)jobs.size();
     if (n_fills == 0 || n_nodes == 0 || n_jobs == 0) return Z2D_OK;
@@ -1364,7 +1418,33 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     const size_t o_sk = al(o_cnt + sizeof(int32_t) * CNT_COUNT);
     const size_t o_sb = al(o_sk + sizeof(StrokeDev) * n_sk);
     const size_t o_tr = al(o_sb + sizeof(SubpathDev) * n_sb);
-    const size_t total = al(o_tr + sizeof(double) * n_tr);
+    // host-built polygons: per polygon its edge count, per contour its
+    // start / size / fill / first edge, then the points
+    const size_t n_poly = has_strokes ? strokes->polys.size() : 0;
+    std::vector<int32_t> poly_fill(n_poly, -1);
+    for (int32_t f = 0; f < n_fills; f++)
+        if (fills[f].poly >= 0) poly_fill[(size_t)fills[f].poly] = f;
+    long long n_pts = 0, n_ctr = 0;
+    for (size_t k = 0; k < n_poly; k++) {
+        const long long np = (long long)strokes->polys[k]->points();
+        if (np > 0x7FFFFFFFll) {
+            set_error("batch too large: more than 2^31 edges in one polygon");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+        n_pts += np;
+        n_ctr += (long long)strokes->polys[k]->ends.size();
+    }
+    if (n_ctr > 0x7FFFFFFFll) {
+        set_error("batch too large: more than 2^31 contours");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    const size_t o_pe = al(o_tr + sizeof(double) * n_tr);
+    const size_t o_cs = al(o_pe + sizeof(int32_t) * n_poly);
+    const size_t o_cn = al(o_cs + sizeof(long long) * (size_t)n_ctr);
+    const size_t o_cf = al(o_cn + sizeof(int32_t) * (size_t)n_ctr);
+    const size_t o_ce = al(o_cf + sizeof(int32_t) * (size_t)n_ctr);
+    const size_t o_pt = al(o_ce + sizeof(int32_t) * (size_t)n_ctr);
+    const size_t total = al(o_pt + sizeof(double) * 2 * (size_t)n_pts);
     if (c.params.ensure(total) || c.staging.ensure(total)) return Z2D_ERR_OUT_OF_MEMORY;
     uint8_t *h = c.staging.as<uint8_t>();
     uint8_t *dv = c.params.as<uint8_t>();
@@ -1373,9 +1453,8 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
         if (grad_of_fill[i] >= 0) fills[i].src.grad = dgrads + grad_of_fill[i];
     // make sure the previous call's kernels no longer read the staging buffer
     Z2D_CUDA(cudaStreamSynchronize(c.stream));
-    if (n_first > 0) memcpy(h + o_nodes, nodes, sizeof(z2d_node) * (size_t)n_first);
-    if (n_second > 0) memcpy(h + o_nodes + sizeof(z2d_node) * (size_t)n_first, nodes2, sizeof(z2d_node) * (size_t)n_second);
-    memcpy(h + o_nfill, node_fill.data(), sizeof(int32_t) * (size_t)n_nodes);
+    if (n_nodes > 0) par_copy(h + o_nodes, nodes, sizeof(z2d_node) * (size_t)n_nodes);
+    par_copy(h + o_nfill, node_fill.data(), sizeof(int32_t) * (size_t)n_nodes);
     if (!grads.empty()) memcpy(h + o_grads, grads.data(), sizeof(DevGradient) * grads.size());
     memcpy(h + o_fills, fills.data(), sizeof(FillCmd) * (size_t)n_fills);
     memcpy(h + o_jobs, jobs.data(), sizeof(DevJob) * (size_t)n_jobs);
@@ -1386,6 +1465,44 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
         memcpy(h + o_sb, strokes->subs.data(), sizeof(SubpathDev) * n_sb);
         if (n_tr > 0) memcpy(h + o_tr, strokes->trig.data(), sizeof(double) * n_tr);
     }
+    if (n_poly > 0) {
+        int32_t *pe = reinterpret_cast<int32_t *>(h + o_pe);
+        long long *cs = reinterpret_cast<long long *>(h + o_cs);
+        int32_t *cn = reinterpret_cast<int32_t *>(h + o_cn), *cf = reinterpret_cast<int32_t *>(h + o_cf);
+        int32_t *ce = reinterpret_cast<int32_t *>(h + o_ce);
+        std::vector<long long> base(n_poly);
+        long long pt = 0, ct = 0;
+        for (size_t k = 0; k < n_poly; k++) {
+            const stroke::Polygon &P = *strokes->polys[k];
+            base[k] = pt;
+            pe[k] = (int32_t)P.points();
+            uint64_t prev = 0;
+            for (uint64_t e : P.ends) {
+                cs[ct] = pt + (long long)prev;
+                cn[ct] = (int32_t)(e - prev);
+                cf[ct] = poly_fill[k];
+                ce[ct] = (int32_t)prev;
+                prev = e;
+                ct++;
+            }
+            pt += (long long)P.points();
+        }
+        // the points, polygon by polygon, over host threads
+        double *hp = reinterpret_cast<double *>(h + o_pt);
+        const size_t nt = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()),
+                                           (size_t)(n_pts >> 20) + 1);
+        std::atomic<size_t> next{0};
+        auto work = [&] {
+            for (size_t k; (k = next.fetch_add(1)) < n_poly;) {
+                const stroke::Polygon &P = *strokes->polys[k];
+                if (!P.xy.empty()) memcpy(hp + 2 * base[k], P.xy.data(), sizeof(double) * P.xy.size());
+            }
+        };
+        std::vector<std::thread> pool;
+        for (size_t t = 1; t < nt; t++) pool.emplace_back(work);
+        work();
+        for (auto &th : pool) th.join();
+    }
     Z2D_CUDA(cudaMemcpyAsync(dv, h, total, cudaMemcpyHostToDevice, c.stream));
     const z2d_node *d_nodes = reinterpret_cast<const z2d_node *>(dv + o_nodes);
     const int32_t *d_nfill = reinterpret_cast<const int32_t *>(dv + o_nfill);
@@ -1395,21 +1512,30 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
 
     // node info, then the per-node leaf counts of the curves' frontier items
     const size_t info_bytes = (sizeof(NodeInfo) * (size_t)n_nodes + 255) & ~(size_t)255;
-    if (c.node_info.ensure(info_bytes + sizeof(uint16_t) * kFrontier * (size_t)n_nodes) ||
+    const size_t items_bytes = (sizeof(uint16_t) * kFrontier * (size_t)n_nodes + 255) & ~(size_t)255;
+    if (c.node_info.ensure(info_bytes + items_bytes + 2 * sizeof(int32_t) * (size_t)n_nodes) ||
         c.fill_state.ensure(sizeof(FillState) * (size_t)n_fills))
         return Z2D_ERR_OUT_OF_MEMORY;
     NodeInfo *d_info = c.node_info.as<NodeInfo>();
     uint16_t *d_items = reinterpret_cast<uint16_t *>(c.node_info.as<uint8_t>() + info_bytes);
+    int32_t *d_curves = reinterpret_cast<int32_t *>(c.node_info.as<uint8_t>() + info_bytes + items_bytes);  // 2 queues
     FillState *d_st = c.fill_state.as<FillState>();
     Z2D_CUDA(cudaMemsetAsync(d_st, 0, sizeof(FillState) * (size_t)n_fills, c.stream));
 
     // ---- flatten
-    const unsigned flat_blocks = (unsigned)std::min<long long>(grid_for(n_nodes, kFlattenWarps), (long long)c.sm_count * 64);
+    const unsigned flat_blocks =
+        (unsigned)std::min<long long>(grid_for((n_nodes + 31) / 32, kFlattenWarps), (long long)c.sm_count * 64);
+    // one warp per queued curve, as many as there could be curves up to a
+    // few resident blocks per SM
+    const unsigned curve_blocks =
+        (unsigned)std::min<long long>(grid_for(n_nodes, kFlattenWarps), (long long)c.sm_count * 8);
     cudaEvent_t tf = c.timer_begin(c.t_flatten);
     k_node_count_w<<<flat_blocks, 32 * kFlattenWarps, 0, c.stream>>>(d_nodes, d_nfill, d_fills, d_info, n_nodes,
-                                                                    d_items, d_cnt + CNT_STATUS);
+                                                                    d_curves, d_cnt);
+    k_curve_count_w<<<curve_blocks, 32 * kFlattenWarps, 0, c.stream>>>(d_nodes, d_nfill, d_fills, d_info, d_curves,
+                                                                      d_cnt, d_items, d_cnt + CNT_STATUS);
     StrokeRun srun;
-    if (has_strokes) {
+    if (n_sk > 0) {
         srun.nodes = d_nodes;
         srun.strokes = reinterpret_cast<const StrokeDev *>(dv + o_sk);
         srun.subs = reinterpret_cast<const SubpathDev *>(dv + o_sb);
@@ -1421,10 +1547,11 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
         const int rc = stroke_count(c, srun, d_cnt + CNT_STATUS);
         if (rc) return rc;
     }
-    k_fill_scan<<<grid_for(n_fills, 64), 64, 0, c.stream>>>(d_nodes, d_fills, d_info, d_st, n_fills, d_cnt,
-                                                             d_cnt + CNT_STATUS, srun.stroke_edges);
+    k_fill_scan<<<grid_for(n_fills, kScanWarps), 32 * kScanWarps, 0, c.stream>>>(
+        d_nodes, d_fills, d_info, d_st, n_fills, d_cnt, d_cnt + CNT_STATUS, srun.stroke_edges,
+        reinterpret_cast<const int32_t *>(dv + o_pe));
     c.timer_end(c.t_flatten, tf);
-    c.launches += 2;
+    c.launches += 3;
     const size_t rb_jobs_off = al(sizeof(int32_t) * CNT_COUNT + 2 * sizeof(long long));
     const size_t rb_bytes = rb_jobs_off + sizeof(DevJob) * (size_t)n_jobs;
     if (c.readback.ensure(rb_bytes)) return Z2D_ERR_OUT_OF_MEMORY;
@@ -1432,7 +1559,7 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     long long *rb_tot = reinterpret_cast<long long *>(rb + CNT_COUNT);  // stroke contour totals (8-aligned: CNT_COUNT even)
     DevJob *rb_jobs = reinterpret_cast<DevJob *>(c.readback.as<uint8_t>() + rb_jobs_off);
     Z2D_CUDA(cudaMemcpyAsync(rb, d_cnt, sizeof(int32_t) * CNT_COUNT, cudaMemcpyDeviceToHost, c.stream));
-    if (has_strokes)
+    if (n_sk > 0)
         Z2D_CUDA(cudaMemcpyAsync(rb_tot, stroke_totals_dev(srun), 2 * sizeof(long long), cudaMemcpyDeviceToHost,
                                  c.stream));
     Z2D_CUDA(cudaStreamSynchronize(c.stream));
@@ -1441,7 +1568,7 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
                                                           : "batch too large: more than 2^31 edges in one polygon");
         return rb[CNT_STATUS];
     }
-    if (has_strokes) {
+    if (n_sk > 0) {
         srun.n_a = rb_tot[0];
         srun.n_b = rb_tot[1];
     }
@@ -1454,15 +1581,29 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     // extents start at +inf/-inf keys: min slots 0xFF.., max slots 0
     tf = c.timer_begin(c.t_flatten);
     k_node_emit_w<<<flat_blocks, 32 * kFlattenWarps, 0, c.stream>>>(d_nodes, d_nfill, d_fills, d_info, d_st, d_edges,
-                                                                   d_items, n_nodes);
-    if (has_strokes) {
+                                                                   n_nodes, d_curves + n_nodes, d_cnt);
+    k_curve_emit_w<<<curve_blocks, 32 * kFlattenWarps, 0, c.stream>>>(d_nodes, d_nfill, d_fills, d_info, d_st,
+                                                                     d_edges, d_curves + n_nodes, d_cnt, d_items);
+    if (n_sk > 0) {
         const int rc = stroke_emit(c, srun, d_fills, d_st, d_edges);
+        if (rc) return rc;
+    }
+    if (n_ctr > 0) {
+        PolyRun pr;
+        pr.pts = reinterpret_cast<const double2 *>(dv + o_pt);
+        pr.start = reinterpret_cast<const long long *>(dv + o_cs);
+        pr.n = reinterpret_cast<const int32_t *>(dv + o_cn);
+        pr.fill = reinterpret_cast<const int32_t *>(dv + o_cf);
+        pr.edge_off = reinterpret_cast<const int32_t *>(dv + o_ce);
+        pr.n_contours = (int32_t)n_ctr;
+        pr.n_points = n_pts;
+        const int rc = poly_emit(c, pr, d_fills, d_st, d_edges);
         if (rc) return rc;
     }
     k_edge_fill<<<n_fills, 128, 0, c.stream>>>(d_st, n_fills, d_edge_fill);
     k_fill_setup<<<grid_for(n_fills, 64), 64, 0, c.stream>>>(d_fills, d_st, n_fills, d_jobs, d_cnt);
     c.timer_end(c.t_flatten, tf);
-    c.launches += 3;
+    c.launches += 4;
     Z2D_CUDA(cudaMemcpyAsync(rb, d_cnt, sizeof(int32_t) * CNT_COUNT, cudaMemcpyDeviceToHost, c.stream));
     Z2D_CUDA(cudaMemcpyAsync(rb_jobs, d_jobs, sizeof(DevJob) * (size_t)n_jobs, cudaMemcpyDeviceToHost, c.stream));
     Z2D_CUDA(cudaStreamSynchronize(c.stream));

@@ -24,6 +24,7 @@ struct FillCmd {
     int32_t fast_kind;  // FAST_* specialisation the rasteriser may use
     int32_t job;        // index of the surface (job) the fill draws on
     int32_t stroke;     // device-stroked command whose polygon this fill draws, or -1
+    int32_t poly;       // host-built polygon this fill draws, or -1
     double tol;         // max(tolerance, 0.001) (painter.zig:103)
     double scale;       // 4 for multisample / supersample, 1 for none (painter.zig:93-97)
     double edge_scale;  // multiplier of node coordinates in Polygon.addEdge: scale, or 1 for
@@ -113,7 +114,9 @@ enum : int32_t {
     CNT_MASK_LO = 2,  // + CNT_MASK_HI = 3
     CNT_EXACT = 4,
     CNT_STATUS = 5,
-    CNT_COUNT = 6
+    CNT_CURVES = 6,       // curves queued by k_node_count_w
+    CNT_CURVES_EMIT = 7,  // curves queued by k_node_emit_w
+    CNT_COUNT = 8
 };
 
 // action-mask byte of the exact path: bit 7 = clear first, bits 0-4 = coverage
@@ -137,15 +140,12 @@ struct DevJob {
 // independent).  `fills` hold the prepared commands grouped by job (node
 // offsets into `nodes`, host memory); grad_of_fill[i] >= 0 names the
 // gradient of fill i in `grads`.
-// The node array is nodes[0, n_first) followed by nodes2[0, n_second)
-// (node_fill covers both).
 // Nodes that no fill owns (node_fill -1) are skipped; device-stroked
 // commands (`strokes`, fills with stroke >= 0) read their nodes from the
-// same array.
+// same array; fills with poly >= 0 draw a host-built polygon of `strokes`.
 struct StrokeSet;
-int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n_first, std::vector<FillCmd> &fills,
+int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n_nodes, std::vector<FillCmd> &fills,
              const std::vector<int32_t> &node_fill, const std::vector<DevGradient> &grads,
-             const std::vector<int32_t> &grad_of_fill, const z2d_node *nodes2 = nullptr, int32_t n_second = 0,
-             const StrokeSet *strokes = nullptr);
+             const std::vector<int32_t> &grad_of_fill, const StrokeSet *strokes = nullptr);
 
 }  // namespace z2dg

@@ -267,23 +267,22 @@ struct Common {
     const Options &o;
     Tf ctm;
     Pen pen;
-    std::vector<std::vector<double>> &result;
+    Polygon &result;
     int error = 0;
 
-    Common(const Options &opts, std::vector<std::vector<double>> &res) : o(opts), result(res) {
+    Common(const Options &opts, Polygon &res) : o(opts), result(res) {
         ctm = Tf{o.ctm[0], o.ctm[1], o.ctm[2], o.ctm[3], o.ctm[4], o.ctm[5]};
         if (o.join == kJoinRound || o.cap == kCapRound) pen = make_pen(o.thickness, o.tolerance, ctm);
     }
 
     // Polygon.addEdgesFromContour: the contour's points, closed later
     void emit(const Contour &c) {
-        std::vector<double> pts;
-        pts.reserve(c.pts.size() * 2);
+        if (c.pts.size() == 0) return;
         c.pts.for_each([&](Pt p) {
-            pts.push_back(p.x);
-            pts.push_back(p.y);
+            result.xy.push_back(p.x);
+            result.xy.push_back(p.y);
         });
-        result.push_back(std::move(pts));
+        result.ends.push_back(result.points());
     }
 
     // join (stroke_plotter.zig:405-545)
@@ -503,7 +502,7 @@ struct SolidPlotter : Common {
     PointBuffer points;
     Side sd;
 
-    SolidPlotter(const Options &opts, std::vector<std::vector<double>> &res) : Common(opts, res) {
+    SolidPlotter(const Options &opts, Polygon &res) : Common(opts, res) {
         sd.set_scale(opts.scale);
     }
 
@@ -573,7 +572,7 @@ struct DashedPlotter : Common {
     Side init_side;
     Slope init_slope{0, 0};
 
-    DashedPlotter(const Options &opts, std::vector<std::vector<double>> &res) : Common(opts, res) {
+    DashedPlotter(const Options &opts, Polygon &res) : Common(opts, res) {
         sd.set_scale(opts.scale);
         init_side.set_scale(opts.scale);
         dasher.init(opts.dashes, opts.n_dashes, opts.dash_offset);
@@ -764,7 +763,7 @@ bool transformation_invertible(const double m[6]) {
 
 bool dashed(const Options &opts) { return opts.n_dashes > 0 && dashes_valid(opts.dashes, opts.n_dashes); }
 
-int plot(const z2d_node *nodes, size_t n_nodes, const Options &opts, std::vector<std::vector<double>> &contours) {
+int plot(const z2d_node *nodes, size_t n_nodes, const Options &opts, Polygon &contours) {
     contours.clear();
     t_arena.clear();
     if (dashed(opts)) {  // stroke_plotter.plot (stroke_plotter.zig:40-44)

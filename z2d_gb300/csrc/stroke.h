@@ -41,10 +41,23 @@ void pen_trig(int32_t n, bool reflect, double *out);
 // Transformation.inverse succeeds (painter.zig:231).
 bool transformation_invertible(const double m[6]);
 
-// stroke_plotter.plot: the closed contours (x, y pairs, already multiplied
-// by opts.scale) whose edges form the stroke polygon, in the order z2d adds
-// them.  Returns Z2D_OK or an error code.
-int plot(const z2d_node *nodes, size_t n_nodes, const Options &opts, std::vector<std::vector<double>> &contours);
+// A polygon as closed contours: contour k is points [ends[k-1], ends[k])
+// of xy (x, y pairs), each point joined to the next and the last to the
+// first.
+struct Polygon {
+    std::vector<double> xy;
+    std::vector<uint64_t> ends;
+    size_t points() const { return xy.size() / 2; }
+    void clear() {
+        xy.clear();
+        ends.clear();
+    }
+};
+
+// stroke_plotter.plot: the closed contours (points already multiplied by
+// opts.scale) whose edges form the stroke polygon, in the order z2d adds
+// them; empty contours are left out.  Returns Z2D_OK or an error code.
+int plot(const z2d_node *nodes, size_t n_nodes, const Options &opts, Polygon &out);
 
 }  // namespace stroke
 }  // namespace z2dg

@@ -499,35 +499,50 @@ __global__ void ks_edges(const SubpathDev *__restrict__ subs, const StrokeDev *_
             add_edge(F, out + (t.na + pos - t.b0), a.x, a.y, b.x, b.y, et, eb, el, er, any);
         }
     }
-    // extents: one set of atomics per warp when the warp draws one fill
+    merge_extents(st_fill, f, any, et, eb, el, er);
+}
+
+// Host-built polygons: each warp takes 32 consecutive points; lane k
+// finds its contour among the (at most 32) contours the chunk touches.
+__global__ void kp_edges(PolyRun run, const FillCmd *__restrict__ fills, FillState *__restrict__ st_fill,
+                         DEdge *__restrict__ edges) {
     const unsigned all = 0xffffffffu;
-    const int32_t f0 = __shfl_sync(all, f, 0);
-    const bool uniform = __all_sync(all, f == f0 || f < 0);
-    if (uniform) {
-        if (!__any_sync(all, any)) return;
-        double mt = any ? et : 1e300, mb = any ? eb : -1e300, ml = any ? el : 1e300, mr = any ? er : -1e300;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            mt = fmin(mt, __shfl_xor_sync(all, mt, o));
-            mb = fmax(mb, __shfl_xor_sync(all, mb, o));
-            ml = fmin(ml, __shfl_xor_sync(all, ml, o));
-            mr = fmax(mr, __shfl_xor_sync(all, mr, o));
+    const int lane = threadIdx.x & 31;
+    const long long n_pts = run.n_points;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long base = ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < n_pts;
+         base += warps * 32) {
+        // the contour holding `base`: the last one starting at or before it
+        int32_t c0 = 0;
+        if (lane == 0) {
+            int32_t lo = 0, hi = run.n_contours - 1;
+            while (lo < hi) {
+                const int32_t mid = (lo + hi + 1) >> 1;
+                if (run.start[mid] <= base) lo = mid;
+                else hi = mid - 1;
+            }
+            c0 = lo;
         }
-        if ((threadIdx.x & 31) == 0 && f0 >= 0) {
-            FillState &S = st_fill[f0];
-            atomicMin(&S.ext[0], dkey(mt));
-            atomicMax(&S.ext[1], dkey(mb));
-            atomicMin(&S.ext[2], dkey(ml));
-            atomicMax(&S.ext[3], dkey(mr));
-            atomicOr(&S.has_edges, 1);
+        c0 = __shfl_sync(all, c0, 0);
+        const int32_t ck = c0 + lane;
+        const long long end_k = ck < run.n_contours ? run.start[ck] + run.n[ck] : 0x7FFFFFFFFFFFFFFFll;
+        const long long pt = base + lane;
+        int32_t my = c0;
+#pragma unroll 8
+        for (int k = 0; k < 32; k++) my += __shfl_sync(all, end_k, k) <= pt ? 1 : 0;
+        int32_t f = -1;
+        double et = 0, eb = 0, el = 0, er = 0;
+        bool any = false;
+        if (pt < n_pts) {
+            const long long s0 = run.start[my];
+            const int32_t n = run.n[my];
+            f = run.fill[my];
+            const long long nx = pt + 1 == s0 + n ? s0 : pt + 1;
+            const double2 a = run.pts[pt], b = run.pts[nx];
+            add_edge(fills[f], edges + st_fill[f].edge_base + run.edge_off[my] + (pt - s0), a.x, a.y, b.x, b.y, et, eb,
+                     el, er, any);
         }
-    } else if (any) {
-        FillState &S = st_fill[f];
-        atomicMin(&S.ext[0], dkey(et));
-        atomicMax(&S.ext[1], dkey(eb));
-        atomicMin(&S.ext[2], dkey(el));
-        atomicMax(&S.ext[3], dkey(er));
-        atomicOr(&S.has_edges, 1);
+        merge_extents(st_fill, f, any, et, eb, el, er);
     }
 }
 
@@ -545,6 +560,18 @@ struct Carve {
 };
 
 }  // namespace
+
+int poly_emit(Ctx &c, const PolyRun &run, const FillCmd *d_fills, FillState *d_st, DEdge *d_edges) {
+    if (run.n_points == 0 || run.n_contours == 0) return Z2D_OK;
+    constexpr int T = 128;
+    const unsigned blocks = (unsigned)std::min<long long>(blocks_for((run.n_points + 31) / 32, T / 32),
+                                                          (long long)c.sm_count * 32);
+    cudaEvent_t ts = c.timer_begin(c.t_stroke);
+    kp_edges<<<blocks, T, 0, c.stream>>>(run, d_fills, d_st, d_edges);
+    c.timer_end(c.t_stroke, ts);
+    c.launches += 1;
+    return Z2D_OK;
+}
 
 const long long *stroke_totals_dev(const StrokeRun &run) {
     return reinterpret_cast<const State *>(run.state)->totals;

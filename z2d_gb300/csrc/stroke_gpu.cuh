@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "fill.cuh"
+#include "stroke.h"
 
 namespace z2dg {
 
@@ -45,15 +46,33 @@ struct SubpathDev {
     int32_t _pad;
 };
 
-// What the host hands over: commands, subpaths and the pens' tables.
+// What the host hands over: device-stroked commands with their subpaths and
+// the pens' tables, and polygons built on the host (dashed strokes), each
+// drawn by the fill whose `poly` names it.
 struct StrokeSet {
     std::vector<StrokeDev> strokes;
     std::vector<SubpathDev> subs;
     std::vector<double> trig;  // (cos t, sin t) pairs
     int64_t n_local = 0;       // sum of the subpaths' node counts
     int64_t n_pen = 0;         // sum of the strokes' pen vertices
-    bool empty() const { return strokes.empty(); }
+    std::vector<const stroke::Polygon *> polys;
+    bool empty() const { return strokes.empty() && polys.empty(); }
 };
+
+// The contours of the host-built polygons on the device (structure of
+// arrays over all contours, in order): contour k is points
+// [start[k], start[k] + n[k]) of the point array, drawn by fill[k], its
+// first edge at edge_off[k] within that fill's edges.
+struct PolyRun {
+    const double2 *pts = nullptr;
+    const long long *start = nullptr;
+    const int32_t *n = nullptr, *fill = nullptr, *edge_off = nullptr;
+    int32_t n_contours = 0;
+    long long n_points = 0;
+};
+// Writes the edges of every host-built polygon's contours (each point to
+// the next, the last to the first) and merges the fills' extents.
+int poly_emit(Ctx &c, const PolyRun &run, const FillCmd *d_fills, FillState *d_st, DEdge *d_edges);
 
 // Device side of a StrokeSet during one run_jobs call.
 struct StrokeRun {
