@@ -275,8 +275,9 @@ Z2D_API uint64_t z2dgpu_ctx_launch_count(const z2dgpu_ctx *ctx);
 Z2D_API int z2dgpu_ctx_set_timing(z2dgpu_ctx *ctx, int enable);
 /* Accumulated milliseconds and launch count of a stage since timing was
  * enabled: "raster" (k_raster), "composite" (compositor kernels), "flatten"
- * (path flattening and fill setup, two intervals per fill call) or "bins"
- * (edge binning, band lists and the exact path).  Returns -1 for an unknown
+ * (path flattening, stroking and fill setup, two intervals per fill call),
+ * "stroke" (the stroke kernels, a share of "flatten") or "bins" (edge
+ * binning, band lists and the exact path).  Returns -1 for an unknown
  * name. */
 Z2D_API double z2dgpu_ctx_kernel_ms(z2dgpu_ctx *ctx, const char *kernel, uint64_t *launches);
 
@@ -298,13 +299,14 @@ Z2D_API int z2dgpu_fill_batch(z2dgpu_ctx *ctx, z2d_surface *surface,
                               const z2d_node *nodes, size_t n_nodes,
                               const z2d_fill_cmd *cmds, size_t n_cmds);
 
-/* painter.stroke (src/painter.zig:214-344): the stroke polygon is built on
- * the host exactly as z2d's stroke plotter builds it (joins, caps, pens)
- * and filled with the non-zero rule by the GPU rasterisers (dashes
- * included).  Hairline mode returns Z2D_ERR_INVALID_ARGUMENT (not supported
- * yet); a
- * transformation that cannot be inverted also returns
- * Z2D_ERR_INVALID_ARGUMENT (Transformation.Error.InvalidMatrix). */
+/* painter.stroke (src/painter.zig:214-344): the stroke polygon z2d's stroke
+ * plotter builds (joins, caps, pens, dashes), filled with the non-zero rule
+ * by the GPU rasterisers.  Solid strokes are tessellated on the device;
+ * dashed ones on the host.  Hairline mode returns Z2D_ERR_INVALID_ARGUMENT
+ * (not supported yet); a transformation that cannot be inverted also
+ * returns Z2D_ERR_INVALID_ARGUMENT (Transformation.Error.InvalidMatrix); a
+ * line_to / curve_to without a current point or a non-finite coordinate
+ * returns Z2D_ERR_INVALID_STATE. */
 Z2D_API int z2dgpu_stroke(z2dgpu_ctx *ctx, z2d_surface *surface,
                           const z2d_pattern *pattern, const z2d_node *nodes,
                           size_t n_nodes, const z2d_stroke_opts *opts);
