@@ -51,6 +51,10 @@ def load_oracle():
                                                     C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.c_size_t,
                                                     C.POINTER(abi.z2d_fill_opts)]
             lib.z2doracle_fill_contours.restype = C.c_int
+            lib.z2doracle_hairline.argtypes = [C.POINTER(abi.z2d_surface), C.POINTER(abi.z2d_pattern),
+                                               C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.c_size_t, C.c_int32,
+                                               C.c_int32, C.c_int32]
+            lib.z2doracle_hairline.restype = C.c_int
             lib.z2doracle_composite.argtypes = [C.POINTER(abi.z2d_surface), C.c_int32, C.c_int32, C.c_int32,
                                                 C.POINTER(abi.z2d_operation), C.c_int32]
             lib.z2doracle_composite.restype = C.c_int
@@ -108,6 +112,24 @@ class Oracle:
         return self.lib.z2doracle_fill_contours(C.byref(s), C.byref(p), pts.ctypes.data_as(C.POINTER(C.c_double)),
                                                 ends.ctypes.data_as(C.POINTER(C.c_uint64)), len(contours),
                                                 C.byref(opts.to_abi()))
+
+    def hairline(self, surface, pattern: Pattern, polylines, operator: str = "src_over", precision: str = "integer",
+                 anti_aliasing: str = "default") -> int:
+        """The hairline rasteriser on polylines (a list of (n, 2) arrays)."""
+        import numpy as np
+        keep: list = []
+        s = _host_abi(surface)
+        p = pattern.to_abi(keep)
+        pts = np.ascontiguousarray(np.concatenate([np.asarray(c, np.float64).reshape(-1, 2) for c in polylines])
+                                   if polylines else np.zeros((1, 2)), dtype=np.float64)
+        ends = np.cumsum([len(c) for c in polylines]).astype(np.uint64) if polylines else np.zeros(1, np.uint64)
+        return self.lib.z2doracle_hairline(C.byref(s), C.byref(p), pts.ctypes.data_as(C.POINTER(C.c_double)),
+                                           ends.ctypes.data_as(C.POINTER(C.c_uint64)), len(polylines),
+                                           abi.OP[operator],
+                                           {"integer": abi.PRECISION_INTEGER, "float": abi.PRECISION_FLOAT}[precision],
+                                           {"none": abi.AA_NONE, "default": abi.AA_DEFAULT,
+                                            "multisample_4x": abi.AA_MULTISAMPLE_4X,
+                                            "supersample_4x": abi.AA_SUPERSAMPLE_4X}[anti_aliasing])
 
     def composite(self, dst, dst_x: int, dst_y: int, ops, precision: str = "integer") -> int:
         keep: list = []

@@ -1830,6 +1830,155 @@ __attribute__((visibility("default"))) z2d_pixel z2doracle_gradient_pixel(const 
     return z2d_pixel{Z2D_FORMAT_RGBA, (uint8_t)v.r, (uint8_t)v.g, (uint8_t)v.b, (uint8_t)v.a};
 }
 
+// ===================================================================
+// Hairlines                         src/internal/raster/hairline.zig
+// ===================================================================
+struct Hair {
+    Sfc &s;
+    const FillSrc &pat;
+    int op, prec;
+    bool aa_none;
+};
+static void hair_opaque(Hair &h, int32_t x, int32_t y, size_t len) { composite_opaque(h.op, h.s, h.pat, x, y, len, h.prec); }
+static void hair_opacity(Hair &h, int32_t x, int32_t y, uint8_t o) {
+    composite_opacity(h.op, h.s, h.pat, x, y, 1, h.prec, o);
+}
+static void delta_step(int32_t a, int32_t b, int32_t &d, int32_t &st) {  // hairline.zig:373-379
+    const int32_t c = b - a;
+    if (c < 0) {
+        d = -c;
+        st = -1;
+    } else {
+        d = c;
+        st = 1;
+    }
+}
+static uint16_t err_inc(int32_t a, int32_t b) {  // hairline.zig:386-394
+    if (a == b) return 0xFFFF;
+    return (uint16_t)(((uint32_t)a << 16) / (uint32_t)b);
+}
+static void draw_horizontal(Hair &h, int32_t x0, int32_t x1, int32_t y) {  // hairline.zig:126-142
+    const int32_t sx = clampi(std::min(x0, x1), 0, h.s.w - 1), ex = clampi(std::max(x0, x1), 0, h.s.w - 1);
+    const int32_t len = ex - sx + 1;
+    if (len > 0) hair_opaque(h, sx, y, (size_t)len);
+}
+static void draw_vertical(Hair &h, int32_t x, int32_t y0, int32_t y1) {  // hairline.zig:144-161
+    const int32_t sy = clampi(std::min(y0, y1), 0, h.s.h - 1), ey = clampi(std::max(y0, y1), 0, h.s.h - 1);
+    for (int32_t y = sy; y <= ey; y++) hair_opaque(h, x, y, 1);
+}
+static void draw_bres_horizontal(Hair &h, int32_t x0, int32_t y0, int32_t x1, int32_t y1) {  // hairline.zig:163-199
+    if (x0 > x1) return draw_bres_horizontal(h, x1, y1, x0, y0);
+    const int32_t dx = x1 - x0;
+    int32_t dy, sy;
+    delta_step(y0, y1, dy, sy);
+    int32_t x = x0, y = y0, d = 2 * dy - dx;
+    const int32_t d_inc = 2 * dy, d_dec = 2 * dx;
+    for (; x <= x1; x++) {
+        hair_opaque(h, x, y, 1);
+        if (d > 0) {
+            y += sy;
+            d -= d_dec;
+        }
+        d += d_inc;
+    }
+}
+static void draw_bres_vertical(Hair &h, int32_t x0, int32_t y0, int32_t x1, int32_t y1) {  // hairline.zig:201-231
+    if (y0 > y1) return draw_bres_vertical(h, x1, y1, x0, y0);
+    const int32_t dy = y1 - y0;
+    int32_t dx, sx;
+    delta_step(x0, x1, dx, sx);
+    int32_t x = x0, y = y0, d = 2 * dx - dy;
+    const int32_t d_inc = 2 * dx, d_dec = 2 * dy;
+    for (; y <= y1; y++) {
+        hair_opaque(h, x, y, 1);
+        if (d > 0) {
+            x += sx;
+            d -= d_dec;
+        }
+        d += d_inc;
+    }
+}
+static void draw_wu_horizontal(Hair &h, int32_t x0, int32_t y0, int32_t x1, int32_t y1) {  // hairline.zig:233-309
+    if (x0 > x1) return draw_wu_horizontal(h, x1, y1, x0, y0);
+    const int32_t dx = x1 - x0;
+    int32_t dy, sy;
+    delta_step(y0, y1, dy, sy);
+    int32_t x = x0, y = y0;
+    uint16_t err = 0;
+    const uint16_t inc = err_inc(dy, dx);
+    hair_opaque(h, x, y, 1);
+    for (x += 1; x < x1; x++) {
+        const uint16_t prev = err;
+        err = (uint16_t)(err + inc);
+        if (err < prev) y += sy;  // overflow
+        const uint8_t comp = (uint8_t)(err >> 8);
+        hair_opacity(h, x, y, (uint8_t)(comp ^ 0xFF));
+        hair_opacity(h, x, y + sy, comp);
+    }
+    hair_opaque(h, x1, y1, 1);
+}
+static void draw_wu_vertical(Hair &h, int32_t x0, int32_t y0, int32_t x1, int32_t y1) {  // hairline.zig:311-365
+    if (y0 > y1) return draw_wu_vertical(h, x1, y1, x0, y0);
+    const int32_t dy = y1 - y0;
+    int32_t dx, sx;
+    delta_step(x0, x1, dx, sx);
+    int32_t x = x0, y = y0;
+    uint16_t err = 0;
+    const uint16_t inc = err_inc(dx, dy);
+    hair_opaque(h, x, y, 1);
+    for (y += 1; y < y1; y++) {
+        const uint16_t prev = err;
+        err = (uint16_t)(err + inc);
+        if (err < prev) x += sx;
+        const uint8_t comp = (uint8_t)(err >> 8);
+        hair_opacity(h, x, y, (uint8_t)(comp ^ 0xFF));
+        hair_opacity(h, x + sx, y, comp);
+    }
+    hair_opaque(h, x1, y1, 1);
+}
+static void draw_line(Hair &h, int32_t x0, int32_t y0, int32_t x1, int32_t y1) {  // hairline.zig:89-124
+    // inBox (hairline.zig:396-406)
+    if ((x0 < 0 || x0 >= h.s.w) && (x1 < 0 || x1 >= h.s.w)) return;
+    if ((y0 < 0 || y0 >= h.s.h) && (y1 < 0 || y1 >= h.s.h)) return;
+    const int32_t dx = std::abs(x1 - x0), dy = std::abs(y1 - y0);
+    if (dx == 0) draw_vertical(h, x0, y0, y1);
+    else if (dy == 0) draw_horizontal(h, x0, x1, y0);
+    else if (dx < dy) h.aa_none ? draw_bres_vertical(h, x0, y0, x1, y1) : draw_wu_vertical(h, x0, y0, x1, y1);
+    else h.aa_none ? draw_bres_horizontal(h, x0, y0, x1, y1) : draw_wu_horizontal(h, x0, y0, x1, y1);
+}
+
+// hairline_rasterizer.run (hairline.zig:29-81) on polylines given as points
+// (polyline_plotter's contours): line_ends[k] is one past polyline k's last
+// point.  `anti_aliasing` is the stroke's own option (Bresenham for none,
+// Wu otherwise).
+__attribute__((visibility("default"))) int z2doracle_hairline(z2d_surface *surface, const z2d_pattern *pattern,
+                                                              const double *points, const uint64_t *line_ends,
+                                                              size_t n_lines, int32_t op, int32_t precision,
+                                                              int32_t anti_aliasing) {
+    if (!surface || !pattern || (n_lines && (!points || !line_ends))) return Z2D_ERR_INVALID_ARGUMENT;
+    if (surface->width < 1 || surface->height < 1) return Z2D_ERR_INVALID_DIMENSIONS;
+    if (pattern->kind == Z2D_PATTERN_PIXEL && !pixel_premultiplied(pattern->pixel))
+        return Z2D_ERR_PIXEL_NOT_PREMULTIPLIED;
+    Sfc s = sfc_from_abi(surface);
+    FillSrc pat;
+    pat.kind = pattern->kind;
+    const int pk = pattern->kind == Z2D_PATTERN_PIXEL      ? Z2D_PARAM_PIXEL
+                   : pattern->kind == Z2D_PATTERN_GRADIENT ? Z2D_PARAM_GRADIENT
+                                                           : Z2D_PARAM_DITHER;
+    pat.src = make_src_from_pattern(pk, *pattern);
+    Hair h{s, pat, op, requires_float(op) ? Z2D_PRECISION_FLOAT : precision, anti_aliasing == Z2D_AA_NONE};
+    uint64_t start = 0;
+    for (size_t k = 0; k < n_lines; k++) {
+        const uint64_t end = line_ends[k];
+        auto X = [&](uint64_t i) { return (int32_t)std::round(points[2 * i]); };
+        auto Y = [&](uint64_t i) { return (int32_t)std::round(points[2 * i + 1]); };
+        if (end == start + 1) hair_opaque(h, X(start), Y(start), 1);
+        for (uint64_t i = start; end > start + 1 && i + 1 < end; i++) draw_line(h, X(i), Y(i), X(i + 1), Y(i + 1));
+        start = end;
+    }
+    return Z2D_OK;
+}
+
 // The rasterisers of painter.fill / painter.stroke on a polygon given as
 // closed contours of already-scaled points (Polygon.addEdgesFromContour,
 // Polygon.zig:115-139, with the polygon's own scale of 1), as

@@ -57,6 +57,8 @@ class StrokeOracle:
             contours, _ = painter.stroke_contours(nodes, opts, surface.format)
         except Z2DError as e:
             return e.code
+        if opts.hairline:  # polylines of polyline_plotter, drawn by the hairline rasteriser
+            return self.oracle.hairline(surface, pattern, contours, opts.operator, opts.precision, opts.anti_aliasing)
         aa = "none" if surface.format == abi.FORMAT_ALPHA1 else opts.anti_aliasing
         fo = FillOptions(anti_aliasing=aa, fill_rule="non_zero", operator=opts.operator, precision=opts.precision)
         return self.oracle.fill_contours(surface, pattern, contours, fo)

@@ -698,6 +698,30 @@ def s057_stroke_bezier_dashed(be, aa):
     return s
 
 
+_HAIRLINE_CLIP_CASES = [  # (x0, y0, x1, y1) on a 100x100 canvas
+    (-25, 50, 75, 60), (25, 50, 125, 60), (-25, 50, 75, 50), (25, 50, 125, 50),
+    (25, -50, 75, 50), (25, 50, 75, 150), (-25, -50, -75, -150), (125, 150, 175, 250),
+    (50, -25, 60, 75), (50, 25, 60, 125), (50, -25, 50, 75), (50, 25, 50, 125),
+    (-50, 25, 50, 75), (50, 25, 150, 75), (-50, -25, -150, -75), (150, 125, 250, 175),
+]
+
+
+def s082_stroke_hairline_clip(be, aa):
+    from z2d_gb300.types import StrokeOptions
+    s = Surface.init("rgb", 200, len(_HAIRLINE_CLIP_CASES) // 2 * 100)
+    for idx, (x0, y0, x1, y1) in enumerate(_HAIRLINE_CLIP_CASES):
+        on = 0x20 * (((idx // 2) & 1) ^ (idx % 2))
+        src = Surface.init_pixel(Pixel.rgb(on, on, on), 100, 100)
+        p = Path()
+        p.move_to(x0, y0)
+        p.line_to(x1, y1)
+        rc = be.stroke(src, Pattern.from_pixel(_white_rgb()), p.nodes, StrokeOptions(anti_aliasing=aa, hairline=True))
+        assert rc == abi.OK
+        rc = be.composite(s, idx % 2 * 100, idx // 2 * 100, [Operation("src", src=src)])
+        assert rc == abi.OK
+    return s
+
+
 STROKE_SCENES = {
     "008_stroke_triangle": s008_stroke_triangle,
     "009_stroke_square": s009_stroke_square,
@@ -716,6 +740,7 @@ STROKE_SCENES = {
     "055_stroke_miter_dashed": s055_stroke_miter_dashed,
     "056_stroke_star_dashed": s056_stroke_star_dashed,
     "057_stroke_bezier_dashed": s057_stroke_bezier_dashed,
+    "082_stroke_hairline_clip": s082_stroke_hairline_clip,
 }
 
 FILL_SCENES = {

@@ -204,7 +204,7 @@ def test_stroke_errors(gpu):
     assert gpu.stroke(s, px, nodes, StrokeOptions(transformation=(1, 2, 2, 4, 0, 0))) == abi.ERR_INVALID_ARGUMENT
     assert gpu.stroke(s, Pattern.from_pixel(Pixel.rgba(200, 2, 3, 4)), nodes,
                       StrokeOptions()) == abi.ERR_PIXEL_NOT_PREMULTIPLIED
-    assert gpu.stroke(s, px, nodes, StrokeOptions(hairline=True)) == abi.ERR_INVALID_ARGUMENT
+    assert gpu.stroke(s, px, nodes, StrokeOptions(hairline=True)) == abi.OK
     assert gpu.stroke(s, px, [], StrokeOptions()) == abi.OK
     assert gpu.stroke(s, px, nodes, StrokeOptions(dashes=(0.0, 0.0))) == abi.OK  # invalid dashes: solid stroke
 
@@ -257,6 +257,107 @@ def test_draw_jobs_mixed(oracle):
                                    dashes=(6.0, 3.0) if (k + j) % 4 == 0 else (),
                                    anti_aliasing=("default", "none", "supersample_4x")[j % 3])
                 ops.append(("stroke", Pattern.from_pixel(random_premultiplied_pixel(rng)), sn, st))
+        for kind, pat, nodes, o in ops:
+            rc = oracle.fill(ref, pat, nodes, o) if kind == "fill" else so.stroke(ref, pat, nodes, o)
+            assert rc == abi.OK
+        jobs.append((dev, ops))
+        refs.append(ref)
+    painter.draw_jobs(jobs)
+    torch.cuda.synchronize()
+    for j, ((dev, _), ref) in enumerate(zip(jobs, refs)):
+        _cmp(dev.to_host(), ref, 0, f"job {j}")
+
+
+def _hairline_path(rng, w, h):
+    """Polylines that cross themselves and leave the surface: lines, curves,
+    lone points, closed and open subpaths."""
+    nodes = []
+    for _ in range(int(rng.integers(1, 4))):
+        nodes.append((abi.MOVE_TO, *rng.uniform([-20, -20], [w + 20, h + 20]), 0, 0, 0, 0))
+        if rng.random() < 0.15:  # a lone point
+            nodes.append((abi.CLOSE_PATH, 0, 0, 0, 0, 0, 0))
+            continue
+        for _ in range(int(rng.integers(1, 7))):
+            if rng.random() < 0.7:
+                nodes.append((abi.LINE_TO, *rng.uniform([-20, -20], [w + 20, h + 20]), 0, 0, 0, 0))
+            else:
+                nodes.append((abi.CURVE_TO, *rng.uniform([-20, -20] * 3, [w + 20, h + 20] * 3)))
+        if rng.random() < 0.5:
+            nodes.append((abi.CLOSE_PATH, 0, 0, 0, 0, 0, 0))
+    return nodes
+
+
+@pytest.mark.parametrize("aa", ["none", "default"])
+@pytest.mark.parametrize("fmt", ["rgba", "rgb", "alpha8", "alpha4", "alpha1"])
+def test_hairlines(gpu, oracle, fmt, aa):
+    """Hairline strokes (Bresenham / Wu segments composited pixel by pixel
+    in path order) against the oracle's hairline rasteriser."""
+    rng = np.random.default_rng(len(fmt) * 7 + (aa == "none"))
+    w, h = 120, 90
+    a, b = _bg(fmt, w, h, 21), _bg(fmt, w, h, 21)
+    so = StrokeOracle(oracle)
+    g = Gradient.linear(0, 0, w, h)
+    g.add_stop(0.0, Color.rgb(1, 0.2, 0, 0.9))
+    g.add_stop(1.0, Color.rgb(0, 0.3, 1, 0.6))
+    for i in range(8):
+        nodes = _hairline_path(rng, w, h)
+        op = ("src_over", "src", "xor", "plus", "src_in", "clear", "color_burn", "multiply")[i]
+        opts = StrokeOptions(hairline=True, anti_aliasing=aa, operator=op,
+                             dashes=(7.0, 3.0) if i % 3 == 2 else (), dash_offset=1.5,
+                             precision="float" if i == 7 else "integer", tolerance=(0.1, 0.5)[i % 2])
+        pat = Pattern.from_gradient(g) if i % 4 == 1 else Pattern.from_pixel(random_premultiplied_pixel(rng))
+        assert gpu.stroke(a, pat, nodes, opts) == abi.OK
+        assert so.stroke(b, pat, nodes, opts) == abi.OK
+    _cmp(a, b, FLOAT_TOL, f"{fmt}/{aa}")
+
+
+def test_hairline_star_overdraw(gpu, oracle):
+    """Segments crossing many times at one pixel with a translucent source:
+    the composites must apply in path order."""
+    s_gpu, s_ref = _bg("rgba", 64, 64, 3), _bg("rgba", 64, 64, 3)
+    nodes = [(abi.MOVE_TO, 32, 2, 0, 0, 0, 0)]
+    for k in range(1, 40):
+        t = k * 2.513
+        nodes.append((abi.LINE_TO, 32 + 30 * math.sin(t), 32 - 30 * math.cos(t), 0, 0, 0, 0))
+    nodes.append((abi.CLOSE_PATH, 0, 0, 0, 0, 0, 0))
+    pat = Pattern.from_pixel(Pixel.rgba(40, 20, 10, 90))
+    so = StrokeOracle(oracle)
+    for aa in ("none", "default"):
+        opts = StrokeOptions(hairline=True, anti_aliasing=aa, operator="src_over")
+        assert gpu.stroke(s_gpu, pat, nodes, opts) == abi.OK
+        assert so.stroke(s_ref, pat, nodes, opts) == abi.OK
+    _cmp(s_gpu, s_ref, 0, "star")
+
+
+def test_draw_jobs_with_hairlines(oracle):
+    """Hairlines interleaved with fills and strokes on many surfaces keep
+    each surface's call order."""
+    torch = pytest.importorskip("torch")
+    from z2d_gb300 import painter
+    from z2d_gb300.workloads import random_fills
+    so = StrokeOracle(oracle)
+    rng = np.random.default_rng(321)
+    jobs, refs = [], []
+    for j in range(12):
+        w, h = int(rng.integers(20, 150)), int(rng.integers(20, 120))
+        fmt = ("rgba", "rgb", "alpha8")[j % 3]
+        dev = _bg(fmt, w, h, 700 + j).to_device("cuda")
+        ref = _bg(fmt, w, h, 700 + j)
+        ops = []
+        fills = random_fills(seed=1300 + j, n=int(rng.integers(1, 5)), w=w, h=h, side_lo=2,
+                             side_hi=max(3, min(w, h)), seg_lo=3, seg_hi=8)
+        for k, (pat, nodes, fo) in enumerate(fills):
+            ops.append(("fill", pat, nodes, fo))
+            if (k + j) % 2 == 0:
+                ops.append(("stroke", Pattern.from_pixel(random_premultiplied_pixel(rng)), _hairline_path(rng, w, h),
+                            StrokeOptions(hairline=True, anti_aliasing=("none", "default")[k % 2])))
+            if k % 3 == 1:
+                ops.append(("stroke", Pattern.from_pixel(random_premultiplied_pixel(rng)),
+                            _open_path(rng, w, h, 3), StrokeOptions(line_width=3.0)))
+        if j % 4 == 0:  # consecutive hairlines at the end
+            for _ in range(2):
+                ops.append(("stroke", Pattern.from_pixel(random_premultiplied_pixel(rng)), _hairline_path(rng, w, h),
+                            StrokeOptions(hairline=True)))
         for kind, pat, nodes, o in ops:
             rc = oracle.fill(ref, pat, nodes, o) if kind == "fill" else so.stroke(ref, pat, nodes, o)
             assert rc == abi.OK

@@ -19,8 +19,8 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 OUT_DIR = PKG / "_lib"
 LIB = OUT_DIR / "libz2dgpu.so"
-SOURCES = ["capi.cu", "composite.cu", "composite_mask.cu", "fill.cu", "server.cu", "stroke.cpp", "stroke_gpu.cu"]
-HEADERS = ["z2d_pixel.cuh", "z2d_internal.h", "fill.cuh", "stroke.h", "stroke_geom.h", "stroke_gpu.cuh", "edges.cuh", "spline.cuh", "blue_noise_64x64.inc"]
+SOURCES = ["capi.cu", "composite.cu", "composite_mask.cu", "fill.cu", "server.cu", "stroke.cpp", "stroke_gpu.cu", "hairline.cu"]
+HEADERS = ["z2d_pixel.cuh", "z2d_internal.h", "fill.cuh", "stroke.h", "stroke_geom.h", "stroke_gpu.cuh", "edges.cuh", "spline.cuh", "raster_px.cuh", "blue_noise_64x64.inc"]
 ARCH = os.environ.get("Z2D_GPU_ARCH", "103a")
 
 

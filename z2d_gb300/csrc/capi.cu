@@ -563,10 +563,6 @@ static int stroke_options(const z2d_stroke_opts &o, int32_t surface_format, int 
 // The checks of a non-empty stroke's path and dashes.
 static int stroke_checks(const z2d_node *nodes, size_t n_nodes, const z2d_stroke_opts &o) {
     if (!nodes) return Z2D_ERR_INVALID_ARGUMENT;
-    if (o.hairline) {
-        set_error("hairline strokes are not supported on the GPU path yet");
-        return Z2D_ERR_INVALID_ARGUMENT;
-    }
     for (uint64_t i = 0; i < o.n_dashes; i++)
         if (!(o.dashes[i] == o.dashes[i]) || !(o.dash_offset == o.dash_offset)) {
             set_error("stroke dashes must be numbers");
@@ -590,7 +586,13 @@ static int stroke_polygon(const z2d_node *nodes, size_t n_nodes, const z2d_strok
     if (n_nodes == 0) return Z2D_OK;
     rc = stroke_checks(nodes, n_nodes, o);
     if (rc) return rc;
-    rc = stroke::plot(nodes, n_nodes, so, contours);
+    if (o.hairline) {  // the polylines of polyline_plotter, unscaled
+        so.tolerance = o.tolerance;
+        scale = 1.0;
+        rc = stroke::polyline(nodes, n_nodes, so, contours);
+    } else {
+        rc = stroke::plot(nodes, n_nodes, so, contours);
+    }
     if (rc) set_error("InvalidState: stroke path node sequence");
     return rc;
 }
@@ -686,30 +688,19 @@ static int prepare_polygon_fill(const z2d_surface &s, int32_t job, const z2d_pat
 // built on host threads (each command independently) and uploaded as
 // their polygons' points (already scaled); fills use the caller's nodes.
 // The caller's node array is uploaded as it is.
-static int draw_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_node *nodes, size_t n_nodes,
+// draw_jobs without hairline commands (the caller has checked the
+// arguments and the command kinds).
+static int draw_core(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_node *nodes, size_t n_nodes,
                      const z2d_draw_cmd *cmds, size_t n_cmds) {
-    if ((n_jobs > 0 && !jobs_in) || (n_cmds > 0 && !cmds) || (n_nodes > 0 && !nodes)) return Z2D_ERR_INVALID_ARGUMENT;
-    if (n_jobs > 0x7FFFFFF || n_cmds > 0x7FFFFFF || n_nodes > 0x7FFFFFFF) {
-        set_error("batch too large");
-        return Z2D_ERR_INVALID_ARGUMENT;
-    }
     std::vector<size_t> strokes;
-    for (size_t i = 0; i < n_cmds; i++) {
-        if (cmds[i].kind == Z2D_DRAW_STROKE) strokes.push_back(i);
-        else if (cmds[i].kind != Z2D_DRAW_FILL) {
-            set_error("draw command: bad kind");
-            return Z2D_ERR_INVALID_ARGUMENT;
-        }
-    }
     // the surface format decides the stroke's anti-aliasing (alpha1: none)
     std::vector<int32_t> cmd_fmt(n_cmds, Z2D_FORMAT_RGBA);
     for (size_t j = 0; j < n_jobs; j++) {
         const z2d_job &jb = jobs_in[j];
-        if (jb.cmd_offset > n_cmds || jb.n_cmds > n_cmds - jb.cmd_offset) {
-            set_error("draw_jobs: job commands outside the command array");
-            return Z2D_ERR_INVALID_ARGUMENT;
+        for (uint64_t k = 0; k < jb.n_cmds; k++) {
+            cmd_fmt[jb.cmd_offset + k] = jb.surface.format;
+            if (cmds[jb.cmd_offset + k].kind == Z2D_DRAW_STROKE) strokes.push_back(jb.cmd_offset + k);
         }
-        for (uint64_t k = 0; k < jb.n_cmds; k++) cmd_fmt[jb.cmd_offset + k] = jb.surface.format;
     }
     // per stroke: options, then the device stroker's input (solid) or the
     // host-built polygon (dashed), in parallel
@@ -861,6 +852,154 @@ static int draw_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_no
     }
     if (fills.empty()) return Z2D_OK;
     return run_jobs(c, jobs, nodes, (int32_t)n_nodes, fills, node_fill, grads, grad_of_fill, &sset);
+}
+
+static bool is_hairline(const z2d_draw_cmd &cm) { return cm.kind == Z2D_DRAW_STROKE && cm.stroke.hairline != 0; }
+
+// Hairline strokes: for every job, the hairline commands
+// [ranges[j].first, ranges[j].second) of its command list, in order
+// (painter.zig:245-262).  The polylines are built on host threads.
+static int draw_hairlines(Ctx &c, const z2d_job *jobs_in, size_t n_jobs,
+                          const std::vector<std::pair<uint64_t, uint64_t>> &ranges, const z2d_node *nodes,
+                          size_t n_nodes, const z2d_draw_cmd *cmds) {
+    std::vector<size_t> hc;   // command index
+    std::vector<int32_t> hj;  // its job
+    for (size_t j = 0; j < n_jobs; j++)
+        for (uint64_t k = ranges[j].first; k < ranges[j].second; k++) {
+            hc.push_back(jobs_in[j].cmd_offset + k);
+            hj.push_back((int32_t)j);
+        }
+    const size_t nh = hc.size();
+    if (nh == 0) return Z2D_OK;
+    std::vector<stroke::Polygon> lines(nh);
+    std::vector<int> rcs(nh, 0);
+    std::vector<std::string> errs(nh);
+    {
+        const size_t nt = std::max<size_t>(1, std::min<size_t>(std::thread::hardware_concurrency(), nh / 256 + 1));
+        std::atomic<size_t> next{0};
+        auto work = [&] {
+            for (size_t k; (k = next.fetch_add(1)) < nh;) {
+                const z2d_draw_cmd &cm = cmds[hc[k]];
+                if (!cm.pattern || cm.node_offset > n_nodes || cm.n_nodes > n_nodes - cm.node_offset) {
+                    rcs[k] = Z2D_ERR_INVALID_ARGUMENT;
+                    errs[k] = "stroke command outside the node array";
+                    continue;
+                }
+                const z2d_node *nd = nodes + cm.node_offset;
+                int aa = 0;
+                stroke::Options so;
+                int rc = stroke_options(cm.stroke, jobs_in[hj[k]].surface.format, aa, so);
+                if (!rc && cm.n_nodes > 0) rc = stroke_checks(nd, cm.n_nodes, cm.stroke);
+                if (!rc && cm.n_nodes > 0) {
+                    so.tolerance = cm.stroke.tolerance;  // the polyline plotter takes it as given
+                    rc = stroke::polyline(nd, cm.n_nodes, so, lines[k]);
+                    if (rc) set_error("InvalidState: stroke path node sequence");
+                    for (double v : lines[k].xy)
+                        if (!rc && !(std::fabs(v) < 1073741824.0)) {
+                            set_error("InvalidState: hairline coordinate out of range");
+                            rc = Z2D_ERR_INVALID_STATE;
+                        }
+                }
+                rcs[k] = rc;
+                if (rc) errs[k] = last_error();
+            }
+        };
+        std::vector<std::thread> pool;
+        for (size_t t = 1; t < nt; t++) pool.emplace_back(work);
+        work();
+        for (auto &t : pool) t.join();
+        for (size_t k = 0; k < nh; k++)
+            if (rcs[k]) {
+                set_error(errs[k].c_str());
+                return rcs[k];
+            }
+    }
+    std::vector<DevJob> jobs(n_jobs);
+    if (n_jobs > 0) memset(jobs.data(), 0, sizeof(DevJob) * n_jobs);
+    for (size_t j = 0; j < n_jobs; j++) {
+        const z2d_job &jb = jobs_in[j];
+        jobs[j].sfc = DevSurface{reinterpret_cast<uint8_t *>(jb.surface.data), jb.surface.format, jb.surface.width,
+                                 jb.surface.height};
+    }
+    std::vector<FillCmd> fills;
+    std::vector<DevGradient> grads;
+    std::vector<int32_t> grad_of_fill;
+    HairSet hs;
+    for (size_t k = 0; k < nh; k++) {
+        const z2d_draw_cmd &cm = cmds[hc[k]];
+        if (cm.pattern->kind == Z2D_PATTERN_PIXEL && !pixel_premultiplied(cm.pattern->pixel)) {
+            set_error("PixelSourceNotPreMultiplied");
+            return Z2D_ERR_PIXEL_NOT_PREMULTIPLIED;
+        }
+        if (lines[k].points() == 0) continue;
+        const int rc = prepare_polygon_fill(jobs_in[hj[k]].surface, hj[k], cm.pattern, cm.stroke.anti_aliasing,
+                                            cm.stroke.op, cm.stroke.precision, cm.stroke.tolerance, fills, grads,
+                                            grad_of_fill);
+        if (rc) return rc;
+        hs.lines.push_back(&lines[k]);
+        hs.fill.push_back((int32_t)fills.size() - 1);
+        hs.aa_none.push_back(cm.stroke.anti_aliasing == Z2D_AA_NONE ? 1 : 0);
+    }
+    return run_hairlines(c, jobs, fills, grads, grad_of_fill, hs);
+}
+
+// Fills and strokes over many device surfaces, in order per surface.
+// Hairline strokes draw as single-pixel composites outside the fill
+// pipeline, so a job list with hairlines runs in phases: the commands up to
+// each job's next hairlines, then those hairlines, and so on.
+static int draw_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_node *nodes, size_t n_nodes,
+                     const z2d_draw_cmd *cmds, size_t n_cmds) {
+    if ((n_jobs > 0 && !jobs_in) || (n_cmds > 0 && !cmds) || (n_nodes > 0 && !nodes)) return Z2D_ERR_INVALID_ARGUMENT;
+    if (n_jobs > 0x7FFFFFF || n_cmds > 0x7FFFFFF || n_nodes > 0x7FFFFFFF) {
+        set_error("batch too large");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    bool any_hairline = false;
+    for (size_t i = 0; i < n_cmds; i++) {
+        if (cmds[i].kind != Z2D_DRAW_STROKE && cmds[i].kind != Z2D_DRAW_FILL) {
+            set_error("draw command: bad kind");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+        any_hairline = any_hairline || is_hairline(cmds[i]);
+    }
+    for (size_t j = 0; j < n_jobs; j++) {
+        const z2d_job &jb = jobs_in[j];
+        if (jb.cmd_offset > n_cmds || jb.n_cmds > n_cmds - jb.cmd_offset) {
+            set_error("draw_jobs: job commands outside the command array");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+    }
+    if (!any_hairline) return draw_core(c, jobs_in, n_jobs, nodes, n_nodes, cmds, n_cmds);
+    std::vector<uint64_t> cursor(n_jobs, 0);
+    std::vector<z2d_job> phase(jobs_in, jobs_in + n_jobs);
+    std::vector<std::pair<uint64_t, uint64_t>> hair(n_jobs);
+    while (true) {
+        bool any = false;
+        for (size_t j = 0; j < n_jobs; j++) {  // commands up to the next hairline
+            uint64_t e = cursor[j];
+            while (e < jobs_in[j].n_cmds && !is_hairline(cmds[jobs_in[j].cmd_offset + e])) e++;
+            phase[j].cmd_offset = jobs_in[j].cmd_offset + cursor[j];
+            phase[j].n_cmds = e - cursor[j];
+            any = any || e > cursor[j];
+            cursor[j] = e;
+        }
+        if (any) {
+            const int rc = draw_core(c, phase.data(), n_jobs, nodes, n_nodes, cmds, n_cmds);
+            if (rc) return rc;
+        }
+        bool more = false;
+        for (size_t j = 0; j < n_jobs; j++) {  // then the hairlines that follow
+            uint64_t e = cursor[j];
+            while (e < jobs_in[j].n_cmds && is_hairline(cmds[jobs_in[j].cmd_offset + e])) e++;
+            hair[j] = {cursor[j], e};
+            more = more || e > cursor[j];
+            cursor[j] = e;
+        }
+        if (!more) break;
+        const int rc = draw_hairlines(c, jobs_in, n_jobs, hair, nodes, n_nodes, cmds);
+        if (rc) return rc;
+    }
+    return Z2D_OK;
 }
 
 static int do_stroke(Ctx &c, z2d_surface *surface, const z2d_pattern *pattern, const z2d_node *nodes, size_t n_nodes,

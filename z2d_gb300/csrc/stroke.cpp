@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -737,12 +738,110 @@ struct DashedPlotter : Common {
     }
 };
 
+// polyline_plotter.plot (polyline_plotter.zig:27-221): the path as open
+// polylines for hairline strokes, without transformation or scale.
+struct PolylinePlotter : Common {
+    Pt first{0, 0}, last{0, 0};
+    int len = 0;  // PointBuffer(1, 2) length, saturating at 3
+    bool use_dasher = false;
+    Dasher dasher;
+    size_t contour_start = 0;  // first point of the current polyline
+
+    PolylinePlotter(const Options &opts, Polygon &res) : Common(opts, res) {
+        use_dasher = dashed(opts);
+        if (use_dasher) {
+            dasher.init(opts.dashes, opts.n_dashes, opts.dash_offset);
+            if (dasher.stuck) error = kErrInvalidState;
+        }
+    }
+    void add(Pt p) {
+        if (len == 0) first = p;
+        last = p;
+        if (len < 3) len++;
+    }
+    void plot_pt(Pt p) {  // Contour.plot with scale 1
+        result.xy.push_back(p.x);
+        result.xy.push_back(p.y);
+    }
+    void end_polyline() {  // the current polyline goes to the result if it has points
+        if (result.points() > contour_start) result.ends.push_back(result.points());
+        contour_start = result.points();
+    }
+    // dashedLineTo (polyline_plotter.zig:186-221)
+    void dashed_line(Pt p0, Pt p1) {
+        Slope sl = slope(p0, p1);
+        const double total = normalize(sl);
+        double remaining = total;
+        double step_len = std::min(dasher.remain, remaining);
+        int64_t guard = 0;
+        while (remaining > 0) {
+            if (++guard > (int64_t)1 << 26) {
+                error = kErrInvalidState;
+                return;
+            }
+            remaining -= step_len;
+            const Pt cdp{p0.x + sl.dx * (total - remaining), p0.y + sl.dy * (total - remaining)};
+            if (!eq(cdp, last)) add(cdp);
+            if (dasher.on) plot_pt(cdp);
+            if (dasher.step(step_len)) {
+                end_polyline();
+                if (dasher.on) plot_pt(cdp);
+            }
+            step_len = std::min(dasher.remain, remaining);
+        }
+    }
+    void move_to(Pt p, bool last_node) {
+        end_polyline();
+        len = 0;
+        if (use_dasher) dasher.reset();
+        if (last_node) return;  // the move_to a Path adds after close_path
+        plot_pt(p);
+        add(p);
+    }
+    void line_to(int, Pt p) {
+        if (len == 0) {
+            error = kErrInvalidState;
+            return;
+        }
+        if (eq(last, p)) return;
+        if (use_dasher) {
+            dashed_line(last, p);
+        } else {
+            plot_pt(p);
+            add(p);
+        }
+    }
+    void curve_to(Pt b, Pt c, Pt d) {
+        if (len == 0) {
+            error = kErrInvalidState;
+            return;
+        }
+        spline(last, b, c, d, [&](Pt q) { line_to(0, q); });
+    }
+    void close_path() {
+        if (len < 2 || eq(last, first)) return;
+        if (use_dasher) {
+            dashed_line(last, first);
+        } else {
+            plot_pt(first);
+            add(first);
+        }
+    }
+    void finish() { end_polyline(); }
+};
+
 template <class P>
 int run(P &p, const z2d_node *nodes, size_t n_nodes) {
     for (size_t i = 0; i < n_nodes && p.error == 0; i++) {
         const z2d_node &nd = nodes[i];
         switch (nd.tag) {
-            case Z2D_MOVE_TO: p.move_to(Pt{nd.p[0], nd.p[1]}); break;
+            case Z2D_MOVE_TO:
+                if constexpr (std::is_same<P, PolylinePlotter>::value) {
+                    p.move_to(Pt{nd.p[0], nd.p[1]}, i == n_nodes - 1);
+                } else {
+                    p.move_to(Pt{nd.p[0], nd.p[1]});
+                }
+                break;
             case Z2D_LINE_TO: p.line_to(p.o.join, Pt{nd.p[0], nd.p[1]}); break;
             case Z2D_CURVE_TO: p.curve_to(Pt{nd.p[0], nd.p[1]}, Pt{nd.p[2], nd.p[3]}, Pt{nd.p[4], nd.p[5]}); break;
             case Z2D_CLOSE_PATH: p.close_path(); break;
@@ -762,6 +861,17 @@ bool transformation_invertible(const double m[6]) {
 }
 
 bool dashed(const Options &opts) { return opts.n_dashes > 0 && dashes_valid(opts.dashes, opts.n_dashes); }
+
+int polyline(const z2d_node *nodes, size_t n_nodes, const Options &opts, Polygon &out) {
+    out.clear();
+    t_arena.clear();
+    Options o = opts;
+    o.join = kJoinMiter;  // no pen
+    o.cap = kCapButt;
+    PolylinePlotter p(o, out);
+    if (p.error) return p.error;
+    return run(p, nodes, n_nodes);
+}
 
 int plot(const z2d_node *nodes, size_t n_nodes, const Options &opts, Polygon &contours) {
     contours.clear();

@@ -59,5 +59,11 @@ struct Polygon {
 // them; empty contours are left out.  Returns Z2D_OK or an error code.
 int plot(const z2d_node *nodes, size_t n_nodes, const Options &opts, Polygon &out);
 
+// polyline_plotter.plot (polyline_plotter.zig:27-141), for hairline
+// strokes: the path as open polylines (contours whose last point is not
+// joined to the first), untransformed and unscaled, dashed when
+// opts.dashes validates; opts.tolerance is used as given.
+int polyline(const z2d_node *nodes, size_t n_nodes, const Options &opts, Polygon &out);
+
 }  // namespace stroke
 }  // namespace z2dg

@@ -74,6 +74,20 @@ struct PolyRun {
 // the next, the last to the first) and merges the fills' extents.
 int poly_emit(Ctx &c, const PolyRun &run, const FillCmd *d_fills, FillState *d_st, DEdge *d_edges);
 
+// Hairline strokes (hairline.cu): per command its polylines (host-built by
+// stroke::polyline), the FillCmd that carries its pattern, operator,
+// precision and surface (job), and whether it draws without anti-aliasing.
+struct HairSet {
+    std::vector<const stroke::Polygon *> lines;
+    std::vector<int32_t> fill;
+    std::vector<int32_t> aa_none;
+};
+// Draws the hairlines in command order on the jobs' device surfaces
+// (hairline.zig: Bresenham or Xiaolin Wu segments, single-pixel
+// composites applied in path order).
+int run_hairlines(Ctx &c, const std::vector<DevJob> &jobs, std::vector<FillCmd> &fills,
+                  const std::vector<DevGradient> &grads, const std::vector<int32_t> &grad_of_fill, const HairSet &hs);
+
 // Device side of a StrokeSet during one run_jobs call.
 struct StrokeRun {
     const z2d_node *nodes = nullptr;
