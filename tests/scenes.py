@@ -12,7 +12,7 @@ from __future__ import annotations
 import math
 
 from z2d_gb300 import abi
-from z2d_gb300.path import Path
+from z2d_gb300.path import Path, tf_rotate, tf_scale, tf_translate
 from z2d_gb300.surface import Surface
 from z2d_gb300.types import Color, FillOptions, Gradient, Operation, Pattern, Pixel, wrap_dither
 
@@ -36,7 +36,39 @@ class Ctx:
         self.line_cap = "butt"
         self.miter_limit = 10.0
         self.dashes = ()
+        self.dash_offset = 0.0
+        self.hairline = False
         self.path = Path()
+
+    # the CTM (src/Context.zig:340-380): the path transforms points with it
+    def set_transformation(self, t):
+        self.transformation = tuple(float(v) for v in t)
+        self.path.transformation = self.transformation
+
+    def get_transformation(self):
+        return self.transformation
+
+    def set_identity(self):
+        self.set_transformation((1.0, 0.0, 0.0, 1.0, 0.0, 0.0))
+
+    def translate(self, tx, ty):
+        self.set_transformation(tf_translate(self.transformation, tx, ty))
+
+    def scale(self, sx, sy):
+        self.set_transformation(tf_scale(self.transformation, sx, sy))
+
+    def rotate(self, angle):
+        self.set_transformation(tf_rotate(self.transformation, angle))
+
+    def set_tolerance(self, t):  # Context.setTolerance (src/Context.zig:303-307)
+        self.tolerance = max(float(t), 0.001)
+        self.path.tolerance = self.tolerance
+
+    def arc(self, xc, yc, r, a1, a2):
+        self.path.arc(xc, yc, r, a1, a2)
+
+    def arc_negative(self, xc, yc, r, a1, a2):
+        self.path.arc_negative(xc, yc, r, a1, a2)
 
     def set_source(self, px: Pixel):
         self.pattern = Pattern.from_pixel(px)
@@ -62,7 +94,8 @@ class Ctx:
         opts = StrokeOptions(anti_aliasing=self.aa, line_cap=self.line_cap, line_join=self.line_join,
                              line_width=self.line_width, miter_limit=self.miter_limit, operator=self.operator,
                              precision=self.precision, tolerance=self.tolerance,
-                             transformation=self.transformation, dashes=self.dashes)
+                             transformation=self.transformation, dashes=self.dashes,
+                             dash_offset=self.dash_offset, hairline=self.hairline)
         rc = self.backend.stroke(self.surface, pat, self.path.nodes, opts)
         if rc != abi.OK:
             raise RuntimeError(f"stroke failed: {rc}")
@@ -698,6 +731,97 @@ def s057_stroke_bezier_dashed(be, aa):
     return s
 
 
+def s081_stroke_hairline(be, aa):
+    W = H = 300
+    s = Surface.init("rgb", 600, 2100)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.hairline = True
+
+    def done():
+        c.stroke()
+        c.reset_path()
+
+    def triangle():
+        m = 10
+        c.move_to(m, m)
+        c.line_to(W - m - 1, m)
+        c.line_to(W // 2 - 1, H - m - 1)
+        c.close_path()
+        done()
+
+    def square():
+        m = 50
+        c.move_to(m, m)
+        c.line_to(W - m - 1, m)
+        c.line_to(W - m - 1, H - m - 1)
+        c.line_to(m, H - m - 1)
+        c.close_path()
+        done()
+
+    def star():
+        m, xs, ys = 20, 3, 5
+        c.move_to(W // 2, m)
+        c.line_to(W - m * xs - 1, H - m - 1)
+        c.line_to(m, m * ys)
+        c.line_to(W - m - 1, m * ys)
+        c.line_to(m * xs, H - m - 1)
+        c.close_path()
+        done()
+
+    def bezier():
+        for y0, cy in ((149, 0), (199, 24), (249, 49)):
+            c.move_to(19, y0)
+            c.curve_to(89, cy, 209, cy, 279, y0)
+            done()
+
+    def arc(x, y, rx, ry):
+        saved = c.get_transformation()
+        c.translate(x + rx / 2, y + ry / 2)
+        c.scale(rx / 2, ry / 2)
+        c.arc(0, 0, 1, 0, 2 * math.pi)
+        c.close_path()
+        c.stroke()
+        c.reset_path()
+        c.set_transformation(saved)
+
+    def circle():
+        arc(W / 6, H / 6, W / 3 * 2, H / 3 * 2)
+
+    def ellipse():
+        arc(W / 3, H / 6, W / 3, H / 3 * 2)
+
+    def dots():
+        for i in range(10):
+            for j in range(50):
+                c.move_to(W // 6 + j * 4, W // 3 + i * 10)
+                c.close_path()
+            done()
+
+    def at(tx, ty, f):
+        c.translate(tx, ty)
+        f()
+        c.set_identity()
+
+    triangle()
+    at(300, 0, square)
+    at(0, 300, star)
+    at(300, 300, bezier)
+    at(0, 600, circle)
+    at(300, 600, ellipse)
+    at(150, 900, dots)
+    c.dashes = (20.0, 5.0)
+    c.dash_offset = -6.0
+    at(0, 1200, triangle)
+    at(300, 1200, square)
+    at(0, 1500, star)
+    at(300, 1500, bezier)
+    at(0, 1800, circle)
+    at(300, 1800, ellipse)
+    return s
+
+
 _HAIRLINE_CLIP_CASES = [  # (x0, y0, x1, y1) on a 100x100 canvas
     (-25, 50, 75, 60), (25, 50, 125, 60), (-25, 50, 75, 50), (25, 50, 125, 50),
     (25, -50, 75, 50), (25, 50, 75, 150), (-25, -50, -75, -150), (125, 150, 175, 250),
@@ -740,6 +864,7 @@ STROKE_SCENES = {
     "055_stroke_miter_dashed": s055_stroke_miter_dashed,
     "056_stroke_star_dashed": s056_stroke_star_dashed,
     "057_stroke_bezier_dashed": s057_stroke_bezier_dashed,
+    "081_stroke_hairline": s081_stroke_hairline,
     "082_stroke_hairline_clip": s082_stroke_hairline_clip,
 }
 
