@@ -10,9 +10,10 @@ GPU library for parity.
 from __future__ import annotations
 
 import math
+from fractions import Fraction
 
 from z2d_gb300 import abi
-from z2d_gb300.path import Path, tf_rotate, tf_scale, tf_translate
+from z2d_gb300.path import Path, tf_distance, tf_inverse, tf_rotate, tf_scale, tf_translate
 from z2d_gb300.surface import Surface
 from z2d_gb300.types import Color, FillOptions, Gradient, Operation, Pattern, Pixel, wrap_dither
 
@@ -59,6 +60,9 @@ class Ctx:
 
     def rotate(self, angle):
         self.set_transformation(tf_rotate(self.transformation, angle))
+
+    def device_to_user_distance(self, x, y):
+        return tf_distance(tf_inverse(self.transformation), x, y)
 
     def set_tolerance(self, t):  # Context.setTolerance (src/Context.zig:303-307)
         self.tolerance = max(float(t), 0.001)
@@ -822,6 +826,229 @@ def s081_stroke_hairline(be, aa):
     return s
 
 
+def s032_fill_arc(be, aa):
+    s = Surface.init("rgb", 300, 300)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    ratio = 0.552284749831
+    cy = 150
+    cx, r = 100, 50
+    p12 = r * ratio
+    c.move_to(cx, cy - r)
+    c.curve_to(cx + p12, cy - r, cx + r, cy - p12, cx + r, cy)
+    c.curve_to(cx + r, cy + p12, cx + p12, cy + r, cx, cy + r)
+    c.curve_to(cx - p12, cy + r, cx - r, cy + p12, cx - r, cy)
+    c.curve_to(cx - r, cy - p12, cx - p12, cy - r, cx, cy - r)
+    c.close_path()
+    c.fill()
+    cx, rM, rm = 200, 50, 25
+    pM, pm = rM * ratio, rm * ratio
+    c.reset_path()
+    c.move_to(cx, cy - rM)
+    c.curve_to(cx + pm, cy - rM, cx + rm, cy - pM, cx + rm, cy)
+    c.curve_to(cx + rm, cy + pM, cx + pm, cy + rM, cx, cy + rM)
+    c.curve_to(cx - pm, cy + rM, cx - rm, cy + pM, cx - rm, cy)
+    c.curve_to(cx - rm, cy - pM, cx - pm, cy - rM, cx, cy - rM)
+    c.close_path()
+    c.fill()
+    return s
+
+
+def s035_arc_command(be, aa):
+    s = Surface.init_pixel(_white_rgb(), 400, 400)
+    c = Ctx(be, s)
+    c.set_source(Pixel.rgb(0xFF, 0, 0))
+    c.aa = aa
+    c.line_width = 5
+    c.move_to(200, 200)
+    c.arc_negative(200, 200, 150, math.pi, math.pi * 1.5)
+    c.close_path()
+    c.fill()
+    c.set_source(Pixel.rgb(0, 0, 0xFF))
+    c.stroke()
+    c.reset_path()
+    c.move_to(175, 175)
+    c.arc(175, 175, 150, math.pi, math.pi * 1.5)
+    c.close_path()
+    c.set_source(Pixel.rgb(0xFF, 0xFF, 0))
+    c.fill()
+    c.set_source(Pixel.rgb(0, 0, 0xFF))
+    c.stroke()
+    return s
+
+
+def s042_arc_ellipses(be, aa):
+    s = Surface.init("rgb", 400, 400)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.line_width = 5
+
+    def ellipse(x, y, rx, ry, reset_ctm):
+        saved = c.get_transformation()
+        c.reset_path()
+        c.translate(x + rx / 2, y + ry / 2)
+        c.scale(rx / 2, ry / 2)
+        c.arc(0, 0, 1, 0, 2 * math.pi)
+        if reset_ctm:
+            c.set_transformation(saved)
+        c.close_path()
+
+    def user_width(lw):
+        ux, uy = c.device_to_user_distance(lw, lw)
+        return uy if ux < uy else ux
+
+    c.translate(10, 10)
+    ellipse(0, 0, 50, 100, True)
+    c.fill()
+    ellipse(100, 0, 50, 100, True)
+    c.stroke()
+    saved_ctm, saved_lw = c.get_transformation(), c.line_width
+    ellipse(200, 0, 50, 100, False)
+    c.line_width = user_width(saved_lw)
+    c.stroke()
+    c.set_transformation(saved_ctm)
+    c.line_width = saved_lw
+    saved_ctm, saved_lw = c.get_transformation(), c.line_width
+    c.rotate(math.pi / 4.0)
+    ellipse(300, 0, 50, 100, False)
+    c.line_width = user_width(saved_lw)
+    c.stroke()
+    c.set_transformation(saved_ctm)
+    c.line_width = saved_lw
+    return s
+
+
+# Zig evaluates constant expressions such as `math.pi / 6.0` at compile time
+# in 128-bit precision and rounds once; the double-precision quotient
+# math.pi / 6.0 is one ulp lower.
+_PI = Fraction("3.14159265358979323846264338327950288419716939937510582097494459")
+_PI_6 = float(_PI / 6)
+
+
+def _user_width(c, lw):
+    ux, uy = c.device_to_user_distance(lw, lw)
+    return uy if ux < uy else ux
+
+
+def s043_rect_transforms(be, aa):
+    s = Surface.init("rgb", 400, 400)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.line_width = 5
+
+    def rect(x, y, h, w, reset_ctm):
+        saved = c.get_transformation()
+        c.reset_path()
+        c.translate(x, y)
+        c.scale(h, w)
+        c.move_to(0, 0)
+        c.line_to(1, 0)
+        c.line_to(1, 1)
+        c.line_to(0, 1)
+        if reset_ctm:
+            c.set_transformation(saved)
+        c.close_path()
+
+    c.translate(10, 10)
+    rect(0, 0, 50, 100, True)
+    c.fill()
+    rect(100, 0, 50, 100, True)
+    c.stroke()
+    saved_ctm, saved_lw = c.get_transformation(), c.line_width
+    rect(200, 0, 50, 100, False)
+    c.line_width = _user_width(c, saved_lw)
+    c.stroke()
+    c.set_transformation(saved_ctm)
+    c.line_width = saved_lw
+    saved_ctm, saved_lw = c.get_transformation(), c.line_width
+    c.rotate(math.pi / 4.0)
+    rect(300, 0, 50, 100, False)
+    c.line_width = _user_width(c, saved_lw)
+    c.stroke()
+    c.set_transformation(saved_ctm)
+    c.line_width = saved_lw
+    return s
+
+
+def s044_line_transforms(be, aa):
+    s = Surface.init("rgb", 700, 400)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.line_width = 10
+
+    def line(i, reverse, rnd):
+        saved_ctm, saved_lw, saved_src = c.get_transformation(), c.line_width, c.pattern
+        c.line_cap = "round" if rnd else "square"
+        y = 50.0
+        if reverse:
+            y += 100
+        if rnd:
+            y += 200
+        if reverse:
+            c.translate(i * 100 + 25, y + 25 * math.sin(_PI_6 * i))
+            c.rotate(-_PI_6 * i)
+        else:
+            c.translate(i * 100 + 25, y - 25 * math.sin(_PI_6 * i))
+            c.rotate(_PI_6 * i)
+        c.scale(2, 1)
+        if reverse:
+            c.move_to(0, 0)
+            c.line_to(25, 0)
+        else:
+            c.move_to(25, 0)
+            c.line_to(0, 0)
+        c.line_width = _user_width(c, saved_lw)
+        c.stroke()
+        c.set_source(Pixel.rgb(0xF3, 0, 0))
+        c.line_width = 1
+        c.stroke()
+        c.line_cap = "butt"
+        c.pattern = saved_src
+        c.line_width = saved_lw
+        c.set_transformation(saved_ctm)
+        c.reset_path()
+
+    for rev, rnd in ((False, False), (True, False), (False, True), (True, True)):
+        for i in range(7):
+            line(float(i), rev, rnd)
+    return s
+
+
+def s045_round_join_transforms(be, aa):
+    s = Surface.init("rgb", 800, 600)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.line_width = 20
+    c.line_cap = "round"
+    c.line_join = "round"
+    for k in range(12):
+        i = float(k)
+        saved_ctm, saved_lw, saved_src = c.get_transformation(), c.line_width, c.pattern
+        x_off = 200 * math.fmod(i, 4.0) + 100 - 50 * math.cos(_PI_6 * i)
+        y_off = 200 * math.floor(i / 4.0) + 75 - 37.5 * math.sin(_PI_6 * i)
+        c.translate(x_off, y_off)
+        c.rotate(_PI_6 * i)
+        c.scale(2, 1)
+        c.move_to(0, 0)
+        c.line_to(25, 75)
+        c.line_to(50, 0)
+        c.line_width = _user_width(c, saved_lw)
+        c.stroke()
+        c.set_source(Pixel.rgb(0xF3, 0, 0))
+        c.line_width = 1
+        c.stroke()
+        c.pattern = saved_src
+        c.line_width = saved_lw
+        c.set_transformation(saved_ctm)
+        c.reset_path()
+    return s
+
+
 _HAIRLINE_CLIP_CASES = [  # (x0, y0, x1, y1) on a 100x100 canvas
     (-25, 50, 75, 60), (25, 50, 125, 60), (-25, 50, 75, 50), (25, 50, 125, 50),
     (25, -50, 75, 50), (25, 50, 75, 150), (-25, -50, -75, -150), (125, 150, 175, 250),
@@ -864,6 +1091,11 @@ STROKE_SCENES = {
     "055_stroke_miter_dashed": s055_stroke_miter_dashed,
     "056_stroke_star_dashed": s056_stroke_star_dashed,
     "057_stroke_bezier_dashed": s057_stroke_bezier_dashed,
+    "035_arc_command": s035_arc_command,
+    "042_arc_ellipses": s042_arc_ellipses,
+    "043_rect_transforms": s043_rect_transforms,
+    "044_line_transforms": s044_line_transforms,
+    "045_round_join_transforms": s045_round_join_transforms,
     "081_stroke_hairline": s081_stroke_hairline,
     "082_stroke_hairline_clip": s082_stroke_hairline_clip,
 }
@@ -890,6 +1122,7 @@ FILL_SCENES = {
     "052_fill_triangle_alpha4_gray_scaledown": _alpha_tri("alpha4", Pixel.alpha8(119)),
     "053_fill_triangle_alpha8_gray_scaleup": _alpha_tri("alpha8", Pixel.alpha4(7)),
     "079_fill_degenerate_lineto": s079_fill_degenerate_lineto,
+    "032_fill_arc": s032_fill_arc,
 }
 
 COMPOSITOR_SCENES = {
