@@ -1049,6 +1049,236 @@ def s045_round_join_transforms(be, aa):
     return s
 
 
+def s027_stroke_bezier_tolerance(be, aa):
+    s = Surface.init("rgb", 300, 300)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.line_width = 5
+    for tol, y0, cy in ((None, 149, 0), (3, 199, 24), (10, 249, 49)):
+        if tol is not None:
+            c.set_tolerance(tol)
+        c.reset_path()
+        c.move_to(19, y0)
+        c.curve_to(89, cy, 209, cy, 279, y0)
+        c.stroke()
+    return s
+
+
+def s029_stroke_lines_round_caps_tolerance(be, aa):
+    s = Surface.init("rgb", 300, 300)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.line_cap = "round"
+    c.line_join = "round"
+    c.line_width = 30
+    for tol, y in ((None, 50), (3, 150), (10, 250)):
+        if tol is not None:
+            c.set_tolerance(tol)
+        c.reset_path()
+        c.move_to(30, y)
+        c.line_to(270, y)
+        c.stroke()
+    return s
+
+
+def s030_stroke_star_round_tolerance(be, aa):
+    s = Surface.init("rgb", 900, 300)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.line_width = 30
+    c.line_join = "round"
+    m, sw, h, xs, ys = 20, 300, 300, 3, 5
+    for tol, xo in ((None, 0.0), (3, 300.0), (10, 600.0)):
+        c.reset_path()
+        if tol is not None:
+            c.set_tolerance(tol)
+        c.move_to(xo + sw // 2, m)
+        c.line_to(xo + sw - m * xs - 1, h - m - 1)
+        c.line_to(xo + m, m * ys)
+        c.line_to(xo + sw - m - 1, m * ys)
+        c.line_to(xo + m * xs, h - m - 1)
+        c.close_path()
+        c.stroke()
+    return s
+
+
+def _poly(c, pts):
+    c.move_to(*pts[0])
+    for q in pts[1:]:
+        c.line_to(*q)
+    c.close_path()
+
+
+def s033_fill_zig_mark(be, aa):
+    s = Surface.init("rgba", 153, 140)
+    c = Ctx(be, s)
+    c.set_source(Pixel.rgb(0xF7, 0xA4, 0x1D))
+    c.aa = aa
+    for pts in (
+        [(46, 22), (28, 44), (19, 30)],
+        [(46, 22), (33, 33), (28, 44), (22, 44), (22, 95), (31, 95), (20, 100), (12, 117), (0, 117), (0, 22)],
+        [(31, 95), (12, 117), (4, 106)],
+        [(56, 22), (62, 36), (37, 44)],
+        [(56, 22), (111, 22), (111, 44), (37, 44), (56, 32)],
+        [(116, 95), (97, 117), (90, 104)],
+        [(116, 95), (100, 104), (97, 117), (42, 117), (42, 95)],
+        [(150, 0), (52, 117), (3, 140), (101, 22)],
+        [(141, 22), (140, 40), (122, 45)],
+        [(153, 22), (153, 117), (106, 117), (120, 105), (125, 95), (131, 95), (131, 45), (122, 45), (132, 36),
+         (141, 22)],
+        [(125, 95), (130, 110), (106, 117)],
+    ):
+        _poly(c, pts)
+    c.fill()
+    return s
+
+
+def s034_stroke_cross(be, aa):
+    s = Surface.init("rgb", 250, 250)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.line_width = 5
+    c.move_to(100, 50)
+    for dx, dy in ((0, 50), (-50, 0), (0, 50), (50, 0), (0, 50), (50, 0), (0, -50), (50, 0), (0, -50), (-50, 0),
+                   (0, -50)):
+        c.path.rel_line_to(dx, dy)
+    c.close_path()
+    c.stroke()
+    return s
+
+
+def _lines(c, groups):
+    for pts, closed in groups:
+        c.move_to(*pts[0])
+        for q in pts[1:]:
+            c.line_to(*q)
+        if closed:
+            c.close_path()
+
+
+def s036_stroke_colinear(be, aa):
+    s = Surface.init("rgb", 100, 240)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.line_width = 4
+    _lines(c, [
+        ([(40, 50), (35, 60), (30, 70), (10, 50)], False),
+        ([(10, 10), (20, 20), (30, 30), (40, 10)], False),
+        ([(90, 50), (85, 60), (80, 70), (60, 50)], True),
+        ([(60, 10), (70, 20), (80, 30), (90, 10)], True),
+        ([(10, 90), (25, 100), (40, 110)], False),
+        ([(10, 150), (25, 140), (40, 130)], False),
+        ([(90, 90), (75, 100), (60, 110)], False),
+        ([(90, 150), (75, 140), (60, 130)], False),
+        ([(10, 170), (30, 190), (20, 180), (40, 170)], False),
+        ([(90, 170), (70, 190), (80, 180), (60, 170)], False),
+        ([(40, 210), (30, 230), (20, 220), (10, 210)], False),
+        ([(60, 210), (70, 230), (80, 220), (90, 210)], False),
+    ])
+    c.stroke()
+    return s
+
+
+def s037_stroke_join_overlap(be, aa):
+    s = Surface.init("rgb", 200, 200)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.line_width = 5
+    c.miter_limit = 4
+    _lines(c, [
+        ([(10, 10), (50, 90), (35, 50)], False),
+        ([(190, 10), (150, 90), (165, 50)], False),
+        ([(10, 190), (50, 110), (35, 150)], False),
+        ([(190, 190), (150, 110), (165, 150)], False),
+    ])
+    c.stroke()
+    return s
+
+
+def s038_stroke_zero_length(be, aa):
+    s = Surface.init("rgb", 60, 60)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.line_width = 10
+    c.line_cap = "round"
+    c.move_to(10, 10)
+    c.close_path()
+    c.move_to(30, 30)
+    c.line_to(30, 30)
+    c.line_to(30, 30)
+    c.close_path()
+    c.move_to(50, 50)
+    c.stroke()
+    return s
+
+
+def s039_stroke_paint_extent_dontclip(be, aa):
+    s = Surface.init("rgb", 50, 80)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.line_width = 5
+    _lines(c, [([(40, 50), (35, 60), (30, 70), (10, 50)], False)])
+    c.stroke()
+    return s
+
+
+def s040_stroke_corner_symmetrical(be, aa):
+    s = Surface.init("rgb", 18, 36)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.move_to(0, 0)
+    c.line_to(18, 36)
+    c.stroke()
+    return s
+
+
+def s041_stroke_noop_lineto(be, aa):
+    s = Surface.init("rgb", 18, 36)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    _lines(c, [([(9, 0), (9, 9), (0, 18), (0, 18)], False)])
+    c.stroke()
+    return s
+
+
+def s073_stroke_sameclose(be, aa):
+    s = Surface.init("rgb", 300, 300)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    m = 50
+    _lines(c, [([(m, m), (300 - m - 1, m), (300 - m - 1, 300 - m - 1), (m, 300 - m - 1), (m, m)], True)])
+    c.stroke()
+    return s
+
+
+def s078_double_close(be, aa):
+    s = Surface.init_pixel(Pixel.from_color(Color.rgb(0.33, 0.33, 0.33)), 300, 300)
+    c = Ctx(be, s)
+    c.aa = aa
+    c.move_to(49, 49)
+    c.line_to(250, 49)
+    c.line_to(250, 250)
+    c.line_to(49, 250)
+    c.close_path()
+    c.close_path()
+    c.set_source(Pixel.rgb(0, 0xFF, 0))
+    c.fill()
+    c.set_source(Pixel.rgb(0xFF, 0, 0xFF))
+    c.stroke()
+    return s
+
+
 _HAIRLINE_CLIP_CASES = [  # (x0, y0, x1, y1) on a 100x100 canvas
     (-25, 50, 75, 60), (25, 50, 125, 60), (-25, 50, 75, 50), (25, 50, 125, 50),
     (25, -50, 75, 50), (25, 50, 75, 150), (-25, -50, -75, -150), (125, 150, 175, 250),
@@ -1091,7 +1321,19 @@ STROKE_SCENES = {
     "055_stroke_miter_dashed": s055_stroke_miter_dashed,
     "056_stroke_star_dashed": s056_stroke_star_dashed,
     "057_stroke_bezier_dashed": s057_stroke_bezier_dashed,
+    "027_bezier_tolerance": s027_stroke_bezier_tolerance,
+    "029_stroke_lines_round_caps_tolerance": s029_stroke_lines_round_caps_tolerance,
+    "030_stroke_star_round_tolerance": s030_stroke_star_round_tolerance,
+    "034_stroke_cross": s034_stroke_cross,
     "035_arc_command": s035_arc_command,
+    "036_stroke_colinear": s036_stroke_colinear,
+    "037_stroke_join_overlap": s037_stroke_join_overlap,
+    "038_stroke_zero_length": s038_stroke_zero_length,
+    "039_stroke_paint_extent_dontclip": s039_stroke_paint_extent_dontclip,
+    "040_stroke_corner_symmetrical": s040_stroke_corner_symmetrical,
+    "041_stroke_noop_lineto": s041_stroke_noop_lineto,
+    "073_stroke_sameclose": s073_stroke_sameclose,
+    "078_double_close": s078_double_close,
     "042_arc_ellipses": s042_arc_ellipses,
     "043_rect_transforms": s043_rect_transforms,
     "044_line_transforms": s044_line_transforms,
@@ -1123,6 +1365,7 @@ FILL_SCENES = {
     "053_fill_triangle_alpha8_gray_scaleup": _alpha_tri("alpha8", Pixel.alpha4(7)),
     "079_fill_degenerate_lineto": s079_fill_degenerate_lineto,
     "032_fill_arc": s032_fill_arc,
+    "033_fill_zig_mark": s033_fill_zig_mark,
 }
 
 COMPOSITOR_SCENES = {

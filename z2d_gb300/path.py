@@ -45,6 +45,29 @@ def tf_rotate(a, angle: float) -> tuple:
     return tf_mul(a, (c, -s, s, c, 0.0, 0.0))
 
 
+def tf_inverse(a) -> tuple:
+    """Transformation.inverse (Transformation.zig:103-162); raises on a
+    matrix that cannot be inverted."""
+    ax, by, cx, dy, tx, ty = a
+    if by == 0 and cx == 0:
+        if ax == 0 or dy == 0:
+            raise ValueError("InvalidMatrix")
+        if ax != 1 or dy != 1:
+            return (1 / ax, 0.0, 0.0, 1 / dy, -tx / ax, -ty / dy)
+        return (1.0, 0.0, 0.0, 1.0, -tx, -ty)
+    det = ax * dy - by * cx
+    if det == 0:
+        raise ValueError("InvalidMatrix")
+    adj = (dy, -by, -cx, ax, by * ty - dy * tx, cx * tx - ax * ty)
+    sc = 1 / det
+    return tuple(v * sc for v in adj)
+
+
+def tf_distance(a, x: float, y: float) -> tuple:
+    """Transformation.userToDeviceDistance: (x, y) through a without translation."""
+    return (a[0] * x + a[1] * y, a[2] * x + a[3] * y)
+
+
 # ---------------------------------------------------------------------- arcs
 # src/internal/arc.zig (after cairo-arc.c): circular arcs as cubic splines.
 _MAX_FULL_CIRCLES = 65536
@@ -193,6 +216,15 @@ class Path:
         self.nodes.append((abi.LINE_TO, p[0], p[1], 0.0, 0.0, 0.0, 0.0))
         self.current = p
         return self
+
+    def rel_line_to(self, x: float, y: float) -> "Path":
+        """Path.relLineTo (Path.zig:187-192): a line to the current point
+        (taken back to user space) plus (x, y)."""
+        if self.current is None:
+            raise ValueError("NoCurrentPoint")
+        inv = tf_inverse(self.transformation)
+        ux, uy = tf_distance(inv, self.current[0], self.current[1])
+        return self.line_to(ux + inv[4] + x, uy + inv[5] + y)
 
     def curve_to(self, x1, y1, x2, y2, x3, y3) -> "Path":
         if self.current is None:
