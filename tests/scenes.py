@@ -1151,7 +1151,7 @@ def s034_stroke_cross(be, aa):
     return s
 
 
-def _lines(c, groups):
+def _polylines(c, groups):
     for pts, closed in groups:
         c.move_to(*pts[0])
         for q in pts[1:]:
@@ -1166,7 +1166,7 @@ def s036_stroke_colinear(be, aa):
     c.set_source(_white_rgb())
     c.aa = aa
     c.line_width = 4
-    _lines(c, [
+    _polylines(c, [
         ([(40, 50), (35, 60), (30, 70), (10, 50)], False),
         ([(10, 10), (20, 20), (30, 30), (40, 10)], False),
         ([(90, 50), (85, 60), (80, 70), (60, 50)], True),
@@ -1191,7 +1191,7 @@ def s037_stroke_join_overlap(be, aa):
     c.aa = aa
     c.line_width = 5
     c.miter_limit = 4
-    _lines(c, [
+    _polylines(c, [
         ([(10, 10), (50, 90), (35, 50)], False),
         ([(190, 10), (150, 90), (165, 50)], False),
         ([(10, 190), (50, 110), (35, 150)], False),
@@ -1225,7 +1225,7 @@ def s039_stroke_paint_extent_dontclip(be, aa):
     c.set_source(_white_rgb())
     c.aa = aa
     c.line_width = 5
-    _lines(c, [([(40, 50), (35, 60), (30, 70), (10, 50)], False)])
+    _polylines(c, [([(40, 50), (35, 60), (30, 70), (10, 50)], False)])
     c.stroke()
     return s
 
@@ -1246,7 +1246,7 @@ def s041_stroke_noop_lineto(be, aa):
     c = Ctx(be, s)
     c.set_source(_white_rgb())
     c.aa = aa
-    _lines(c, [([(9, 0), (9, 9), (0, 18), (0, 18)], False)])
+    _polylines(c, [([(9, 0), (9, 9), (0, 18), (0, 18)], False)])
     c.stroke()
     return s
 
@@ -1257,7 +1257,7 @@ def s073_stroke_sameclose(be, aa):
     c.set_source(_white_rgb())
     c.aa = aa
     m = 50
-    _lines(c, [([(m, m), (300 - m - 1, m), (300 - m - 1, 300 - m - 1), (m, 300 - m - 1), (m, m)], True)])
+    _polylines(c, [([(m, m), (300 - m - 1, m), (300 - m - 1, 300 - m - 1), (m, 300 - m - 1), (m, m)], True)])
     c.stroke()
     return s
 
