@@ -1279,6 +1279,203 @@ def s078_double_close(be, aa):
     return s
 
 
+def s058_stroke_misc_dashes(be, aa):
+    s = Surface.init("rgb", 600, 2000)
+    c = Ctx(be, s)
+    c.set_source(_white_rgb())
+    c.aa = aa
+    c.line_width = 3
+    c.dashes = (25.0, 5.0)
+
+    def at(tx, ty):
+        c.set_identity()
+        c.translate(tx, ty)
+
+    def line(pts, close=False):
+        c.move_to(*pts[0])
+        for q in pts[1:]:
+            c.line_to(*q)
+        if close:
+            c.close_path()
+        c.stroke()
+        c.reset_path()
+
+    c.translate(50, 50)
+    line([(100, 0), (200, 200), (0, 200)], True)
+    at(350, 50)
+    line([(0, 0), (0, 200), (200, 200), (200, 0)], True)
+    d = 200
+    at(50 + d / 2, 350 + d / 2)  # circle
+    c.scale(d / 2, d / 2)
+    c.arc(0, 0, 1, 0, 2 * math.pi)
+    c.set_identity()
+    c.stroke()
+    c.reset_path()
+    at(350 + d / 2, 350 + d / 2)  # fill + stroke
+    c.scale(d / 2, d / 2)
+    c.arc(0, 0, 1, 0, 2 * math.pi)
+    c.close_path()
+    c.set_identity()
+    c.set_source(Pixel.rgb(0xAA, 0xAA, 0xAA))
+    c.fill()
+    c.set_source(_white_rgb())
+    c.stroke()
+    c.reset_path()
+    elw = 6.0  # ellipse, no transform on the stroke
+    c.line_width = elw
+    xd, yd = 100, 200
+    at(100 + xd / 2, 650 + yd / 2)
+    c.scale(xd / 2, yd / 2)
+    c.arc(0, 0, 1, 0, 2 * math.pi)
+    c.set_identity()
+    c.stroke()
+    c.reset_path()
+    at(400 + xd / 2, 650 + yd / 2)  # ellipse, transform on the stroke
+    c.scale(xd / 2, yd / 2)
+    c.arc(0, 0, 1, 0, 2 * math.pi)
+    c.line_width = _user_width(c, elw)
+    c.stroke()
+    c.set_identity()
+    c.reset_path()
+    at(50, 950)  # square through the transform
+    c.scale(200, 200)
+    c.move_to(0, 0)
+    c.line_to(0, 1)
+    c.line_to(1, 1)
+    c.line_to(1, 0)
+    c.close_path()
+    c.line_width = _user_width(c, elw)
+    c.stroke()
+    c.set_identity()
+    c.reset_path()
+    c.line_width = 3  # odd dash arrays
+    at(350, 950)
+    c.dashes = (28.0,)
+    line([(0, 0), (200, 0)])
+    at(350, 990)
+    c.dashes = (25.0, 5.0, 3.0)
+    line([(0, 0), (200, 0)])
+    c.line_width = 10  # capping
+    for cap, y in (("round", 1030), ("square", 1070), ("butt", 1110)):
+        c.line_cap = cap
+        at(350, y)
+        c.dashes = (28.0,)
+        line([(0, 0), (200, 0)])
+    c.line_cap = "round"  # dots
+    at(350, 1150)
+    c.dashes = (0.0, 20.0)
+    line([(0, 0), (200, 0)])
+    c.line_cap = "square"  # squares aligned to the slope
+    at(50, 1250)
+    c.dashes = (0.0, 20.0)
+    c.move_to(0, 0)
+    c.line_to(0, 200)
+    c.move_to(20, 0)
+    c.line_to(200, 200)
+    c.stroke()
+    c.reset_path()
+    c.line_cap = "butt"  # offsets
+    c.line_width = 3
+    c.set_identity()
+    c.dashes = (25.0,)
+    c.dash_offset = 12.5
+    c.translate(350, 1225)
+    line([(0, 0), (200, 0), (200, 100), (0, 100)], True)
+    at(350, 1350)
+    c.dash_offset = -12.5
+    line([(0, 0), (200, 0), (200, 100), (0, 100)], True)
+    c.line_width = 10
+    c.set_identity()
+    c.dashes = ()
+    c.dash_offset = 0.0
+    c.translate(150, 1550)
+    line([(0, 0), (300, 0)])
+    at(150, 1570)
+    c.dashes = (30.0, 10.0)
+    c.dash_offset = 0.0
+    line([(0, 0), (300, 0)])
+    for y, off in ((1590, 30.0), (1610, -30.0), (1630, 10.0)):
+        at(150, y)
+        c.dash_offset = off
+        line([(0, 0), (300, 0)])
+    c.set_source(Pixel.rgba(127, 0, 0, 127))  # RGBA{255, 0, 0, 127}.multiply()
+    at(150, 1590)
+    c.dashes = ()
+    c.dash_offset = 0.0
+    for y, dx in ((1590, -30), (1610, 30), (1630, -10)):
+        at(150, y)
+        c.move_to(0, 0)
+        c.path.rel_line_to(dx, 0)
+        c.stroke()
+        c.reset_path()
+    c.set_source(_white_rgb())  # octagon
+    at(200, 1725)
+    c.dash_offset = 0.0
+    c.dashes = (180.0, 30.0)
+    line([(136.737609507049, 188.692435121084), (63.2623904929514, 188.692435121084),
+          (11.3075648789165, 136.737609507049), (11.3075648789165, 63.2623904929514),
+          (63.2623904929513, 11.3075648789165), (136.737609507049, 11.3075648789165),
+          (188.692435121084, 63.2623904929513), (188.692435121084, 136.737609507049)], True)
+    return s
+
+
+def _oob_scene(draws):
+    def scene(be, aa):
+        s = Surface.init_pixel(Pixel.from_color(Color.rgb(0.33, 0.33, 0.33)), 300, 300)
+        c = Ctx(be, s)
+        c.aa = aa
+        for k, (tx, ty, pts, first_line) in enumerate(draws):
+            c.reset_path()
+            c.set_identity()
+            c.translate(tx, ty)
+            (c.line_to if first_line else c.move_to)(*pts[0])
+            for q in pts[1:]:
+                c.line_to(*q)
+            c.close_path()
+            c.set_source(Pixel.rgb(0, 0xFF, 0))
+            c.fill()
+            c.set_source(Pixel.rgb(0xFF, 0, 0xFF))
+            c.stroke()
+        return s
+    return scene
+
+
+_W, _CX, _M = 300, 150, 10
+s075_oob_draw_corners = _oob_scene([
+    (-_M, -_M, [(_CX, _CX), (-_CX, _CX), (_CX, -_CX)], True),
+    (_M, -_M, [(_CX, _CX), (_W + _CX, _CX), (_W + _CX, -_CX), (_CX, -_CX)], False),
+    (-_M, _M, [(_CX, _CX), (-_CX, _CX), (-_CX, _W + _CX), (_CX, _W + _CX)], False),
+    (_M, _M, [(_CX, _CX), (_W + _CX, _CX), (_W + _CX, _W + _CX), (_CX, _W + _CX)], False),
+])
+s076_oob_draw_sides = _oob_scene([
+    (0, -_M, [(_CX - _M, _CX), (_CX - _M, -_CX), (_CX + _M, -_CX), (_CX + _M, _CX)], False),
+    (0, _M, [(_CX - _M, _CX), (_CX - _M, _W + _CX), (_CX + _M, _W + _CX), (_CX + _M, _CX)], False),
+    (-_M, 0, [(_CX, _CX - _M), (-_CX, _CX - _M), (-_CX, _CX + _M), (_CX, _CX + _M)], False),
+    (_M, 0, [(_CX, _CX - _M), (_W + _CX, _CX - _M), (_W + _CX, _CX + _M), (_CX, _CX + _M)], False),
+])
+
+
+def s077_oob_draw_full_outside(be, aa):
+    s = Surface.init("rgb", 300, 300)
+    c = Ctx(be, s)
+    c.aa = aa
+    for cx, cy in ((-300, -300), (600, -300), (600, 600), (-300, 600), (-300, 150), (600, 150), (150, -300),
+                   (150, 600)):
+        c.reset_path()
+        c.set_identity()
+        c.translate(cx, cy)
+        c.move_to(cx - 20, cy - 20)
+        c.line_to(cx + 20, cy - 20)
+        c.line_to(cx + 20, cy + 20)
+        c.line_to(cx - 20, cy + 20)
+        c.close_path()
+        c.set_source(Pixel.rgb(0, 0xFF, 0))
+        c.fill()
+        c.set_source(Pixel.rgb(0xFF, 0, 0xFF))
+        c.stroke()
+    return s
+
+
 _HAIRLINE_CLIP_CASES = [  # (x0, y0, x1, y1) on a 100x100 canvas
     (-25, 50, 75, 60), (25, 50, 125, 60), (-25, 50, 75, 50), (25, 50, 125, 50),
     (25, -50, 75, 50), (25, 50, 75, 150), (-25, -50, -75, -150), (125, 150, 175, 250),
@@ -1332,7 +1529,11 @@ STROKE_SCENES = {
     "039_stroke_paint_extent_dontclip": s039_stroke_paint_extent_dontclip,
     "040_stroke_corner_symmetrical": s040_stroke_corner_symmetrical,
     "041_stroke_noop_lineto": s041_stroke_noop_lineto,
+    "058_stroke_misc_dashes": s058_stroke_misc_dashes,
     "073_stroke_sameclose": s073_stroke_sameclose,
+    "075_oob_draw_corners": s075_oob_draw_corners,
+    "076_oob_draw_sides": s076_oob_draw_sides,
+    "077_oob_draw_full_outside": s077_oob_draw_full_outside,
     "078_double_close": s078_double_close,
     "042_arc_ellipses": s042_arc_ellipses,
     "043_rect_transforms": s043_rect_transforms,
