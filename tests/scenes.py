@@ -418,6 +418,89 @@ def s061_linear_gradient(be, aa=None):
     return dst
 
 
+def _gradient_draw(be, dst, scratch, sx, sy, g):
+    assert be.composite(scratch, 0, 0, [Operation("src_over", src=Pattern.from_gradient(g))]) == abi.OK
+    assert be.composite(dst, sx, sy, [Operation("src_over", src=scratch)]) == abi.OK
+
+
+def s062_hsl_gradient(be, aa=None):
+    dst = Surface.init("rgb", 100, 200)
+    for w, h, sx, sy, x0, y0, x1, y1, c0, c1 in (
+        (100, 100, 0, 0, 0, 49, 99, 49, Color.hsl(300, 1, 0.5), Color.hsl(60, 1, 0.5)),
+        (50, 100, 0, 100, 0, 49, 49, 49, Color.hsl(0, 1, 0.5), Color.hsl(0, 0, 0.5)),
+        (50, 100, 50, 100, 49, 49, 0, 49, Color.hsl(180, 1, 0.5), Color.hsl(180, 0, 0.5)),
+        (100, 50, 0, 100, 49, 0, 49, 49, Color.hsl(0, 0, 1, 1), Color.hsl(0, 0, 0.5, 0)),
+        (100, 50, 0, 150, 49, 49, 49, 0, Color.hsl(0, 0, 0, 1), Color.hsl(0, 0, 0.5, 0)),
+    ):
+        g = Gradient.linear(x0, y0, x1, y1, method="hsl", polar="shorter")
+        g.add_stop(0, c0)
+        g.add_stop(1, c1)
+        _gradient_draw(be, dst, Surface.init("rgba", w, h), sx, sy, g)
+    return dst
+
+
+def s063_radial_gradient(be, aa=None):
+    dst = Surface.init("rgba", 300, 500)
+    cases = [(100 * x, 100 * y, 49 + 25 * (float(x) - 1), 49 + 25 * (float(y) - 1), 5, 49, 49, 50)
+             for y in range(3) for x in range(3)]
+    cases += [(0, 300, 49, 49, 0, 49, 49, 50), (100, 300, 49, 49, 50, 49, 49, 0), (200, 300, 49, 49, 50, 49, 49, 50),
+              (0, 400, 49, 49, 0, 49, 49, 0), (100, 400, 10, 49, 0, 49, 49, 25), (200, 400, 49, 49, 49, 49, 49, 50)]
+    for sx, sy, ix, iy, ir, ox, oy, orad in cases:
+        g = Gradient.radial(ix, iy, ir, ox, oy, orad)
+        g.add_stop(0, Color.rgb(1, 0, 0))
+        g.add_stop(0.5, Color.rgb(0, 1, 0))
+        g.add_stop(1, Color.rgb(0, 0, 1))
+        _gradient_draw(be, dst, Surface.init("rgba", 100, 100), sx, sy, g)
+    return dst
+
+
+def _rgb_stops(g):
+    g.add_stop(0, Color.rgb(1, 0, 0))
+    g.add_stop(0.5, Color.rgb(0, 1, 0))
+    g.add_stop(1, Color.rgb(0, 0, 1))
+    return g
+
+
+def s064_radial_source(be, aa):
+    s = Surface.init("rgb", 100, 100)
+    c = Ctx(be, s)
+    c.aa = aa
+    c.pattern = Pattern.from_gradient(_rgb_stops(Gradient.radial(49, 49, 0, 49, 49, 50)))
+    _poly(c, [(0, 0), (100, 0), (100, 100), (0, 100)])
+    c.fill()
+    return s
+
+
+def s065_conic_gradient(be, aa=None):
+    dst = Surface.init("rgba", 200, 200)
+    for y in range(2):
+        for x in range(2):
+            g = Gradient.conic(49, 49, math.pi / 2.0 * float(y * 2 + x), method="hsl", polar="increasing")
+            g.add_stop(0, Color.hsl(0, 1, 0.5))
+            g.add_stop(1, Color.hsl(360, 1, 0.5))
+            _gradient_draw(be, dst, Surface.init("rgba", 100, 100), 100 * x, 100 * y, g)
+    return dst
+
+
+def s066_conic_pie_gradient(be, aa):
+    s = Surface.init("rgb", 300, 300)
+    g = Gradient.conic(149, 149, 0)
+    third, two_thirds = Fraction(1, 3), Fraction(2, 3)
+    g.add_stop(0, Color.rgb(1, 0, 0))
+    g.add_stop(float(third), Color.rgb(1, 0, 0))
+    g.add_stop(float(third + Fraction("0.005")), Color.rgb(0, 1, 0))
+    g.add_stop(float(two_thirds), Color.rgb(0, 1, 0))
+    g.add_stop(float(two_thirds + Fraction("0.005")), Color.rgb(0, 0, 1))
+    g.add_stop(1, Color.rgb(0, 0, 1))
+    c = Ctx(be, s)
+    c.aa = aa
+    c.pattern = Pattern.from_gradient(g)
+    c.arc(149, 149, 100, 0, math.pi * 2)
+    c.close_path()
+    c.fill()
+    return s
+
+
 # ------------------------------------------------------------- stroke scenes
 def _stroke_canvas(be, aa, w, h):
     s = Surface.init("rgb", w, h)
@@ -1567,10 +1650,15 @@ FILL_SCENES = {
     "079_fill_degenerate_lineto": s079_fill_degenerate_lineto,
     "032_fill_arc": s032_fill_arc,
     "033_fill_zig_mark": s033_fill_zig_mark,
+    "064_radial_source": s064_radial_source,
+    "066_conic_pie_gradient": s066_conic_pie_gradient,
 }
 
 COMPOSITOR_SCENES = {
     "061_linear_gradient": s061_linear_gradient,
+    "062_hsl_gradient": s062_hsl_gradient,
+    "063_radial_gradient": s063_radial_gradient,
+    "065_conic_gradient": s065_conic_gradient,
 }
 
 # AA mode -> golden suffix (spec/main_spec.zig:564-634, 772-831)
