@@ -13,7 +13,7 @@ import math
 from fractions import Fraction
 
 from z2d_gb300 import abi
-from z2d_gb300.path import Path, tf_distance, tf_inverse, tf_rotate, tf_scale, tf_translate
+from z2d_gb300.path import Path, tf_distance, tf_inverse, tf_mul, tf_rotate, tf_scale, tf_translate
 from z2d_gb300.surface import Surface
 from z2d_gb300.types import Color, FillOptions, Gradient, Operation, Pattern, Pixel, wrap_dither
 
@@ -60,6 +60,19 @@ class Ctx:
 
     def rotate(self, angle):
         self.set_transformation(tf_rotate(self.transformation, angle))
+
+    def set_source_pattern(self, pattern):
+        """Context.setSource (src/Context.zig:115-121): a gradient takes the
+        current transformation."""
+        if pattern.kind == abi.PATTERN_GRADIENT:
+            try:
+                pattern.gradient.set_transformation(self.transformation)
+            except ValueError:
+                return
+        self.pattern = pattern
+
+    def mul(self, m):
+        self.set_transformation(tf_mul(self.transformation, m))
 
     def device_to_user_distance(self, x, y):
         return tf_distance(tf_inverse(self.transformation), x, y)
@@ -498,6 +511,90 @@ def s066_conic_pie_gradient(be, aa):
     c.arc(149, 149, 100, 0, math.pi * 2)
     c.close_path()
     c.fill()
+    return s
+
+
+def _f32(fr: Fraction) -> float:
+    """The f32 nearest to an exact value (Zig rounds compile-time constants
+    once; a double in between could round twice)."""
+    import numpy as np
+    c = np.float32(float(fr))
+    best = c
+    for cand in (np.nextafter(c, np.float32(-np.inf)), np.nextafter(c, np.float32(np.inf))):
+        if abs(Fraction(float(cand)) - fr) < abs(Fraction(float(best)) - fr):
+            best = cand
+    return float(best)
+
+
+def _unit_square(c, size):
+    _poly(c, [(0, 0), (size, 0), (size, size), (0, size)])
+
+
+def s067_gradient_transforms(be, aa):
+    s = Surface.init("rgb", 200, 200)
+    c = Ctx(be, s)
+    c.scale(2, 2)
+    c.aa = aa
+    c.set_source_pattern(Pattern.from_gradient(_rgb_stops(Gradient.linear(0, 0, 50, 50))))
+    _unit_square(c, 50)
+    c.fill()
+    radial = _rgb_stops(Gradient.radial(25, 50, 0, 25, 50, 50))
+    c.set_identity()
+    c.mul((1.0, 0.5, 0.0, 1.0, 0.0, 0.0))  # skew: by = 0.5
+    c.translate(100, 0)
+    c.set_source_pattern(Pattern.from_gradient(radial))
+    c.set_identity()
+    c.translate(100, 0)
+    c.reset_path()
+    _unit_square(c, 100)
+    c.fill()
+    conic = Gradient.conic(50, 50, 0, method="hsl", polar="increasing")
+    conic.add_stop(0, Color.hsl(0, 1, 0.5))
+    conic.add_stop(1, Color.hsl(360, 1, 0.5))
+    c.set_identity()
+    c.scale(2, 1)
+    c.translate(0, 100)
+    c.set_source_pattern(Pattern.from_gradient(conic))
+    c.reset_path()
+    _unit_square(c, 100)
+    c.fill()
+    return s
+
+
+def s068_gradient_deband(be, aa=None):
+    dst = Surface.init_pixel(Pixel.rgb(255, 255, 255), 500, 500)
+    for sy, gray, bits, dither in ((0, False, 8, "none"), (100, False, 8, "bayer"), (200, True, 8, "none"),
+                                   (300, True, 4, "none"), (400, True, 4, "bayer")):
+        fmt = ("alpha4" if bits == 4 else "alpha8") if gray else "rgb"
+        scratch = Surface.init(fmt, 500, 100)
+        g = Gradient.linear(0, 50, 500, 50)
+        if gray:
+            g.add_stop(0, Color.rgb(1, 1, 1, 0))
+            g.add_stop(1, Color.rgb(0, 0, 0, 1))
+        else:
+            g.add_stop(0, Color.rgb(*(_f32(Fraction(v, 255)) for v in (27, 93, 124))))
+            g.add_stop(1, Color.rgb(*(_f32(Fraction(v, 255)) for v in (38, 32, 16))))
+        assert be.composite(scratch, 0, 0, [Operation("src_over", src=Pattern.dither(dither, g, bits))]) == abi.OK
+        assert be.composite(dst, 0, sy, [Operation("src_over", src=scratch)]) == abi.OK
+    return dst
+
+
+def s069_gradient_dither_context(be, aa):
+    s = Surface.init("alpha4", 400, 150)
+    g = Gradient.linear(0, 25, 400, 25)
+    g.add_stop(0, Color.rgb(0, 0, 0, 0))
+    g.add_stop(1, Color.rgb(1, 1, 1, 1))
+    c = Ctx(be, s)
+    c.aa = aa
+    for ty, dither in ((None, "none"), (50, "bayer"), (100, "blue_noise")):
+        if ty is not None:
+            c.reset_path()
+            c.set_identity()
+            c.translate(0, ty)
+        c.set_source_pattern(Pattern.from_gradient(g))
+        c.dither = dither
+        _poly(c, [(0, 0), (400, 0), (400, 50), (0, 50)])
+        c.fill()
     return s
 
 
@@ -1652,6 +1749,8 @@ FILL_SCENES = {
     "033_fill_zig_mark": s033_fill_zig_mark,
     "064_radial_source": s064_radial_source,
     "066_conic_pie_gradient": s066_conic_pie_gradient,
+    "067_gradient_transforms": s067_gradient_transforms,
+    "069_gradient_dither_context": s069_gradient_dither_context,
 }
 
 COMPOSITOR_SCENES = {
@@ -1659,6 +1758,7 @@ COMPOSITOR_SCENES = {
     "062_hsl_gradient": s062_hsl_gradient,
     "063_radial_gradient": s063_radial_gradient,
     "065_conic_gradient": s065_conic_gradient,
+    "068_gradient_deband": s068_gradient_deband,
 }
 
 # AA mode -> golden suffix (spec/main_spec.zig:564-634, 772-831)
