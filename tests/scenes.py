@@ -598,6 +598,30 @@ def s069_gradient_dither_context(be, aa):
     return s
 
 
+def s070_compositor_ops(be, aa):
+    s = Surface.init_pixel(Pixel.rgb(255, 255, 255), 460, 3090)
+    for i, op in enumerate(abi.OPERATORS):
+        for j in range(4):
+            transparent = (j % 2) == 1
+            bg = Pixel.from_color(Color.rgb(0.69, 0.23, 0.21, 0.9) if transparent else Color.rgb(0.69, 0.23, 0.21))
+            fg = Pixel.from_color(Color.rgb(0.56, 0.50, 0.89, 0.8) if transparent else Color.rgb(0.56, 0.50, 0.89))
+            scratch = Surface.init("rgba", 100, 100)
+            c = Ctx(be, scratch)
+            c.aa = aa
+            c.precision = "integer" if j < 2 else "float"
+            c.set_source(bg)
+            _poly(c, [(0, 0), (75, 0), (75, 75), (0, 75)])
+            c.fill()
+            c.set_source(fg)
+            c.operator = op
+            c.reset_path()
+            c.translate(25, 25)
+            _poly(c, [(0, 0), (75, 0), (75, 75), (0, 75)])
+            c.fill()
+            assert be.composite(s, 10 + 110 * j, 10 + 110 * i, [Operation("src_over", src=scratch)]) == abi.OK
+    return s
+
+
 # ------------------------------------------------------------- stroke scenes
 def _stroke_canvas(be, aa, w, h):
     s = Surface.init("rgb", w, h)
@@ -1751,6 +1775,7 @@ FILL_SCENES = {
     "066_conic_pie_gradient": s066_conic_pie_gradient,
     "067_gradient_transforms": s067_gradient_transforms,
     "069_gradient_dither_context": s069_gradient_dither_context,
+    "070_compositor_ops": s070_compositor_ops,
 }
 
 COMPOSITOR_SCENES = {
