@@ -622,6 +622,20 @@ def s070_compositor_ops(be, aa):
     return s
 
 
+def s059_stroke_star_gradient(be, aa):
+    w = h = 300
+    s = Surface.init("rgb", w, h)
+    c = Ctx(be, s)
+    c.aa = aa
+    c.line_width = 10
+    c.line_join = "round"
+    m, xs, ys = 20, 3, 5
+    c.set_source_pattern(Pattern.from_gradient(_rgb_stops(Gradient.linear(m * 3, h // 2, w - m * 3, h // 2))))
+    _poly(c, [(w // 2, m), (w - m * xs - 1, h - m - 1), (m, m * ys), (w - m - 1, m * ys), (m * xs, h - m - 1)])
+    c.stroke()
+    return s
+
+
 # ------------------------------------------------------------- stroke scenes
 def _stroke_canvas(be, aa, w, h):
     s = Surface.init("rgb", w, h)
@@ -1734,6 +1748,7 @@ STROKE_SCENES = {
     "040_stroke_corner_symmetrical": s040_stroke_corner_symmetrical,
     "041_stroke_noop_lineto": s041_stroke_noop_lineto,
     "058_stroke_misc_dashes": s058_stroke_misc_dashes,
+    "059_stroke_star_gradient": s059_stroke_star_gradient,
     "073_stroke_sameclose": s073_stroke_sameclose,
     "075_oob_draw_corners": s075_oob_draw_corners,
     "076_oob_draw_sides": s076_oob_draw_sides,
