@@ -221,7 +221,7 @@ typedef struct z2d_stroke_opts {
     int32_t line_cap;          /* Z2D_CAP_* */
     int32_t op;                /* Z2D_OP_* */
     int32_t precision;         /* Z2D_PRECISION_* */
-    int32_t hairline;          /* nonzero: hairline mode (not supported yet) */
+    int32_t hairline;          /* nonzero: hairline mode (1-pixel Bresenham / Wu lines) */
     double line_width;
     double miter_limit;
     double tolerance;
@@ -302,9 +302,9 @@ Z2D_API int z2dgpu_fill_batch(z2dgpu_ctx *ctx, z2d_surface *surface,
 /* painter.stroke (src/painter.zig:214-344): the stroke polygon z2d's stroke
  * plotter builds (joins, caps, pens, dashes), filled with the non-zero rule
  * by the GPU rasterisers.  Solid strokes are tessellated on the device;
- * dashed ones on the host.  Hairline mode returns Z2D_ERR_INVALID_ARGUMENT
- * (not supported yet); a transformation that cannot be inverted also
- * returns Z2D_ERR_INVALID_ARGUMENT (Transformation.Error.InvalidMatrix); a
+ * dashed ones on the host; hairlines are drawn by the hairline rasteriser
+ * (hairline.zig).  A transformation that cannot be inverted returns
+ * Z2D_ERR_INVALID_ARGUMENT (Transformation.Error.InvalidMatrix); a
  * line_to / curve_to without a current point or a non-finite coordinate
  * returns Z2D_ERR_INVALID_STATE. */
 Z2D_API int z2dgpu_stroke(z2dgpu_ctx *ctx, z2d_surface *surface,
@@ -313,7 +313,8 @@ Z2D_API int z2dgpu_stroke(z2dgpu_ctx *ctx, z2d_surface *surface,
 
 /* Host only (no device work): the polygon painter.stroke would rasterise
  * for a surface of `surface_format`, as closed contours of points already
- * multiplied by the rasteriser scale (written to *scale).  points receives
+ * multiplied by the rasteriser scale (written to *scale).  For hairline
+ * strokes: the open polylines of polyline_plotter, scale 1.  points receives
  * x, y pairs, contour_ends[k] the index one past contour k's last point.
  * The counts are returned even when the capacities are too small. */
 Z2D_API int z2dgpu_stroke_contours(const z2d_node *nodes, size_t n_nodes,
