@@ -323,6 +323,26 @@ Z2D_API int z2dgpu_stroke_contours(const z2d_node *nodes, size_t n_nodes,
                                    uint64_t *contour_ends, size_t cap_contours,
                                    uint64_t *n_contours, double *scale);
 
+/* ---- PNG export (src/export_png.zig) ---- */
+enum { Z2D_PROFILE_NONE = -1, Z2D_PROFILE_LINEAR = 0, Z2D_PROFILE_SRGB = 1 };
+/* png_exporter.writeToPNGFile (export_png.zig:56-87) to memory: the PNG file
+ * of a surface (host or device memory) with the exporter's encoding
+ * (demultiplied RGBA/RGB, alpha as grayscale, packed alpha4/2/1), a gAMA
+ * chunk and the sRGB gamma on the pixels when color_profile asks for them.
+ * The bytes are allocated by the library: *out, *out_len; release them with
+ * z2dgpu_free.  The IDAT stream is zlib's default compression where the
+ * library was built with zlib, stored deflate blocks otherwise (the decoded
+ * image is the same). */
+Z2D_API int z2dgpu_png_encode(z2dgpu_ctx *ctx, const z2d_surface *surface, int32_t color_profile, uint8_t **out,
+                              size_t *out_len);
+/* The PNG's uncompressed image data: per row a filter byte (0) followed by
+ * the row's encoded pixels (writePNGIDATStream, export_png.zig:153-311).
+ * Allocated like z2dgpu_png_encode's output. */
+Z2D_API int z2dgpu_png_scanlines(z2dgpu_ctx *ctx, const z2d_surface *surface, int32_t color_profile, uint8_t **out,
+                                 size_t *out_len);
+/* Releases memory the library returned. */
+Z2D_API void z2dgpu_free(void *p);
+
 /* Many independent surfaces in one device pass: for every job, the
  * equivalent of calling painter.fill for its commands in order on its
  * surface (z2d's callers loop over surfaces; there is no batch call in z2d

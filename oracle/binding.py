@@ -55,6 +55,9 @@ def load_oracle():
                                                C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.c_size_t, C.c_int32,
                                                C.c_int32, C.c_int32]
             lib.z2doracle_hairline.restype = C.c_int
+            lib.z2doracle_png_scanlines.argtypes = [C.POINTER(abi.z2d_surface), C.c_int32, C.c_void_p, C.c_size_t,
+                                                    C.POINTER(C.c_size_t)]
+            lib.z2doracle_png_scanlines.restype = C.c_int
             lib.z2doracle_composite.argtypes = [C.POINTER(abi.z2d_surface), C.c_int32, C.c_int32, C.c_int32,
                                                 C.POINTER(abi.z2d_operation), C.c_int32]
             lib.z2doracle_composite.restype = C.c_int
@@ -130,6 +133,20 @@ class Oracle:
                                            {"none": abi.AA_NONE, "default": abi.AA_DEFAULT,
                                             "multisample_4x": abi.AA_MULTISAMPLE_4X,
                                             "supersample_4x": abi.AA_SUPERSAMPLE_4X}[anti_aliasing])
+
+    def png_scanlines(self, surface, profile=None) -> bytes:
+        """The PNG exporter's uncompressed image data for `surface`
+        (profile None, "linear" or "srgb")."""
+        import numpy as np
+        s = _host_abi(surface)
+        pr = {None: -1, "linear": 0, "srgb": 1}[profile]
+        n = C.c_size_t()
+        rc = self.lib.z2doracle_png_scanlines(C.byref(s), pr, None, 0, C.byref(n))
+        if rc:
+            raise RuntimeError(f"z2doracle_png_scanlines: {rc}")
+        out = np.zeros(max(1, n.value), np.uint8)
+        self.lib.z2doracle_png_scanlines(C.byref(s), pr, out.ctypes.data, n.value, C.byref(n))
+        return out[:n.value].tobytes()
 
     def composite(self, dst, dst_x: int, dst_y: int, ops, precision: str = "integer") -> int:
         keep: list = []

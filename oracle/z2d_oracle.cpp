@@ -1979,6 +1979,65 @@ __attribute__((visibility("default"))) int z2doracle_hairline(z2d_surface *surfa
     return Z2D_OK;
 }
 
+// ===================================================================
+// PNG scanlines                     src/export_png.zig:153-372
+// ===================================================================
+// The unfiltered image data writeToPNGFile compresses: per row a 0 filter
+// byte, then the row's pixels as writePNGIDATStream encodes them.
+// `profile`: -1 none, 0 linear, 1 sRGB (gamma applied by encodeRGBAVec).
+// Writes at most `cap` bytes to `out`; returns the full size in *len.
+__attribute__((visibility("default"))) int z2doracle_png_scanlines(const z2d_surface *surface, int32_t profile,
+                                                                   uint8_t *out, size_t cap, size_t *len) {
+    if (!surface || !len) return Z2D_ERR_INVALID_ARGUMENT;
+    if (surface->width < 1 || surface->height < 1) return Z2D_ERR_INVALID_DIMENSIONS;
+    const Sfc s = sfc_from_abi(surface);
+    const bool wide = s.fmt == Z2D_FORMAT_RGBA || s.fmt == Z2D_FORMAT_ARGB || s.fmt == Z2D_FORMAT_RGB ||
+                      s.fmt == Z2D_FORMAT_XRGB;
+    const bool alpha = s.fmt == Z2D_FORMAT_RGBA || s.fmt == Z2D_FORMAT_ARGB;
+    const size_t bits = wide ? (alpha ? 32 : 24) : (size_t)fmt_bits(s.fmt);
+    const size_t row_bytes = 1 + ((size_t)s.w * bits + 7) / 8;
+    *len = row_bytes * (size_t)s.h;
+    std::vector<uint8_t> row(row_bytes);
+    for (int32_t y = 0; y < s.h; y++) {
+        std::fill(row.begin(), row.end(), 0);
+        for (int32_t x = 0; x < s.w; x++) {
+            const Px p = raw_get(s, (size_t)s.w * y + x);
+            if (wide) {  // encodeRGBAVec
+                uint32_t r = p.r, g = p.g, b = p.b, a = alpha ? p.a : 255;
+                if (alpha) {  // RGBA16.demultiply
+                    r = a == 0 ? 0 : r * 255 / std::max(1u, a);
+                    g = a == 0 ? 0 : g * 255 / std::max(1u, a);
+                    b = a == 0 ? 0 : b * 255 / std::max(1u, a);
+                }
+                if (profile == 1) {  // decodeRGBAVecRaw, applyGammaVec, encodeRGBAVecRaw
+                    auto enc = [](uint32_t c, bool gamma) {
+                        float v = (float)c / 255.0f;
+                        if (gamma) v = zpow(v, kInvGamma);
+                        return (uint32_t)std::round(255.0f * v);
+                    };
+                    r = enc(r, true);
+                    g = enc(g, true);
+                    b = enc(b, true);
+                    a = enc(a, false);
+                }
+                uint8_t *o = row.data() + 1 + (size_t)x * (alpha ? 4 : 3);
+                o[0] = (uint8_t)r;
+                o[1] = (uint8_t)g;
+                o[2] = (uint8_t)b;
+                if (alpha) o[3] = (uint8_t)a;
+            } else if (s.fmt == Z2D_FORMAT_ALPHA8) {
+                row[1 + (size_t)x] = p.a;
+            } else {  // most significant bits first
+                const int nb = fmt_bits(s.fmt), per = 8 / nb;
+                row[1 + (size_t)x / per] |= (uint8_t)(p.a << (8 - nb - (x % per) * nb));
+            }
+        }
+        const size_t at = row_bytes * (size_t)y;
+        if (out && at < cap) memcpy(out + at, row.data(), std::min(row_bytes, cap - at));
+    }
+    return Z2D_OK;
+}
+
 // The rasterisers of painter.fill / painter.stroke on a polygon given as
 // closed contours of already-scaled points (Polygon.addEdgesFromContour,
 // Polygon.zig:115-139, with the polygon's own scale of 1), as

@@ -67,6 +67,26 @@ def read_png(path: str):
     return w, h, depth, ctype, rows
 
 
+def png_chunks(data: bytes):
+    """(type, body) of every chunk, checking each CRC."""
+    assert data[:8] == b"\x89PNG\r\n\x1a\n", "not a PNG"
+    pos, out = 8, []
+    while pos < len(data):
+        (ln,) = struct.unpack(">I", data[pos:pos + 4])
+        typ, body = data[pos + 4:pos + 8], data[pos + 8:pos + 8 + ln]
+        (crc,) = struct.unpack(">I", data[pos + 8 + ln:pos + 12 + ln])
+        assert zlib.crc32(typ + body) & 0xFFFFFFFF == crc, f"bad CRC in {typ}"
+        out.append((typ, body))
+        pos += 12 + ln
+    return out
+
+
+def golden_scanlines(path: str) -> bytes:
+    """The PNG's decompressed image data (filter bytes included)."""
+    chunks = png_chunks(open(path, "rb").read())
+    return zlib.decompress(b"".join(body for typ, body in chunks if typ == b"IDAT"))
+
+
 def golden_pixels(path: str) -> np.ndarray:
     """Decoded golden as (h, w, c) uint8 values (c = 1 for grey)."""
     w, h, depth, ctype, rows = read_png(path)

@@ -636,6 +636,55 @@ def s059_stroke_star_gradient(be, aa):
     return s
 
 
+def _gamma_scene(be, aa=None):
+    """spec/071_gamma_linear.zig and 072_gamma_srgb.zig (the same drawing,
+    exported with the linear or the sRGB profile)."""
+    W, H = 400, 300
+    s = Surface.init("rgb", W, H)
+    c = Ctx(be, s)
+    c.aa = "none"
+
+    def gray(pos, profile):
+        col = Color.rgb(0.3, 0.3, 0.3) if profile == "linear" else Color.srgb(0.3, 0.3, 0.3)
+        c.set_source(Pixel.from_color(col))
+        c.translate(0, pos * H / 2)
+        _poly(c, [(0, 0), (W, 0), (W, H // 2), (0, H // 2)])
+        c.set_identity()
+        c.fill()
+        c.reset_path()
+
+    def gradient(pos, stop_profile, method):
+        mk = Color.rgb if stop_profile == "linear" else Color.srgb
+        off = 30.0
+        gw, gh = W - off * 2, (H - off * 2) / 4
+        g = Gradient.linear(0, gh / 2, gw, gh / 2, method=method)
+        g.add_stop(0, mk(0.80, 0, 0))
+        g.add_stop(0.5, mk(0, 0.80, 0))
+        g.add_stop(1, mk(0, 0, 0.80))
+        c.translate(off, off + gh * pos)
+        c.set_source_pattern(Pattern.from_gradient(g))
+        _poly(c, [(0, 0), (gw, 0), (gw, gh), (0, gh)])
+        c.set_identity()
+        c.fill()
+        c.reset_path()
+        c.set_source(Pixel.rgb(0, 0, 0))
+
+    gray(0, "linear")
+    gray(1, "srgb")
+    gradient(0, "linear", "linear_rgb")
+    gradient(1, "srgb", "linear_rgb")
+    gradient(2, "linear", "srgb")
+    gradient(3, "srgb", "srgb")
+    return s
+
+
+# scenes whose goldens carry a colour profile: name -> (scene, profile)
+EXPORT_SCENES = {
+    "071_gamma_linear": (_gamma_scene, "linear"),
+    "072_gamma_srgb": (_gamma_scene, "srgb"),
+}
+
+
 # ------------------------------------------------------------- stroke scenes
 def _stroke_canvas(be, aa, w, h):
     s = Surface.init("rgb", w, h)

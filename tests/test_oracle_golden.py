@@ -6,9 +6,9 @@ import os
 import numpy as np
 import pytest
 
-from pngio import export_pixels, golden_pixels
+from pngio import export_pixels, golden_pixels, golden_scanlines
 from backends import StrokeOracle
-from scenes import AA_SUFFIX, COMPOSITOR_SCENES, FILL_SCENES, STROKE_SCENES
+from scenes import AA_SUFFIX, COMPOSITOR_SCENES, EXPORT_SCENES, FILL_SCENES, STROKE_SCENES
 from z2d_gb300.types import Color, Pixel
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -61,3 +61,22 @@ def test_compositor_kat(oracle, prec, idx, case):
     r = oracle.run_pixel(prec, Pixel(bg.format, bg.r, bg.g, bg.b, bg.a),
                          Pixel(fg.format, fg.r, fg.g, fg.b, fg.a), case["op"])
     assert [r.r, r.g, r.b, r.a] == case["expected"]
+
+
+@pytest.mark.parametrize("aa", list(AA_SUFFIX))
+@pytest.mark.parametrize("name", sorted(list(FILL_SCENES) + list(STROKE_SCENES)))
+def test_png_scanlines_match_golden(oracle, golden_dir, name, aa):
+    """The exporter's uncompressed image data (export_png.zig:153-372) of the
+    oracle's render equals the golden PNG's, byte for byte."""
+    path = os.path.join(golden_dir, name + AA_SUFFIX[aa] + ".png")
+    if not os.path.exists(path):
+        path = os.path.join(golden_dir, name + "_smooth.png")
+    scene = FILL_SCENES.get(name) or STROKE_SCENES[name]
+    assert oracle.png_scanlines(scene(StrokeOracle(oracle), aa)) == golden_scanlines(path)
+
+
+@pytest.mark.parametrize("name", sorted(list(COMPOSITOR_SCENES) + list(EXPORT_SCENES)))
+def test_png_scanlines_match_golden_compositor(oracle, golden_dir, name):
+    scene, profile = EXPORT_SCENES.get(name, (COMPOSITOR_SCENES.get(name), None))
+    assert oracle.png_scanlines(scene(StrokeOracle(oracle)), profile) == \
+        golden_scanlines(os.path.join(golden_dir, name + ".png"))

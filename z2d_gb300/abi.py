@@ -148,5 +148,7 @@ EXPORTED_SYMBOLS = [
     "z2dgpu_stroke_contours",
     "z2dgpu_composite",
     "z2dgpu_composite_noalloc", "z2dgpu_server_create", "z2dgpu_server_submit", "z2dgpu_server_wait",
-    "z2dgpu_server_stats", "z2dgpu_server_destroy",
+    "z2dgpu_server_stats", "z2dgpu_server_destroy", "z2dgpu_png_encode", "z2dgpu_png_scanlines", "z2dgpu_free",
 ]
+
+PROFILE = {None: -1, "linear": 0, "srgb": 1}  # color.RGBProfile of the PNG exporter

@@ -1259,6 +1259,44 @@ Z2D_API int z2dgpu_stroke_contours(const z2d_node *nodes, size_t n_nodes, const 
     return Z2D_OK;
 }
 
+static int png_common(z2dgpu_ctx *c, const z2d_surface *surface, int32_t profile, bool file, uint8_t **out,
+                      size_t *out_len) {
+    if (!c || !out || !out_len) return Z2D_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    *out_len = 0;
+    int rc = check_surface(surface);
+    if (rc) return rc;
+    if (profile != Z2D_PROFILE_NONE && profile != Z2D_PROFILE_LINEAR && profile != Z2D_PROFILE_SRGB) {
+        set_error("png: bad color profile");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    Z2D_CUDA(cudaSetDevice(c->device));
+    DevSurface ds;
+    rc = stage_in(*c, *surface, c->surface, ds);
+    if (rc) return rc;
+    std::vector<uint8_t> bytes;
+    rc = file ? png_file(*c, ds, profile, bytes) : png_scanlines(*c, ds, profile, bytes);
+    if (rc) return rc;
+    uint8_t *p = static_cast<uint8_t *>(malloc(std::max<size_t>(1, bytes.size())));
+    if (!p) return Z2D_ERR_OUT_OF_MEMORY;
+    if (!bytes.empty()) memcpy(p, bytes.data(), bytes.size());
+    *out = p;
+    *out_len = bytes.size();
+    return Z2D_OK;
+}
+
+Z2D_API int z2dgpu_png_encode(z2dgpu_ctx *c, const z2d_surface *surface, int32_t color_profile, uint8_t **out,
+                              size_t *out_len) {
+    return png_common(c, surface, color_profile, true, out, out_len);
+}
+
+Z2D_API int z2dgpu_png_scanlines(z2dgpu_ctx *c, const z2d_surface *surface, int32_t color_profile, uint8_t **out,
+                                 size_t *out_len) {
+    return png_common(c, surface, color_profile, false, out, out_len);
+}
+
+Z2D_API void z2dgpu_free(void *p) { free(p); }
+
 Z2D_API int z2dgpu_draw_jobs(z2dgpu_ctx *c, const z2d_job *jobs, size_t n_jobs, const z2d_node *nodes, size_t n_nodes,
                              const z2d_draw_cmd *cmds, size_t n_cmds) {
     if (!c) return Z2D_ERR_INVALID_ARGUMENT;

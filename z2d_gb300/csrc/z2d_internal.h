@@ -84,6 +84,13 @@ struct Ctx {
 
 }  // namespace z2dg
 
+namespace z2dg {
+// The PNG exporter (png.cu): the unfiltered scanline stream of a device
+// surface as export_png.zig encodes it, and the whole PNG file.
+int png_scanlines(Ctx &c, const DevSurface &s, int profile, std::vector<uint8_t> &raw);
+int png_file(Ctx &c, const DevSurface &s, int profile, std::vector<uint8_t> &png);
+}  // namespace z2dg
+
 // The opaque handle of include/z2dgpu.h is a context.
 struct z2dgpu_ctx : public z2dg::Ctx {};
 

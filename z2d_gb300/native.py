@@ -90,6 +90,12 @@ def load(build_if_missing: bool = True):
         lib.z2dgpu_server_wait.argtypes = [C.c_void_p, C.c_uint64, C.c_int32, P(C.c_double)]
         lib.z2dgpu_server_stats.argtypes = [C.c_void_p, P(C.c_uint64), P(C.c_uint64), P(C.c_double)]
         lib.z2dgpu_server_destroy.argtypes = [C.c_void_p]
+        for name in ("z2dgpu_png_encode", "z2dgpu_png_scanlines"):
+            getattr(lib, name).argtypes = [C.c_void_p, P(abi.z2d_surface), C.c_int32, P(P(C.c_uint8)),
+                                           P(C.c_size_t)]
+            getattr(lib, name).restype = C.c_int
+        lib.z2dgpu_free.argtypes = [C.c_void_p]
+        lib.z2dgpu_free.restype = None
         for name in ("z2dgpu_server_create", "z2dgpu_server_submit", "z2dgpu_server_wait", "z2dgpu_server_stats",
                      "z2dgpu_server_destroy"):
             getattr(lib, name).restype = C.c_int

@@ -70,11 +70,17 @@ class Pixel:
 
     @staticmethod
     def from_color(color: "Color") -> "Pixel":
-        """Pixel.fromColor (src/pixel.zig:119-121) for linear RGB colors:
-        round(255 x) then integer premultiply (src/color.zig:272-289)."""
-        if color.space != abi.COLOR_LINEAR_RGB:
-            raise NotImplementedError("from_color: only linear RGB colors are converted host-side")
-        v = [int(math.floor(float(np.float32(255.0) * np.float32(c)) + 0.5)) for c in color.c]
+        """Pixel.fromColor (src/pixel.zig:119-121) for linear and sRGB colors:
+        sRGB gamma removed (pow 2.2, rounded to f32), round(255 x), then
+        integer premultiply (src/color.zig:272-289)."""
+        if color.space == abi.COLOR_SRGB:  # SRGB.removeGamma: pow(x, 2.2) in f32
+            lin = [float(np.float32(math.pow(float(c), float(np.float32(2.2))))) if c not in (0.0, 1.0) else c
+                   for c in color.c[:3]] + [color.c[3]]
+        elif color.space == abi.COLOR_LINEAR_RGB:
+            lin = list(color.c)
+        else:
+            raise NotImplementedError("from_color: HSL colors are not converted host-side")
+        v = [int(math.floor(float(np.float32(255.0) * np.float32(c)) + 0.5)) for c in lin]
         r, g, b, a = v
         return Pixel.rgba(r * a // 255, g * a // 255, b * a // 255, a)
 
