@@ -444,8 +444,10 @@ def jobs_arm(ctx, stream, dev, steps=3):
     for _ in range(steps):
         restore()
         t0 = time.perf_counter()
+        torch.cuda.nvtx.range_push("jobs_step")  # lets a profiler select these launches
         pb.draw_jobs(ctx)
         stream.synchronize()
+        torch.cuda.nvtx.range_pop()
         walls.append(time.perf_counter() - t0)
     stage_ms = {k: ctx.kernel_ms(k)[0] / steps for k in ("flatten", "stroke", "bins", "raster")}
     ctx.set_timing(False)
@@ -561,6 +563,33 @@ def jobs_arm(ctx, stream, dev, steps=3):
 
 SERVE_RATES = (5000, 20000, 50000)  # requests per second (Poisson arrivals)
 SERVE_SECONDS = 1.5                 # arrival window per rate
+
+
+def png_arm(ctx, surf, peak_gbs):
+    """PNG export of the benchmark's 4096x4096 RGBA surface (device
+    resident, as the batched arm leaves it): the exporter's encoding kernel
+    k_png_rows (4 B read and 4 B written per pixel, plus a filter byte per
+    row) timed with CUDA events (the context's "export" stage), and the
+    whole file: device encoding, copy back and zlib on the host."""
+    from z2d_gb300 import png
+    import torch
+    reps = 5
+    png.scanlines(surf, None, ctx)  # warm
+    ctx.set_timing(True)
+    for _ in range(reps):
+        torch.cuda.nvtx.range_push("png_export")
+        png.scanlines(surf, None, ctx)
+        torch.cuda.nvtx.range_pop()
+    ms = ctx.kernel_ms("export")[0] / reps
+    ctx.set_timing(False)
+    t0 = time.perf_counter()
+    data = png.encode(surf, None, ctx)
+    file_s = time.perf_counter() - t0
+    alg = W * H * 4 + H * (1 + 4 * W)
+    gbs = alg / (ms / 1e3) / 1e9
+    return {"kernel": "k_png_rows", "kernel_ms": ms, "alg_bytes": alg, "gbs": gbs, "frac_of_measured_hbm": gbs / peak_gbs,
+            "file_ms": file_s * 1e3, "png_bytes": len(data), "file_mpix_s": W * H / 1e6 / file_s,
+            "note": "file = device encoding + copy back + zlib default level on one host thread"}
 
 
 def serving_arm(dev):
@@ -812,7 +841,7 @@ def run_ours(args):
     raster_ms_per = raster_ms / max(raster_n, 1)
     achieved = alg_bytes / (raster_ms_per / 1e3) / 1e9
     arms = set(args.arms.split(",")) if args.arms not in ("all", "") else {"compositor", "breadth", "star", "jobs",
-                                                                            "serving", "cpu"}
+                                                                            "serving", "cpu", "png"}
     comp = comp_roof = star = jobs = None
     if "compositor" in arms:
         comp = compositor_sweep(ctx, stream, dev)
@@ -827,6 +856,7 @@ def run_ours(args):
         star = star_latency(ctx, dev)
     if "jobs" in arms:
         jobs = jobs_arm(ctx, stream, dev)
+    png_res = png_arm(ctx, surf, peaks["hbm_gbs"]) if "png" in arms else None
     serving = serving_arm(dev) if "serving" in arms else None
     cpu_v, cpu_dt = cpu_sample(bg, fills, px, CPU_SAMPLE_FILLS) if "cpu" in arms else (None, 0.0)
     line = {
@@ -846,6 +876,7 @@ def run_ours(args):
         "star_300": star,
         "jobs": jobs,
         "serving": serving,
+        "png": png_res,
         "batched_over_plain": (mpix_step / (total_ms / args.steps / 1e3)) / (plain_mpix / (plain_ms / 1e3)),
         "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": "k_raster", "achieved": achieved, "peak": peaks["hbm_gbs"],
@@ -872,8 +903,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--arms", default="all",
                     help="extra arms beside the batched / e2e / per-call fill arms: 'all', 'none' or a comma "
-                         "list of compositor, breadth, star, jobs, serving, cpu (shorter runs for profiling)")
+                         "list of compositor, breadth, star, jobs, serving, cpu, png (shorter runs for profiling)")
+    ap.add_argument("--jobs", type=int, default=4096,
+                    help="surfaces of the batched-jobs arm (smaller for profiling captures)")
     args = ap.parse_args()
+    globals()["N_JOBS"] = args.jobs
     if args.impl == "reference":
         run_reference(args)
     else:

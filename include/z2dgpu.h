@@ -276,9 +276,9 @@ Z2D_API int z2dgpu_ctx_set_timing(z2dgpu_ctx *ctx, int enable);
 /* Accumulated milliseconds and launch count of a stage since timing was
  * enabled: "raster" (k_raster), "composite" (compositor kernels), "flatten"
  * (path flattening, stroking and fill setup, two intervals per fill call),
- * "stroke" (the stroke kernels, a share of "flatten") or "bins" (edge
- * binning, band lists and the exact path).  Returns -1 for an unknown
- * name. */
+ * "stroke" (the stroke kernels, a share of "flatten"), "bins" (edge
+ * binning, band lists and the exact path) or "export" (the PNG encoding
+ * kernel).  Returns -1 for an unknown name. */
 Z2D_API double z2dgpu_ctx_kernel_ms(z2dgpu_ctx *ctx, const char *kernel, uint64_t *launches);
 
 /* Bytes of pixel storage for a surface (src/surface.zig:382-395, 621-635). */

@@ -1172,7 +1172,7 @@ Z2D_API int z2dgpu_ctx_destroy(z2dgpu_ctx *c) {
     for (DevBuf *b : bufs) b->release();
     c->staging.release();
     c->readback.release();
-    for (Ctx::Timer *t : {&c->t_raster, &c->t_composite, &c->t_flatten, &c->t_bins, &c->t_stroke}) c->timer_collect(*t);
+    for (Ctx::Timer *t : {&c->t_raster, &c->t_composite, &c->t_flatten, &c->t_bins, &c->t_stroke, &c->t_export}) c->timer_collect(*t);
     if (c->own_stream) cudaStreamDestroy(c->stream);
     delete c;
     return Z2D_OK;
@@ -1188,7 +1188,7 @@ Z2D_API uint64_t z2dgpu_ctx_launch_count(const z2dgpu_ctx *c) { return c ? c->la
 
 Z2D_API int z2dgpu_ctx_set_timing(z2dgpu_ctx *c, int enable) {
     if (!c) return Z2D_ERR_INVALID_ARGUMENT;
-    for (Ctx::Timer *t : {&c->t_raster, &c->t_composite, &c->t_flatten, &c->t_bins, &c->t_stroke}) {
+    for (Ctx::Timer *t : {&c->t_raster, &c->t_composite, &c->t_flatten, &c->t_bins, &c->t_stroke, &c->t_export}) {
         c->timer_collect(*t);
         *t = Ctx::Timer{};
     }
@@ -1204,6 +1204,7 @@ Z2D_API double z2dgpu_ctx_kernel_ms(z2dgpu_ctx *c, const char *kernel, uint64_t 
     else if (strcmp(kernel, "flatten") == 0) t = &c->t_flatten;
     else if (strcmp(kernel, "bins") == 0) t = &c->t_bins;
     else if (strcmp(kernel, "stroke") == 0) t = &c->t_stroke;
+    else if (strcmp(kernel, "export") == 0) t = &c->t_export;
     if (!t) return -1.0;
     c->timer_collect(*t);
     if (launches) *launches = t->n;

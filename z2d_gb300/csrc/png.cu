@@ -171,8 +171,10 @@ int png_scanlines(Ctx &c, const DevSurface &s, int profile, std::vector<uint8_t>
     uint8_t *d = c.surface2.as<uint8_t>();
     const long long n_units = units * s.h;
     if (n_units > 0) {
+        cudaEvent_t te = c.timer_begin(c.t_export);
         k_png_rows<<<(unsigned)((n_units + 255) / 256), 256, 0, c.stream>>>(s, profile == Z2D_PROFILE_SRGB ? 1 : 0, d,
                                                                           row_bytes, units, n_units);
+        c.timer_end(c.t_export, te);
         c.launches++;
     }
     raw.resize(total);

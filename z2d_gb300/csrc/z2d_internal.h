@@ -76,7 +76,7 @@ struct Ctx {
         std::vector<cudaEvent_t> pending;  // start/stop pairs not yet read
         double ms = 0;
         uint64_t n = 0;
-    } t_raster, t_composite, t_flatten, t_bins, t_stroke;
+    } t_raster, t_composite, t_flatten, t_bins, t_stroke, t_export;
     cudaEvent_t timer_begin(Timer &t);
     void timer_end(Timer &t, cudaEvent_t start);
     void timer_collect(Timer &t);
