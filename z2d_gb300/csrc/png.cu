@@ -18,8 +18,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #ifdef Z2D_HAVE_ZLIB
@@ -45,7 +47,15 @@ __global__ void k_png_rows(DevSurface s, int srgb, uint8_t *__restrict__ out, lo
                            long long units_per_row, long long n_units) {
     const long long u = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= n_units) return;
-    const long long y = u / units_per_row, k = u % units_per_row;
+    long long y, k;
+    if (n_units <= 0xFFFFFFFFll) {  // 32-bit division where it is enough
+        const uint32_t uu = (uint32_t)u, up = (uint32_t)units_per_row;
+        y = uu / up;
+        k = uu - (uint32_t)y * up;
+    } else {
+        y = u / units_per_row;
+        k = u - y * units_per_row;
+    }
     uint8_t *row = out + y * row_bytes;
     if (k == 0) row[0] = 0;  // filter type: none
     const int fmt = s.fmt;
@@ -55,10 +65,12 @@ __global__ void k_png_rows(DevSurface s, int srgb, uint8_t *__restrict__ out, lo
         uint32_t r = p.r, g = p.g, b = p.b, a = p.a;
         const bool has_alpha = fmt == Z2D_FORMAT_RGBA || fmt == Z2D_FORMAT_ARGB;
         if (has_alpha) {  // RGBA16.demultiply (pixel_vector.zig:27-60)
-            const uint32_t den = a > 1u ? a : 1u;
-            r = a == 0 ? 0 : r * 255u / den;
-            g = a == 0 ? 0 : g * 255u / den;
-            b = a == 0 ? 0 : b * 255u / den;
+            // x / a as umulhi(x, ceil(2^32 / a)): exact for x <= 255 * 255
+            // (the error x / 2^32 stays below 1 / a)
+            const uint32_t m = a > 1u ? 0xFFFFFFFFu / a + 1u : 0u;
+            r = a == 0 ? 0 : (a == 1 ? r * 255u : __umulhi(r * 255u, m));
+            g = a == 0 ? 0 : (a == 1 ? g * 255u : __umulhi(g * 255u, m));
+            b = a == 0 ? 0 : (a == 1 ? b * 255u : __umulhi(b * 255u, m));
         } else {
             a = 255;
         }
@@ -124,14 +136,52 @@ void chunk(std::vector<uint8_t> &o, const char type[4], const uint8_t *data, siz
     put32(o, crc_table().update(0, o.data() + at, n + 4));
 }
 
-// A zlib stream of `raw` (RFC 1950/1951): zlib's default compression when the
-// library was found at build time, stored blocks otherwise.
+// A zlib stream of `raw` (RFC 1950/1951): zlib's default compression level
+// when the library was found at build time (pieces compressed on all host
+// threads), stored blocks otherwise.
 bool zlib_stream(const uint8_t *raw, size_t n, std::vector<uint8_t> &out) {
 #ifdef Z2D_HAVE_ZLIB
-    uLongf len = compressBound((uLong)n);
-    out.resize(len);
-    if (compress2(out.data(), &len, raw, (uLong)n, Z_DEFAULT_COMPRESSION) != Z_OK) return false;
-    out.resize(len);
+    // Pieces of the data are deflated in parallel, each a raw deflate stream
+    // ending on a byte boundary (a sync flush; the last piece finishes the
+    // stream), so that their concatenation is one valid deflate stream.
+    const size_t nt = std::max(1u, std::thread::hardware_concurrency());
+    const size_t piece = std::max<size_t>((size_t)1 << 20, (n + nt - 1) / nt);
+    const size_t n_pieces = std::max<size_t>(1, (n + piece - 1) / piece);
+    std::vector<std::vector<uint8_t>> parts(n_pieces);
+    std::vector<int> ok(n_pieces, 0);
+    std::atomic<size_t> next{0};
+    auto work = [&] {
+        for (size_t k; (k = next.fetch_add(1)) < n_pieces;) {
+            const size_t a = k * piece, m = std::min(piece, n - a);
+            z_stream z;
+            memset(&z, 0, sizeof(z));
+            if (deflateInit2(&z, Z_DEFAULT_COMPRESSION, Z_DEFLATED, -15, 8, Z_DEFAULT_STRATEGY) != Z_OK) continue;
+            std::vector<uint8_t> &o = parts[k];
+            o.resize(deflateBound(&z, (uLong)m) + 16);
+            z.next_in = const_cast<Bytef *>(raw + a);
+            z.avail_in = (uInt)m;
+            z.next_out = o.data();
+            z.avail_out = (uInt)o.size();
+            const int r = deflate(&z, k + 1 == n_pieces ? Z_FINISH : Z_SYNC_FLUSH);
+            ok[k] = (k + 1 == n_pieces ? r == Z_STREAM_END : r == Z_OK) && z.avail_in == 0;
+            o.resize(o.size() - z.avail_out);
+            deflateEnd(&z);
+        }
+    };
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < std::min(nt, n_pieces); t++) pool.emplace_back(work);
+    work();
+    for (auto &t : pool) t.join();
+    out.clear();
+    out.push_back(0x78);  // zlib header: deflate, 32 KiB window, default level
+    out.push_back(0x9C);
+    for (size_t k = 0; k < n_pieces; k++) {
+        if (!ok[k]) return false;
+        out.insert(out.end(), parts[k].begin(), parts[k].end());
+    }
+    uLong ad = adler32(0L, Z_NULL, 0);
+    for (size_t i = 0; i < n; i += (size_t)1 << 30) ad = adler32(ad, raw + i, (uInt)std::min(n - i, (size_t)1 << 30));
+    put32(out, (uint32_t)ad);
     return true;
 #else
     out.clear();
