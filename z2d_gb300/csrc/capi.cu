@@ -1168,7 +1168,7 @@ Z2D_API int z2dgpu_ctx_destroy(z2dgpu_ctx *c) {
     cudaStreamSynchronize(c->stream);
     DevBuf *bufs[] = {&c->params, &c->nodes, &c->node_info, &c->edges, &c->fill_state, &c->counters, &c->band_fills,
                       &c->bins, &c->bin_offsets, &c->masks, &c->surface, &c->surface2, &c->surface3, &c->scan_tmp,
-                      &c->stroke_a, &c->stroke_b, &c->stroke_c};
+                      &c->stroke_a, &c->stroke_b, &c->stroke_c, &c->curve_pool};
     for (DevBuf *b : bufs) b->release();
     c->staging.release();
     c->readback.release();

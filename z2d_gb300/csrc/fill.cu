@@ -346,9 +346,18 @@ __device__ __forceinline__ int warp_excl_sum(int v, int lane, int &total) {
 // curve start (consecutive leaves share their end points, so the lineTo
 // sequence start, a1, a2, ..., d is the chord sequence), and every item has
 // fewer than 65536 leaves.
+// Each lane also keeps the start points of the leaves it walks, up to
+// kScratch of them, interleaved across the warp in `scr` (scr_n counts
+// them, beyond kScratch too); n_items and leaves return the frontier size
+// and the curve's leaf count.
+constexpr int kScratch = 64;
 __device__ bool curve_count_warp(double sx, double sy, const double *p, double tol, WarpFrontier &fr, int lane,
-                                 int32_t &n_emit, int32_t &n_added, uint16_t *item_leaves, int32_t &chords) {
+                                 int32_t &n_emit, int32_t &n_added, uint16_t *item_leaves, int32_t &chords,
+                                 double2 *scr, int32_t &scr_n, int &n_items, int32_t &leaves_out) {
     chords = 0;
+    scr_n = 0;
+    n_items = 0;
+    leaves_out = 0;
     if (pt_eq(sx, sy, p[0], p[1]) && pt_eq(p[2], p[3], p[4], p[5])) {  // Spline.zig:39-42
         n_emit = 1;
         n_added = pt_eq(sx, sy, p[4], p[5]) ? 0 : 1;
@@ -356,6 +365,7 @@ __device__ bool curve_count_warp(double sx, double sy, const double *p, double t
     }
     const Tol tol2 = make_tol(tol);
     const int n = frontier_expand(sx, sy, p, tol2, fr, lane);
+    n_items = n;
     bool ok = true, small = true;
     int32_t emit_tot = 0, add_tot = 0, leaf_tot = 0;
     double carry_x = sx, carry_y = sy;
@@ -366,6 +376,8 @@ __device__ bool curve_count_warp(double sx, double sy, const double *p, double t
         if (i < n) {
             ok &= walk_leaves(fr.k[i], fr.leaf[i] != 0, tol2, [&](const Knots &k) {
                 leaves++;
+                if (scr_n < kScratch) scr[scr_n * 32 + lane] = make_double2(k.ax, k.ay);
+                scr_n++;
                 if (pt_eq(k.ax, k.ay, sx, sy)) return;  // decomposeInto plots no point equal to the start
                 const double x = k.ax, y = k.ay;
                 if (cnt == 0) {
@@ -403,6 +415,7 @@ __device__ bool curve_count_warp(double sx, double sy, const double *p, double t
     }
     // final lineTo(d)
     chords = (__all_sync(0xffffffffu, small) && leaf_tot == emit_tot + 1) ? 1 : 0;
+    leaves_out = leaf_tot;
     emit_tot += 1;
     add_tot += pt_eq(p[4], p[5], carry_x, carry_y) ? 0 : 1;
     n_emit = emit_tot;
@@ -458,22 +471,30 @@ __global__ void __launch_bounds__(32 * kFlattenWarps) k_node_count_w(const z2d_n
                 }
             }
         }
+        inf.pool = -1;
         if (i < n_nodes && !curve) info[i] = inf;
         queue_push(curve, i, curves, counters + CNT_CURVES, lane);
     }
 }
 
+// Besides the counts, a chord curve whose leaves all fit the lanes' scratch
+// leaves its polyline (leaf starts, then d) in the curve pool, so that the
+// emit pass copies points instead of subdividing the curve again.
 __global__ void __launch_bounds__(32 * kFlattenWarps) k_curve_count_w(const z2d_node *__restrict__ nodes,
                                                                       const int32_t *__restrict__ node_fill,
                                                                       const FillCmd *__restrict__ fills,
                                                                       NodeInfo *__restrict__ info,
                                                                       const int32_t *__restrict__ curves,
-                                                                      const int32_t *__restrict__ counters,
+                                                                      int32_t *__restrict__ counters,
                                                                       uint16_t *__restrict__ item_leaves,
-                                                                      int32_t *__restrict__ status) {
+                                                                      int32_t *__restrict__ status,
+                                                                      double2 *__restrict__ scratch,
+                                                                      double2 *__restrict__ pool, int32_t pool_cap) {
     __shared__ WarpFrontier frs[kFlattenWarps];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned all = 0xffffffffu;
     WarpFrontier &fr = frs[w];
+    double2 *scr = scratch + (size_t)(blockIdx.x * kFlattenWarps + w) * (32 * kScratch);
     const int32_t n = counters[CNT_CURVES];
     for (int32_t q = blockIdx.x * kFlattenWarps + w; q < n; q += gridDim.x * kFlattenWarps) {
         const int32_t i = curves[q];
@@ -482,9 +503,35 @@ __global__ void __launch_bounds__(32 * kFlattenWarps) k_curve_count_w(const z2d_
         const double sx = pv.tag == Z2D_CURVE_TO ? pv.p[4] : pv.p[0];
         const double sy = pv.tag == Z2D_CURVE_TO ? pv.p[5] : pv.p[1];
         NodeInfo inf{};
-        if (!curve_count_warp(sx, sy, nd.p, fills[node_fill[i]].tol, fr, lane, inf.n_emit, inf.n_added,
-                              item_leaves + (size_t)i * kFrontier, inf.chords)) {
-            if (lane == 0) atomicExch(status, Z2D_ERR_INVALID_STATE);
+        int32_t scr_n = 0, leaves = 0;
+        int n_items = 0;
+        uint16_t *il = item_leaves + (size_t)i * kFrontier;
+        const bool ok = curve_count_warp(sx, sy, nd.p, fills[node_fill[i]].tol, fr, lane, inf.n_emit, inf.n_added, il,
+                                         inf.chords, scr, scr_n, n_items, leaves);
+        if (!ok && lane == 0) atomicExch(status, Z2D_ERR_INVALID_STATE);
+        inf.pool = -1;
+        if (ok && inf.chords && __all_sync(all, scr_n <= kScratch)) {
+            int32_t base = -1;
+            if (lane == 0) {
+                const int32_t b = atomicAdd(&counters[CNT_POOL], leaves + 1);
+                base = (b >= 0 && (long long)b + leaves + 1 <= pool_cap) ? b : -1;
+            }
+            base = __shfl_sync(all, base, 0);
+            if (base >= 0) {
+                __syncwarp();  // item_leaves of the other lanes are visible
+                int32_t off = 0, src = 0;
+                for (int b0 = 0; b0 < n_items; b0 += 32) {
+                    const int i2 = b0 + lane;
+                    const int32_t cnt = i2 < n_items ? (int32_t)il[i2] : 0;
+                    int tot = 0;
+                    const int32_t at = off + warp_excl_sum(cnt, lane, tot);
+                    for (int32_t j = 0; j < cnt; j++) pool[base + at + j] = scr[(src + j) * 32 + lane];
+                    src += cnt;
+                    off += tot;
+                }
+                if (lane == 0) pool[base + leaves] = make_double2(nd.p[4], nd.p[5]);
+                inf.pool = base;
+            }
         }
         if (lane == 0) info[i] = inf;
         __syncwarp();
@@ -597,7 +644,8 @@ __global__ void __launch_bounds__(32 * kFlattenWarps) k_curve_emit_w(const z2d_n
                                                                      DEdge *__restrict__ edges,
                                                                      const int32_t *__restrict__ curves,
                                                                      const int32_t *__restrict__ counters,
-                                                                     const uint16_t *__restrict__ item_leaves) {
+                                                                     const uint16_t *__restrict__ item_leaves,
+                                                                     const double2 *__restrict__ pool) {
     __shared__ WarpFrontier frs[kFlattenWarps];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     WarpFrontier &fr = frs[w];
@@ -605,13 +653,21 @@ __global__ void __launch_bounds__(32 * kFlattenWarps) k_curve_emit_w(const z2d_n
     for (int32_t q = blockIdx.x * kFlattenWarps + w; q < n; q += gridDim.x * kFlattenWarps) {
         const int32_t i = curves[q];
         const NodeInfo inf = info[i];
-        const z2d_node nd = nodes[i];
         const int32_t f = node_fill[i];
         const FillCmd &F = fills[f];
         DEdge *out = edges + st[f].edge_base + inf.edge_off;
         double et = 0, eb = 0, el = 0, er = 0;
         bool any = false;
-        curve_emit_warp(F, out, inf, nd.p, item_leaves + (size_t)i * kFrontier, fr, lane, et, eb, el, er, any);
+        if (inf.pool >= 0) {  // the count pass kept the polyline: edge k joins points k and k + 1
+            const double2 *P = pool + inf.pool;
+            for (int32_t k = lane; k < inf.n_emit; k += 32) {
+                const double2 a = P[k], b = P[k + 1];
+                add_edge(F, out + k, a.x, a.y, b.x, b.y, et, eb, el, er, any);
+            }
+        } else {
+            const z2d_node nd = nodes[i];
+            curve_emit_warp(F, out, inf, nd.p, item_leaves + (size_t)i * kFrontier, fr, lane, et, eb, el, er, any);
+        }
         merge_extents(st, f, any, et, eb, el, er);
         __syncwarp();
     }
@@ -1481,11 +1537,18 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     // few resident blocks per SM
     const unsigned curve_blocks =
         (unsigned)std::min<long long>(grid_for(n_nodes, kFlattenWarps), (long long)c.sm_count * 8);
+    // per curve warp: kScratch leaf points per lane; then the curve pool
+    const size_t scratch_pts = (size_t)curve_blocks * kFlattenWarps * 32 * kScratch;
+    const int32_t pool_cap = (int32_t)std::min<long long>(64ll << 20, std::max<long long>(1ll << 20, 16ll * n_nodes));
+    if (c.curve_pool.ensure(sizeof(double2) * (scratch_pts + (size_t)pool_cap))) return Z2D_ERR_OUT_OF_MEMORY;
+    double2 *d_scratch = c.curve_pool.as<double2>();
+    double2 *d_pool = d_scratch + scratch_pts;
     cudaEvent_t tf = c.timer_begin(c.t_flatten);
     k_node_count_w<<<flat_blocks, 32 * kFlattenWarps, 0, c.stream>>>(d_nodes, d_nfill, d_fills, d_info, n_nodes,
                                                                     d_curves, d_cnt);
     k_curve_count_w<<<curve_blocks, 32 * kFlattenWarps, 0, c.stream>>>(d_nodes, d_nfill, d_fills, d_info, d_curves,
-                                                                      d_cnt, d_items, d_cnt + CNT_STATUS);
+                                                                      d_cnt, d_items, d_cnt + CNT_STATUS, d_scratch,
+                                                                      d_pool, pool_cap);
     StrokeRun srun;
     if (n_sk > 0) {
         srun.nodes = d_nodes;
@@ -1535,7 +1598,8 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     k_node_emit_w<<<flat_blocks, 32 * kFlattenWarps, 0, c.stream>>>(d_nodes, d_nfill, d_fills, d_info, d_st, d_edges,
                                                                    n_nodes, d_curves + n_nodes, d_cnt);
     k_curve_emit_w<<<curve_blocks, 32 * kFlattenWarps, 0, c.stream>>>(d_nodes, d_nfill, d_fills, d_info, d_st,
-                                                                     d_edges, d_curves + n_nodes, d_cnt, d_items);
+                                                                     d_edges, d_curves + n_nodes, d_cnt, d_items,
+                                                                     d_pool);
     if (n_sk > 0) {
         const int rc = stroke_emit(c, srun, d_fills, d_st, d_edges);
         if (rc) return rc;

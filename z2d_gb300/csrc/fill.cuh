@@ -42,6 +42,8 @@ struct NodeInfo {
     int32_t n_added;
     int32_t edge_off;
     int32_t chords; // curve whose edges are its subdivision leaves' chords (see k_node_emit_w)
+    int32_t pool;   // first of its leaves' points in the curve pool, or -1 (see k_curve_count_w)
+    int32_t _pad;
 };
 
 // Polygon.Edge plus its rounded active range: the edge is active on sample
@@ -116,7 +118,8 @@ enum : int32_t {
     CNT_STATUS = 5,
     CNT_CURVES = 6,       // curves queued by k_node_count_w
     CNT_CURVES_EMIT = 7,  // curves queued by k_node_emit_w
-    CNT_COUNT = 8
+    CNT_POOL = 8,         // points used in the curve pool
+    CNT_COUNT = 10
 };
 
 // action-mask byte of the exact path: bit 7 = clear first, bits 0-4 = coverage

@@ -67,6 +67,7 @@ struct Ctx {
     DevBuf stroke_a;    // device stroker: per node / subpath / stroke state
     DevBuf stroke_b;    // device stroker: per point state
     DevBuf stroke_c;    // device stroker: contour points
+    DevBuf curve_pool;  // leaf points of flattened curves (count pass -> emit pass)
     HostBuf staging;    // pinned upload staging
     HostBuf readback;   // pinned readback
     cudaEvent_t done = nullptr;
