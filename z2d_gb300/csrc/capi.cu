@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "fill.cuh"
+#include "host_pool.h"
 #include "stroke.h"
 #include "stroke_gpu.cuh"
 #include "z2d_internal.h"
@@ -241,25 +242,69 @@ static bool pixel_premultiplied(const z2d_pixel &p) {  // canDemultiply (src/pix
     return true;
 }
 
-// PathNode.isClosedNodeSet (src/internal/path_nodes.zig:23-36)
-static bool is_closed(const z2d_node *nodes, size_t n) {
-    if (n == 0) return false;
-    bool closed = false;
+// The node checks of painter.fill in one pass: PathNode.isClosedNodeSet
+// (src/internal/path_nodes.zig:23-36), then per node in order its tag, a
+// current point for line_to / curve_to (fill_plotter.zig reports
+// InvalidState), finite coordinates and z2d's +-2^24 coordinate range.
+// PathNotClosed takes precedence over the per-node errors.
+static int check_nodes(const z2d_node *nodes, size_t n) {
+    bool closed = false, closed_ok = true, seen_move = false;
+    size_t bad = n;  // first node failing a per-node check
     for (size_t i = 0; i < n; i++) {
-        switch (nodes[i].tag) {
-            case Z2D_MOVE_TO:
-                if (!closed && i != 0) return false;
-                break;
-            case Z2D_CLOSE_PATH: closed = true; break;
-            default: closed = false; break;
+        const z2d_node &nd = nodes[i];
+        const int32_t tag = nd.tag;
+        if (tag == Z2D_MOVE_TO) {
+            if (!closed && i != 0) closed_ok = false;
+            seen_move = true;
+        } else if (tag == Z2D_CLOSE_PATH) {
+            closed = true;
+        } else {
+            closed = false;
+        }
+        if (bad < n) continue;
+        if (tag < Z2D_MOVE_TO || tag > Z2D_CLOSE_PATH || ((tag == Z2D_LINE_TO || tag == Z2D_CURVE_TO) && !seen_move)) {
+            bad = i;
+            continue;
+        }
+        // |p| <= 2^24 is false for NaN and the infinities as well
+        const int np = tag == Z2D_CURVE_TO ? 6 : tag == Z2D_CLOSE_PATH ? 0 : 2;
+        bool ok = true;
+        for (int k = 0; k < np; k++) ok &= std::fabs(nd.p[k]) <= 16777216.0;
+        if (!ok) bad = i;
+    }
+    if (!closed_ok || !closed) {
+        set_error("PathNotClosed");
+        return Z2D_ERR_PATH_NOT_CLOSED;
+    }
+    if (bad == n) return Z2D_OK;
+    const z2d_node &nd = nodes[bad];
+    if (nd.tag < Z2D_MOVE_TO || nd.tag > Z2D_CLOSE_PATH) {
+        set_error("node: bad tag");
+        return Z2D_ERR_INVALID_ARGUMENT;
+    }
+    if (nd.tag == Z2D_LINE_TO || nd.tag == Z2D_CURVE_TO) {
+        bool moved = false;
+        for (size_t i = 0; i < bad && !moved; i++) moved = nodes[i].tag == Z2D_MOVE_TO;
+        if (!moved) {
+            set_error("InvalidState: line_to/curve_to without a current point");
+            return Z2D_ERR_INVALID_STATE;
         }
     }
-    return closed;
+    const int np = nd.tag == Z2D_CURVE_TO ? 6 : 2;
+    for (int k = 0; k < np; k++) {
+        if (!std::isfinite(nd.p[k])) {
+            set_error("InvalidState: non-finite coordinate");
+            return Z2D_ERR_INVALID_STATE;
+        }
+        if (std::fabs(nd.p[k]) > 16777216.0) break;
+    }
+    set_error("coordinate outside +-2^24 (z2d's Path clamps to the i24 range)");
+    return Z2D_ERR_INVALID_ARGUMENT;
 }
 
 // The validation of painter.fill (src/painter.zig:73-91) plus the
 // conditions under which fill_plotter.plot reports InvalidState.
-static int check_fill(const z2d_surface &s, const z2d_pattern &p, const z2d_node *nodes, size_t n, const z2d_fill_opts &o) {
+static int check_fill(const z2d_pattern &p, const z2d_node *nodes, size_t n, const z2d_fill_opts &o) {
     if (p.kind == Z2D_PATTERN_PIXEL) {
         const int rc = check_pixel(p.pixel);
         if (rc) return rc;
@@ -279,36 +324,7 @@ static int check_fill(const z2d_surface &s, const z2d_pattern &p, const z2d_node
     }
     if (n == 0) return Z2D_OK;
     if (!nodes) return Z2D_ERR_INVALID_ARGUMENT;
-    if (!is_closed(nodes, n)) {
-        set_error("PathNotClosed");
-        return Z2D_ERR_PATH_NOT_CLOSED;
-    }
-    bool seen_move = false;
-    for (size_t i = 0; i < n; i++) {
-        const z2d_node &nd = nodes[i];
-        if (nd.tag < Z2D_MOVE_TO || nd.tag > Z2D_CLOSE_PATH) {
-            set_error("node: bad tag");
-            return Z2D_ERR_INVALID_ARGUMENT;
-        }
-        if (nd.tag == Z2D_MOVE_TO) seen_move = true;
-        if ((nd.tag == Z2D_LINE_TO || nd.tag == Z2D_CURVE_TO) && !seen_move) {
-            set_error("InvalidState: line_to/curve_to without a current point");
-            return Z2D_ERR_INVALID_STATE;
-        }
-        const int np = nd.tag == Z2D_CURVE_TO ? 6 : nd.tag == Z2D_CLOSE_PATH ? 0 : 2;
-        for (int k = 0; k < np; k++) {
-            if (!std::isfinite(nd.p[k])) {
-                set_error("InvalidState: non-finite coordinate");
-                return Z2D_ERR_INVALID_STATE;
-            }
-            if (std::fabs(nd.p[k]) > 16777216.0) {
-                set_error("coordinate outside +-2^24 (z2d's Path clamps to the i24 range)");
-                return Z2D_ERR_INVALID_ARGUMENT;
-            }
-        }
-    }
-    (void)s;
-    return Z2D_OK;
+    return check_nodes(nodes, n);
 }
 
 static int check_surface(const z2d_surface *s) {
@@ -358,108 +374,131 @@ static int stage_out(Ctx &c, const z2d_surface &s, const DevSurface &d) {
     return Z2D_OK;
 }
 
-// Appends the prepared commands of a list of fills on surface `s` (job
-// `job` of the batch).  node_fill must hold n_nodes entries, -1 for nodes
-// no command has claimed yet.
-static int prepare_fills(const z2d_surface &s, int32_t job, const z2d_node *nodes, size_t n_nodes,
-                         const z2d_fill_cmd *cmds, size_t n_cmds, std::vector<FillCmd> &fills,
-                         std::vector<int32_t> &node_fill, std::vector<DevGradient> &grads,
-                         std::vector<int32_t> &grad_of_fill) {
-    if (n_nodes > 0x7FFFFFFF || n_cmds > 0x7FFFFFF || fills.size() + n_cmds > 0x7FFFFFF) {
-        set_error("batch too large");
+// One fill command prepared for the device: painter.fill's checks, its
+// anti-aliasing, precision and tolerance adjustments, and the pattern as a
+// compositor source (grad receives a gradient's table when needs_grad).
+static int prepare_fill(const z2d_surface &s, int32_t job, const z2d_node *nodes, size_t n_nodes,
+                        const z2d_fill_cmd &cm, FillCmd &F, DevGradient &grad, bool &needs_grad) {
+    needs_grad = false;
+    if (!cm.pattern) return Z2D_ERR_INVALID_ARGUMENT;
+    if (cm.node_offset > n_nodes || cm.n_nodes > n_nodes - cm.node_offset) {
+        set_error("fill command outside the node array");
         return Z2D_ERR_INVALID_ARGUMENT;
     }
-    for (size_t i = 0; i < n_cmds; i++) {
-        const z2d_fill_cmd &cm = cmds[i];
-        if (!cm.pattern) return Z2D_ERR_INVALID_ARGUMENT;
-        if (cm.node_offset > n_nodes || cm.n_nodes > n_nodes - cm.node_offset) {
-            set_error("fill command outside the node array");
-            return Z2D_ERR_INVALID_ARGUMENT;
-        }
-        const z2d_node *nd = nodes + cm.node_offset;
-        int rc = check_fill(s, *cm.pattern, nd, cm.n_nodes, cm.opts);
-        if (rc) return rc;
-        if (cm.n_nodes == 0) continue;  // painter.fill returns early
-        // painter.fill's AA choice (painter.zig:86-97): alpha1 surfaces
-        // always draw without anti-aliasing; default is multisample
-        const int aa = (s.format == Z2D_FORMAT_ALPHA1) ? Z2D_AA_NONE : cm.opts.anti_aliasing;
-        FillCmd F;
-        memset(&F, 0, sizeof(F));
-        F.node_off = (int32_t)cm.node_offset;
-        F.n_nodes = (int32_t)cm.n_nodes;
-        F.job = job;
-        F.stroke = -1;
-        F.poly = -1;
-        F.aa = (aa == Z2D_AA_NONE || aa == Z2D_AA_SUPERSAMPLE_4X) ? aa : Z2D_AA_MULTISAMPLE_4X;
-        F.rule = cm.opts.fill_rule;
-        F.op = cm.opts.op;
-        F.precision = requires_float(F.op) ? Z2D_PRECISION_FLOAT : cm.opts.precision;
-        F.tol = std::fmax(cm.opts.tolerance, 0.001);
-        F.scale = F.aa == Z2D_AA_NONE ? 1.0 : 4.0;
-        F.edge_scale = F.scale;
-        F.pattern_kind = cm.pattern->kind;
-        const int pk = cm.pattern->kind == Z2D_PATTERN_PIXEL      ? Z2D_PARAM_PIXEL
-                       : cm.pattern->kind == Z2D_PATTERN_GRADIENT ? Z2D_PARAM_GRADIENT
-                                                                  : Z2D_PARAM_DITHER;
-        bool needs_grad = false;
-        DevGradient g;
-        rc = make_dev_src_from_pattern(pk, *cm.pattern, F.src, needs_grad, g);
-        if (rc) return rc;
-        if (needs_grad) {
-            grad_of_fill.push_back((int32_t)grads.size());
-            grads.push_back(g);
-        } else {
-            grad_of_fill.push_back(-1);
-        }
-        if (F.pattern_kind == Z2D_PATTERN_PIXEL) {
-            const Px px = F.src.px;
-            bool opaque = (px.fmt == Z2D_FORMAT_XRGB || px.fmt == Z2D_FORMAT_RGB) ? true : px.a == fmt_max(px.fmt);
-            F.reduces = (F.op == Z2D_OP_SRC) || (F.op == Z2D_OP_SRC_OVER && opaque);
-            F.px_paint = convert_px(px, s.format);
-            F.px_rgba = to_i16(convert_px(px, Z2D_FORMAT_RGBA));
-            if (F.op == Z2D_OP_SRC_OVER && F.precision == Z2D_PRECISION_INTEGER) F.fast_kind = FAST_PIXEL_SRC_OVER;
-        }
-        const int32_t fi = (int32_t)fills.size();
-        for (size_t k = 0; k < cm.n_nodes; k++) {
-            if (node_fill[cm.node_offset + k] != -1) {
-                set_error("fill commands must not share nodes");
-                return Z2D_ERR_INVALID_ARGUMENT;
-            }
-            node_fill[cm.node_offset + k] = fi;
-        }
-        fills.push_back(F);
+    int rc = check_fill(*cm.pattern, nodes + cm.node_offset, cm.n_nodes, cm.opts);
+    if (rc || cm.n_nodes == 0) return rc;  // painter.fill returns early on an empty path
+    // painter.fill's AA choice (painter.zig:86-97): alpha1 surfaces
+    // always draw without anti-aliasing; default is multisample
+    const int aa = (s.format == Z2D_FORMAT_ALPHA1) ? Z2D_AA_NONE : cm.opts.anti_aliasing;
+    memset(&F, 0, sizeof(F));
+    F.node_off = (int32_t)cm.node_offset;
+    F.n_nodes = (int32_t)cm.n_nodes;
+    F.job = job;
+    F.stroke = -1;
+    F.poly = -1;
+    F.aa = (aa == Z2D_AA_NONE || aa == Z2D_AA_SUPERSAMPLE_4X) ? aa : Z2D_AA_MULTISAMPLE_4X;
+    F.rule = cm.opts.fill_rule;
+    F.op = cm.opts.op;
+    F.precision = requires_float(F.op) ? Z2D_PRECISION_FLOAT : cm.opts.precision;
+    F.tol = std::fmax(cm.opts.tolerance, 0.001);
+    F.scale = F.aa == Z2D_AA_NONE ? 1.0 : 4.0;
+    F.edge_scale = F.scale;
+    F.pattern_kind = cm.pattern->kind;
+    const int pk = cm.pattern->kind == Z2D_PATTERN_PIXEL      ? Z2D_PARAM_PIXEL
+                   : cm.pattern->kind == Z2D_PATTERN_GRADIENT ? Z2D_PARAM_GRADIENT
+                                                              : Z2D_PARAM_DITHER;
+    rc = make_dev_src_from_pattern(pk, *cm.pattern, F.src, needs_grad, grad);
+    if (rc) return rc;
+    if (F.pattern_kind == Z2D_PATTERN_PIXEL) {
+        const Px px = F.src.px;
+        bool opaque = (px.fmt == Z2D_FORMAT_XRGB || px.fmt == Z2D_FORMAT_RGB) ? true : px.a == fmt_max(px.fmt);
+        F.reduces = (F.op == Z2D_OP_SRC) || (F.op == Z2D_OP_SRC_OVER && opaque);
+        F.px_paint = convert_px(px, s.format);
+        F.px_rgba = to_i16(convert_px(px, Z2D_FORMAT_RGBA));
+        if (F.op == Z2D_OP_SRC_OVER && F.precision == Z2D_PRECISION_INTEGER) F.fast_kind = FAST_PIXEL_SRC_OVER;
     }
     return Z2D_OK;
 }
 
-// True when the fills own every node and their node ranges follow each
-// other in order, so the caller's node array can be uploaded as it is.
-static bool nodes_in_order(size_t n_nodes, const std::vector<FillCmd> &fills) {
-    size_t next = 0;
-    for (const FillCmd &F : fills) {
-        if ((size_t)F.node_off != next) return false;
-        next += (size_t)F.n_nodes;
+// Appends the prepared commands of a list of fills on surface `s` (job
+// `job` of the batch), skipping empty paths.  Large lists are prepared on
+// the host pool, 64 commands per task; the first failing command in list
+// order decides the error.
+static int prepare_fills(const z2d_surface &s, int32_t job, const z2d_node *nodes, size_t n_nodes,
+                         const z2d_fill_cmd *cmds, size_t n_cmds, std::vector<FillCmd> &fills,
+                         std::vector<DevGradient> &grads, std::vector<int32_t> &grad_of_fill) {
+    if (n_nodes > 0x7FFFFFFF || n_cmds > 0x7FFFFFF || fills.size() + n_cmds > 0x7FFFFFF) {
+        set_error("batch too large");
+        return Z2D_ERR_INVALID_ARGUMENT;
     }
-    return next == n_nodes;
+    constexpr size_t kTask = 64;
+    if (n_cmds < 2 * kTask) {
+        for (size_t i = 0; i < n_cmds; i++) {
+            FillCmd F;
+            DevGradient g;
+            bool needs_grad;
+            const int rc = prepare_fill(s, job, nodes, n_nodes, cmds[i], F, g, needs_grad);
+            if (rc) return rc;
+            if (cmds[i].n_nodes == 0) continue;
+            grad_of_fill.push_back(needs_grad ? (int32_t)grads.size() : -1);
+            if (needs_grad) grads.push_back(g);
+            fills.push_back(F);
+        }
+        return Z2D_OK;
+    }
+    const size_t base = fills.size();
+    std::vector<FillCmd> F(n_cmds);
+    std::vector<DevGradient> G(n_cmds);
+    std::vector<uint8_t> NG(n_cmds);
+    std::vector<int> RC(n_cmds, 0);
+    HostPool::get().run((n_cmds + kTask - 1) / kTask, [&](size_t t) {
+        for (size_t i = t * kTask, e = std::min(n_cmds, i + kTask); i < e; i++) {
+            bool needs_grad = false;
+            RC[i] = prepare_fill(s, job, nodes, n_nodes, cmds[i], F[i], G[i], needs_grad);
+            NG[i] = needs_grad;
+        }
+    });
+    fills.reserve(base + n_cmds);
+    for (size_t i = 0; i < n_cmds; i++) {
+        if (RC[i]) {  // again on this thread, for its message
+            FillCmd f;
+            DevGradient g;
+            bool ng;
+            return prepare_fill(s, job, nodes, n_nodes, cmds[i], f, g, ng);
+        }
+        if (cmds[i].n_nodes == 0) continue;
+        grad_of_fill.push_back(NG[i] ? (int32_t)grads.size() : -1);
+        if (NG[i]) grads.push_back(G[i]);
+        fills.push_back(F[i]);
+    }
+    return Z2D_OK;
 }
 
-// Keeps only the nodes some fill owns, in order, and points the fills at
-// their nodes in the compacted array.
-static void compact_nodes(const z2d_node *nodes, size_t n_nodes, const std::vector<int32_t> &node_fill,
-                          std::vector<FillCmd> &fills, std::vector<z2d_node> &used, std::vector<int32_t> &used_fill) {
-    used.clear();
-    used_fill.clear();
-    used.reserve(n_nodes);
-    used_fill.reserve(n_nodes);
-    std::vector<int32_t> new_off(fills.size(), -1);
-    for (size_t i = 0; i < n_nodes; i++) {
-        const int32_t f = node_fill[i];
-        if (f < 0) continue;
-        if (new_off[f] < 0) new_off[f] = (int32_t)used.size();
-        used.push_back(nodes[i]);
-        used_fill.push_back(f);
+// painter.fill draws each path from its own nodes: the node ranges of the
+// fills (stroke fills own none) must not overlap.
+static int check_fills_disjoint(const std::vector<FillCmd> &fills) {
+    bool sorted = true;
+    int64_t end = 0;
+    for (const FillCmd &F : fills) {
+        if (F.n_nodes == 0) continue;
+        if (F.node_off < end) {
+            sorted = false;
+            break;
+        }
+        end = (int64_t)F.node_off + F.n_nodes;
     }
-    for (size_t f = 0; f < fills.size(); f++) fills[f].node_off = new_off[f];
+    if (sorted) return Z2D_OK;
+    std::vector<std::pair<int32_t, int32_t>> r;
+    r.reserve(fills.size());
+    for (const FillCmd &F : fills)
+        if (F.n_nodes > 0) r.emplace_back(F.node_off, F.n_nodes);
+    std::sort(r.begin(), r.end());
+    for (size_t i = 1; i < r.size(); i++)
+        if ((int64_t)r[i - 1].first + r[i - 1].second > r[i].first) {
+            set_error("fill commands must not share nodes");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
+    return Z2D_OK;
 }
 
 static int do_fill_batch(Ctx &c, z2d_surface *surface, const z2d_node *nodes, size_t n_nodes, const z2d_fill_cmd *cmds,
@@ -468,14 +507,13 @@ static int do_fill_batch(Ctx &c, z2d_surface *surface, const z2d_node *nodes, si
     if (rc) return rc;
     if (n_cmds > 0 && !cmds) return Z2D_ERR_INVALID_ARGUMENT;
     std::vector<FillCmd> fills;
-    std::vector<int32_t> node_fill(n_nodes, -1), grad_of_fill;
+    std::vector<int32_t> grad_of_fill;
     std::vector<DevGradient> grads;
-    rc = prepare_fills(*surface, 0, nodes, n_nodes, cmds, n_cmds, fills, node_fill, grads, grad_of_fill);
+    rc = prepare_fills(*surface, 0, nodes, n_nodes, cmds, n_cmds, fills, grads, grad_of_fill);
     if (rc) return rc;
     if (fills.empty()) return Z2D_OK;
-    std::vector<z2d_node> used;
-    std::vector<int32_t> used_fill;
-    compact_nodes(nodes, n_nodes, node_fill, fills, used, used_fill);
+    rc = check_fills_disjoint(fills);
+    if (rc) return rc;
     std::vector<DevJob> jobs(1);
     memset(jobs.data(), 0, sizeof(DevJob));
     rc = stage_in(c, *surface, c.surface, jobs[0].sfc);
@@ -483,7 +521,7 @@ static int do_fill_batch(Ctx &c, z2d_surface *surface, const z2d_node *nodes, si
     jobs[0].fill0 = 0;
     jobs[0].fill1 = (int32_t)fills.size();
     const DevSurface ds = jobs[0].sfc;
-    rc = run_jobs(c, jobs, used.data(), (int32_t)used.size(), fills, used_fill, grads, grad_of_fill);
+    rc = run_jobs(c, jobs, nodes, (int32_t)n_nodes, fills, grads, grad_of_fill);
     if (rc) return rc;
     return stage_out(c, *surface, ds);
 }
@@ -497,7 +535,7 @@ int fill_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_node *nod
         return Z2D_ERR_INVALID_ARGUMENT;
     }
     std::vector<FillCmd> fills;
-    std::vector<int32_t> node_fill(n_nodes, -1), grad_of_fill;
+    std::vector<int32_t> grad_of_fill;
     std::vector<DevGradient> grads;
     std::vector<DevJob> jobs(n_jobs);
     if (n_jobs > 0) memset(jobs.data(), 0, sizeof(DevJob) * n_jobs);
@@ -516,17 +554,15 @@ int fill_jobs(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_node *nod
         jobs[j].sfc = DevSurface{reinterpret_cast<uint8_t *>(jb.surface.data), jb.surface.format, jb.surface.width,
                                  jb.surface.height};
         jobs[j].fill0 = (int32_t)fills.size();
-        rc = prepare_fills(jb.surface, (int32_t)j, nodes, n_nodes, cmds + jb.cmd_offset, jb.n_cmds, fills, node_fill,
-                           grads, grad_of_fill);
+        rc = prepare_fills(jb.surface, (int32_t)j, nodes, n_nodes, cmds + jb.cmd_offset, jb.n_cmds, fills, grads,
+                           grad_of_fill);
         if (rc) return rc;
         jobs[j].fill1 = (int32_t)fills.size();
     }
     if (fills.empty()) return Z2D_OK;
-    if (nodes_in_order(n_nodes, fills)) return run_jobs(c, jobs, nodes, (int32_t)n_nodes, fills, node_fill, grads, grad_of_fill);
-    std::vector<z2d_node> used;
-    std::vector<int32_t> used_fill;
-    compact_nodes(nodes, n_nodes, node_fill, fills, used, used_fill);
-    return run_jobs(c, jobs, used.data(), (int32_t)used.size(), fills, used_fill, grads, grad_of_fill);
+    const int rc = check_fills_disjoint(fills);
+    if (rc) return rc;
+    return run_jobs(c, jobs, nodes, (int32_t)n_nodes, fills, grads, grad_of_fill);
 }
 
 // ------------------------------------------------------------------ strokes
@@ -674,8 +710,7 @@ static int prepare_polygon_fill(const z2d_surface &s, int32_t job, const z2d_pat
     nd[0].tag = Z2D_MOVE_TO;
     nd[1].tag = Z2D_CLOSE_PATH;
     fc.n_nodes = 2;
-    std::vector<int32_t> owner(2, -1);
-    const int rc = prepare_fills(s, job, nd, 2, &fc, 1, fills, owner, grads, grad_of_fill);
+    const int rc = prepare_fills(s, job, nd, 2, &fc, 1, fills, grads, grad_of_fill);
     if (rc) return rc;
     fills.back().node_off = 0;
     fills.back().n_nodes = 0;
@@ -751,7 +786,7 @@ static int draw_core(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_no
     std::vector<int64_t> stroke_of(n_cmds, -1);
     for (size_t k = 0; k < ns; k++) stroke_of[strokes[k]] = (int64_t)k;
     std::vector<FillCmd> fills;
-    std::vector<int32_t> node_fill(n_nodes, -1), grad_of_fill;
+    std::vector<int32_t> grad_of_fill;
     std::vector<DevGradient> grads;
     std::vector<DevJob> jobs(n_jobs);
     if (n_jobs > 0) memset(jobs.data(), 0, sizeof(DevJob) * n_jobs);
@@ -778,8 +813,7 @@ static int draw_core(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_no
                 fc.node_offset = cm.node_offset;
                 fc.n_nodes = cm.n_nodes;
                 fc.opts = cm.fill;
-                rc = prepare_fills(jb.surface, (int32_t)j, nodes, n_nodes, &fc, 1, fills, node_fill, grads,
-                                   grad_of_fill);
+                rc = prepare_fills(jb.surface, (int32_t)j, nodes, n_nodes, &fc, 1, fills, grads, grad_of_fill);
                 if (rc) return rc;
                 continue;
             }
@@ -851,7 +885,9 @@ static int draw_core(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_no
         jobs[j].fill1 = (int32_t)fills.size();
     }
     if (fills.empty()) return Z2D_OK;
-    return run_jobs(c, jobs, nodes, (int32_t)n_nodes, fills, node_fill, grads, grad_of_fill, &sset);
+    const int rc = check_fills_disjoint(fills);
+    if (rc) return rc;
+    return run_jobs(c, jobs, nodes, (int32_t)n_nodes, fills, grads, grad_of_fill, &sset);
 }
 
 static bool is_hairline(const z2d_draw_cmd &cm) { return cm.kind == Z2D_DRAW_STROKE && cm.stroke.hairline != 0; }

@@ -40,6 +40,7 @@
 #include <vector>
 
 #include "fill.cuh"
+#include "host_pool.h"
 #include "edges.cuh"
 #include "spline.cuh"
 #include "raster_px.cuh"
@@ -1378,29 +1379,21 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
         if ((touched >> q) & 1u) store_raw(dst, (size_t)W * y + px0 + q, raw[q]);
 }
 
+// The fill owning each node: warp f writes f over fill f's node range (the
+// ranges are disjoint; fills drawing stroke polygons own no nodes).
+__global__ void k_node_owner(const FillCmd *__restrict__ fills, int32_t n_fills, int32_t *__restrict__ node_fill) {
+    const int32_t f = (int32_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (f >= n_fills) return;
+    const int32_t o = fills[f].node_off, n = fills[f].n_nodes;
+    for (int32_t k = lane; k < n; k += 32) node_fill[o + k] = f;
+}
+
 // ----------------------------------------------------------- host side
 static inline unsigned grid_for(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
-// memcpy, split over host threads when it is large
-static void par_copy(void *dst, const void *src, size_t bytes) {
-    constexpr size_t kChunk = (size_t)64 << 20;
-    const size_t nt = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), bytes / kChunk + 1);
-    if (nt <= 1) {
-        memcpy(dst, src, bytes);
-        return;
-    }
-    const size_t per = (bytes + nt - 1) / nt;
-    std::vector<std::thread> pool;
-    for (size_t t = 0; t < nt; t++) {
-        const size_t a = t * per, b = std::min(bytes, a + per);
-        if (a >= b) break;
-        pool.emplace_back([=] { memcpy(static_cast<uint8_t *>(dst) + a, static_cast<const uint8_t *>(src) + a, b - a); });
-    }
-    for (auto &th : pool) th.join();
-}
-
 int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n_nodes, std::vector<FillCmd> &fills,
-             const std::vector<int32_t> &node_fill, const std::vector<DevGradient> &grads,
+             const std::vector<DevGradient> &grads,
              const std::vector<int32_t> &grad_of_fill, const StrokeSet *strokes) {
     if (n_nodes < 0) return Z2D_ERR_INVALID_ARGUMENT;
     const int32_t n_fills = (int32_t)fills.size();
@@ -1412,11 +1405,10 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
         J.gband_base = J.tile_base = 0;
         J.list_base = 0;
     }
-    // ---- upload: nodes | node_fill | gradients | fills | jobs | counters
+    // ---- upload: nodes | gradients | fills | jobs | counters
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
     const size_t o_nodes = 0;
-    const size_t o_nfill = al(o_nodes + sizeof(z2d_node) * (size_t)n_nodes);
-    const size_t o_grads = al(o_nfill + sizeof(int32_t) * (size_t)n_nodes);
+    const size_t o_grads = al(o_nodes + sizeof(z2d_node) * (size_t)n_nodes);
     const size_t o_fills = al(o_grads + sizeof(DevGradient) * grads.size());
     const size_t o_jobs = al(o_fills + sizeof(FillCmd) * (size_t)n_fills);
     const size_t o_cnt = al(o_jobs + sizeof(DevJob) * (size_t)n_jobs);
@@ -1461,8 +1453,7 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
         if (grad_of_fill[i] >= 0) fills[i].src.grad = dgrads + grad_of_fill[i];
     // make sure the previous call's kernels no longer read the staging buffer
     Z2D_CUDA(cudaStreamSynchronize(c.stream));
-    if (n_nodes > 0) par_copy(h + o_nodes, nodes, sizeof(z2d_node) * (size_t)n_nodes);
-    par_copy(h + o_nfill, node_fill.data(), sizeof(int32_t) * (size_t)n_nodes);
+    if (n_nodes > 0) pool_copy(h + o_nodes, nodes, sizeof(z2d_node) * (size_t)n_nodes);
     if (!grads.empty()) memcpy(h + o_grads, grads.data(), sizeof(DevGradient) * grads.size());
     memcpy(h + o_fills, fills.data(), sizeof(FillCmd) * (size_t)n_fills);
     memcpy(h + o_jobs, jobs.data(), sizeof(DevJob) * (size_t)n_jobs);
@@ -1513,7 +1504,6 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     }
     Z2D_CUDA(cudaMemcpyAsync(dv, h, total, cudaMemcpyHostToDevice, c.stream));
     const z2d_node *d_nodes = reinterpret_cast<const z2d_node *>(dv + o_nodes);
-    const int32_t *d_nfill = reinterpret_cast<const int32_t *>(dv + o_nfill);
     const FillCmd *d_fills = reinterpret_cast<const FillCmd *>(dv + o_fills);
     DevJob *d_jobs = reinterpret_cast<DevJob *>(dv + o_jobs);
     int32_t *d_cnt = reinterpret_cast<int32_t *>(dv + o_cnt);
@@ -1521,14 +1511,21 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     // node info, then the per-node leaf counts of the curves' frontier items
     const size_t info_bytes = (sizeof(NodeInfo) * (size_t)n_nodes + 255) & ~(size_t)255;
     const size_t items_bytes = (sizeof(uint16_t) * kFrontier * (size_t)n_nodes + 255) & ~(size_t)255;
-    if (c.node_info.ensure(info_bytes + items_bytes + 2 * sizeof(int32_t) * (size_t)n_nodes) ||
+    if (c.node_info.ensure(info_bytes + items_bytes + 3 * sizeof(int32_t) * (size_t)n_nodes) ||
         c.fill_state.ensure(sizeof(FillState) * (size_t)n_fills))
         return Z2D_ERR_OUT_OF_MEMORY;
     NodeInfo *d_info = c.node_info.as<NodeInfo>();
     uint16_t *d_items = reinterpret_cast<uint16_t *>(c.node_info.as<uint8_t>() + info_bytes);
     int32_t *d_curves = reinterpret_cast<int32_t *>(c.node_info.as<uint8_t>() + info_bytes + items_bytes);  // 2 queues
+    int32_t *d_nfill = d_curves + 2 * (size_t)n_nodes;
     FillState *d_st = c.fill_state.as<FillState>();
     Z2D_CUDA(cudaMemsetAsync(d_st, 0, sizeof(FillState) * (size_t)n_fills, c.stream));
+    // each node's fill; nodes no fill owns (stroke commands' nodes, gaps) keep -1
+    long long owned = 0;
+    for (const FillCmd &F : fills) owned += F.n_nodes;
+    if (owned < n_nodes) Z2D_CUDA(cudaMemsetAsync(d_nfill, 0xFF, sizeof(int32_t) * (size_t)n_nodes, c.stream));
+    k_node_owner<<<grid_for(n_fills, 8), 256, 0, c.stream>>>(d_fills, n_fills, d_nfill);
+    c.launches++;
 
     // ---- flatten
     const unsigned flat_blocks =

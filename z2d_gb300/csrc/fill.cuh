@@ -141,14 +141,14 @@ struct DevJob {
 
 // Runs ordered lists of fills on device surfaces (one list per job; jobs are
 // independent).  `fills` hold the prepared commands grouped by job (node
-// offsets into `nodes`, host memory); grad_of_fill[i] >= 0 names the
-// gradient of fill i in `grads`.
-// Nodes that no fill owns (node_fill -1) are skipped; device-stroked
+// offsets into `nodes`, host memory; the fills' node ranges are disjoint);
+// grad_of_fill[i] >= 0 names the gradient of fill i in `grads`.
+// Nodes that no fill owns are skipped; device-stroked
 // commands (`strokes`, fills with stroke >= 0) read their nodes from the
 // same array; fills with poly >= 0 draw a host-built polygon of `strokes`.
 struct StrokeSet;
 int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n_nodes, std::vector<FillCmd> &fills,
-             const std::vector<int32_t> &node_fill, const std::vector<DevGradient> &grads,
+             const std::vector<DevGradient> &grads,
              const std::vector<int32_t> &grad_of_fill, const StrokeSet *strokes = nullptr);
 
 }  // namespace z2dg
