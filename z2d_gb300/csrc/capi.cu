@@ -446,31 +446,52 @@ static int prepare_fills(const z2d_surface &s, int32_t job, const z2d_node *node
         }
         return Z2D_OK;
     }
-    const size_t base = fills.size();
-    std::vector<FillCmd> F(n_cmds);
-    std::vector<DevGradient> G(n_cmds);
+    // commands are prepared in place at fills[base + i]; a gradient table
+    // can only come from a command whose pattern is not a pixel, and goes
+    // to its slot among those
+    const size_t base = fills.size(), gbase = grads.size();
+    std::vector<int32_t> slot(n_cmds);
+    size_t n_slots = 0;
+    for (size_t i = 0; i < n_cmds; i++)
+        slot[i] = (cmds[i].pattern && cmds[i].pattern->kind != Z2D_PATTERN_PIXEL) ? (int32_t)n_slots++ : -1;
+    fills.resize(base + n_cmds);
+    grads.resize(gbase + n_slots);
     std::vector<uint8_t> NG(n_cmds);
     std::vector<int> RC(n_cmds, 0);
     HostPool::get().run((n_cmds + kTask - 1) / kTask, [&](size_t t) {
+        DevGradient scratch;
         for (size_t i = t * kTask, e = std::min(n_cmds, i + kTask); i < e; i++) {
             bool needs_grad = false;
-            RC[i] = prepare_fill(s, job, nodes, n_nodes, cmds[i], F[i], G[i], needs_grad);
-            NG[i] = needs_grad;
+            DevGradient &g = slot[i] >= 0 ? grads[gbase + (size_t)slot[i]] : scratch;
+            RC[i] = prepare_fill(s, job, nodes, n_nodes, cmds[i], fills[base + i], g, needs_grad);
+            NG[i] = needs_grad && slot[i] >= 0;
+            if (needs_grad && slot[i] < 0) RC[i] = Z2D_ERR_INVALID_ARGUMENT;  // not reached: pixels need no table
         }
     });
-    fills.reserve(base + n_cmds);
+    // keep the non-empty commands and the tables they use, in order
+    size_t nf = base, ng = gbase;
     for (size_t i = 0; i < n_cmds; i++) {
         if (RC[i]) {  // again on this thread, for its message
+            fills.resize(base);
+            grads.resize(gbase);
             FillCmd f;
             DevGradient g;
-            bool ng;
-            return prepare_fill(s, job, nodes, n_nodes, cmds[i], f, g, ng);
+            bool needs_grad;
+            const int rc = prepare_fill(s, job, nodes, n_nodes, cmds[i], f, g, needs_grad);
+            return rc ? rc : Z2D_ERR_INVALID_ARGUMENT;
         }
         if (cmds[i].n_nodes == 0) continue;
-        grad_of_fill.push_back(NG[i] ? (int32_t)grads.size() : -1);
-        if (NG[i]) grads.push_back(G[i]);
-        fills.push_back(F[i]);
+        if (NG[i]) {
+            if (ng != gbase + (size_t)slot[i]) grads[ng] = grads[gbase + (size_t)slot[i]];
+            grad_of_fill.push_back((int32_t)ng++);
+        } else {
+            grad_of_fill.push_back(-1);
+        }
+        if (nf != base + i) fills[nf] = fills[base + i];
+        nf++;
     }
+    fills.resize(nf);
+    grads.resize(ng);
     return Z2D_OK;
 }
 

@@ -1405,10 +1405,11 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
         J.gband_base = J.tile_base = 0;
         J.list_base = 0;
     }
-    // ---- upload: nodes | gradients | fills | jobs | counters
+    // ---- upload: gradients | fills | jobs | counters | strokes | polygons
+    // through the pinned staging buffer, then the nodes straight from the
+    // caller's memory
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
-    const size_t o_nodes = 0;
-    const size_t o_grads = al(o_nodes + sizeof(z2d_node) * (size_t)n_nodes);
+    const size_t o_grads = 0;
     const size_t o_fills = al(o_grads + sizeof(DevGradient) * grads.size());
     const size_t o_jobs = al(o_fills + sizeof(FillCmd) * (size_t)n_fills);
     const size_t o_cnt = al(o_jobs + sizeof(DevJob) * (size_t)n_jobs);
@@ -1445,7 +1446,9 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     const size_t o_ce = al(o_cf + sizeof(int32_t) * (size_t)n_ctr);
     const size_t o_pt = al(o_ce + sizeof(int32_t) * (size_t)n_ctr);
     const size_t total = al(o_pt + sizeof(double) * 2 * (size_t)n_pts);
-    if (c.params.ensure(total) || c.staging.ensure(total)) return Z2D_ERR_OUT_OF_MEMORY;
+    const size_t o_nodes = total;
+    if (c.params.ensure(o_nodes + sizeof(z2d_node) * (size_t)n_nodes) || c.staging.ensure(total))
+        return Z2D_ERR_OUT_OF_MEMORY;
     uint8_t *h = c.staging.as<uint8_t>();
     uint8_t *dv = c.params.as<uint8_t>();
     const DevGradient *dgrads = reinterpret_cast<const DevGradient *>(dv + o_grads);
@@ -1453,7 +1456,9 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
         if (grad_of_fill[i] >= 0) fills[i].src.grad = dgrads + grad_of_fill[i];
     // make sure the previous call's kernels no longer read the staging buffer
     Z2D_CUDA(cudaStreamSynchronize(c.stream));
-    if (n_nodes > 0) pool_copy(h + o_nodes, nodes, sizeof(z2d_node) * (size_t)n_nodes);
+    // (the flatten kernels are done with the nodes at the first readback
+    // below, so the caller's array is free again when this call returns)
+    Z2D_CUDA(cudaMemcpyAsync(dv + o_nodes, nodes, sizeof(z2d_node) * (size_t)n_nodes, cudaMemcpyHostToDevice, c.stream));
     if (!grads.empty()) memcpy(h + o_grads, grads.data(), sizeof(DevGradient) * grads.size());
     memcpy(h + o_fills, fills.data(), sizeof(FillCmd) * (size_t)n_fills);
     memcpy(h + o_jobs, jobs.data(), sizeof(DevJob) * (size_t)n_jobs);

@@ -43,13 +43,14 @@ class HostPool {
             fn_ = &fn;
             n_ = n;
             next_.store(0);
-            active_ = n_workers_;
             gen_++;
         }
         cv_.notify_all();
-        drain();
+        for (size_t i; (i = next_.fetch_add(1)) < n;) fn(i);
+        // every item is claimed; wait for the workers still running theirs.
+        // Workers that wake later find fn_ cleared and go back to sleep.
         std::unique_lock<std::mutex> lk(mu_);
-        done_cv_.wait(lk, [&] { return active_ == 0; });
+        done_cv_.wait(lk, [&] { return in_run_ == 0; });
         fn_ = nullptr;
     }
 
@@ -60,20 +61,23 @@ class HostPool {
         for (unsigned t = 0; t < nw; t++) std::thread([this] { loop(); }).detach();
         n_workers_ = nw;
     }
-    void drain() {
-        for (size_t i; (i = next_.fetch_add(1)) < n_;) (*fn_)(i);
-    }
     void loop() {
         uint64_t seen = 0;
         for (;;) {
+            const std::function<void(size_t)> *fn;
+            size_t n;
             {
                 std::unique_lock<std::mutex> lk(mu_);
                 cv_.wait(lk, [&] { return gen_ != seen; });
                 seen = gen_;
+                fn = fn_;
+                n = n_;
+                if (!fn) continue;
+                in_run_++;
             }
-            drain();
+            for (size_t i; (i = next_.fetch_add(1)) < n;) (*fn)(i);
             std::lock_guard<std::mutex> lk(mu_);
-            if (--active_ == 0) done_cv_.notify_one();
+            if (--in_run_ == 0) done_cv_.notify_one();
         }
     }
 
@@ -84,7 +88,7 @@ class HostPool {
     const std::function<void(size_t)> *fn_ = nullptr;
     size_t n_ = 0;
     std::atomic<size_t> next_{0};
-    size_t active_ = 0;
+    size_t in_run_ = 0;  // workers inside the current run
     uint64_t gen_ = 0;
 };
 
