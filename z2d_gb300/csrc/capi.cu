@@ -367,8 +367,54 @@ static int stage_in(Ctx &c, const z2d_surface &s, DevBuf &buf, DevSurface &out) 
     out.data = buf.as<uint8_t>();
     return Z2D_OK;
 }
+// stage_in with the copy on the context's copy stream, so that it overlaps
+// the work queued on c.stream before the first await_surface().
+static int stage_in_async(Ctx &c, const z2d_surface &s, DevBuf &buf, DevSurface &out) {
+    if (s.location == Z2D_MEM_DEVICE) return stage_in(c, s, buf, out);
+    if (!c.copy_stream) {
+        Z2D_CUDA(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
+        Z2D_CUDA(cudaEventCreateWithFlags(&c.call_start, cudaEventDisableTiming));
+        Z2D_CUDA(cudaEventCreateWithFlags(&c.surface_ready, cudaEventDisableTiming));
+    }
+    out.fmt = s.format;
+    out.w = s.width;
+    out.h = s.height;
+    const size_t bytes = sfc_bytes(s);
+    if (buf.ensure(((bytes + 15) & ~(size_t)15) + 16)) return Z2D_ERR_OUT_OF_MEMORY;
+    // after everything already queued on c.stream (earlier users of buf)
+    Z2D_CUDA(cudaEventRecord(c.call_start, c.stream));
+    Z2D_CUDA(cudaStreamWaitEvent(c.copy_stream, c.call_start, 0));
+    Z2D_CUDA(cudaMemcpyAsync(buf.ptr, s.data, bytes, cudaMemcpyHostToDevice, c.copy_stream));
+    Z2D_CUDA(cudaEventRecord(c.surface_ready, c.copy_stream));
+    c.surface_pending = true;
+    out.data = buf.as<uint8_t>();
+    return Z2D_OK;
+}
+int Ctx::await_surface() {
+    if (!surface_pending) return Z2D_OK;
+    surface_pending = false;
+    Z2D_CUDA(cudaStreamWaitEvent(stream, surface_ready, 0));
+    return Z2D_OK;
+}
+// Ends a call that staged its surface with stage_in_async: on every path
+// out of the call the upload is awaited (the caller's host memory must not be
+// read after the call returns).
+struct SurfaceUploadGuard {
+    Ctx &c;
+    ~SurfaceUploadGuard() {
+        if (c.surface_pending) {
+            c.surface_pending = false;
+            cudaEventSynchronize(c.surface_ready);
+        }
+    }
+};
+
 static int stage_out(Ctx &c, const z2d_surface &s, const DevSurface &d) {
     if (s.location == Z2D_MEM_DEVICE) return Z2D_OK;
+    {
+        const int rc = c.await_surface();
+        if (rc) return rc;
+    }
     Z2D_CUDA(cudaMemcpyAsync(s.data, d.data, sfc_bytes(s), cudaMemcpyDeviceToHost, c.stream));
     Z2D_CUDA(cudaStreamSynchronize(c.stream));
     return Z2D_OK;
@@ -537,7 +583,8 @@ static int do_fill_batch(Ctx &c, z2d_surface *surface, const z2d_node *nodes, si
     if (rc) return rc;
     std::vector<DevJob> jobs(1);
     memset(jobs.data(), 0, sizeof(DevJob));
-    rc = stage_in(c, *surface, c.surface, jobs[0].sfc);
+    SurfaceUploadGuard guard{c};
+    rc = stage_in_async(c, *surface, c.surface, jobs[0].sfc);
     if (rc) return rc;
     jobs[0].fill0 = 0;
     jobs[0].fill1 = (int32_t)fills.size();
@@ -1230,6 +1277,12 @@ Z2D_API int z2dgpu_ctx_destroy(z2dgpu_ctx *c) {
     c->staging.release();
     c->readback.release();
     for (Ctx::Timer *t : {&c->t_raster, &c->t_composite, &c->t_flatten, &c->t_bins, &c->t_stroke, &c->t_export}) c->timer_collect(*t);
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        cudaStreamDestroy(c->copy_stream);
+        cudaEventDestroy(c->call_start);
+        cudaEventDestroy(c->surface_ready);
+    }
     if (c->own_stream) cudaStreamDestroy(c->stream);
     delete c;
     return Z2D_OK;

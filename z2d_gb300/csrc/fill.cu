@@ -1213,25 +1213,46 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
                     }
                 }
                 __syncwarp();
-                const int pairs = per >> 1;
                 const bool eo = F.rule == Z2D_FILL_EVEN_ODD;
-                (void)pairs;
-                for (int s = 0; s < sc; s++) {
+                // each lane's winding change per sample row, then the
+                // winding at the lane's first column: the exclusive scans of
+                // rows (0, 1) and (2, 3) run packed as lo + 65536 hi (every
+                // partial sum is bounded by the band's edge count, at most
+                // kMaxBandEdges < 2^15 in magnitude, so the halves stay apart)
+                int32_t tot[4] = {0, 0, 0, 0};
+#pragma unroll
+                for (int s = 0; s < 4; s++) {
+                    if (s >= sc) break;
+                    const uint32_t *row = words + s * kWordsPerSubRow;
+                    for (uint32_t m = words[kTouchOff + s * 32 + lane]; m; m &= m - 1) {
+                        const uint32_t v = row[((__ffs(m) - 1) << 5) | lane];
+                        tot[s] += (int32_t)(v & 0xFFFFu) + (int32_t)(v >> 16) - 0x10000;
+                    }
+                }
+                const int32_t t01 = tot[0] + tot[1] * 65536, t23 = tot[2] + tot[3] * 65536;
+                int32_t i01 = t01, i23 = t23;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int32_t u01 = __shfl_up_sync(0xffffffffu, i01, o);
+                    const int32_t u23 = __shfl_up_sync(0xffffffffu, i23, o);
+                    if (lane >= o) {
+                        i01 += u01;
+                        i23 += u23;
+                    }
+                }
+                const int32_t x01 = i01 - t01, x23 = i23 - t23;
+                int32_t wrow[4];
+                wrow[0] = (int32_t)(int16_t)(x01 & 0xFFFF);
+                wrow[1] = (x01 - wrow[0]) >> 16;
+                wrow[2] = (int32_t)(int16_t)(x23 & 0xFFFF);
+                wrow[3] = (x23 - wrow[2]) >> 16;
+#pragma unroll
+                for (int s = 0; s < 4; s++) {
+                    if (s >= sc) break;
                     uint32_t *row = words + s * kWordsPerSubRow;
                     uint32_t *touch = words + kTouchOff + s * 32 + lane;
                     const uint32_t touched = *touch;  // pairs of this lane that received crossings
-                    int32_t tot = 0;
-                    for (uint32_t m = touched; m; m &= m - 1) {
-                        const uint32_t v = row[((__ffs(m) - 1) << 5) | lane];
-                        tot += (int32_t)(v & 0xFFFFu) + (int32_t)(v >> 16) - 0x10000;
-                    }
-                    int32_t incl = tot;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-                        if (lane >= o) incl += t;
-                    }
-                    int32_t wnd = incl - tot;
+                    int32_t wnd = wrow[s];
                     // Between touched pairs the winding is constant, so inside
                     // bits are filled a range at a time.
                     bool in = eo ? ((wnd & 1) != 0) : (wnd != 0);
@@ -1736,6 +1757,10 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
             Z2D_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         }
         attr_set.fetch_or(dev_bit, std::memory_order_relaxed);
+    }
+    {
+        const int rc = c.await_surface();  // a host surface's upload
+        if (rc) return rc;
     }
     cudaEvent_t t0 = c.timer_begin(c.t_raster);
     if (n_jobs == 1) k_raster<false><<<(unsigned)n_tiles, kRasterThreads, smem, c.stream>>>(A);

@@ -71,6 +71,15 @@ struct Ctx {
     HostBuf staging;    // pinned upload staging
     HostBuf readback;   // pinned readback
     cudaEvent_t done = nullptr;
+    // upload of a host surface overlapping the flatten kernels: the copy runs
+    // on copy_stream after call_start (the call's first point on `stream`);
+    // `stream` waits for surface_ready before the first kernel that reads the
+    // surface (surface_pending says whether that wait is still owed)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t call_start = nullptr, surface_ready = nullptr;
+    bool surface_pending = false;
+    // Makes `stream` wait for a pending surface upload (no-op otherwise).
+    int await_surface();
     // kernel timing (z2dgpu_ctx_set_timing)
     bool timing = false;
     struct Timer {
