@@ -677,7 +677,7 @@ __global__ void __launch_bounds__(32 * kFlattenWarps) k_curve_emit_w(const z2d_n
 __device__ __forceinline__ int32_t clampi(int32_t v, int32_t lo, int32_t hi) { return max(lo, min(v, hi)); }
 
 __global__ void k_fill_setup(const FillCmd *__restrict__ fills, FillState *__restrict__ st, int32_t n_fills,
-                             DevJob *__restrict__ jobs, int32_t *__restrict__ counters) {
+                             DevJob *__restrict__ jobs, int32_t *__restrict__ counters, RasterFill *__restrict__ rf) {
     const int32_t f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= n_fills) return;
     const FillCmd F = fills[f];
@@ -781,6 +781,19 @@ __global__ void k_fill_setup(const FillCmd *__restrict__ fills, FillState *__res
     atomicMin(&J.tcol_lo, cx0 / kTileCols);
     atomicMax(&J.tcol_hi, (max(cx1, cx0 + 1) - 1) / kTileCols);
     st[f] = S;
+    RasterFill R;
+    R.start_x = S.start_x;
+    R.end_x = S.end_x;
+    R.start_y = S.start_y;
+    R.end_y = S.end_y;
+    R.meta = ((uint32_t)F.op & RF_OP_MASK) | ((uint32_t)F.aa << RF_AA_SHIFT) |
+             (F.rule == Z2D_FILL_EVEN_ODD ? RF_EVEN_ODD : 0u) | ((uint32_t)F.fast_kind << RF_FAST_SHIFT) |
+             ((S.flags & FILL_EXACT) ? RF_EXACT : 0u) | ((S.flags & FILL_SS_ZERO) ? RF_SS_ZERO : 0u) |
+             (bounded ? RF_BOUNDED : 0u);
+    R.px = (F.src.pix.r & 0xFFu) | ((F.src.pix.g & 0xFFu) << 8) | ((F.src.pix.b & 0xFFu) << 16) |
+           ((F.src.pix.a & 0xFFu) << 24);
+    R._pad[0] = R._pad[1] = 0;
+    rf[f] = R;
 }
 
 // Band range of an edge's active sample rows within the fill's draw rows.
@@ -881,7 +894,8 @@ __device__ __forceinline__ int32_t job_of(const DevJob *__restrict__ jobs, int32
 }
 
 // One CTA per global band: the job's fills touching the band, in call order
-// (ordered compaction), with the tile-column range each one can affect.
+// (ordered compaction), with the tile-column range each one can affect and
+// the fill's (fill, band) slot of the band.
 __global__ void __launch_bounds__(256) k_band_lists(const FillState *__restrict__ st, const DevJob *__restrict__ jobs,
                                                     int32_t n_jobs, int32_t *__restrict__ band_count,
                                                     int4 *__restrict__ band_fills) {
@@ -906,6 +920,7 @@ __global__ void __launch_bounds__(256) k_band_lists(const FillState *__restrict_
             hit = S.active && b >= S.band0 && b <= S.band1;
             ent.y = S.cull_x0;
             ent.z = S.cull_x1;
+            ent.w = S.fb_base + (b - S.band0);
         }
         const unsigned m = __ballot_sync(0xffffffffu, hit);
         if (lane == 0) warp_tot[wid] = __popc(m);
@@ -1101,7 +1116,8 @@ struct RasterArgs {
     const int32_t *bins;
     const int32_t *bin_off;
     const int32_t *band_count;  // per global band
-    const int4 *band_fills;     // {fill, cull_x0, cull_x1, 0} per band, in call order
+    const int4 *band_fills;     // {fill, cull_x0, cull_x1, (fill, band) slot} per band, in call order
+    const RasterFill *rfills;
     const uint8_t *masks;
     int32_t n_jobs;
 };
@@ -1167,26 +1183,29 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
         if (valid) ent = list[k0 + lane];
         uint32_t hits = __ballot_sync(0xffffffffu, valid && ent.z > x0 && ent.y < x0 + kTileCols);
         while (hits) {
-            const int32_t f = __shfl_sync(0xffffffffu, ent.x, __ffs(hits) - 1);
+            const int src = __ffs(hits) - 1;
+            const int32_t f = __shfl_sync(0xffffffffu, ent.x, src);
+            const int32_t fb = __shfl_sync(0xffffffffu, ent.w, src);
             hits &= hits - 1;
-            const FillState &S = A.st[f];
-            const FillCmd &F = A.fills[f];
-            const int32_t op = F.op;
-            const bool bounded = is_bounded(op);
-            const bool ssaa = F.aa == Z2D_AA_SUPERSAMPLE_4X;
+            const int4 ra = __ldg(reinterpret_cast<const int4 *>(A.rfills + f));
+            const int4 rb = __ldg(reinterpret_cast<const int4 *>(A.rfills + f) + 1);
+            const int32_t start_x = ra.x, end_x = ra.y, start_y = ra.z, end_y = ra.w;
+            const uint32_t meta = (uint32_t)rb.x;
+            const int32_t aa = (int32_t)((meta >> RF_AA_SHIFT) & 3u);
+            const bool bounded = (meta & RF_BOUNDED) != 0;
+            const bool ssaa = aa == Z2D_AA_SUPERSAMPLE_4X;
             const bool boxed = bounded || ssaa;  // touches only [start_x, end_x) x [start_y, end_y]
-            if (boxed && (S.end_x <= x0 || S.start_x >= x0 + kTileCols)) continue;
-            const bool direct = F.aa == Z2D_AA_NONE;
-            const bool exact = (S.flags & FILL_EXACT) != 0;
-            const bool in_rows = y >= S.start_y && y <= S.end_y;
+            if (boxed && (end_x <= x0 || start_x >= x0 + kTileCols)) continue;
+            const bool direct = aa == Z2D_AA_NONE;
+            const bool exact = (meta & RF_EXACT) != 0;
+            const bool in_rows = y >= start_y && y <= end_y;
             if (!in_rows && boxed) continue;
             const int32_t sc = direct ? 1 : 4, per = 8 * sc;
             // coverage of pixel q (0..16) is byte q / 2 of cov_ev (q even)
             // or cov_od (q odd)
             uint32_t cov_ev = 0, cov_od = 0;
-            if (!exact && in_rows && !(S.flags & FILL_SS_ZERO)) {
+            if (!exact && in_rows && !(meta & RF_SS_ZERO)) {
                 const int32_t sub0 = y * sc, col0 = x0 * sc, ncol = kTileCols * sc;
-                const int32_t fb = S.fb_base + (b - S.band0);
                 const int32_t e0 = A.bin_off[fb], e1 = A.bin_off[fb + 1];
                 // sample rows stay below 2^22, where sr + 0.5 is exact in f32
                 const bool f32_ok = sub0 < (1 << 22);
@@ -1213,7 +1232,7 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
                     }
                 }
                 __syncwarp();
-                const bool eo = F.rule == Z2D_FILL_EVEN_ODD;
+                const bool eo = (meta & RF_EVEN_ODD) != 0;
                 // each lane's winding change per sample row, then the
                 // winding at the lane's first column: the exclusive scans of
                 // rows (0, 1) and (2, 3) run packed as lo + 65536 hi (every
@@ -1289,7 +1308,7 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
                 }
                 __syncwarp();
             }
-            if (F.fast_kind == FAST_PIXEL_SRC_OVER && !exact && bounded) {
+            if (((meta >> RF_FAST_SHIFT) & 3u) == FAST_PIXEL_SRC_OVER && !exact && bounded) {
                 // Pixel source, integer src_over: the compositeOpaque /
                 // compositeOpacity paths reduce to src_over(d, pixel) at full
                 // coverage and src_over(d, dst_in(pixel, opacity)) otherwise.
@@ -1297,9 +1316,10 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
                 // same with the downsampled mask value as opacity; at zero
                 // coverage both leave the pixel as it is.
                 // (A bounded fill outside its rows was skipped above.)
-                const I16 px = F.src.pix;
+                const uint32_t pw = (uint32_t)rb.y;
+                const I16 px{pw & 0xFFu, (pw >> 8) & 0xFFu, (pw >> 16) & 0xFFu, pw >> 24};
                 const int full = direct ? 1 : 16;
-                const int32_t xlo = S.start_x, xhi = direct ? W : min(S.end_x, W);
+                const int32_t xlo = start_x, xhi = direct ? W : min(end_x, W);
                 if (fmt <= Z2D_FORMAT_RGBA) {
                     // Lane k holds the source word for coverage k: the pixel
                     // at k = full, dst_in(pixel, opacity(k)) below it.
@@ -1336,6 +1356,8 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
                 }
                 continue;
             }
+            const FillState &S = A.st[f];
+            const FillCmd &F = A.fills[f];
             if (ssaa) {
                 // every pixel of the composite region runs the batch
                 // [dst_in(pattern, mask), op] (supersample.zig:171-184)
@@ -1537,9 +1559,11 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     // node info, then the per-node leaf counts of the curves' frontier items
     const size_t info_bytes = (sizeof(NodeInfo) * (size_t)n_nodes + 255) & ~(size_t)255;
     const size_t items_bytes = (sizeof(uint16_t) * kFrontier * (size_t)n_nodes + 255) & ~(size_t)255;
+    const size_t st_bytes = (sizeof(FillState) * (size_t)n_fills + 255) & ~(size_t)255;
     if (c.node_info.ensure(info_bytes + items_bytes + 3 * sizeof(int32_t) * (size_t)n_nodes) ||
-        c.fill_state.ensure(sizeof(FillState) * (size_t)n_fills))
+        c.fill_state.ensure(st_bytes + sizeof(RasterFill) * (size_t)n_fills))
         return Z2D_ERR_OUT_OF_MEMORY;
+    RasterFill *d_rf = reinterpret_cast<RasterFill *>(c.fill_state.as<uint8_t>() + st_bytes);
     NodeInfo *d_info = c.node_info.as<NodeInfo>();
     uint16_t *d_items = reinterpret_cast<uint16_t *>(c.node_info.as<uint8_t>() + info_bytes);
     int32_t *d_curves = reinterpret_cast<int32_t *>(c.node_info.as<uint8_t>() + info_bytes + items_bytes);  // 2 queues
@@ -1640,7 +1664,7 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
         if (rc) return rc;
     }
     k_edge_fill<<<n_fills, 128, 0, c.stream>>>(d_st, n_fills, d_edge_fill);
-    k_fill_setup<<<grid_for(n_fills, 64), 64, 0, c.stream>>>(d_fills, d_st, n_fills, d_jobs, d_cnt);
+    k_fill_setup<<<grid_for(n_fills, 64), 64, 0, c.stream>>>(d_fills, d_st, n_fills, d_jobs, d_cnt, d_rf);
     c.timer_end(c.t_flatten, tf);
     c.launches += 4;
     Z2D_CUDA(cudaMemcpyAsync(rb, d_cnt, sizeof(int32_t) * CNT_COUNT, cudaMemcpyDeviceToHost, c.stream));
@@ -1744,6 +1768,7 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     A.bin_off = d_fb_off;
     A.band_count = d_band_count;
     A.band_fills = d_band_fills;
+    A.rfills = d_rf;
     A.masks = c.masks.as<uint8_t>();
     A.n_jobs = n_jobs;
     A.job0 = jobs[0];

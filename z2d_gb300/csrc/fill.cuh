@@ -109,6 +109,25 @@ struct FillState {
     int32_t cull_x0, cull_x1;   // columns a tile must overlap to be affected
 };
 
+// What k_raster reads of a fill on its common path, in two 16-byte loads
+// (written by k_fill_setup from the FillCmd and FillState).
+struct RasterFill {
+    int32_t start_x, end_x, start_y, end_y;  // FillState's draw box
+    uint32_t meta;  // RF_* fields below
+    uint32_t px;    // pattern pixel's RGBA lanes (FillCmd.px_rgba), one byte each: r | g << 8 | b << 16 | a << 24
+    int32_t _pad[2];
+};
+static_assert(sizeof(RasterFill) == 32, "RasterFill: two 16-byte loads");
+enum : uint32_t {
+    RF_OP_MASK = 0x1F,        // operator
+    RF_AA_SHIFT = 5,          // anti-aliasing mode, 2 bits
+    RF_EVEN_ODD = 1u << 7,    // fill rule
+    RF_FAST_SHIFT = 8,        // FillCmd.fast_kind, 2 bits
+    RF_EXACT = 1u << 10,      // FILL_EXACT
+    RF_SS_ZERO = 1u << 11,    // FILL_SS_ZERO
+    RF_BOUNDED = 1u << 12,    // the operator is bounded
+};
+
 // counters (int32 slots; the mask byte count is a 64-bit pair)
 enum : int32_t {
     CNT_EDGES = 0,
