@@ -514,8 +514,9 @@ __global__ void __launch_bounds__(32 * kFlattenWarps) k_curve_count_w(const z2d_
         if (ok && inf.chords && __all_sync(all, scr_n <= kScratch)) {
             int32_t base = -1;
             if (lane == 0) {
-                const int32_t b = atomicAdd(&counters[CNT_POOL], leaves + 1);
-                base = (b >= 0 && (long long)b + leaves + 1 <= pool_cap) ? b : -1;
+                const unsigned long long b = atomicAdd(reinterpret_cast<unsigned long long *>(&counters[CNT_POOL]),
+                                                       (unsigned long long)(leaves + 1));
+                base = (b + (unsigned long long)(leaves + 1) <= (unsigned long long)pool_cap) ? (int32_t)b : -1;
             }
             base = __shfl_sync(all, base, 0);
             if (base >= 0) {
@@ -1586,7 +1587,9 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
         (unsigned)std::min<long long>(grid_for(n_nodes, kFlattenWarps), (long long)c.sm_count * 8);
     // per curve warp: kScratch leaf points per lane; then the curve pool
     const size_t scratch_pts = (size_t)curve_blocks * kFlattenWarps * 32 * kScratch;
-    const int32_t pool_cap = (int32_t)std::min<long long>(64ll << 20, std::max<long long>(1ll << 20, 16ll * n_nodes));
+    // pool capacity: 16 points per node, or what the previous call asked for
+    const int32_t pool_cap = (int32_t)std::min<long long>(
+        64ll << 20, std::max<long long>({1ll << 20, 16ll * n_nodes, c.pool_demand + c.pool_demand / 4}));
     if (c.curve_pool.ensure(sizeof(double2) * (scratch_pts + (size_t)pool_cap))) return Z2D_ERR_OUT_OF_MEMORY;
     double2 *d_scratch = c.curve_pool.as<double2>();
     double2 *d_pool = d_scratch + scratch_pts;
@@ -1625,6 +1628,8 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
         Z2D_CUDA(cudaMemcpyAsync(rb_tot, stroke_totals_dev(srun), 2 * sizeof(long long), cudaMemcpyDeviceToHost,
                                  c.stream));
     Z2D_CUDA(cudaStreamSynchronize(c.stream));
+    c.pool_demand = (long long)std::min<unsigned long long>(
+        64ull << 20, ((unsigned long long)(uint32_t)rb[CNT_POOL + 1] << 32) | (uint32_t)rb[CNT_POOL]);
     if (rb[CNT_STATUS] != 0) {
         set_error(rb[CNT_STATUS] == Z2D_ERR_INVALID_STATE ? "curve subdivision exceeded its depth bound"
                                                           : "batch too large: more than 2^31 edges in one polygon");

@@ -137,7 +137,7 @@ enum : int32_t {
     CNT_STATUS = 5,
     CNT_CURVES = 6,       // curves queued by k_node_count_w
     CNT_CURVES_EMIT = 7,  // curves queued by k_node_emit_w
-    CNT_POOL = 8,         // points used in the curve pool
+    CNT_POOL = 8,         // points asked of the curve pool (64-bit pair, + 9)
     CNT_COUNT = 10
 };
 

@@ -68,6 +68,7 @@ struct Ctx {
     DevBuf stroke_b;    // device stroker: per point state
     DevBuf stroke_c;    // device stroker: contour points
     DevBuf curve_pool;  // leaf points of flattened curves (count pass -> emit pass)
+    long long pool_demand = 0;  // curve-pool points the last flatten asked for
     HostBuf staging;    // pinned upload staging
     HostBuf readback;   // pinned readback
     cudaEvent_t done = nullptr;
