@@ -759,6 +759,34 @@ static int stroke_prepare(const z2d_node *nodes, size_t n_nodes, const stroke::O
     return Z2D_OK;
 }
 
+// The fill command of a polygon drawn with a pattern and options (the
+// pattern part of prepare_fill), for polygons that come from elsewhere than
+// nodes: non-zero rule, points already scaled.
+static int prepare_polygon_fill_one(const z2d_surface &s, int32_t job, const z2d_pattern *pattern, int aa,
+                                    int32_t op, int32_t precision, double tolerance, FillCmd &F, DevGradient &grad,
+                                    bool &needs_grad) {
+    z2d_fill_cmd fc;
+    memset(&fc, 0, sizeof(fc));
+    fc.pattern = pattern;
+    fc.opts.anti_aliasing = aa;
+    fc.opts.fill_rule = Z2D_FILL_NON_ZERO;  // painter.zig:306-341
+    fc.opts.op = op;
+    fc.opts.precision = precision;
+    fc.opts.tolerance = tolerance;
+    // a placeholder closed path so that prepare_fill keeps the command
+    z2d_node nd[2];
+    memset(nd, 0, sizeof(nd));
+    nd[0].tag = Z2D_MOVE_TO;
+    nd[1].tag = Z2D_CLOSE_PATH;
+    fc.n_nodes = 2;
+    const int rc = prepare_fill(s, job, nd, 2, fc, F, grad, needs_grad);
+    if (rc) return rc;
+    F.node_off = 0;
+    F.n_nodes = 0;
+    F.edge_scale = 1.0;  // the stroker's points are already scaled
+    return Z2D_OK;
+}
+
 // A prepared fill drawing a pattern with given options (the pattern part
 // of prepare_fills), for polygons that come from elsewhere than nodes.
 static int prepare_polygon_fill(const z2d_surface &s, int32_t job, const z2d_pattern *pattern, int aa, int32_t op,
@@ -808,17 +836,20 @@ static int draw_core(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_no
     // per stroke: options, then the device stroker's input (solid) or the
     // host-built polygon (dashed), in parallel
     const size_t ns = strokes.size();
-    std::vector<stroke::Polygon> polys(ns);
+    if (c.poly_cache.size() < ns) c.poly_cache.resize(ns);
+    std::vector<stroke::Polygon> &polys = c.poly_cache;
     std::vector<StrokePrep> preps(ns);
     std::vector<stroke::Options> sopts(ns);
     std::vector<uint8_t> on_device(ns, 0);
     std::vector<int> aas(ns, 0), rcs(ns, 0);
     std::vector<std::string> errs(ns);
     {
-        const size_t nt = std::max<size_t>(1, std::min<size_t>(std::thread::hardware_concurrency(), ns / 256 + 1));
-        std::atomic<size_t> next{0};
-        auto work = [&] {
-            for (size_t k; (k = next.fetch_add(1)) < ns;) {
+        // on the host pool, 16 strokes per task (the pool's threads keep
+        // their point arenas between calls)
+        constexpr size_t kTask = 16;
+        auto work = [&](size_t t) {
+            for (size_t k = t * kTask, k1 = std::min(ns, k + kTask); k < k1; k++) {
+                polys[k].clear();  // (an earlier call's polygon)
                 const z2d_draw_cmd &cm = cmds[strokes[k]];
                 if (!cm.pattern || cm.node_offset > n_nodes || cm.n_nodes > n_nodes - cm.node_offset) {
                     rcs[k] = Z2D_ERR_INVALID_ARGUMENT;
@@ -841,10 +872,7 @@ static int draw_core(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_no
                 if (rc) errs[k] = last_error();
             }
         };
-        std::vector<std::thread> pool;
-        for (size_t t = 1; t < nt; t++) pool.emplace_back(work);
-        work();
-        for (auto &t : pool) t.join();
+        HostPool::get().run((ns + kTask - 1) / kTask, work);
         for (size_t k = 0; k < ns; k++)
             if (rcs[k]) {
                 set_error(errs[k].c_str());
@@ -853,58 +881,113 @@ static int draw_core(Ctx &c, const z2d_job *jobs_in, size_t n_jobs, const z2d_no
     }
     std::vector<int64_t> stroke_of(n_cmds, -1);
     for (size_t k = 0; k < ns; k++) stroke_of[strokes[k]] = (int64_t)k;
+    // Every (job, command) entry in job order is prepared on the host pool:
+    // its fill command (a fill's, or the fill drawing a stroke's polygon)
+    // and gradient table; the loop below then assembles them in order, and
+    // the first failing entry (or job) in that order decides the error.
+    std::vector<int> job_rc(n_jobs, 0);
+    std::vector<size_t> ent_job, ent_cmd;
+    ent_job.reserve(n_cmds);
+    ent_cmd.reserve(n_cmds);
+    for (size_t j = 0; j < n_jobs; j++) {
+        const z2d_job &jb = jobs_in[j];
+        job_rc[j] = check_surface(&jb.surface);
+        if (!job_rc[j] && jb.surface.location != Z2D_MEM_DEVICE) job_rc[j] = -1;  // reported below
+        if (job_rc[j]) continue;
+        for (uint64_t q = 0; q < jb.n_cmds; q++) {
+            ent_job.push_back(j);
+            ent_cmd.push_back(jb.cmd_offset + q);
+        }
+    }
+    const size_t n_ent = ent_cmd.size();
+    std::vector<FillCmd> ent_fill(n_ent);
+    std::vector<int32_t> ent_slot(n_ent, -1);  // gradient slot (patterns other than pixels)
+    int32_t n_slots = 0;
+    for (size_t e = 0; e < n_ent; e++)
+        if (cmds[ent_cmd[e]].pattern && cmds[ent_cmd[e]].pattern->kind != Z2D_PATTERN_PIXEL) ent_slot[e] = n_slots++;
+    std::vector<DevGradient> ent_grad((size_t)n_slots);
+    std::vector<uint8_t> ent_drawn(n_ent, 0), ent_ng(n_ent, 0);
+    std::vector<int> ent_rc(n_ent, 0);
+    // prepares entry e into the slots above; `scratch` takes a gradient a
+    // pixel pattern would never ask for
+    auto prepare_entry = [&](size_t e, DevGradient &scratch) -> int {
+        const size_t j = ent_job[e], i = ent_cmd[e];
+        const z2d_job &jb = jobs_in[j];
+        const z2d_draw_cmd &cm = cmds[i];
+        DevGradient &g = ent_slot[e] >= 0 ? ent_grad[(size_t)ent_slot[e]] : scratch;
+        bool ng = false;
+        int rc;
+        if (cm.kind == Z2D_DRAW_FILL) {
+            z2d_fill_cmd fc;
+            fc.pattern = cm.pattern;
+            fc.node_offset = cm.node_offset;
+            fc.n_nodes = cm.n_nodes;
+            fc.opts = cm.fill;
+            rc = prepare_fill(jb.surface, (int32_t)j, nodes, n_nodes, fc, ent_fill[e], g, ng);
+            if (!rc && cm.n_nodes > 0) ent_drawn[e] = 1;
+        } else {
+            const size_t k = (size_t)stroke_of[i];
+            if (cm.pattern->kind == Z2D_PATTERN_PIXEL && !pixel_premultiplied(cm.pattern->pixel)) {
+                set_error("PixelSourceNotPreMultiplied");
+                return Z2D_ERR_PIXEL_NOT_PREMULTIPLIED;
+            }
+            const bool drawn = on_device[k] ? !preps[k].subs.empty() : polys[k].points() > 0;
+            if (!drawn) return Z2D_OK;  // nothing is drawn
+            rc = prepare_polygon_fill_one(jb.surface, (int32_t)j, cm.pattern, aas[k], cm.stroke.op,
+                                          cm.stroke.precision, cm.stroke.tolerance, ent_fill[e], g, ng);
+            if (!rc) ent_drawn[e] = 1;
+        }
+        ent_ng[e] = ng && ent_slot[e] >= 0;
+        if (ng && ent_slot[e] < 0) rc = Z2D_ERR_INVALID_ARGUMENT;  // not reached: pixels need no table
+        return rc;
+    };
+    constexpr size_t kTask = 256;
+    HostPool::get().run((n_ent + kTask - 1) / kTask, [&](size_t t) {
+        DevGradient scratch;
+        for (size_t e = t * kTask, e1 = std::min(n_ent, e + kTask); e < e1; e++) ent_rc[e] = prepare_entry(e, scratch);
+    });
     std::vector<FillCmd> fills;
     std::vector<int32_t> grad_of_fill;
     std::vector<DevGradient> grads;
+    fills.reserve(n_ent);
+    grad_of_fill.reserve(n_ent);
     std::vector<DevJob> jobs(n_jobs);
     if (n_jobs > 0) memset(jobs.data(), 0, sizeof(DevJob) * n_jobs);
     StrokeSet sset;
     std::vector<std::pair<int32_t, int32_t>> trig_keys;  // (n, reflect) of each table, in trig order
     std::vector<int32_t> trig_at;
+    size_t e = 0;
     for (size_t j = 0; j < n_jobs; j++) {
         const z2d_job &jb = jobs_in[j];
-        int rc = check_surface(&jb.surface);
-        if (rc) return rc;
-        if (jb.surface.location != Z2D_MEM_DEVICE) {
+        if (job_rc[j]) {
+            if (job_rc[j] > 0) return check_surface(&jb.surface);  // again on this thread, for its message
             set_error("draw_jobs: surfaces must be in device memory");
             return Z2D_ERR_INVALID_ARGUMENT;
         }
         jobs[j].sfc = DevSurface{reinterpret_cast<uint8_t *>(jb.surface.data), jb.surface.format, jb.surface.width,
                                  jb.surface.height};
         jobs[j].fill0 = (int32_t)fills.size();
-        for (uint64_t q = 0; q < jb.n_cmds; q++) {
+        for (uint64_t q = 0; q < jb.n_cmds; q++, e++) {
             const size_t i = jb.cmd_offset + q;
             const z2d_draw_cmd &cm = cmds[i];
-            if (cm.kind == Z2D_DRAW_FILL) {
-                z2d_fill_cmd fc;
-                fc.pattern = cm.pattern;
-                fc.node_offset = cm.node_offset;
-                fc.n_nodes = cm.n_nodes;
-                fc.opts = cm.fill;
-                rc = prepare_fills(jb.surface, (int32_t)j, nodes, n_nodes, &fc, 1, fills, grads, grad_of_fill);
-                if (rc) return rc;
-                continue;
+            if (ent_rc[e]) {  // again on this thread, for its message
+                DevGradient scratch;
+                const int rc = prepare_entry(e, scratch);
+                return rc ? rc : ent_rc[e];
             }
+            if (!ent_drawn[e]) continue;
+            grad_of_fill.push_back(ent_ng[e] ? (int32_t)grads.size() : -1);
+            if (ent_ng[e]) grads.push_back(ent_grad[(size_t)ent_slot[e]]);
+            fills.push_back(ent_fill[e]);
+            if (cm.kind == Z2D_DRAW_FILL) continue;
             const size_t k = (size_t)stroke_of[i];
-            if (cm.pattern->kind == Z2D_PATTERN_PIXEL && !pixel_premultiplied(cm.pattern->pixel)) {
-                set_error("PixelSourceNotPreMultiplied");
-                return Z2D_ERR_PIXEL_NOT_PREMULTIPLIED;
-            }
             if (!on_device[k]) {  // a host-built polygon
-                if (polys[k].points() == 0) continue;  // nothing is drawn
-                rc = prepare_polygon_fill(jb.surface, (int32_t)j, cm.pattern, aas[k], cm.stroke.op,
-                                          cm.stroke.precision, cm.stroke.tolerance, fills, grads, grad_of_fill);
-                if (rc) return rc;
                 fills.back().poly = (int32_t)sset.polys.size();
                 sset.polys.push_back(&polys[k]);
                 continue;
             }
             // a device-stroked command
             StrokePrep &pr = preps[k];
-            if (pr.subs.empty()) continue;  // nothing is drawn
-            rc = prepare_polygon_fill(jb.surface, (int32_t)j, cm.pattern, aas[k], cm.stroke.op, cm.stroke.precision,
-                                      cm.stroke.tolerance, fills, grads, grad_of_fill);
-            if (rc) return rc;
             const stroke::Options &so = sopts[k];
             StrokeDev S;
             memset(&S, 0, sizeof(S));

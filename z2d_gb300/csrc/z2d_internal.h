@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/z2dgpu.h"
+#include "stroke.h"
 #include "z2d_pixel.cuh"
 
 namespace z2dg {
@@ -69,6 +70,9 @@ struct Ctx {
     DevBuf stroke_c;    // device stroker: contour points
     DevBuf curve_pool;  // leaf points of flattened curves (count pass -> emit pass)
     long long pool_demand = 0;  // curve-pool points the last flatten asked for
+    // dashed strokes' polygons of z2dgpu_draw_jobs, kept with their
+    // capacity across calls (building them then touches no fresh pages)
+    std::vector<stroke::Polygon> poly_cache;
     HostBuf staging;    // pinned upload staging
     HostBuf readback;   // pinned readback
     cudaEvent_t done = nullptr;
