@@ -230,6 +230,71 @@ def test_dashed_strokes(gpu, oracle, dashes, offset, cap):
     _cmp(a, b, 0, f"{dashes}/{offset}/{cap}")
 
 
+def _dash_path(rng, w, h):
+    """Subpaths of lines and curves, some closed, with repeated points and
+    points returning to the start (the dasher's degenerate cases)."""
+    nodes = []
+    for _ in range(int(rng.integers(1, 4))):
+        start = rng.uniform([5, 5], [w - 5, h - 5])
+        nodes.append((abi.MOVE_TO, *start, 0, 0, 0, 0))
+        last = start
+        for _ in range(int(rng.integers(1, 7))):
+            r = rng.random()
+            if r < 0.1:  # the same point again
+                nodes.append((abi.LINE_TO, *last, 0, 0, 0, 0))
+            elif r < 0.55:
+                last = rng.uniform([5, 5], [w - 5, h - 5])
+                nodes.append((abi.LINE_TO, *last, 0, 0, 0, 0))
+            else:
+                c = rng.uniform([5, 5, 5, 5, 5, 5], [w - 5, h - 5] * 3)
+                nodes.append((abi.CURVE_TO, *c))
+                last = c[4:]
+        if rng.random() < 0.2:
+            nodes.append((abi.LINE_TO, *start, 0, 0, 0, 0))
+        if rng.random() < 0.5:
+            nodes.append((abi.CLOSE_PATH, 0, 0, 0, 0, 0, 0))
+    return nodes
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_dashed_random_batch(oracle, seed):
+    """Dashed strokes with random dash arrays (zero-length entries
+    included), offsets, caps, joins, widths and transforms, drawn in one
+    z2dgpu_draw_jobs call over many surfaces (their polygons uploaded and
+    rasterised with the fills), against the oracle's rasteriser."""
+    torch = pytest.importorskip("torch")
+    from z2d_gb300 import painter
+    so = StrokeOracle(oracle)
+    rng = np.random.default_rng(4242 + seed)
+    jobs, refs = [], []
+    for j in range(24):
+        w, h = int(rng.integers(40, 160)), int(rng.integers(40, 120))
+        dev = _bg("rgba", w, h, 700 + j).to_device("cuda")
+        ref = _bg("rgba", w, h, 700 + j)
+        ops = []
+        for k in range(5):
+            nd = int(rng.integers(1, 6))
+            dashes = tuple(float(v) if rng.random() > 0.2 else 0.0 for v in rng.uniform(0.5, 25.0, nd))
+            if not any(dashes):
+                dashes = (4.0,) + dashes[1:]
+            offset = float(rng.choice([0.0, rng.uniform(-30, 30), rng.uniform(0, 200)]))
+            opts = StrokeOptions(line_width=float(rng.uniform(0.5, 14)),
+                                 line_join=("miter", "round", "bevel")[int(rng.integers(0, 3))],
+                                 line_cap=("butt", "round", "square")[int(rng.integers(0, 3))],
+                                 miter_limit=float(rng.uniform(1.0, 12.0)),
+                                 dashes=dashes, dash_offset=offset,
+                                 transformation=TRANSFORMS[list(TRANSFORMS)[int(rng.integers(0, 4))]])
+            ops.append(("stroke", Pattern.from_pixel(random_premultiplied_pixel(rng)), _dash_path(rng, w, h), opts))
+        for kind, pat, nodes, o in ops:
+            assert so.stroke(ref, pat, nodes, o) == abi.OK
+        jobs.append((dev, ops))
+        refs.append(ref)
+    painter.draw_jobs(jobs)
+    torch.cuda.synchronize()
+    for j, ((dev, _), ref) in enumerate(zip(jobs, refs)):
+        _cmp(dev.to_host(), ref, 0, f"job {j}")
+
+
 def test_draw_jobs_mixed(oracle):
     """z2dgpu_draw_jobs: fills and strokes (dashed or not) interleaved over
     many surfaces equal the same calls one by one."""
