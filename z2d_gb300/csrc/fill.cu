@@ -1135,7 +1135,6 @@ constexpr uint32_t kBias2 = 0x80008000u;
 // columns per lane: 32 with 4x sampling, 8 without); the pair holding it is
 // stored at ((c % per) / 2) * 32 + lane, so a warp reading pair k of every
 // lane touches 32 consecutive words.
-__device__ __forceinline__ int pair_index(int c, int per) { return (((c % per) >> 1) << 5) | (c / per); }
 
 // One CTA per tile of 4 rows x 256 pixels; warp w owns pixel row w of the
 // tile and lane l its pixels [8l, 8l+8).  Warps never wait for each other:
@@ -1201,7 +1200,7 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
             const bool exact = (meta & RF_EXACT) != 0;
             const bool in_rows = y >= start_y && y <= end_y;
             if (!in_rows && boxed) continue;
-            const int32_t sc = direct ? 1 : 4, per = 8 * sc;
+            const int32_t sc = direct ? 1 : 4, per = 8 * sc, lg_per = direct ? 3 : 5;
             // coverage of pixel q (0..16) is byte q / 2 of cov_ev (q even)
             // or cov_od (q odd)
             uint32_t cov_ev = 0, cov_od = 0;
@@ -1211,24 +1210,48 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
                 // sample rows stay below 2^22, where sr + 0.5 is exact in f32
                 const bool f32_ok = sub0 < (1 << 22);
                 const float fsub = (float)sub0 + 0.5f;
-                for (int32_t ei = e0 + lane; ei < e1; ei += 32) {
-                    const int32_t id = A.bins[ei];
-                    const float4 ef = __ldg(reinterpret_cast<const float4 *>(A.edges + id));
-                    const int2 er = __ldg(reinterpret_cast<const int2 *>(&A.edges[id].rt));
-                    const int32_t dir = __float_as_int(ef.w);
-                    const int32_t lo = max(er.x, sub0), hi = min(er.y, sub0 + sc);
-                    for (int32_t sr = lo; sr < hi; sr++) {
-                        int32_t X;
-                        if (!(f32_ok && crossing_f32(ef.x, ef.y, ef.z, fsub + (float)(sr - sub0), X))) {
-                            const DEdge &e = A.edges[id];
-                            X = (int32_t)round(e.x_start + (e.x_inc * (((double)sr + 0.5) - e.top)));
+                // one edge per lane; crossings at or left of the tile's
+                // first sample column all land on column 0, so they are
+                // summed across the warp and added once (instead of one
+                // atomic per edge on the same word)
+                for (int32_t base = e0; base < e1; base += 32) {
+                    const int32_t ei = base + lane;
+                    int32_t id = 0, dir = 0, lo = 0, hi = 0;
+                    float4 ef = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    if (ei < e1) {
+                        id = A.bins[ei];
+                        ef = __ldg(reinterpret_cast<const float4 *>(A.edges + id));
+                        const int2 er = __ldg(reinterpret_cast<const int2 *>(&A.edges[id].rt));
+                        dir = __float_as_int(ef.w);
+                        lo = max(er.x, sub0);
+                        hi = min(er.y, sub0 + sc);
+                    }
+                    for (int r = 0; r < sc; r++) {  // uniform across the warp
+                        const int32_t sr = sub0 + r;
+                        int32_t left = 0;
+                        if (sr >= lo && sr < hi) {
+                            int32_t X;
+                            if (!(f32_ok && crossing_f32(ef.x, ef.y, ef.z, fsub + (float)r, X))) {
+                                const DEdge &e = A.edges[id];
+                                X = (int32_t)round(e.x_start + (e.x_inc * (((double)sr + 0.5) - e.top)));
+                            }
+                            const int32_t c = X - col0;
+                            if (c <= 0) {
+                                left = dir;
+                            } else if (c < ncol) {
+                                // per is 8 or 32 and c > 0: shifts and masks
+                                const int lane_c = c >> lg_per, pair = (c & (per - 1)) >> 1;
+                                const uint32_t inc = (c & 1) ? ((uint32_t)dir << 16) : (uint32_t)dir;
+                                atomicAdd(&words[r * kWordsPerSubRow + ((pair << 5) | lane_c)], inc);
+                                atomicOr(&words[kTouchOff + r * 32 + lane_c], 1u << pair);
+                            }
                         }
-                        int32_t c = X - col0;
-                        if (c < 0) c = 0;
-                        if (c < ncol) {
-                            const uint32_t inc = (c & 1) ? ((uint32_t)dir << 16) : (uint32_t)dir;
-                            atomicAdd(&words[(sr - sub0) * kWordsPerSubRow + pair_index(c, per)], inc);
-                            atomicOr(&words[kTouchOff + (sr - sub0) * 32 + c / per], 1u << ((c % per) >> 1));
+                        // column 0 is the low half of lane 0's pair 0; a net
+                        // zero changes no winding and needs no visit
+                        const int32_t sum = __reduce_add_sync(0xffffffffu, left);
+                        if (lane == 0 && sum != 0) {
+                            atomicAdd(&words[r * kWordsPerSubRow], (uint32_t)sum);
+                            atomicOr(&words[kTouchOff + r * 32], 1u);
                         }
                     }
                 }
