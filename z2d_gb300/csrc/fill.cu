@@ -1256,6 +1256,17 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
                     }
                 }
                 __syncwarp();
+                // no crossing in or left of the tile on any sample row: the
+                // winding is 0 across the tile, nothing is covered
+                uint32_t any_touch = 0;
+#pragma unroll
+                for (int s = 0; s < 4; s++)
+                    if (s < sc) any_touch |= words[kTouchOff + s * 32 + lane];
+                if (!__any_sync(0xffffffffu, any_touch != 0)) {
+                    if (bounded) continue;  // zero coverage draws nothing
+                    goto composite;         // unbounded operators still clear
+                }
+                {
                 const bool eo = (meta & RF_EVEN_ODD) != 0;
                 // each lane's winding change per sample row, then the
                 // winding at the lane's first column: the exclusive scans of
@@ -1331,7 +1342,9 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
                     }
                 }
                 __syncwarp();
+                }
             }
+        composite:
             if (((meta >> RF_FAST_SHIFT) & 3u) == FAST_PIXEL_SRC_OVER && !exact && bounded) {
                 // Pixel source, integer src_over: the compositeOpaque /
                 // compositeOpacity paths reduce to src_over(d, pixel) at full
