@@ -1128,7 +1128,8 @@ struct RasterArgs {
 // kMaxBandEdges edges in a band can never carry a counter across halves).
 constexpr int kWordsPerSubRow = 512;
 constexpr int kTouchOff = 4 * kWordsPerSubRow;  // then 4 x 32 words: pairs touched per (sample row, lane)
-constexpr int kWarpWords = kTouchOff + 4 * 32;
+constexpr int kTotOff = kTouchOff + 4 * 32;     // then 4 x 32 words: winding change per (sample row, lane)
+constexpr int kWarpWords = kTotOff + 4 * 32;
 constexpr uint32_t kBias2 = 0x80008000u;
 
 // Sample column c of a sub-scanline belongs to lane c / per (per = sample
@@ -1244,6 +1245,7 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
                                 const uint32_t inc = (c & 1) ? ((uint32_t)dir << 16) : (uint32_t)dir;
                                 atomicAdd(&words[r * kWordsPerSubRow + ((pair << 5) | lane_c)], inc);
                                 atomicOr(&words[kTouchOff + r * 32 + lane_c], 1u << pair);
+                                atomicAdd(&words[kTotOff + r * 32 + lane_c], (uint32_t)dir);
                             }
                         }
                         // column 0 is the low half of lane 0's pair 0; a net
@@ -1252,6 +1254,7 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
                         if (lane == 0 && sum != 0) {
                             atomicAdd(&words[r * kWordsPerSubRow], (uint32_t)sum);
                             atomicOr(&words[kTouchOff + r * 32], 1u);
+                            atomicAdd(&words[kTotOff + r * 32], (uint32_t)sum);
                         }
                     }
                 }
@@ -1273,15 +1276,13 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
                 // rows (0, 1) and (2, 3) run packed as lo + 65536 hi (every
                 // partial sum is bounded by the band's edge count, at most
                 // kMaxBandEdges < 2^15 in magnitude, so the halves stay apart)
+                // (the crossings also summed each lane's winding change)
                 int32_t tot[4] = {0, 0, 0, 0};
 #pragma unroll
                 for (int s = 0; s < 4; s++) {
                     if (s >= sc) break;
-                    const uint32_t *row = words + s * kWordsPerSubRow;
-                    for (uint32_t m = words[kTouchOff + s * 32 + lane]; m; m &= m - 1) {
-                        const uint32_t v = row[((__ffs(m) - 1) << 5) | lane];
-                        tot[s] += (int32_t)(v & 0xFFFFu) + (int32_t)(v >> 16) - 0x10000;
-                    }
+                    tot[s] = (int32_t)words[kTotOff + s * 32 + lane];
+                    words[kTotOff + s * 32 + lane] = 0u;
                 }
                 const int32_t t01 = tot[0] + tot[1] * 65536, t23 = tot[2] + tot[3] * 65536;
                 int32_t i01 = t01, i23 = t23;
