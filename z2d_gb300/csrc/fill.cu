@@ -1373,9 +1373,12 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
                         const int c = (int)((((q & 1) ? cov_od : cov_ev) >> (8 * (q >> 1))) & 0xFFu);
                         const uint32_t L = __shfl_sync(0xffffffffu, lut_w, c);
                         const int32_t x = px0 + q;
-                        if (c == 0 || x < xlo || x >= xhi) continue;
-                        raw[q] = word_src_over(raw[q], L, has_alpha);
-                        touched |= 1u << q;
+                        // without a branch: the lanes of a warp mostly agree
+                        // on composing, and a select costs less than a split
+                        const bool on = c != 0 && x >= xlo && x < xhi;
+                        const uint32_t nv = word_src_over(raw[q], L, has_alpha);
+                        raw[q] = on ? nv : raw[q];
+                        touched |= (uint32_t)on << q;
                     }
                     continue;
                 }
