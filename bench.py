@@ -50,7 +50,7 @@ PLAIN_FILLS = 300         # per-call arm: fills drawn with one z2dgpu_fill each
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch,
 # from the ncu captures summarised under profiles/
 TRAFFIC = {
-    "k_raster": (214_299_136, "profiles/k_raster_rgba4096_2000paths.md"),
+    "k_raster": (215_802_624, "profiles/k_raster_rgba4096_2000paths.md"),
     "k_mask_op": (544_317_696, "profiles/k_mask_op_rgba8192_src_over.md"),
 }
 
