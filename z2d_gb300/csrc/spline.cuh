@@ -59,32 +59,29 @@ __device__ __forceinline__ bool f32_trunc(double v, float &out) {
 
 // The decision errorSq(k) < tol2 of Spline.decomposeInto, taken in f32 when
 // that is safe.  GB300 runs f64 at a small fraction of its f32 rate, and the
-// error test is most of the subdivision's f64 work; only the control-point
-// differences (exact f64 subtractions, as in errorSq) stay in f64.  Every
-// f32 quantity carries an error bound built from first-order rounding
-// analysis with slack: inputs (truncation) < 2u, each operation u
-// (u = 2^-24), propagated through the projection and the squared norms.
+// error test is most of the subdivision's f64 work.  Every f32 quantity
+// carries an absolute error bound built from first-order rounding analysis
+// with slack: each input's own bound, each operation u (u = 2^-24),
+// propagated through the projection and the squared norms.
 // Returns 1 / 0 when the f32 value is farther than its bound from tol2 and,
 // on the projection branches, from the branch condition; -1 otherwise (the
 // caller then evaluates errorSq in f64).
-__device__ __forceinline__ int error_sq_lt_f32(double bx64, double by64, double cx64, double cy64, bool proj,
-                                               double dx64, double dy64, float tol2f, float tol2e) {
+__device__ __forceinline__ int error_sq_lt_f32_core(float bx, float by, float cx, float cy, float ebx, float eby,
+                                                    float ecx, float ecy, bool proj, float dx, float dy, float edx,
+                                                    float edy, float tol2f, float tol2e) {
     const float U = 5.9604644775390625e-8f;  // 2^-24
-    float bx, by, cx, cy, dx = 0.0f, dy = 0.0f;
-    if (!f32_trunc(bx64, bx) || !f32_trunc(by64, by) || !f32_trunc(cx64, cx) || !f32_trunc(cy64, cy)) return -1;
-    float ebx = 2.0f * U * fabsf(bx), eby = 2.0f * U * fabsf(by), ecx = 2.0f * U * fabsf(cx), ecy = 2.0f * U * fabsf(cy);
     if (proj) {
-        if (!f32_trunc(dx64, dx) || !f32_trunc(dy64, dy)) return -1;
-        const float edx = 2.0f * U * fabsf(dx), edy = 2.0f * U * fabsf(dy);
         const float dd = dx * dx + dy * dy;
-        const float edd = 8.0f * U * dd;
+        // the inputs' errors carried through the squares, then the roundings
+        const float edd = 2.0f * fabsf(dx) * edx + edx * edx + 2.0f * fabsf(dy) * edy + edy * edy + 3.0f * U * dd;
 #pragma unroll
         for (int i = 0; i < 2; i++) {
             float &px = i ? cx : bx, &py = i ? cy : by;
             float &epx = i ? ecx : ebx, &epy = i ? ecy : eby;
             const float t1 = px * dx, t2 = py * dy;
             const float pd = t1 + t2;
-            const float epd = 8.0f * U * (fabsf(t1) + fabsf(t2));
+            const float epd = fabsf(dx) * epx + fabsf(px) * edx + epx * edx + fabsf(dy) * epy + fabsf(py) * edy +
+                              epy * edy + 2.0f * U * (fabsf(t1) + fabsf(t2));
             const float diff = pd - dd;
             const float m = 1.125f * (epd + edd) + 2.0f * U * fabsf(diff) + 1e-30f;
             if (diff > m) {  // pd >= dd: subtract the whole chord
@@ -117,6 +114,38 @@ __device__ __forceinline__ int error_sq_lt_f32(double bx64, double by64, double 
     if (e - E > tol2f) return 0;
     return -1;
 }
+// From the exact f64 differences b - a, c - a, d - a (truncation error < 2u
+// of each).
+__device__ __forceinline__ int error_sq_lt_f32(double bx64, double by64, double cx64, double cy64, bool proj,
+                                               double dx64, double dy64, float tol2f, float tol2e) {
+    const float U = 5.9604644775390625e-8f;  // 2^-24
+    float bx, by, cx, cy, dx = 0.0f, dy = 0.0f;
+    if (!f32_trunc(bx64, bx) || !f32_trunc(by64, by) || !f32_trunc(cx64, cx) || !f32_trunc(cy64, cy)) return -1;
+    if (proj && (!f32_trunc(dx64, dx) || !f32_trunc(dy64, dy))) return -1;
+    return error_sq_lt_f32_core(bx, by, cx, cy, 2.0f * U * fabsf(bx), 2.0f * U * fabsf(by), 2.0f * U * fabsf(cx),
+                                2.0f * U * fabsf(cy), proj, dx, dy, 2.0f * U * fabsf(dx), 2.0f * U * fabsf(dy), tol2f,
+                                tol2e);
+}
+// From the knots' coordinates, truncated to f32 (error < 2u of each) and
+// subtracted in f32 (one more rounding): no f64 instruction at all, at the
+// price of wider bounds (the coordinates' size instead of the differences').
+__device__ __forceinline__ int error_sq_lt_f32_pts(double ax64, double ay64, double bx64, double by64, double cx64,
+                                                   double cy64, double dx64, double dy64, bool proj, float tol2f,
+                                                   float tol2e) {
+    const float U = 5.9604644775390625e-8f;  // 2^-24
+    float ax, ay, pbx, pby, pcx, pcy, pdx = 0.0f, pdy = 0.0f;
+    if (!f32_trunc(ax64, ax) || !f32_trunc(ay64, ay) || !f32_trunc(bx64, pbx) || !f32_trunc(by64, pby) ||
+        !f32_trunc(cx64, pcx) || !f32_trunc(cy64, pcy))
+        return -1;
+    if (proj && (!f32_trunc(dx64, pdx) || !f32_trunc(dy64, pdy))) return -1;
+    const float bx = pbx - ax, by = pby - ay, cx = pcx - ax, cy = pcy - ay, dx = pdx - ax, dy = pdy - ay;
+    const float eax = 2.0f * U * fabsf(ax), eay = 2.0f * U * fabsf(ay);
+    return error_sq_lt_f32_core(bx, by, cx, cy, eax + 2.0f * U * fabsf(pbx) + U * fabsf(bx),
+                                eay + 2.0f * U * fabsf(pby) + U * fabsf(by), eax + 2.0f * U * fabsf(pcx) + U * fabsf(cx),
+                                eay + 2.0f * U * fabsf(pcy) + U * fabsf(cy), proj, dx, dy,
+                                eax + 2.0f * U * fabsf(pdx) + U * fabsf(dx), eay + 2.0f * U * fabsf(pdy) + U * fabsf(dy),
+                                tol2f, tol2e);
+}
 
 // The squared tolerance of a subdivision, in f64 and as a truncated f32
 // with its error bound.
@@ -138,8 +167,12 @@ __device__ __forceinline__ Tol make_tol(double tol) {
 __device__ __forceinline__ bool below_tol(const Knots &k, const Tol &t) {
     if (t.f_ok) {
         const bool proj = k.ax != k.dx || k.ay != k.dy;
-        const int r = error_sq_lt_f32(k.bx - k.ax, k.by - k.ay, k.cx - k.ax, k.cy - k.ay, proj, k.dx - k.ax,
-                                      k.dy - k.ay, t.f, t.e);
+        // from the coordinates first (no f64), then from the exact f64
+        // differences, then errorSq itself
+        int r = error_sq_lt_f32_pts(k.ax, k.ay, k.bx, k.by, k.cx, k.cy, k.dx, k.dy, proj, t.f, t.e);
+        if (r >= 0) return r != 0;
+        r = error_sq_lt_f32(k.bx - k.ax, k.by - k.ay, k.cx - k.ax, k.cy - k.ay, proj, k.dx - k.ax, k.dy - k.ay, t.f,
+                            t.e);
         if (r >= 0) return r != 0;
     }
     return error_sq(k) < t.d;
