@@ -1190,6 +1190,9 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
             hits &= hits - 1;
             const int4 ra = __ldg(reinterpret_cast<const int4 *>(A.rfills + f));
             const int4 rb = __ldg(reinterpret_cast<const int4 *>(A.rfills + f) + 1);
+            // the band's edge range, loaded alongside the record rather than
+            // after the tests on it (fb is a valid slot either way)
+            const int32_t e0 = __ldg(A.bin_off + fb), e1 = __ldg(A.bin_off + fb + 1);
             const int32_t start_x = ra.x, end_x = ra.y, start_y = ra.z, end_y = ra.w;
             const uint32_t meta = (uint32_t)rb.x;
             const int32_t aa = (int32_t)((meta >> RF_AA_SHIFT) & 3u);
@@ -1207,7 +1210,6 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
             uint32_t cov_ev = 0, cov_od = 0;
             if (!exact && in_rows && !(meta & RF_SS_ZERO)) {
                 const int32_t sub0 = y * sc, col0 = x0 * sc, ncol = kTileCols * sc;
-                const int32_t e0 = A.bin_off[fb], e1 = A.bin_off[fb + 1];
                 // sample rows stay below 2^22, where sr + 0.5 is exact in f32
                 const bool f32_ok = sub0 < (1 << 22);
                 const float fsub = (float)sub0 + 0.5f;
