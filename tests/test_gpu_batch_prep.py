@@ -135,3 +135,69 @@ def test_node_check_order(case, code):
         painter.fill(s, pat, nodes, FillOptions())
     assert e.value.code == code
     assert not s.data.any()
+
+
+def _draw_jobs_ops(rng_seed, n_jobs, per_job, w, h):
+    from z2d_gb300.types import StrokeOptions
+    fills = random_fills(seed=rng_seed, n=n_jobs * per_job, w=w, h=h, side_lo=4, side_hi=40, seg_lo=3, seg_hi=6)
+    jobs = []
+    for j in range(n_jobs):
+        ops = []
+        for k in range(per_job):
+            pat, nodes, fo = fills[j * per_job + k]
+            if k % 3 == 1:
+                ops.append(("stroke", pat, nodes, StrokeOptions(line_width=2.0, dashes=(3.0, 2.0) if k % 2 else ())))
+            else:
+                ops.append(("fill", pat, nodes, fo))
+        jobs.append(ops)
+    return jobs
+
+
+def test_draw_jobs_first_failing_entry_decides_the_error():
+    """z2dgpu_draw_jobs prepares its (job, command) entries on host threads;
+    the first failing entry in job order decides the error and no surface
+    is drawn."""
+    torch = pytest.importorskip("torch")
+    w, h = 48, 40
+    ops = _draw_jobs_ops(21, 12, 30, w, h)  # 360 entries: the threaded path
+    bad_px = Pattern.from_pixel(Pixel.rgba(200, 2, 3, 4))
+    k1 = ops[7][4]   # a stroke entry of job 7 (k % 3 == 1)
+    ops[7][4] = (k1[0], bad_px, k1[2], k1[3])
+    k2 = ops[9][3]   # a later fill entry with an open path
+    ops[9][3] = (k2[0], k2[1], k2[2][:-2].copy(), k2[3])
+    surfaces = [_bg(w, h, 30 + j).to_device("cuda") for j in range(12)]
+    before = [s.to_host().data.copy() for s in surfaces]
+    with pytest.raises(Z2DError) as e:
+        painter.draw_jobs(list(zip(surfaces, ops)))
+    assert e.value.code == abi.ERR_PIXEL_NOT_PREMULTIPLIED
+    torch.cuda.synchronize()
+    for s, b in zip(surfaces, before):
+        assert np.array_equal(s.to_host().data, b)
+    ops[7][4] = k1  # now the open path is the first failure
+    with pytest.raises(Z2DError) as e:
+        painter.draw_jobs(list(zip(surfaces, ops)))
+    assert e.value.code == abi.ERR_PATH_NOT_CLOSED
+
+
+def test_draw_jobs_threaded_matches_oracle(oracle):
+    """A draw_jobs call large enough for the threaded preparation equals the
+    commands drawn one by one by the oracle."""
+    torch = pytest.importorskip("torch")
+    import sys
+    sys.path.insert(0, __import__("os").path.dirname(__file__))
+    from backends import StrokeOracle
+    w, h = 64, 48
+    ops = _draw_jobs_ops(22, 10, 30, w, h)
+    so = StrokeOracle(oracle)
+    surfaces, refs = [], []
+    for j in range(10):
+        surfaces.append(_bg(w, h, 60 + j).to_device("cuda"))
+        ref = _bg(w, h, 60 + j)
+        for kind, pat, nodes, o in ops[j]:
+            rc = oracle.fill(ref, pat, nodes, o) if kind == "fill" else so.stroke(ref, pat, nodes, o)
+            assert rc == abi.OK
+        refs.append(ref)
+    painter.draw_jobs(list(zip(surfaces, ops)))
+    torch.cuda.synchronize()
+    for s, r in zip(surfaces, refs):
+        assert np.array_equal(s.to_host().data, r.data)
