@@ -95,11 +95,11 @@ class ClockSampler:
     def __init__(self, index=0):
         self.proc = None
         self.index = index
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        import tempfile
+        self.path = os.path.join(tempfile.gettempdir(), f"z2d_bench_clocks_{os.getpid()}.csv")
 
     def start(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -168,16 +168,35 @@ def union_box_pixels(fills):
     return int(cov.sum())
 
 
-def cpu_sample(bg, fills, px, n_fills):
+def cpu_sample(bg, fills, px, n_fills, snapshot_at=None):
+    """The oracle on the whole workload, single-threaded: Mpix/s, seconds,
+    the final surface and a copy of the surface after `snapshot_at` fills
+    (both kept for the parity check of the GPU arms)."""
     from oracle import Oracle
     from z2d_gb300.surface import Surface
     o = Oracle()
     s = Surface("rgba", W, H, bg.copy())
-    t0 = time.perf_counter()
-    for pat, nodes, opts in fills[:n_fills]:
+    snap = None
+    dt = 0.0
+    for i, (pat, nodes, opts) in enumerate(fills[:n_fills]):
+        if i == snapshot_at:
+            snap = s.data.copy()
+        t0 = time.perf_counter()
         o.fill(s, pat, nodes, opts)
-    dt = time.perf_counter() - t0
-    return sum(px[:n_fills]) / 1e6 / dt, dt
+        dt += time.perf_counter() - t0
+    if snapshot_at is not None and snapshot_at >= n_fills:
+        snap = s.data.copy()
+    return sum(px[:n_fills]) / 1e6 / dt, dt, s.data, snap
+
+
+def diff_stats(got, ref):
+    """Differing bytes, differing pixels and the largest channel difference
+    of two RGBA surfaces."""
+    a = np.asarray(got, np.uint8).reshape(-1, 4).astype(np.int16)
+    b = np.asarray(ref, np.uint8).reshape(-1, 4).astype(np.int16)
+    d = np.abs(a - b)
+    return {"differing_bytes": int((d > 0).sum()), "differing_pixels": int((d > 0).any(1).sum()),
+            "max_diff": int(d.max(initial=0))}
 
 
 def host_threads():
@@ -789,6 +808,7 @@ def run_ours(args):
         e1.synchronize()
         step_ms.append(e0.elapsed_time(e1))
     launches = ctx.launch_count - launches0
+    out_batched = surf_t.cpu().numpy()  # the last timed step's surface, for the parity check
     raster_ms, raster_n = ctx.kernel_ms("raster")
     stage = {k: ctx.kernel_ms(k)[0] / args.steps for k in ("flatten", "bins", "raster")}
     ctx.set_timing(False)
@@ -812,6 +832,7 @@ def run_ours(args):
         painter.fill_batch_arrays(hsurf, nodes, cmds, ctx=ctx)
         e2e_s.append(time.perf_counter() - t0)
     e2e_value = mpix_step * args.steps / sum(e2e_s)
+    out_e2e = host.copy()
     h2d = bg.nbytes + nodes.nbytes + len(fills) * 64
     d2h = bg.nbytes
 
@@ -831,6 +852,7 @@ def run_ours(args):
     plain_ms = e0.elapsed_time(e1)
     plain_mpix = sum(px[:PLAIN_FILLS]) / 1e6
     call_us.sort()
+    out_plain = surf_t.cpu().numpy()
 
     if rank != 0:
         clocks.stop()
@@ -841,7 +863,7 @@ def run_ours(args):
     raster_ms_per = raster_ms / max(raster_n, 1)
     achieved = alg_bytes / (raster_ms_per / 1e3) / 1e9
     arms = set(args.arms.split(",")) if args.arms not in ("all", "") else {"compositor", "breadth", "star", "jobs",
-                                                                            "serving", "cpu", "png"}
+                                                                            "serving", "cpu", "png", "parity"}
     comp = comp_roof = star = jobs = None
     if "compositor" in arms:
         comp = compositor_sweep(ctx, stream, dev)
@@ -858,7 +880,18 @@ def run_ours(args):
         jobs = jobs_arm(ctx, stream, dev)
     png_res = png_arm(ctx, surf, peaks["hbm_gbs"]) if "png" in arms else None
     serving = serving_arm(dev) if "serving" in arms else None
-    cpu_v, cpu_dt = cpu_sample(bg, fills, px, CPU_SAMPLE_FILLS) if "cpu" in arms else (None, 0.0)
+    # the oracle draws the whole workload (the CPU baseline) and the same
+    # surfaces are compared with the GPU arms' outputs (outside any timing)
+    parity = None
+    if "cpu" in arms or "parity" in arms:
+        cpu_v, cpu_dt, ref_all, ref_plain = cpu_sample(bg, fills, px, CPU_SAMPLE_FILLS, snapshot_at=PLAIN_FILLS)
+        if CPU_SAMPLE_FILLS == N_FILLS:
+            parity = {"reference": f"oracle (C++ restatement of z2d), all {N_FILLS} fills on the 4096x4096 surface",
+                      "batched": diff_stats(out_batched, ref_all), "e2e": diff_stats(out_e2e, ref_all),
+                      "plain": dict(diff_stats(out_plain, ref_plain), fills=PLAIN_FILLS)}
+            parity["bit_exact"] = all(parity[k]["differing_bytes"] == 0 for k in ("batched", "e2e", "plain"))
+    else:
+        cpu_v, cpu_dt = None, 0.0
     line = {
         "metric": "Mpix/s fill+composite (src_over, 4096x4096 RGBA, 2000 random paths)",
         "value": value, "unit": "Mpix/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -878,6 +911,7 @@ def run_ours(args):
         "serving": serving,
         "png": png_res,
         "batched_over_plain": (mpix_step / (total_ms / args.steps / 1e3)) / (plain_mpix / (plain_ms / 1e3)),
+        "parity": parity,
         "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": "k_raster", "achieved": achieved, "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": TRAFFIC["k_raster"][0],
@@ -903,7 +937,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--arms", default="all",
                     help="extra arms beside the batched / e2e / per-call fill arms: 'all', 'none' or a comma "
-                         "list of compositor, breadth, star, jobs, serving, cpu, png (shorter runs for profiling)")
+                         "list of compositor, breadth, star, jobs, serving, cpu, png, parity (shorter runs for profiling)")
     ap.add_argument("--jobs", type=int, default=4096,
                     help="surfaces of the batched-jobs arm (smaller for profiling captures)")
     args = ap.parse_args()

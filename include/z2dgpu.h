@@ -381,7 +381,11 @@ Z2D_API int z2dgpu_composite(z2dgpu_ctx *ctx, z2d_surface *dst, int32_t dst_x,
  * array is shared by all calls on a device: calls whose GPU work overlaps
  * (other streams, other threads) race on it, while calls queued in order on
  * one stream do not.  The first call on a device looks up the array's
- * device address, so make that call before any stream capture. */
+ * device address, so make that call before any stream capture; the address
+ * is kept for the life of the process, so do not use this entry point on a
+ * device after cudaDeviceReset there.  A call with gradient params is
+ * rejected with Z2D_ERR_INVALID_ARGUMENT while `stream` is capturing: their
+ * descriptors are copied from memory that does not outlive the call. */
 Z2D_API int z2dgpu_composite_noalloc(int device, void *stream, z2d_surface *dst,
                                      int32_t dst_x, int32_t dst_y, int32_t n_ops,
                                      const z2d_operation *ops, int32_t precision);

@@ -65,6 +65,10 @@ def load_oracle():
             lib.z2doracle_run_pixel.restype = abi.z2d_pixel
             lib.z2doracle_pixel_from_color.argtypes = [abi.z2d_color]
             lib.z2doracle_pixel_from_color.restype = abi.z2d_pixel
+            lib.z2doracle_pow_f32.argtypes = [C.c_float, C.c_float]
+            lib.z2doracle_pow_f32.restype = C.c_float
+            lib.z2doracle_atan2.argtypes = [C.c_double, C.c_double]
+            lib.z2doracle_atan2.restype = C.c_double
             lib.z2doracle_gradient_offset.argtypes = [C.POINTER(abi.z2d_gradient), C.c_int32, C.c_int32]
             lib.z2doracle_gradient_offset.restype = C.c_float
             lib.z2doracle_gradient_pixel.argtypes = [C.POINTER(abi.z2d_gradient), C.c_int32, C.c_int32]
@@ -163,6 +167,14 @@ class Oracle:
 
     def pixel_from_color(self, color):
         return self.lib.z2doracle_pixel_from_color(color.to_abi())
+
+    def pow_f32(self, x: float, y: float) -> float:
+        """std.math.pow(f32, x, y) as z2d computes it."""
+        return self.lib.z2doracle_pow_f32(x, y)
+
+    def atan2(self, y: float, x: float) -> float:
+        """std.math.atan2(f64, y, x) as z2d computes it."""
+        return self.lib.z2doracle_atan2(y, x)
 
     def gradient_offset(self, gradient, x: int, y: int) -> float:
         keep: list = []

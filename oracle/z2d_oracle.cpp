@@ -484,17 +484,323 @@ I16 encode_raw(F4 v) { return I16{enc_ch(v.r), enc_ch(v.g), enc_ch(v.b), enc_ch(
 const float kGamma = 2.2f;             // src/color.zig:206-209
 const float kInvGamma = 1.0f / 2.2f;
 
-// std.math.pow(f32, x, y) for the exponents z2d uses (2.2, 1/2.2, 1):
-// special cases follow Zig's pow (y == 0 or x == 1 -> 1, y == 1 -> x,
-// x == 0 -> 0 for y > 0); the general case is evaluated in double and
-// rounded once, which is within one f32 ulp of Zig's result.
+// -------------------------------------------------------------------
+// The Zig standard-library math z2d calls, restated so that the oracle
+// computes what z2d computes (not the host libm's correctly rounded
+// results).  z2d is a freestanding Zig library (no libc is linked), so
+// Zig's @exp / @log on f32 lower to compiler_rt's expf / logf, which are
+// Zig ports of musl's expf.c / logf.c (themselves FreeBSD msun e_expf.c /
+// e_logf.c); std.math.pow (lib/std/math/pow.zig) is Zig's port of Go's
+// math.Pow; std.math.atan2 / atan (lib/std/math/atan2.zig, atan.zig) are
+// ports of musl's atan2.c / atan.c (FreeBSD e_atan2.c / s_atan.c).
+// Written from those published algorithms; every constant below was
+// checked against its bit pattern, and expf / logf / atan against
+// high-precision values (< 1 ulp).
+// -------------------------------------------------------------------
+uint32_t f32_bits(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+float f32_from(uint32_t u) {
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+uint32_t f64_hi(double d) {
+    uint64_t u;
+    std::memcpy(&u, &d, 8);
+    return (uint32_t)(u >> 32);
+}
+uint32_t f64_lo(double d) {
+    uint64_t u;
+    std::memcpy(&u, &d, 8);
+    return (uint32_t)u;
+}
+
+// std.math.scalbn / ldexp for f32: x * 2^n (exact while the result is
+// normal; below that, rounded once by the final multiply).
+float zscalbnf(float x, int n) {
+    if (n > 127) {
+        x *= f32_from(0x7F000000u);  // 2^127
+        n -= 127;
+        if (n > 127) {
+            x *= f32_from(0x7F000000u);
+            n -= 127;
+            if (n > 127) n = 127;
+        }
+    } else if (n < -126) {
+        x *= f32_from(0x0C800000u);  // 2^-102
+        n += 102;
+        if (n < -126) {
+            x *= f32_from(0x0C800000u);
+            n += 102;
+            if (n < -126) n = -126;
+        }
+    }
+    return x * f32_from((uint32_t)(0x7F + n) << 23);
+}
+
+// compiler_rt expf (musl src/math/expf.c, pre-2017 FreeBSD form):
+// x = k*ln2 + r, exp(r) from a degree-2 rational approximation.
+float zexpf(float x) {
+    const float half[2] = {0.5f, -0.5f};
+    const float ln2hi = f32_from(0x3F317200u), ln2lo = f32_from(0x35BFBE8Eu), invln2 = f32_from(0x3FB8AA3Bu);
+    const float P1 = 11184783.0f / 67108864.0f;   //  0xaaaa8f * 2^-26
+    const float P2 = -11883029.0f / 4294967296.0f;  // -0xb55215 * 2^-32
+    uint32_t hx = f32_bits(x);
+    const int sign = (int)(hx >> 31);
+    hx &= 0x7FFFFFFFu;
+    if (x != x) return x;
+    if (hx >= 0x42AEAC50u) {                       // |x| >= 87.33655
+        if (hx > 0x7F800000u) return x;            // NaN
+        if (hx >= 0x42B17218u && !sign) return x * f32_from(0x7F000000u);  // overflow
+        if (sign && hx >= 0x42CFF1B5u) return 0.0f;  // x <= -103.972084
+    }
+    int k;
+    float hi, lo;
+    if (hx > 0x3EB17218u) {                        // |x| > 0.5 ln2
+        if (hx > 0x3F851592u) k = (int)(invln2 * x + half[sign]);  // |x| > 1.5 ln2
+        else k = 1 - sign - sign;
+        const float fk = (float)k;
+        hi = x - fk * ln2hi;
+        lo = fk * ln2lo;
+        x = hi - lo;
+    } else if (hx > 0x39000000u) {                 // |x| > 2^-14
+        k = 0;
+        hi = x;
+        lo = 0.0f;
+    } else {
+        return 1.0f + x;
+    }
+    const float xx = x * x;
+    const float c = x - xx * (P1 + xx * P2);
+    const float y = 1.0f + (x * c / (2.0f - c) - lo + hi);
+    return k == 0 ? y : zscalbnf(y, k);
+}
+
+// compiler_rt logf (musl src/math/logf.c, pre-2017 FreeBSD form): x
+// reduced into [sqrt(2)/2, sqrt(2)], log(1+f) = f - hfsq + s*(hfsq+R).
+float zlogf(float x) {
+    const float ln2_hi = f32_from(0x3F317180u), ln2_lo = f32_from(0x3717F7D1u);
+    const float Lg1 = 11184810.0f / 16777216.0f;  // 0xaaaaaa * 2^-24
+    const float Lg2 = 13420051.0f / 33554432.0f;  // 0xccce13 * 2^-25
+    const float Lg3 = 9562606.0f / 33554432.0f;   // 0x91e9ee * 2^-25
+    const float Lg4 = 16293414.0f / 67108864.0f;  // 0xf89e26 * 2^-26
+    uint32_t ix = f32_bits(x);
+    int k = 0;
+    if (ix < 0x00800000u || (ix >> 31)) {
+        if ((ix << 1) == 0) return -INFINITY;
+        if (ix >> 31) return NAN;
+        k -= 25;                                   // subnormal: scale up
+        x *= f32_from(0x4C000000u);                // 2^25
+        ix = f32_bits(x);
+    } else if (ix >= 0x7F800000u) {
+        return x;
+    } else if (ix == 0x3F800000u) {
+        return 0.0f;
+    }
+    ix += 0x3F800000u - 0x3F3504F3u;
+    k += (int)(ix >> 23) - 0x7F;
+    ix = (ix & 0x007FFFFFu) + 0x3F3504F3u;
+    x = f32_from(ix);
+    const float f = x - 1.0f;
+    const float s = f / (2.0f + f);
+    const float z = s * s;
+    const float w = z * z;
+    const float t1 = w * (Lg2 + w * Lg4);
+    const float t2 = z * (Lg1 + w * Lg3);
+    const float R = t2 + t1;
+    const float hfsq = 0.5f * f * f;
+    const float dk = (float)k;
+    return s * (hfsq + R) + dk * ln2_lo - hfsq + f + dk * ln2_hi;
+}
+
+// std.math.frexp for f32: x = m * 2^e with m in [0.5, 1).
+float zfrexpf(float x, int *e) {
+    uint32_t u = f32_bits(x);
+    int ex = (int)((u >> 23) & 0xFF);
+    if (ex == 0) {
+        if ((u << 1) == 0) {
+            *e = 0;
+            return x;
+        }
+        x *= f32_from(0x5F800000u);  // 2^64
+        u = f32_bits(x);
+        ex = (int)((u >> 23) & 0xFF) - 64;
+    } else if (ex == 0xFF) {
+        *e = 0;
+        return x;
+    }
+    *e = ex - 126;
+    return f32_from((u & 0x807FFFFFu) | 0x3F000000u);
+}
+
+// std.math.pow(f32, x, y) (lib/std/math/pow.zig, Go's math.Pow): special
+// cases, then x^y = exp(yf*log(x)) * x^yi with yf in (-0.5, 0.5] and x^yi
+// by repeated squaring of frexp(x), scaled by 2^ae at the end.  z2d calls
+// it with y = 2.2 and 1/2.2 (src/color.zig:336-351,
+// src/internal/color_vector.zig:210-240).
+bool zis_odd_int(float y) {
+    if (std::fabs(y) >= 16777216.0f) return false;  // beyond 2^24 every float is even
+    const float t = std::trunc(y);
+    if (t != y) return false;
+    return ((int64_t)t & 1) != 0;
+}
 float zpow(float x, float y) {
     if (y == 0.0f || x == 1.0f) return 1.0f;
-    if (x != x || y != y) return x + y;
+    if (x != x || y != y) return NAN;
     if (y == 1.0f) return x;
-    if (x == 0.0f) return y > 0 ? 0.0f : INFINITY;
+    if (x == 0.0f) {
+        if (y < 0.0f) return zis_odd_int(y) ? std::copysign(INFINITY, x) : INFINITY;
+        return zis_odd_int(y) ? x : 0.0f;
+    }
+    if (std::isinf(y)) {
+        if (x == -1.0f) return 1.0f;
+        return ((std::fabs(x) < 1.0f) == (y > 0.0f)) ? 0.0f : INFINITY;
+    }
+    if (std::isinf(x)) {
+        if (x < 0.0f) return zpow(1.0f / x, -y);  // pow(-0, -y)
+        return y < 0.0f ? 0.0f : INFINITY;
+    }
     if (y == 0.5f) return std::sqrt(x);
-    return (float)std::pow((double)x, (double)y);
+    if (y == -0.5f) return 1.0f / std::sqrt(x);
+    float yi = std::trunc(std::fabs(y));
+    float yf = std::fabs(y) - yi;
+    if (yf != 0.0f && x < 0.0f) return NAN;
+    if (yi >= 2147483648.0f) {
+        if (x == -1.0f) return 1.0f;
+        return ((std::fabs(x) < 1.0f) == (y > 0.0f)) ? 0.0f : INFINITY;
+    }
+    float a1 = 1.0f;
+    int ae = 0;
+    if (yf != 0.0f) {
+        if (yf > 0.5f) {
+            yf -= 1.0f;
+            yi += 1.0f;
+        }
+        a1 = zexpf(yf * zlogf(x));
+    }
+    int xe;
+    float x1 = zfrexpf(x, &xe);
+    for (int32_t i = (int32_t)yi; i != 0; i >>= 1) {
+        if (xe < -(1 << 9) || (1 << 9) < xe) {
+            ae += xe;
+            break;
+        }
+        if (i & 1) {
+            a1 *= x1;
+            ae += xe;
+        }
+        x1 *= x1;
+        xe <<= 1;
+        if (x1 < 0.5f) {
+            x1 += x1;
+            xe -= 1;
+        }
+    }
+    if (y < 0.0f) {
+        a1 = 1.0f / a1;
+        ae = -ae;
+    }
+    return zscalbnf(a1, ae);
+}
+
+// std.math.atan for f64 (musl src/math/atan.c / FreeBSD s_atan.c):
+// reduction to |x| < 7/16 around atan(0.5), atan(1), atan(1.5), atan(inf),
+// then an odd polynomial of degree 23 split in two halves.
+double zatan(double x) {
+    static const double atanhi[4] = {4.63647609000806093515e-01, 7.85398163397448278999e-01,
+                                     9.82793723247329054082e-01, 1.57079632679489655800e+00};
+    static const double atanlo[4] = {2.26987774529616870924e-17, 3.06161699786838301793e-17,
+                                     1.39033110312309984516e-17, 6.12323399573676603587e-17};
+    static const double aT[11] = {3.33333333333329318027e-01, -1.99999999998764832476e-01,
+                                  1.42857142725034663711e-01, -1.11111104054623557880e-01,
+                                  9.09088713343650656196e-02, -7.69187620504482999495e-02,
+                                  6.66107313738753120669e-02, -5.83357013379057348645e-02,
+                                  4.97687799461593236017e-02, -3.65315727442169155270e-02,
+                                  1.62858201153657823623e-02};
+    uint32_t ix = f64_hi(x);
+    const uint32_t sign = ix >> 31;
+    ix &= 0x7FFFFFFFu;
+    if (ix >= 0x44100000u) {                       // |x| >= 2^66
+        if (x != x) return x;
+        const double z = atanhi[3] + 0x1p-120;
+        return sign ? -z : z;
+    }
+    int id;
+    if (ix < 0x3FDC0000u) {                        // |x| < 0.4375
+        if (ix < 0x3E400000u) return x;            // |x| < 2^-27
+        id = -1;
+    } else {
+        x = std::fabs(x);
+        if (ix < 0x3FF30000u) {                    // |x| < 1.1875
+            if (ix < 0x3FE60000u) {                // 7/16 <= |x| < 11/16
+                id = 0;
+                x = (2.0 * x - 1.0) / (2.0 + x);
+            } else {                               // 11/16 <= |x| < 19/16
+                id = 1;
+                x = (x - 1.0) / (x + 1.0);
+            }
+        } else if (ix < 0x40038000u) {             // |x| < 2.4375
+            id = 2;
+            x = (x - 1.5) / (1.0 + 1.5 * x);
+        } else {                                   // 2.4375 <= |x| < 2^66
+            id = 3;
+            x = -1.0 / x;
+        }
+    }
+    const double z = x * x;
+    const double w = z * z;
+    const double s1 = z * (aT[0] + w * (aT[2] + w * (aT[4] + w * (aT[6] + w * (aT[8] + w * aT[10])))));
+    const double s2 = w * (aT[1] + w * (aT[3] + w * (aT[5] + w * (aT[7] + w * aT[9]))));
+    if (id < 0) return x - x * (s1 + s2);
+    const double r = atanhi[id] - ((x * (s1 + s2) - atanlo[id]) - x);
+    return sign ? -r : r;
+}
+
+// std.math.atan2 for f64 (musl src/math/atan2.c / FreeBSD e_atan2.c); the
+// conic gradient's angle (src/gradient.zig:739).
+double zatan2(double y, double x) {
+    const double pi = 3.1415926535897931160E+00, pi_lo = 1.2246467991473531772E-16;
+    if (x != x || y != y) return x + y;
+    uint32_t ix = f64_hi(x), iy = f64_hi(y);
+    const uint32_t lx = f64_lo(x), ly = f64_lo(y);
+    if (((ix - 0x3FF00000u) | lx) == 0) return zatan(y);  // x == 1.0
+    const uint32_t m = ((iy >> 31) & 1u) | ((ix >> 30) & 2u);
+    ix &= 0x7FFFFFFFu;
+    iy &= 0x7FFFFFFFu;
+    if ((iy | ly) == 0) {
+        if (m <= 1) return y;
+        return m == 2 ? pi : -pi;
+    }
+    if ((ix | lx) == 0) return (m & 1) ? -pi / 2 : pi / 2;
+    if (ix == 0x7FF00000u) {
+        if (iy == 0x7FF00000u) {
+            switch (m) {
+                case 0: return pi / 4;
+                case 1: return -pi / 4;
+                case 2: return 3 * pi / 4;
+                default: return -3 * pi / 4;
+            }
+        }
+        switch (m) {
+            case 0: return 0.0;
+            case 1: return -0.0;
+            case 2: return pi;
+            default: return -pi;
+        }
+    }
+    if (ix + (64u << 20) < iy || iy == 0x7FF00000u) return (m & 1) ? -pi / 2 : pi / 2;
+    double z;
+    if ((m & 2) && iy + (64u << 20) < ix) z = 0.0;
+    else z = zatan(std::fabs(y / x));
+    switch (m) {
+        case 0: return z;
+        case 1: return -z;
+        case 2: return pi - (z - pi_lo);
+        default: return (z - pi_lo) - pi;
+    }
 }
 
 // Zig @mod on floats: fmod, then shifted into [0, b) when the numerator is
@@ -769,7 +1075,7 @@ float grad_offset(const Grad &gr, int32_t x, int32_t y) {
         return -1;
     }
     const double dx = px - gr.g[0], dy = py - gr.g[1];
-    const double ang = zmod(std::atan2(dy, dx) - gr.angle, M_PI * 2);
+    const double ang = zmod(zatan2(dy, dx) - gr.angle, M_PI * 2);
     return (float)(ang / (M_PI * 2));
 }
 
@@ -1769,6 +2075,11 @@ __attribute__((visibility("default"))) z2d_pixel z2doracle_pixel_from_color(z2d_
 }
 
 // Gradient.getOffset (src/gradient.zig:239-243).
+// std.math.pow(f32) as restated above (pinned to z2d's gamma KATs).
+__attribute__((visibility("default"))) float z2doracle_pow_f32(float x, float y) { return zpow(x, y); }
+// std.math.atan2(f64) as restated above.
+__attribute__((visibility("default"))) double z2doracle_atan2(double y, double x) { return zatan2(y, x); }
+
 __attribute__((visibility("default"))) float z2doracle_gradient_offset(const z2d_gradient *g, int32_t x, int32_t y) {
     const Grad gr = make_grad(*g);
     return grad_offset(gr, x, y);

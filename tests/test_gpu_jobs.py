@@ -68,7 +68,7 @@ def test_jobs_mixed(oracle):
         specs.append((fmts[j % len(fmts)], w, h, j, fills))
     got, ref = _run(oracle, specs)
     for j, (a, b) in enumerate(zip(got, ref)):
-        _cmp(a, b, f"job {j} ({specs[j][0]} {specs[j][1]}x{specs[j][2]})", tol=1)
+        _cmp(a, b, f"job {j} ({specs[j][0]} {specs[j][1]}x{specs[j][2]})")
 
 
 def test_jobs_batched_workload_slice(oracle):

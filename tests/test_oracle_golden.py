@@ -80,3 +80,53 @@ def test_png_scanlines_match_golden_compositor(oracle, golden_dir, name):
     scene, profile = EXPORT_SCENES.get(name, (COMPOSITOR_SCENES.get(name), None))
     assert oracle.png_scanlines(scene(StrokeOracle(oracle)), profile) == \
         golden_scanlines(os.path.join(golden_dir, name + ".png"))
+
+
+def _math_kats(kind):
+    with open(os.path.join(HERE, "golden", "math_kats.json")) as f:
+        return json.load(f)[kind]
+
+
+@pytest.mark.parametrize("case", _math_kats("pow_f32"), ids=lambda c: f"{c['exponent']}-{c['x']}")
+def test_pow_f32_kat(oracle, case):
+    """std.math.pow(f32) as z2d computes it: the exact values z2d's own
+    SRGB.removeGamma / applyGamma tests expect (src/color.zig:1030-1056,
+    compared there with expectEqualDeep)."""
+    g = np.float32(2.2)
+    y = g if case["exponent"] == "gamma" else np.float32(1.0) / g
+    got = np.float32(oracle.pow_f32(float(case["x"]), float(y)))
+    assert got == np.float32(case["expected"])
+
+
+def test_pow_f32_kats_reject_rounded_double_pow():
+    """The KATs discriminate: pow evaluated in double and rounded once (the
+    host libm) misses some of them, so the exact restatement is needed."""
+    g = np.float32(2.2)
+    misses = 0
+    for case in _math_kats("pow_f32"):
+        y = g if case["exponent"] == "gamma" else np.float32(1.0) / g
+        misses += np.float32(float(case["x"]) ** float(y)) != np.float32(case["expected"])
+    assert misses > 0
+
+
+@pytest.mark.parametrize("case", _math_kats("conic_offset"), ids=lambda c: c["name"])
+def test_conic_offset_kat(oracle, case):
+    """Conic.getOffset (std.math.atan2(f64), src/gradient.zig:731-741):
+    z2d's exact expected offsets (src/gradient.zig:1702-1766)."""
+    from z2d_gb300.types import Gradient
+    g = Gradient.conic(case["center_x"], case["center_y"], case["angle"])
+    if case["scale"]:
+        g.set_transformation((case["scale"][0], 0.0, 0.0, case["scale"][1], 0.0, 0.0))
+    assert np.float32(oracle.gradient_offset(g, case["x"], case["y"])) == np.float32(case["expected"])
+
+
+def test_atan2_accuracy(oracle):
+    """The atan2 restatement stays within one ulp of the correctly rounded
+    value over all quadrants (a check on its constants and reduction)."""
+    rng = np.random.default_rng(5)
+    ys = np.concatenate([rng.normal(0, 100, 4000), rng.uniform(-1e-3, 1e-3, 500), [0.0, -0.0, 1.0, -1.0]])
+    xs = np.concatenate([rng.normal(0, 100, 4000), rng.uniform(-1e3, 1e3, 500), [1.0, -1.0, 0.0, 2.0]])
+    for y, x in zip(ys, xs):
+        got = oracle.atan2(float(y), float(x))
+        ref = np.arctan2(y, x)
+        assert abs(got - ref) <= np.spacing(abs(ref)) + 1e-300

@@ -76,20 +76,73 @@ def _cmp(a, b, what):
     assert int(d.max(initial=0)) <= TOL, f"{what}: {int((d > 0).sum())} bytes differ"
 
 
+def _dev_calls(w, h):
+    return [([Operation(o.operator, dst=_dev(o.dst) if isinstance(o.dst, Surface) else o.dst,
+                        src=_dev(o.src) if isinstance(o.src, Surface) else o.src) for o in ops], x, y, prec)
+            for ops, x, y, prec in _calls(w, h)]
+
+
 @pytest.mark.parametrize("fmt", ["rgba", "rgb", "alpha8", "alpha2"])
 def test_noalloc_matches_composite(fmt):
+    """Each call, checked after it completes."""
     torch = pytest.importorskip("torch")
     w, h = 157, 93
     ctx = default_context()
     a, b = _dev(_bg(fmt, w, h, 21)), _dev(_bg(fmt, w, h, 21))
     stream = torch.cuda.current_stream().cuda_stream
-    for i, (ops, x, y, prec) in enumerate(_calls(w, h)):
-        dev_ops = [Operation(o.operator, dst=_dev(o.dst) if isinstance(o.dst, Surface) else o.dst,
-                             src=_dev(o.src) if isinstance(o.src, Surface) else o.src) for o in ops]
-        run_noalloc(a, x, y, dev_ops, prec, device=0, stream=stream)
-        SurfaceCompositor.run(b, x, y, dev_ops, prec, ctx=ctx)
+    for i, (ops, x, y, prec) in enumerate(_dev_calls(w, h)):
+        run_noalloc(a, x, y, ops, prec, device=0, stream=stream)
+        SurfaceCompositor.run(b, x, y, ops, prec, ctx=ctx)
         torch.cuda.synchronize()
         _cmp(a, b, f"{fmt} call {i}")
+
+
+@pytest.mark.parametrize("fmt", ["rgba", "alpha8"])
+def test_noalloc_calls_queued_on_one_stream(fmt):
+    """All four calls queued back to back on one stream, one synchronisation
+    at the end: each call rewrites the shared descriptor array while the
+    previous call's kernels may not have run yet, which stream order makes
+    safe.  The final surface equals the context path's after the same calls."""
+    torch = pytest.importorskip("torch")
+    w, h = 157, 93
+    ctx = default_context()
+    a, b = _dev(_bg(fmt, w, h, 31)), _dev(_bg(fmt, w, h, 31))
+    calls = _dev_calls(w, h)
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    for ops, x, y, prec in calls:
+        run_noalloc(a, x, y, ops, prec, device=0, stream=s.cuda_stream)
+    s.synchronize()
+    for ops, x, y, prec in calls:
+        SurfaceCompositor.run(b, x, y, ops, prec, ctx=ctx)
+    torch.cuda.synchronize()
+    _cmp(a, b, f"{fmt} after four queued calls")
+
+
+def test_noalloc_rejects_gradients_while_capturing():
+    """A call with a gradient param on a capturing stream is refused before
+    it queues anything (its descriptors would be copied from memory that
+    does not outlive the call); the capture itself stays valid."""
+    torch = pytest.importorskip("torch")
+    w, h = 32, 16
+    a = _dev(_bg("rgba", w, h, 3))
+    ops = [Operation("src_over", src=Pattern.from_gradient(_grad("linear", 9)))]
+    s = torch.cuda.Stream()
+    run_noalloc(a, 0, 0, ops, device=0, stream=s.cuda_stream)  # first call on the device: outside any capture
+    s.synchronize()
+    x = torch.zeros(16, device="cuda")
+    g = torch.cuda.CUDAGraph()
+    err = None
+    with torch.cuda.graph(g, stream=s):
+        try:
+            run_noalloc(a, 0, 0, ops, device=0, stream=s.cuda_stream)
+        except Z2DError as e:
+            err = e
+        x.add_(1)
+    assert err is not None and err.code == abi.ERR_INVALID_ARGUMENT
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(x.sum()) == 16.0
 
 
 def test_noalloc_rejects():

@@ -1589,7 +1589,10 @@ Z2D_API int z2dgpu_composite(z2dgpu_ctx *c, z2d_surface *dst, int32_t dst_x, int
 // g_noalloc_gradients instead of context scratch, and no context (with its
 // own allocations) is involved.  The first call on a device looks up the
 // scratch's device address; that call should come before any stream
-// capture.  Calls share the scratch: calls that overlap on the GPU race.
+// capture.  The address is kept for the life of the process, so the entry
+// point must not be used on a device after cudaDeviceReset there.  Calls
+// share the scratch: calls that overlap on the GPU race.  A call with
+// gradient params is rejected while `stream` is capturing.
 Z2D_API int z2dgpu_composite_noalloc(int device, void *stream, z2d_surface *dst, int32_t dst_x, int32_t dst_y,
                                      int32_t n_ops, const z2d_operation *ops, int32_t precision) {
     int rc = check_surface(dst);
@@ -1674,8 +1677,18 @@ Z2D_API int z2dgpu_composite_noalloc(int device, void *stream, z2d_surface *dst,
     Z2D_CUDA(cudaDeviceGetAttribute(&c.sm_count, cudaDevAttrMultiProcessorCount, device));
     // Every descriptor a kernel reads is written here, so nothing in the
     // scratch has to start at zero.  The copy reads `grads` before it returns.
-    if (n_grads > 0)
+    if (n_grads > 0) {
+        // A capturing stream would record a copy node that reads `grads`
+        // again at every replay, after this stack frame is gone.
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        Z2D_CUDA(cudaStreamIsCapturing(c.stream, &cap));
+        if (cap != cudaStreamCaptureStatusNone) {
+            set_error("composite_noalloc: gradient params cannot be used while the stream is capturing "
+                      "(their descriptors are copied from memory that does not outlive the call)");
+            return Z2D_ERR_INVALID_ARGUMENT;
+        }
         Z2D_CUDA(cudaMemcpyAsync(scratch, grads, sizeof(DevGradient) * (size_t)n_grads, cudaMemcpyHostToDevice, c.stream));
+    }
     return launch_composite(c, J);
 }
 

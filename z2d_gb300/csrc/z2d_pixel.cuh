@@ -9,6 +9,7 @@
 #include <stdint.h>
 
 #include "../../include/z2dgpu.h"
+#include "zig_math.cuh"
 
 #define Z2D_HD __host__ __device__ __forceinline__
 #define Z2D_D __device__ __forceinline__
@@ -407,16 +408,8 @@ Z2D_D uint32_t enc_ch(float x) {
 Z2D_D I16 encode_raw(F4 v) { return I16{enc_ch(v.r), enc_ch(v.g), enc_ch(v.b), enc_ch(v.a)}; }
 
 // ------------------------------------------------------------ colors
-// std.math.pow(f32, x, y) for the exponents z2d uses; general case in
-// double, rounded once.
-Z2D_HD float zpow(float x, float y) {
-    if (y == 0.0f || x == 1.0f) return 1.0f;
-    if (x != x || y != y) return x + y;
-    if (y == 1.0f) return x;
-    if (x == 0.0f) return y > 0.0f ? 0.0f : INFINITY;
-    if (y == 0.5f) return sqrtf(x);
-    return (float)pow((double)x, (double)y);
-}
+// std.math.pow(f32, x, y) as Zig computes it (zig_math.cuh)
+Z2D_HD float zpow(float x, float y) { return zm::powf_(x, y); }
 Z2D_HD float zmodf(float a, float b) {
     const float r = fmodf(a, b);
     return a < 0.0f ? fmodf(r + b, b) : r;
@@ -604,7 +597,7 @@ Z2D_D float grad_offset(const DevGradient &gr, int32_t x, int32_t y) {
     }
     const double dx = px - gr.g[0], dy = py - gr.g[1];
     const double twopi = 6.283185307179586;
-    const double ang = zmod(atan2(dy, dx) - gr.angle, twopi);
+    const double ang = zmod(zm::atan2_(dy, dx) - gr.angle, twopi);
     return (float)(ang / twopi);
 }
 
