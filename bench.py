@@ -611,32 +611,39 @@ def png_arm(ctx, surf, peak_gbs):
             "note": "file = device encoding + copy back + zlib default level on one host thread"}
 
 
+SERVE_LANES = 3           # server lanes (batches drawn concurrently)
+SERVE_POOL = 4 << 30      # device surface pool of the server
+SERVE_OUT_RING = 2048     # host result buffers, reused round-robin by the requests
+SERVE_PARITY = 4096       # requests of the fastest rate compared with the oracle
+
+
 def serving_arm(dev):
     """The serving configuration: requests arrive as a Poisson process and go
-    through the native request queue (z2d_gb300.server, one worker thread
-    batching up to 512 requests within 300 us).  Mix: 80 % glyph-like
-    requests (one outline of 20-200 cubics on its own 64x64 RGBA surface;
-    half with a linear-gradient source), 20 % jobs of the batched-jobs
-    distribution with sides up to 512.  Every request draws on its own
-    surface.  Reported per rate: achieved request rate, latency p50/p99
-    (submit to completion, measured by the server) and Mpix/s of surface
-    area."""
+    through the continuous-batching server (z2d_gb300.server: SERVE_LANES
+    lanes drawing batches concurrently, up to 512 requests per batch, a
+    300 us batching window).  Each request draws on a surface the server
+    allocates from its device pool (cleared) and reads the result back into
+    a host buffer, so latency is end to end (submit to pixels in host
+    memory).  Mix: 80 % glyph-like requests (one outline of 20-200 cubics on
+    a 64x64 RGBA surface; half with a linear-gradient source), 20 % jobs of
+    the batched-jobs distribution with sides up to 512.  Reported per rate:
+    achieved request rate, latency p50/p99 (measured by the server) and
+    Mpix/s of surface area.  The last SERVE_PARITY requests of the fastest
+    rate are compared with the same requests drawn alone by the oracle."""
     import ctypes as C
     import threading
-    import torch
     from z2d_gb300 import abi
     from z2d_gb300.server import Server
-    from z2d_gb300.surface import Surface
-    from z2d_gb300.types import Color, FillOptions, Gradient, Pattern, Pixel
+    from z2d_gb300.types import Color, FillOptions, Gradient, Pattern
     from z2d_gb300.workloads import batched_jobs, glyph_path, job_fills, random_premultiplied_pixel
     rng = np.random.default_rng(SEED + 21)
     n_req = int(max(SERVE_RATES) * SERVE_SECONDS)
-    pool = 2000  # distinct request contents; request k draws pool entry k % pool on its own surface
+    pool = 2000  # distinct request contents; request k draws pool entry k % pool
     jobs = batched_jobs(SEED + 22, pool // 5, side_lo=16, side_hi=512, paths_lo=1, paths_hi=50)
     grad = Gradient.linear(0, 0, 64, 64)
     grad.add_stop(0.0, Color.rgb(0.9, 0.1, 0.1, 1.0))
     grad.add_stop(1.0, Color.rgb(0.1, 0.2, 0.9, 0.8))
-    reqs = []  # (w, h, nodes, cmds ctypes array, keep)
+    reqs = []  # (w, h, nodes, cmds ctypes array, keep, fills)
     ji = 0
     for i in range(pool):
         if i % 5 == 4 and ji < len(jobs):
@@ -659,35 +666,40 @@ def serving_arm(dev):
             cmds[k].opts = opts.to_abi()
             off += len(nd)
             arrs.append(nd)
-        reqs.append((w, h, np.ascontiguousarray(np.concatenate(arrs)), cmds, keep))
-    sizes = [reqs[k % pool][0] * reqs[k % pool][1] * 4 for k in range(n_req)]
-    starts, tot = [], 0
-    for sz in sizes:
-        starts.append(tot)
-        tot += (sz + 255) // 256 * 256
-    buf = torch.zeros(tot, dtype=torch.uint8, device=dev)
-    sfcs = []
-    for k, (o, sz) in enumerate(zip(starts, sizes)):
-        w, h = reqs[k % pool][0], reqs[k % pool][1]
-        sfcs.append(Surface("rgba", w, h, buf[o:o + sz]).to_abi())
+        reqs.append((w, h, np.ascontiguousarray(np.concatenate(arrs)), cmds, keep, fills))
+    # request k reads back into ring slot k % SERVE_OUT_RING (one slot holds
+    # the largest surface, 512x512 RGBA); at the fastest rate the ring spans
+    # ~40 ms of arrivals, far beyond a request's latency, so no two requests
+    # in flight share a slot
+    ring = np.zeros((SERVE_OUT_RING, 512 * 512 * 4), np.uint8)
     results = {}
-    with Server(max_batch_jobs=512, max_wait_us=300) as srv:
+    parity = None
+    with Server(max_batch_jobs=512, max_wait_us=300, lanes=SERVE_LANES, pool_bytes=SERVE_POOL) as srv:
         lib = srv.lib
-        # warm-up
-        for i in range(64):
-            w, h, nodes, cmds, _ = reqs[i]
-            srv.wait(_submit(lib, srv.handle, sfcs[i], nodes, cmds))
+
+        def out_buf(k):
+            w, h = reqs[k % pool][0], reqs[k % pool][1]
+            return ring[k % SERVE_OUT_RING, :w * h * 4]
+
+        for i in range(64):  # warm-up
+            w, h, nodes, cmds, _, _ = reqs[i]
+            srv.wait(_submit_new(lib, srv.handle, w, h, out_buf(i), nodes, cmds))
         for rate in SERVE_RATES:
             n = int(rate * SERVE_SECONDS)
             arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+            bufs = [out_buf(k) for k in range(n)]
             tickets = [0] * n
             lat = [0.0] * n
             submitted = threading.Semaphore(0)
+            check_from = n - SERVE_PARITY if rate == max(SERVE_RATES) else n
+            kept = []
 
             def waiter():
                 for k in range(n):
                     submitted.acquire()
                     lat[k] = srv.wait(tickets[k])
+                    if k >= check_from:  # copied before its ring slot is reused
+                        kept.append((k, bufs[k].copy()))
 
             th = threading.Thread(target=waiter)
             th.start()
@@ -695,31 +707,48 @@ def serving_arm(dev):
             for k in range(n):
                 while time.perf_counter() - t0 < arrivals[k]:
                     pass
-                w, h, nodes, cmds, _ = reqs[k % pool]
-                tickets[k] = _submit(lib, srv.handle, sfcs[k], nodes, cmds)
+                w, h, nodes, cmds, _, _ = reqs[k % pool]
+                tickets[k] = _submit_new(lib, srv.handle, w, h, bufs[k], nodes, cmds)
                 submitted.release()
             t_sub = time.perf_counter() - t0
             th.join()
             wall = time.perf_counter() - t0
             ls = sorted(lat)
-            px = sum(sizes[:n]) // 4
+            px = sum(reqs[k % pool][0] * reqs[k % pool][1] for k in range(n))
             results[str(rate)] = {"requests": n, "offered_per_s": rate, "submitted_per_s": n / t_sub,
                                   "completed_per_s": n / wall, "p50_us": ls[n // 2], "p99_us": ls[int(n * 0.99) - 1],
                                   "mpix_s": px / 1e6 / wall}
-        b, r, busy = srv.stats()
+            if kept:
+                parity = {"rate": rate, "requests_checked": len(kept), "kept": kept}
+        info = srv.info()
+    if parity is not None:
+        from oracle import Oracle
+        from z2d_gb300.surface import Surface
+        o = Oracle()
+        bad = 0
+        for k, got in parity.pop("kept"):
+            w, h, _, _, _, fills = reqs[k % pool]
+            ref = Surface.init("rgba", w, h)
+            for pat, nd, opts in fills:
+                o.fill(ref, pat, nd, opts)
+            bad += int(not np.array_equal(got, ref.data))
+        parity["differing_requests"] = bad
+        parity["reference"] = "each request drawn alone on a cleared surface by the oracle"
     return {"workload": "Poisson arrivals; 80% glyphs (20-200 cubics, 64x64, half gradient), 20% jobs "
-                        "(sides 16-512, 1-50 paths); one surface per request",
-            "server": {"max_batch_jobs": 512, "max_wait_us": 300, "batches": b, "requests": r, "busy_ms": busy},
-            "rates": results}
+                        "(sides 16-512, 1-50 paths); one pool surface per request, result read back to host",
+            "server": {"max_batch_jobs": 512, "max_wait_us": 300, "lanes": SERVE_LANES, "pool_bytes": SERVE_POOL,
+                       "info": info},
+            "rates": results, "parity": parity}
 
 
-def _submit(lib, handle, sfc, nodes, cmds):
+def _submit_new(lib, handle, w, h, out, nodes, cmds):
     import ctypes as C
     from z2d_gb300 import abi
     from z2d_gb300.native import check
     t = C.c_uint64()
-    check(lib.z2dgpu_server_submit(handle, C.byref(sfc), nodes.ctypes.data_as(C.POINTER(abi.z2d_node)), len(nodes),
-                                   cmds, len(cmds), C.byref(t)))
+    check(lib.z2dgpu_server_submit_new(handle, abi.FORMAT_RGBA, w, h, None, out.ctypes.data_as(C.c_void_p),
+                                       nodes.ctypes.data_as(C.POINTER(abi.z2d_node)), len(nodes), cmds, len(cmds),
+                                       C.byref(t)))
     return t.value
 
 

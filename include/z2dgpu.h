@@ -391,33 +391,71 @@ Z2D_API int z2dgpu_composite_noalloc(int device, void *stream, z2d_surface *dst,
                                      const z2d_operation *ops, int32_t precision);
 
 /* ---------------------------------------------------------------- serving
- * A request queue in front of z2dgpu_fill_jobs, for callers that submit fills
- * for many surfaces from many threads (no counterpart in z2d).  One worker
- * thread per server owns a context and a stream; it draws the requests that
- * arrived within `max_wait_us` of the oldest waiting one (at most
- * `max_batch_jobs` per pass) in one z2dgpu_fill_jobs pass.  Requests on the
- * same surface are drawn in submission order; requests are copied at
- * submit, so the caller's node/command/pattern buffers can be reused when
- * submit returns, but surfaces (device memory) must stay valid until the
- * request completes. */
+ * Continuous batching in front of z2dgpu_fill_jobs, for callers that submit
+ * fills for many surfaces from many threads (no counterpart in z2d, whose
+ * painter.fill is one synchronous call, src/painter.zig:66-72).  The server
+ * runs `lanes` workers, each with its own context and stream: a free lane
+ * takes the requests queued at that moment (after at most `max_wait_us` of
+ * batching window, up to `max_batch_jobs`) and draws them in one pass, while
+ * the other lanes take the requests that keep arriving, so several batches
+ * are on the GPU at once.  A request draws either on a caller-owned device
+ * surface (z2dgpu_server_submit) or on a surface the server allocates from
+ * its device pool (z2dgpu_server_submit_new).  The pool is one allocation
+ * made at creation: `pool_bytes`, at most 40 GB and at most 7/8 of the HBM
+ * the driver reports free (cudaMemGetInfo); a pool request is admitted into
+ * a batch once the pool can hold its surface, in arrival order.  Requests on
+ * the same caller-owned surface are drawn in submission order.  Requests are
+ * copied at submit, so the caller's node/command/pattern/initial-pixel
+ * buffers can be reused when submit returns; caller-owned surfaces and
+ * `out` buffers must stay valid until the request completes. */
 typedef struct z2dgpu_server z2dgpu_server;
 
+typedef struct z2dgpu_server_opts {
+    int32_t max_batch_jobs; /* requests per pass, >= 1 */
+    int32_t max_wait_us;    /* batching window after the oldest queued request, >= 0 */
+    int32_t lanes;          /* workers drawing batches concurrently, 1..16 */
+    int64_t pool_bytes;     /* device surface pool for z2dgpu_server_submit_new; 0 = none */
+} z2dgpu_server_opts;
+
+typedef struct z2dgpu_server_stats_t {
+    uint64_t batches, requests;
+    uint64_t deferred;         /* times a pool request waited for pool space */
+    double busy_ms;            /* time the lanes spent drawing, summed */
+    int32_t lanes, max_inflight; /* most batches that were being drawn at once */
+    int64_t pool_bytes, pool_peak_bytes;
+} z2dgpu_server_stats_t;
+
+Z2D_API int z2dgpu_server_create2(z2dgpu_server **server, int device, const z2dgpu_server_opts *opts);
+/* z2dgpu_server_create2 with 2 lanes and no pool. */
 Z2D_API int z2dgpu_server_create(z2dgpu_server **server, int device, int32_t max_batch_jobs,
                                  int32_t max_wait_us);
-/* Queues painter.fill for cmds[0..n_cmds) in order on `surface`; *ticket
- * identifies the request. */
+/* Queues painter.fill for cmds[0..n_cmds) in order on `surface` (device
+ * memory); *ticket identifies the request. */
 Z2D_API int z2dgpu_server_submit(z2dgpu_server *server, const z2d_surface *surface,
                                  const z2d_node *nodes, size_t n_nodes,
                                  const z2d_fill_cmd *cmds, size_t n_cmds, uint64_t *ticket);
+/* Queues painter.fill for cmds[0..n_cmds) on a new width x height surface
+ * of `format` from the server's pool, initialised from `init` (host memory
+ * in z2d's layout; NULL: cleared to zero).  When the request completes the
+ * drawn pixels are in `out` (host memory, z2d's layout and length; NULL:
+ * not read back).  The pool block is released at completion.  A surface
+ * larger than the whole pool is Z2D_ERR_OUT_OF_MEMORY; a server without a
+ * pool is Z2D_ERR_INVALID_STATE. */
+Z2D_API int z2dgpu_server_submit_new(z2dgpu_server *server, int32_t format, int32_t width,
+                                     int32_t height, const void *init, void *out,
+                                     const z2d_node *nodes, size_t n_nodes,
+                                     const z2d_fill_cmd *cmds, size_t n_cmds, uint64_t *ticket);
 /* Waits for a request (timeout_ms < 0: no limit) and returns its status, or
  * Z2D_ERR_TIMEOUT if it is still pending (the ticket stays valid).
  * *latency_us (optional) = completion time - submit time. */
 Z2D_API int z2dgpu_server_wait(z2dgpu_server *server, uint64_t ticket, int32_t timeout_ms,
                                double *latency_us);
-/* Passes run, requests completed and worker busy time so far. */
+/* Passes run, requests completed and lane busy time so far. */
 Z2D_API int z2dgpu_server_stats(z2dgpu_server *server, uint64_t *batches, uint64_t *requests,
                                 double *busy_ms);
-/* Draws every queued request, then stops the worker and frees the server. */
+/* All counters, including the overlap of batches and the pool's use. */
+Z2D_API int z2dgpu_server_info(z2dgpu_server *server, z2dgpu_server_stats_t *out);
+/* Draws every queued request, then stops the lanes and frees the server. */
 Z2D_API int z2dgpu_server_destroy(z2dgpu_server *server);
 
 #endif /* Z2DGPU_H */

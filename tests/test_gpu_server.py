@@ -118,3 +118,112 @@ def test_server_rejects_host_surface():
         with pytest.raises(Z2DError) as e:
             srv.submit(_bg(8, 8, 1), random_fills(seed=1, n=1, w=8, h=8, side_lo=2, side_hi=6, seg_lo=3, seg_hi=4))
         assert e.value.code == abi.ERR_INVALID_ARGUMENT
+
+
+def _pool_requests(n, seed):
+    """Requests on pool surfaces: several formats, random sizes, half of
+    them starting from a seeded background, half cleared."""
+    rng = np.random.default_rng(seed)
+    fmts = ["rgba", "rgba", "rgb", "alpha8", "alpha4", "alpha1"]
+    out = []
+    for i in range(n):
+        fmt = fmts[i % len(fmts)]
+        w, h = int(rng.integers(1, 140)), int(rng.integers(1, 120))
+        fills = random_fills(seed=seed * 1000 + i, n=int(rng.integers(0, 6)), w=w, h=h, side_lo=2,
+                             side_hi=max(3, min(w, h)), seg_lo=3, seg_hi=12)
+        for k, (_, _, o) in enumerate(fills):
+            o.anti_aliasing = ("default", "none", "supersample_4x")[(i + k) % 3]
+        init = None
+        if i % 2:
+            s = Surface.init(fmt, w, h)
+            s.data[:] = rng.integers(0, 256, s.data.size, dtype=np.uint8)
+            if fmt == "rgba":
+                s.data[:] = premultiplied_background(rng, w, h)
+            init = s.data.copy()
+        out.append((fmt, w, h, fills, init))
+    return out
+
+
+def _drawn_alone(oracle, fmt, w, h, fills, init):
+    s = Surface.init(fmt, w, h)
+    if init is not None:
+        s.data[:] = init
+    for pat, nodes, opts in fills:
+        assert oracle.fill(s, pat, nodes, opts) == abi.OK
+    return s.numpy()
+
+
+@pytest.mark.parametrize("lanes", [1, 3])
+def test_server_pool_surfaces_match_drawn_alone(oracle, lanes):
+    """Every request on a pool surface, drawn in batches that overlap on the
+    GPU, reads back exactly what drawing it alone gives."""
+    pytest.importorskip("torch")
+    reqs = _pool_requests(90, seed=20 + lanes)
+    outs = [np.zeros(abi.surface_bytes(abi.FORMAT_NAMES.index(f), w, h), np.uint8) for f, w, h, _, _ in reqs]
+    with Server(max_batch_jobs=16, max_wait_us=100, lanes=lanes, pool_bytes=64 << 20) as srv:
+        ts = [srv.submit_new(f, w, h, fills, init=init, out=outs[i]) for i, (f, w, h, fills, init) in enumerate(reqs)]
+        for t in ts:
+            srv.wait(t)
+        info = srv.info()
+    assert info["requests"] == len(reqs) and info["lanes"] == lanes
+    assert info["pool_peak_bytes"] <= info["pool_bytes"]
+    for i, (f, w, h, fills, init) in enumerate(reqs):
+        ref = _drawn_alone(oracle, f, w, h, fills, init)
+        assert np.array_equal(outs[i], ref), f"request {i} ({f} {w}x{h}): {int((outs[i] != ref).sum())} bytes differ"
+
+
+def test_server_batches_overlap_on_the_gpu(oracle):
+    """With two lanes and a backlog of requests, a second batch starts while
+    the first is still being drawn; results are still those drawn alone."""
+    pytest.importorskip("torch")
+    rng = np.random.default_rng(3)
+    reqs = []
+    for i in range(240):
+        w, h = int(rng.integers(200, 400)), int(rng.integers(150, 300))
+        reqs.append(("rgba", w, h, random_fills(seed=9000 + i, n=int(rng.integers(4, 12)), w=w, h=h, side_lo=8,
+                                                side_hi=min(w, h), seg_lo=3, seg_hi=40), None))
+    outs = [np.zeros(w * h * 4, np.uint8) for _, w, h, _, _ in reqs]
+    with Server(max_batch_jobs=24, max_wait_us=0, lanes=2, pool_bytes=256 << 20) as srv:
+        ts = [srv.submit_new(f, w, h, fills, out=outs[i]) for i, (f, w, h, fills, _) in enumerate(reqs)]
+        for t in ts:
+            srv.wait(t)
+        info = srv.info()
+    assert info["batches"] >= 2
+    assert info["max_inflight"] >= 2, info
+    for i in range(0, len(reqs), 7):
+        f, w, h, fills, init = reqs[i]
+        assert np.array_equal(outs[i], _drawn_alone(oracle, f, w, h, fills, init)), f"request {i}"
+
+
+def test_server_pool_admission_waits_for_space(oracle):
+    """A pool that holds only a few surfaces at a time: requests wait for
+    space (deferred admissions), the pool's high-water mark stays within
+    it, and every result is still exact."""
+    pytest.importorskip("torch")
+    reqs = [("rgba", 64, 64, random_fills(seed=7000 + i, n=3, w=64, h=64, side_lo=4, side_hi=60, seg_lo=3,
+                                          seg_hi=20), None) for i in range(120)]
+    outs = [np.zeros(64 * 64 * 4, np.uint8) for _ in reqs]
+    pool = 4 * 64 * 64 * 4  # room for four surfaces
+    with Server(max_batch_jobs=32, max_wait_us=0, lanes=2, pool_bytes=pool) as srv:
+        ts = [srv.submit_new(f, w, h, fills, out=outs[i]) for i, (f, w, h, fills, _) in enumerate(reqs)]
+        for t in ts:
+            srv.wait(t)
+        info = srv.info()
+    assert info["pool_bytes"] == pool
+    assert info["pool_peak_bytes"] <= pool
+    assert info["deferred"] > 0
+    for i, (f, w, h, fills, init) in enumerate(reqs):
+        assert np.array_equal(outs[i], _drawn_alone(oracle, f, w, h, fills, init)), f"request {i}"
+
+
+def test_server_pool_rejections():
+    pytest.importorskip("torch")
+    fills = random_fills(seed=1, n=1, w=8, h=8, side_lo=2, side_hi=6, seg_lo=3, seg_hi=4)
+    with Server(pool_bytes=1 << 16) as srv:
+        with pytest.raises(Z2DError) as e:
+            srv.submit_new("rgba", 512, 512, fills)  # 1 MiB surface, 64 KiB pool
+        assert e.value.code == abi.ERR_OUT_OF_MEMORY
+    with Server() as srv:  # no pool
+        with pytest.raises(Z2DError) as e:
+            srv.submit_new("rgba", 8, 8, fills)
+        assert e.value.code == abi.ERR_INVALID_STATE

@@ -61,6 +61,17 @@ class z2d_pixel(C.Structure):
                 ("b", C.c_uint8), ("a", C.c_uint8)]
 
 
+class z2dgpu_server_opts(C.Structure):
+    _fields_ = [("max_batch_jobs", C.c_int32), ("max_wait_us", C.c_int32), ("lanes", C.c_int32),
+                ("pool_bytes", C.c_int64)]
+
+
+class z2dgpu_server_stats_t(C.Structure):
+    _fields_ = [("batches", C.c_uint64), ("requests", C.c_uint64), ("deferred", C.c_uint64), ("busy_ms", C.c_double),
+                ("lanes", C.c_int32), ("max_inflight", C.c_int32), ("pool_bytes", C.c_int64),
+                ("pool_peak_bytes", C.c_int64)]
+
+
 class z2d_surface(C.Structure):
     _fields_ = [("format", C.c_int32), ("width", C.c_int32), ("height", C.c_int32),
                 ("location", C.c_int32), ("data", C.c_void_p)]
@@ -148,7 +159,8 @@ EXPORTED_SYMBOLS = [
     "z2dgpu_stroke_contours",
     "z2dgpu_composite",
     "z2dgpu_composite_noalloc", "z2dgpu_server_create", "z2dgpu_server_submit", "z2dgpu_server_wait",
-    "z2dgpu_server_stats", "z2dgpu_server_destroy", "z2dgpu_png_encode", "z2dgpu_png_scanlines", "z2dgpu_free",
+    "z2dgpu_server_stats", "z2dgpu_server_destroy", "z2dgpu_server_create2", "z2dgpu_server_submit_new",
+    "z2dgpu_server_info", "z2dgpu_png_encode", "z2dgpu_png_scanlines", "z2dgpu_free",
 ]
 
 PROFILE = {None: -1, "linear": 0, "srgb": 1}  # color.RGBProfile of the PNG exporter

@@ -146,8 +146,18 @@ int make_dev_gradient(const z2d_gradient &g, DevGradient &out) {
         order[j] = v;
     }
     for (int i = 0; i < g.n_stops; i++) {
+        const z2d_color &col = g.stops[order[i].idx].color;
         out.offsets[i] = order[i].off;
-        out.colors[i] = g.stops[order[i].idx].color;
+        out.prep[i] = prepare_stop(g.method, col);
+    }
+    if (g.type == Z2D_GRADIENT_LINEAR) {  // Linear.getOffset's per-gradient terms (src/gradient.zig:355-359)
+        out.lin_dx = g.geom[2] - g.geom[0];
+        out.lin_dy = g.geom[3] - g.geom[1];
+        double dist = 0.0;
+        dist += out.lin_dx * out.lin_dx;
+        dist += out.lin_dy * out.lin_dy;
+        out.lin_zero = dist == 0.0;
+        out.lin_inv = out.lin_zero ? 0.0 : 1.0 / dist;
     }
     if (g.type == Z2D_GRADIENT_RADIAL) {  // Radial.initBuffer (src/gradient.zig:401-438)
         const double ir = std::fmax(0.0, g.geom[2]), orr = std::fmax(0.0, g.geom[5]);

@@ -88,11 +88,15 @@ __global__ void __launch_bounds__(256) k_composite_flat(const CompJob J, size_t 
         uint32_t w[4] = {v.x, v.y, v.z, v.w};
         if constexpr (FMT <= Z2D_FORMAT_RGBA) {
             const size_t i0 = c * 4;
+            // (x, y) of the chunk's first pixel, then stepped along the rows
+            int32_t y = (int32_t)(i0 / (size_t)W), x = (int32_t)(i0 - (size_t)y * W);
 #pragma unroll
             for (int j = 0; j < 4; j++) {
-                const size_t i = i0 + j;
-                const int32_t y = (int32_t)(i / (size_t)W), x = (int32_t)(i - (size_t)y * W);
                 w[j] = i16_to_word(run_batch<PREC>(J, x, y, word_to_i16(w[j], FMT)), FMT);
+                if (++x == W) {
+                    x = 0;
+                    y++;
+                }
             }
         } else {
             constexpr int BITS = FMT == Z2D_FORMAT_ALPHA8 ? 8 : FMT == Z2D_FORMAT_ALPHA4 ? 4 : FMT == Z2D_FORMAT_ALPHA2 ? 2 : 1;
@@ -100,6 +104,7 @@ __global__ void __launch_bounds__(256) k_composite_flat(const CompJob J, size_t 
             constexpr uint32_t MASK = (1u << BITS) - 1u;
             const size_t i0 = c * 4 * PER_WORD;
             const size_t total = (size_t)W * (size_t)J.dst.h;
+            int32_t y = (int32_t)(i0 / (size_t)W), x = (int32_t)(i0 - (size_t)y * W);
 #pragma unroll 1
             for (int j = 0; j < 4; j++) {
                 uint32_t out = w[j];
@@ -107,9 +112,13 @@ __global__ void __launch_bounds__(256) k_composite_flat(const CompJob J, size_t 
                 for (int k = 0; k < PER_WORD; k++) {
                     const size_t i = i0 + (size_t)j * PER_WORD + k;
                     if (i >= total) break;
-                    const int32_t y = (int32_t)(i / (size_t)W), x = (int32_t)(i - (size_t)y * W);
+                    const int32_t px = x, py = y;
+                    if (++x == W) {
+                        x = 0;
+                        y++;
+                    }
                     const uint32_t raw = (w[j] >> (k * BITS)) & MASK;
-                    const I16 r = run_batch<PREC>(J, x, y, I16{0, 0, 0, scale_alpha(raw, BITS, 8)});
+                    const I16 r = run_batch<PREC>(J, px, py, I16{0, 0, 0, scale_alpha(raw, BITS, 8)});
                     const uint32_t nv = scale_alpha(r.a & 0xFFu, 8, BITS);
                     out = (out & ~(MASK << (k * BITS))) | (nv << (k * BITS));
                 }

@@ -117,14 +117,18 @@ static int fmt_slot(int fmt) {
 }
 
 bool try_mask_batch(Ctx &c, const CompJob &J, bool flat) {
-    if (!flat || J.precision != Z2D_PRECISION_INTEGER || J.n_ops != 2) return false;
+    if (!flat || J.n_ops != 2) return false;
     const CompOp &o0 = J.ops[0], &o1 = J.ops[1];
     if (o0.op != Z2D_OP_DST_IN || o0.dst.kind != SRC_PIXEL || o0.src.kind != SRC_SURFACE) return false;
     if (o0.src.sfc.fmt != Z2D_FORMAT_ALPHA8 || o0.src.sfc.w != J.dst.w || o0.src.sfc.h < J.dst.h) return false;
-    if (o1.dst.kind != SRC_NONE || o1.src.kind != SRC_NONE || J.dst.fmt > Z2D_FORMAT_ALPHA8) return false;
+    if (o1.dst.kind != SRC_NONE || o1.src.kind != SRC_NONE) return false;
     if (o1.op < 0 || o1.op >= Z2D_OP_COUNT) return false;
     if ((reinterpret_cast<uintptr_t>(o0.src.sfc.data) & 15) != 0) return false;
     const size_t px = (size_t)J.dst.w * J.dst.h;
+    // float precision and the packed formats (composite_fused.cu)
+    if (J.precision == Z2D_PRECISION_FLOAT)
+        return launch_mask_float(c, J.dst.data, J.dst.fmt, o0.src.sfc.data, px, o1.op, o0.dst.pixf);
+    if (fmt_packed(J.dst.fmt)) return launch_mask_packed(c, J.dst.data, J.dst.fmt, o0.src.sfc.data, px, o1.op, o0.dst.pix);
     const int per = J.dst.fmt <= Z2D_FORMAT_RGBA ? 4 : 16;
     if (px % per != 0) return false;
     const size_t n_chunks = px / per;

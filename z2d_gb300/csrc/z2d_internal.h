@@ -143,5 +143,10 @@ const char *last_error();
 // Launches the whole-surface mask batch [dst_in(pixel, alpha8 mask), op]
 // when J has that shape (composite_mask.cu); returns false otherwise.
 bool try_mask_batch(Ctx &c, const CompJob &J, bool flat);
+// The same batch in float precision (4-byte formats, alpha8) and on the
+// packed alpha formats in integer precision (composite_fused.cu); false
+// when the surface does not fit the kernel's layout.
+bool launch_mask_float(Ctx &c, uint8_t *dst, int fmt, const uint8_t *mask, size_t px, int op, const F4 &spf);
+bool launch_mask_packed(Ctx &c, uint8_t *dst, int fmt, const uint8_t *mask, size_t px, int op, const I16 &spx);
 
 }  // namespace z2dg

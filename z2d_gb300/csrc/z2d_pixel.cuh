@@ -414,9 +414,18 @@ Z2D_HD float zmodf(float a, float b) {
     const float r = fmodf(a, b);
     return a < 0.0f ? fmodf(r + b, b) : r;
 }
+// fmod, exact: for b <= |a| < 2b the difference a -/+ b is exact (Sterbenz),
+// so only operands of two or more periods reach the library fmod.
+Z2D_D double fmod_exact(double a, double b) {
+    const double m = fabs(a);
+    if (m < b) return a;
+    if (m < 2.0 * b) return a < 0.0 ? a + b : a - b;
+    return fmod(a, b);
+}
+// Zig's @mod on f64 (fmod, moved into [0, b) for a negative numerator)
 Z2D_D double zmod(double a, double b) {
-    const double r = fmod(a, b);
-    return a < 0.0 ? fmod(r + b, b) : r;
+    const double r = fmod_exact(a, b);
+    return a < 0.0 ? fmod_exact(r + b, b) : r;
 }
 
 constexpr float kGamma = 2.2f;
@@ -448,12 +457,12 @@ Z2D_HD RGBf linear_from_color(const z2d_color &c) {
     }
     return o;
 }
-Z2D_D RGBf srgb_from_color(const z2d_color &c) {
+Z2D_HD RGBf srgb_from_color(const z2d_color &c) {
     if (c.space == Z2D_COLOR_SRGB) return RGBf{c.c[0], c.c[1], c.c[2], c.c[3]};
     const RGBf lin = (c.space == Z2D_COLOR_HSL) ? hsl_to_rgb(HSLf{c.c[0], c.c[1], c.c[2], c.c[3]}) : RGBf{c.c[0], c.c[1], c.c[2], c.c[3]};
     return RGBf{zpow(lin.r, Z2D_INV_GAMMA), zpow(lin.g, Z2D_INV_GAMMA), zpow(lin.b, Z2D_INV_GAMMA), lin.a};
 }
-Z2D_D HSLf hsl_from_rgb(RGBf s) {
+Z2D_HD HSLf hsl_from_rgb(RGBf s) {
     const float mx = fmaxf(s.r, fmaxf(s.g, s.b)), mn = fminf(s.r, fminf(s.g, s.b));
     const float range = mx - mn, light = (mn + mx) / 2.0f;
     float sat = (light == 0.0f || light == 1.0f) ? 0.0f : (mx - light) / fminf(light, 1.0f - light);
@@ -470,76 +479,38 @@ Z2D_D HSLf hsl_from_rgb(RGBf s) {
     }
     return HSLf{hue, sat, light, s.a};
 }
-Z2D_D HSLf hsl_from_color(const z2d_color &c) {
+Z2D_HD HSLf hsl_from_color(const z2d_color &c) {
     if (c.space == Z2D_COLOR_HSL) return HSLf{c.c[0], c.c[1], c.c[2], c.c[3]};
     return hsl_from_rgb(linear_from_color(c));
 }
 Z2D_D float lerpf(float a, float b, float t) { return a + (b - a) * t; }
-Z2D_D RGBf rgb_interp(RGBf a, RGBf b, float t) {
-    const RGBf am{a.r * a.a, a.g * a.a, a.b * a.a, a.a}, bm{b.r * b.a, b.g * b.a, b.b * b.a, b.a};
-    const RGBf o{lerpf(am.r, bm.r, t), lerpf(am.g, bm.g, t), lerpf(am.b, bm.b, t), lerpf(am.a, bm.a, t)};
-    if (o.a == 0.0f) return RGBf{0.f, 0.f, 0.f, o.a};
-    return RGBf{o.r / o.a, o.g / o.a, o.b / o.a, o.a};
-}
-Z2D_D HSLf hsl_interp(HSLf a, HSLf b, float t, int polar) {
-    const HSLf am{a.h, a.s * a.a, a.l * a.a, a.a}, bm{b.h, b.s * b.a, b.l * b.a, b.a};
-    float ah = am.h, bh = bm.h;
-    if (polar == Z2D_INTERP_HSL_SHORTER) {
-        const bool gt = bh - ah > 180.0f, lt = bh - ah < -180.0f;
-        if (gt) ah = ah + 360.0f;
-        if (lt) bh = bh + 360.0f;
-    } else if (polar == Z2D_INTERP_HSL_LONGER) {
-        const float delta = bh - ah;
-        const bool c1 = (0.0f < delta) && (delta < 180.0f), c2 = (-180.0f < delta) && (delta <= 0.0f);
-        if (c1) ah = ah + 360.0f;
-        if (c2) bh = bh + 360.0f;
-    } else if (polar == Z2D_INTERP_HSL_INCREASING) {
-        if (bh < ah) bh = bh + 360.0f;
-    } else {
-        if (ah < bh) ah = ah + 360.0f;
-    }
-    const float h = am.h + (bh - ah) * t;
-    const HSLf o{zmodf(h, 360.0f), lerpf(am.s, bm.s, t), lerpf(am.l, bm.l, t), lerpf(am.a, bm.a, t)};
-    if (o.a == 0.0f) return HSLf{o.h, 0.0f, 0.0f, o.a};
-    return HSLf{o.h, o.s / o.a, o.l / o.a, o.a};
-}
 Z2D_D I16 premul16(I16 v) {
     return I16{((v.r * v.a) & 0xFFFFu) / 255u, ((v.g * v.a) & 0xFFFFu) / 255u, ((v.b * v.a) & 0xFFFFu) / 255u, v.a};
 }
 Z2D_D I16 encode_linear(RGBf c) { return premul16(I16{enc_ch(c.r), enc_ch(c.g), enc_ch(c.b), enc_ch(c.a)}); }
 
-Z2D_D I16 interp_encode(int method, const z2d_color &c0, const z2d_color &c1, float t) {
-    if (method == Z2D_INTERP_LINEAR_RGB) {
-        const RGBf a = linear_from_color(c0), b = linear_from_color(c1);
-        const RGBf am{a.r * a.a, a.g * a.a, a.b * a.a, a.a}, bm{b.r * b.a, b.g * b.a, b.b * b.a, b.a};
-        return I16{enc_ch(lerpf(am.r, bm.r, t)), enc_ch(lerpf(am.g, bm.g, t)), enc_ch(lerpf(am.b, bm.b, t)), enc_ch(lerpf(am.a, bm.a, t))};
-    }
-    if (method == Z2D_INTERP_SRGB) {
-        const RGBf d = rgb_interp(srgb_from_color(c0), srgb_from_color(c1), t);
-        return encode_linear(RGBf{zpow(d.r, kGamma), zpow(d.g, kGamma), zpow(d.b, kGamma), d.a});
-    }
-    return encode_linear(hsl_to_rgb(hsl_interp(hsl_from_color(c0), hsl_from_color(c1), t, method)));
-}
-Z2D_D RGBf interp_linear(int method, const z2d_color &c0, const z2d_color &c1, float t) {
-    if (method == Z2D_INTERP_LINEAR_RGB) return rgb_interp(linear_from_color(c0), linear_from_color(c1), t);
-    if (method == Z2D_INTERP_SRGB) {
-        const RGBf d = rgb_interp(srgb_from_color(c0), srgb_from_color(c1), t);
-        return RGBf{zpow(d.r, kGamma), zpow(d.g, kGamma), zpow(d.b, kGamma), d.a};
-    }
-    return hsl_to_rgb(hsl_interp(hsl_from_color(c0), hsl_from_color(c1), t, method));
-}
 
 // --------------------------------------------------------- gradients
 // Gradient prepared on the host: stops clamped and sorted
 // (src/gradient.zig:797-811), radial pre-calcs (:401-438), conic angle
 // normalised (:666-681).
+// Per stop, its colour in the gradient's interpolation space, premultiplied
+// by its alpha: LinearRGB (r*a, g*a, b*a, a) for linear_rgb, SRGB the same
+// for srgb, HSL (h, s*a, l*a, a) for the hsl methods.  That is the first
+// step of interpolateEncode / interpolate on each of the two stops
+// (src/color.zig, src/internal/color_vector.zig); it depends on the stop
+// only, so it is computed once on the host (same IEEE operations).
 struct DevGradient {
     int32_t type, method, n_stops, has_tf;
     double g[6];
     double tf[6];
     double inner_r, outer_r, cdx, cdy, dr, min_dr, a, inv_a, angle;
+    // Linear.getOffset's per-gradient terms (src/gradient.zig:355-359):
+    // end - start and 1 / |end - start|^2; lin_zero: zero-length gradient
+    double lin_dx, lin_dy, lin_inv;
+    int32_t lin_zero, pad_;
     float offsets[kMaxStops];
-    z2d_color colors[kMaxStops];
+    RGBf prep[kMaxStops];
 };
 
 Z2D_D double clampd(double v, double lo, double hi) { return fmax(lo, fmin(v, hi)); }
@@ -556,17 +527,12 @@ Z2D_D float grad_offset(const DevGradient &gr, int32_t x, int32_t y) {
         py += gr.tf[5];
     }
     if (gr.type == Z2D_GRADIENT_LINEAR) {
-        const double dx = gr.g[2] - gr.g[0], dy = gr.g[3] - gr.g[1];
-        double dist = 0.0;
-        dist += dx * dx;
-        dist += dy * dy;
-        if (dist == 0.0) return -1.0f;
-        const double inv = 1.0 / dist;
+        if (gr.lin_zero) return -1.0f;
         const double spx = px - gr.g[0], spy = py - gr.g[1];
         double d = 0.0;
-        d += dx * spx;
-        d += dy * spy;
-        return (float)clampd(d * inv, 0.0, 1.0);
+        d += gr.lin_dx * spx;
+        d += gr.lin_dy * spy;
+        return (float)clampd(d * gr.lin_inv, 0.0, 1.0);
     }
     if (gr.type == Z2D_GRADIENT_RADIAL) {
         const double pdx = px - gr.g[0], pdy = py - gr.g[1];
@@ -628,10 +594,76 @@ Z2D_D Search grad_search(const DevGradient &gr, float offset) {
     const float st = gr.offsets[mid], en = gr.offsets[mid + 1], rl = en - st;
     return Search{mid, mid + 1, (rl != 0.0f) ? (o - st) / rl : 0.0f};
 }
-Z2D_D z2d_color stop_color(const DevGradient &gr, int i) {
-    // LinearRGB.init(0,0,0,0) for the transparent result of an invalid offset
-    if (i < 0) return z2d_color{Z2D_COLOR_LINEAR_RGB, {0.f, 0.f, 0.f, 0.f}};
-    return gr.colors[i];
+// The prepared colour of stop i; i < 0 is the transparent result of an
+// invalid offset, LinearRGB.init(0,0,0,0), which is zero in every space.
+Z2D_D RGBf stop_prep(const DevGradient &gr, int i) {
+    if (i < 0) return RGBf{0.f, 0.f, 0.f, 0.f};
+    return gr.prep[i];
+}
+
+// The first step of the interpolation on a stop's colour (see DevGradient).
+Z2D_HD RGBf prepare_stop(int method, const z2d_color &c) {
+    if (method == Z2D_INTERP_LINEAR_RGB) {
+        const RGBf a = linear_from_color(c);
+        return RGBf{a.r * a.a, a.g * a.a, a.b * a.a, a.a};
+    }
+    if (method == Z2D_INTERP_SRGB) {
+        const RGBf a = srgb_from_color(c);
+        return RGBf{a.r * a.a, a.g * a.a, a.b * a.a, a.a};
+    }
+    const HSLf h = hsl_from_color(c);
+    return RGBf{h.h, h.s * h.a, h.l * h.a, h.a};
+}
+
+// LinearRGB / SRGB interpolate from premultiplied stops: the lerp, then
+// demultiply (src/color.zig:356-372).
+Z2D_D RGBf rgb_lerp_demul(RGBf am, RGBf bm, float t) {
+    const RGBf o{lerpf(am.r, bm.r, t), lerpf(am.g, bm.g, t), lerpf(am.b, bm.b, t), lerpf(am.a, bm.a, t)};
+    if (o.a == 0.0f) return RGBf{0.f, 0.f, 0.f, o.a};
+    return RGBf{o.r / o.a, o.g / o.a, o.b / o.a, o.a};
+}
+// HSL.interpolate from premultiplied stops (polar hue handling, then
+// demultiply of saturation and lightness).
+Z2D_D HSLf hsl_lerp_demul(RGBf am, RGBf bm, float t, int polar) {
+    float ah = am.r, bh = bm.r;
+    if (polar == Z2D_INTERP_HSL_SHORTER) {
+        const bool gt = bh - ah > 180.0f, lt = bh - ah < -180.0f;
+        if (gt) ah = ah + 360.0f;
+        if (lt) bh = bh + 360.0f;
+    } else if (polar == Z2D_INTERP_HSL_LONGER) {
+        const float delta = bh - ah;
+        const bool c1 = (0.0f < delta) && (delta < 180.0f), c2 = (-180.0f < delta) && (delta <= 0.0f);
+        if (c1) ah = ah + 360.0f;
+        if (c2) bh = bh + 360.0f;
+    } else if (polar == Z2D_INTERP_HSL_INCREASING) {
+        if (bh < ah) bh = bh + 360.0f;
+    } else {
+        if (ah < bh) ah = ah + 360.0f;
+    }
+    const float h = am.r + (bh - ah) * t;
+    const HSLf o{zmodf(h, 360.0f), lerpf(am.g, bm.g, t), lerpf(am.b, bm.b, t), lerpf(am.a, bm.a, t)};
+    if (o.a == 0.0f) return HSLf{o.h, 0.0f, 0.0f, o.a};
+    return HSLf{o.h, o.s / o.a, o.l / o.a, o.a};
+}
+// interpolateEncode: the integer lanes of the interpolated colour.
+Z2D_D I16 interp_encode_prep(int method, RGBf am, RGBf bm, float t) {
+    if (method == Z2D_INTERP_LINEAR_RGB)
+        return I16{enc_ch(lerpf(am.r, bm.r, t)), enc_ch(lerpf(am.g, bm.g, t)), enc_ch(lerpf(am.b, bm.b, t)),
+                   enc_ch(lerpf(am.a, bm.a, t))};
+    if (method == Z2D_INTERP_SRGB) {
+        const RGBf d = rgb_lerp_demul(am, bm, t);
+        return encode_linear(RGBf{zpow(d.r, kGamma), zpow(d.g, kGamma), zpow(d.b, kGamma), d.a});
+    }
+    return encode_linear(hsl_to_rgb(hsl_lerp_demul(am, bm, t, method)));
+}
+// interpolate: the linear colour (float precision, dither sources).
+Z2D_D RGBf interp_linear_prep(int method, RGBf am, RGBf bm, float t) {
+    if (method == Z2D_INTERP_LINEAR_RGB) return rgb_lerp_demul(am, bm, t);
+    if (method == Z2D_INTERP_SRGB) {
+        const RGBf d = rgb_lerp_demul(am, bm, t);
+        return RGBf{zpow(d.r, kGamma), zpow(d.g, kGamma), zpow(d.b, kGamma), d.a};
+    }
+    return hsl_to_rgb(hsl_lerp_demul(am, bm, t, method));
 }
 
 // -------------------------------------------------------------- dither
@@ -672,7 +704,7 @@ Z2D_D RGBf dither_linear(const DevSrc &s, int32_t x, int32_t y) {
     RGBf c;
     if (s.dither_source == Z2D_DITHER_SRC_GRADIENT) {
         const Search r = grad_search(*s.grad, grad_offset(*s.grad, x, y));
-        c = interp_linear(s.grad->method, stop_color(*s.grad, r.i0), stop_color(*s.grad, r.i1), r.offset);
+        c = interp_linear_prep(s.grad->method, stop_prep(*s.grad, r.i0), stop_prep(*s.grad, r.i1), r.offset);
     } else {
         c = s.dither_base;
     }
@@ -692,7 +724,7 @@ Z2D_D I16 src_i16(const DevSrc &s, int32_t x, int32_t y, size_t idx) {
         case SRC_PIXEL: return s.pix;
         case SRC_GRADIENT: {
             const Search r = grad_search(*s.grad, grad_offset(*s.grad, x, y));
-            return interp_encode(s.grad->method, stop_color(*s.grad, r.i0), stop_color(*s.grad, r.i1), r.offset);
+            return interp_encode_prep(s.grad->method, stop_prep(*s.grad, r.i0), stop_prep(*s.grad, r.i1), r.offset);
         }
         case SRC_DITHER: return encode_linear(dither_linear(s, x, y));
         case SRC_SURFACE: return load_px(s.sfc, idx);
@@ -704,7 +736,7 @@ Z2D_D F4 src_f4(const DevSrc &s, int32_t x, int32_t y, size_t idx) {
         case SRC_PIXEL: return s.pixf;
         case SRC_GRADIENT: {
             const Search r = grad_search(*s.grad, grad_offset(*s.grad, x, y));
-            const RGBf c = interp_linear(s.grad->method, stop_color(*s.grad, r.i0), stop_color(*s.grad, r.i1), r.offset);
+            const RGBf c = interp_linear_prep(s.grad->method, stop_prep(*s.grad, r.i0), stop_prep(*s.grad, r.i1), r.offset);
             return F4{c.r, c.g, c.b, c.a};
         }
         case SRC_DITHER: {

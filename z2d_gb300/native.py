@@ -85,6 +85,11 @@ def load(build_if_missing: bool = True):
         lib.z2dgpu_composite_noalloc.argtypes = [C.c_int, C.c_void_p, P(abi.z2d_surface), C.c_int32, C.c_int32,
                                                  C.c_int32, P(abi.z2d_operation), C.c_int32]
         lib.z2dgpu_server_create.argtypes = [P(C.c_void_p), C.c_int, C.c_int32, C.c_int32]
+        lib.z2dgpu_server_create2.argtypes = [P(C.c_void_p), C.c_int, P(abi.z2dgpu_server_opts)]
+        lib.z2dgpu_server_submit_new.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                                                 P(abi.z2d_node), C.c_size_t, P(abi.z2d_fill_cmd), C.c_size_t,
+                                                 P(C.c_uint64)]
+        lib.z2dgpu_server_info.argtypes = [C.c_void_p, P(abi.z2dgpu_server_stats_t)]
         lib.z2dgpu_server_submit.argtypes = [C.c_void_p, P(abi.z2d_surface), P(abi.z2d_node), C.c_size_t,
                                              P(abi.z2d_fill_cmd), C.c_size_t, P(C.c_uint64)]
         lib.z2dgpu_server_wait.argtypes = [C.c_void_p, C.c_uint64, C.c_int32, P(C.c_double)]
@@ -96,7 +101,8 @@ def load(build_if_missing: bool = True):
             getattr(lib, name).restype = C.c_int
         lib.z2dgpu_free.argtypes = [C.c_void_p]
         lib.z2dgpu_free.restype = None
-        for name in ("z2dgpu_server_create", "z2dgpu_server_submit", "z2dgpu_server_wait", "z2dgpu_server_stats",
+        for name in ("z2dgpu_server_create", "z2dgpu_server_create2", "z2dgpu_server_submit",
+                     "z2dgpu_server_submit_new", "z2dgpu_server_wait", "z2dgpu_server_stats", "z2dgpu_server_info",
                      "z2dgpu_server_destroy"):
             getattr(lib, name).restype = C.c_int
         for name in ("z2dgpu_ctx_create", "z2dgpu_ctx_destroy", "z2dgpu_ctx_synchronize", "z2dgpu_fill",
