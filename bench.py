@@ -64,6 +64,21 @@ def load_peaks():
         return PEAKS_FALLBACK, "fallback"
 
 
+def settle_tuning(ctx, step, max_calls=12):
+    """Runs `step` until the rasteriser's autotuner has decided the schedule
+    for this kind of pass (it times one candidate schedule per pass at
+    first); returns what it chose and how many passes that took."""
+    calls = 0
+    state = ctx.raster_tuning()
+    while calls < max_calls:
+        step()
+        calls += 1
+        state = ctx.raster_tuning()
+        if state["decided"] != 0:
+            break
+    return dict(state, passes=calls)
+
+
 def workload():
     from z2d_gb300.workloads import fill_box_pixels, premultiplied_background, random_fills
     rng = np.random.default_rng(SEED)
@@ -388,7 +403,6 @@ def compositor_breadth(ctx, stream, dev, reps=2):
 
 N_JOBS = 4096             # batched-jobs arm: RGBA jobs, sides log-uniform [16, 2048], 1-200 paths each
 JOBS_PLAIN_FILLS = 1500   # per-call sample of the jobs arm (complete jobs, in order)
-JOBS_CPU_SECONDS = 10.0   # CPU sample of the jobs arm: whole jobs in order until this much wall time
 
 
 JOBS_STROKED = 0.3        # share of paths stroked instead of filled
@@ -458,6 +472,13 @@ def jobs_arm(ctx, stream, dev, steps=3):
 
     restore()
     pb.draw_jobs(ctx)  # warm
+
+    def tune_step():
+        restore()
+        pb.draw_jobs(ctx)
+        stream.synchronize()
+
+    tuning = settle_tuning(ctx, tune_step)
     ctx.set_timing(True)
     walls = []
     for _ in range(steps):
@@ -469,6 +490,8 @@ def jobs_arm(ctx, stream, dev, steps=3):
         torch.cuda.nvtx.range_pop()
         walls.append(time.perf_counter() - t0)
     stage_ms = {k: ctx.kernel_ms(k)[0] / steps for k in ("flatten", "stroke", "bins", "raster")}
+    out_jobs = buf.cpu().numpy()  # the last timed pass's surfaces, for the parity check
+    pristine_host = pristine.cpu().numpy()
     ctx.set_timing(False)
     # one call per surface, first jobs
     restore()
@@ -519,10 +542,11 @@ def jobs_arm(ctx, stream, dev, steps=3):
         "note": "wall time of the call (host validation, stroke building, packing, uploads, kernels); "
                 "inputs in host memory, surfaces on the device",
         "generation_s": t_gen,
+        "autotune": tuning,
     }
     del buf, pristine, surfaces
-    # CPU restatement on all host threads, one job per thread, whole jobs in
-    # order until JOBS_CPU_SECONDS have passed
+    # CPU restatement on all host threads, one job per thread: every job,
+    # drawn from its seeded background, is compared with the GPU's pass
     from oracle import load_oracle
     from concurrent.futures import ThreadPoolExecutor
     import ctypes as C
@@ -532,7 +556,7 @@ def jobs_arm(ctx, stream, dev, steps=3):
 
     def prepare(j):
         w, h = jobs[j][0], jobs[j][1]
-        host = np.zeros(w * h * 4, np.uint8)
+        host = pristine_host[starts[j]:starts[j] + sizes[j]].copy()
         keep, calls = [], []
         for kind, pat, nd, o in ops_of(j):
             p = pat.to_abi(keep)
@@ -565,18 +589,29 @@ def jobs_arm(ctx, stream, dev, steps=3):
     nt = host_threads()
     k = nf = 0
     cpu_s = 0.0
+    bad_jobs, bad_px = [], 0
     with ThreadPoolExecutor(nt) as ex:
-        while k < len(jobs) and cpu_s < JOBS_CPU_SECONDS:
+        while k < len(jobs):
             chunk = list(range(k, min(len(jobs), k + 4 * nt)))
             work = [prepare(j) for j in chunk]
             t0 = time.perf_counter()
             list(ex.map(run, work))
             cpu_s += time.perf_counter() - t0
+            for j, item in zip(chunk, work):
+                got = out_jobs[starts[j]:starts[j] + sizes[j]]
+                if not np.array_equal(got, item[1]):
+                    bad_jobs.append(j)
+                    bad_px += int((got.reshape(-1, 4) != item[1].reshape(-1, 4)).any(1).sum())
             k = chunk[-1] + 1
             nf += sum(cmd_cnt[j] for j in chunk)
     out["cpu"] = {"value": sum(jobs[j][0] * jobs[j][1] for j in range(k)) / 1e6 / cpu_s, "jobs": k, "commands": nf,
                   "cores": nt, "seconds": cpu_s, "kind": "port",
-                  "note": "stroke polygons built on the host beforehand (not timed); fills and polygons rasterised"}
+                  "note": "every job; stroke polygons built on the host beforehand (not timed), fills and polygons "
+                          "rasterised"}
+    out["parity"] = {"jobs_checked": k, "differing_jobs": len(bad_jobs), "differing_pixels": bad_px,
+                     "first_differing": bad_jobs[:8],
+                     "reference": "oracle on host threads, every job from its seeded background; stroked paths "
+                                  "rasterised from the host stroke builder's polygons"}
     return out
 
 
@@ -612,6 +647,7 @@ def png_arm(ctx, surf, peak_gbs):
 
 
 SERVE_LANES = 3           # server lanes (batches drawn concurrently)
+SERVE_WAIT_US = 0         # batching window: none, a free lane takes what is queued
 SERVE_POOL = 4 << 30      # device surface pool of the server
 SERVE_OUT_RING = 2048     # host result buffers, reused round-robin by the requests
 SERVE_PARITY = 4096       # requests of the fastest rate compared with the oracle
@@ -620,8 +656,8 @@ SERVE_PARITY = 4096       # requests of the fastest rate compared with the oracl
 def serving_arm(dev):
     """The serving configuration: requests arrive as a Poisson process and go
     through the continuous-batching server (z2d_gb300.server: SERVE_LANES
-    lanes drawing batches concurrently, up to 512 requests per batch, a
-    300 us batching window).  Each request draws on a surface the server
+    lanes drawing batches concurrently, up to 512 requests per batch; a free
+    lane takes whatever is queued, so batches grow with the load).  Each request draws on a surface the server
     allocates from its device pool (cleared) and reads the result back into
     a host buffer, so latency is end to end (submit to pixels in host
     memory).  Mix: 80 % glyph-like requests (one outline of 20-200 cubics on
@@ -674,16 +710,21 @@ def serving_arm(dev):
     ring = np.zeros((SERVE_OUT_RING, 512 * 512 * 4), np.uint8)
     results = {}
     parity = None
-    with Server(max_batch_jobs=512, max_wait_us=300, lanes=SERVE_LANES, pool_bytes=SERVE_POOL) as srv:
+    with Server(max_batch_jobs=512, max_wait_us=SERVE_WAIT_US, lanes=SERVE_LANES, pool_bytes=SERVE_POOL) as srv:
         lib = srv.lib
 
         def out_buf(k):
             w, h = reqs[k % pool][0], reqs[k % pool][1]
             return ring[k % SERVE_OUT_RING, :w * h * 4]
 
-        for i in range(64):  # warm-up
-            w, h, nodes, cmds, _, _ = reqs[i]
-            srv.wait(_submit_new(lib, srv.handle, w, h, out_buf(i), nodes, cmds))
+        # warm-up: a burst of every request content, so that the lanes' device
+        # buffers have grown to their working size before anything is timed
+        # (growing one synchronises the device)
+        for rep in range(2):
+            ts = [_submit_new(lib, srv.handle, reqs[i][0], reqs[i][1], out_buf(i), reqs[i][2], reqs[i][3])
+                  for i in range(pool)]
+            for t in ts:
+                srv.wait(t)
         for rate in SERVE_RATES:
             n = int(rate * SERVE_SECONDS)
             arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
@@ -736,7 +777,7 @@ def serving_arm(dev):
         parity["reference"] = "each request drawn alone on a cleared surface by the oracle"
     return {"workload": "Poisson arrivals; 80% glyphs (20-200 cubics, 64x64, half gradient), 20% jobs "
                         "(sides 16-512, 1-50 paths); one pool surface per request, result read back to host",
-            "server": {"max_batch_jobs": 512, "max_wait_us": 300, "lanes": SERVE_LANES, "pool_bytes": SERVE_POOL,
+            "server": {"max_batch_jobs": 512, "max_wait_us": SERVE_WAIT_US, "lanes": SERVE_LANES, "pool_bytes": SERVE_POOL,
                        "info": info},
             "rates": results, "parity": parity}
 
@@ -813,7 +854,13 @@ def run_ours(args):
             surf_t.copy_(bg_dev)
             flush.fill_(1)
 
-    # ---- warm-up
+    # ---- the autotuner's exploration of this pass (untimed), then warm-up
+    def tune_step():
+        restore()
+        painter.fill_batch_arrays(surf, nodes, cmds, ctx=ctx)
+        stream.synchronize()
+
+    tuning = settle_tuning(ctx, tune_step)
     for _ in range(max(args.warmup, 1)):
         restore()
         painter.fill_batch_arrays(surf, nodes, cmds, ctx=ctx)
@@ -939,6 +986,7 @@ def run_ours(args):
         "jobs": jobs,
         "serving": serving,
         "png": png_res,
+        "autotune": tuning,
         "batched_over_plain": (mpix_step / (total_ms / args.steps / 1e3)) / (plain_mpix / (plain_ms / 1e3)),
         "parity": parity,
         "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

@@ -273,6 +273,21 @@ Z2D_API uint64_t z2dgpu_ctx_launch_count(const z2dgpu_ctx *ctx);
  * events on its stream and accumulates their device time.  Reading a time
  * synchronizes the context.  No reference counterpart (instrumentation). */
 Z2D_API int z2dgpu_ctx_set_timing(z2dgpu_ctx *ctx, int enable);
+/* The rasteriser's schedule on this context (no counterpart in z2d).  By
+ * default an autotuner picks it per kind of pass (one surface or many, its
+ * number of tiles, the mean fills per band) by timing the candidates on the
+ * first passes of each kind, and caches its choices in raster_tune.json
+ * beside the library (Z2D_TUNE_FILE overrides the path; Z2D_TUNE=off keeps
+ * the default schedule).  ctas_per_sm >= 0 forces a schedule: resident CTAs
+ * per SM (0 = as many as fit) and queue order (0 = tile order, 1 = tiles of
+ * the bands with the most fills first); ctas_per_sm = -1 returns to the
+ * tuner.  Every schedule draws the same pixels. */
+Z2D_API int z2dgpu_ctx_set_raster(z2dgpu_ctx *ctx, int32_t ctas_per_sm, int32_t order);
+/* The tuner's state for the kind of pass this context drew last: *decided =
+ * 1 with its schedule, 0 while candidates are still being timed, -1 when
+ * tuning is off. */
+Z2D_API int z2dgpu_ctx_raster_tuning(z2dgpu_ctx *ctx, int32_t *decided, int32_t *ctas_per_sm,
+                                     int32_t *order);
 /* Accumulated milliseconds and launch count of a stage since timing was
  * enabled: "raster" (k_raster), "composite" (compositor kernels), "flatten"
  * (path flattening, stroking and fill setup, two intervals per fill call),

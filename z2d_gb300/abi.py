@@ -154,7 +154,7 @@ def surface_bytes(fmt: int, width: int, height: int) -> int:
 EXPORTED_SYMBOLS = [
     "z2dgpu_version", "z2dgpu_last_error", "z2dgpu_ctx_create", "z2dgpu_ctx_destroy",
     "z2dgpu_ctx_synchronize", "z2dgpu_ctx_launch_count", "z2dgpu_ctx_set_timing",
-    "z2dgpu_ctx_kernel_ms", "z2dgpu_surface_bytes",
+    "z2dgpu_ctx_kernel_ms", "z2dgpu_ctx_set_raster", "z2dgpu_ctx_raster_tuning", "z2dgpu_surface_bytes",
     "z2dgpu_fill", "z2dgpu_fill_batch", "z2dgpu_fill_jobs", "z2dgpu_draw_jobs", "z2dgpu_stroke",
     "z2dgpu_stroke_contours",
     "z2dgpu_composite",

@@ -19,7 +19,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 OUT_DIR = PKG / "_lib"
 LIB = OUT_DIR / "libz2dgpu.so"
-SOURCES = ["capi.cu", "composite.cu", "composite_mask.cu", "composite_fused.cu", "fill.cu", "server.cu", "stroke.cpp", "stroke_gpu.cu", "hairline.cu", "png.cu"]
+SOURCES = ["capi.cu", "composite.cu", "composite_mask.cu", "composite_fused.cu", "fill.cu", "server.cu", "stroke.cpp", "stroke_gpu.cu", "hairline.cu", "png.cu", "tune.cu"]
 HEADERS = ["z2d_pixel.cuh", "z2d_internal.h", "fill.cuh", "stroke.h", "stroke_geom.h", "stroke_gpu.cuh", "edges.cuh", "spline.cuh", "raster_px.cuh", "host_pool.h", "blue_noise_64x64.inc", "zig_math.cuh"]
 ARCH = os.environ.get("Z2D_GPU_ARCH", "103a")
 
@@ -74,7 +74,7 @@ def build(force: bool = False, verbose: bool = False) -> pathlib.Path:
     if force or jobs or _stale(LIB, objs):
         tmp = OUT_DIR / f"libz2dgpu.{os.getpid()}.so"
         cmd = [nvcc(), f"-gencode=arch=compute_{ARCH},code=sm_{ARCH}", "-shared", "-o", str(tmp),
-               *[str(o) for o in objs], "-lcudart"] + (["-lz"] if HAVE_ZLIB else [])
+               *[str(o) for o in objs], "-lcudart", "-ldl"] + (["-lz"] if HAVE_ZLIB else [])
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             print(r.stdout + r.stderr)

@@ -1365,8 +1365,9 @@ Z2D_API int z2dgpu_ctx_destroy(z2dgpu_ctx *c) {
     cudaStreamSynchronize(c->stream);
     DevBuf *bufs[] = {&c->params, &c->nodes, &c->node_info, &c->edges, &c->fill_state, &c->counters, &c->band_fills,
                       &c->bins, &c->bin_offsets, &c->masks, &c->surface, &c->surface2, &c->surface3, &c->scan_tmp,
-                      &c->stroke_a, &c->stroke_b, &c->stroke_c, &c->curve_pool};
+                      &c->stroke_a, &c->stroke_b, &c->stroke_c, &c->curve_pool, &c->tile_order};
     for (DevBuf *b : bufs) b->release();
+    c->tune_collect(true);
     c->staging.release();
     c->readback.release();
     for (Ctx::Timer *t : {&c->t_raster, &c->t_composite, &c->t_flatten, &c->t_bins, &c->t_stroke, &c->t_export}) c->timer_collect(*t);
@@ -1396,6 +1397,26 @@ Z2D_API int z2dgpu_ctx_set_timing(z2dgpu_ctx *c, int enable) {
         *t = Ctx::Timer{};
     }
     c->timing = enable != 0;
+    return Z2D_OK;
+}
+
+Z2D_API int z2dgpu_ctx_set_raster(z2dgpu_ctx *c, int32_t ctas_per_sm, int32_t order) {
+    if (!c || ctas_per_sm < -1 || ctas_per_sm > 64 || (ctas_per_sm >= 0 && (order < 0 || order > 1)))
+        return Z2D_ERR_INVALID_ARGUMENT;
+    c->raster_forced = ctas_per_sm >= 0;
+    c->raster_ctas_per_sm = ctas_per_sm >= 0 ? ctas_per_sm : 0;
+    c->raster_order = ctas_per_sm >= 0 ? order : 0;
+    return Z2D_OK;
+}
+
+Z2D_API int z2dgpu_ctx_raster_tuning(z2dgpu_ctx *c, int32_t *decided, int32_t *ctas_per_sm, int32_t *order) {
+    if (!c || !decided || !ctas_per_sm || !order) return Z2D_ERR_INVALID_ARGUMENT;
+    c->tune_collect(true);
+    int ct = 0, od = 0;
+    const int st = c->last_key.multi < 0 ? 0 : tune_state(c->last_key, &ct, &od);
+    *decided = st;
+    *ctas_per_sm = ct;
+    *order = od;
     return Z2D_OK;
 }
 

@@ -1121,6 +1121,9 @@ struct RasterArgs {
     const RasterFill *rfills;
     const uint8_t *masks;
     int32_t n_jobs;
+    unsigned long long *queue;  // work-queue counter, zero at launch
+    unsigned long long n_items; // tiles x rows
+    const int32_t *order;       // tile order of the queue, or null (tile index order)
 };
 
 // Winding deltas of one warp: up to 4 sample rows x 1024 sample columns,
@@ -1137,25 +1140,23 @@ constexpr uint32_t kBias2 = 0x80008000u;
 // stored at ((c % per) / 2) * 32 + lane, so a warp reading pair k of every
 // lane touches 32 consecutive words.
 
-// One CTA per tile of 4 rows x 256 pixels; warp w owns pixel row w of the
-// tile and lane l its pixels [8l, 8l+8).  Warps never wait for each other:
-// each walks the band's fills in call order, accumulates the winding deltas
-// of its row's 4 (or 1) sample rows from the fill's band edges, prefix-scans
-// them across the warp, turns the inside bits into coverage and composites
-// its 8 pixels, which stay in registers from the first fill to the last.
-// MULTI = false draws a one-surface batch from A.job0, whose fields are
-// kernel parameters (warp-uniform values that need no registers);
-// MULTI = true finds each CTA's job in the job table.
+// One work item is one pixel row of a tile of 4 rows x 256 pixels: lane l
+// owns the row's pixels [8l, 8l+8).  The warp walks the band's fills in call
+// order, accumulates the winding deltas of its row's 4 (or 1) sample rows
+// from the fill's band edges, prefix-scans them across the warp, turns the
+// inside bits into coverage and composites its 8 pixels, which stay in
+// registers from the first fill to the last.  `words` is the warp's own
+// shared-memory scratch.  MULTI = false draws a one-surface batch from
+// A.job0, whose fields are kernel parameters (warp-uniform values that need
+// no registers); MULTI = true finds the tile's job in the job table.
 template <bool MULTI>
-__global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A) {
-    extern __shared__ uint32_t smem[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t *words = smem + warp * kWarpWords;
-    // CTA -> (job, band, tile column): jobs hold consecutive CTA ranges
+__device__ __forceinline__ void raster_row(const RasterArgs &A, const int32_t tile, const int warp, const int lane,
+                                           uint32_t *words) {
+    // tile -> (job, band, tile column): jobs hold consecutive tile ranges
     int32_t jb = 0;
-    if constexpr (MULTI) jb = job_of(A.jobs, A.n_jobs, blockIdx.x, [](const DevJob &J) { return (long long)J.tile_base; });
+    if constexpr (MULTI) jb = job_of(A.jobs, A.n_jobs, tile, [](const DevJob &J) { return (long long)J.tile_base; });
     const DevJob &JB = MULTI ? A.jobs[jb] : A.job0;
-    const int32_t local = blockIdx.x - JB.tile_base, ncols = JB.tcol_hi - JB.tcol_lo + 1;
+    const int32_t local = tile - JB.tile_base, ncols = JB.tcol_hi - JB.tcol_lo + 1;
     const int32_t lb = local / ncols;
     const int32_t b = JB.band_lo + lb;
     const int32_t cnt = A.band_count[JB.gband_base + lb];
@@ -1463,6 +1464,44 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
 #pragma unroll
     for (int q = 0; q < 8; q++)
         if ((touched >> q) & 1u) store_raw(dst, (size_t)W * y + px0 + q, raw[q]);
+}
+
+// Work estimate of each raster tile for the cost-ordered queue: the number
+// of fills in its band's list (every one is visited by the tile's rows).
+__global__ void k_tile_cost(const DevJob *__restrict__ jobs, int32_t n_jobs, const int32_t *__restrict__ band_count,
+                            int32_t n_tiles, int32_t *__restrict__ cost, int32_t *__restrict__ idx) {
+    const int32_t t = (int32_t)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (t >= n_tiles) return;
+    const int32_t j = job_of(jobs, n_jobs, t, [](const DevJob &J) { return (long long)J.tile_base; });
+    const DevJob J = jobs[j];
+    const int32_t ncols = J.tcol_hi - J.tcol_lo + 1;
+    cost[t] = band_count[J.gband_base + (t - J.tile_base) / ncols];
+    idx[t] = t;
+}
+
+// Persistent rasteriser: a grid of resident CTAs whose warps take (tile,
+// row) items from a device work queue (one 64-bit counter) until it is
+// empty.  Items are numbered tile * 4 + row, tiles job after job (or in the
+// order of A.order, when given), so the four rows of a tile are taken
+// together and share their band's lists in cache.  A warp that finishes a
+// cheap row takes the next item at once: the work of bands with many fills
+// spreads over all warps instead of holding a CTA slot until its slowest
+// warp is done.
+template <bool MULTI>
+__global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A) {
+    extern __shared__ uint32_t smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t *words = smem + warp * kWarpWords;
+    for (;;) {
+        unsigned long long item = 0;
+        if (lane == 0) item = atomicAdd(A.queue, 1ull);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= A.n_items) break;
+        const long long t = (long long)(item / kTileRows);
+        const int32_t tile = A.order ? A.order[t] : (int32_t)t;
+        __syncwarp();  // the previous item's reads of `words` are done before it is reset
+        raster_row<MULTI>(A, tile, (int)(item % kTileRows), lane, words);
+    }
 }
 
 // The fill owning each node: warp f writes f over fill f's node range (the
@@ -1834,10 +1873,66 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
         const int rc = c.await_surface();  // a host surface's upload
         if (rc) return rc;
     }
+    // persistent grid: every SM filled to the kernel's residency (or the
+    // tuned CTAs per SM), never more CTAs than tiles
+    static std::atomic<int> occ_cache[2];
+    int occ = occ_cache[n_jobs == 1 ? 0 : 1].load(std::memory_order_relaxed);
+    if (occ <= 0) {
+        if (n_jobs == 1) Z2D_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_raster<false>, kRasterThreads, smem));
+        else Z2D_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_raster<true>, kRasterThreads, smem));
+        occ = std::max(occ, 1);
+        occ_cache[n_jobs == 1 ? 0 : 1].store(occ, std::memory_order_relaxed);
+    }
+    // the schedule: forced on the context, or the tuner's for this kind of pass
+    const TuneKey key = tune_key(n_jobs, n_tiles, n_slots, n_gbands);
+    c.last_key = key;
+    RasterPlan plan{c.raster_ctas_per_sm, c.raster_order, -1};
+    if (!c.raster_forced) {
+        c.tune_collect(false);
+        plan = tune_pick(key);
+    }
+    cudaEvent_t tune_t0 = nullptr, tune_t1 = nullptr;
+    if (plan.candidate >= 0) {
+        if (cudaEventCreate(&tune_t0) != cudaSuccess || cudaEventCreate(&tune_t1) != cudaSuccess) {
+            if (tune_t0) cudaEventDestroy(tune_t0);
+            tune_t0 = tune_t1 = nullptr;
+            plan.candidate = -1;
+        } else {
+            Z2D_CUDA(cudaEventRecord(tune_t0, c.stream));
+        }
+    }
+    const int per_sm = plan.ctas > 0 ? std::min(plan.ctas, occ) : occ;
+    const unsigned grid = (unsigned)std::min<long long>(n_tiles, (long long)c.sm_count * per_sm);
+    A.queue = reinterpret_cast<unsigned long long *>(d_cnt + CNT_QUEUE);
+    A.n_items = (unsigned long long)n_tiles * kTileRows;
+    A.order = nullptr;
+    if (plan.order == 1 && n_tiles > 1) {
+        // longest bands first: tiles sorted by their band's fill count
+        const size_t nt = (size_t)n_tiles;
+        size_t sort_bytes = 0;
+        cub::DeviceRadixSort::SortPairsDescending(nullptr, sort_bytes, (const int32_t *)nullptr, (int32_t *)nullptr,
+                                                  (const int32_t *)nullptr, (int32_t *)nullptr, (int)nt, 0, 32,
+                                                  c.stream);
+        const size_t arr = (sizeof(int32_t) * nt + 255) & ~(size_t)255;
+        if (c.tile_order.ensure(4 * arr + sort_bytes)) return Z2D_ERR_OUT_OF_MEMORY;
+        uint8_t *b = c.tile_order.as<uint8_t>();
+        int32_t *cost = reinterpret_cast<int32_t *>(b), *idx = reinterpret_cast<int32_t *>(b + arr);
+        int32_t *cost_s = reinterpret_cast<int32_t *>(b + 2 * arr), *order = reinterpret_cast<int32_t *>(b + 3 * arr);
+        k_tile_cost<<<grid_for((long long)nt, 256), 256, 0, c.stream>>>(d_jobs, n_jobs, d_band_count, (int32_t)nt, cost,
+                                                                         idx);
+        Z2D_CUDA(cub::DeviceRadixSort::SortPairsDescending(b + 4 * arr, sort_bytes, cost, cost_s, idx, order, (int)nt,
+                                                           0, 32, c.stream));
+        c.launches += 2;
+        A.order = order;
+    }
     cudaEvent_t t0 = c.timer_begin(c.t_raster);
-    if (n_jobs == 1) k_raster<false><<<(unsigned)n_tiles, kRasterThreads, smem, c.stream>>>(A);
-    else k_raster<true><<<(unsigned)n_tiles, kRasterThreads, smem, c.stream>>>(A);
+    if (n_jobs == 1) k_raster<false><<<grid, kRasterThreads, smem, c.stream>>>(A);
+    else k_raster<true><<<grid, kRasterThreads, smem, c.stream>>>(A);
     c.timer_end(c.t_raster, t0);
+    if (plan.candidate >= 0) {
+        Z2D_CUDA(cudaEventRecord(tune_t1, c.stream));
+        c.tune_pending.push_back(TunePending{key, plan.candidate, tune_t0, tune_t1});
+    }
     c.launches++;
     Z2D_CUDA(cudaGetLastError());
     return Z2D_OK;

@@ -138,7 +138,8 @@ enum : int32_t {
     CNT_CURVES = 6,       // curves queued by k_node_count_w
     CNT_CURVES_EMIT = 7,  // curves queued by k_node_emit_w
     CNT_POOL = 8,         // points asked of the curve pool (64-bit pair, + 9)
-    CNT_COUNT = 10
+    CNT_QUEUE = 10,       // k_raster's work-queue counter (64-bit pair, + 11)
+    CNT_COUNT = 12
 };
 
 // action-mask byte of the exact path: bit 7 = clear first, bits 0-4 = coverage

@@ -44,6 +44,31 @@ struct HostBuf {
     T *as() const { return reinterpret_cast<T *>(ptr); }
 };
 
+// The rasteriser's schedule tuner (tune.cu): a pass is keyed by whether it
+// draws one surface or many, log2 of its tiles and log2 of the mean fills
+// per band list.
+struct TuneKey {
+    int multi, tiles, load;
+    bool operator<(const TuneKey &o) const {
+        return multi != o.multi ? multi < o.multi : tiles != o.tiles ? tiles < o.tiles : load < o.load;
+    }
+};
+struct RasterPlan {
+    int ctas;       // resident CTAs per SM, 0 = as many as fit
+    int order;      // 0 tile order, 1 longest bands first
+    int candidate;  // the tuner's candidate being measured, or -1
+};
+struct TunePending {
+    TuneKey key;
+    int candidate;
+    cudaEvent_t start, stop;
+};
+TuneKey tune_key(int32_t n_jobs, long long n_tiles, long long n_slots, long long n_gbands);
+RasterPlan tune_pick(const TuneKey &k);
+void tune_report(const TuneKey &k, int candidate, float ms);
+// 1: decided (ctas, order set), 0: still exploring, -1: tuning off
+int tune_state(const TuneKey &k, int *ctas, int *order);
+
 struct Ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -70,6 +95,16 @@ struct Ctx {
     DevBuf stroke_c;    // device stroker: contour points
     DevBuf curve_pool;  // leaf points of flattened curves (count pass -> emit pass)
     long long pool_demand = 0;  // curve-pool points the last flatten asked for
+    // k_raster's schedule when forced by z2dgpu_ctx_set_raster (otherwise the
+    // tuner's): resident CTAs per SM (0: as many as fit) and queue order (0
+    // tile order, 1 longest bands first)
+    bool raster_forced = false;
+    int raster_ctas_per_sm = 0;
+    int raster_order = 0;
+    std::vector<TunePending> tune_pending;  // tuner measurements not yet read
+    TuneKey last_key{-1, 0, 0};             // key of the last pass
+    void tune_collect(bool wait);
+    DevBuf tile_order;          // cost-ordered queue: keys, indices, sorted copies, sort scratch
     // dashed strokes' polygons of z2dgpu_draw_jobs, kept with their
     // capacity across calls (building them then touches no fresh pages)
     std::vector<stroke::Polygon> poly_cache;
