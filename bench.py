@@ -547,12 +547,13 @@ def jobs_arm(ctx, stream, dev, steps=3):
     del buf, pristine, surfaces
     # CPU restatement on all host threads, one job per thread: every job,
     # drawn from its seeded background, is compared with the GPU's pass
-    from oracle import load_oracle
+    from oracle import Oracle, load_oracle
     from concurrent.futures import ThreadPoolExecutor
     import ctypes as C
     from z2d_gb300 import abi as A
     from z2d_gb300.types import nodes_to_abi
     lib = load_oracle()
+    orc = Oracle()
 
     def prepare(j):
         w, h = jobs[j][0], jobs[j][1]
@@ -566,7 +567,7 @@ def jobs_arm(ctx, stream, dev, steps=3):
                 keep += [fo, arr]
                 calls.append(("fill", C.byref(p), arr, len(nd), C.byref(fo)))
             else:
-                contours, _ = painter.stroke_contours(nd, o, "rgba")
+                contours, _ = orc.stroke_contours(nd, o, "rgba")
                 pts = np.ascontiguousarray(np.concatenate(contours) if contours else np.zeros((1, 2)))
                 ends = (np.cumsum([len(c_) for c_ in contours]) if contours else np.zeros(1)).astype(np.uint64)
                 fo = A.z2d_fill_opts(anti_aliasing=A.AA_DEFAULT, fill_rule=A.FILL_NON_ZERO, op=A.OP["src_over"],
@@ -606,12 +607,12 @@ def jobs_arm(ctx, stream, dev, steps=3):
             nf += sum(cmd_cnt[j] for j in chunk)
     out["cpu"] = {"value": sum(jobs[j][0] * jobs[j][1] for j in range(k)) / 1e6 / cpu_s, "jobs": k, "commands": nf,
                   "cores": nt, "seconds": cpu_s, "kind": "port",
-                  "note": "every job; stroke polygons built on the host beforehand (not timed), fills and polygons "
-                          "rasterised"}
+                  "note": "every job; stroke polygons built beforehand by the oracle's stroker (not timed), fills "
+                          "and polygons rasterised"}
     out["parity"] = {"jobs_checked": k, "differing_jobs": len(bad_jobs), "differing_pixels": bad_px,
                      "first_differing": bad_jobs[:8],
-                     "reference": "oracle on host threads, every job from its seeded background; stroked paths "
-                                  "rasterised from the host stroke builder's polygons"}
+                     "reference": "oracle on host threads, every job from its seeded background; strokes "
+                                  "tessellated by the oracle's own stroker"}
     return out
 
 

@@ -279,15 +279,17 @@ Z2D_API int z2dgpu_ctx_set_timing(z2dgpu_ctx *ctx, int enable);
  * first passes of each kind, and caches its choices in raster_tune.json
  * beside the library (Z2D_TUNE_FILE overrides the path; Z2D_TUNE=off keeps
  * the default schedule).  ctas_per_sm >= 0 forces a schedule: resident CTAs
- * per SM (0 = as many as fit) and queue order (0 = tile order, 1 = tiles of
- * the bands with the most fills first); ctas_per_sm = -1 returns to the
+ * per SM (0 = as many as fit), queue order (0 = tile order, 1 = tiles of
+ * the bands with the most fills first) and queue item (1 = a whole 4-row
+ * tile per CTA, 0 = one tile row per warp); ctas_per_sm = -1 returns to the
  * tuner.  Every schedule draws the same pixels. */
-Z2D_API int z2dgpu_ctx_set_raster(z2dgpu_ctx *ctx, int32_t ctas_per_sm, int32_t order);
+Z2D_API int z2dgpu_ctx_set_raster(z2dgpu_ctx *ctx, int32_t ctas_per_sm, int32_t order,
+                                  int32_t tile_items);
 /* The tuner's state for the kind of pass this context drew last: *decided =
  * 1 with its schedule, 0 while candidates are still being timed, -1 when
  * tuning is off. */
 Z2D_API int z2dgpu_ctx_raster_tuning(z2dgpu_ctx *ctx, int32_t *decided, int32_t *ctas_per_sm,
-                                     int32_t *order);
+                                     int32_t *order, int32_t *tile_items);
 /* Accumulated milliseconds and launch count of a stage since timing was
  * enabled: "raster" (k_raster), "composite" (compositor kernels), "flatten"
  * (path flattening, stroking and fill setup, two intervals per fill call),

@@ -18,9 +18,10 @@ from z2d_gb300.types import FillOptions, Operation, Pattern, nodes_to_abi
 
 HERE = pathlib.Path(__file__).resolve().parent
 SRC = HERE / "z2d_oracle.cpp"
+SRC_STROKE = HERE / "z2d_stroke.cpp"
 BUILD = HERE / "_build"
 LIB = BUILD / "libz2doracle.so"
-DEPS = [SRC, HERE.parent / "include" / "z2dgpu.h", HERE.parent / "z2d_gb300" / "csrc" / "blue_noise_64x64.inc"]
+DEPS = [SRC, SRC_STROKE, HERE.parent / "include" / "z2dgpu.h", HERE.parent / "z2d_gb300" / "csrc" / "blue_noise_64x64.inc"]
 CXXFLAGS = ["-std=c++17", "-O3", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared"]
 
 _lock = threading.Lock()
@@ -33,7 +34,7 @@ def build_oracle(force: bool = False) -> pathlib.Path:
     if not force and LIB.exists() and all(LIB.stat().st_mtime >= d.stat().st_mtime for d in DEPS):
         return LIB
     tmp = BUILD / f"libz2doracle.{os.getpid()}.so"
-    cmd = ["g++", *CXXFLAGS, "-o", str(tmp), str(SRC)]
+    cmd = ["g++", *CXXFLAGS, "-o", str(tmp), str(SRC), str(SRC_STROKE)]
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB)
     return LIB
@@ -65,6 +66,12 @@ def load_oracle():
             lib.z2doracle_run_pixel.restype = abi.z2d_pixel
             lib.z2doracle_pixel_from_color.argtypes = [abi.z2d_color]
             lib.z2doracle_pixel_from_color.restype = abi.z2d_pixel
+            lib.z2doracle_stroke_contours.argtypes = [C.POINTER(abi.z2d_node), C.c_size_t,
+                                                      C.POINTER(abi.z2d_stroke_opts), C.c_int32,
+                                                      C.POINTER(C.c_double), C.c_size_t, C.POINTER(C.c_uint64),
+                                                      C.POINTER(C.c_uint64), C.c_size_t, C.POINTER(C.c_uint64),
+                                                      C.POINTER(C.c_double)]
+            lib.z2doracle_stroke_contours.restype = C.c_int
             lib.z2doracle_pow_f32.argtypes = [C.c_float, C.c_float]
             lib.z2doracle_pow_f32.restype = C.c_float
             lib.z2doracle_atan2.argtypes = [C.c_double, C.c_double]
@@ -167,6 +174,35 @@ class Oracle:
 
     def pixel_from_color(self, color):
         return self.lib.z2doracle_pixel_from_color(color.to_abi())
+
+    def stroke_contours(self, nodes, opts, surface_format="rgba"):
+        """The oracle's own stroke tessellation (z2d_stroke.cpp): the closed
+        contours painter.stroke would rasterise on a surface of
+        `surface_format` (hairlines: the open polylines), as a list of
+        (n, 2) arrays of already-scaled points, and the rasteriser scale.
+        Raises Z2DError with z2d's error on failure."""
+        import numpy as np
+        from z2d_gb300.native import Z2DError
+        from z2d_gb300.types import _fmt
+        keep: list = []
+        arr = nodes_to_abi(nodes)
+        o = opts.to_abi(keep)
+        fmt = _fmt(surface_format)
+        npts, nc, sc = C.c_uint64(), C.c_uint64(), C.c_double()
+        rc = self.lib.z2doracle_stroke_contours(arr, len(nodes), C.byref(o), fmt, None, 0, C.byref(npts), None, 0,
+                                                C.byref(nc), C.byref(sc))
+        if rc:
+            raise Z2DError(rc, "oracle stroke")
+        pts = np.zeros(max(1, npts.value) * 2, np.float64)
+        ends = np.zeros(max(1, nc.value), np.uint64)
+        self.lib.z2doracle_stroke_contours(arr, len(nodes), C.byref(o), fmt, pts.ctypes.data_as(C.POINTER(C.c_double)),
+                                           npts.value, C.byref(npts), ends.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                           nc.value, C.byref(nc), C.byref(sc))
+        out, start = [], 0
+        for e in ends[:nc.value]:
+            out.append(pts[2 * start:2 * int(e)].reshape(-1, 2).copy())
+            start = int(e)
+        return out, sc.value
 
     def pow_f32(self, x: float, y: float) -> float:
         """std.math.pow(f32, x, y) as z2d computes it."""

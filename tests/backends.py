@@ -37,9 +37,11 @@ class GpuBackend:
 
 
 class StrokeOracle:
-    """The oracle with painter.stroke: z2d's stroke polygon comes from the
-    library's host-side stroke builder (z2dgpu_stroke_contours, pinned to
-    z2d by the stroke scenes' golden PNGs) and is rasterised by the oracle."""
+    """The oracle with painter.stroke: the stroke polygon (or hairline
+    polylines) comes from the oracle's own restatement of z2d's stroke
+    tessellation (oracle/z2d_stroke.cpp, pinned to z2d by the stroke scenes'
+    golden PNGs) and is rasterised by the oracle; nothing of the library
+    takes part."""
 
     def __init__(self, oracle):
         self.oracle = oracle
@@ -51,10 +53,9 @@ class StrokeOracle:
         return self.oracle.composite(dst, x, y, ops, precision)
 
     def stroke(self, surface, pattern, nodes, opts):
-        from z2d_gb300 import painter
         from z2d_gb300.types import FillOptions
         try:
-            contours, _ = painter.stroke_contours(nodes, opts, surface.format)
+            contours, _ = self.oracle.stroke_contours(nodes, opts, surface.format)
         except Z2DError as e:
             return e.code
         if opts.hairline:  # polylines of polyline_plotter, drawn by the hairline rasteriser

@@ -15,7 +15,7 @@ from z2d_gb300.workloads import premultiplied_background, random_fills
 
 pytestmark = pytest.mark.gpu
 
-SCHEDULES = [(0, 0), (0, 1), (4, 0), (4, 1), (2, 1), (1, 0)]
+SCHEDULES = [(0, 0, 1), (0, 1, 1), (0, 0, 0), (0, 1, 0), (4, 1, 1), (2, 1, 0), (1, 0, 1)]
 
 
 def _bg(w, h, seed):
@@ -34,11 +34,11 @@ def one_surface(oracle):
     return w, h, fills, ref.numpy()
 
 
-@pytest.mark.parametrize("ctas,order", SCHEDULES)
-def test_schedule_one_surface(one_surface, ctas, order):
+@pytest.mark.parametrize("ctas,order,tile_items", SCHEDULES)
+def test_schedule_one_surface(one_surface, ctas, order, tile_items):
     w, h, fills, ref = one_surface
     ctx = Context(0)
-    ctx.set_raster(ctas, order)
+    ctx.set_raster(ctas, order, tile_items)
     s = _bg(w, h, 3)
     painter.fill_batch(s, fills, ctx=ctx)
     got = s.numpy()
@@ -46,8 +46,8 @@ def test_schedule_one_surface(one_surface, ctas, order):
     ctx.close()
 
 
-@pytest.mark.parametrize("ctas,order", SCHEDULES)
-def test_schedule_many_surfaces(oracle, ctas, order):
+@pytest.mark.parametrize("ctas,order,tile_items", SCHEDULES)
+def test_schedule_many_surfaces(oracle, ctas, order, tile_items):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(8)
     specs = []
@@ -56,7 +56,7 @@ def test_schedule_many_surfaces(oracle, ctas, order):
         specs.append((w, h, random_fills(seed=500 + j, n=int(rng.integers(1, 20)), w=w, h=h, side_lo=4,
                                          side_hi=min(w, h), seg_lo=3, seg_hi=20)))
     ctx = Context(0)
-    ctx.set_raster(ctas, order)
+    ctx.set_raster(ctas, order, tile_items)
     dev = [_bg(w, h, 60 + j).to_device("cuda") for j, (w, h, _) in enumerate(specs)]
     painter.fill_jobs([(d, f) for d, (_, _, f) in zip(dev, specs)], ctx=ctx)
     torch.cuda.synchronize()
@@ -89,7 +89,7 @@ def test_autotuner_decides_and_caches(one_surface):
     path = os.environ.get("Z2D_TUNE_FILE")
     if path and os.path.exists(path):
         lines = [json.loads(x) for x in open(path) if x.strip()]
-        assert lines and all({"multi", "tiles", "load", "ctas", "order", "ms"} <= set(d) for d in lines)
+        assert lines and all({"multi", "tiles", "load", "ctas", "order", "cta_items", "ms"} <= set(d) for d in lines)
 
 
 def test_set_raster_rejects():
@@ -97,6 +97,8 @@ def test_set_raster_rejects():
     ctx = Context(0)
     with pytest.raises(Z2DError):
         ctx.set_raster(4, 2)
+    with pytest.raises(Z2DError):
+        ctx.set_raster(4, 0, 2)
     with pytest.raises(Z2DError):
         ctx.set_raster(-2, 0)
     ctx.set_raster(-1, 0)  # back to the tuner

@@ -29,8 +29,8 @@ def test_fill_scene_matches_golden(oracle, golden_dir, name, aa):
 @pytest.mark.parametrize("aa", list(AA_SUFFIX))
 @pytest.mark.parametrize("name", list(STROKE_SCENES))
 def test_stroke_scene_matches_golden(oracle, golden_dir, name, aa):
-    """Pins the host stroke builder (z2dgpu_stroke_contours) to z2d: its
-    polygons, rasterised by the oracle, reproduce the golden PNGs."""
+    """Pins the oracle's own stroke tessellation (oracle/z2d_stroke.cpp) to
+    z2d: its polygons, rasterised by the oracle, reproduce the golden PNGs."""
     path = os.path.join(golden_dir, name + AA_SUFFIX[aa] + ".png")
     if not os.path.exists(path):
         path = os.path.join(golden_dir, name + "_smooth.png")
@@ -130,3 +130,39 @@ def test_atan2_accuracy(oracle):
         got = oracle.atan2(float(y), float(x))
         ref = np.arctan2(y, x)
         assert abs(got - ref) <= np.spacing(abs(ref)) + 1e-300
+
+
+def _random_strokes(n, seed):
+    from z2d_gb300.types import StrokeOptions
+    from z2d_gb300.workloads import random_path
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        nodes = random_path(rng, 300, 200, 10, 250, 3, 20)
+        dashed = i % 3 == 0
+        tf = (1.0, 0.0, 0.0, 1.0, 0.0, 0.0) if i % 4 else (1.5, 0.3, -0.2, 0.8, 4.0, -3.0)
+        so = StrokeOptions(line_width=float(rng.uniform(0.5, 20)), line_join=("miter", "round", "bevel")[i % 3],
+                           line_cap=("butt", "round", "square")[(i // 3) % 3],
+                           dashes=tuple(rng.uniform(0, 40, int(rng.integers(2, 7)))) if dashed else (),
+                           dash_offset=float(rng.uniform(-20, 20)) if dashed else 0.0, hairline=(i % 17 == 0),
+                           transformation=tf, tolerance=float(rng.choice([0.05, 0.1, 0.5])))
+        out.append((nodes, so))
+    return out
+
+
+def test_host_stroke_builder_matches_oracle_stroker(oracle):
+    """The library's host stroke builder (z2dgpu_stroke_contours, which
+    builds dashed strokes for z2dgpu_draw_jobs) and the oracle's independent
+    restatement produce bit-identical polygons on random solid and dashed
+    strokes of every join and cap, through plain and skewed transformations,
+    and identical hairline polylines (the dasher's empty polylines, which
+    draw nothing, aside)."""
+    from z2d_gb300 import painter
+    for i, (nodes, so) in enumerate(_random_strokes(300, 21)):
+        a, sa = painter.stroke_contours(nodes, so, "rgba")
+        b, sb = oracle.stroke_contours(nodes, so, "rgba")
+        if so.hairline:
+            b = [c for c in b if len(c)]
+        assert sa == sb and len(a) == len(b), f"stroke {i}: {len(a)} vs {len(b)} contours"
+        for k, (x, y) in enumerate(zip(a, b)):
+            assert x.shape == y.shape and np.array_equal(x, y), f"stroke {i} contour {k}"

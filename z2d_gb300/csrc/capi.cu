@@ -1400,23 +1400,27 @@ Z2D_API int z2dgpu_ctx_set_timing(z2dgpu_ctx *c, int enable) {
     return Z2D_OK;
 }
 
-Z2D_API int z2dgpu_ctx_set_raster(z2dgpu_ctx *c, int32_t ctas_per_sm, int32_t order) {
-    if (!c || ctas_per_sm < -1 || ctas_per_sm > 64 || (ctas_per_sm >= 0 && (order < 0 || order > 1)))
+Z2D_API int z2dgpu_ctx_set_raster(z2dgpu_ctx *c, int32_t ctas_per_sm, int32_t order, int32_t tile_items) {
+    if (!c || ctas_per_sm < -1 || ctas_per_sm > 64 ||
+        (ctas_per_sm >= 0 && (order < 0 || order > 1 || tile_items < 0 || tile_items > 1)))
         return Z2D_ERR_INVALID_ARGUMENT;
     c->raster_forced = ctas_per_sm >= 0;
     c->raster_ctas_per_sm = ctas_per_sm >= 0 ? ctas_per_sm : 0;
     c->raster_order = ctas_per_sm >= 0 ? order : 0;
+    c->raster_cta_items = ctas_per_sm >= 0 ? tile_items : 1;
     return Z2D_OK;
 }
 
-Z2D_API int z2dgpu_ctx_raster_tuning(z2dgpu_ctx *c, int32_t *decided, int32_t *ctas_per_sm, int32_t *order) {
-    if (!c || !decided || !ctas_per_sm || !order) return Z2D_ERR_INVALID_ARGUMENT;
+Z2D_API int z2dgpu_ctx_raster_tuning(z2dgpu_ctx *c, int32_t *decided, int32_t *ctas_per_sm, int32_t *order,
+                                     int32_t *tile_items) {
+    if (!c || !decided || !ctas_per_sm || !order || !tile_items) return Z2D_ERR_INVALID_ARGUMENT;
     c->tune_collect(true);
-    int ct = 0, od = 0;
-    const int st = c->last_key.multi < 0 ? 0 : tune_state(c->last_key, &ct, &od);
+    int ct = 0, od = 0, it = 1;
+    const int st = c->last_key.multi < 0 ? 0 : tune_state(c->last_key, &ct, &od, &it);
     *decided = st;
     *ctas_per_sm = ct;
     *order = od;
+    *tile_items = it;
     return Z2D_OK;
 }
 

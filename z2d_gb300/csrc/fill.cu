@@ -1122,7 +1122,7 @@ struct RasterArgs {
     const uint8_t *masks;
     int32_t n_jobs;
     unsigned long long *queue;  // work-queue counter, zero at launch
-    unsigned long long n_items; // tiles x rows
+    unsigned long long n_items; // tiles (CTA items) or tiles x rows (warp items)
     const int32_t *order;       // tile order of the queue, or null (tile index order)
 };
 
@@ -1479,28 +1479,43 @@ __global__ void k_tile_cost(const DevJob *__restrict__ jobs, int32_t n_jobs, con
     idx[t] = t;
 }
 
-// Persistent rasteriser: a grid of resident CTAs whose warps take (tile,
-// row) items from a device work queue (one 64-bit counter) until it is
-// empty.  Items are numbered tile * 4 + row, tiles job after job (or in the
-// order of A.order, when given), so the four rows of a tile are taken
-// together and share their band's lists in cache.  A warp that finishes a
-// cheap row takes the next item at once: the work of bands with many fills
-// spreads over all warps instead of holding a CTA slot until its slowest
-// warp is done.
-template <bool MULTI>
+// Persistent rasteriser: a grid of resident CTAs that take items from a
+// device work queue (one 64-bit counter) until it is empty; tiles are
+// queued job after job, or in the order of A.order when given.
+//  * CTA_ITEMS: an item is a whole tile; the CTA's four warps draw its four
+//    rows and meet at a barrier before the next tile, so the rows share the
+//    band's fill list and edges in the SM's L1.
+//  * otherwise an item is one (tile, row) pair, numbered tile * 4 + row,
+//    taken by a single warp: a warp that finishes a cheap row takes the
+//    next item at once instead of holding its CTA until the slowest warp of
+//    the tile is done.
+template <bool MULTI, bool CTA_ITEMS>
 __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A) {
     extern __shared__ uint32_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t *words = smem + warp * kWarpWords;
-    for (;;) {
-        unsigned long long item = 0;
-        if (lane == 0) item = atomicAdd(A.queue, 1ull);
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= A.n_items) break;
-        const long long t = (long long)(item / kTileRows);
-        const int32_t tile = A.order ? A.order[t] : (int32_t)t;
-        __syncwarp();  // the previous item's reads of `words` are done before it is reset
-        raster_row<MULTI>(A, tile, (int)(item % kTileRows), lane, words);
+    if constexpr (CTA_ITEMS) {
+        __shared__ unsigned long long next_tile;
+        for (;;) {
+            if (threadIdx.x == 0) next_tile = atomicAdd(A.queue, 1ull);
+            __syncthreads();
+            const unsigned long long t = next_tile;
+            __syncthreads();  // every thread has read it before it is replaced
+            if (t >= A.n_items) break;
+            const int32_t tile = A.order ? A.order[t] : (int32_t)t;
+            raster_row<MULTI>(A, tile, warp, lane, words);
+        }
+    } else {
+        for (;;) {
+            unsigned long long item = 0;
+            if (lane == 0) item = atomicAdd(A.queue, 1ull);
+            item = __shfl_sync(0xffffffffu, item, 0);
+            if (item >= A.n_items) break;
+            const long long t = (long long)(item / kTileRows);
+            const int32_t tile = A.order ? A.order[t] : (int32_t)t;
+            __syncwarp();  // the previous item's reads of `words` are done before it is reset
+            raster_row<MULTI>(A, tile, (int)(item % kTileRows), lane, words);
+        }
     }
 }
 
@@ -1863,7 +1878,7 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     static std::atomic<uint64_t> attr_set{0};
     const uint64_t dev_bit = 1ull << (c.device & 63);
     if (!(attr_set.load(std::memory_order_relaxed) & dev_bit)) {
-        for (auto k : {k_raster<false>, k_raster<true>}) {
+        for (auto k : {k_raster<false, false>, k_raster<true, false>, k_raster<false, true>, k_raster<true, true>}) {
             Z2D_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             Z2D_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         }
@@ -1878,15 +1893,15 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     static std::atomic<int> occ_cache[2];
     int occ = occ_cache[n_jobs == 1 ? 0 : 1].load(std::memory_order_relaxed);
     if (occ <= 0) {
-        if (n_jobs == 1) Z2D_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_raster<false>, kRasterThreads, smem));
-        else Z2D_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_raster<true>, kRasterThreads, smem));
+        if (n_jobs == 1) Z2D_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_raster<false, false>, kRasterThreads, smem));
+        else Z2D_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_raster<true, false>, kRasterThreads, smem));
         occ = std::max(occ, 1);
         occ_cache[n_jobs == 1 ? 0 : 1].store(occ, std::memory_order_relaxed);
     }
     // the schedule: forced on the context, or the tuner's for this kind of pass
     const TuneKey key = tune_key(n_jobs, n_tiles, n_slots, n_gbands);
     c.last_key = key;
-    RasterPlan plan{c.raster_ctas_per_sm, c.raster_order, -1};
+    RasterPlan plan{c.raster_ctas_per_sm, c.raster_order, c.raster_cta_items, -1};
     if (!c.raster_forced) {
         c.tune_collect(false);
         plan = tune_pick(key);
@@ -1904,7 +1919,7 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     const int per_sm = plan.ctas > 0 ? std::min(plan.ctas, occ) : occ;
     const unsigned grid = (unsigned)std::min<long long>(n_tiles, (long long)c.sm_count * per_sm);
     A.queue = reinterpret_cast<unsigned long long *>(d_cnt + CNT_QUEUE);
-    A.n_items = (unsigned long long)n_tiles * kTileRows;
+    A.n_items = (unsigned long long)n_tiles * (plan.cta_items ? 1 : kTileRows);
     A.order = nullptr;
     if (plan.order == 1 && n_tiles > 1) {
         // longest bands first: tiles sorted by their band's fill count
@@ -1926,8 +1941,13 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
         A.order = order;
     }
     cudaEvent_t t0 = c.timer_begin(c.t_raster);
-    if (n_jobs == 1) k_raster<false><<<grid, kRasterThreads, smem, c.stream>>>(A);
-    else k_raster<true><<<grid, kRasterThreads, smem, c.stream>>>(A);
+    if (plan.cta_items) {
+        if (n_jobs == 1) k_raster<false, true><<<grid, kRasterThreads, smem, c.stream>>>(A);
+        else k_raster<true, true><<<grid, kRasterThreads, smem, c.stream>>>(A);
+    } else {
+        if (n_jobs == 1) k_raster<false, false><<<grid, kRasterThreads, smem, c.stream>>>(A);
+        else k_raster<true, false><<<grid, kRasterThreads, smem, c.stream>>>(A);
+    }
     c.timer_end(c.t_raster, t0);
     if (plan.candidate >= 0) {
         Z2D_CUDA(cudaEventRecord(tune_t1, c.stream));

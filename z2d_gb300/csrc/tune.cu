@@ -1,13 +1,14 @@
 // tune.cu -- the autotuner of the persistent rasteriser's schedule.
 //
-// k_raster runs as a persistent grid whose warps pull (tile, row) items from
-// a device queue (fill.cu).  Two things shape its schedule: how many CTAs of
-// 4 warps stay resident per SM (more hide latency, fewer leave each warp
-// more L1 and less contention on the shared counters) and the order of the
-// queue (tile order keeps a band's rows together; longest-band-first, an
-// LPT schedule, keeps the slowest items from starting last).  Which is
-// faster depends on the workload: how many tiles a pass has and how many
-// fills a band's list holds.
+// k_raster runs as a persistent grid that pulls work items from a device
+// queue (fill.cu).  Three things shape its schedule: how many CTAs of 4
+// warps stay resident per SM (more hide latency, fewer leave each warp more
+// L1), the size of an item (a whole tile, whose four rows share the band's
+// data in one SM's L1, or a single tile row, which balances better when
+// rows differ in cost) and the order of the queue (tile order, or
+// longest-band-first, an LPT schedule that keeps the slowest items from
+// starting last).  Which is fastest depends on the workload: how many tiles
+// a pass has and how many fills a band's list holds.
 //
 // The tuner keys a pass by (one surface or many, log2 of its tiles, log2 of
 // the mean fills per band list).  The first passes of a new key each run a
@@ -16,8 +17,9 @@
 // are cached in a JSON file (raster_tune.json beside libz2dgpu.so, or the
 // path in Z2D_TUNE_FILE) and loaded on first use, so a later process starts
 // from them.  Z2D_TUNE=off keeps the default schedule (all resident CTAs,
-// tile order).  Every schedule draws the same pixels: tiles are disjoint and
-// each row's fills run in call order whatever the queue order.
+// tile order, a tile per CTA).  Every schedule draws the same pixels: tiles
+// are disjoint and each row's fills run in call order whatever the queue
+// order.
 #include <cuda_runtime.h>
 #include <dlfcn.h>
 
@@ -37,10 +39,10 @@ namespace z2dg {
 namespace {
 
 struct Candidate {
-    int ctas, order;
+    int ctas, order, cta_items;
 };
 // CTAs per SM 0 = as many as fit (6 for k_raster)
-constexpr Candidate kCandidates[] = {{0, 0}, {0, 1}, {4, 0}, {4, 1}, {2, 0}, {2, 1}};
+constexpr Candidate kCandidates[] = {{0, 0, 1}, {0, 1, 1}, {0, 0, 0}, {0, 1, 0}, {4, 0, 1}, {4, 1, 0}, {2, 1, 0}};
 constexpr int kNumCandidates = sizeof(kCandidates) / sizeof(kCandidates[0]);
 
 struct Entry {
@@ -65,7 +67,7 @@ std::string tune_path() {
     return "raster_tune.json";
 }
 
-// {"multi": m, "tiles": t, "load": l, "ctas": c, "order": o, "ms": x} per line
+// {"multi": m, "tiles": t, "load": l, "ctas": c, "order": o, "cta_items": i, "ms": x} per line
 void load_locked() {
     g_loaded = true;
     FILE *f = std::fopen(tune_path().c_str(), "r");
@@ -73,13 +75,16 @@ void load_locked() {
     char line[512];
     while (std::fgets(line, sizeof line, f)) {
         TuneKey k{};
-        int ctas = 0, order = 0;
+        int ctas = 0, order = 0, items = 0;
         double ms = 0;
-        if (std::sscanf(line, " {\"multi\": %d, \"tiles\": %d, \"load\": %d, \"ctas\": %d, \"order\": %d, \"ms\": %lf",
-                        &k.multi, &k.tiles, &k.load, &ctas, &order, &ms) != 6)
+        if (std::sscanf(line,
+                        " {\"multi\": %d, \"tiles\": %d, \"load\": %d, \"ctas\": %d, \"order\": %d, \"cta_items\": %d, "
+                        "\"ms\": %lf",
+                        &k.multi, &k.tiles, &k.load, &ctas, &order, &items, &ms) != 7)
             continue;
         for (int i = 0; i < kNumCandidates; i++)
-            if (kCandidates[i].ctas == ctas && kCandidates[i].order == order) g_table[k].best = i;
+            if (kCandidates[i].ctas == ctas && kCandidates[i].order == order && kCandidates[i].cta_items == items)
+                g_table[k].best = i;
     }
     std::fclose(f);
 }
@@ -94,8 +99,10 @@ void save_locked() {
         const Entry &e = kv.second;
         const Candidate &c = kCandidates[e.best];
         const double ms = e.n[e.best] ? e.ms[e.best] / e.n[e.best] : 0.0;
-        std::fprintf(f, "{\"multi\": %d, \"tiles\": %d, \"load\": %d, \"ctas\": %d, \"order\": %d, \"ms\": %.4f}\n",
-                     kv.first.multi, kv.first.tiles, kv.first.load, c.ctas, c.order, ms);
+        std::fprintf(f,
+                     "{\"multi\": %d, \"tiles\": %d, \"load\": %d, \"ctas\": %d, \"order\": %d, \"cta_items\": %d, "
+                     "\"ms\": %.4f}\n",
+                     kv.first.multi, kv.first.tiles, kv.first.load, c.ctas, c.order, c.cta_items, ms);
     }
     std::fclose(f);
     std::rename(tmp.c_str(), path.c_str());
@@ -122,13 +129,16 @@ TuneKey tune_key(int32_t n_jobs, long long n_tiles, long long n_slots, long long
 
 RasterPlan tune_pick(const TuneKey &k) {
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!mode_locked()) return RasterPlan{0, 0, -1};
+    if (!mode_locked()) return RasterPlan{0, 0, 1, -1};
     if (!g_loaded) load_locked();
     Entry &e = g_table[k];
-    if (e.best >= 0) return RasterPlan{kCandidates[e.best].ctas, kCandidates[e.best].order, -1};
+    const auto plan = [](int i, int cand) {
+        return RasterPlan{kCandidates[i].ctas, kCandidates[i].order, kCandidates[i].cta_items, cand};
+    };
+    if (e.best >= 0) return plan(e.best, -1);
     for (int i = 0; i < kNumCandidates; i++)
-        if (e.n[i] == 0) return RasterPlan{kCandidates[i].ctas, kCandidates[i].order, i};
-    return RasterPlan{0, 0, -1};
+        if (e.n[i] == 0) return plan(i, i);
+    return RasterPlan{0, 0, 1, -1};
 }
 
 void tune_report(const TuneKey &k, int candidate, float ms) {
@@ -147,7 +157,7 @@ void tune_report(const TuneKey &k, int candidate, float ms) {
     save_locked();
 }
 
-int tune_state(const TuneKey &k, int *ctas, int *order) {
+int tune_state(const TuneKey &k, int *ctas, int *order, int *cta_items) {
     std::lock_guard<std::mutex> lk(g_mu);
     if (!mode_locked()) return -1;
     if (!g_loaded) load_locked();
@@ -155,6 +165,7 @@ int tune_state(const TuneKey &k, int *ctas, int *order) {
     if (it == g_table.end() || it->second.best < 0) return 0;
     *ctas = kCandidates[it->second.best].ctas;
     *order = kCandidates[it->second.best].order;
+    *cta_items = kCandidates[it->second.best].cta_items;
     return 1;
 }
 

@@ -56,6 +56,7 @@ struct TuneKey {
 struct RasterPlan {
     int ctas;       // resident CTAs per SM, 0 = as many as fit
     int order;      // 0 tile order, 1 longest bands first
+    int cta_items;  // 1: a queue item is a tile (one CTA), 0: a tile row (one warp)
     int candidate;  // the tuner's candidate being measured, or -1
 };
 struct TunePending {
@@ -67,7 +68,7 @@ TuneKey tune_key(int32_t n_jobs, long long n_tiles, long long n_slots, long long
 RasterPlan tune_pick(const TuneKey &k);
 void tune_report(const TuneKey &k, int candidate, float ms);
 // 1: decided (ctas, order set), 0: still exploring, -1: tuning off
-int tune_state(const TuneKey &k, int *ctas, int *order);
+int tune_state(const TuneKey &k, int *ctas, int *order, int *cta_items);
 
 struct Ctx {
     int device = 0;
@@ -96,11 +97,12 @@ struct Ctx {
     DevBuf curve_pool;  // leaf points of flattened curves (count pass -> emit pass)
     long long pool_demand = 0;  // curve-pool points the last flatten asked for
     // k_raster's schedule when forced by z2dgpu_ctx_set_raster (otherwise the
-    // tuner's): resident CTAs per SM (0: as many as fit) and queue order (0
-    // tile order, 1 longest bands first)
+    // tuner's): resident CTAs per SM (0: as many as fit), queue order (0
+    // tile order, 1 longest bands first) and item size (1 tile, 0 tile row)
     bool raster_forced = false;
     int raster_ctas_per_sm = 0;
     int raster_order = 0;
+    int raster_cta_items = 1;
     std::vector<TunePending> tune_pending;  // tuner measurements not yet read
     TuneKey last_key{-1, 0, 0};             // key of the last pass
     void tune_collect(bool wait);

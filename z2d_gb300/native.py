@@ -60,9 +60,9 @@ def load(build_if_missing: bool = True):
         lib.z2dgpu_ctx_launch_count.restype = C.c_uint64
         lib.z2dgpu_ctx_set_timing.argtypes = [C.c_void_p, C.c_int]
         lib.z2dgpu_ctx_set_timing.restype = C.c_int
-        lib.z2dgpu_ctx_set_raster.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+        lib.z2dgpu_ctx_set_raster.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
         lib.z2dgpu_ctx_set_raster.restype = C.c_int
-        lib.z2dgpu_ctx_raster_tuning.argtypes = [C.c_void_p, P(C.c_int32), P(C.c_int32), P(C.c_int32)]
+        lib.z2dgpu_ctx_raster_tuning.argtypes = [C.c_void_p, P(C.c_int32), P(C.c_int32), P(C.c_int32), P(C.c_int32)]
         lib.z2dgpu_ctx_raster_tuning.restype = C.c_int
         lib.z2dgpu_ctx_kernel_ms.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_uint64)]
         lib.z2dgpu_ctx_kernel_ms.restype = C.c_double
@@ -153,17 +153,18 @@ class Context:
     def set_timing(self, enable: bool) -> None:
         check(self.lib.z2dgpu_ctx_set_timing(self.handle, 1 if enable else 0))
 
-    def set_raster(self, ctas_per_sm: int = -1, order: int = 0) -> None:
+    def set_raster(self, ctas_per_sm: int = -1, order: int = 0, tile_items: int = 1) -> None:
         """Forces the rasteriser's schedule (resident CTAs per SM, 0 = as many
         as fit; queue order 0 = tiles in order, 1 = bands with the most fills
-        first); ctas_per_sm = -1 returns to the autotuner."""
-        check(self.lib.z2dgpu_ctx_set_raster(self.handle, ctas_per_sm, order))
+        first; queue item 1 = a tile per CTA, 0 = a tile row per warp);
+        ctas_per_sm = -1 returns to the autotuner."""
+        check(self.lib.z2dgpu_ctx_set_raster(self.handle, ctas_per_sm, order, tile_items))
 
     def raster_tuning(self) -> dict:
         """The autotuner's state for the last pass drawn on this context."""
-        d, ct, od = C.c_int32(), C.c_int32(), C.c_int32()
-        check(self.lib.z2dgpu_ctx_raster_tuning(self.handle, C.byref(d), C.byref(ct), C.byref(od)))
-        return {"decided": d.value, "ctas_per_sm": ct.value, "order": od.value}
+        d, ct, od, it = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        check(self.lib.z2dgpu_ctx_raster_tuning(self.handle, C.byref(d), C.byref(ct), C.byref(od), C.byref(it)))
+        return {"decided": d.value, "ctas_per_sm": ct.value, "order": od.value, "tile_items": it.value}
 
     def kernel_ms(self, kernel: str):
         n = C.c_uint64()
