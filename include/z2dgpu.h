@@ -27,9 +27,10 @@
  *   ALPHA8 1 B/px
  *   ALPHA4/2/1 packed: pixel i (flat index w*y+x) occupies bits
  *     [i*bits, i*bits+bits) little-endian (LSB first); rows are NOT byte
- *     aligned.  Buffer length ceil(w*h*bits/8); DEVICE buffers of these
- *     formats must be allocated up to the next multiple of 4 bytes (pixels
- *     are updated with 32-bit atomics).
+ *     aligned.  Buffer length ceil(w*h*bits/8), host or device.  (Pixels
+ *     are updated with 32-bit word atomics; a device buffer whose length is
+ *     not a multiple of 4 bytes is drawn on a padded copy and copied back,
+ *     so nothing past its length is touched.)
  *
  * Threading: a context owns one CUDA stream and device scratch; calls on one
  * context must not overlap.  Use one context per host thread.
@@ -278,11 +279,12 @@ Z2D_API int z2dgpu_ctx_set_timing(z2dgpu_ctx *ctx, int enable);
  * number of tiles, the mean fills per band) by timing the candidates on the
  * first passes of each kind, and caches its choices in raster_tune.json
  * beside the library (Z2D_TUNE_FILE overrides the path; Z2D_TUNE=off keeps
- * the default schedule).  ctas_per_sm >= 0 forces a schedule: resident CTAs
- * per SM (0 = as many as fit), queue order (0 = tile order, 1 = tiles of
- * the bands with the most fills first) and queue item (1 = a whole 4-row
- * tile per CTA, 0 = one tile row per warp); ctas_per_sm = -1 returns to the
- * tuner.  Every schedule draws the same pixels. */
+ * the default schedule).  ctas_per_sm >= -1 forces a schedule: the grid
+ * (-1 = one CTA per tile, not persistent; 0 = a persistent grid of as many
+ * resident CTAs as fit; n = n per SM), the queue order (0 = tile order, 1 =
+ * tiles of the bands with the most fills first) and the queue item (1 = a
+ * whole 4-row tile per CTA, 0 = one tile row per warp); ctas_per_sm = -2
+ * returns to the tuner.  Every schedule draws the same pixels. */
 Z2D_API int z2dgpu_ctx_set_raster(z2dgpu_ctx *ctx, int32_t ctas_per_sm, int32_t order,
                                   int32_t tile_items);
 /* The tuner's state for the kind of pass this context drew last: *decided =
@@ -390,7 +392,7 @@ Z2D_API int z2dgpu_composite(z2dgpu_ctx *ctx, z2d_surface *dst, int32_t dst_x,
  * counterpart in z2d.  It takes no context: the work is queued on `stream`
  * (a cudaStream_t; NULL = the default stream) of `device`, and the call
  * returns after launch.  `dst` and every surface param must be in device
- * memory (packed formats padded to a multiple of 4 bytes).  Gradient
+ * memory (packed formats of any length).  Gradient
  * descriptors go to a fixed device array inside the library, so one call
  * takes at most 4 gradient params (pattern gradients and gradient-sourced
  * dithers); more are rejected with Z2D_ERR_INVALID_ARGUMENT.  Each call

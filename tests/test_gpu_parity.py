@@ -196,3 +196,55 @@ def test_errors(gpu):
     no_move = [(abi.LINE_TO, 5, 5, 0, 0, 0, 0), (abi.CLOSE_PATH, 0, 0, 0, 0, 0, 0)]
     assert gpu.fill(s, Pattern.from_pixel(Pixel.rgba(1, 2, 3, 4)), no_move, FillOptions()) == abi.ERR_INVALID_STATE
     assert gpu.fill(s, Pattern.from_pixel(Pixel.rgba(1, 2, 3, 4)), [], FillOptions()) == abi.OK
+
+
+@pytest.mark.parametrize("n_stops", [33, 100, 257])
+@pytest.mark.parametrize("method", ["linear_rgb", "srgb", "hsl"])
+def test_gradient_many_stops(gpu, oracle, n_stops, method):
+    """z2d's stop list has no length limit (src/gradient.zig:183-198): stop
+    lists beyond the 32 held inline travel as tables beside the
+    descriptors, through fills, the compositor and a dither source."""
+    rng = np.random.default_rng(n_stops)
+    g = Gradient.linear(3, 9, 150, 70, method=method)
+    for off in rng.uniform(-0.1, 1.1, n_stops):  # unsorted, some clamped, some repeated
+        c = rng.uniform(0, 1, 4)
+        g.add_stop(float(round(off, 2)), Color.rgb(*map(float, c)))
+    w, h = 160, 80
+    a, b = _bg("rgba", w, h, 12), _bg("rgba", w, h, 12)
+    for i, pat in enumerate((Pattern.from_gradient(g), Pattern.dither("bayer", g, 8))):
+        nodes = random_path(rng, w, h, 30, 150, 3, 12)
+        opts = FillOptions(precision="float" if i else "integer")
+        assert gpu.fill(a, pat, nodes, opts) == abi.OK
+        assert oracle.fill(b, pat, nodes, opts) == abi.OK
+    _cmp(a, b, 0, f"fill {n_stops}")
+    ops = [Operation("src_over", src=Pattern.from_gradient(g))]
+    assert gpu.composite(a, 0, 0, ops) == abi.OK
+    assert oracle.composite(b, 0, 0, ops) == abi.OK
+    _cmp(a, b, 0, f"composite {n_stops}")
+
+
+@pytest.mark.parametrize("rule", ["non_zero", "even_odd"])
+@pytest.mark.parametrize("aa", ["none", "default", "supersample_4x"])
+def test_unbalanced_rows_many_active_edges(gpu, oracle, rule, aa):
+    """Closed two-point subpaths add one edge each and leave rows unbalanced,
+    which z2d draws with its literal sorted-span loop (the GPU's exact path).
+    Here 33 such edges cross the same rows, in pairs at equal x with opposite
+    directions, so more than 24 crossings of a row are sorted and ties must
+    be ordered.  z2d sorts them with std.sort.pdqContext, which is not in the
+    reference tree; the oracle and the GPU both order ties stably, and this
+    pins that they agree on every pixel."""
+    w, h = 200, 100
+    nodes = []
+    for k in range(33):
+        x = 4.0 + 5.5 * (k // 2)
+        y0, y1 = (8.0, 92.0) if k % 2 == 0 else (93.0, 7.0)  # opposite directions at the same x
+        nodes += [(abi.MOVE_TO, x, y0, 0, 0, 0, 0), (abi.LINE_TO, x + 0.25 * (k % 3), y1, 0, 0, 0, 0),
+                  (abi.CLOSE_PATH, 0, 0, 0, 0, 0, 0)]
+    nodes += [(abi.MOVE_TO, 1.0, 50.0, 0, 0, 0, 0), (abi.LINE_TO, 199.0, 50.5, 0, 0, 0, 0), (abi.LINE_TO, 100.0, 99.0, 0, 0, 0, 0),
+              (abi.CLOSE_PATH, 0, 0, 0, 0, 0, 0)]
+    pat = Pattern.from_pixel(Pixel.rgba(40, 90, 140, 230))
+    opts = FillOptions(anti_aliasing=aa, fill_rule=rule)
+    a, b = _bg("rgba", w, h, 13), _bg("rgba", w, h, 13)
+    assert gpu.fill(a, pat, nodes, opts) == abi.OK
+    assert oracle.fill(b, pat, nodes, opts) == abi.OK
+    _cmp(a, b, 0, f"{rule}/{aa}")

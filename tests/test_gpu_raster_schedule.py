@@ -15,7 +15,7 @@ from z2d_gb300.workloads import premultiplied_background, random_fills
 
 pytestmark = pytest.mark.gpu
 
-SCHEDULES = [(0, 0, 1), (0, 1, 1), (0, 0, 0), (0, 1, 0), (4, 1, 1), (2, 1, 0), (1, 0, 1)]
+SCHEDULES = [(-1, 0, 1), (-1, 1, 1), (0, 0, 1), (0, 1, 1), (0, 0, 0), (0, 1, 0), (4, 1, 1), (2, 1, 0), (1, 0, 1)]
 
 
 def _bg(w, h, seed):
@@ -100,6 +100,6 @@ def test_set_raster_rejects():
     with pytest.raises(Z2DError):
         ctx.set_raster(4, 0, 2)
     with pytest.raises(Z2DError):
-        ctx.set_raster(-2, 0)
-    ctx.set_raster(-1, 0)  # back to the tuner
+        ctx.set_raster(-3, 0)
+    ctx.set_raster(-2, 0)  # back to the tuner
     ctx.close()

@@ -115,8 +115,8 @@ void Ctx::timer_collect(Timer &t) {
 // ---------------------------------------------- descriptor preparation
 int make_dev_gradient(const z2d_gradient &g, DevGradient &out) {
     memset(&out, 0, sizeof(out));
-    if (g.n_stops < 0 || g.n_stops > kMaxStops || (g.n_stops > 0 && !g.stops)) {
-        set_errorf("gradient: 0..%d stops supported", kMaxStops);
+    if (g.n_stops < 0 || (g.n_stops > 0 && !g.stops)) {
+        set_error("gradient: bad stop list");
         return Z2D_ERR_INVALID_ARGUMENT;
     }
     if (g.type < Z2D_GRADIENT_LINEAR || g.type > Z2D_GRADIENT_CONIC || g.method < 0 || g.method > Z2D_INTERP_HSL_DECREASING) {
@@ -138,14 +138,17 @@ int make_dev_gradient(const z2d_gradient &g, DevGradient &out) {
         float off;
         int idx;
     };
+    if (g.n_stops > kMaxStops) {
+        out.src = &g;  // the table is built where the descriptors are uploaded (put_ext_stops)
+    }
     S order[kMaxStops];  // stable insertion sort on the stack (no allocation)
-    for (int i = 0; i < g.n_stops; i++) {
+    for (int i = 0; i < g.n_stops && i < kMaxStops && g.n_stops <= kMaxStops; i++) {
         const S v{std::fmax(0.0f, std::fmin(g.stops[i].offset, 1.0f)), i};
         int j = i;
         for (; j > 0 && v.off < order[j - 1].off; j--) order[j] = order[j - 1];
         order[j] = v;
     }
-    for (int i = 0; i < g.n_stops; i++) {
+    for (int i = 0; i < g.n_stops && g.n_stops <= kMaxStops; i++) {
         const z2d_color &col = g.stops[order[i].idx].color;
         out.offsets[i] = order[i].off;
         out.prep[i] = prepare_stop(g.method, col);
@@ -179,6 +182,40 @@ int make_dev_gradient(const z2d_gradient &g, DevGradient &out) {
         out.angle = g.geom[2] < 0.0 ? std::fmod(r + twopi, twopi) : r;
     }
     return Z2D_OK;
+}
+
+size_t ext_stops_bytes(const DevGradient *g, size_t n) {
+    size_t b = 0;
+    for (size_t i = 0; i < n; i++)
+        if (g[i].n_stops > kMaxStops) b += ext_table_bytes(g[i].n_stops);
+    return b;
+}
+
+void put_ext_stops(DevGradient *g, size_t n, uint8_t *host, uint8_t *dev) {
+    size_t off = 0;
+    std::vector<std::pair<float, int>> order;
+    for (size_t i = 0; i < n; i++) {
+        DevGradient &d = g[i];
+        if (d.n_stops <= kMaxStops || !d.src) continue;
+        const z2d_gradient &src = *d.src;
+        // Stop.List.addAssumeCapacity (src/gradient.zig:797-811): clamped
+        // offsets in ascending order, equal offsets in insertion order
+        order.resize((size_t)src.n_stops);
+        for (int k = 0; k < src.n_stops; k++)
+            order[(size_t)k] = {std::fmax(0.0f, std::fmin(src.stops[k].offset, 1.0f)), k};
+        std::stable_sort(order.begin(), order.end(),
+                         [](const std::pair<float, int> &a, const std::pair<float, int> &b) { return a.first < b.first; });
+        const size_t o_off = off, o_prep = off + ((sizeof(float) * (size_t)src.n_stops + 15) & ~(size_t)15);
+        float *ho = reinterpret_cast<float *>(host + o_off);
+        RGBf *hp = reinterpret_cast<RGBf *>(host + o_prep);
+        for (int k = 0; k < src.n_stops; k++) {
+            ho[k] = order[(size_t)k].first;
+            hp[k] = prepare_stop(src.method, src.stops[order[(size_t)k].second].color);
+        }
+        d.ext_off = reinterpret_cast<const float *>(dev + o_off);
+        d.ext_prep = reinterpret_cast<const RGBf *>(dev + o_prep);
+        off += ext_table_bytes(src.n_stops);
+    }
 }
 
 static bool valid_format(int f) { return f >= Z2D_FORMAT_ARGB && f <= Z2D_FORMAT_ALPHA1; }
@@ -361,19 +398,27 @@ static int check_surface(const z2d_surface *s) {
 
 static size_t sfc_bytes(const z2d_surface &s) { return ((size_t)s.width * (size_t)s.height * (size_t)fmt_bits(s.format) + 7) / 8; }
 
-// Device view of a surface; host surfaces are staged through `buf` (sized
-// up to a 4-byte multiple so packed word atomics stay in bounds).
+// A packed device surface whose length is not a whole number of 32-bit
+// words: its word atomics need a padded copy (see PackedPads).
+static bool needs_pad(const z2d_surface &s) {
+    return s.location == Z2D_MEM_DEVICE && fmt_packed(s.format) && sfc_bytes(s) % 4 != 0;
+}
+
+// Device view of a surface; host surfaces, and packed device surfaces of an
+// odd length, are staged through `buf` (sized up to a 16-byte multiple so
+// packed word atomics stay in bounds).
 static int stage_in(Ctx &c, const z2d_surface &s, DevBuf &buf, DevSurface &out) {
     out.fmt = s.format;
     out.w = s.width;
     out.h = s.height;
-    if (s.location == Z2D_MEM_DEVICE) {
+    if (s.location == Z2D_MEM_DEVICE && !needs_pad(s)) {
         out.data = reinterpret_cast<uint8_t *>(s.data);
         return Z2D_OK;
     }
     const size_t bytes = sfc_bytes(s);
     if (buf.ensure(((bytes + 15) & ~(size_t)15) + 16)) return Z2D_ERR_OUT_OF_MEMORY;
-    Z2D_CUDA(cudaMemcpyAsync(buf.ptr, s.data, bytes, cudaMemcpyHostToDevice, c.stream));
+    Z2D_CUDA(cudaMemcpyAsync(buf.ptr, s.data, bytes,
+                             s.location == Z2D_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c.stream));
     out.data = buf.as<uint8_t>();
     return Z2D_OK;
 }
@@ -420,7 +465,11 @@ struct SurfaceUploadGuard {
 };
 
 static int stage_out(Ctx &c, const z2d_surface &s, const DevSurface &d) {
-    if (s.location == Z2D_MEM_DEVICE) return Z2D_OK;
+    if (s.location == Z2D_MEM_DEVICE) {
+        if (needs_pad(s))  // back from the padded copy, in stream order
+            Z2D_CUDA(cudaMemcpyAsync(s.data, d.data, sfc_bytes(s), cudaMemcpyDeviceToDevice, c.stream));
+        return Z2D_OK;
+    }
     {
         const int rc = c.await_surface();
         if (rc) return rc;
@@ -1401,13 +1450,14 @@ Z2D_API int z2dgpu_ctx_set_timing(z2dgpu_ctx *c, int enable) {
 }
 
 Z2D_API int z2dgpu_ctx_set_raster(z2dgpu_ctx *c, int32_t ctas_per_sm, int32_t order, int32_t tile_items) {
-    if (!c || ctas_per_sm < -1 || ctas_per_sm > 64 ||
-        (ctas_per_sm >= 0 && (order < 0 || order > 1 || tile_items < 0 || tile_items > 1)))
+    // ctas_per_sm: -2 = the tuner, -1 = one CTA per tile, 0.. = persistent
+    if (!c || ctas_per_sm < -2 || ctas_per_sm > 64 ||
+        (ctas_per_sm >= -1 && (order < 0 || order > 1 || tile_items < 0 || tile_items > 1)))
         return Z2D_ERR_INVALID_ARGUMENT;
-    c->raster_forced = ctas_per_sm >= 0;
-    c->raster_ctas_per_sm = ctas_per_sm >= 0 ? ctas_per_sm : 0;
-    c->raster_order = ctas_per_sm >= 0 ? order : 0;
-    c->raster_cta_items = ctas_per_sm >= 0 ? tile_items : 1;
+    c->raster_forced = ctas_per_sm >= -1;
+    c->raster_ctas_per_sm = ctas_per_sm >= -1 ? ctas_per_sm : 0;
+    c->raster_order = ctas_per_sm >= -1 ? order : 0;
+    c->raster_cta_items = ctas_per_sm >= -1 ? tile_items : 1;
     return Z2D_OK;
 }
 
@@ -1605,10 +1655,13 @@ Z2D_API int z2dgpu_composite(z2dgpu_ctx *c, z2d_surface *dst, int32_t dst_x, int
         }
     }
     if (!grads.empty()) {
-        const size_t bytes = sizeof(DevGradient) * grads.size();
+        const size_t gbytes = (sizeof(DevGradient) * grads.size() + 255) & ~(size_t)255;
+        const size_t bytes = gbytes + ext_stops_bytes(grads.data(), grads.size());
         if (c->params.ensure(bytes) || c->staging.ensure(bytes)) return Z2D_ERR_OUT_OF_MEMORY;
         Z2D_CUDA(cudaStreamSynchronize(c->stream));
-        memcpy(c->staging.ptr, grads.data(), bytes);
+        memcpy(c->staging.ptr, grads.data(), sizeof(DevGradient) * grads.size());
+        put_ext_stops(c->staging.as<DevGradient>(), grads.size(), c->staging.as<uint8_t>() + gbytes,
+                      c->params.as<uint8_t>() + gbytes);
         Z2D_CUDA(cudaMemcpyAsync(c->params.ptr, c->staging.ptr, bytes, cudaMemcpyHostToDevice, c->stream));
         for (size_t i = 0; i < grad_users.size(); i++) grad_users[i]->grad = c->params.as<DevGradient>() + i;
     }
@@ -1690,6 +1743,10 @@ Z2D_API int z2dgpu_composite_noalloc(int device, void *stream, z2d_surface *dst,
                 DevGradient g;
                 rc = make_dev_src_from_pattern(p.kind, p.pattern, o, needs_grad, g);
                 if (rc) return rc;
+                if (needs_grad && g.n_stops > kMaxStops) {
+                    set_errorf("composite_noalloc: at most %d stops per gradient", kMaxStops);
+                    return Z2D_ERR_INVALID_ARGUMENT;
+                }
                 if (needs_grad) {
                     if (n_grads == kNoAllocGradients) {
                         set_errorf("composite_noalloc: at most %d gradient parameters per call", kNoAllocGradients);

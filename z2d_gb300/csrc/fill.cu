@@ -1124,6 +1124,7 @@ struct RasterArgs {
     unsigned long long *queue;  // work-queue counter, zero at launch
     unsigned long long n_items; // tiles (CTA items) or tiles x rows (warp items)
     const int32_t *order;       // tile order of the queue, or null (tile index order)
+    int32_t one_per_tile;       // not persistent: CTA i draws the i-th tile of the queue
 };
 
 // Winding deltas of one warp: up to 4 sample rows x 1024 sample columns,
@@ -1495,6 +1496,11 @@ __global__ void __launch_bounds__(kRasterThreads, 6) k_raster(const RasterArgs A
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t *words = smem + warp * kWarpWords;
     if constexpr (CTA_ITEMS) {
+        if (A.one_per_tile) {  // a grid of one CTA per tile, dispatched in queue order
+            const int32_t tile = A.order ? A.order[blockIdx.x] : (int32_t)blockIdx.x;
+            raster_row<MULTI>(A, tile, warp, lane, words);
+            return;
+        }
         __shared__ unsigned long long next_tile;
         for (;;) {
             if (threadIdx.x == 0) next_tile = atomicAdd(A.queue, 1ull);
@@ -1545,12 +1551,19 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
         J.gband_base = J.tile_base = 0;
         J.list_base = 0;
     }
+    // packed surfaces of an odd length are drawn on padded copies
+    PackedPads pads;
+    {
+        const int rc = pads.begin(c, jobs.size(), [&](size_t j) -> DevSurface & { return jobs[j].sfc; });
+        if (rc) return rc;
+    }
     // ---- upload: gradients | fills | jobs | counters | strokes | polygons
     // through the pinned staging buffer, then the nodes straight from the
     // caller's memory
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
     const size_t o_grads = 0;
-    const size_t o_fills = al(o_grads + sizeof(DevGradient) * grads.size());
+    const size_t o_ext = al(o_grads + sizeof(DevGradient) * grads.size());  // stop tables of long gradients
+    const size_t o_fills = al(o_ext + ext_stops_bytes(grads.data(), grads.size()));
     const size_t o_jobs = al(o_fills + sizeof(FillCmd) * (size_t)n_fills);
     const size_t o_cnt = al(o_jobs + sizeof(DevJob) * (size_t)n_jobs);
     const bool has_strokes = strokes && !strokes->empty();
@@ -1599,7 +1612,10 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     // (the flatten kernels are done with the nodes at the first readback
     // below, so the caller's array is free again when this call returns)
     Z2D_CUDA(cudaMemcpyAsync(dv + o_nodes, nodes, sizeof(z2d_node) * (size_t)n_nodes, cudaMemcpyHostToDevice, c.stream));
-    if (!grads.empty()) memcpy(h + o_grads, grads.data(), sizeof(DevGradient) * grads.size());
+    if (!grads.empty()) {
+        memcpy(h + o_grads, grads.data(), sizeof(DevGradient) * grads.size());
+        put_ext_stops(reinterpret_cast<DevGradient *>(h + o_grads), grads.size(), h + o_ext, dv + o_ext);
+    }
     memcpy(h + o_fills, fills.data(), sizeof(FillCmd) * (size_t)n_fills);
     memcpy(h + o_jobs, jobs.data(), sizeof(DevJob) * (size_t)n_jobs);
     int32_t *cnt_h = reinterpret_cast<int32_t *>(h + o_cnt);
@@ -1797,7 +1813,7 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
         n_tiles += nb * nc;
         n_slots += nb * (J.fill1 - J.fill0);
     }
-    if (n_gbands == 0) return Z2D_OK;  // nothing is drawn
+    if (n_gbands == 0) return pads.finish(c);  // nothing is drawn
     if (n_tiles > 0x7FFFFFFFll || n_gbands > 0x7FFFFFFFll) {
         set_error("batch too large: more than 2^31 tiles");
         return Z2D_ERR_INVALID_ARGUMENT;
@@ -1916,8 +1932,13 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
             Z2D_CUDA(cudaEventRecord(tune_t0, c.stream));
         }
     }
+    // ctas < 0: one CTA per tile (a tile per item), else a persistent grid
     const int per_sm = plan.ctas > 0 ? std::min(plan.ctas, occ) : occ;
-    const unsigned grid = (unsigned)std::min<long long>(n_tiles, (long long)c.sm_count * per_sm);
+    const bool one_per_tile = plan.ctas < 0;
+    const unsigned grid =
+        one_per_tile ? (unsigned)n_tiles : (unsigned)std::min<long long>(n_tiles, (long long)c.sm_count * per_sm);
+    if (one_per_tile) plan.cta_items = 1;
+    A.one_per_tile = one_per_tile ? 1 : 0;
     A.queue = reinterpret_cast<unsigned long long *>(d_cnt + CNT_QUEUE);
     A.n_items = (unsigned long long)n_tiles * (plan.cta_items ? 1 : kTileRows);
     A.order = nullptr;
@@ -1955,7 +1976,7 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     }
     c.launches++;
     Z2D_CUDA(cudaGetLastError());
-    return Z2D_OK;
+    return pads.finish(c);
 }
 
 }  // namespace z2dg

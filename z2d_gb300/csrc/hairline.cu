@@ -261,17 +261,24 @@ inline unsigned blocks_for(long long n, int threads) { return (unsigned)((n + th
 
 }  // namespace
 
-int run_hairlines(Ctx &c, const std::vector<DevJob> &jobs, std::vector<FillCmd> &fills,
+int run_hairlines(Ctx &c, const std::vector<DevJob> &jobs_in, std::vector<FillCmd> &fills,
                   const std::vector<DevGradient> &grads, const std::vector<int32_t> &grad_of_fill,
                   const HairSet &hs) {
     const size_t n_cmd = hs.lines.size();
     if (n_cmd == 0) return Z2D_OK;
+    // packed surfaces of an odd length are drawn on padded copies
+    std::vector<DevJob> jobs(jobs_in);
+    PackedPads pads;
+    {
+        const int rc = pads.begin(c, jobs.size(), [&](size_t j) -> DevSurface & { return jobs[j].sfc; });
+        if (rc) return rc;
+    }
     long long n_pts = 0, n_lines = 0;
     for (size_t k = 0; k < n_cmd; k++) {
         n_pts += (long long)hs.lines[k]->points();
         n_lines += (long long)hs.lines[k]->ends.size();
     }
-    if (n_pts == 0) return Z2D_OK;
+    if (n_pts == 0) return pads.finish(c);
     if (n_lines > 0x7FFFFFFFll || jobs.size() > 0x7FFFFFFFu) {
         set_error("batch too large");
         return Z2D_ERR_INVALID_ARGUMENT;
@@ -285,7 +292,8 @@ int run_hairlines(Ctx &c, const std::vector<DevJob> &jobs, std::vector<FillCmd> 
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
     const size_t n_fills = fills.size(), n_jobs = jobs.size();
     const size_t o_grads = 0;
-    const size_t o_fills = al(o_grads + sizeof(DevGradient) * grads.size());
+    const size_t o_ext = al(o_grads + sizeof(DevGradient) * grads.size());  // stop tables of long gradients
+    const size_t o_fills = al(o_ext + ext_stops_bytes(grads.data(), grads.size()));
     const size_t o_jobs = al(o_fills + sizeof(FillCmd) * n_fills);
     const size_t o_cf = al(o_jobs + sizeof(DevJob) * n_jobs);
     const size_t o_ca = al(o_cf + sizeof(int32_t) * n_cmd);
@@ -301,7 +309,10 @@ int run_hairlines(Ctx &c, const std::vector<DevJob> &jobs, std::vector<FillCmd> 
     for (size_t i = 0; i < n_fills; i++)
         if (grad_of_fill[i] >= 0) fills[i].src.grad = dgrads + grad_of_fill[i];
     Z2D_CUDA(cudaStreamSynchronize(c.stream));  // the staging buffer is free again
-    if (!grads.empty()) memcpy(h + o_grads, grads.data(), sizeof(DevGradient) * grads.size());
+    if (!grads.empty()) {
+        memcpy(h + o_grads, grads.data(), sizeof(DevGradient) * grads.size());
+        put_ext_stops(reinterpret_cast<DevGradient *>(h + o_grads), grads.size(), h + o_ext, dv + o_ext);
+    }
     memcpy(h + o_fills, fills.data(), sizeof(FillCmd) * n_fills);
     memcpy(h + o_jobs, jobs.data(), sizeof(DevJob) * n_jobs);
     memcpy(h + o_cf, hs.fill.data(), sizeof(int32_t) * n_cmd);
@@ -358,7 +369,7 @@ int run_hairlines(Ctx &c, const std::vector<DevJob> &jobs, std::vector<FillCmd> 
     Z2D_CUDA(cudaStreamSynchronize(c.stream));
     const long long n_ops = rb[0];
     c.launches += 3;
-    if (n_ops <= 0) return Z2D_OK;
+    if (n_ops <= 0) return pads.finish(c);
     if (n_ops > 0x7FFFFFFFll) {
         set_error("batch too large: more than 2^31 hairline pixels");
         return Z2D_ERR_INVALID_ARGUMENT;
@@ -391,7 +402,7 @@ int run_hairlines(Ctx &c, const std::vector<DevJob> &jobs, std::vector<FillCmd> 
     kh_apply<<<blocks_for(n_ops, T), T, 0, c.stream>>>(keys2, seq2, opv, fop, n_ops, invalid, A.fills, A.jobs);
     c.timer_end(c.t_stroke, ts);
     c.launches += 3;
-    return Z2D_OK;
+    return pads.finish(c);
 }
 
 }  // namespace z2dg

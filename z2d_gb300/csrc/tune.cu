@@ -10,16 +10,18 @@
 // starting last).  Which is fastest depends on the workload: how many tiles
 // a pass has and how many fills a band's list holds.
 //
+// The fourth candidate shape is no persistence at all: one CTA per tile, as
+// many CTAs as tiles, in queue order, scheduled by the hardware.
+//
 // The tuner keys a pass by (one surface or many, log2 of its tiles, log2 of
 // the mean fills per band list).  The first passes of a new key each run a
 // different candidate schedule with CUDA events around the raster launch;
 // once every candidate has run, the fastest is kept for the key.  Decisions
 // are cached in a JSON file (raster_tune.json beside libz2dgpu.so, or the
 // path in Z2D_TUNE_FILE) and loaded on first use, so a later process starts
-// from them.  Z2D_TUNE=off keeps the default schedule (all resident CTAs,
-// tile order, a tile per CTA).  Every schedule draws the same pixels: tiles
-// are disjoint and each row's fills run in call order whatever the queue
-// order.
+// from them.  Z2D_TUNE=off keeps the default schedule (one CTA per tile, in
+// tile order).  Every schedule draws the same pixels: tiles are disjoint and
+// each row's fills run in call order whatever the queue order.
 #include <cuda_runtime.h>
 #include <dlfcn.h>
 
@@ -41,8 +43,10 @@ namespace {
 struct Candidate {
     int ctas, order, cta_items;
 };
-// CTAs per SM 0 = as many as fit (6 for k_raster)
-constexpr Candidate kCandidates[] = {{0, 0, 1}, {0, 1, 1}, {0, 0, 0}, {0, 1, 0}, {4, 0, 1}, {4, 1, 0}, {2, 1, 0}};
+// CTAs per SM: -1 = not persistent (one CTA per tile, dispatched in queue
+// order), 0 = as many as fit (6 for k_raster), else that many
+constexpr Candidate kCandidates[] = {{-1, 0, 1}, {-1, 1, 1}, {0, 0, 0}, {0, 1, 0},
+                                     {0, 0, 1}, {0, 1, 1}, {4, 0, 0}, {2, 1, 0}};
 constexpr int kNumCandidates = sizeof(kCandidates) / sizeof(kCandidates[0]);
 
 struct Entry {
@@ -101,8 +105,11 @@ void save_locked() {
         const double ms = e.n[e.best] ? e.ms[e.best] / e.n[e.best] : 0.0;
         std::fprintf(f,
                      "{\"multi\": %d, \"tiles\": %d, \"load\": %d, \"ctas\": %d, \"order\": %d, \"cta_items\": %d, "
-                     "\"ms\": %.4f}\n",
+                     "\"ms\": %.4f, \"candidates_ms\": [",
                      kv.first.multi, kv.first.tiles, kv.first.load, c.ctas, c.order, c.cta_items, ms);
+        for (int i = 0; i < kNumCandidates; i++)  // every candidate's time, for the record (0: not measured here)
+            std::fprintf(f, "%s%.4f", i ? ", " : "", e.n[i] ? e.ms[i] / e.n[i] : 0.0);
+        std::fprintf(f, "]}\n");
     }
     std::fclose(f);
     std::rename(tmp.c_str(), path.c_str());
@@ -129,7 +136,7 @@ TuneKey tune_key(int32_t n_jobs, long long n_tiles, long long n_slots, long long
 
 RasterPlan tune_pick(const TuneKey &k) {
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!mode_locked()) return RasterPlan{0, 0, 1, -1};
+    if (!mode_locked()) return RasterPlan{-1, 0, 1, -1};
     if (!g_loaded) load_locked();
     Entry &e = g_table[k];
     const auto plan = [](int i, int cand) {
@@ -138,7 +145,7 @@ RasterPlan tune_pick(const TuneKey &k) {
     if (e.best >= 0) return plan(e.best, -1);
     for (int i = 0; i < kNumCandidates; i++)
         if (e.n[i] == 0) return plan(i, i);
-    return RasterPlan{0, 0, 1, -1};
+    return RasterPlan{-1, 0, 1, -1};
 }
 
 void tune_report(const TuneKey &k, int candidate, float ms) {

@@ -107,6 +107,7 @@ struct Ctx {
     TuneKey last_key{-1, 0, 0};             // key of the last pass
     void tune_collect(bool wait);
     DevBuf tile_order;          // cost-ordered queue: keys, indices, sorted copies, sort scratch
+    DevBuf pad_buf;             // padded copies of packed surfaces (PackedPads)
     // dashed strokes' polygons of z2dgpu_draw_jobs, kept with their
     // capacity across calls (building them then touches no fresh pages)
     std::vector<stroke::Polygon> poly_cache;
@@ -147,12 +148,76 @@ int png_file(Ctx &c, const DevSurface &s, int profile, std::vector<uint8_t> &png
 struct z2dgpu_ctx : public z2dg::Ctx {};
 
 namespace z2dg {
+// Packed (alpha4 / alpha2 / alpha1) pixels are updated with 32-bit word
+// atomics, which would reach up to 3 bytes past a surface buffer of z2d's
+// exact length (ceil(w * h * bits / 8)).  Such a surface -- packed, its
+// length not a whole number of words, not already in one of the context's
+// padded staging buffers -- is drawn on a padded copy in c.pad_buf: copied
+// in when the guard starts, its own length copied back by finish(), which
+// also points the surface back at the caller's buffer.  An error path that
+// never calls finish() leaves the caller's surface as it was.
+struct PackedPads {
+    struct Entry {
+        uint8_t *orig, *pad;
+        size_t len;
+        DevSurface *sfc;
+    };
+    std::vector<Entry> list;
+    template <class SfcOf>
+    int begin(Ctx &c, size_t n, SfcOf sfc_of) {
+        auto staged = [&](const uint8_t *p) {
+            for (DevBuf *b : {&c.surface, &c.surface2, &c.surface3})
+                if (b->ptr && p >= b->as<uint8_t>() && p < b->as<uint8_t>() + b->cap) return true;
+            return false;
+        };
+        size_t total = 0;
+        for (size_t j = 0; j < n; j++) {
+            DevSurface &s = sfc_of(j);
+            const size_t len = ((size_t)s.w * (size_t)s.h * (size_t)fmt_bits(s.fmt) + 7) / 8;
+            if (!fmt_packed(s.fmt) || len % 4 == 0 || staged(s.data)) continue;
+            list.push_back(Entry{s.data, nullptr, len, &s});
+            total += (len + 255) & ~(size_t)255;
+        }
+        if (list.empty()) return Z2D_OK;
+        if (c.pad_buf.ensure(total)) return Z2D_ERR_OUT_OF_MEMORY;
+        size_t off = 0;
+        for (Entry &e : list) {
+            e.pad = c.pad_buf.as<uint8_t>() + off;
+            const cudaError_t r = cudaMemcpyAsync(e.pad, e.orig, e.len, cudaMemcpyDeviceToDevice, c.stream);
+            if (r != cudaSuccess) return cuda_fail(r, "cudaMemcpyAsync (padded surface)");
+            e.sfc->data = e.pad;
+            off += (e.len + 255) & ~(size_t)255;
+        }
+        return Z2D_OK;
+    }
+    int finish(Ctx &c) {
+        for (const Entry &e : list) {
+            e.sfc->data = e.orig;
+            const cudaError_t r = cudaMemcpyAsync(e.orig, e.pad, e.len, cudaMemcpyDeviceToDevice, c.stream);
+            if (r != cudaSuccess) return cuda_fail(r, "cudaMemcpyAsync (padded surface)");
+        }
+        list.clear();
+        return Z2D_OK;
+    }
+};
+}  // namespace z2dg
+
+namespace z2dg {
 
 // -------------------------------------------------- descriptor conversion
 // Fills `out` for a pattern or compositor param.  Gradients are written to
 // `grad_host` (the caller uploads them and patches DevSrc::grad).
 // Returns Z2D_OK or an error code.
 int make_dev_gradient(const z2d_gradient &g, DevGradient &out);
+// Stop tables of the gradients with more than kMaxStops stops: their size,
+// and put_ext_stops, which writes them at `host` (to be uploaded to `dev`)
+// and points each such gradient of g[0..n) (the copy being uploaded) at its
+// table; the caller's gradient descriptions must still be valid.
+inline size_t ext_table_bytes(int n_stops) {
+    return ((sizeof(float) * (size_t)n_stops + 15) & ~(size_t)15) + sizeof(RGBf) * (size_t)n_stops;
+}
+size_t ext_stops_bytes(const DevGradient *g, size_t n);
+void put_ext_stops(DevGradient *g, size_t n, uint8_t *host, uint8_t *dev);
 int make_dev_src_from_pattern(int param_kind, const z2d_pattern &p, DevSrc &out, bool &needs_grad,
                               DevGradient &grad_out);
 

@@ -509,6 +509,13 @@ struct DevGradient {
     // end - start and 1 / |end - start|^2; lin_zero: zero-length gradient
     double lin_dx, lin_dy, lin_inv;
     int32_t lin_zero, pad_;
+    // Up to kMaxStops stops live inline.  A longer stop list (z2d's grows
+    // without bound, src/gradient.zig:183-198) is a table in device memory
+    // written with the descriptors (ext_off / ext_prep); `src` is the
+    // caller's description it is built from, read on the host only.
+    const float *ext_off;
+    const RGBf *ext_prep;
+    const z2d_gradient *src;
     float offsets[kMaxStops];
     RGBf prep[kMaxStops];
 };
@@ -575,30 +582,31 @@ struct Search {
 Z2D_D Search grad_search(const DevGradient &gr, float offset) {
     const int n = gr.n_stops;
     if (offset < 0.0f || n == 0) return Search{-1, -1, 0.0f};
+    const float *const offsets = n > kMaxStops ? gr.ext_off : gr.offsets;
     const float o = fminf(offset, 1.0f);
     int left = 0, right = n, mid = 0;
     while (left < right) {
         mid = left + (right - left) / 2;
-        if (o >= gr.offsets[mid] && (mid == n - 1 || o <= gr.offsets[mid + 1])) break;
-        if (o < gr.offsets[mid]) {
+        if (o >= offsets[mid] && (mid == n - 1 || o <= offsets[mid + 1])) break;
+        if (o < offsets[mid]) {
             right = mid;
             continue;
         }
-        if (o > gr.offsets[mid]) {
+        if (o > offsets[mid]) {
             left = mid + 1;
             continue;
         }
     }
-    if (mid == n - 1) return Search{mid, mid, o - gr.offsets[mid]};
-    if (mid == 0 && o < gr.offsets[mid]) return Search{mid, mid, o / gr.offsets[mid]};
-    const float st = gr.offsets[mid], en = gr.offsets[mid + 1], rl = en - st;
+    if (mid == n - 1) return Search{mid, mid, o - offsets[mid]};
+    if (mid == 0 && o < offsets[mid]) return Search{mid, mid, o / offsets[mid]};
+    const float st = offsets[mid], en = offsets[mid + 1], rl = en - st;
     return Search{mid, mid + 1, (rl != 0.0f) ? (o - st) / rl : 0.0f};
 }
 // The prepared colour of stop i; i < 0 is the transparent result of an
 // invalid offset, LinearRGB.init(0,0,0,0), which is zero in every space.
 Z2D_D RGBf stop_prep(const DevGradient &gr, int i) {
     if (i < 0) return RGBf{0.f, 0.f, 0.f, 0.f};
-    return gr.prep[i];
+    return gr.n_stops > kMaxStops ? gr.ext_prep[i] : gr.prep[i];
 }
 
 // The first step of the interpolation on a stop's colour (see DevGradient).

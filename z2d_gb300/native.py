@@ -153,11 +153,12 @@ class Context:
     def set_timing(self, enable: bool) -> None:
         check(self.lib.z2dgpu_ctx_set_timing(self.handle, 1 if enable else 0))
 
-    def set_raster(self, ctas_per_sm: int = -1, order: int = 0, tile_items: int = 1) -> None:
-        """Forces the rasteriser's schedule (resident CTAs per SM, 0 = as many
-        as fit; queue order 0 = tiles in order, 1 = bands with the most fills
-        first; queue item 1 = a tile per CTA, 0 = a tile row per warp);
-        ctas_per_sm = -1 returns to the autotuner."""
+    def set_raster(self, ctas_per_sm: int = -2, order: int = 0, tile_items: int = 1) -> None:
+        """Forces the rasteriser's schedule (grid: -1 = one CTA per tile, 0 =
+        persistent with as many resident CTAs as fit, n = n per SM; queue
+        order 0 = tiles in order, 1 = bands with the most fills first; queue
+        item 1 = a tile per CTA, 0 = a tile row per warp); ctas_per_sm = -2
+        returns to the autotuner."""
         check(self.lib.z2dgpu_ctx_set_raster(self.handle, ctas_per_sm, order, tile_items))
 
     def raster_tuning(self) -> dict:

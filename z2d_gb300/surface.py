@@ -72,10 +72,10 @@ class Surface:
         if data is None:
             data = np.zeros(nbytes, np.uint8)
         if getattr(data, "numel", None) is not None:  # torch tensor
-            # packed formats on the device are padded to a 4-byte multiple
+            # z2d's length, or (packed formats) padded to a 4-byte multiple
             padded = (nbytes + 3) // 4 * 4 if self.format >= abi.FORMAT_ALPHA4 else nbytes
-            if data.numel() not in (nbytes, padded) or (self.format >= abi.FORMAT_ALPHA4 and data.numel() != padded):
-                raise ValueError(f"surface buffer has {data.numel()} bytes, need {padded}")
+            if data.numel() not in (nbytes, padded):
+                raise ValueError(f"surface buffer has {data.numel()} bytes, need {nbytes}")
         elif data.size != nbytes:
             raise ValueError(f"surface buffer has {data.size} bytes, need {nbytes}")
         self.data = data
