@@ -47,12 +47,43 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
 CPU_SAMPLE_FILLS = 2000   # cpu_baseline sample: the whole workload (~10-20 s single-threaded)
 REF_STEP_FILLS = 400      # --impl reference: fills per timed step
 PLAIN_FILLS = 300         # per-call arm: fills drawn with one z2dgpu_fill each
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch,
-# from the ncu captures summarised under profiles/
-TRAFFIC = {
-    "k_raster": (215_802_624, "profiles/k_raster_rgba4096_2000paths.md"),
-    "k_mask_op": (544_317_696, "profiles/k_mask_op_rgba8192_src_over.md"),
-}
+# Per-launch counters of the dominant kernels (DRAM bytes read + written,
+# instructions executed), from ncu captures of this workload; the file
+# records the hash of the CUDA sources of the build it captured, and the
+# bench line says whether that is the build being measured.
+COUNTERS_FILE = os.path.join(ROOT, "profiles", "counters_rgba4096_2000paths.json")
+
+
+def source_hash():
+    """SHA-256 (first 16 hex digits) of the library's CUDA and C++ sources:
+    the identity of the build whose kernels are measured."""
+    import hashlib
+    csrc = os.path.join(ROOT, "z2d_gb300", "csrc")
+    h = hashlib.sha256()
+    for name in sorted(os.listdir(csrc)):
+        if name.endswith((".cu", ".cuh", ".h", ".cpp", ".inc")):
+            h.update(name.encode())
+            with open(os.path.join(csrc, name), "rb") as f:
+                h.update(f.read())
+    with open(os.path.join(ROOT, "include", "z2dgpu.h"), "rb") as f:
+        h.update(f.read())
+    return h.hexdigest()[:16]
+
+
+def load_counters():
+    try:
+        with open(COUNTERS_FILE) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+def kernel_counter(counters, kernel, key):
+    """A captured per-launch counter, or None when it was not captured."""
+    try:
+        return counters["kernels"][kernel][key]
+    except Exception:
+        return None
 
 
 def load_peaks():
@@ -212,6 +243,25 @@ def diff_stats(got, ref):
     d = np.abs(a - b)
     return {"differing_bytes": int((d > 0).sum()), "differing_pixels": int((d > 0).any(1).sum()),
             "max_diff": int(d.max(initial=0))}
+
+
+def issue_roofline(counters, launch_ms, clk):
+    """k_raster is bound by instruction issue, not HBM: instructions
+    executed per launch (ncu, smsp__inst_executed.sum) over its measured
+    duration, against the issue peak of one warp instruction per cycle per
+    SM sub-partition (4 per SM) at the SM clock sampled during the run."""
+    inst = kernel_counter(counters, "k_raster", "inst_executed")
+    if not inst or not launch_ms:
+        return None
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = (clk or {}).get("sm_mhz") or (clk or {}).get("sm_max_mhz") or 2070.0
+    peak = sms * 4 * mhz * 1e6  # warp instructions per second
+    achieved = inst / (launch_ms / 1e3)
+    return {"bound": "issue", "kernel": "k_raster", "achieved": achieved, "peak": peak,
+            "unit": "warp inst/s", "frac": achieved / peak, "inst_per_launch": inst,
+            "source": os.path.relpath(COUNTERS_FILE, ROOT), "sm_mhz": mhz,
+            "note": "peak = SMs x 4 sub-partitions x 1 warp instruction per cycle x the sampled SM clock"}
 
 
 def host_threads():
@@ -935,6 +985,8 @@ def run_ours(args):
         clocks.stop()
         return
     peaks, peak_kind = load_peaks()
+    counters = load_counters()
+    build_id = source_hash()
     union_px = union_box_pixels(fills)
     alg_bytes = 2 * 4 * union_px  # read + write of every surface pixel a fill box touches
     raster_ms_per = raster_ms / max(raster_n, 1)
@@ -946,7 +998,8 @@ def run_ours(args):
         comp = compositor_sweep(ctx, stream, dev)
         comp_roof = {"bound": "hbm", "kernel": "k_mask_op<RGBA, src_over>", "achieved": comp["gbs_src_over"],
                      "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": comp["gbs_src_over"] / peaks["hbm_gbs"],
-                     "traffic": TRAFFIC["k_mask_op"][0], "traffic_source": TRAFFIC["k_mask_op"][1],
+                     "traffic": kernel_counter(counters, "k_mask_op_rgba_src_over_8192", "dram_bytes"),
+                     "traffic_source": os.path.relpath(COUNTERS_FILE, ROOT),
                      "alg_bytes_per_launch": comp["bytes_per_px"] * 8192 * 8192, "peak_source": peak_kind}
     clk = clocks.stop()  # sampled over the batched, e2e, plain and compositor timed regions
     if comp is not None and "breadth" in arms:
@@ -970,11 +1023,11 @@ def run_ours(args):
     else:
         cpu_v, cpu_dt = None, 0.0
     line = {
-        "metric": "Mpix/s fill+composite (src_over, 4096x4096 RGBA, 2000 random paths)",
+        "metric": f"Mpix/s fill+composite (src_over, {W}x{H} RGBA, {N_FILLS} random paths)",
         "value": value, "unit": "Mpix/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded)",
-        "config": {"workload": "plain_large_4096x4096_2000_paths", "surface": "rgba 4096x4096",
+        "config": {"workload": f"plain_large_{W}x{H}_{N_FILLS}_paths", "surface": f"rgba {W}x{H}",
                    "paths": N_FILLS, "mpix_per_step": mpix_step, "l2": "flushed (256 MiB write) before each step",
                    "mode": "batched (z2dgpu_fill_batch, device-resident surface)"},
         "stage_ms_per_step": stage,
@@ -992,10 +1045,13 @@ def run_ours(args):
         "parity": parity,
         "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": "k_raster", "achieved": achieved, "peak": peaks["hbm_gbs"],
-                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": TRAFFIC["k_raster"][0],
-                     "traffic_source": TRAFFIC["k_raster"][1],
+                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                     "traffic": kernel_counter(counters, "k_raster", "dram_bytes"),
+                     "traffic_source": os.path.relpath(COUNTERS_FILE, ROOT),
+                     "traffic_build": counters.get("source_hash") if counters else None, "build": build_id,
                      "peak_source": peak_kind, "alg_bytes_per_launch": alg_bytes,
                      "launch_ms": raster_ms_per},
+        "compute_roofline": issue_roofline(counters, raster_ms_per, clk),
         "cpu_baseline": {"value": cpu_v, "unit": "Mpix/s", "cores": 1, "kind": "port",
                          "sample": f"first {CPU_SAMPLE_FILLS} of {N_FILLS} fills, {cpu_dt:.1f} s"},
         "compositor": comp,
@@ -1018,8 +1074,15 @@ def main():
                          "list of compositor, breadth, star, jobs, serving, cpu, png, parity (shorter runs for profiling)")
     ap.add_argument("--jobs", type=int, default=4096,
                     help="surfaces of the batched-jobs arm (smaller for profiling captures)")
+    ap.add_argument("--size", type=int, default=4096,
+                    help="side of the fill workload's surface (smaller only for profiling captures)")
+    ap.add_argument("--fills", type=int, default=2000,
+                    help="paths of the fill workload (smaller only for profiling captures)")
     args = ap.parse_args()
     globals()["N_JOBS"] = args.jobs
+    globals()["W"] = globals()["H"] = args.size
+    globals()["N_FILLS"] = globals()["CPU_SAMPLE_FILLS"] = args.fills
+    globals()["PLAIN_FILLS"] = min(PLAIN_FILLS, args.fills)
     if args.impl == "reference":
         run_reference(args)
     else:
