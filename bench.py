@@ -86,6 +86,46 @@ def kernel_counter(counters, kernel, key):
         return None
 
 
+NCU_KEYS = {"dram__bytes_read.sum": "dram_read", "dram__bytes_write.sum": "dram_write",
+            "smsp__inst_executed.sum": "inst_executed", "gpu__time_duration.sum": "duration_ns"}
+
+
+def write_counters(specs):
+    """Writes the counters file from `ncu --csv` logs: each spec is
+    NAME=CSV, NAME the key the bench reads (k_raster,
+    k_mask_op_rgba_src_over_8192) and CSV one capture of that kernel
+    (the last launch in it is taken).  The file carries the source hash of
+    the tree it was written from, which must be the tree that was
+    captured."""
+    import csv
+    out = load_counters() or {}
+    if out.get("source_hash") != source_hash():
+        out = {}
+    out["source_hash"] = source_hash()
+    kernels = out.setdefault("kernels", {})
+    for spec in specs:
+        name, path = spec.split("=", 1)
+        with open(path) as f:
+            lines = f.read().splitlines()
+        start = next(i for i, l in enumerate(lines) if l.startswith('"ID"'))
+        launches = {}
+        for row in csv.DictReader(lines[start:]):
+            m = NCU_KEYS.get(row["Metric Name"])
+            if m:
+                d = launches.setdefault(row["ID"], {"kernel": row["Kernel Name"], "grid": row.get("Grid Size"),
+                                                    "block": row.get("Block Size")})
+                d[m] = float(row["Metric Value"].replace(",", ""))
+        last = launches[max(launches, key=int)]
+        if "dram_read" in last and "dram_write" in last:
+            last["dram_bytes"] = last["dram_read"] + last["dram_write"]
+        last["capture"] = os.path.basename(path)
+        kernels[name] = last
+    with open(COUNTERS_FILE, "w") as f:
+        json.dump(out, f, indent=1)
+        f.write("\n")
+    print(json.dumps(out))
+
+
 def load_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -1078,7 +1118,12 @@ def main():
                     help="side of the fill workload's surface (smaller only for profiling captures)")
     ap.add_argument("--fills", type=int, default=2000,
                     help="paths of the fill workload (smaller only for profiling captures)")
+    ap.add_argument("--counters-from", action="append", default=[], metavar="NAME=CSV",
+                    help="write the per-launch counters file from ncu --csv captures and exit")
     args = ap.parse_args()
+    if args.counters_from:
+        write_counters(args.counters_from)
+        return
     globals()["N_JOBS"] = args.jobs
     globals()["W"] = globals()["H"] = args.size
     globals()["N_FILLS"] = globals()["CPU_SAMPLE_FILLS"] = args.fills
