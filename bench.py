@@ -94,7 +94,8 @@ def write_counters(specs):
     """Writes the counters file from `ncu --csv` logs: each spec is
     NAME=CSV, NAME the key the bench reads (k_raster,
     k_mask_op_rgba_src_over_8192) and CSV one capture of that kernel
-    (the last launch in it is taken).  The file carries the source hash of
+    (the last launch in it is taken; captures of one kernel with different
+    metrics merge).  The file carries the source hash of
     the tree it was written from, which must be the tree that was
     captured."""
     import csv
@@ -116,10 +117,11 @@ def write_counters(specs):
                                                     "block": row.get("Block Size")})
                 d[m] = float(row["Metric Value"].replace(",", ""))
         last = launches[max(launches, key=int)]
-        if "dram_read" in last and "dram_write" in last:
-            last["dram_bytes"] = last["dram_read"] + last["dram_write"]
-        last["capture"] = os.path.basename(path)
-        kernels[name] = last
+        k = kernels.setdefault(name, {})
+        k.update(last)  # several captures of one kernel (metric groups) merge
+        if "dram_read" in k and "dram_write" in k:
+            k["dram_bytes"] = k["dram_read"] + k["dram_write"]
+        k.setdefault("captures", []).append(os.path.basename(path))
     with open(COUNTERS_FILE, "w") as f:
         json.dump(out, f, indent=1)
         f.write("\n")
@@ -440,7 +442,8 @@ def compositor_breadth(ctx, stream, dev, reps=2):
     from z2d_gb300 import abi, compositor
     from z2d_gb300.surface import Surface
     from z2d_gb300.types import Color, Gradient, Operation, Pattern, Pixel
-    n = 8192
+    n = BREADTH_SIZE
+    k = n / 8192  # geometry of the gradients scales with the surface
     g = torch.Generator(device=dev)
     g.manual_seed(SEED + 7)
     mask = Surface("alpha8", n, n, torch.randint(0, 256, (n * n,), device=dev, generator=g,
@@ -460,6 +463,8 @@ def compositor_breadth(ctx, stream, dev, reps=2):
     out = {"formats": {}, "float_ops_rgba": {}, "sources_rgba_src_over": {}}
     bpp = {"rgb": 4, "alpha8": 1, "alpha4": 0.5, "alpha2": 0.25, "alpha1": 0.125}
     for fmt, b in bpp.items():
+        if BREADTH_ONLY and BREADTH_ONLY not in fmt:
+            continue
         nbytes = abi.surface_bytes(abi.FORMAT_NAMES.index(fmt), n, n)
         t = torch.randint(0, 256, ((nbytes + 3) // 4 * 4,), device=dev, generator=g, dtype=torch.int32).to(torch.uint8)
         dst = Surface(fmt, n, n, t)
@@ -472,17 +477,21 @@ def compositor_breadth(ctx, stream, dev, reps=2):
     t = torch.randint(0, 256, (n * n * 4,), device=dev, generator=g, dtype=torch.int32).to(torch.uint8)
     dst = Surface("rgba", n, n, t)
     for op in ["src_over"] + sorted(abi.FLOAT_ONLY_OPS):
+        if BREADTH_ONLY and BREADTH_ONLY not in "float/" + op:
+            continue
         ms = timed(dst, pix, op, "float")
         out["float_ops_rgba"][op] = {"ms": round(ms, 4), "mpix_s": n * n / 1e6 / (ms / 1e3)}
     for kind in ("linear", "radial", "conic"):
         for method in ("linear_rgb", "srgb", "hsl"):
-            gr = {"linear": Gradient.linear(100, 200, 8000, 7000, method=method),
-                  "radial": Gradient.radial(4000, 4000, 50, 4100, 4200, 5000, method=method),
-                  "conic": Gradient.conic(4096, 4096, 0.3, method=method)}[kind]
+            gr = {"linear": Gradient.linear(100 * k, 200 * k, 8000 * k, 7000 * k, method=method),
+                  "radial": Gradient.radial(4000 * k, 4000 * k, 50 * k, 4100 * k, 4200 * k, 5000 * k, method=method),
+                  "conic": Gradient.conic(4096 * k, 4096 * k, 0.3, method=method)}[kind]
             for i, c in enumerate((Color.rgb(1, 0, 0, 1), Color.rgb(0, 1, 0, 0.6), Color.rgb(0, 0, 1, 0.8),
                                    Color.rgb(1, 1, 0, 1))):
                 gr.add_stop(i / 3, c)
             for dither in ("none", "bayer", "blue_noise"):
+                if BREADTH_ONLY and BREADTH_ONLY not in f"{kind}/{method}/{dither}":
+                    continue
                 src = Pattern.from_gradient(gr) if dither == "none" else Pattern.dither(dither, gr, 8)
                 ms = timed(dst, src, "src_over")
                 out["sources_rgba_src_over"][f"{kind}/{method}/{dither}"] = {
@@ -491,6 +500,8 @@ def compositor_breadth(ctx, stream, dev, reps=2):
     return out
 
 
+BREADTH_SIZE = 8192       # compositor breadth arm: side of its surfaces
+BREADTH_ONLY = ""         # ... and only the cells whose name contains this (profiling captures)
 N_JOBS = 4096             # batched-jobs arm: RGBA jobs, sides log-uniform [16, 2048], 1-200 paths each
 JOBS_PLAIN_FILLS = 1500   # per-call sample of the jobs arm (complete jobs, in order)
 
@@ -1118,6 +1129,10 @@ def main():
                     help="side of the fill workload's surface (smaller only for profiling captures)")
     ap.add_argument("--fills", type=int, default=2000,
                     help="paths of the fill workload (smaller only for profiling captures)")
+    ap.add_argument("--breadth-size", type=int, default=8192,
+                    help="side of the compositor breadth arm's surfaces (smaller only for profiling captures)")
+    ap.add_argument("--breadth-only", default="",
+                    help="run only the breadth cells whose name contains this, e.g. linear/linear_rgb/none")
     ap.add_argument("--counters-from", action="append", default=[], metavar="NAME=CSV",
                     help="write the per-launch counters file from ncu --csv captures and exit")
     args = ap.parse_args()
@@ -1125,6 +1140,8 @@ def main():
         write_counters(args.counters_from)
         return
     globals()["N_JOBS"] = args.jobs
+    globals()["BREADTH_SIZE"] = args.breadth_size
+    globals()["BREADTH_ONLY"] = args.breadth_only
     globals()["W"] = globals()["H"] = args.size
     globals()["N_FILLS"] = globals()["CPU_SAMPLE_FILLS"] = args.fills
     globals()["PLAIN_FILLS"] = min(PLAIN_FILLS, args.fills)

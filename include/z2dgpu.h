@@ -342,6 +342,14 @@ Z2D_API int z2dgpu_stroke_contours(const z2d_node *nodes, size_t n_nodes,
                                    uint64_t *contour_ends, size_t cap_contours,
                                    uint64_t *n_contours, double *scale);
 
+/* Gradient.getOffset (gradient.zig:239-243) of the w x h pixels from
+ * (x0, y0), row-major into the host array `offsets`, exactly as the fill
+ * and compositor kernels evaluate them (-1 = no colour).  *n_f64, when not
+ * NULL, receives how many of them the double-word evaluation left to the
+ * f64 code.  A diagnostic for the offsets; w * h <= 2^28. */
+Z2D_API int z2dgpu_gradient_offsets(z2dgpu_ctx *ctx, const z2d_gradient *gradient, int32_t x0, int32_t y0, int32_t w,
+                                    int32_t h, float *offsets, int64_t *n_f64);
+
 /* ---- PNG export (src/export_png.zig) ---- */
 enum { Z2D_PROFILE_NONE = -1, Z2D_PROFILE_LINEAR = 0, Z2D_PROFILE_SRGB = 1 };
 /* png_exporter.writeToPNGFile (export_png.zig:56-87) to memory: the PNG file

@@ -78,6 +78,9 @@ def load_oracle():
             lib.z2doracle_atan2.restype = C.c_double
             lib.z2doracle_gradient_offset.argtypes = [C.POINTER(abi.z2d_gradient), C.c_int32, C.c_int32]
             lib.z2doracle_gradient_offset.restype = C.c_float
+            lib.z2doracle_gradient_offsets.argtypes = [C.POINTER(abi.z2d_gradient), C.c_int32, C.c_int32, C.c_int32,
+                                                       C.c_int32, C.c_void_p]
+            lib.z2doracle_gradient_offsets.restype = None
             lib.z2doracle_gradient_pixel.argtypes = [C.POINTER(abi.z2d_gradient), C.c_int32, C.c_int32]
             lib.z2doracle_gradient_pixel.restype = abi.z2d_pixel
             lib.z2doracle_dither_pixel.argtypes = [C.POINTER(abi.z2d_pattern), C.c_int32, C.c_int32]
@@ -217,6 +220,15 @@ class Oracle:
         g = gradient.to_abi(keep)
         return self.lib.z2doracle_gradient_offset(C.byref(g), x, y)
 
+
+    def gradient_offsets(self, gradient, x0: int, y0: int, w: int, h: int):
+        """Gradient.getOffset for a w x h block of pixels (float32, row-major)."""
+        import numpy as np
+        keep = []
+        g = gradient.to_abi(keep)
+        out = np.empty((h, w), dtype=np.float32)
+        self.lib.z2doracle_gradient_offsets(C.byref(g), x0, y0, w, h, out.ctypes.data)
+        return out
     def gradient_pixel(self, gradient, x: int, y: int):
         keep: list = []
         g = gradient.to_abi(keep)

@@ -2085,6 +2085,14 @@ __attribute__((visibility("default"))) float z2doracle_gradient_offset(const z2d
     return grad_offset(gr, x, y);
 }
 
+// The offsets of a w x h block of pixels starting at (x0, y0), row-major.
+__attribute__((visibility("default"))) void z2doracle_gradient_offsets(const z2d_gradient *g, int32_t x0, int32_t y0,
+                                                                       int32_t w, int32_t h, float *out) {
+    const Grad gr = make_grad(*g);
+    for (int32_t j = 0; j < h; j++)
+        for (int32_t i = 0; i < w; i++) out[(size_t)j * (size_t)w + (size_t)i] = grad_offset(gr, x0 + i, y0 + j);
+}
+
 // Edge list of fill_plotter.plot (fill_plotter.zig:21-97): writes up to
 // `cap` edges as (y0, y1, x_start, x_inc) and the extents
 // (top, bottom, left, right); returns the edge count or a negative status.

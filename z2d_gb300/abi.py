@@ -160,7 +160,7 @@ EXPORTED_SYMBOLS = [
     "z2dgpu_composite",
     "z2dgpu_composite_noalloc", "z2dgpu_server_create", "z2dgpu_server_submit", "z2dgpu_server_wait",
     "z2dgpu_server_stats", "z2dgpu_server_destroy", "z2dgpu_server_create2", "z2dgpu_server_submit_new",
-    "z2dgpu_server_info", "z2dgpu_png_encode", "z2dgpu_png_scanlines", "z2dgpu_free",
+    "z2dgpu_server_info", "z2dgpu_png_encode", "z2dgpu_png_scanlines", "z2dgpu_free", "z2dgpu_gradient_offsets",
 ]
 
 PROFILE = {None: -1, "linear": 0, "srgb": 1}  # color.RGBProfile of the PNG exporter

@@ -113,6 +113,50 @@ void Ctx::timer_collect(Timer &t) {
 }
 
 // ---------------------------------------------- descriptor preparation
+// The double-word constants of the gradient's fast offsets (grad_fast.cuh):
+// each f64 value split into float hi + lo.  The fast path is left off when
+// a constant is not finite or a nonzero one lies outside [2^-60, 2^60]
+// (both words of every split are then normal floats).
+static void fast_constants(DevGradient &d) {
+    GradFast &F = d.fz;
+    F.mode = kFastNone;
+    bool sane = true;
+    auto split = [&](double v) {
+        if (!std::isfinite(v) || (v != 0.0 && (std::fabs(v) < 0x1p-60 || std::fabs(v) > 0x1p60))) sane = false;
+        DW w;
+        w.h = (float)v;
+        w.l = std::isfinite(v) ? (float)(v - (double)w.h) : 0.0f;
+        return w;
+    };
+    if (d.has_tf)
+        for (int i = 0; i < 6; i++) F.tf[i] = split(d.tf[i]);
+    F.g0 = split(d.g[0]);
+    F.g1 = split(d.g[1]);
+    if (d.type == Z2D_GRADIENT_LINEAR) {
+        if (d.lin_zero) {
+            F.mode = kFastVoid;
+            return;
+        }
+        F.k[0] = split(d.lin_dx);
+        F.k[1] = split(d.lin_dy);
+        F.k[2] = split(d.lin_inv);
+        if (sane) F.mode = kFastLinear;
+    } else if (d.type == Z2D_GRADIENT_RADIAL) {
+        if (d.inner_r == 0.0 && d.outer_r == 0.0) {
+            F.mode = kFastVoid;
+            return;
+        }
+        // the per-pixel products of the f64 code, formed the same way
+        const double ir_dr = d.inner_r * d.dr, nir2 = -d.inner_r * d.inner_r;
+        const double k[8] = {d.cdx, d.cdy, ir_dr, nir2, d.a, d.inv_a, d.dr, d.min_dr};
+        for (int i = 0; i < 8; i++) F.k[i] = split(k[i]);
+        if (sane) F.mode = d.a == 0.0 ? kFastRadialA0 : kFastRadial;
+    } else {
+        F.k[0] = split(d.angle);
+        if (sane) F.mode = kFastConic;
+    }
+}
+
 int make_dev_gradient(const z2d_gradient &g, DevGradient &out) {
     memset(&out, 0, sizeof(out));
     if (g.n_stops < 0 || (g.n_stops > 0 && !g.stops)) {
@@ -181,6 +225,7 @@ int make_dev_gradient(const z2d_gradient &g, DevGradient &out) {
         const double r = std::fmod(g.geom[2], twopi);
         out.angle = g.geom[2] < 0.0 ? std::fmod(r + twopi, twopi) : r;
     }
+    fast_constants(out);
     return Z2D_OK;
 }
 
@@ -1670,6 +1715,46 @@ Z2D_API int z2dgpu_composite(z2dgpu_ctx *c, z2d_surface *dst, int32_t dst_x, int
     rc = launch_composite(*c, J);
     if (rc) return rc;
     return stage_out(*c, *dst, J.dst);
+}
+
+// Gradient offsets of a block of pixels, as the compositor and the
+// rasteriser evaluate them; counts the pixels that took the f64 code.
+__global__ void k_grad_offsets(const DevGradient *__restrict__ g, int32_t x0, int32_t y0, int32_t w, long long n,
+                               float *__restrict__ out, unsigned long long *__restrict__ n_slow) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool slow = false;
+    if (i < n) out[i] = grad_offset_ex(*g, x0 + (int32_t)(i % w), y0 + (int32_t)(i / w), slow);
+    const unsigned b = __ballot_sync(0xffffffffu, slow);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(n_slow, (unsigned long long)__popc(b));
+}
+
+Z2D_API int z2dgpu_gradient_offsets(z2dgpu_ctx *c, const z2d_gradient *g, int32_t x0, int32_t y0, int32_t w, int32_t h,
+                                    float *offsets, int64_t *n_f64) {
+    if (!c || !g || !offsets || w <= 0 || h <= 0 || (long long)w * h > (1ll << 28)) return Z2D_ERR_INVALID_ARGUMENT;
+    Z2D_CUDA(cudaSetDevice(c->device));
+    DevGradient dg;
+    const int rc = make_dev_gradient(*g, dg);
+    if (rc) return rc;
+    const long long n = (long long)w * h;
+    const size_t o_out = 1024, o_cnt = o_out + ((sizeof(float) * (size_t)n + 255) & ~(size_t)255);
+    if (c->params.ensure(o_cnt + 256) || c->staging.ensure(sizeof(DevGradient) + 16)) return Z2D_ERR_OUT_OF_MEMORY;
+    static_assert(sizeof(DevGradient) <= 1024, "descriptor fits before the offsets");
+    Z2D_CUDA(cudaStreamSynchronize(c->stream));
+    memcpy(c->staging.ptr, &dg, sizeof(DevGradient));
+    uint8_t *dv = c->params.as<uint8_t>();
+    Z2D_CUDA(cudaMemcpyAsync(dv, c->staging.ptr, sizeof(DevGradient), cudaMemcpyHostToDevice, c->stream));
+    Z2D_CUDA(cudaMemsetAsync(dv + o_cnt, 0, sizeof(unsigned long long), c->stream));
+    k_grad_offsets<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(
+        reinterpret_cast<const DevGradient *>(dv), x0, y0, w, n, reinterpret_cast<float *>(dv + o_out),
+        reinterpret_cast<unsigned long long *>(dv + o_cnt));
+    c->launches++;
+    Z2D_CUDA(cudaGetLastError());
+    unsigned long long slow = 0;
+    Z2D_CUDA(cudaMemcpyAsync(offsets, dv + o_out, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    Z2D_CUDA(cudaMemcpyAsync(&slow, dv + o_cnt, sizeof(slow), cudaMemcpyDeviceToHost, c->stream));
+    Z2D_CUDA(cudaStreamSynchronize(c->stream));
+    if (n_f64) *n_f64 = (int64_t)slow;
+    return Z2D_OK;
 }
 
 // SurfaceCompositor.run for callers that are not allowed to allocate device

@@ -9,11 +9,12 @@
 //    512 contiguous mask bytes and 64-256 contiguous destination bytes per
 //    load instruction: no shuffles or atomics are needed because every
 //    destination word is owned by one lane.  The operator is a template
-//    parameter; per pixel the lane extracts the destination bits, scales
-//    them to 8 bits (Alpha(T).scaleIntoIntAlpha), runs IntegerOps.dstIn on
-//    the pixel source's alpha and the operator on the alpha lane, and packs
-//    the result back (z2d's packed formats only carry alpha; the operators'
-//    alpha lanes read alphas only).
+//    parameter; its result on one pixel depends on the mask byte and the
+//    destination value only, so each CTA first tabulates it for every
+//    pair (IntegerOps.dstIn on the pixel source's alpha, the operator on the
+//    alpha lane after Alpha(T).scaleIntoIntAlpha, the scale back; z2d's
+//    packed formats only carry alpha and the operators' alpha lanes read
+//    alphas only), and every pixel becomes a table lookup.
 //  * k_mask_float<FMT, OP>: float precision (StrideCompositor.runPrecision
 //    with .float, compositor.zig:540-621) on the 4-byte formats and alpha8,
 //    pixel source.  x / 255 for the 256 byte values comes from a shared
@@ -56,13 +57,49 @@ struct PackedUnit<1> {
     static __device__ __forceinline__ T put(uint64_t v) { return (uint16_t)v; }
 };
 
+// The packed kernels' result table.  With a pixel source the result of
+// [dst_in(source, mask), op] on one packed pixel depends only on its mask
+// byte m and its destination value v (2^BITS of them): the table holds it
+// for all 256 x 2^BITS pairs, BITS bits each, at bit (m * 2^BITS + v) * BITS.
+// Every CTA evaluates the table once with the operator's own arithmetic,
+// then each pixel is one shared-memory lookup instead of the operator.  The
+// table is kept in 32 copies interleaved by word (word w of copy l at
+// w * 32 + l), and lane l reads copy l: every lane of a warp reads its own
+// bank, so random mask bytes never conflict.
+template <int BITS>
+struct PackedTable {
+    static constexpr int LOGB = BITS == 4 ? 2 : BITS == 2 ? 1 : 0;
+    static constexpr int POS_M = BITS + LOGB;              // log2(2^BITS * BITS): bits per mask byte
+    static constexpr int WORDS = (256 << POS_M) / 32;      // 512, 64, 16
+    static constexpr size_t SMEM = (size_t)(WORDS * 32 + WORDS) * sizeof(uint32_t);
+};
+
 template <int FMT, int OP>
 __global__ void __launch_bounds__(kFusedThreads) k_mask_packed(uint8_t *__restrict__ dst, const uint8_t *__restrict__ mask,
                                                                size_t n_items, uint32_t spa) {
     constexpr int BITS = FMT == Z2D_FORMAT_ALPHA4 ? 4 : FMT == Z2D_FORMAT_ALPHA2 ? 2 : 1;
     constexpr uint32_t MAXV = (1u << BITS) - 1u;
+    using TB = PackedTable<BITS>;
     using U = PackedUnit<BITS>;
     using T = typename U::T;
+    extern __shared__ uint32_t tab[];
+    uint32_t *const words = tab + TB::WORDS * 32;
+    for (int w = threadIdx.x; w < TB::WORDS; w += kFusedThreads) {
+        uint32_t word = 0;
+#pragma unroll 1
+        for (int b = 0; b < 32; b += BITS) {
+            const uint32_t pos = (uint32_t)w * 32u + (uint32_t)b;
+            const uint32_t m = pos >> TB::POS_M, v = (pos >> TB::LOGB) & MAXV;
+            const uint32_t ra = (spa * m) / 255u;  // IntegerOps.dstIn, alpha lane
+            const I16 r = int_op(OP, I16{0u, 0u, 0u, scale_alpha(v, BITS, 8)}, I16{0u, 0u, 0u, ra});
+            word |= scale_alpha(r.a & 0xFFu, 8, BITS) << b;
+        }
+        words[w] = word;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < TB::WORDS * 32; i += kFusedThreads) tab[i] = words[i >> 5];
+    __syncthreads();
+    const uint32_t *const mine = tab + (threadIdx.x & 31u);
     T *const d = reinterpret_cast<T *>(dst);
     const uint4 *const m = reinterpret_cast<const uint4 *>(mask);
     const size_t tile = (size_t)kFusedThreads * kFusedUnroll;
@@ -87,10 +124,10 @@ __global__ void __launch_bounds__(kFusedThreads) k_mask_packed(uint8_t *__restri
 #pragma unroll
             for (int j = 0; j < 16; j++) {
                 const uint32_t mb = (mw[j >> 2] >> (8 * (j & 3))) & 0xFFu;
-                const uint32_t ra = (spa * mb) / 255u;  // IntegerOps.dstIn, alpha lane
                 const uint32_t raw = (uint32_t)(in >> (j * BITS)) & MAXV;
-                const I16 r = int_op(OP, I16{0u, 0u, 0u, scale_alpha(raw, BITS, 8)}, I16{0u, 0u, 0u, ra});
-                out |= (uint64_t)scale_alpha(r.a & 0xFFu, 8, BITS) << (j * BITS);
+                const uint32_t pos = (mb << TB::POS_M) | (raw << TB::LOGB);
+                const uint32_t word = mine[pos & ~31u];
+                out |= (uint64_t)((word >> (pos & 31u)) & MAXV) << (j * BITS);
             }
             d[it] = U::put(out);
         }
@@ -173,10 +210,11 @@ static std::atomic<int> g_packed_occ[3][Z2D_OP_COUNT];
 static std::atomic<int> g_float_occ[5][Z2D_OP_COUNT];
 
 template <class K>
-static size_t grid_for(std::atomic<int> &slot, K k, const Ctx &c, size_t units) {
+static size_t grid_for(std::atomic<int> &slot, K k, const Ctx &c, size_t units, size_t smem = 0) {
     int occ = slot.load(std::memory_order_relaxed);
     if (occ <= 0) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kFusedThreads, 0) != cudaSuccess || occ <= 0) occ = 4;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kFusedThreads, smem) != cudaSuccess || occ <= 0) occ = 1;
         slot.store(occ, std::memory_order_relaxed);
     }
     const size_t tile = (size_t)kFusedThreads * kFusedUnroll;
@@ -201,10 +239,11 @@ bool launch_mask_packed(Ctx &c, uint8_t *dst, int fmt, const uint8_t *mask, size
         case Z2D_FORMAT_ALPHA1: k = packed_table<Z2D_FORMAT_ALPHA1>(ops)[op]; slot = 2; break;
         default: return false;
     }
+    const size_t smem = bits == 4 ? PackedTable<4>::SMEM : bits == 2 ? PackedTable<2>::SMEM : PackedTable<1>::SMEM;
     const size_t n_items = px / 16;
-    const size_t blocks = grid_for(g_packed_occ[slot][op], k, c, n_items);
+    const size_t blocks = grid_for(g_packed_occ[slot][op], k, c, n_items, smem);
     if (blocks == 0) return true;
-    k<<<(unsigned)blocks, kFusedThreads, 0, c.stream>>>(dst, mask, n_items, spx.a);
+    k<<<(unsigned)blocks, kFusedThreads, smem, c.stream>>>(dst, mask, n_items, spx.a);
     c.launches++;
     return true;
 }

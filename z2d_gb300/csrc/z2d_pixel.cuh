@@ -9,6 +9,7 @@
 #include <stdint.h>
 
 #include "../../include/z2dgpu.h"
+#include "grad_fast.cuh"
 #include "zig_math.cuh"
 
 #define Z2D_HD __host__ __device__ __forceinline__
@@ -509,6 +510,8 @@ struct DevGradient {
     // end - start and 1 / |end - start|^2; lin_zero: zero-length gradient
     double lin_dx, lin_dy, lin_inv;
     int32_t lin_zero, pad_;
+    // the same offsets on double-word floats (grad_fast.cuh)
+    GradFast fz;
     // Up to kMaxStops stops live inline.  A longer stop list (z2d's grows
     // without bound, src/gradient.zig:183-198) is a table in device memory
     // written with the descriptors (ext_off / ext_prep); `src` is the
@@ -522,8 +525,8 @@ struct DevGradient {
 
 Z2D_D double clampd(double v, double lo, double hi) { return fmax(lo, fmin(v, hi)); }
 
-// Gradient.getOffset (src/gradient.zig:239-243, 349-372, 605-648, 731-741)
-Z2D_D float grad_offset(const DevGradient &gr, int32_t x, int32_t y) {
+// The f64 evaluation (the reference arithmetic).
+Z2D_D float grad_offset_f64(const DevGradient &gr, int32_t x, int32_t y) {
     if (gr.type == Z2D_GRADIENT_RADIAL && gr.inner_r == 0.0 && gr.outer_r == 0.0) return -1.0f;
     double px = (double)x + 0.5, py = (double)y + 0.5;
     if (gr.has_tf) {
@@ -572,6 +575,30 @@ Z2D_D float grad_offset(const DevGradient &gr, int32_t x, int32_t y) {
     const double twopi = 6.283185307179586;
     const double ang = zmod(zm::atan2_(dy, dx) - gr.angle, twopi);
     return (float)(ang / twopi);
+}
+
+// Gradient.getOffset (src/gradient.zig:239-243, 349-372, 605-648, 731-741):
+// the double-word evaluation when it decides the f32 result, else the f64
+// code above (`slow` is set then).
+Z2D_D float grad_offset_ex(const DevGradient &gr, int32_t x, int32_t y, bool &slow) {
+    const int32_t mode = gr.fz.mode;
+    if (mode == kFastVoid) return -1.0f;
+    if (mode != kFastNone && (uint32_t)(x + (1 << 22)) < (1u << 23) && (uint32_t)(y + (1 << 22)) < (1u << 23)) {
+        const float fx = (float)x + 0.5f, fy = (float)y + 0.5f;
+        const bool tf = gr.has_tf != 0;
+        float t = 0.0f;
+        int done;
+        if (mode == kFastLinear) done = fast_linear(gr.fz, tf, fx, fy, t);
+        else if (mode == kFastConic) done = fast_conic(gr.fz, tf, fx, fy, t);
+        else done = fast_radial(gr.fz, tf, mode == kFastRadialA0, fx, fy, t);
+        if (done) return t;
+    }
+    slow = true;
+    return grad_offset_f64(gr, x, y);
+}
+Z2D_D float grad_offset(const DevGradient &gr, int32_t x, int32_t y) {
+    bool slow = false;
+    return grad_offset_ex(gr, x, y, slow);
 }
 
 struct Search {

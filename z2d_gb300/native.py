@@ -105,6 +105,9 @@ def load(build_if_missing: bool = True):
             getattr(lib, name).restype = C.c_int
         lib.z2dgpu_free.argtypes = [C.c_void_p]
         lib.z2dgpu_free.restype = None
+        lib.z2dgpu_gradient_offsets.argtypes = [C.c_void_p, P(abi.z2d_gradient), C.c_int32, C.c_int32, C.c_int32,
+                                                C.c_int32, C.c_void_p, P(C.c_int64)]
+        lib.z2dgpu_gradient_offsets.restype = C.c_int
         for name in ("z2dgpu_server_create", "z2dgpu_server_create2", "z2dgpu_server_submit",
                      "z2dgpu_server_submit_new", "z2dgpu_server_wait", "z2dgpu_server_stats", "z2dgpu_server_info",
                      "z2dgpu_server_destroy"):
@@ -166,6 +169,17 @@ class Context:
         d, ct, od, it = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
         check(self.lib.z2dgpu_ctx_raster_tuning(self.handle, C.byref(d), C.byref(ct), C.byref(od), C.byref(it)))
         return {"decided": d.value, "ctas_per_sm": ct.value, "order": od.value, "tile_items": it.value}
+
+    def gradient_offsets(self, gradient, x0: int, y0: int, w: int, h: int):
+        """The offsets the kernels evaluate for a w x h block of pixels
+        (float32, row-major) and how many took the f64 code."""
+        import numpy as np
+        keep: list = []
+        g = gradient.to_abi(keep)
+        out = np.empty((h, w), dtype=np.float32)
+        n = C.c_int64()
+        check(self.lib.z2dgpu_gradient_offsets(self.handle, C.byref(g), x0, y0, w, h, out.ctypes.data, C.byref(n)))
+        return out, int(n.value)
 
     def kernel_ms(self, kernel: str):
         n = C.c_uint64()
