@@ -342,6 +342,67 @@ Z2D_API int z2dgpu_stroke_contours(const z2d_node *nodes, size_t n_nodes,
                                    uint64_t *contour_ends, size_t cap_contours,
                                    uint64_t *n_contours, double *scale);
 
+/* ---- Path building on the device (src/Path.zig, src/internal/arc.zig,
+ * src/internal/Glyph.zig) ----
+ * A path program is the sequence of Path calls that builds one path, with
+ * the Path's transformation and tolerance at its start.  The device runs
+ * each program as z2d's Path would and writes the device-space nodes it
+ * would hold: user points clamped to the i24 range and mapped by the
+ * transformation, a move_to to the point of a trailing move_to dropped,
+ * close as close_path plus a move_to back to the subpath's start, rel*
+ * points relative to the current point mapped back through the inverse
+ * transformation, arcs as arc.zig's cubic splines (Zig's f64 sin / cos /
+ * tan), glyph outlines as Outline.init + appendToPath. */
+enum {
+    Z2D_PATH_MOVE_TO = 0,           /* v: x, y */
+    Z2D_PATH_LINE_TO = 1,           /* v: x, y */
+    Z2D_PATH_CURVE_TO = 2,          /* v: x1, y1, x2, y2, x3, y3 */
+    Z2D_PATH_REL_MOVE_TO = 3,       /* v: dx, dy */
+    Z2D_PATH_REL_LINE_TO = 4,       /* v: dx, dy */
+    Z2D_PATH_REL_CURVE_TO = 5,      /* v: dx1, dy1, dx2, dy2, dx3, dy3 */
+    Z2D_PATH_ARC = 6,               /* v: xc, yc, radius, angle1, angle2 (Path.arc) */
+    Z2D_PATH_ARC_NEGATIVE = 7,      /* v: as ARC (Path.arcNegative) */
+    Z2D_PATH_CLOSE = 8,
+    Z2D_PATH_SET_TRANSFORMATION = 9,/* v: ax, by, cx, dy, tx, ty (Path.transformation = v) */
+    Z2D_PATH_SET_TOLERANCE = 10,    /* v: tolerance (Path.tolerance) */
+    Z2D_PATH_RESET = 11,            /* Path.reset: clears the nodes and the points */
+    Z2D_PATH_GLYPH = 12             /* v: first point, points, first contour end, contours,
+                                     *    units per em: a simple glyph's outline (Glyph.zig
+                                     *    runOutline) appended with the current transformation */
+};
+typedef struct z2d_path_cmd {
+    int32_t op;
+    int32_t _pad;
+    double v[6];
+} z2d_path_cmd;
+typedef struct z2d_path_program {
+    uint64_t cmd_offset, n_cmds;  /* the program's commands in the command array */
+    double transformation[6];     /* ax, by, cx, dy, tx, ty at the start */
+    double tolerance;             /* Path.tolerance at the start (z2d's default: 0.1) */
+} z2d_path_program;
+/* A glyph outline point (TrueType simple glyph): font units; bit 0 of
+ * flags = on-curve.  Contours are given by the index of their last point. */
+typedef struct z2d_glyph_point {
+    int16_t x, y;
+    uint16_t flags;
+    uint16_t _pad;
+} z2d_glyph_point;
+/* Runs every program and writes its nodes, program after program, to
+ * `nodes` (host or device memory, cap_nodes entries): program p's nodes are
+ * nodes[offsets[p] .. offsets[p+1]) (offsets has n_programs + 1 entries and
+ * is filled even when the nodes do not fit, which returns
+ * Z2D_ERR_OUT_OF_MEMORY).  status[p] (may be NULL) is 0 or the program's
+ * first error, where it stopped: Z2D_ERR_INVALID_STATE for NoCurrentPoint
+ * (curve_to / rel* without a current point), Z2D_ERR_INVALID_ARGUMENT for
+ * InvalidMatrix (rel* or a glyph with a transformation that cannot be
+ * inverted), a malformed glyph, an unknown command, an arc angle beyond
+ * 2^20 * pi/2 or arc angles so far apart that whole turns no longer change
+ * them (z2d would loop there).  Its nodes up to the error are kept. */
+Z2D_API int z2dgpu_build_paths(z2dgpu_ctx *ctx, const z2d_path_program *programs, size_t n_programs,
+                               const z2d_path_cmd *cmds, size_t n_cmds, const z2d_glyph_point *glyph_points,
+                               size_t n_glyph_points, const uint16_t *glyph_ends, size_t n_glyph_ends,
+                               z2d_node *nodes, size_t cap_nodes, uint64_t *offsets, int32_t *status);
+
 /* Gradient.getOffset (gradient.zig:239-243) of the w x h pixels from
  * (x0, y0), row-major into the host array `offsets`, exactly as the fill
  * and compositor kernels evaluate them (-1 = no colour).  *n_f64, when not

@@ -19,9 +19,10 @@ from z2d_gb300.types import FillOptions, Operation, Pattern, nodes_to_abi
 HERE = pathlib.Path(__file__).resolve().parent
 SRC = HERE / "z2d_oracle.cpp"
 SRC_STROKE = HERE / "z2d_stroke.cpp"
+SRC_PATH = HERE / "z2d_path.cpp"
 BUILD = HERE / "_build"
 LIB = BUILD / "libz2doracle.so"
-DEPS = [SRC, SRC_STROKE, HERE.parent / "include" / "z2dgpu.h", HERE.parent / "z2d_gb300" / "csrc" / "blue_noise_64x64.inc"]
+DEPS = [SRC, SRC_STROKE, SRC_PATH, HERE.parent / "include" / "z2dgpu.h", HERE.parent / "z2d_gb300" / "csrc" / "blue_noise_64x64.inc"]
 CXXFLAGS = ["-std=c++17", "-O3", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared"]
 
 _lock = threading.Lock()
@@ -34,7 +35,7 @@ def build_oracle(force: bool = False) -> pathlib.Path:
     if not force and LIB.exists() and all(LIB.stat().st_mtime >= d.stat().st_mtime for d in DEPS):
         return LIB
     tmp = BUILD / f"libz2doracle.{os.getpid()}.so"
-    cmd = ["g++", *CXXFLAGS, "-o", str(tmp), str(SRC), str(SRC_STROKE)]
+    cmd = ["g++", *CXXFLAGS, "-o", str(tmp), str(SRC), str(SRC_STROKE), str(SRC_PATH)]
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB)
     return LIB
@@ -81,6 +82,14 @@ def load_oracle():
             lib.z2doracle_gradient_offsets.argtypes = [C.POINTER(abi.z2d_gradient), C.c_int32, C.c_int32, C.c_int32,
                                                        C.c_int32, C.c_void_p]
             lib.z2doracle_gradient_offsets.restype = None
+            lib.z2doracle_build_paths.argtypes = [C.POINTER(abi.z2d_path_program), C.c_size_t,
+                                                  C.POINTER(abi.z2d_path_cmd), C.c_size_t,
+                                                  C.POINTER(abi.z2d_glyph_point), C.c_size_t, C.POINTER(C.c_uint16),
+                                                  C.c_size_t, C.c_void_p, C.c_size_t, C.POINTER(C.c_uint64),
+                                                  C.POINTER(C.c_int32)]
+            lib.z2doracle_build_paths.restype = C.c_int
+            lib.z2doracle_zig_trig.argtypes = [C.c_int, C.c_double, C.POINTER(C.c_int)]
+            lib.z2doracle_zig_trig.restype = C.c_double
             lib.z2doracle_gradient_pixel.argtypes = [C.POINTER(abi.z2d_gradient), C.c_int32, C.c_int32]
             lib.z2doracle_gradient_pixel.restype = abi.z2d_pixel
             lib.z2doracle_dither_pixel.argtypes = [C.POINTER(abi.z2d_pattern), C.c_int32, C.c_int32]
@@ -220,6 +229,20 @@ class Oracle:
         g = gradient.to_abi(keep)
         return self.lib.z2doracle_gradient_offset(C.byref(g), x, y)
 
+
+    def zig_trig(self, which: str, x: float):
+        """Zig's f64 sin / cos / tan as the oracle restates them (None beyond
+        the medium argument range)."""
+        ok = C.c_int()
+        v = self.lib.z2doracle_zig_trig({"sin": 0, "cos": 1, "tan": 2}[which], x, C.byref(ok))
+        return v if ok.value else None
+
+    def build_paths(self, programs):
+        """Path programs built by the oracle's Path restatement: (nodes per
+        program as NODE_DTYPE arrays, status per program)."""
+        from z2d_gb300.path_program import pack_programs, unpack_nodes
+        packed = pack_programs(programs)
+        return unpack_nodes(packed, lambda *a: self.lib.z2doracle_build_paths(*a))
 
     def gradient_offsets(self, gradient, x0: int, y0: int, w: int, h: int):
         """Gradient.getOffset for a w x h block of pixels (float32, row-major)."""

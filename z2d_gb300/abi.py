@@ -81,6 +81,24 @@ class z2d_node(C.Structure):
     _fields_ = [("tag", C.c_int32), ("_pad", C.c_int32), ("p", C.c_double * 6)]
 
 
+# path programs (include/z2dgpu.h: z2dgpu_build_paths)
+(PATH_MOVE_TO, PATH_LINE_TO, PATH_CURVE_TO, PATH_REL_MOVE_TO, PATH_REL_LINE_TO, PATH_REL_CURVE_TO, PATH_ARC,
+ PATH_ARC_NEGATIVE, PATH_CLOSE, PATH_SET_TRANSFORMATION, PATH_SET_TOLERANCE, PATH_RESET, PATH_GLYPH) = range(13)
+
+
+class z2d_path_cmd(C.Structure):
+    _fields_ = [("op", C.c_int32), ("_pad", C.c_int32), ("v", C.c_double * 6)]
+
+
+class z2d_path_program(C.Structure):
+    _fields_ = [("cmd_offset", C.c_uint64), ("n_cmds", C.c_uint64), ("transformation", C.c_double * 6),
+                ("tolerance", C.c_double)]
+
+
+class z2d_glyph_point(C.Structure):
+    _fields_ = [("x", C.c_int16), ("y", C.c_int16), ("flags", C.c_uint16), ("_pad", C.c_uint16)]
+
+
 class z2d_color(C.Structure):
     _fields_ = [("space", C.c_int32), ("c", C.c_float * 4)]
 
@@ -160,7 +178,7 @@ EXPORTED_SYMBOLS = [
     "z2dgpu_composite",
     "z2dgpu_composite_noalloc", "z2dgpu_server_create", "z2dgpu_server_submit", "z2dgpu_server_wait",
     "z2dgpu_server_stats", "z2dgpu_server_destroy", "z2dgpu_server_create2", "z2dgpu_server_submit_new",
-    "z2dgpu_server_info", "z2dgpu_png_encode", "z2dgpu_png_scanlines", "z2dgpu_free", "z2dgpu_gradient_offsets",
+    "z2dgpu_server_info", "z2dgpu_png_encode", "z2dgpu_png_scanlines", "z2dgpu_free", "z2dgpu_gradient_offsets", "z2dgpu_build_paths",
 ]
 
 PROFILE = {None: -1, "linear": 0, "srgb": 1}  # color.RGBProfile of the PNG exporter

@@ -1717,6 +1717,16 @@ Z2D_API int z2dgpu_composite(z2dgpu_ctx *c, z2d_surface *dst, int32_t dst_x, int
     return stage_out(*c, *dst, J.dst);
 }
 
+Z2D_API int z2dgpu_build_paths(z2dgpu_ctx *c, const z2d_path_program *programs, size_t n_programs,
+                               const z2d_path_cmd *cmds, size_t n_cmds, const z2d_glyph_point *glyph_points,
+                               size_t n_glyph_points, const uint16_t *glyph_ends, size_t n_glyph_ends,
+                               z2d_node *nodes, size_t cap_nodes, uint64_t *offsets, int32_t *status) {
+    if (!c) return Z2D_ERR_INVALID_ARGUMENT;
+    Z2D_CUDA(cudaSetDevice(c->device));
+    return build_paths(*c, programs, n_programs, cmds, n_cmds, glyph_points, n_glyph_points, glyph_ends,
+                       n_glyph_ends, nodes, cap_nodes, offsets, status);
+}
+
 // Gradient offsets of a block of pixels, as the compositor and the
 // rasteriser evaluate them; counts the pixels that took the f64 code.
 __global__ void k_grad_offsets(const DevGradient *__restrict__ g, int32_t x0, int32_t y0, int32_t w, long long n,

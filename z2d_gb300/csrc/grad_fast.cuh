@@ -110,6 +110,11 @@ __device__ __forceinline__ float dw_abs_h(DW x) { return fabsf(x.h); }
 
 constexpr float kFastErr = 0x1p-38f;   // bound factor on the absolute-value expression
 constexpr float kFastFloor = 0x1p-100f;
+// For the conic's short chains (one to four operations from exact or split
+// inputs) the sum of both evaluations' errors is below 2^-43.7 x the
+// absolute-value expression; 2^-42 keeps a margin of three and leaves the
+// 1 / r amplification near the centre room.
+constexpr float kFastErrShort = 0x1p-42f;
 
 // The f32 that every value within e of x rounds to, clamped to [0, 1]
 // (round and clamp commute: 0 and 1 are floats); false when they differ.
@@ -263,8 +268,8 @@ __device__ __forceinline__ int fast_conic(const GradFast &F, bool has_tf, float 
     float ax, ay;
     fast_point(F, has_tf, fx, fy, px, py, ax, ay);
     const DW dx = dw_sub(px, F.g0), dy = dw_sub(py, F.g1);
-    const float ex = (ax + dw_abs_h(F.g0)) * kFastErr + kFastFloor;
-    const float ey = (ay + dw_abs_h(F.g1)) * kFastErr + kFastFloor;
+    const float ex = (ax + dw_abs_h(F.g0)) * kFastErrShort + kFastFloor;
+    const float ey = (ay + dw_abs_h(F.g1)) * kFastErrShort + kFastFloor;
     // (|x.l| <= 2^-24 |x.h|: the 0.99999 factors cover the low words)
     const float r_lo = fmaxf(fabsf(dx.h) * 0.99999f - ex, fabsf(dy.h) * 0.99999f - ey);
     if (!(r_lo > 0.0f)) return 0;
@@ -284,18 +289,20 @@ __device__ __forceinline__ int fast_conic(const GradFast &F, bool has_tf, float 
     if (swap) th = dw_sub(kDwPi2, th);
     if (dx.h < 0.0f) th = dw_sub(kDwPi, th);
     if (dy.h < 0.0f) th = dw_neg(th);
-    const float eth = 2.0f * (ex + ey) / r_lo + 0x1p-36f;
+    // atan2's own error: below 2^-43.5 for this evaluation (absolute, the
+    // angle is at most pi), below 2^-51 for fdlibm's
+    const float eth = 2.0f * (ex + ey) / r_lo + kFastErr;
     const DW v = dw_sub(th, F.k[0]);
-    const float ev = eth + (fabsf(th.h) + dw_abs_h(F.k[0])) * kFastErr + kFastFloor;
+    const float ev = eth + (fabsf(th.h) + dw_abs_h(F.k[0])) * kFastErrShort + kFastFloor;
     if (!(fabsf(v.h) * 0.99999f > ev)) return 0;  // at the wrap to 2 pi
     DW ang = v;
     if (v.h < 0.0f) {
         const DW u = dw_add(v, kDwTwoPi);
-        if (!(fabsf(u.h) * 0.99999f > ev + 8.0f * kFastErr)) return 0;  // at -2 pi
+        if (!(fabsf(u.h) * 0.99999f > ev + 8.0f * kFastErrShort)) return 0;  // at -2 pi
         ang = u.h > 0.0f ? u : dw_add(u, kDwTwoPi);
     }
     const DW t = dw_mul(ang, kDwInvTwoPi);
-    const float et = (ev + 16.0f * kFastErr) * 0.16f + fabsf(t.h) * kFastErr + kFastFloor;
+    const float et = (ev + 16.0f * kFastErrShort) * 0.16f + fabsf(t.h) * kFastErrShort + kFastFloor;
     return dw_round(t, et, false, out) ? 1 : 0;
 }
 

@@ -108,6 +108,10 @@ def load(build_if_missing: bool = True):
         lib.z2dgpu_gradient_offsets.argtypes = [C.c_void_p, P(abi.z2d_gradient), C.c_int32, C.c_int32, C.c_int32,
                                                 C.c_int32, C.c_void_p, P(C.c_int64)]
         lib.z2dgpu_gradient_offsets.restype = C.c_int
+        lib.z2dgpu_build_paths.argtypes = [C.c_void_p, P(abi.z2d_path_program), C.c_size_t, P(abi.z2d_path_cmd),
+                                           C.c_size_t, P(abi.z2d_glyph_point), C.c_size_t, P(C.c_uint16),
+                                           C.c_size_t, C.c_void_p, C.c_size_t, P(C.c_uint64), P(C.c_int32)]
+        lib.z2dgpu_build_paths.restype = C.c_int
         for name in ("z2dgpu_server_create", "z2dgpu_server_create2", "z2dgpu_server_submit",
                      "z2dgpu_server_submit_new", "z2dgpu_server_wait", "z2dgpu_server_stats", "z2dgpu_server_info",
                      "z2dgpu_server_destroy"):
