@@ -296,6 +296,8 @@ int make_dev_src_from_pattern(int param_kind, const z2d_pattern &p, DevSrc &out,
         const int rc = make_dev_gradient(*p.gradient, grad_out);
         if (rc) return rc;
         needs_grad = true;
+        out.grad_type = grad_out.type;
+        out.grad_method = grad_out.method;
     }
     if (out.kind == SRC_DITHER) {
         if (p.dither_type < Z2D_DITHER_NONE || p.dither_type > Z2D_DITHER_BLUE_NOISE || p.dither_scale < 1 || p.dither_scale > 15 ||

@@ -226,7 +226,7 @@ int launch_composite(Ctx &c, const CompJob &J) {
         if (o.src.kind == SRC_SURFACE && (o.src.sfc.w != J.dst.w || o.src.sfc.h < J.dst.h)) flat = false;
     }
     cudaEvent_t t0 = c.timer_begin(c.t_composite);
-    if (try_mask_batch(c, J, flat)) {
+    if (try_mask_batch(c, J, flat) || try_mask_grad(c, J, flat)) {
     } else if (J.precision == Z2D_PRECISION_FLOAT) {
         launch_fmt<Z2D_PRECISION_FLOAT>(c, J, flat);
     } else {

@@ -21,6 +21,7 @@
 // Z2D_ERR_INVALID_ARGUMENT); its nodes up to there are kept, as in z2d.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "z2d_internal.h"
@@ -80,10 +81,13 @@ __device__ __forceinline__ double clamp_i24(double v) { return fmax(-8388608.0, 
 constexpr int kErrNoCurrentPoint = Z2D_ERR_INVALID_STATE;
 constexpr int kErrInvalidMatrix = Z2D_ERR_INVALID_ARGUMENT;
 
-// The node sink: counts, and writes when `out` is set.
+// The node sink: counts, and writes when `out` is set.  A reset or a
+// rolled-back glyph moves n back; hw is the highest n reached, the room the
+// program needs while it runs.
 struct Sink {
     z2d_node *out;
     long long n;
+    long long hw;
     __device__ void put(int32_t tag, double a = 0, double b = 0, double c = 0, double d = 0, double e = 0,
                         double f = 0) {
         if (out) {
@@ -98,6 +102,7 @@ struct Sink {
             nd.p[5] = f;
         }
         n++;
+        if (n > hw) hw = n;
     }
 };
 
@@ -455,9 +460,9 @@ struct BuildArgs {
     int64_t n_gpts;
     const uint16_t *gends;
     int64_t n_gends;
-    const unsigned long long *offsets;  // emit pass: each program's first node
+    const unsigned long long *offsets;  // emit pass: each program's room in `nodes`
     z2d_node *nodes;
-    unsigned long long *counts;  // count pass
+    unsigned long long *counts;  // count pass: nodes kept, then room needed (2 per program)
     int32_t *status;
 };
 
@@ -465,7 +470,7 @@ __global__ void k_build_paths(const BuildArgs A) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= A.n_progs) return;
     const z2d_path_program &pg = A.progs[p];
-    Sink sink{A.nodes ? A.nodes + A.offsets[p] : nullptr, 0};
+    Sink sink{A.nodes ? A.nodes + A.offsets[p] : nullptr, 0, 0};
     PathState P;
     P.tf = Tf{pg.transformation[0], pg.transformation[1], pg.transformation[2], pg.transformation[3],
               pg.transformation[4], pg.transformation[5]};
@@ -522,8 +527,21 @@ __global__ void k_build_paths(const BuildArgs A) {
             default: P.err = Z2D_ERR_INVALID_ARGUMENT; break;
         }
     }
-    if (A.counts) A.counts[p] = (unsigned long long)sink.n;
+    if (A.counts) {
+        A.counts[2 * p] = (unsigned long long)sink.n;
+        A.counts[2 * p + 1] = (unsigned long long)sink.hw;
+    }
     if (A.status) A.status[p] = P.err;
+}
+
+// Programs whose room exceeded their kept nodes: their nodes move from the
+// room layout to the packed one (one CTA per program).
+__global__ void k_pack_nodes(const unsigned long long *__restrict__ room, const unsigned long long *__restrict__ out_off,
+                             int64_t n_progs, const z2d_node *__restrict__ src, z2d_node *__restrict__ dst) {
+    for (int64_t p = blockIdx.x; p < n_progs; p += gridDim.x) {
+        const unsigned long long s = room[p], d = out_off[p], n = out_off[p + 1] - out_off[p];
+        for (unsigned long long k = threadIdx.x; k < n; k += blockDim.x) dst[d + k] = src[s + k];
+    }
 }
 
 }  // namespace
@@ -548,10 +566,13 @@ int build_paths(Ctx &c, const z2d_path_program *progs, size_t n_progs, const z2d
     const size_t o_gpts = o_cmds + al(sizeof(z2d_path_cmd) * n_cmds);
     const size_t o_gends = o_gpts + al(sizeof(z2d_glyph_point) * n_gpts);
     const size_t o_cnt = o_gends + al(sizeof(uint16_t) * n_gends);
-    const size_t o_st = o_cnt + al(sizeof(unsigned long long) * (n_progs + 1));
+    const size_t o_room = o_cnt + al(sizeof(unsigned long long) * 2 * n_progs);
+    const size_t o_out = o_room + al(sizeof(unsigned long long) * (n_progs + 1));
+    const size_t o_st = o_out + al(sizeof(unsigned long long) * (n_progs + 1));
     const size_t in_bytes = o_cnt;
     const size_t total = o_st + al(sizeof(int32_t) * n_progs);
-    if (c.params.ensure(total) || c.staging.ensure(in_bytes + 16)) return Z2D_ERR_OUT_OF_MEMORY;
+    if (c.params.ensure(total) || c.staging.ensure(std::max(in_bytes, sizeof(unsigned long long) * 2 * (n_progs + 1)) + 16))
+        return Z2D_ERR_OUT_OF_MEMORY;
     Z2D_CUDA(cudaStreamSynchronize(c.stream));
     uint8_t *h = c.staging.as<uint8_t>(), *dv = c.params.as<uint8_t>();
     memcpy(h + o_progs, progs, sizeof(z2d_path_program) * n_progs);
@@ -568,40 +589,60 @@ int build_paths(Ctx &c, const z2d_path_program *progs, size_t n_progs, const z2d
     A.gends = reinterpret_cast<const uint16_t *>(dv + o_gends);
     A.n_gends = (int64_t)n_gends;
     unsigned long long *d_cnt = reinterpret_cast<unsigned long long *>(dv + o_cnt);
+    unsigned long long *d_room = reinterpret_cast<unsigned long long *>(dv + o_room);
+    unsigned long long *d_out = reinterpret_cast<unsigned long long *>(dv + o_out);
     int32_t *d_st = reinterpret_cast<int32_t *>(dv + o_st);
     const unsigned blocks = (unsigned)((n_progs + 127) / 128);
-    // count pass
+    // count pass: nodes kept and room needed per program
     A.offsets = nullptr;
     A.nodes = nullptr;
     A.counts = d_cnt;
     A.status = d_st;
     k_build_paths<<<blocks, 128, 0, c.stream>>>(A);
     c.launches++;
-    std::vector<unsigned long long> cnt(n_progs);
-    Z2D_CUDA(cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(unsigned long long) * n_progs, cudaMemcpyDeviceToHost,
+    std::vector<unsigned long long> cnt(2 * n_progs), room(n_progs + 1);
+    Z2D_CUDA(cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(unsigned long long) * 2 * n_progs, cudaMemcpyDeviceToHost,
                              c.stream));
     Z2D_CUDA(cudaStreamSynchronize(c.stream));
-    unsigned long long tot = 0;
+    unsigned long long tot = 0, rtot = 0;
+    bool packed = true;
     for (size_t p = 0; p < n_progs; p++) {
         offsets[p] = tot;
-        tot += cnt[p];
+        room[p] = rtot;
+        tot += cnt[2 * p];
+        rtot += cnt[2 * p + 1];
+        packed = packed && cnt[2 * p] == cnt[2 * p + 1];
     }
     offsets[n_progs] = tot;
+    room[n_progs] = rtot;
     if (tot > cap_nodes) {
         set_error("build_paths: the node array holds fewer nodes than the programs build (offsets are filled)");
         return Z2D_ERR_OUT_OF_MEMORY;
     }
-    // emit pass into device scratch, then to the caller
-    if (c.edges.ensure(sizeof(z2d_node) * (size_t)std::max<unsigned long long>(tot, 1))) return Z2D_ERR_OUT_OF_MEMORY;
-    Z2D_CUDA(cudaMemcpyAsync(d_cnt, offsets, sizeof(unsigned long long) * n_progs, cudaMemcpyHostToDevice,
-                             c.stream));
-    A.offsets = d_cnt;
+    // emit pass into device scratch laid out by room, packed when a reset or
+    // a rolled-back glyph left a program with fewer nodes than its room,
+    // then to the caller
+    const size_t scratch = (size_t)std::max<unsigned long long>(rtot, 1) + (packed ? 0 : (size_t)std::max<unsigned long long>(tot, 1));
+    if (c.edges.ensure(sizeof(z2d_node) * scratch)) return Z2D_ERR_OUT_OF_MEMORY;
+    memcpy(h, room.data(), sizeof(unsigned long long) * (n_progs + 1));
+    memcpy(h + sizeof(unsigned long long) * (n_progs + 1), offsets, sizeof(unsigned long long) * (n_progs + 1));
+    Z2D_CUDA(cudaMemcpyAsync(d_room, h, sizeof(unsigned long long) * (n_progs + 1), cudaMemcpyHostToDevice, c.stream));
+    Z2D_CUDA(cudaMemcpyAsync(d_out, h + sizeof(unsigned long long) * (n_progs + 1),
+                             sizeof(unsigned long long) * (n_progs + 1), cudaMemcpyHostToDevice, c.stream));
+    A.offsets = d_room;
     A.nodes = c.edges.as<z2d_node>();
     A.counts = nullptr;
     k_build_paths<<<blocks, 128, 0, c.stream>>>(A);
     c.launches++;
+    z2d_node *result = A.nodes;
+    if (!packed) {
+        result = A.nodes + std::max<unsigned long long>(rtot, 1);
+        const unsigned pb = (unsigned)std::min<size_t>(n_progs, (size_t)c.sm_count * 16);
+        k_pack_nodes<<<pb, 128, 0, c.stream>>>(d_room, d_out, (int64_t)n_progs, A.nodes, result);
+        c.launches++;
+    }
     Z2D_CUDA(cudaGetLastError());
-    if (tot) Z2D_CUDA(cudaMemcpyAsync(nodes, A.nodes, sizeof(z2d_node) * (size_t)tot, cudaMemcpyDefault, c.stream));
+    if (tot) Z2D_CUDA(cudaMemcpyAsync(nodes, result, sizeof(z2d_node) * (size_t)tot, cudaMemcpyDefault, c.stream));
     if (status) Z2D_CUDA(cudaMemcpyAsync(status, d_st, sizeof(int32_t) * n_progs, cudaMemcpyDeviceToHost, c.stream));
     Z2D_CUDA(cudaStreamSynchronize(c.stream));
     return Z2D_OK;

@@ -250,6 +250,9 @@ bool try_mask_batch(Ctx &c, const CompJob &J, bool flat);
 // when the surface does not fit the kernel's layout.
 bool launch_mask_float(Ctx &c, uint8_t *dst, int fmt, const uint8_t *mask, size_t px, int op, const F4 &spf);
 bool launch_mask_packed(Ctx &c, uint8_t *dst, int fmt, const uint8_t *mask, size_t px, int op, const I16 &spx);
+// The same batch with a gradient or dithered-gradient source on the 4-byte
+// formats in integer precision (composite_grad.cu).
+bool try_mask_grad(Ctx &c, const CompJob &J, bool flat);
 // Path programs built on the device (path_build.cu).
 int build_paths(Ctx &c, const z2d_path_program *progs, size_t n_progs, const z2d_path_cmd *cmds, size_t n_cmds,
                 const z2d_glyph_point *gpts, size_t n_gpts, const uint16_t *gends, size_t n_gends, z2d_node *nodes,

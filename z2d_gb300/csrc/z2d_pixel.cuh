@@ -702,8 +702,11 @@ Z2D_D RGBf interp_linear_prep(int method, RGBf am, RGBf bm, float t) {
 }
 
 // -------------------------------------------------------------- dither
-// one copy per translation unit, so no relocatable device code is needed
-static __constant__ uint16_t c_blue_noise[4096] = {
+// one copy per translation unit, so no relocatable device code is needed.
+// Global memory read through the read-only cache, not __constant__: the
+// lanes of a warp read 32 different entries, which the constant cache
+// would serialise.
+static __device__ const uint16_t g_blue_noise[4096] = {
 #include "blue_noise_64x64.inc"
 };
 
@@ -716,7 +719,7 @@ Z2D_D float blue_noise(int32_t x, int32_t y) {
     int32_t xm = x % 64, ym = y % 64;
     if (xm < 0) xm += 64;
     if (ym < 0) ym += 64;
-    return (float)c_blue_noise[(xm << 6) | ym] * (2.0f / 8192.0f) - (4095.0f / 8192.0f);
+    return (float)__ldg(&g_blue_noise[(xm << 6) | ym]) * (2.0f / 8192.0f) - (4095.0f / 8192.0f);
 }
 
 // ---------------------------------------------------------- sources
@@ -733,6 +736,7 @@ struct DevSrc {
     Px px;             // the pixel in its own format (fast paths)
     DevSurface sfc;    // SURFACE
     const DevGradient *grad;
+    int32_t grad_type, grad_method;  // the gradient's kind and method, for choosing a kernel on the host
 };
 
 Z2D_D RGBf dither_linear(const DevSrc &s, int32_t x, int32_t y) {
