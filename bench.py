@@ -1081,6 +1081,18 @@ def run_ours(args):
         "config": {"workload": f"plain_large_{W}x{H}_{N_FILLS}_paths", "surface": f"rgba {W}x{H}",
                    "paths": N_FILLS, "mpix_per_step": mpix_step, "l2": "flushed (256 MiB write) before each step",
                    "mode": "batched (z2dgpu_fill_batch, device-resident surface)"},
+        "summary": {
+            "batched_mpix_s": value, "e2e_mpix_s": e2e_value, "plain_mpix_s": plain_mpix / (plain_ms / 1e3),
+            "plain_p50_us": call_us[len(call_us) // 2],
+            "star_300_p50_us": star["device"]["p50_us"] if star else None,
+            "batched_over_plain": (mpix_step / (total_ms / args.steps / 1e3)) / (plain_mpix / (plain_ms / 1e3)),
+            "jobs_batched_over_per_surface": (jobs["value"] / jobs["per_surface"]["value"]
+                                              if jobs and jobs.get("per_surface") else None),
+            "c2_bit_exact": parity["bit_exact"] if parity else None,
+            "c4_bit_exact": (jobs["parity"]["differing_pixels"] == 0 if jobs and jobs.get("parity") else None),
+            "c5_bit_exact": (serving["parity"]["differing_requests"] == 0
+                             if serving and serving.get("parity") else None),
+        },
         "stage_ms_per_step": stage,
         "plain": {"value": plain_mpix / (plain_ms / 1e3), "unit": "Mpix/s", "ms": plain_ms,
                   "calls": PLAIN_FILLS, "note": f"z2dgpu_fill per path, first {PLAIN_FILLS} fills",

@@ -26,8 +26,16 @@ constexpr int kGradThreads = 256;
 
 enum : int { kLinRGB = 0, kSRGB = 1, kHSL = 2 };
 
+// Out of line: the f64 offsets (taken for a pixel in thousands) and
+// std.math.pow (three per sRGB pixel), so that each instantiation's loop
+// stays small enough for the instruction cache.
+__device__ __noinline__ float offset_f64_call(const DevGradient &g, int32_t x, int32_t y) {
+    return grad_offset_f64(g, x, y);
+}
+__device__ __noinline__ float gamma_call(float x) { return zpow(x, kGamma); }
+
 template <int KIND>
-__device__ __forceinline__ float offset_of(const DevGradient &g, int32_t x, int32_t y) {
+__device__ __forceinline__ float offset_inline(const DevGradient &g, int32_t x, int32_t y) {
     // the kind is known here, so only its evaluation is compiled in
     if ((uint32_t)(x + (1 << 22)) < (1u << 23) && (uint32_t)(y + (1 << 22)) < (1u << 23)) {
         const int32_t mode = g.fz.mode;
@@ -43,7 +51,23 @@ __device__ __forceinline__ float offset_of(const DevGradient &g, int32_t x, int3
             if (done) return t;
         }
     }
-    return grad_offset_f64(g, x, y);
+    return offset_f64_call(g, x, y);
+}
+
+// The linear offset inline; the radial and conic evaluations (several
+// times its code) out of line, one copy per kind.
+template <int KIND>
+__device__ __noinline__ float offset_call(const DevGradient &g, int32_t x, int32_t y) {
+    return offset_inline<KIND>(g, x, y);
+}
+template <int KIND>
+__device__ __forceinline__ float offset_of(const DevGradient &g, int32_t x, int32_t y) {
+    if constexpr (KIND == Z2D_GRADIENT_LINEAR) return offset_inline<KIND>(g, x, y);
+    else return offset_call<KIND>(g, x, y);
+}
+// HSL.interpolate + toLinearRGB, out of line (fmod and the hue cases)
+__device__ __noinline__ RGBf hsl_call(RGBf a, RGBf b, float t, int method) {
+    return hsl_to_rgb(hsl_lerp_demul(a, b, t, method));
 }
 
 // The source's colour lanes at (x, y): interpolateEncode, or the dithered
@@ -52,15 +76,27 @@ template <int KIND, int METHOD, bool DITH>
 __device__ __forceinline__ I16 grad_lanes(const DevSrc &s, const DevGradient &g, int32_t x, int32_t y) {
     const Search r = grad_search(g, offset_of<KIND>(g, x, y));
     const RGBf a = stop_prep(g, r.i0), b = stop_prep(g, r.i1);
+    // (SRGB.interpolate then toLinearRGB, as interp_encode_prep /
+    // interp_linear_prep do, with the gamma out of line)
     if constexpr (!DITH) {
-        if constexpr (METHOD == kLinRGB) return interp_encode_prep(Z2D_INTERP_LINEAR_RGB, a, b, r.offset);
-        else if constexpr (METHOD == kSRGB) return interp_encode_prep(Z2D_INTERP_SRGB, a, b, r.offset);
-        else return encode_linear(hsl_to_rgb(hsl_lerp_demul(a, b, r.offset, g.method)));
+        if constexpr (METHOD == kLinRGB) {
+            return interp_encode_prep(Z2D_INTERP_LINEAR_RGB, a, b, r.offset);
+        } else if constexpr (METHOD == kSRGB) {
+            const RGBf d = rgb_lerp_demul(a, b, r.offset);
+            return encode_linear(RGBf{gamma_call(d.r), gamma_call(d.g), gamma_call(d.b), d.a});
+        } else {
+            return encode_linear(hsl_call(a, b, r.offset, g.method));
+        }
     } else {
         RGBf c;
-        if constexpr (METHOD == kLinRGB) c = rgb_lerp_demul(a, b, r.offset);
-        else if constexpr (METHOD == kSRGB) c = interp_linear_prep(Z2D_INTERP_SRGB, a, b, r.offset);
-        else c = hsl_to_rgb(hsl_lerp_demul(a, b, r.offset, g.method));
+        if constexpr (METHOD == kLinRGB) {
+            c = rgb_lerp_demul(a, b, r.offset);
+        } else if constexpr (METHOD == kSRGB) {
+            const RGBf d = rgb_lerp_demul(a, b, r.offset);
+            c = RGBf{gamma_call(d.r), gamma_call(d.g), gamma_call(d.b), d.a};
+        } else {
+            c = hsl_call(a, b, r.offset, g.method);
+        }
         const float m = s.dither_type == Z2D_DITHER_BAYER ? bayer(x, y) : blue_noise(x, y);
         const float scale = 1.0f / (float)((1 << s.dither_scale) - 1);
         return encode_linear(RGBf{fmaxf(0.0f, fminf(c.r + m * scale, 1.0f)), fmaxf(0.0f, fminf(c.g + m * scale, 1.0f)),
@@ -90,7 +126,7 @@ __global__ void __launch_bounds__(kGradThreads) k_mask_grad(uint8_t *__restrict_
             const I16 sl = grad_lanes<KIND, METHOD, DITH>(src, g, px, py);
             // IntegerOps.dstIn(d = source, s = mask), then the operator
             const I16 rl = int_op(Z2D_OP_DST_IN, sl, I16{0u, 0u, 0u, (mw >> (8 * j)) & 0xFFu});
-            w[j] = i16_to_word(int_op(op, word_to_i16(w[j], fmt), rl), fmt);
+            w[j] = i16_to_word(int_op_any(op, word_to_i16(w[j], fmt), rl), fmt);
             if (++px == W) {
                 px = 0;
                 py++;
