@@ -695,6 +695,13 @@ static int do_fill_batch(Ctx &c, z2d_surface *surface, const z2d_node *nodes, si
     jobs[0].fill0 = 0;
     jobs[0].fill1 = (int32_t)fills.size();
     const DevSurface ds = jobs[0].sfc;
+    if (fills.size() == 1) {  // a single short path: one upload, one launch
+        bool done = false;
+        rc = run_small_fill(c, jobs[0], nodes, fills[0], grad_of_fill[0] >= 0 ? &grads[(size_t)grad_of_fill[0]] : nullptr,
+                            done);
+        if (rc) return rc;
+        if (done) return stage_out(c, *surface, ds);
+    }
     rc = run_jobs(c, jobs, nodes, (int32_t)n_nodes, fills, grads, grad_of_fill);
     if (rc) return rc;
     return stage_out(c, *surface, ds);
@@ -1461,11 +1468,16 @@ Z2D_API int z2dgpu_ctx_destroy(z2dgpu_ctx *c) {
     cudaStreamSynchronize(c->stream);
     DevBuf *bufs[] = {&c->params, &c->nodes, &c->node_info, &c->edges, &c->fill_state, &c->counters, &c->band_fills,
                       &c->bins, &c->bin_offsets, &c->masks, &c->surface, &c->surface2, &c->surface3, &c->scan_tmp,
-                      &c->stroke_a, &c->stroke_b, &c->stroke_c, &c->curve_pool, &c->tile_order};
+                      &c->stroke_a, &c->stroke_b, &c->stroke_c, &c->curve_pool, &c->tile_order, &c->pad_buf,
+                      &c->small_params};
     for (DevBuf *b : bufs) b->release();
     c->tune_collect(true);
     c->staging.release();
     c->readback.release();
+    for (int i = 0; i < 2; i++) {
+        c->small_stage[i].release();
+        if (c->small_done[i]) cudaEventDestroy(c->small_done[i]);
+    }
     for (Ctx::Timer *t : {&c->t_raster, &c->t_composite, &c->t_flatten, &c->t_bins, &c->t_stroke, &c->t_export}) c->timer_collect(*t);
     if (c->copy_stream) {
         cudaStreamSynchronize(c->copy_stream);

@@ -1538,6 +1538,20 @@ __global__ void k_node_owner(const FillCmd *__restrict__ fills, int32_t n_fills,
 // ----------------------------------------------------------- host side
 static inline unsigned grid_for(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
+// k_raster's shared-memory attributes: per device, set once on each.
+static int raster_attributes(Ctx &c) {
+    static std::atomic<uint64_t> attr_set{0};
+    const uint64_t dev_bit = 1ull << (c.device & 63);
+    if (attr_set.load(std::memory_order_relaxed) & dev_bit) return Z2D_OK;
+    const size_t smem = sizeof(uint32_t) * kWarpWords * kTileRows;
+    for (auto k : {k_raster<false, false>, k_raster<true, false>, k_raster<false, true>, k_raster<true, true>}) {
+        Z2D_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        Z2D_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    }
+    attr_set.fetch_or(dev_bit, std::memory_order_relaxed);
+    return Z2D_OK;
+}
+
 int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n_nodes, std::vector<FillCmd> &fills,
              const std::vector<DevGradient> &grads,
              const std::vector<int32_t> &grad_of_fill, const StrokeSet *strokes) {
@@ -1890,15 +1904,9 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     A.n_jobs = n_jobs;
     A.job0 = jobs[0];
     const size_t smem = sizeof(uint32_t) * kWarpWords * kTileRows;
-    // function attributes are per device: set once on each
-    static std::atomic<uint64_t> attr_set{0};
-    const uint64_t dev_bit = 1ull << (c.device & 63);
-    if (!(attr_set.load(std::memory_order_relaxed) & dev_bit)) {
-        for (auto k : {k_raster<false, false>, k_raster<true, false>, k_raster<false, true>, k_raster<true, true>}) {
-            Z2D_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            Z2D_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-        }
-        attr_set.fetch_or(dev_bit, std::memory_order_relaxed);
+    {
+        const int rc = raster_attributes(c);
+        if (rc) return rc;
     }
     {
         const int rc = c.await_surface();  // a host surface's upload
@@ -1977,6 +1985,354 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     c.launches++;
     Z2D_CUDA(cudaGetLastError());
     return pads.finish(c);
+}
+
+// ------------------------------------------------------- small fills
+// One fill of a short path: everything up to the rasteriser runs on the
+// host (a few microseconds for a few hundred edges) and reaches the device
+// in one upload, so the call costs one copy and one launch instead of the
+// pipeline's launches and size readbacks.  The host steps restate the same
+// z2d code as the device kernels, with the same f64 operations in the same
+// order (the host is compiled without FP contraction), so the edges, the
+// fill's box and the tiles are the device pipeline's; bins list a band's
+// edges in any order (the rasteriser's sums do not depend on it).
+namespace {
+
+constexpr int32_t kSmallMaxNodes = 4096;
+constexpr size_t kSmallMaxEdges = 8192;
+constexpr size_t kSmallMaxBins = 1 << 17;
+constexpr int kSmallMaxDepth = 40;  // below the device subdivision bound
+
+struct HostFlatten {
+    const FillCmd &F;
+    std::vector<DEdge> &edges;
+    double et = 0, eb = 0, el = 0, er = 0;
+    bool any = false, overflow = false;
+    // PointBuffer(1, 3) of fill_plotter: its first and last points and length
+    double fx = 0, fy = 0, lx = 0, ly = 0;
+    int count = 0;
+
+    // Polygon.addEdge (Polygon.zig:61-109), as add_edge in edges.cuh
+    void edge(double x0, double y0, double x1, double y1) {
+        if (edges.size() >= kSmallMaxEdges) {
+            overflow = true;
+            return;
+        }
+        const double ax = x0 * F.edge_scale, ay = y0 * F.edge_scale, bx = x1 * F.edge_scale, by = y1 * F.edge_scale;
+        DEdge e{};
+        if (ay < by) {
+            e.top = ay;
+            e.x_start = ax;
+            e.x_inc = (bx - ax) / (by - ay);
+            e.dir = -1;
+            e.rb = (int32_t)std::round(by);
+        } else if (ay > by) {
+            e.top = by;
+            e.x_start = bx;
+            e.x_inc = (ax - bx) / (ay - by);
+            e.dir = 1;
+            e.rb = (int32_t)std::round(ay);
+        } else {
+            e.rt = 1;
+            e.rb = 0;
+            edges.push_back(e);
+            return;
+        }
+        e.rt = (int32_t)std::round(e.top);
+        e.fxs = (float)e.x_start;
+        e.fxi = (float)e.x_inc;
+        e.ftp = (float)e.top;
+        const double bot = ay < by ? by : ay;
+        const double l = ax < bx ? ax : bx, r = ax < bx ? bx : ax;
+        if (!any) {
+            et = e.top, eb = bot, el = l, er = r;
+            any = true;
+        } else {
+            if (e.top < et) et = e.top;
+            if (bot > eb) eb = bot;
+            if (l < el) el = l;
+            if (r > er) er = r;
+        }
+        edges.push_back(e);
+    }
+    // lineTo through the point buffer (fill_plotter.zig:44-51, 100-118)
+    void line_to(double x, double y) {
+        if (lx == x && ly == y) return;
+        edge(lx, ly, x, y);
+        lx = x;
+        ly = y;
+        count = count < 3 ? count + 1 : 3;
+    }
+    struct K {
+        double ax, ay, bx, by, cx, cy, dx, dy;
+    };
+    static double error_sq(const K &k) {  // Spline.Knots.errorSq (Spline.zig:83-123)
+        double bx = k.bx - k.ax, by = k.by - k.ay, cx = k.cx - k.ax, cy = k.cy - k.ay;
+        if (k.ax != k.dx || k.ay != k.dy) {
+            const double dx = k.dx - k.ax, dy = k.dy - k.ay;
+            const double dd = dx * dx + dy * dy;
+            const double bd = bx * dx + by * dy;
+            if (bd >= dd) {
+                bx -= dx;
+                by -= dy;
+            } else {
+                bx -= bd / dd * dx;
+                by -= bd / dd * dy;
+            }
+            const double cd = cx * dx + cy * dy;
+            if (cd >= dd) {
+                cx -= dx;
+                cy -= dy;
+            } else {
+                cx -= cd / dd * dx;
+                cy -= cd / dd * dy;
+            }
+        }
+        const double be = bx * bx + by * by, ce = cx * cx + cy * cy;
+        return be > ce ? be : ce;
+    }
+    // Spline.decompose / decomposeInto (Spline.zig:37-79): depth-first, the
+    // first half before the second, leaves' start points then d
+    bool curve(const double *p) {
+        const double ax = lx, ay = ly;
+        if (ax == p[0] && ay == p[1] && p[2] == p[4] && p[3] == p[5]) {
+            line_to(p[4], p[5]);
+            return true;
+        }
+        const double tol2 = F.tol * F.tol;
+        struct Item {
+            K k;
+            int depth;
+        };
+        Item stack[kSmallMaxDepth + 2];
+        int top = 0;
+        stack[top++] = Item{K{ax, ay, p[0], p[1], p[2], p[3], p[4], p[5]}, 0};
+        auto half = [](double a, double b) { return a + ((b - a) / 2); };
+        while (top > 0) {
+            Item it = stack[--top];
+            K &k = it.k;
+            if (error_sq(k) < tol2) {
+                if (!(k.ax == ax && k.ay == ay)) line_to(k.ax, k.ay);
+                if (overflow) return true;
+                continue;
+            }
+            if (it.depth >= kSmallMaxDepth) return false;
+            // deCasteljau: k becomes the first half, s2 the second
+            const double abx = half(k.ax, k.bx), aby = half(k.ay, k.by);
+            const double bcx = half(k.bx, k.cx), bcy = half(k.by, k.cy);
+            const double cdx = half(k.cx, k.dx), cdy = half(k.cy, k.dy);
+            const double abbcx = half(abx, bcx), abbcy = half(aby, bcy);
+            const double bccdx = half(bcx, cdx), bccdy = half(bcy, cdy);
+            const double fx_ = half(abbcx, bccdx), fy_ = half(abbcy, bccdy);
+            const K s2{fx_, fy_, bccdx, bccdy, cdx, cdy, k.dx, k.dy};
+            const K s1{k.ax, k.ay, abx, aby, abbcx, abbcy, fx_, fy_};
+            stack[top++] = Item{s2, it.depth + 1};
+            stack[top++] = Item{s1, it.depth + 1};
+        }
+        line_to(p[4], p[5]);
+        return true;
+    }
+    // fill_plotter.plot (fill_plotter.zig:21-97); false: not for this path
+    bool plot(const z2d_node *nodes, int32_t n, bool &open_chain) {
+        for (int32_t i = 0; i < n && !overflow; i++) {
+            const z2d_node &nd = nodes[i];
+            switch (nd.tag) {
+                case Z2D_MOVE_TO:
+                    if (i == n - 1) return true;  // the auto-added move_to after close_path
+                    fx = lx = nd.p[0];
+                    fy = ly = nd.p[1];
+                    count = 1;
+                    break;
+                case Z2D_LINE_TO:
+                    if (count == 0) return false;  // InvalidState: the pipeline reports it
+                    line_to(nd.p[0], nd.p[1]);
+                    break;
+                case Z2D_CURVE_TO:
+                    if (count == 0) return false;
+                    if (!curve(nd.p)) return false;
+                    break;
+                default:  // close_path
+                    if (count >= 3) {
+                        if (!(lx == fx && ly == fy)) {
+                            edge(lx, ly, fx, fy);
+                            lx = fx;
+                            ly = fy;
+                        }
+                    } else if (count > 0 && !(lx == fx && ly == fy)) {
+                        open_chain = true;
+                    }
+                    break;
+            }
+        }
+        return !overflow;
+    }
+};
+
+}  // namespace
+
+int run_small_fill(Ctx &c, DevJob &job, const z2d_node *nodes, const FillCmd &F, const DevGradient *grad, bool &done) {
+    done = false;
+    if (F.aa != Z2D_AA_MULTISAMPLE_4X || F.stroke >= 0 || F.poly >= 0 || F.n_nodes > kSmallMaxNodes ||
+        F.n_nodes <= 0 || fmt_packed(job.sfc.fmt))
+        return Z2D_OK;
+    if (grad && grad->n_stops > kMaxStops) return Z2D_OK;
+    // ---- flatten (fill_plotter.plot)
+    static thread_local std::vector<DEdge> edges;
+    edges.clear();
+    HostFlatten H{F, edges};
+    bool open_chain = false;
+    if (!H.plot(nodes + F.node_off, F.n_nodes, open_chain) || open_chain) return Z2D_OK;
+    const int32_t sw = job.sfc.w, sh = job.sfc.h;
+    // ---- k_fill_setup: Polygon.inBox, then multisample.run's draw box
+    FillState S{};
+    S.n_edges = (int32_t)edges.size();
+    S.has_edges = H.any ? 1 : 0;
+    done = true;
+    if (!H.any || H.er < 0.0 || H.eb < 0.0) return Z2D_OK;  // nothing is drawn
+    const double sc = F.scale;
+    {
+        const int32_t psx = (int32_t)std::floor(H.el / sc), psy = (int32_t)std::floor(H.et / sc);
+        const int32_t pex = (int32_t)std::ceil(H.er / sc), pey = (int32_t)std::ceil(H.eb / sc);
+        const int32_t pw = pex - psx, ph = pey - psy;
+        if (pw == 0 || ph == 0 || psx + pw < 0 || psy + ph < 0 || psx >= sw || psy >= sh) return Z2D_OK;
+    }
+    auto clampi_h = [](int32_t v, int32_t lo, int32_t hi) { return std::max(lo, std::min(v, hi)); };
+    S.active = 1;
+    S.start_y = clampi_h((int32_t)std::floor(H.et / 4.0), 0, sh - 1);
+    S.end_y = clampi_h((int32_t)std::ceil(H.eb / 4.0), S.start_y, sh - 1);
+    S.start_x = clampi_h((int32_t)std::floor(H.el / 4.0), 0, sw - 1);
+    S.end_x = clampi_h((int32_t)std::ceil(H.er / 4.0), S.start_x, sw);
+    const bool bounded = is_bounded(F.op);
+    const int32_t ty0 = bounded ? S.start_y : 0, ty1 = bounded ? S.end_y : sh - 1;
+    S.band0 = ty0 / kTileRows;
+    S.band1 = ty1 / kTileRows;
+    S.fb_base = 0;
+    S.cull_x0 = bounded ? S.start_x : 0;
+    S.cull_x1 = bounded ? S.end_x : sw;
+    DevJob J = job;
+    J.fill0 = 0;
+    J.fill1 = 1;
+    J.band_lo = S.band0;
+    J.band_hi = S.band1;
+    J.tcol_lo = S.cull_x0 / kTileCols;
+    J.tcol_hi = (std::max(S.cull_x1, S.cull_x0 + 1) - 1) / kTileCols;
+    J.gband_base = J.tile_base = 0;
+    J.list_base = 0;
+    const int32_t n_bands = S.band1 - S.band0 + 1;
+    const long long n_tiles = (long long)n_bands * (J.tcol_hi - J.tcol_lo + 1);
+    RasterFill R{};
+    R.start_x = S.start_x;
+    R.end_x = S.end_x;
+    R.start_y = S.start_y;
+    R.end_y = S.end_y;
+    R.meta = ((uint32_t)F.op & RF_OP_MASK) | ((uint32_t)F.aa << RF_AA_SHIFT) |
+             (F.rule == Z2D_FILL_EVEN_ODD ? RF_EVEN_ODD : 0u) | ((uint32_t)F.fast_kind << RF_FAST_SHIFT) |
+             (bounded ? RF_BOUNDED : 0u);
+    R.px = (F.src.pix.r & 0xFFu) | ((F.src.pix.g & 0xFFu) << 8) | ((F.src.pix.b & 0xFFu) << 16) |
+           ((F.src.pix.a & 0xFFu) << 24);
+    // ---- bins: each edge in the bands of its active sample rows (edge_bands)
+    static thread_local std::vector<int32_t> cnt, off, bins;
+    cnt.assign((size_t)n_bands + 1, 0);
+    const int32_t S_ = (int32_t)F.scale;
+    auto bands_of = [&](const DEdge &e, int32_t &b0, int32_t &b1) {
+        if (e.dir == 0) return false;
+        const int32_t lo = std::max(e.rt, S.start_y * S_), hi = std::min(e.rb, (S.end_y + 1) * S_);
+        if (lo >= hi) return false;
+        b0 = lo / (kTileRows * S_);
+        b1 = (hi - 1) / (kTileRows * S_);
+        return true;
+    };
+    size_t n_bins = 0;
+    for (const DEdge &e : edges) {
+        int32_t b0, b1;
+        if (!bands_of(e, b0, b1)) continue;
+        for (int32_t b = b0; b <= b1; b++) cnt[(size_t)(b - S.band0)]++;
+        n_bins += (size_t)(b1 - b0 + 1);
+    }
+    if (n_bins > kSmallMaxBins) {
+        done = false;
+        return Z2D_OK;
+    }
+    for (int32_t v : cnt)
+        if (v > kMaxBandEdges) {
+            done = false;  // the pipeline reports it
+            return Z2D_OK;
+        }
+    off.assign((size_t)n_bands + 1, 0);
+    for (int32_t b = 0; b < n_bands; b++) off[(size_t)b + 1] = off[(size_t)b] + cnt[(size_t)b];
+    bins.assign(std::max<size_t>(n_bins, 1), 0);
+    for (int32_t b = 0; b < n_bands; b++) cnt[(size_t)b] = off[(size_t)b];
+    for (size_t i = 0; i < edges.size(); i++) {
+        int32_t b0, b1;
+        if (!bands_of(edges[i], b0, b1)) continue;
+        for (int32_t b = b0; b <= b1; b++) bins[(size_t)cnt[(size_t)(b - S.band0)]++] = (int32_t)i;
+    }
+    // ---- one upload: fill, state, raster record, edges, bins, offsets,
+    // band lists, gradient
+    auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    const size_t o_fill = 0, o_st = al(sizeof(FillCmd)), o_rf = o_st + al(sizeof(FillState));
+    const size_t o_edges = o_rf + al(sizeof(RasterFill));
+    const size_t o_bins = o_edges + al(sizeof(DEdge) * std::max<size_t>(edges.size(), 1));
+    const size_t o_off = o_bins + al(sizeof(int32_t) * bins.size());
+    const size_t o_cnt = o_off + al(sizeof(int32_t) * ((size_t)n_bands + 1));
+    const size_t o_list = o_cnt + al(sizeof(int32_t) * (size_t)n_bands);
+    const size_t o_grad = o_list + al(sizeof(int4) * (size_t)n_bands);
+    const size_t total = o_grad + (grad ? al(sizeof(DevGradient)) : 0);
+    const int slot = c.small_slot;
+    c.small_slot ^= 1;
+    HostBuf &hb = c.small_stage[slot];
+    if (!c.small_done[slot]) Z2D_CUDA(cudaEventCreateWithFlags(&c.small_done[slot], cudaEventDisableTiming));
+    Z2D_CUDA(cudaEventSynchronize(c.small_done[slot]));  // the slot's previous upload has been read
+    if (hb.ensure(total) || c.small_params.ensure(total)) return Z2D_ERR_OUT_OF_MEMORY;
+    uint8_t *h = hb.as<uint8_t>(), *dv = c.small_params.as<uint8_t>();
+    FillCmd Fd = F;
+    if (grad) Fd.src.grad = reinterpret_cast<const DevGradient *>(dv + o_grad);
+    memcpy(h + o_fill, &Fd, sizeof(FillCmd));
+    memcpy(h + o_st, &S, sizeof(FillState));
+    memcpy(h + o_rf, &R, sizeof(RasterFill));
+    if (!edges.empty()) memcpy(h + o_edges, edges.data(), sizeof(DEdge) * edges.size());
+    memcpy(h + o_bins, bins.data(), sizeof(int32_t) * bins.size());
+    memcpy(h + o_off, off.data(), sizeof(int32_t) * ((size_t)n_bands + 1));
+    int32_t *bc = reinterpret_cast<int32_t *>(h + o_cnt);
+    int4 *bl = reinterpret_cast<int4 *>(h + o_list);
+    for (int32_t b = 0; b < n_bands; b++) {
+        bc[b] = 1;
+        bl[b] = make_int4(0, S.cull_x0, S.cull_x1, b);
+    }
+    if (grad) memcpy(h + o_grad, grad, sizeof(DevGradient));
+    Z2D_CUDA(cudaMemcpyAsync(dv, h, total, cudaMemcpyHostToDevice, c.stream));
+    Z2D_CUDA(cudaEventRecord(c.small_done[slot], c.stream));
+    // ---- the rasteriser, one CTA per tile
+    RasterArgs A{};
+    A.job0 = J;
+    A.jobs = nullptr;
+    A.fills = reinterpret_cast<const FillCmd *>(dv + o_fill);
+    A.st = reinterpret_cast<const FillState *>(dv + o_st);
+    A.edges = reinterpret_cast<const DEdge *>(dv + o_edges);
+    A.bins = reinterpret_cast<const int32_t *>(dv + o_bins);
+    A.bin_off = reinterpret_cast<const int32_t *>(dv + o_off);
+    A.band_count = reinterpret_cast<const int32_t *>(dv + o_cnt);
+    A.band_fills = reinterpret_cast<const int4 *>(dv + o_list);
+    A.rfills = reinterpret_cast<const RasterFill *>(dv + o_rf);
+    A.masks = nullptr;
+    A.n_jobs = 1;
+    A.queue = nullptr;
+    A.n_items = (unsigned long long)n_tiles;
+    A.order = nullptr;
+    A.one_per_tile = 1;
+    const int rc = raster_attributes(c);
+    if (rc) return rc;
+    {
+        const int rs = c.await_surface();
+        if (rs) return rs;
+    }
+    const size_t smem = sizeof(uint32_t) * kWarpWords * kTileRows;
+    cudaEvent_t t0 = c.timer_begin(c.t_raster);
+    k_raster<false, true><<<(unsigned)n_tiles, kRasterThreads, smem, c.stream>>>(A);
+    c.timer_end(c.t_raster, t0);
+    c.launches++;
+    Z2D_CUDA(cudaGetLastError());
+    return Z2D_OK;
 }
 
 }  // namespace z2dg

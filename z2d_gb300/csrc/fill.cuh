@@ -166,6 +166,15 @@ struct DevJob {
 // Nodes that no fill owns are skipped; device-stroked
 // commands (`strokes`, fills with stroke >= 0) read their nodes from the
 // same array; fills with poly >= 0 draw a host-built polygon of `strokes`.
+// One small fill on one surface with a single upload and a single launch:
+// the host flattens the path (fill_plotter.plot, Spline.decompose,
+// Polygon.addEdge), sets the fill up (inBox, multisample.run's draw box)
+// and bins its edges; the rasteriser draws the tiles.  Sets `done` = false
+// without touching the device when the fill is not one it takes (another
+// anti-aliasing mode, a stroke, an open two-point chain, too many edges or
+// bands, a packed surface), and the caller runs the full pipeline.
+int run_small_fill(Ctx &c, DevJob &job, const z2d_node *nodes, const FillCmd &F, const DevGradient *grad, bool &done);
+
 struct StrokeSet;
 int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n_nodes, std::vector<FillCmd> &fills,
              const std::vector<DevGradient> &grads,

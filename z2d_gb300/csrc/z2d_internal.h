@@ -113,6 +113,13 @@ struct Ctx {
     std::vector<stroke::Polygon> poly_cache;
     HostBuf staging;    // pinned upload staging
     HostBuf readback;   // pinned readback
+    // the one-upload path of a single small fill (fill.cu, run_small_fill):
+    // two pinned staging slots, each free again once its upload event has
+    // passed, and the device copy of the latest upload (stream ordered)
+    HostBuf small_stage[2];
+    cudaEvent_t small_done[2] = {nullptr, nullptr};
+    int small_slot = 0;
+    DevBuf small_params;
     cudaEvent_t done = nullptr;
     // upload of a host surface overlapping the flatten kernels: the copy runs
     // on copy_stream after call_start (the call's first point on `stream`);
