@@ -1097,8 +1097,9 @@ def run_ours(args):
         "plain": {"value": plain_mpix / (plain_ms / 1e3), "unit": "Mpix/s", "ms": plain_ms,
                   "calls": PLAIN_FILLS, "note": f"z2dgpu_fill per path, first {PLAIN_FILLS} fills",
                   "latency_us": {"p50": call_us[len(call_us) // 2], "p99": call_us[int(len(call_us) * 0.99) - 1],
-                                 "note": "host wall time per call (the call returns after its fill is queued "
-                                         "and its sizes are read back)"}},
+                                 "note": "host wall time per painter.fill call, Python marshalling included (a "
+                                         "short path returns once its one upload and raster launch are queued; "
+                                         "a longer one after the pipeline's size readbacks)"}},
         "star_300": star,
         "jobs": jobs,
         "serving": serving,
