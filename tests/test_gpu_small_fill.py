@@ -1,10 +1,11 @@
-"""A single fill's one-upload path against the pipeline and the oracle.
+"""The one-upload path for few short fills against the pipeline and the oracle.
 
-z2dgpu_fill with one short path flattens and bins on the host and launches
-only the rasteriser (run_small_fill); the same fill inside a batch takes
-the full device pipeline.  Each case draws the fill both ways (the batch
-adds a second fill that lies off the surface, which draws nothing) and
-compares both surfaces with the oracle's, byte for byte: lines and curves,
+A call whose fills are few and short flattens and bins on the host and
+launches only the rasteriser (run_small_jobs); a call beyond its limits
+takes the full device pipeline.  Each case draws the fill both ways (the
+pipeline's batch adds a second fill of 4,200 nodes that lies off the
+surface and draws nothing) and compares both surfaces with the oracle's,
+byte for byte: lines and curves,
 even-odd and non-zero, every operator class (bounded, unbounded, float
 only), gradient sources, paths partly or wholly off the surface, negative
 coordinates, horizontal and degenerate edges, repeated points, open
@@ -39,8 +40,12 @@ def _bg(seed, fmt="rgba"):
 
 
 def _off_surface():
+    """Off the surface, and more nodes than the one-upload path takes."""
     p = Path()
-    p.move_to(-500, -500).line_to(-400, -500).line_to(-450, -420).close()
+    p.move_to(-5000, -5000)
+    for k in range(4200):
+        p.line_to(-4000 - (k % 7), -5000 + k * 0.01)
+    p.close()
     return p.to_array()
 
 
@@ -139,3 +144,47 @@ def test_beyond_limits(gpu, oracle):
 def test_formats(gpu, oracle, fmt):
     nodes = random_path(np.random.default_rng(11), W, H, side_lo=100.0, side_hi=280.0)
     _check(gpu, oracle, Pattern.from_pixel(Pixel.rgba(80, 80, 200, 220)), nodes, FillOptions(), fmt=fmt, what=fmt)
+
+
+def _dev_jobs(oracle, specs):
+    import torch
+    dev, ref = [], []
+    for fmt, w, h, seed, fills in specs:
+        s0 = Surface.init(fmt, w, h)
+        if fmt in ("rgba", "argb"):
+            s0.data[:] = premultiplied_background(np.random.default_rng(seed), w, h)
+        dev.append(s0.to_device("cuda"))
+        r = Surface.init(fmt, w, h)
+        r.data[:] = s0.data
+        for pat, nodes, opts in fills:
+            assert oracle.fill(r, pat, nodes, opts) == abi.OK
+        ref.append(r)
+    return dev, ref
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_many_surfaces(oracle, seed):
+    """fill_jobs with a few short fills per surface: the one-upload path
+    over several surfaces (the multi-surface rasteriser), then the same jobs
+    with a large off-surface fill added to the last one (the pipeline)."""
+    import torch
+    rng = np.random.default_rng(1300 + seed)
+    specs = []
+    for j in range(int(rng.integers(2, 9))):
+        w, h = int(rng.integers(8, 260)), int(rng.integers(8, 200))
+        fills = []
+        for k in range(int(rng.integers(1, 5))):
+            nodes = random_path(rng, w, h, side_lo=4.0, side_hi=float(max(w, h)), seg_hi=16)
+            op = str(rng.choice(["src_over", "src_over", "multiply", "src_in", "xor", "hue"]))
+            fills.append((Pattern.from_pixel(Pixel.rgba(int(rng.integers(0, 120)), 90, 40, 200)), nodes,
+                          FillOptions(operator=op, fill_rule=str(rng.choice(["non_zero", "even_odd"])))))
+        specs.append((str(rng.choice(["rgba", "rgb", "alpha8"])), w, h, seed * 31 + j, fills))
+    for big in (False, True):
+        dev, ref = _dev_jobs(oracle, specs)
+        jobs = [(d, list(sp[4])) for d, sp in zip(dev, specs)]
+        if big:
+            jobs[-1][1].append((Pattern.from_pixel(Pixel.rgba(1, 2, 3, 4)), _off_surface(), FillOptions()))
+        painter.fill_jobs(jobs)
+        torch.cuda.synchronize()
+        for k, (d, r) in enumerate(zip(dev, ref)):
+            assert np.array_equal(d.to_host().numpy(), r.numpy()), f"job {k} ({'pipeline' if big else 'one upload'})"

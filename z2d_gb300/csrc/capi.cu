@@ -695,13 +695,6 @@ static int do_fill_batch(Ctx &c, z2d_surface *surface, const z2d_node *nodes, si
     jobs[0].fill0 = 0;
     jobs[0].fill1 = (int32_t)fills.size();
     const DevSurface ds = jobs[0].sfc;
-    if (fills.size() == 1) {  // a single short path: one upload, one launch
-        bool done = false;
-        rc = run_small_fill(c, jobs[0], nodes, fills[0], grad_of_fill[0] >= 0 ? &grads[(size_t)grad_of_fill[0]] : nullptr,
-                            done);
-        if (rc) return rc;
-        if (done) return stage_out(c, *surface, ds);
-    }
     rc = run_jobs(c, jobs, nodes, (int32_t)n_nodes, fills, grads, grad_of_fill);
     if (rc) return rc;
     return stage_out(c, *surface, ds);

@@ -151,7 +151,10 @@ GradKernel pick_method(int method, bool dith) {
     return dith ? k_mask_grad<KIND, kHSL, true> : k_mask_grad<KIND, kHSL, false>;
 }
 
-std::atomic<int> g_grad_occ{0};
+// Resident blocks per SM of each instantiation (3 kinds x 3 methods x
+// dither or not), looked up once: the grid is sized to what fits at once,
+// so that no block of the grid-stride loop waits for a second wave.
+std::atomic<int> g_grad_occ[3][3][2];
 
 }  // namespace
 
@@ -183,10 +186,12 @@ bool try_mask_grad(Ctx &c, const CompJob &J, bool flat) {
     GradKernel k = kind == Z2D_GRADIENT_LINEAR   ? pick_method<Z2D_GRADIENT_LINEAR>(method, dith)
                    : kind == Z2D_GRADIENT_RADIAL ? pick_method<Z2D_GRADIENT_RADIAL>(method, dith)
                                                  : pick_method<Z2D_GRADIENT_CONIC>(method, dith);
-    int occ = g_grad_occ.load(std::memory_order_relaxed);
+    const int mslot = method == Z2D_INTERP_LINEAR_RGB ? 0 : method == Z2D_INTERP_SRGB ? 1 : 2;
+    std::atomic<int> &slot = g_grad_occ[kind - Z2D_GRADIENT_LINEAR][mslot][dith ? 1 : 0];
+    int occ = slot.load(std::memory_order_relaxed);
     if (occ <= 0) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kGradThreads, 0) != cudaSuccess || occ <= 0) occ = 2;
-        g_grad_occ.store(occ, std::memory_order_relaxed);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kGradThreads, 0) != cudaSuccess || occ <= 0) occ = 1;
+        slot.store(occ, std::memory_order_relaxed);
     }
     const size_t n_chunks = px / 4;
     size_t blocks = (n_chunks + kGradThreads - 1) / kGradThreads;

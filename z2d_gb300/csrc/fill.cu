@@ -1559,6 +1559,11 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     const int32_t n_fills = (int32_t)fills.size();
     const int32_t n_jobs = (int32_t)jobs.size();
     if (n_fills == 0 || n_nodes == 0 || n_jobs == 0) return Z2D_OK;
+    if (!strokes) {  // few short fills: one upload, one launch
+        bool done = false;
+        const int rc = run_small_jobs(c, jobs, nodes, fills, grads, grad_of_fill, done);
+        if (rc || done) return rc;
+    }
     for (DevJob &J : jobs) {
         J.band_lo = J.tcol_lo = 0x7FFFFFFF;
         J.band_hi = J.tcol_hi = -1;
@@ -1998,9 +2003,11 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
 // edges in any order (the rasteriser's sums do not depend on it).
 namespace {
 
-constexpr int32_t kSmallMaxNodes = 4096;
-constexpr size_t kSmallMaxEdges = 8192;
-constexpr size_t kSmallMaxBins = 1 << 17;
+constexpr int32_t kSmallMaxNodes = 4096;       // nodes of all the call's fills
+constexpr size_t kSmallMaxEdges = 8192;        // their edges
+constexpr size_t kSmallMaxBins = 1 << 17;      // (edge, band) pairs
+constexpr long long kSmallMaxBands = 1 << 16;  // (fill, band) slots and band-list entries
+constexpr size_t kSmallMaxJobs = 4096;
 constexpr int kSmallMaxDepth = 40;  // below the device subdivision bound
 
 struct HostFlatten {
@@ -2170,114 +2177,186 @@ struct HostFlatten {
 
 }  // namespace
 
-int run_small_fill(Ctx &c, DevJob &job, const z2d_node *nodes, const FillCmd &F, const DevGradient *grad, bool &done) {
+int run_small_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, const std::vector<FillCmd> &fills,
+                   const std::vector<DevGradient> &grads, const std::vector<int32_t> &grad_of_fill, bool &done) {
     done = false;
-    if (F.aa != Z2D_AA_MULTISAMPLE_4X || F.stroke >= 0 || F.poly >= 0 || F.n_nodes > kSmallMaxNodes ||
-        F.n_nodes <= 0 || fmt_packed(job.sfc.fmt))
-        return Z2D_OK;
-    if (grad && grad->n_stops > kMaxStops) return Z2D_OK;
-    // ---- flatten (fill_plotter.plot)
-    static thread_local std::vector<DEdge> edges;
-    edges.clear();
-    HostFlatten H{F, edges};
-    bool open_chain = false;
-    if (!H.plot(nodes + F.node_off, F.n_nodes, open_chain) || open_chain) return Z2D_OK;
-    const int32_t sw = job.sfc.w, sh = job.sfc.h;
-    // ---- k_fill_setup: Polygon.inBox, then multisample.run's draw box
-    FillState S{};
-    S.n_edges = (int32_t)edges.size();
-    S.has_edges = H.any ? 1 : 0;
-    done = true;
-    if (!H.any || H.er < 0.0 || H.eb < 0.0) return Z2D_OK;  // nothing is drawn
-    const double sc = F.scale;
-    {
-        const int32_t psx = (int32_t)std::floor(H.el / sc), psy = (int32_t)std::floor(H.et / sc);
-        const int32_t pex = (int32_t)std::ceil(H.er / sc), pey = (int32_t)std::ceil(H.eb / sc);
-        const int32_t pw = pex - psx, ph = pey - psy;
-        if (pw == 0 || ph == 0 || psx + pw < 0 || psy + ph < 0 || psx >= sw || psy >= sh) return Z2D_OK;
+    const size_t n_fills = fills.size(), n_jobs = jobs.size();
+    if (n_fills == 0 || n_jobs == 0 || n_jobs > kSmallMaxJobs) return Z2D_OK;
+    long long total_nodes = 0;
+    for (const FillCmd &F : fills) {
+        if (F.aa != Z2D_AA_MULTISAMPLE_4X || F.stroke >= 0 || F.poly >= 0 || F.n_nodes <= 0) return Z2D_OK;
+        total_nodes += F.n_nodes;
     }
+    if (total_nodes > kSmallMaxNodes) return Z2D_OK;
+    for (const DevJob &J : jobs)
+        if (fmt_packed(J.sfc.fmt)) return Z2D_OK;
+    for (const DevGradient &g : grads)
+        if (g.n_stops > kMaxStops) return Z2D_OK;
+    // ---- flatten every fill (fill_plotter.plot)
+    static thread_local std::vector<DEdge> edges;
+    static thread_local std::vector<FillState> st;
+    static thread_local std::vector<RasterFill> rf;
+    static thread_local std::vector<double> ext;  // et, eb, el, er per fill
+    edges.clear();
+    st.assign(n_fills, FillState{});
+    rf.assign(n_fills, RasterFill{});
+    ext.assign(4 * n_fills, 0.0);
+    for (size_t f = 0; f < n_fills; f++) {
+        const size_t e0 = edges.size();
+        HostFlatten H{fills[f], edges};
+        bool open_chain = false;
+        if (!H.plot(nodes + fills[f].node_off, fills[f].n_nodes, open_chain) || open_chain) return Z2D_OK;
+        st[f].edge_base = (int32_t)e0;
+        st[f].n_edges = (int32_t)(edges.size() - e0);
+        st[f].has_edges = H.any ? 1 : 0;
+        ext[4 * f] = H.et, ext[4 * f + 1] = H.eb, ext[4 * f + 2] = H.el, ext[4 * f + 3] = H.er;
+    }
+    // ---- k_fill_setup per fill: Polygon.inBox, multisample.run's draw box,
+    // the bands and tile columns it touches
     auto clampi_h = [](int32_t v, int32_t lo, int32_t hi) { return std::max(lo, std::min(v, hi)); };
-    S.active = 1;
-    S.start_y = clampi_h((int32_t)std::floor(H.et / 4.0), 0, sh - 1);
-    S.end_y = clampi_h((int32_t)std::ceil(H.eb / 4.0), S.start_y, sh - 1);
-    S.start_x = clampi_h((int32_t)std::floor(H.el / 4.0), 0, sw - 1);
-    S.end_x = clampi_h((int32_t)std::ceil(H.er / 4.0), S.start_x, sw);
-    const bool bounded = is_bounded(F.op);
-    const int32_t ty0 = bounded ? S.start_y : 0, ty1 = bounded ? S.end_y : sh - 1;
-    S.band0 = ty0 / kTileRows;
-    S.band1 = ty1 / kTileRows;
-    S.fb_base = 0;
-    S.cull_x0 = bounded ? S.start_x : 0;
-    S.cull_x1 = bounded ? S.end_x : sw;
-    DevJob J = job;
-    J.fill0 = 0;
-    J.fill1 = 1;
-    J.band_lo = S.band0;
-    J.band_hi = S.band1;
-    J.tcol_lo = S.cull_x0 / kTileCols;
-    J.tcol_hi = (std::max(S.cull_x1, S.cull_x0 + 1) - 1) / kTileCols;
-    J.gband_base = J.tile_base = 0;
-    J.list_base = 0;
-    const int32_t n_bands = S.band1 - S.band0 + 1;
-    const long long n_tiles = (long long)n_bands * (J.tcol_hi - J.tcol_lo + 1);
-    RasterFill R{};
-    R.start_x = S.start_x;
-    R.end_x = S.end_x;
-    R.start_y = S.start_y;
-    R.end_y = S.end_y;
-    R.meta = ((uint32_t)F.op & RF_OP_MASK) | ((uint32_t)F.aa << RF_AA_SHIFT) |
-             (F.rule == Z2D_FILL_EVEN_ODD ? RF_EVEN_ODD : 0u) | ((uint32_t)F.fast_kind << RF_FAST_SHIFT) |
-             (bounded ? RF_BOUNDED : 0u);
-    R.px = (F.src.pix.r & 0xFFu) | ((F.src.pix.g & 0xFFu) << 8) | ((F.src.pix.b & 0xFFu) << 16) |
-           ((F.src.pix.a & 0xFFu) << 24);
+    static thread_local std::vector<DevJob> J;
+    J = jobs;
+    for (DevJob &jb : J) {
+        jb.band_lo = jb.tcol_lo = 0x7FFFFFFF;
+        jb.band_hi = jb.tcol_hi = -1;
+        jb.gband_base = jb.tile_base = 0;
+        jb.list_base = 0;
+    }
+    long long n_fb = 0;
+    for (size_t f = 0; f < n_fills; f++) {
+        const FillCmd &F = fills[f];
+        FillState &S = st[f];
+        DevJob &jb = J[(size_t)F.job];
+        const int32_t sw = jb.sfc.w, sh = jb.sfc.h;
+        const double et = ext[4 * f], eb = ext[4 * f + 1], el = ext[4 * f + 2], er = ext[4 * f + 3];
+        if (!S.has_edges || er < 0.0 || eb < 0.0) continue;
+        const double sc = F.scale;
+        const int32_t psx = (int32_t)std::floor(el / sc), psy = (int32_t)std::floor(et / sc);
+        const int32_t pex = (int32_t)std::ceil(er / sc), pey = (int32_t)std::ceil(eb / sc);
+        const int32_t pw = pex - psx, ph = pey - psy;
+        if (pw == 0 || ph == 0 || psx + pw < 0 || psy + ph < 0 || psx >= sw || psy >= sh) continue;
+        S.active = 1;
+        S.start_y = clampi_h((int32_t)std::floor(et / 4.0), 0, sh - 1);
+        S.end_y = clampi_h((int32_t)std::ceil(eb / 4.0), S.start_y, sh - 1);
+        S.start_x = clampi_h((int32_t)std::floor(el / 4.0), 0, sw - 1);
+        S.end_x = clampi_h((int32_t)std::ceil(er / 4.0), S.start_x, sw);
+        const bool bounded = is_bounded(F.op);
+        S.band0 = (bounded ? S.start_y : 0) / kTileRows;
+        S.band1 = (bounded ? S.end_y : sh - 1) / kTileRows;
+        S.fb_base = (int32_t)n_fb;
+        n_fb += S.band1 - S.band0 + 1;
+        S.cull_x0 = bounded ? S.start_x : 0;
+        S.cull_x1 = bounded ? S.end_x : sw;
+        jb.band_lo = std::min(jb.band_lo, S.band0);
+        jb.band_hi = std::max(jb.band_hi, S.band1);
+        jb.tcol_lo = std::min(jb.tcol_lo, S.cull_x0 / kTileCols);
+        jb.tcol_hi = std::max(jb.tcol_hi, (std::max(S.cull_x1, S.cull_x0 + 1) - 1) / kTileCols);
+        RasterFill &R = rf[f];
+        R.start_x = S.start_x;
+        R.end_x = S.end_x;
+        R.start_y = S.start_y;
+        R.end_y = S.end_y;
+        R.meta = ((uint32_t)F.op & RF_OP_MASK) | ((uint32_t)F.aa << RF_AA_SHIFT) |
+                 (F.rule == Z2D_FILL_EVEN_ODD ? RF_EVEN_ODD : 0u) | ((uint32_t)F.fast_kind << RF_FAST_SHIFT) |
+                 (bounded ? RF_BOUNDED : 0u);
+        R.px = (F.src.pix.r & 0xFFu) | ((F.src.pix.g & 0xFFu) << 8) | ((F.src.pix.b & 0xFFu) << 16) |
+               ((F.src.pix.a & 0xFFu) << 24);
+    }
+    done = true;
+    if (n_fb == 0) return Z2D_OK;  // nothing is drawn
+    if (n_fb > kSmallMaxBands) {
+        done = false;
+        return Z2D_OK;
+    }
+    // ---- layout: global bands, tiles and band-list storage, job after job
+    long long n_gbands = 0, n_tiles = 0, n_slots = 0;
+    for (DevJob &jb : J) {
+        jb.gband_base = (int32_t)n_gbands;
+        jb.tile_base = (int32_t)n_tiles;
+        jb.list_base = n_slots;
+        if (jb.band_hi < jb.band_lo || jb.tcol_hi < jb.tcol_lo) {
+            jb.band_lo = 0;
+            jb.band_hi = -1;
+            jb.tcol_lo = 0;
+            jb.tcol_hi = -1;
+            continue;
+        }
+        const long long nb = jb.band_hi - jb.band_lo + 1, nc = jb.tcol_hi - jb.tcol_lo + 1;
+        n_gbands += nb;
+        n_tiles += nb * nc;
+        n_slots += nb * (jb.fill1 - jb.fill0);
+    }
+    if (n_slots > kSmallMaxBands || n_tiles > 0x7FFFFFFF) {
+        done = false;
+        return Z2D_OK;
+    }
     // ---- bins: each edge in the bands of its active sample rows (edge_bands)
-    static thread_local std::vector<int32_t> cnt, off, bins;
-    cnt.assign((size_t)n_bands + 1, 0);
-    const int32_t S_ = (int32_t)F.scale;
-    auto bands_of = [&](const DEdge &e, int32_t &b0, int32_t &b1) {
-        if (e.dir == 0) return false;
-        const int32_t lo = std::max(e.rt, S.start_y * S_), hi = std::min(e.rb, (S.end_y + 1) * S_);
-        if (lo >= hi) return false;
-        b0 = lo / (kTileRows * S_);
-        b1 = (hi - 1) / (kTileRows * S_);
-        return true;
+    static thread_local std::vector<int32_t> cnt, off, bins, bcount;
+    static thread_local std::vector<int4> blist;
+    cnt.assign((size_t)n_fb + 1, 0);
+    auto for_bands = [&](auto &&visit) {
+        for (size_t f = 0; f < n_fills; f++) {
+            const FillState &S = st[f];
+            if (!S.active) continue;
+            const int32_t S_ = (int32_t)fills[f].scale;
+            for (int32_t k = 0; k < S.n_edges; k++) {
+                const DEdge &e = edges[(size_t)(S.edge_base + k)];
+                if (e.dir == 0) continue;
+                const int32_t lo = std::max(e.rt, S.start_y * S_), hi = std::min(e.rb, (S.end_y + 1) * S_);
+                if (lo >= hi) continue;
+                const int32_t b0 = lo / (kTileRows * S_), b1 = (hi - 1) / (kTileRows * S_);
+                for (int32_t b = b0; b <= b1; b++) visit(S.fb_base + (b - S.band0), S.edge_base + k);
+            }
+        }
     };
     size_t n_bins = 0;
-    for (const DEdge &e : edges) {
-        int32_t b0, b1;
-        if (!bands_of(e, b0, b1)) continue;
-        for (int32_t b = b0; b <= b1; b++) cnt[(size_t)(b - S.band0)]++;
-        n_bins += (size_t)(b1 - b0 + 1);
-    }
+    for_bands([&](int32_t fb, int32_t) {
+        cnt[(size_t)fb]++;
+        n_bins++;
+    });
     if (n_bins > kSmallMaxBins) {
         done = false;
         return Z2D_OK;
     }
-    for (int32_t v : cnt)
-        if (v > kMaxBandEdges) {
+    for (long long fb = 0; fb < n_fb; fb++)
+        if (cnt[(size_t)fb] > kMaxBandEdges) {
             done = false;  // the pipeline reports it
             return Z2D_OK;
         }
-    off.assign((size_t)n_bands + 1, 0);
-    for (int32_t b = 0; b < n_bands; b++) off[(size_t)b + 1] = off[(size_t)b] + cnt[(size_t)b];
+    off.assign((size_t)n_fb + 1, 0);
+    for (long long fb = 0; fb < n_fb; fb++) off[(size_t)fb + 1] = off[(size_t)fb] + cnt[(size_t)fb];
     bins.assign(std::max<size_t>(n_bins, 1), 0);
-    for (int32_t b = 0; b < n_bands; b++) cnt[(size_t)b] = off[(size_t)b];
-    for (size_t i = 0; i < edges.size(); i++) {
-        int32_t b0, b1;
-        if (!bands_of(edges[i], b0, b1)) continue;
-        for (int32_t b = b0; b <= b1; b++) bins[(size_t)cnt[(size_t)(b - S.band0)]++] = (int32_t)i;
+    for (long long fb = 0; fb < n_fb; fb++) cnt[(size_t)fb] = off[(size_t)fb];
+    for_bands([&](int32_t fb, int32_t e) { bins[(size_t)cnt[(size_t)fb]++] = e; });
+    // ---- band lists (k_band_lists): the job's fills touching each band, in order
+    bcount.assign(std::max<long long>(n_gbands, 1), 0);
+    blist.assign(std::max<long long>(n_slots, 1), make_int4(0, 0, 0, 0));
+    for (const DevJob &jb : J) {
+        if (jb.band_hi < jb.band_lo) continue;
+        const int32_t nf = jb.fill1 - jb.fill0;
+        for (int32_t b = jb.band_lo; b <= jb.band_hi; b++) {
+            const int32_t lb = b - jb.band_lo;
+            int4 *out = blist.data() + jb.list_base + (long long)lb * nf;
+            int32_t k = 0;
+            for (int32_t f = jb.fill0; f < jb.fill1; f++) {
+                const FillState &S = st[(size_t)f];
+                if (S.active && b >= S.band0 && b <= S.band1)
+                    out[k++] = make_int4(f, S.cull_x0, S.cull_x1, S.fb_base + (b - S.band0));
+            }
+            bcount[(size_t)(jb.gband_base + lb)] = k;
+        }
     }
-    // ---- one upload: fill, state, raster record, edges, bins, offsets,
-    // band lists, gradient
+    // ---- one upload
     auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
-    const size_t o_fill = 0, o_st = al(sizeof(FillCmd)), o_rf = o_st + al(sizeof(FillState));
-    const size_t o_edges = o_rf + al(sizeof(RasterFill));
+    const size_t o_jobs = 0, o_fill = al(sizeof(DevJob) * n_jobs);
+    const size_t o_st = o_fill + al(sizeof(FillCmd) * n_fills), o_rf = o_st + al(sizeof(FillState) * n_fills);
+    const size_t o_edges = o_rf + al(sizeof(RasterFill) * n_fills);
     const size_t o_bins = o_edges + al(sizeof(DEdge) * std::max<size_t>(edges.size(), 1));
     const size_t o_off = o_bins + al(sizeof(int32_t) * bins.size());
-    const size_t o_cnt = o_off + al(sizeof(int32_t) * ((size_t)n_bands + 1));
-    const size_t o_list = o_cnt + al(sizeof(int32_t) * (size_t)n_bands);
-    const size_t o_grad = o_list + al(sizeof(int4) * (size_t)n_bands);
-    const size_t total = o_grad + (grad ? al(sizeof(DevGradient)) : 0);
+    const size_t o_cnt = o_off + al(sizeof(int32_t) * ((size_t)n_fb + 1));
+    const size_t o_list = o_cnt + al(sizeof(int32_t) * bcount.size());
+    const size_t o_grad = o_list + al(sizeof(int4) * blist.size());
+    const size_t total = o_grad + al(sizeof(DevGradient) * std::max<size_t>(grads.size(), 1));
     const int slot = c.small_slot;
     c.small_slot ^= 1;
     HostBuf &hb = c.small_stage[slot];
@@ -2285,27 +2364,27 @@ int run_small_fill(Ctx &c, DevJob &job, const z2d_node *nodes, const FillCmd &F,
     Z2D_CUDA(cudaEventSynchronize(c.small_done[slot]));  // the slot's previous upload has been read
     if (hb.ensure(total) || c.small_params.ensure(total)) return Z2D_ERR_OUT_OF_MEMORY;
     uint8_t *h = hb.as<uint8_t>(), *dv = c.small_params.as<uint8_t>();
-    FillCmd Fd = F;
-    if (grad) Fd.src.grad = reinterpret_cast<const DevGradient *>(dv + o_grad);
-    memcpy(h + o_fill, &Fd, sizeof(FillCmd));
-    memcpy(h + o_st, &S, sizeof(FillState));
-    memcpy(h + o_rf, &R, sizeof(RasterFill));
+    memcpy(h + o_jobs, J.data(), sizeof(DevJob) * n_jobs);
+    FillCmd *hf = reinterpret_cast<FillCmd *>(h + o_fill);
+    memcpy(hf, fills.data(), sizeof(FillCmd) * n_fills);
+    const DevGradient *dgrads = reinterpret_cast<const DevGradient *>(dv + o_grad);
+    for (size_t f = 0; f < n_fills; f++)
+        if (grad_of_fill[f] >= 0) hf[f].src.grad = dgrads + grad_of_fill[f];
+    memcpy(h + o_st, st.data(), sizeof(FillState) * n_fills);
+    memcpy(h + o_rf, rf.data(), sizeof(RasterFill) * n_fills);
     if (!edges.empty()) memcpy(h + o_edges, edges.data(), sizeof(DEdge) * edges.size());
     memcpy(h + o_bins, bins.data(), sizeof(int32_t) * bins.size());
-    memcpy(h + o_off, off.data(), sizeof(int32_t) * ((size_t)n_bands + 1));
-    int32_t *bc = reinterpret_cast<int32_t *>(h + o_cnt);
-    int4 *bl = reinterpret_cast<int4 *>(h + o_list);
-    for (int32_t b = 0; b < n_bands; b++) {
-        bc[b] = 1;
-        bl[b] = make_int4(0, S.cull_x0, S.cull_x1, b);
-    }
-    if (grad) memcpy(h + o_grad, grad, sizeof(DevGradient));
+    memcpy(h + o_off, off.data(), sizeof(int32_t) * ((size_t)n_fb + 1));
+    memcpy(h + o_cnt, bcount.data(), sizeof(int32_t) * bcount.size());
+    memcpy(h + o_list, blist.data(), sizeof(int4) * blist.size());
+    if (!grads.empty()) memcpy(h + o_grad, grads.data(), sizeof(DevGradient) * grads.size());
     Z2D_CUDA(cudaMemcpyAsync(dv, h, total, cudaMemcpyHostToDevice, c.stream));
     Z2D_CUDA(cudaEventRecord(c.small_done[slot], c.stream));
+    if (n_tiles == 0) return Z2D_OK;
     // ---- the rasteriser, one CTA per tile
     RasterArgs A{};
-    A.job0 = J;
-    A.jobs = nullptr;
+    A.job0 = J[0];
+    A.jobs = reinterpret_cast<const DevJob *>(dv + o_jobs);
     A.fills = reinterpret_cast<const FillCmd *>(dv + o_fill);
     A.st = reinterpret_cast<const FillState *>(dv + o_st);
     A.edges = reinterpret_cast<const DEdge *>(dv + o_edges);
@@ -2315,7 +2394,7 @@ int run_small_fill(Ctx &c, DevJob &job, const z2d_node *nodes, const FillCmd &F,
     A.band_fills = reinterpret_cast<const int4 *>(dv + o_list);
     A.rfills = reinterpret_cast<const RasterFill *>(dv + o_rf);
     A.masks = nullptr;
-    A.n_jobs = 1;
+    A.n_jobs = (int32_t)n_jobs;
     A.queue = nullptr;
     A.n_items = (unsigned long long)n_tiles;
     A.order = nullptr;
@@ -2328,7 +2407,8 @@ int run_small_fill(Ctx &c, DevJob &job, const z2d_node *nodes, const FillCmd &F,
     }
     const size_t smem = sizeof(uint32_t) * kWarpWords * kTileRows;
     cudaEvent_t t0 = c.timer_begin(c.t_raster);
-    k_raster<false, true><<<(unsigned)n_tiles, kRasterThreads, smem, c.stream>>>(A);
+    if (n_jobs == 1) k_raster<false, true><<<(unsigned)n_tiles, kRasterThreads, smem, c.stream>>>(A);
+    else k_raster<true, true><<<(unsigned)n_tiles, kRasterThreads, smem, c.stream>>>(A);
     c.timer_end(c.t_raster, t0);
     c.launches++;
     Z2D_CUDA(cudaGetLastError());

@@ -166,14 +166,17 @@ struct DevJob {
 // Nodes that no fill owns are skipped; device-stroked
 // commands (`strokes`, fills with stroke >= 0) read their nodes from the
 // same array; fills with poly >= 0 draw a host-built polygon of `strokes`.
-// One small fill on one surface with a single upload and a single launch:
-// the host flattens the path (fill_plotter.plot, Spline.decompose,
-// Polygon.addEdge), sets the fill up (inBox, multisample.run's draw box)
-// and bins its edges; the rasteriser draws the tiles.  Sets `done` = false
-// without touching the device when the fill is not one it takes (another
-// anti-aliasing mode, a stroke, an open two-point chain, too many edges or
-// bands, a packed surface), and the caller runs the full pipeline.
-int run_small_fill(Ctx &c, DevJob &job, const z2d_node *nodes, const FillCmd &F, const DevGradient *grad, bool &done);
+// A call with few short fills, on one surface or many, in a single upload
+// and a single launch: the host flattens the paths (fill_plotter.plot,
+// Spline.decompose, Polygon.addEdge), sets the fills up (inBox,
+// multisample.run's draw box), bins their edges and lays out the band
+// lists; the rasteriser draws the tiles.  Sets `done` = false without
+// touching the device when the call is not one it takes (another
+// anti-aliasing mode, strokes, an open two-point chain, more nodes, edges or
+// bands than its limits, a packed surface, a gradient with a stop table),
+// and the caller runs the full pipeline.
+int run_small_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, const std::vector<FillCmd> &fills,
+                   const std::vector<DevGradient> &grads, const std::vector<int32_t> &grad_of_fill, bool &done);
 
 struct StrokeSet;
 int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n_nodes, std::vector<FillCmd> &fills,
