@@ -49,14 +49,23 @@ def _off_surface():
     return p.to_array()
 
 
-def _check(gpu, oracle, pat, nodes, opts, seed=0, fmt="rgba", what=""):
+def _check(gpu, oracle, pat, nodes, opts, seed=0, fmt="rgba", what="", small=None):
+    """Draws the fill alone and in the pipeline's batch; `small` says whether
+    the single call must take the one-upload path (at most one launch) or
+    must not (None: either)."""
     a, b, c = _bg(seed, fmt), _bg(seed, fmt), _bg(seed, fmt)
+    n0 = gpu.ctx.launch_count
     assert gpu.fill(a, pat, nodes, opts) == abi.OK
-    painter.fill_batch(b, [(pat, nodes, opts), (pat, _off_surface(), opts)])
+    n1 = gpu.ctx.launch_count
+    painter.fill_batch(b, [(pat, nodes, opts), (pat, _off_surface(), opts)], ctx=gpu.ctx)
+    n2 = gpu.ctx.launch_count
     assert oracle.fill(c, pat, nodes, opts) == abi.OK
     ca = c.numpy()
     assert np.array_equal(a.numpy(), ca), f"{what}: single call differs from the oracle"
     assert np.array_equal(b.numpy(), ca), f"{what}: pipeline differs from the oracle"
+    assert n2 - n1 > 1, f"{what}: the batch did not take the pipeline"
+    if small is not None:
+        assert (n1 - n0 <= 1) == small, f"{what}: {n1 - n0} launches for the single call"
 
 
 @pytest.mark.parametrize("seed", range(16))
@@ -111,7 +120,8 @@ def _poly(points, close=True):
     ("open chain", [(10, 10), (200, 150)]),
 ])
 def test_shapes(gpu, oracle, name, points):
-    _check(gpu, oracle, Pattern.from_pixel(Pixel.rgba(0, 120, 240, 255)), _poly(points), FillOptions(), what=name)
+    _check(gpu, oracle, Pattern.from_pixel(Pixel.rgba(0, 120, 240, 255)), _poly(points), FillOptions(), what=name,
+           small=name != "open chain")
 
 
 def test_curves_and_subpaths(gpu, oracle):
@@ -121,7 +131,7 @@ def test_curves_and_subpaths(gpu, oracle):
     p.move_to(140, 100).curve_to(140, 100, 150, 110, 150, 110).line_to(160, 90).close()  # degenerate curve
     for rule in ("non_zero", "even_odd"):
         _check(gpu, oracle, Pattern.from_pixel(Pixel.rgba(90, 30, 120, 200)), p.to_array(),
-               FillOptions(fill_rule=rule), what=rule)
+               FillOptions(fill_rule=rule), what=rule, small=True)
 
 
 def test_beyond_limits(gpu, oracle):
@@ -133,11 +143,11 @@ def test_beyond_limits(gpu, oracle):
         p.line_to(*map(float, rng.uniform(0, [W, H])))
     p.close()
     _check(gpu, oracle, Pattern.from_pixel(Pixel.rgba(10, 200, 90, 255)), p.to_array(),
-           FillOptions(fill_rule="even_odd"), what="5000 lines")
+           FillOptions(fill_rule="even_odd"), what="5000 lines", small=False)
     q = Path()
     q.move_to(0, 0).curve_to(1e5, 0, -1e5, 200, 300, 200).close()  # many subdivision leaves
     _check(gpu, oracle, Pattern.from_pixel(Pixel.rgba(10, 200, 90, 255)), q.to_array(),
-           FillOptions(tolerance=0.001), what="long curve")
+           FillOptions(tolerance=0.001), what="long curve", small=False)
 
 
 @pytest.mark.parametrize("fmt", ["rgb", "alpha8", "xrgb", "argb"])
@@ -170,21 +180,25 @@ def test_many_surfaces(oracle, seed):
     import torch
     rng = np.random.default_rng(1300 + seed)
     specs = []
-    for j in range(int(rng.integers(2, 9))):
+    for j in range(int(rng.integers(2, 7))):
         w, h = int(rng.integers(8, 260)), int(rng.integers(8, 200))
         fills = []
-        for k in range(int(rng.integers(1, 5))):
-            nodes = random_path(rng, w, h, side_lo=4.0, side_hi=float(max(w, h)), seg_hi=16)
+        for k in range(int(rng.integers(1, 3))):
+            nodes = random_path(rng, w, h, side_lo=4.0, side_hi=float(min(40, max(w, h))), seg_hi=5)
             op = str(rng.choice(["src_over", "src_over", "multiply", "src_in", "xor", "hue"]))
             fills.append((Pattern.from_pixel(Pixel.rgba(int(rng.integers(0, 120)), 90, 40, 200)), nodes,
                           FillOptions(operator=op, fill_rule=str(rng.choice(["non_zero", "even_odd"])))))
         specs.append((str(rng.choice(["rgba", "rgb", "alpha8"])), w, h, seed * 31 + j, fills))
+    from z2d_gb300.native import default_context
+    ctx = default_context()
     for big in (False, True):
         dev, ref = _dev_jobs(oracle, specs)
         jobs = [(d, list(sp[4])) for d, sp in zip(dev, specs)]
         if big:
             jobs[-1][1].append((Pattern.from_pixel(Pixel.rgba(1, 2, 3, 4)), _off_surface(), FillOptions()))
-        painter.fill_jobs(jobs)
+        n0 = ctx.launch_count
+        painter.fill_jobs(jobs, ctx=ctx)
         torch.cuda.synchronize()
+        assert (ctx.launch_count - n0 <= 1) == (not big), "the call did not take the intended path"
         for k, (d, r) in enumerate(zip(dev, ref)):
             assert np.array_equal(d.to_host().numpy(), r.numpy()), f"job {k} ({'pipeline' if big else 'one upload'})"

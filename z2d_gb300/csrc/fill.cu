@@ -2003,16 +2003,25 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
 // edges in any order (the rasteriser's sums do not depend on it).
 namespace {
 
+// The host's work grows with the edges (about 20-30 ns each to flatten and
+// bin) while the pipeline's cost is mostly fixed (~100 us of launches and
+// readbacks for a small call), so the path takes calls whose edge count,
+// estimated before and counted while flattening, stays below a budget:
+// one surface up to 4,096 edges; several (as in the server's passes under
+// load, where the pipeline's fixed cost is shared) up to 1,024 on at most
+// 8 surfaces.
 constexpr int32_t kSmallMaxNodes = 4096;       // nodes of all the call's fills
-constexpr size_t kSmallMaxEdges = 8192;        // their edges
+constexpr size_t kSmallEdgesOne = 4096;        // edge budget, one surface
+constexpr size_t kSmallEdgesMany = 1024;       // edge budget, several surfaces
+constexpr size_t kSmallMaxJobs = 8;
 constexpr size_t kSmallMaxBins = 1 << 17;      // (edge, band) pairs
 constexpr long long kSmallMaxBands = 1 << 16;  // (fill, band) slots and band-list entries
-constexpr size_t kSmallMaxJobs = 4096;
 constexpr int kSmallMaxDepth = 40;  // below the device subdivision bound
 
 struct HostFlatten {
     const FillCmd &F;
     std::vector<DEdge> &edges;
+    size_t max_edges;
     double et = 0, eb = 0, el = 0, er = 0;
     bool any = false, overflow = false;
     // PointBuffer(1, 3) of fill_plotter: its first and last points and length
@@ -2021,7 +2030,7 @@ struct HostFlatten {
 
     // Polygon.addEdge (Polygon.zig:61-109), as add_edge in edges.cuh
     void edge(double x0, double y0, double x1, double y1) {
-        if (edges.size() >= kSmallMaxEdges) {
+        if (edges.size() >= max_edges) {
             overflow = true;
             return;
         }
@@ -2175,6 +2184,38 @@ struct HostFlatten {
     }
 };
 
+// An estimate of a path's edges before flattening it: one per line_to and
+// close_path, and for a curve 2^k leaves with k the levels of halving that
+// bring the initial knots' errorSq below tol^2 (each halving divides it by
+// about 16).
+size_t estimate_edges(const z2d_node *nodes, int32_t n, double tol) {
+    size_t est = 0;
+    double lx = 0, ly = 0;
+    const double tol2 = tol * tol;
+    for (int32_t i = 0; i < n; i++) {
+        const z2d_node &nd = nodes[i];
+        if (nd.tag == Z2D_CURVE_TO) {
+            const HostFlatten::K k{lx, ly, nd.p[0], nd.p[1], nd.p[2], nd.p[3], nd.p[4], nd.p[5]};
+            const double e = HostFlatten::error_sq(k);
+            size_t leaves = 1;
+            if (e >= tol2) {
+                const double lv = std::ceil(std::log2(e / tol2) / 4.0);
+                leaves = lv >= 20.0 ? ((size_t)1 << 20) : ((size_t)1 << (size_t)std::max(0.0, lv));
+            }
+            est += leaves;
+            lx = nd.p[4];
+            ly = nd.p[5];
+        } else {
+            est += 1;
+            if (nd.tag != Z2D_CLOSE_PATH) {
+                lx = nd.p[0];
+                ly = nd.p[1];
+            }
+        }
+    }
+    return est;
+}
+
 }  // namespace
 
 int run_small_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, const std::vector<FillCmd> &fills,
@@ -2182,12 +2223,18 @@ int run_small_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, con
     done = false;
     const size_t n_fills = fills.size(), n_jobs = jobs.size();
     if (n_fills == 0 || n_jobs == 0 || n_jobs > kSmallMaxJobs) return Z2D_OK;
+    const size_t budget = n_jobs == 1 ? kSmallEdgesOne : kSmallEdgesMany;
     long long total_nodes = 0;
     for (const FillCmd &F : fills) {
         if (F.aa != Z2D_AA_MULTISAMPLE_4X || F.stroke >= 0 || F.poly >= 0 || F.n_nodes <= 0) return Z2D_OK;
         total_nodes += F.n_nodes;
     }
     if (total_nodes > kSmallMaxNodes) return Z2D_OK;
+    size_t est = 0;
+    for (const FillCmd &F : fills) {
+        est += estimate_edges(nodes + F.node_off, F.n_nodes, F.tol);
+        if (est > budget) return Z2D_OK;
+    }
     for (const DevJob &J : jobs)
         if (fmt_packed(J.sfc.fmt)) return Z2D_OK;
     for (const DevGradient &g : grads)
@@ -2203,7 +2250,7 @@ int run_small_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, con
     ext.assign(4 * n_fills, 0.0);
     for (size_t f = 0; f < n_fills; f++) {
         const size_t e0 = edges.size();
-        HostFlatten H{fills[f], edges};
+        HostFlatten H{fills[f], edges, budget};
         bool open_chain = false;
         if (!H.plot(nodes + fills[f].node_off, fills[f].n_nodes, open_chain) || open_chain) return Z2D_OK;
         st[f].edge_base = (int32_t)e0;
