@@ -1215,50 +1215,50 @@ __device__ __forceinline__ void raster_row(const RasterArgs &A, const int32_t ti
                 // sample rows stay below 2^22, where sr + 0.5 is exact in f32
                 const bool f32_ok = sub0 < (1 << 22);
                 const float fsub = (float)sub0 + 0.5f;
-                // One (edge, sample row) pair per lane: sc lanes per edge, 32 / sc
-                // edges at a time, so that a band holding few edges of the
-                // fill still fills the warp.  Crossings at or left of the
-                // tile's first sample column all land on column 0: they are
-                // summed over the lanes of each sample row and added once
-                // (instead of one atomic per edge on the same word).
-                {
-                    const int r = lane & (sc - 1), lg_sc = direct ? 0 : 2;
-                    const int32_t sr = sub0 + r;
-                    const float fs = fsub + (float)r;
-                    for (int32_t base = e0; base < e1; base += 32 >> lg_sc) {
-                        const int32_t ei = base + (lane >> lg_sc);
+                // one edge per lane; crossings at or left of the tile's
+                // first sample column all land on column 0, so they are
+                // summed across the warp and added once (instead of one
+                // atomic per edge on the same word)
+                for (int32_t base = e0; base < e1; base += 32) {
+                    const int32_t ei = base + lane;
+                    int32_t id = 0, dir = 0, lo = 0, hi = 0;
+                    float4 ef = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    if (ei < e1) {
+                        id = A.bins[ei];
+                        ef = __ldg(reinterpret_cast<const float4 *>(A.edges + id));
+                        const int2 er = __ldg(reinterpret_cast<const int2 *>(&A.edges[id].rt));
+                        dir = __float_as_int(ef.w);
+                        lo = max(er.x, sub0);
+                        hi = min(er.y, sub0 + sc);
+                    }
+                    for (int r = 0; r < sc; r++) {  // uniform across the warp
+                        const int32_t sr = sub0 + r;
                         int32_t left = 0;
-                        if (ei < e1) {
-                            const int32_t id = A.bins[ei];
-                            const float4 ef = __ldg(reinterpret_cast<const float4 *>(A.edges + id));
-                            const int2 er = __ldg(reinterpret_cast<const int2 *>(&A.edges[id].rt));
-                            const int32_t dir = __float_as_int(ef.w);
-                            if (sr >= er.x && sr < er.y) {
-                                int32_t X;
-                                if (!(f32_ok && crossing_f32(ef.x, ef.y, ef.z, fs, X))) {
-                                    const DEdge &e = A.edges[id];
-                                    X = (int32_t)round(e.x_start + (e.x_inc * (((double)sr + 0.5) - e.top)));
-                                }
-                                const int32_t c = X - col0;
-                                if (c <= 0) {
-                                    left = dir;
-                                } else if (c < ncol) {
-                                    // per is 8 or 32 and c > 0: shifts and masks
-                                    const int lane_c = c >> lg_per, pair = (c & (per - 1)) >> 1;
-                                    const uint32_t inc = (c & 1) ? ((uint32_t)dir << 16) : (uint32_t)dir;
-                                    atomicAdd(&words[r * kWordsPerSubRow + ((pair << 5) | lane_c)], inc);
-                                    atomicOr(&words[kTouchOff + r * 32 + lane_c], 1u << pair);
-                                    atomicAdd(&words[kTotOff + r * 32 + lane_c], (uint32_t)dir);
-                                }
+                        if (sr >= lo && sr < hi) {
+                            int32_t X;
+                            if (!(f32_ok && crossing_f32(ef.x, ef.y, ef.z, fsub + (float)r, X))) {
+                                const DEdge &e = A.edges[id];
+                                X = (int32_t)round(e.x_start + (e.x_inc * (((double)sr + 0.5) - e.top)));
+                            }
+                            const int32_t c = X - col0;
+                            if (c <= 0) {
+                                left = dir;
+                            } else if (c < ncol) {
+                                // per is 8 or 32 and c > 0: shifts and masks
+                                const int lane_c = c >> lg_per, pair = (c & (per - 1)) >> 1;
+                                const uint32_t inc = (c & 1) ? ((uint32_t)dir << 16) : (uint32_t)dir;
+                                atomicAdd(&words[r * kWordsPerSubRow + ((pair << 5) | lane_c)], inc);
+                                atomicOr(&words[kTouchOff + r * 32 + lane_c], 1u << pair);
+                                atomicAdd(&words[kTotOff + r * 32 + lane_c], (uint32_t)dir);
                             }
                         }
                         // column 0 is the low half of lane 0's pair 0; a net
                         // zero changes no winding and needs no visit
-                        for (int o = sc; o < 32; o <<= 1) left += __shfl_xor_sync(0xffffffffu, left, o);
-                        if (lane < sc && left != 0) {  // lane == r
-                            atomicAdd(&words[r * kWordsPerSubRow], (uint32_t)left);
+                        const int32_t sum = __reduce_add_sync(0xffffffffu, left);
+                        if (lane == 0 && sum != 0) {
+                            atomicAdd(&words[r * kWordsPerSubRow], (uint32_t)sum);
                             atomicOr(&words[kTouchOff + r * 32], 1u);
-                            atomicAdd(&words[kTotOff + r * 32], (uint32_t)left);
+                            atomicAdd(&words[kTotOff + r * 32], (uint32_t)sum);
                         }
                     }
                 }
