@@ -596,7 +596,9 @@ Z2D_D float grad_offset_ex(const DevGradient &gr, int32_t x, int32_t y, bool &sl
     slow = true;
     return grad_offset_f64(gr, x, y);
 }
-Z2D_D float grad_offset(const DevGradient &gr, int32_t x, int32_t y) {
+// Out of line: the kernels that composite every kind of source (the
+// rasteriser among them) keep their registers for their own loops.
+static __device__ __noinline__ float grad_offset(const DevGradient &gr, int32_t x, int32_t y) {
     bool slow = false;
     return grad_offset_ex(gr, x, y, slow);
 }
