@@ -20,7 +20,7 @@ CSRC = PKG / "csrc"
 OUT_DIR = PKG / "_lib"
 LIB = OUT_DIR / "libz2dgpu.so"
 SOURCES = ["capi.cu", "composite.cu", "composite_mask.cu", "composite_fused.cu", "composite_grad.cu", "fill.cu", "server.cu", "stroke.cpp", "stroke_gpu.cu", "hairline.cu", "png.cu", "tune.cu", "path_build.cu"]
-HEADERS = ["z2d_pixel.cuh", "z2d_internal.h", "fill.cuh", "stroke.h", "stroke_geom.h", "stroke_gpu.cuh", "edges.cuh", "spline.cuh", "raster_px.cuh", "host_pool.h", "blue_noise_64x64.inc", "zig_math.cuh", "grad_fast.cuh", "zig_trig.cuh"]
+HEADERS = ["z2d_pixel.cuh", "z2d_internal.h", "fill.cuh", "stroke.h", "stroke_geom.h", "stroke_gpu.cuh", "edges.cuh", "spline.cuh", "raster_px.cuh", "host_pool.h", "blue_noise_64x64.inc", "zig_math.cuh", "grad_fast.cuh", "zig_trig.cuh", "f64_int.cuh"]
 ARCH = os.environ.get("Z2D_GPU_ARCH", "103a")
 
 

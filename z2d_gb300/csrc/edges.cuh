@@ -5,6 +5,7 @@
 #include <stdint.h>
 #include <string.h>
 
+#include "f64_int.cuh"
 #include "fill.cuh"
 
 namespace z2dg {
@@ -25,23 +26,46 @@ __host__ __device__ __forceinline__ double dkey_inv(unsigned long long k) {
 #endif
 }
 
+// The f64 operations of addEdge that have exact integer forms
+// (f64_int.cuh), with the f64 instruction for the operands they decline.
+__device__ __forceinline__ double scale_coord(double v, double s) {
+    bool ok;
+    const double r = f64_scale_pow2(v, s, ok);
+    if (ok) return r;
+    return f64_mul_hw(v, s);
+}
+__device__ __forceinline__ int32_t round_i32(double v) {
+    bool ok;
+    const int32_t r = f64_round_i32(v, ok);
+    if (ok) return r;
+    return f64_round_i32_hw(v);
+}
+__device__ __forceinline__ float to_f32(double v) {
+    bool ok;
+    const float r = f64_to_f32(v, ok);
+    if (ok) return r;
+    return f64_to_f32_hw(v);
+}
+
 __device__ __forceinline__ void add_edge(const FillCmd &F, DEdge *out, double x0, double y0, double x1, double y1,
                                          double &et, double &eb, double &el, double &er, bool &any) {
     // Polygon.addEdge (Polygon.zig:61-109)
-    const double ax = x0 * F.edge_scale, ay = y0 * F.edge_scale, bx = x1 * F.edge_scale, by = y1 * F.edge_scale;
+    const double ax = scale_coord(x0, F.edge_scale), ay = scale_coord(y0, F.edge_scale);
+    const double bx = scale_coord(x1, F.edge_scale), by = scale_coord(y1, F.edge_scale);
     DEdge e;
-    if (ay < by) {
+    const bool down = f64_lt(ay, by);
+    if (down) {
         e.top = ay;
         e.x_start = ax;
-        e.x_inc = (bx - ax) / (by - ay);
+        e.x_inc = f64_div_dev(bx - ax, by - ay);
         e.dir = -1;
-        e.rb = (int32_t)round(by);
-    } else if (ay > by) {
+        e.rb = round_i32(by);
+    } else if (f64_lt(by, ay)) {
         e.top = by;
         e.x_start = bx;
-        e.x_inc = (ax - bx) / (ay - by);
+        e.x_inc = f64_div_dev(ax - bx, ay - by);
         e.dir = 1;
-        e.rb = (int32_t)round(ay);
+        e.rb = round_i32(ay);
     } else {
         e.top = 0;
         e.x_start = 0;
@@ -53,20 +77,21 @@ __device__ __forceinline__ void add_edge(const FillCmd &F, DEdge *out, double x0
         *out = e;
         return;
     }
-    e.rt = (int32_t)round(e.top);
-    e.fxs = (float)e.x_start;
-    e.fxi = (float)e.x_inc;
-    e.ftp = (float)e.top;
-    const double bot = ay < by ? by : ay;
-    const double l = ax < bx ? ax : bx, r = ax < bx ? bx : ax;
+    e.rt = round_i32(e.top);
+    e.fxs = to_f32(e.x_start);
+    e.fxi = to_f32(e.x_inc);
+    e.ftp = to_f32(e.top);
+    const double bot = down ? by : ay;
+    const bool lr = f64_lt(ax, bx);
+    const double l = lr ? ax : bx, r = lr ? bx : ax;
     if (!any) {
         et = e.top; eb = bot; el = l; er = r;
         any = true;
     } else {
-        if (e.top < et) et = e.top;
-        if (bot > eb) eb = bot;
-        if (l < el) el = l;
-        if (r > er) er = r;
+        if (f64_lt(e.top, et)) et = e.top;
+        if (f64_lt(eb, bot)) eb = bot;
+        if (f64_lt(l, el)) el = l;
+        if (f64_lt(er, r)) er = r;
     }
     *out = e;
 }
@@ -82,20 +107,23 @@ __device__ __forceinline__ void merge_extents(FillState *st, int32_t f, bool any
     const int lead = __ffs(am) - 1;
     const int32_t f0 = __shfl_sync(all, f, lead);
     if (__all_sync(all, !any || f == f0)) {
-        double mt = any ? et : 1e300, mb = any ? eb : -1e300, ml = any ? el : 1e300, mr = any ? er : -1e300;
+        // reduced as ordered keys: integer minima and maxima (f64 min/max
+        // instructions run on GB300's narrow f64 pipe)
+        unsigned long long mt = any ? dkey(et) : ~0ull, mb = any ? dkey(eb) : 0ull;
+        unsigned long long ml = any ? dkey(el) : ~0ull, mr = any ? dkey(er) : 0ull;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            mt = fmin(mt, __shfl_xor_sync(all, mt, o));
-            mb = fmax(mb, __shfl_xor_sync(all, mb, o));
-            ml = fmin(ml, __shfl_xor_sync(all, ml, o));
-            mr = fmax(mr, __shfl_xor_sync(all, mr, o));
+            mt = min(mt, __shfl_xor_sync(all, mt, o));
+            mb = max(mb, __shfl_xor_sync(all, mb, o));
+            ml = min(ml, __shfl_xor_sync(all, ml, o));
+            mr = max(mr, __shfl_xor_sync(all, mr, o));
         }
         if ((int)(threadIdx.x & 31) == lead) {
             FillState &S = st[f0];
-            atomicMin(&S.ext[0], dkey(mt));
-            atomicMax(&S.ext[1], dkey(mb));
-            atomicMin(&S.ext[2], dkey(ml));
-            atomicMax(&S.ext[3], dkey(mr));
+            atomicMin(&S.ext[0], mt);
+            atomicMax(&S.ext[1], mb);
+            atomicMin(&S.ext[2], ml);
+            atomicMax(&S.ext[3], mr);
             atomicOr(&S.has_edges, 1);
         }
     } else if (any) {

@@ -3,12 +3,16 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
+#include "f64_int.cuh"
 #include "fill.cuh"
 
 namespace z2dg {
 
-__device__ __forceinline__ bool pt_eq(double ax, double ay, double bx, double by) { return ax == bx && ay == by; }
+__host__ __device__ __forceinline__ bool pt_eq(double ax, double ay, double bx, double by) {
+    return f64_eq(ax, bx) && f64_eq(ay, by);
+}
 
 struct Knots {
     double ax, ay, bx, by, cx, cy, dx, dy;
@@ -164,18 +168,27 @@ __device__ __forceinline__ Tol make_tol(double tol) {
 }
 
 // errorSq(k) < t.d, exactly as the f64 comparison decides it.
-__device__ __forceinline__ bool below_tol(const Knots &k, const Tol &t) {
+// The rarely needed tests of below_tol, out of line so that the
+// subdivision loops that inline below_tol stay small in the instruction
+// cache.
+static __device__ __noinline__ bool below_tol_slow(Knots k, Tol t, bool proj) {
     if (t.f_ok) {
-        const bool proj = k.ax != k.dx || k.ay != k.dy;
-        // from the coordinates first (no f64), then from the exact f64
-        // differences, then errorSq itself
-        int r = error_sq_lt_f32_pts(k.ax, k.ay, k.bx, k.by, k.cx, k.cy, k.dx, k.dy, proj, t.f, t.e);
-        if (r >= 0) return r != 0;
-        r = error_sq_lt_f32(k.bx - k.ax, k.by - k.ay, k.cx - k.ax, k.cy - k.ay, proj, k.dx - k.ax, k.dy - k.ay, t.f,
-                            t.e);
+        const int r = error_sq_lt_f32(k.bx - k.ax, k.by - k.ay, k.cx - k.ax, k.cy - k.ay, proj, k.dx - k.ax,
+                                      k.dy - k.ay, t.f, t.e);
         if (r >= 0) return r != 0;
     }
     return error_sq(k) < t.d;
+}
+
+__device__ __forceinline__ bool below_tol(const Knots &k, const Tol &t) {
+    const bool proj = !pt_eq(k.ax, k.ay, k.dx, k.dy);
+    if (t.f_ok) {
+        // from the coordinates first (no f64), then from the exact f64
+        // differences, then errorSq itself
+        const int r = error_sq_lt_f32_pts(k.ax, k.ay, k.bx, k.by, k.cx, k.cy, k.dx, k.dy, proj, t.f, t.e);
+        if (r >= 0) return r != 0;
+    }
+    return below_tol_slow(k, t, proj);
 }
 
 // x / 2.  For normal x whose half is normal this only lowers the exponent,
@@ -187,7 +200,14 @@ __device__ __forceinline__ double half_of(double x) {
     if (e > 1u && e < 0x7FFu) return __longlong_as_double(b - (1ll << 52));
     return x / 2;
 }
-__device__ __forceinline__ double lerp_half(double a, double b) { return a + half_of(b - a); }
+// The f64 form, out of line so that it runs only on the lanes that need it.
+static __device__ __noinline__ double lerp_half_f64(double a, double b) { return a + half_of(b - a); }
+__device__ __forceinline__ double lerp_half(double a, double b) {
+    bool done;
+    const double r = lerp_half_int(a, b, done);
+    if (done) return r;
+    return lerp_half_f64(a, b);
+}
 
 // Knots.deCasteljau (Spline.zig:128-152): k becomes the first half, the
 // second half is returned.

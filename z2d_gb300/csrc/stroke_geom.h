@@ -3,15 +3,24 @@
 //
 // Every function is plain IEEE f64 arithmetic (+, -, *, /, sqrt; the build
 // turns off FMA contraction on both sides), so host and device produce the
-// same bits for the same inputs.  Trigonometry (the pen) stays on the host.
+// same bits for the same inputs.  On the device, divisions use the exact
+// integer long division of f64_int.cuh (the same quotient as the f64
+// instructions, which GB300 runs at 1/64 of its f32 rate).  Trigonometry
+// (the pen) stays on the host.
 #pragma once
 #include <math.h>
 #include <stdint.h>
 
+#include "f64_int.cuh"
 #ifdef __CUDACC__
 #define Z2D_HD __host__ __device__ __forceinline__
+// out of line on the device: one copy of the larger pieces serves every
+// call site of the element kernels, which keeps them small in the
+// instruction cache
+#define Z2D_HD_CALL static __host__ __device__ __noinline__
 #else
 #define Z2D_HD inline
+#define Z2D_HD_CALL inline
 #endif
 
 namespace z2dg {
@@ -21,6 +30,16 @@ struct Pt {
     double x, y;
 };
 Z2D_HD bool eq(Pt a, Pt b) { return a.x == b.x && a.y == b.y; }
+
+// a / b: on the device through the integer long division of f64_int.cuh
+// (the same IEEE quotient; an f64 division costs several f64 instructions).
+Z2D_HD double div(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return f64_div_dev(a, b);
+#else
+    return a / b;
+#endif
+}
 
 // Transformation.zig
 struct Tf {
@@ -119,8 +138,8 @@ Z2D_HD double normalize(Slope &s) {
         }
     } else {
         mag = hypot2(s.dx, s.dy);
-        rx = s.dx / mag;
-        ry = s.dy / mag;
+        rx = div(s.dx, mag);
+        ry = div(s.dy, mag);
     }
     s.dx = rx;
     s.dy = ry;
@@ -147,7 +166,7 @@ struct Face {
     Pt p0_cw, p0_ccw, p1_cw, p1_ccw;
 };
 // Face.initSlope (Face.zig:50-94)
-Z2D_HD Face face_init2(Pt p0, Pt p1, Slope dev_slope, double thickness, const Tf &ctm) {
+Z2D_HD_CALL Face face_init2(Pt p0, Pt p1, Slope dev_slope, double thickness, const Tf &ctm) {
     const double half = thickness / 2;
     double ox, oy;
     Slope user_slope = dev_slope;
@@ -190,10 +209,10 @@ Z2D_HD Pt intersect(const Face &in, const Face &out, bool clockwise) {
     const Pt ip = clockwise ? in.p1_ccw : in.p1_cw;
     const Pt op = clockwise ? out.p0_ccw : out.p0_cw;
     const Slope is = normalized(in.dev_slope), os = normalized(out.dev_slope);
-    const double ry = ((op.x - ip.x) * is.dy * os.dy - op.y * os.dx * is.dy + ip.y * is.dx * os.dy) /
-                      (is.dx * os.dy - os.dx * is.dy);
-    const double rx = (fabs(is.dy) >= fabs(os.dy)) ? (ry - ip.y) * is.dx / is.dy + ip.x
-                                                    : (ry - op.y) * os.dx / os.dy + op.x;
+    const double ry = div((op.x - ip.x) * is.dy * os.dy - op.y * os.dx * is.dy + ip.y * is.dx * os.dy,
+                          is.dx * os.dy - os.dx * is.dy);
+    const double rx = (fabs(is.dy) >= fabs(os.dy)) ? div((ry - ip.y) * is.dx, is.dy) + ip.x
+                                                    : div((ry - op.y) * os.dx, os.dy) + op.x;
     return Pt{rx, ry};
 }
 

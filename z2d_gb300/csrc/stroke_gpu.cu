@@ -320,6 +320,12 @@ __device__ __forceinline__ void element(O &o, const StrokeDev &T, const PenVerte
     };
     const Tf ctm = tf_of(T);
     const bool pcw = st.pcw != 0;
+    // Every case below draws at most two caps or one join; they are
+    // gathered into one cap call and one join call, so that the kernel
+    // holds a single copy of each.
+    int n_caps = 0, jmode = -1;
+    Pt c0{}, c1{}, j0{}, j1{}, j2{};
+    bool ccw = pcw;
     switch (st.kind) {
         case SK_DOT:  // plot_dot of stroke_plotter (round caps only)
             if (k == 0) {
@@ -327,32 +333,60 @@ __device__ __forceinline__ void element(O &o, const StrokeDev &T, const PenVerte
                 for (int32_t i = 0; i < T.pen_n; i++) o.A(Pt{c.x + pen[i].point.x, c.y + pen[i].point.y});
             }
             return;
-        case SK_SINGLE:  // plotSingle (stroke_plotter.zig:232-279)
-            if (k == 0) {
-                const Pt a = P(0), b = P(1);
-                cap(o, T, ctm, pen, sg::face_init(b, a, T.thickness, ctm), true);
-                cap(o, T, ctm, pen, sg::face_init(a, b, T.thickness, ctm), true);
-            }
-            return;
+        case SK_SINGLE:  // plotSingle (stroke_plotter.zig:232-279): caps of b->a, then a->b
+            if (k != 0) return;
+            n_caps = 2;
+            c0 = P(1);
+            c1 = P(0);
+            ccw = true;
+            break;
         case SK_OPEN:  // plotOpenJoined (stroke_plotter.zig:281-363)
-            if (k == 0) cap(o, T, ctm, pen, sg::face_init(P(1), P(0), T.thickness, ctm), pcw);
-            else if (k == n - 1) cap(o, T, ctm, pen, sg::face_init(P(n - 2), P(n - 1), T.thickness, ctm), pcw);
-            else join(o, T, ctm, pen, q_mode[st.q0 + k + 1], P(k - 1), P(k), P(k + 1), pcw);
-            return;
+            if (k == 0) {
+                n_caps = 1;
+                c0 = P(1);
+                c1 = P(0);
+            } else if (k == n - 1) {
+                n_caps = 1;
+                c0 = P(n - 2);
+                c1 = P(n - 1);
+            } else {
+                jmode = q_mode[st.q0 + k + 1];
+                j0 = P(k - 1);
+                j1 = P(k);
+                j2 = P(k + 1);
+            }
+            break;
         case SK_CLOSED: {  // plotClosedJoined (stroke_plotter.zig:365-403)
             const bool back_to_start = sg::eq(P(n - 1), P(0));
-            if (k >= 1 && k <= n - 2) join(o, T, ctm, pen, q_mode[st.q0 + k + 1], P(k - 1), P(k), P(k + 1), pcw);
-            else if (k == n - 1) {
-                if (!back_to_start) join(o, T, ctm, pen, T.join, P(n - 2), P(n - 1), P(0), pcw);
-            } else if (!back_to_start) {
-                join(o, T, ctm, pen, T.join, P(n - 1), P(0), P(1), pcw);
+            if (k >= 1 && k <= n - 2) {
+                jmode = q_mode[st.q0 + k + 1];
+                j0 = P(k - 1);
+                j1 = P(k);
+                j2 = P(k + 1);
+            } else if (k == n - 1) {
+                if (back_to_start) return;
+                jmode = T.join;
+                j0 = P(n - 2);
+                j1 = P(n - 1);
+                j2 = P(0);
             } else {
-                join(o, T, ctm, pen, T.join, P(n - 2), P(0), P(1), pcw);
+                jmode = T.join;
+                j0 = back_to_start ? P(n - 2) : P(n - 1);
+                j1 = P(0);
+                j2 = P(1);
             }
-            return;
+            break;
         }
         default: return;
     }
+#pragma unroll 1
+    for (int i = 0; i < n_caps; i++) {
+        cap(o, T, ctm, pen, sg::face_init(c0, c1, T.thickness, ctm), ccw);
+        const Pt t = c0;  // the second cap of plotSingle runs the other way
+        c0 = c1;
+        c1 = t;
+    }
+    if (jmode >= 0) join(o, T, ctm, pen, jmode, j0, j1, j2, pcw);
 }
 
 __global__ void ks_elem_count(const SubpathDev *__restrict__ subs, const StrokeDev *__restrict__ strokes,
