@@ -113,7 +113,7 @@ struct Ctx {
     std::vector<stroke::Polygon> poly_cache;
     HostBuf staging;    // pinned upload staging
     HostBuf readback;   // pinned readback
-    // the one-upload path of a single small fill (fill.cu, run_small_fill):
+    // the one-upload path of few short fills (fill.cu, run_small_jobs):
     // two pinned staging slots, each free again once its upload event has
     // passed, and the device copy of the latest upload (stream ordered)
     HostBuf small_stage[2];
