@@ -210,8 +210,10 @@ __device__ __forceinline__ double lerp_half(double a, double b) {
 }
 
 // Knots.deCasteljau (Spline.zig:128-152): k becomes the first half, the
-// second half is returned.
-__device__ __forceinline__ Knots de_casteljau(Knots &k) {
+// second half is returned.  Out of line: one copy serves the frontier
+// expansion and the depth-first walks (flatten of the 2,000-path batch
+// 0.72 -> 0.68 ms against the inlined copies).
+static __device__ __noinline__ Knots de_casteljau(Knots &k) {
     const double abx = lerp_half(k.ax, k.bx), aby = lerp_half(k.ay, k.by);
     const double bcx = lerp_half(k.bx, k.cx), bcy = lerp_half(k.by, k.cy);
     const double cdx = lerp_half(k.cx, k.dx), cdy = lerp_half(k.cy, k.dy);
