@@ -201,3 +201,38 @@ def test_draw_jobs_threaded_matches_oracle(oracle):
     torch.cuda.synchronize()
     for s, r in zip(surfaces, refs):
         assert np.array_equal(s.to_host().data, r.data)
+
+
+def test_draw_jobs_many_nodes_matches_oracle(oracle):
+    """A draw_jobs call of more than 2^20 nodes (200-segment paths, solid
+    and dashed strokes among them) equals the oracle's drawing of each
+    job's commands in order."""
+    torch = pytest.importorskip("torch")
+    import sys
+    sys.path.insert(0, __import__("os").path.dirname(__file__))
+    from backends import StrokeOracle
+    from z2d_gb300.types import StrokeOptions
+    w, h, n_jobs, per_job = 96, 80, 8, 660
+    fills = random_fills(seed=23, n=n_jobs * per_job, w=w, h=h, side_lo=8, side_hi=80, seg_lo=200, seg_hi=200)
+    assert sum(len(f[1]) for f in fills) > (1 << 20)
+    so = StrokeOracle(oracle)
+    ops, surfaces, refs = [], [], []
+    for j in range(n_jobs):
+        job = []
+        for k in range(per_job):
+            pat, nodes, fo = fills[j * per_job + k]
+            if k % 40 == 7:
+                job.append(("stroke", pat, nodes, StrokeOptions(line_width=1.5, dashes=(4.0, 3.0) if k % 80 == 7 else ())))
+            else:
+                job.append(("fill", pat, nodes, fo))
+        ops.append(job)
+        surfaces.append(_bg(w, h, 90 + j).to_device("cuda"))
+        ref = _bg(w, h, 90 + j)
+        for kind, pat, nodes, o in job:
+            rc = oracle.fill(ref, pat, nodes, o) if kind == "fill" else so.stroke(ref, pat, nodes, o)
+            assert rc == abi.OK
+        refs.append(ref)
+    painter.draw_jobs(list(zip(surfaces, ops)))
+    torch.cuda.synchronize()
+    for j, (s, r) in enumerate(zip(surfaces, refs)):
+        assert np.array_equal(s.to_host().data, r.data), f"job {j}"
