@@ -1712,10 +1712,21 @@ int run_jobs(Ctx &c, std::vector<DevJob> &jobs, const z2d_node *nodes, int32_t n
     // ---- flatten
     const unsigned flat_blocks =
         (unsigned)std::min<long long>(grid_for((n_nodes + 31) / 32, kFlattenWarps), (long long)c.sm_count * 64);
-    // one warp per queued curve, as many as there could be curves up to a
-    // few resident blocks per SM
+    // one warp per queued curve, as many as there could be curves up to the
+    // blocks the SMs hold at once: a grid of one wave, so the grid-stride
+    // loop over the queue has no partial second wave
+    static std::atomic<int> curve_occ{0};
+    int curve_res = curve_occ.load(std::memory_order_relaxed);
+    if (curve_res <= 0) {
+        int a = 0, b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_curve_count_w, 32 * kFlattenWarps, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_curve_emit_w, 32 * kFlattenWarps, 0) != cudaSuccess)
+            a = b = 4;
+        curve_res = std::max(1, std::min(a, b));
+        curve_occ.store(curve_res, std::memory_order_relaxed);
+    }
     const unsigned curve_blocks =
-        (unsigned)std::min<long long>(grid_for(n_nodes, kFlattenWarps), (long long)c.sm_count * 8);
+        (unsigned)std::min<long long>(grid_for(n_nodes, kFlattenWarps), (long long)c.sm_count * curve_res);
     // per curve warp: kScratch leaf points per lane; then the curve pool
     const size_t scratch_pts = (size_t)curve_blocks * kFlattenWarps * 32 * kScratch;
     // pool capacity: 16 points per node, or what the previous call asked for
