@@ -925,6 +925,25 @@ def star_latency(ctx, dev, iters=200):
     return res
 
 
+def max_over_ranks(ms, world, device):
+    """The slowest rank's time: every rank runs the same replica of the
+    workload, so the job's time is the maximum (an all-reduce of one value;
+    no data moves between ranks otherwise)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_value(world, mpix_step, steps, total_ms):
+    """Whole-job throughput of `world` replicas (weak scaling): every rank
+    drew mpix_step per step for `steps` steps in at most total_ms."""
+    return world * mpix_step * steps / (total_ms / 1e3)
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -990,12 +1009,8 @@ def run_ours(args):
     raster_ms, raster_n = ctx.kernel_ms("raster")
     stage = {k: ctx.kernel_ms(k)[0] / args.steps for k in ("flatten", "bins", "raster")}
     ctx.set_timing(False)
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * mpix_step * args.steps / (total_ms / 1e3)
+    total_ms = max_over_ranks(sum(step_ms), world, dev)
+    value = replicas_value(world, mpix_step, args.steps, total_ms)
 
     # ---- e2e: pinned host surface through the C ABI (H2D + D2H inside)
     host_t = torch.empty(bg.size, dtype=torch.uint8, pin_memory=True)
@@ -1005,11 +1020,13 @@ def run_ours(args):
     for _ in range(args.steps):
         host[:] = bg
         restore()
+        if world > 1:
+            dist.barrier()
         stream.synchronize()
         t0 = time.perf_counter()
         painter.fill_batch_arrays(hsurf, nodes, cmds, ctx=ctx)
         e2e_s.append(time.perf_counter() - t0)
-    e2e_value = mpix_step * args.steps / sum(e2e_s)
+    e2e_value = replicas_value(world, mpix_step, args.steps, max_over_ranks(1e3 * sum(e2e_s), world, dev))
     out_e2e = host.copy()
     h2d = bg.nbytes + nodes.nbytes + len(fills) * 64
     d2h = bg.nbytes
